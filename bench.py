@@ -1,0 +1,337 @@
+#!/usr/bin/env python
+"""Benchmark of the collision-query hot path on one or more GPUs.
+
+Default workload (N=1): batched first-contact queries on the interlocking-tori
+meshes -- 1M segments per GPU, start states uniform in [-2, 2]^3 (world units)
+with Shoemake rotations, ends displaced by N(0, 0.3^2) and rotated by
+U[0, pi], stepped at verify_delta = 0.001 in the unit frame exactly as
+UnitWorld::transitStateToWithContact does.  The metric is collision checks per
+second: the isValid calls the sequential reference loop makes for the batch
+(first contact + 1 per colliding segment, every step of a free one).
+
+One "step" = one pw_segments_first_contact call over the whole resident batch.
+Launch: python bench.py [--gpus N --steps K --warmup W] [--impl reference];
+N > 1 runs under torch.distributed.run, one rank per GPU, weak scaling (each
+rank its own seeded batch, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from puzzletunneldiscovery_gb300 import workloads as W  # noqa: E402
+
+METRIC = "collision checks/sec (first-contact segment queries, interlocking tori)"
+UNIT = "checks/s"
+DELTA = 0.001
+# per-unit algorithmic bytes of the traversal kernel (roofline section)
+BYTES_NODE_PAIR = 2 * 32      # env node + robot node (two float4 each)
+BYTES_LEAF_PAIR = 2 * 48      # env triangle + robot triangle (three float4 each)
+BYTES_SEGMENT = 2 * 56 + 4    # two states in, one int32 out
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _meshes():
+    return W.cfg_interlocking_tori()
+
+
+def _batch(n, scale, seed):
+    return W.segment_batch(n, -2.0, 2.0, scale, seed=seed)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks_%d.csv" % os.getpid())
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None:
+            return None
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 7 and parts[0].replace(".", "").isdigit():
+                    rows.append(parts)
+        except Exception:
+            return None
+        if not rows:
+            return None
+        sm = [float(r[0]) for r in rows]
+        mx = max(float(r[1]) for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(q0, q1, target_s=12.0, max_n=None):
+    """The oracle (CPU restatement of the reference path) on a bounded sample, all host threads."""
+    from oracle import oracle as O
+    O.build()
+    Ve, Fe, Vr, Fr = _meshes()
+    ow = O.OracleWorld(Ve, Fe, Vr, Fr)
+    cores = os.cpu_count() or 1
+    n = 128
+    total = len(q0) if max_n is None else min(len(q0), max_n)
+    while True:
+        n = min(n, total)
+        t0 = time.perf_counter()
+        _, checks = ow.segments_first_contact(q0[:n], q1[:n], DELTA, mode=0, nthreads=cores)
+        dt = time.perf_counter() - t0
+        if dt >= target_s or n >= total:
+            break
+        n = min(total, max(n * 2, int(n * target_s / max(dt, 1e-3) * 1.1)))
+    return {"value": float(checks.sum()) / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "first %d segments of the rank-0 batch (%d reference checks, %.1f s)"
+                      % (n, int(checks.sum()), dt)}
+
+
+def run_reference(args):
+    """--impl reference: the CPU restatement of the reference path, timed on the host cores."""
+    ws, rank, _ = _dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    Ve, Fe, Vr, Fr = _meshes()
+    ow = O.OracleWorld(Ve, Fe, Vr, Fr)
+    cores = os.cpu_count() or 1
+    q0, q1 = _batch(args.n, ow.scene_scale, seed=0)
+    sample = args.ref_sample
+    times, checks = [], []
+    for it in range(args.warmup + args.steps):
+        lo = (it * sample) % max(1, len(q0) - sample)
+        t0 = time.perf_counter()
+        _, c = ow.segments_first_contact(q0[lo:lo + sample], q1[lo:lo + sample], DELTA, mode=0, nthreads=cores)
+        dt = time.perf_counter() - t0
+        if it >= args.warmup:
+            times.append(dt)
+            checks.append(int(c.sum()))
+    value = sum(checks) / sum(times)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded interlocking-tori segments)",
+            "config": {"workload": "segments_first_contact/interlocking_tori", "n_segments": args.n,
+                       "verify_delta": DELTA, "sample_per_step": sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "%d segments per step of the %d-segment batch" % (sample, args.n)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import puzzletunneldiscovery_gb300 as pw
+
+    ws, rank, local = _dist_env()
+    if ws > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    Ve, Fe, Vr, Fr = _meshes()
+    uw = pw.UnitWorld(local)
+    uw.load_env_mesh(Ve, Fe)
+    uw.load_robot_mesh(Vr, Fr)
+    uw.scaleToUnit()
+    uw.angleModel(0.0, 0.0)
+    q0, q1 = _batch(args.n, uw.scene_scale, seed=rank)
+    a = torch.from_numpy(q0).to(dev)
+    b = torch.from_numpy(q1).to(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def barrier():
+        if ws > 1:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    for _ in range(args.warmup):
+        uw.first_contact_steps(a, b, DELTA)
+    barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stats = []
+    stream = torch.cuda.current_stream(dev)
+    with ClockSampler(local) as clk:
+        barrier()
+        for i in range(args.steps):
+            flush.zero_()                      # L2 flush between timed steps (not timed)
+            ev[i][0].record(stream)
+            f = uw.first_contact_steps(a, b, DELTA)
+            ev[i][1].record(stream)
+            stats.append(uw.last_stats())      # synchronises; outside the event pair
+        barrier()
+    step_ms = [s.elapsed_time(e) for s, e in ev]
+    my_ms = sum(step_ms)
+    my_checks = sum(s["reference_checks"] for s in stats)
+    if ws > 1:
+        t = torch.tensor([my_ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        c = torch.tensor([my_checks], device=dev, dtype=torch.float64)
+        dist.all_reduce(c, op=dist.ReduceOp.SUM)
+        tot_ms, tot_checks = float(t.item()), float(c.item())
+    else:
+        tot_ms, tot_checks = my_ms, float(my_checks)
+    value = tot_checks / (tot_ms / 1e3)
+
+    # end to end through the public API with host buffers (pinned), copies inside the timed region
+    ha = torch.from_numpy(q0).pin_memory()
+    hb = torch.from_numpy(q1).pin_memory()
+    hout = torch.empty(args.n, dtype=torch.int32).pin_memory()
+    e2e_ms, e2e_checks = 0.0, 0
+    barrier()
+    for i in range(args.steps):
+        flush.zero_()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        da = ha.to(dev, non_blocking=True)
+        db = hb.to(dev, non_blocking=True)
+        f = uw.first_contact_steps(da, db, DELTA)
+        hout.copy_(f, non_blocking=True)
+        s1.record(stream)
+        torch.cuda.synchronize(dev)
+        e2e_ms += s0.elapsed_time(s1)
+        e2e_checks += uw.last_stats()["reference_checks"]
+    if ws > 1:
+        t = torch.tensor([e2e_ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        c = torch.tensor([e2e_checks], device=dev, dtype=torch.float64)
+        dist.all_reduce(c, op=dist.ReduceOp.SUM)
+        e2e_ms, e2e_checks = float(t.item()), float(c.item())
+    e2e_value = e2e_checks / (e2e_ms / 1e3)
+
+    if rank != 0:
+        if ws > 1:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    # roofline of the dominant (traversal) kernel
+    trav_ms = sum(s["traverse_ms"] for s in stats) / len(stats)
+    node = sum(s["node_tests"] for s in stats) / len(stats)
+    leaf = sum(s["leaf_tests"] for s in stats) / len(stats)
+    alg_bytes = node * BYTES_NODE_PAIR + leaf * BYTES_LEAF_PAIR + args.n * BYTES_SEGMENT
+    achieved = alg_bytes / (trav_ms / 1e3) / 1e9
+    peak, peak_kind = _peaks()
+    traffic = None
+    tpq = _traffic_per_query()
+    if tpq is not None:
+        traffic = tpq * sum(s["queries"] for s in stats) / len(stats)
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic, "kernel": "k_segments", "kernel_ms": trav_ms,
+            "peak_source": peak_kind, "algorithmic_bytes": alg_bytes}
+    cpu = None
+    if ws == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(q0, q1, target_s=args.cpu_seconds)
+    last = stats[-1]
+    fc = f.cpu().numpy()
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 traversal + f64 state math/re-tests",
+            "data": "synthetic (seeded interlocking-tori segments; no published data set for this path)",
+            "config": {"workload": "segments_first_contact/interlocking_tori",
+                       "meshes": "torus R=1 r=0.25 64x32 (4096 tris) x2, interlocked",
+                       "n_segments_per_gpu": args.n, "verify_delta": DELTA, "mode": "transit_state_to",
+                       "l2": "flushed (256 MB write) between timed steps; per-step working set > L2",
+                       "parallelism": "replicas" if ws == 1 else "shard-per-rank (weak)"},
+            "roofline": roof, "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(2 * args.n * 56 * ws),
+                    "d2h_bytes_per_step": int(4 * args.n * ws)},
+            "clocks": clk.summary(),
+            "gpu_launches": 6 * args.steps,
+            "detail": {"reference_checks_per_step": tot_checks / args.steps,
+                       "gpu_queries_per_step": last["queries"], "node_tests": last["node_tests"],
+                       "leaf_tests": last["leaf_tests"], "fp64_retests": last["retests"],
+                       "fp64_retest_rate_per_leaf": last["retests"] / max(1, last["leaf_tests"]),
+                       "inline_retests": last["inline_retests"], "retest_ms": last["retest_ms"],
+                       "segments_per_s": args.n * ws / (tot_ms / args.steps / 1e3),
+                       "free_fraction": float((fc == -1).mean()), "step_ms": step_ms}}
+    print(json.dumps(line))
+    if ws > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def _traffic_per_query():
+    """DRAM bytes per (segment, step) query of the traversal kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "k_segments_traffic.txt")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_query"):
+                return float(line.split("=")[1])
+    except Exception:
+        pass
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=1_000_000, help="segments per GPU")
+    ap.add_argument("--ref-sample", type=int, default=400, help="segments per reference-arm step")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

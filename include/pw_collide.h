@@ -1,0 +1,159 @@
+/*
+ * pw_collide.h -- C ABI of the GB300 collision-query engine (libpwcollide.so).
+ *
+ * Drop-in boundary for the collision-query path of pyosr's UnitWorld
+ * (lib/pyosr/module.cc:127-250, class UnitWorld; C++ in lib/osr/unit_world.cc).
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, returns an
+ * int status (PW_OK or a PW_ERR_* code; the message is in pw_last_error()),
+ * and never throws.  Batched queries take DEVICE pointers and a cudaStream_t
+ * passed as `void *` (NULL = legacy default stream) and are asynchronous on
+ * that stream.  Functions marked "host" take host memory and are synchronous.
+ *
+ * States are 7 doubles [x, y, z, w, qx, qy, qz] (lib/osr/osr_state.h:20-33),
+ * row-major, one state per row.
+ *
+ * One world serves one query at a time: queries share the world's scratch
+ * buffers, so concurrent queries on one world must be ordered on one stream.
+ */
+#ifndef PW_COLLIDE_H
+#define PW_COLLIDE_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define PW_API __attribute__((visibility("default")))
+#else
+#define PW_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PW_OK 0
+#define PW_ERR_INVALID_ARG 1   /* bad pointer, size or value */
+#define PW_ERR_CUDA 2          /* a CUDA runtime call failed */
+#define PW_ERR_NO_MODEL 3      /* query before load/scale/angle set-up (isDisentangled throws here too) */
+#define PW_ERR_OUT_OF_MEMORY 4
+#define PW_ERR_CAPACITY 5      /* caller buffer too small; the required size is reported */
+#define PW_ERR_INTERNAL 6      /* a device-side consistency check failed */
+
+#define PW_GEO_ENV 0           /* UnitWorld::GEO_ENV, lib/osr/unit_world.h:26 */
+#define PW_GEO_ROB 1           /* UnitWorld::GEO_ROB, lib/osr/unit_world.h:27 */
+
+#define PW_SEG_TRANSIT 0       /* transit_state_to(_with_contact): step = verify_delta */
+#define PW_SEG_TRANSITION 1    /* is_valid_transition: step = min(dist / 2, verify_delta) */
+
+/* First-contact codes written by pw_segments_first_contact (>= 0: step index). */
+#define PW_STEP_FREE (-1)      /* every step free: the reference's `done` is true */
+#define PW_STEP_NONE (-2)      /* verify_delta >= dist: no step checked, `done` false (unit_world.cc:445-447) */
+
+typedef struct pw_world pw_world;
+
+typedef struct pw_world_info {
+	double scene_scale;          /* UnitWorld::getSceneScale, 1 / max(span_env, span_rob) as float */
+	double robot_center[3];      /* Scene::getCenter of the robot (possibly enforced) */
+	double robot_ompl_center[3]; /* Scene::getOMPLCenter: float mean of the robot vertices */
+	double scene_matrix[16];     /* getSceneMatrix, row-major 4x4 */
+	double robot_matrix[16];     /* getRobotMatrix, row-major 4x4 */
+	int64_t env_vertices, env_faces, robot_vertices, robot_faces;
+	int32_t env_bvh_depth, robot_bvh_depth;
+	int32_t ready;               /* 1 once angle_model has built both CD models */
+	int32_t device;
+} pw_world_info;
+
+typedef struct pw_query_stats {
+	int64_t queries;             /* states or (segment, step) pairs examined */
+	int64_t node_tests;          /* BVH node-pair box tests */
+	int64_t leaf_tests;          /* FP32 triangle-pair tests */
+	int64_t retests;             /* triangle pairs re-tested in FP64 */
+	int64_t retest_hits;         /* FP64 re-tests that found contact */
+	int64_t inline_retests;      /* FP64 re-tests done in the traversal kernel (queue full) */
+	int64_t work_items;          /* work items the persistent kernel executed */
+	int64_t reference_checks;    /* isValid calls the sequential reference loop makes for the same batch */
+	double traverse_ms;          /* device time of the traversal kernel (CUDA events on the query stream) */
+	double retest_ms;            /* device time of the FP64 re-test kernel */
+} pw_query_stats;
+
+/* Thread-local message for the last failing call on this thread. */
+PW_API const char *pw_last_error(void);
+
+/* World life cycle.  Replaces UnitWorld::UnitWorld / ~UnitWorld (unit_world.cc:64-74). */
+PW_API int pw_world_create(pw_world **out, int device);
+PW_API int pw_world_destroy(pw_world *w);
+
+/* host: UnitWorld::loadModelFromFile / loadRobotFromFile (unit_world.cc:94-110) for an
+ * already-parsed triangle mesh: nv float32 vertices (x, y, z) and nf uint32 index triples. */
+PW_API int pw_world_load_env(pw_world *w, const float *V, int64_t nv, const uint32_t *F, int64_t nf);
+PW_API int pw_world_load_robot(pw_world *w, const float *V, int64_t nv, const uint32_t *F, int64_t nf);
+
+/* host: UnitWorld::enforceRobotCenter (unit_world.cc:114-118). */
+PW_API int pw_world_enforce_robot_center(pw_world *w, const double center[3]);
+
+/* host: UnitWorld::scaleToUnit (unit_world.cc:123-131). */
+PW_API int pw_world_scale_to_unit(pw_world *w);
+
+/* host: UnitWorld::angleModel (unit_world.cc:137-161): builds the CD vertices of both
+ * meshes and their BVHs on the device.  Both angles must be 0, as in the reference. */
+PW_API int pw_world_angle_model(pw_world *w, float latitude, float longitude);
+
+/* host: UnitWorld::setPerturbation / getPerturbation (unit_world.cc:164-175). */
+PW_API int pw_world_set_perturbation(pw_world *w, const double q[7]);
+PW_API int pw_world_get_perturbation(const pw_world *w, double q[7]);
+
+/* host: scene_scale, centres, scene_matrix / robot_matrix (module.cc:245-250). */
+PW_API int pw_world_info_get(const pw_world *w, pw_world_info *out);
+
+/* host: CD-model geometry, CDModel::vertices / faces (cdmodel.cc:232-242).
+ * geo = PW_GEO_ENV (in the perturbation frame) or PW_GEO_ROB (robot local frame). */
+PW_API int pw_world_cd_vertices(const pw_world *w, int geo, double *out);
+PW_API int pw_world_cd_faces(const pw_world *w, int geo, int32_t *out);
+
+/* device, async: UnitWorld::isValid (unit_world.cc:215-247) for n states.
+ * valid[i] = 1 when the robot at states[i] touches no env triangle. */
+PW_API int pw_states_valid(pw_world *w, const double *states, int64_t n, uint8_t *valid, void *stream);
+
+/* device, async: UnitWorld::isDisentangled (unit_world.cc:249-264) for n states. */
+PW_API int pw_states_disentangled(pw_world *w, const double *states, int64_t n, uint8_t *disentangled, void *stream);
+
+/* device, async: UnitWorld::transitStateToWithContact (unit_world.cc:405-474) in PW_SEG_TRANSIT
+ * mode, or isValidTransition (unit_world.cc:477-486) in PW_SEG_TRANSITION mode, for n segments
+ * from[i] -> to[i].  first_step[i] = index of the first colliding step (0 = the first state
+ * checked, at delta = verify_delta), PW_STEP_FREE or PW_STEP_NONE.  verify_delta must be > 0
+ * and dist / verify_delta below 2^30 (the reference loop never ends for verify_delta <= 0). */
+PW_API int pw_segments_first_contact(pw_world *w, const double *from, const double *to, int64_t n,
+                              double verify_delta, int mode, int32_t *first_step, void *stream);
+
+/* host in, host out, synchronous: UnitWorld::intersectingSegments (unit_world.cc:959-1012).
+ * Writes up to `capacity` rows sorted by (env face, robot face): segment begins/ends (3 doubles
+ * each), lengths, face pairs (env, robot) and coplanar flags; *count = total pairs found.
+ * Returns PW_ERR_CAPACITY (with *count set) when capacity < *count. */
+PW_API int pw_intersecting_segments(pw_world *w, const double q[7], int64_t capacity, double *begins,
+                             double *ends, double *mags, int32_t *face_pairs, int32_t *coplanar,
+                             int64_t *count);
+
+/* host: state-frame conversions (unit_world.cc:526-539, 689-711, 713-737). */
+PW_API int pw_world_translate_to_unit(const pw_world *w, const double *in, int64_t n, double *out);
+PW_API int pw_world_translate_from_unit(const pw_world *w, const double *in, int64_t n, double *out);
+PW_API int pw_world_translate_ompl_to_unit(const pw_world *w, const double *in, int64_t n, double *out);
+PW_API int pw_world_translate_unit_to_ompl(const pw_world *w, const double *in, int64_t n, double *out,
+                                    int to_angle_axis);
+
+/* host: statistics of the last query on this world (synchronises its stream). */
+PW_API int pw_world_last_stats(pw_world *w, pw_query_stats *out);
+
+/* host: SE(3) state math with the engine's deterministic FP64 routines.
+ * distance (osr_state.cc:130-154) and interpolate (osr_state.cc:27-44). */
+PW_API int pw_state_distance(const double a[7], const double b[7], double *out);
+PW_API int pw_state_interpolate(const double a[7], const double b[7], double tau, double out[7]);
+
+/* host: the k-th state the reference stepping loop checks on a segment and its tau
+ * (unit_world.cc:445-470); *num_steps = number of steps of the whole segment. */
+PW_API int pw_segment_step_state(const double from[7], const double to[7], double verify_delta, int64_t k,
+                          double out[7], double *tau, int64_t *num_steps);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PW_COLLIDE_H */

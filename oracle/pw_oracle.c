@@ -110,17 +110,17 @@ static double or_atan01(double z)
 	/* half-angle: atan(z) = 2 atan(z / (1 + sqrt(1 + z^2))) */
 	const double w = z / (1.0 + sqrt(1.0 + z * z));
 	const double s = w * w;
-	double p = 1.0 / 23.0;
-	p = p * s - 1.0 / 21.0;
-	p = p * s + 1.0 / 19.0;
-	p = p * s - 1.0 / 17.0;
-	p = p * s + 1.0 / 15.0;
-	p = p * s - 1.0 / 13.0;
-	p = p * s + 1.0 / 11.0;
-	p = p * s - 1.0 / 9.0;
-	p = p * s + 1.0 / 7.0;
-	p = p * s - 1.0 / 5.0;
-	p = p * s + 1.0 / 3.0;
+	double p = 0.043478260869565216;
+	p = p * s - 0.047619047619047616;
+	p = p * s + 0.05263157894736842;
+	p = p * s - 0.058823529411764705;
+	p = p * s + 0.06666666666666667;
+	p = p * s - 0.07692307692307693;
+	p = p * s + 0.09090909090909091;
+	p = p * s - 0.1111111111111111;
+	p = p * s + 0.14285714285714285;
+	p = p * s - 0.2;
+	p = p * s + 0.3333333333333333;
 	const double a = w - w * (s * p);
 	double r = 2.0 * a;
 	if (shifted)
@@ -995,7 +995,8 @@ OR_EXPORT int64_t or_transit_with_contact(const or_world *w, const double from[7
 {
 	const double dist = or_distance(from, to);
 	memcpy(last_free, from, sizeof(double) * 7);
-	if (!(verify_delta > 0.0) || (dist == dist && verify_delta < dist && dist / verify_delta > 1073741824.0)) {
+	if (!(verify_delta >= dist) && dist == dist &&
+	    (!(verify_delta > 0.0) || dist / verify_delta > 1073741824.0)) {
 		/* the reference loop never ends for delta <= 0; the step cap keeps it finite */
 		memcpy(state, from, sizeof(double) * 7);
 		*done = 0; *last_tau_out = 0.0f; *tau_out = 0.0f;
@@ -1112,10 +1113,10 @@ OR_EXPORT void or_segments_first_contact(const or_world *w, const double *q0, co
 OR_EXPORT int64_t or_segment_steps(const double from[7], const double to[7], double verify_delta)
 {
 	const double dist = or_distance(from, to);
-	if (!(verify_delta > 0.0) || (dist == dist && verify_delta < dist && dist / verify_delta > 1073741824.0))
-		return -1;
 	if (verify_delta >= dist || !(dist == dist))
 		return 0;
+	if (!(verify_delta > 0.0) || dist / verify_delta > 1073741824.0)
+		return -1;
 	double delta = verify_delta;
 	int64_t k = 0;
 	while (delta <= dist) {

@@ -1,0 +1,119 @@
+// pw_internal.cuh -- data layout shared by the world set-up and the query kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "pw_collide.h"
+
+// One mesh on the device.  Triangles and BVH leaves share "slot" order (the
+// Morton order of the build); FP64 data stays in the original face order.
+//   nodeA[i] = (centre.xyz, left child)   nodeB[i] = (half-extent.xyz, right child)
+//   internal nodes 0 .. ntri-2 (root 0), leaves ntri-1 .. 2*ntri-2 (slot = i - leaf_base).
+//   triA/B/C[slot] = FP32 vertices 0/1/2 (w of triA = original face id).
+// Boxes are conservative: they contain the FP64 vertices exactly.
+struct MeshDev {
+	int32_t ntri = 0;
+	int32_t nvert = 0;
+	int32_t leaf_base = 0;
+	int32_t depth = 0;
+	float4 *nodeA = nullptr, *nodeB = nullptr;
+	float4 *triA = nullptr, *triB = nullptr, *triC = nullptr;
+	double *V64 = nullptr;   // nvert x 3 (env: perturbation frame; robot: local frame)
+	int32_t *F = nullptr;    // ntri x 3
+	float r1 = 0.f;          // L1 bound of any point of any node box (robot: local frame)
+	float emax = 0.f;        // max |coordinate| of any vertex
+};
+
+struct WorldDev {
+	MeshDev env, rob;
+	float del_env;           // FP32 rounding bound of an env vertex coordinate
+};
+
+// Per-query device counters; zeroed before every query.
+struct QueryCounters {
+	unsigned long long work;        // next work item of the persistent kernels
+	unsigned long long retest_count;
+	unsigned long long stat[8];     // see STAT_* below
+	unsigned long long ref_checks;  // isValid calls of the sequential reference loop
+	unsigned int error;             // device-side consistency failure (PW_ERR_INTERNAL)
+	unsigned int pad;
+};
+enum {
+	STAT_QUERIES = 0,
+	STAT_NODE_TESTS = 1,
+	STAT_LEAF_TESTS = 2,
+	STAT_RETESTS = 3,
+	STAT_RETEST_HITS = 4,
+	STAT_INLINE = 5,
+	STAT_ITEMS = 6,
+	STAT_TOTAL_ITEMS = 7,
+};
+
+// A triangle pair whose FP32 verdict fell inside the error band.
+struct RetestEntry {
+	uint32_t query;   // state index or segment index
+	uint32_t step;    // segment step (0 for states)
+	uint32_t env_tri; // original face ids
+	uint32_t rob_tri;
+};
+
+// Per-segment constants of the stepping loop, built on the device.
+struct SegParams {
+	double a[7], b[7];        // from / to states (as given)
+	double qa[4], qb[4];      // normalised rotations
+	double d, theta, stheta;  // slerp constants
+	double dist, inv_dist, step;
+	int32_t linear;
+	int32_t nsteps;           // steps the reference loop takes (0: none)
+	int64_t ckpt_base;        // first checkpoint slot
+};
+
+struct DeviceBuffer {
+	void *ptr = nullptr;
+	size_t bytes = 0;
+	cudaError_t reserve(size_t need);
+	void release();
+	~DeviceBuffer() { release(); }
+};
+
+struct pw_world {
+	int device = 0;
+	bool has_env = false, has_rob = false, scaled = false, ready = false;
+	std::vector<float> Ve, Vr;
+	std::vector<uint32_t> Fe, Fr;
+	float scale = 1.0f;
+	float center[3] = { 0, 0, 0 };
+	float ompl_center[3] = { 0, 0, 0 };
+	double pert[7] = { 0, 0, 0, 1, 0, 0, 0 };
+	double pertR[9], pert_t[3];
+	std::vector<double> env_local, env_world, rob_local;
+	double env_box_c[3], env_box_h[3], rob_box_c[3], rob_box_h[3];
+	WorldDev dev;
+	// owned device allocations of the meshes
+	std::vector<void *> mesh_allocs;
+	// query scratch
+	DeviceBuffer counters;     // QueryCounters
+	DeviceBuffer retest;       // RetestEntry[retest_cap]
+	uint64_t retest_cap = 0;
+	DeviceBuffer seg_params, seg_ckpt, seg_keys, seg_order, seg_keys2, seg_order2, round_off, cub_tmp, misc;
+	cudaStream_t last_stream = nullptr;
+	cudaEvent_t ev[4] = { nullptr, nullptr, nullptr, nullptr }; // traversal start/end, re-test start/end
+	bool timed = false;
+	int64_t last_states = -1;   // size of the last state batch (-1: the last query was segments)
+	int num_sms = 0;
+};
+
+// error plumbing (pw_world.cu)
+int pw_fail(int code, const std::string &msg);
+int pw_cuda_fail(cudaError_t e, const char *what);
+#define PW_CUDA(call)                                         \
+	do {                                                      \
+		cudaError_t e__ = (call);                             \
+		if (e__ != cudaSuccess) return pw_cuda_fail(e__, #call); \
+	} while (0)
+
+int pw_build_mesh_device(pw_world *w, MeshDev &m, const std::vector<double> &V64, const std::vector<uint32_t> &F);
+void pw_free_mesh_device(pw_world *w);

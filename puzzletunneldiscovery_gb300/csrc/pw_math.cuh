@@ -1,0 +1,558 @@
+// pw_math.cuh -- deterministic FP64 math shared by host and device code.
+//
+// Every FP64 operation here is separately rounded: on the device through the
+// __d*_rn intrinsics (which the compiler never fuses into FMAs), on the host
+// through plain operators compiled with -ffp-contract=off.  Host and device
+// therefore produce bit-identical states, transforms and triangle verdicts.
+//
+// Restated behaviour:
+//   state -> transform           lib/osr/osr_state.cc:16-25 (raw quaternion)
+//   interpolate (lerp + slerp)   lib/osr/osr_state.cc:27-44
+//   decompose / compose          lib/osr/osr_state.cc:85-119
+//   distance                     lib/osr/osr_state.cc:130-154
+//   triangle-triangle test       Moeller, JGT 2(2) 1997 (lib/tritri/Moller97d.cc:220,579)
+// sin / acos / atan2 are this file's own: Taylor series after complement and
+// half-angle argument reduction, accurate to a few ulp on the ranges used.
+#pragma once
+
+#include <math.h>
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define PW_HD __host__ __device__ __forceinline__
+#else
+#define PW_HD inline
+#endif
+
+namespace pwm {
+
+#if defined(__CUDA_ARCH__)
+PW_HD double add(double a, double b) { return __dadd_rn(a, b); }
+PW_HD double sub(double a, double b) { return __dsub_rn(a, b); }
+PW_HD double mul(double a, double b) { return __dmul_rn(a, b); }
+PW_HD double dvd(double a, double b) { return __ddiv_rn(a, b); }
+PW_HD double rt(double a) { return __dsqrt_rn(a); }
+#else
+PW_HD double add(double a, double b) { return a + b; }
+PW_HD double sub(double a, double b) { return a - b; }
+PW_HD double mul(double a, double b) { return a * b; }
+PW_HD double dvd(double a, double b) { return a / b; }
+PW_HD double rt(double a) { return sqrt(a); }
+#endif
+PW_HD double dabs(double a) { return a >= 0.0 ? a : -a; }
+
+constexpr double PIO2_HI = 1.5707963267948965579989817342720925807952880859375;
+constexpr double PIO2_LO = 6.123233995736766035868820147291818e-17;
+constexpr double PIO4_HI = 0.78539816339744827899949086713604629039764404296875;
+constexpr double PIO4_LO = 3.061616997868383017934410073645909e-17;
+constexpr double TAN_PI_8 = 0.41421356237309503;
+constexpr double SLERP_ONE = 1.0 - 2.220446049250313080847e-16;
+
+PW_HD double sin_kernel(double x)
+{
+	const double z = mul(x, x);
+	double p = 2.8114572543455207632e-15;
+	p = sub(mul(p, z), 7.6471637318198164759e-13);
+	p = add(mul(p, z), 1.6059043836821614599e-10);
+	p = sub(mul(p, z), 2.5052108385441718775e-08);
+	p = add(mul(p, z), 2.7557319223985890653e-06);
+	p = sub(mul(p, z), 1.9841269841269841270e-04);
+	p = add(mul(p, z), 8.3333333333333333333e-03);
+	p = sub(mul(p, z), 1.6666666666666666667e-01);
+	return add(x, mul(x, mul(z, p)));
+}
+
+PW_HD double cos_kernel(double y)
+{
+	const double z = mul(y, y);
+	double p = -1.5619206968586225271e-16;
+	p = add(mul(p, z), 4.7794773323873852974e-14);
+	p = sub(mul(p, z), 1.1470745597729724714e-11);
+	p = add(mul(p, z), 2.0876756987868098979e-09);
+	p = sub(mul(p, z), 2.7557319223985890653e-07);
+	p = add(mul(p, z), 2.4801587301587301587e-05);
+	p = sub(mul(p, z), 1.3888888888888888889e-03);
+	p = add(mul(p, z), 4.1666666666666666667e-02);
+	p = sub(mul(p, z), 5.0000000000000000000e-01);
+	return add(1.0, mul(z, p));
+}
+
+// sin(x) for x in [-pi/4, pi/2 + small].
+PW_HD double sin_q(double x)
+{
+	if (x <= PIO4_HI)
+		return sin_kernel(x);
+	return cos_kernel(add(sub(PIO2_HI, x), PIO2_LO));
+}
+
+// atan(z) for z in [0, 1].
+PW_HD double atan01(double z)
+{
+	bool shifted = false;
+	if (z > TAN_PI_8) {
+		z = dvd(sub(z, 1.0), add(z, 1.0));
+		shifted = true;
+	}
+	const double w = dvd(z, add(1.0, rt(add(1.0, mul(z, z)))));
+	const double s = mul(w, w);
+	double p = 0.043478260869565216;
+	p = sub(mul(p, s), 0.047619047619047616);
+	p = add(mul(p, s), 0.05263157894736842);
+	p = sub(mul(p, s), 0.058823529411764705);
+	p = add(mul(p, s), 0.06666666666666667);
+	p = sub(mul(p, s), 0.07692307692307693);
+	p = add(mul(p, s), 0.09090909090909091);
+	p = sub(mul(p, s), 0.1111111111111111);
+	p = add(mul(p, s), 0.14285714285714285);
+	p = sub(mul(p, s), 0.2);
+	p = add(mul(p, s), 0.3333333333333333);
+	const double a = sub(w, mul(w, mul(s, p)));
+	double r = mul(2.0, a);
+	if (shifted)
+		r = add(PIO4_HI, add(r, PIO4_LO));
+	return r;
+}
+
+// atan2(y, x) for y >= 0, x >= 0.
+PW_HD double atan2q(double y, double x)
+{
+	if (y == 0.0)
+		return 0.0;
+	if (y <= x)
+		return atan01(dvd(y, x));
+	return add(sub(PIO2_HI, atan01(dvd(x, y))), PIO2_LO);
+}
+
+// acos(a) for a in [0, 1].
+PW_HD double acos01(double a)
+{
+	return mul(2.0, atan2q(rt(sub(1.0, a)), rt(add(1.0, a))));
+}
+
+// ---------------------------------------------------------------- states
+
+// Quaternions are (w, x, y, z); squared norm summed in storage order x, y, z, w.
+PW_HD void quat_normalize(const double *qin, double *q)
+{
+	const double w = qin[0], x = qin[1], y = qin[2], z = qin[3];
+	const double n2 = add(add(add(mul(x, x), mul(y, y)), mul(z, z)), mul(w, w));
+	if (n2 > 0.0) {
+		const double n = rt(n2);
+		q[0] = dvd(w, n); q[1] = dvd(x, n); q[2] = dvd(y, n); q[3] = dvd(z, n);
+	} else {
+		q[0] = w; q[1] = x; q[2] = y; q[3] = z;
+	}
+}
+
+// Unit-quaternion rotation formula applied to raw coefficients (w, x, y, z).
+PW_HD void quat_to_matrix(const double *q, double *R)
+{
+	const double w = q[0], x = q[1], y = q[2], z = q[3];
+	const double tx = mul(2.0, x), ty = mul(2.0, y), tz = mul(2.0, z);
+	const double twx = mul(tx, w), twy = mul(ty, w), twz = mul(tz, w);
+	const double txx = mul(tx, x), txy = mul(ty, x), txz = mul(tz, x);
+	const double tyy = mul(ty, y), tyz = mul(tz, y), tzz = mul(tz, z);
+	R[0] = sub(1.0, add(tyy, tzz)); R[1] = sub(txy, twz);           R[2] = add(txz, twy);
+	R[3] = add(txy, twz);           R[4] = sub(1.0, add(txx, tzz)); R[5] = sub(tyz, twx);
+	R[6] = sub(txz, twy);           R[7] = add(tyz, twx);           R[8] = sub(1.0, add(txx, tyy));
+}
+
+PW_HD void xform_point(const double *R, const double *t, const double *p, double *o)
+{
+#pragma unroll
+	for (int i = 0; i < 3; i++) {
+		double s = mul(R[3 * i + 0], p[0]);
+		s = add(s, mul(R[3 * i + 1], p[1]));
+		s = add(s, mul(R[3 * i + 2], p[2]));
+		o[i] = add(s, t[i]);
+	}
+}
+
+PW_HD void state_transform(const double *q, double *R, double *t)
+{
+	const double quat[4] = { q[3], q[4], q[5], q[6] };
+	quat_to_matrix(quat, R);
+	t[0] = q[0]; t[1] = q[1]; t[2] = q[2];
+}
+
+// a * conj(b)
+PW_HD void quat_mul_conj(const double *a, const double *b, double *o)
+{
+	const double bw = b[0], bx = -b[1], by = -b[2], bz = -b[3];
+	o[0] = sub(sub(sub(mul(a[0], bw), mul(a[1], bx)), mul(a[2], by)), mul(a[3], bz));
+	o[1] = sub(add(add(mul(a[0], bx), mul(a[1], bw)), mul(a[2], bz)), mul(a[3], by));
+	o[2] = add(add(sub(mul(a[0], by), mul(a[1], bz)), mul(a[2], bw)), mul(a[3], bx));
+	o[3] = add(sub(add(mul(a[0], bz), mul(a[1], by)), mul(a[2], bx)), mul(a[3], bw));
+}
+
+PW_HD double angular_distance(const double *a, const double *b)
+{
+	double d[4];
+	quat_mul_conj(a, b, d);
+	const double vn = rt(add(add(mul(d[1], d[1]), mul(d[2], d[2])), mul(d[3], d[3])));
+	return mul(2.0, atan2q(vn, dabs(d[0])));
+}
+
+PW_HD double distance(const double *a, const double *b)
+{
+	double qa[4], qb[4];
+	const double ra[4] = { a[3], a[4], a[5], a[6] };
+	const double rb[4] = { b[3], b[4], b[5], b[6] };
+	quat_normalize(ra, qa);
+	quat_normalize(rb, qb);
+	const double dx = sub(a[0], b[0]), dy = sub(a[1], b[1]), dz = sub(a[2], b[2]);
+	const double tr = rt(add(add(mul(dx, dx), mul(dy, dy)), mul(dz, dz)));
+	return add(tr, angular_distance(qa, qb));
+}
+
+// Per-segment constants of the interpolation: normalised rotations, their dot,
+// the slerp angle and its sine (theta / sin only used when !linear).
+struct SlerpParams {
+	double qa[4], qb[4];
+	double d, theta, stheta;
+	int linear;
+};
+
+PW_HD void slerp_setup(const double *a, const double *b, SlerpParams &P)
+{
+	const double ra[4] = { a[3], a[4], a[5], a[6] };
+	const double rb[4] = { b[3], b[4], b[5], b[6] };
+	quat_normalize(ra, P.qa);
+	quat_normalize(rb, P.qb);
+	P.d = add(add(add(mul(P.qa[1], P.qb[1]), mul(P.qa[2], P.qb[2])), mul(P.qa[3], P.qb[3])), mul(P.qa[0], P.qb[0]));
+	const double absd = dabs(P.d);
+	P.linear = absd >= SLERP_ONE;
+	if (!P.linear) {
+		P.theta = acos01(absd);
+		P.stheta = sin_q(P.theta);
+	} else {
+		P.theta = 0.0;
+		P.stheta = 0.0;
+	}
+}
+
+// interpolate(a, b, tau) given the segment's slerp constants.
+PW_HD void interpolate_p(const double *a, const double *b, const SlerpParams &P, double tau, double *out)
+{
+	const double omt = sub(1.0, tau);
+#pragma unroll
+	for (int i = 0; i < 3; i++)
+		out[i] = add(mul(a[i], omt), mul(b[i], tau));
+	double s0, s1;
+	if (P.linear) {
+		s0 = omt;
+		s1 = tau;
+	} else {
+		s0 = dvd(sin_q(mul(omt, P.theta)), P.stheta);
+		s1 = dvd(sin_q(mul(tau, P.theta)), P.stheta);
+	}
+	if (P.d < 0.0)
+		s1 = -s1;
+#pragma unroll
+	for (int i = 0; i < 4; i++)
+		out[3 + i] = add(mul(s0, P.qa[i]), mul(s1, P.qb[i]));
+}
+
+PW_HD void interpolate(const double *a, const double *b, double tau, double *out)
+{
+	SlerpParams P;
+	slerp_setup(a, b, P);
+	interpolate_p(a, b, P, tau, out);
+}
+
+// One iteration of the reference's delta update (unit_world.cc:463-470).
+PW_HD double advance_delta(double delta, double dist, double step)
+{
+	if (delta < dist) {
+		delta = add(delta, step);
+		return dist < delta ? dist : delta;
+	}
+	return add(delta, step);
+}
+
+// ---------------------------------------------------------------- Moeller
+
+PW_HD void sub3(const double *a, const double *b, double *o)
+{
+	o[0] = sub(a[0], b[0]); o[1] = sub(a[1], b[1]); o[2] = sub(a[2], b[2]);
+}
+PW_HD void cross3(const double *a, const double *b, double *o)
+{
+	o[0] = sub(mul(a[1], b[2]), mul(a[2], b[1]));
+	o[1] = sub(mul(a[2], b[0]), mul(a[0], b[2]));
+	o[2] = sub(mul(a[0], b[1]), mul(a[1], b[0]));
+}
+PW_HD double dot3(const double *a, const double *b)
+{
+	return add(add(mul(a[0], b[0]), mul(a[1], b[1])), mul(a[2], b[2]));
+}
+
+PW_HD int edge_edge(double ax, double ay, const double *v0, const double *u0, const double *u1, int i0, int i1)
+{
+	const double bx = sub(u0[i0], u1[i0]);
+	const double by = sub(u0[i1], u1[i1]);
+	const double cx = sub(v0[i0], u0[i0]);
+	const double cy = sub(v0[i1], u0[i1]);
+	const double f = sub(mul(ay, bx), mul(ax, by));
+	const double d = sub(mul(by, cx), mul(bx, cy));
+	if ((f > 0.0 && d >= 0.0 && d <= f) || (f < 0.0 && d <= 0.0 && d >= f)) {
+		const double e = sub(mul(ax, cy), mul(ay, cx));
+		if (f > 0.0) {
+			if (e >= 0.0 && e <= f)
+				return 1;
+		} else {
+			if (e <= 0.0 && e >= f)
+				return 1;
+		}
+	}
+	return 0;
+}
+
+PW_HD int edge_against_tri(const double *v0, const double *v1, const double *const *U, int i0, int i1)
+{
+	const double ax = sub(v1[i0], v0[i0]);
+	const double ay = sub(v1[i1], v0[i1]);
+	if (edge_edge(ax, ay, v0, U[0], U[1], i0, i1)) return 1;
+	if (edge_edge(ax, ay, v0, U[1], U[2], i0, i1)) return 1;
+	if (edge_edge(ax, ay, v0, U[2], U[0], i0, i1)) return 1;
+	return 0;
+}
+
+PW_HD int point_in_tri(const double *p, const double *const *U, int i0, int i1)
+{
+	double dd[3];
+#pragma unroll
+	for (int k = 0; k < 3; k++) {
+		const double *a0 = U[k];
+		const double *a1 = U[k == 2 ? 0 : k + 1];
+		const double a = sub(a1[i1], a0[i1]);
+		const double b = -sub(a1[i0], a0[i0]);
+		const double c = sub(mul(-a, a0[i0]), mul(b, a0[i1]));
+		dd[k] = add(add(mul(a, p[i0]), mul(b, p[i1])), c);
+	}
+	return (mul(dd[0], dd[1]) > 0.0 && mul(dd[0], dd[2]) > 0.0) ? 1 : 0;
+}
+
+PW_HD int coplanar_test(const double *N, const double *const *V, const double *const *U)
+{
+	const double a0 = dabs(N[0]), a1 = dabs(N[1]), a2 = dabs(N[2]);
+	int i0, i1;
+	if (a0 > a1) {
+		if (a0 > a2) { i0 = 1; i1 = 2; }
+		else         { i0 = 0; i1 = 1; }
+	} else {
+		if (a2 > a1) { i0 = 0; i1 = 1; }
+		else         { i0 = 0; i1 = 2; }
+	}
+	if (edge_against_tri(V[0], V[1], U, i0, i1)) return 1;
+	if (edge_against_tri(V[1], V[2], U, i0, i1)) return 1;
+	if (edge_against_tri(V[2], V[0], U, i0, i1)) return 1;
+	if (point_in_tri(V[0], U, i0, i1)) return 1;
+	if (point_in_tri(U[0], V, i0, i1)) return 1;
+	return 0;
+}
+
+PW_HD void plane_dists(const double *const *S, const double *const *T, double eps, double *N, double *dist)
+{
+	double e1[3], e2[3];
+	sub3(S[1], S[0], e1);
+	sub3(S[2], S[0], e2);
+	cross3(e1, e2, N);
+	const double d = -dot3(N, S[0]);
+#pragma unroll
+	for (int k = 0; k < 3; k++) {
+		double v = add(dot3(N, T[k]), d);
+		if (dabs(v) < eps)
+			v = 0.0;
+		dist[k] = v;
+	}
+}
+
+PW_HD int lone_vertex(const double *D)
+{
+	if (mul(D[0], D[1]) > 0.0) return 2;
+	if (mul(D[0], D[2]) > 0.0) return 1;
+	if (mul(D[1], D[2]) > 0.0 || D[0] != 0.0) return 0;
+	if (D[1] != 0.0) return 1;
+	if (D[2] != 0.0) return 2;
+	return -1;
+}
+
+PW_HD void others(int lone, int &o1, int &o2)
+{
+	if (lone == 0) { o1 = 1; o2 = 2; }
+	else if (lone == 1) { o1 = 0; o2 = 2; }
+	else { o1 = 0; o2 = 1; }
+}
+
+PW_HD int max_axis(const double *D)
+{
+	double m = dabs(D[0]);
+	int idx = 0;
+	const double b = dabs(D[1]), c = dabs(D[2]);
+	if (b > m) { m = b; idx = 1; }
+	if (c > m) { m = c; idx = 2; }
+	return idx;
+}
+
+PW_HD void interval(const double *const *T, const double *D, int lone, int ax, double *out)
+{
+	int o1, o2;
+	others(lone, o1, o2);
+	const double pl = T[lone][ax];
+	out[0] = add(pl, dvd(mul(sub(T[o1][ax], pl), D[lone]), sub(D[lone], D[o1])));
+	out[1] = add(pl, dvd(mul(sub(T[o2][ax], pl), D[lone]), sub(D[lone], D[o2])));
+}
+
+// Boolean test: V = env triangle (first), U = robot triangle (second).
+PW_HD int tri_tri(const double *V0, const double *V1, const double *V2,
+                  const double *U0, const double *U1, const double *U2, double eps)
+{
+	const double *V[3] = { V0, V1, V2 };
+	const double *U[3] = { U0, U1, U2 };
+	double N1[3], N2[3], du[3], dv[3];
+	plane_dists(V, U, eps, N1, du);
+	if (mul(du[0], du[1]) > 0.0 && mul(du[0], du[2]) > 0.0)
+		return 0;
+	plane_dists(U, V, eps, N2, dv);
+	if (mul(dv[0], dv[1]) > 0.0 && mul(dv[0], dv[2]) > 0.0)
+		return 0;
+	double Dl[3];
+	cross3(N1, N2, Dl);
+	const int ax = max_axis(Dl);
+	const int lv = lone_vertex(dv);
+	if (lv < 0)
+		return coplanar_test(N1, V, U);
+	const int lu = lone_vertex(du);
+	if (lu < 0)
+		return coplanar_test(N1, V, U);
+	double iv[2], iu[2];
+	interval(V, dv, lv, ax, iv);
+	interval(U, du, lu, ax, iu);
+	if (iv[0] > iv[1]) { const double c = iv[0]; iv[0] = iv[1]; iv[1] = c; }
+	if (iu[0] > iu[1]) { const double c = iu[0]; iu[0] = iu[1]; iu[1] = c; }
+	if (iv[1] < iu[0] || iu[1] < iv[0])
+		return 0;
+	return 1;
+}
+
+PW_HD void interval_pts(const double *const *T, const double *D, int lone, int ax,
+                        double *iv, double *p0, double *p1)
+{
+	int o1, o2;
+	others(lone, o1, o2);
+	const double *A = T[lone];
+	const double pl = A[ax];
+	double r = dvd(D[lone], sub(D[lone], D[o1]));
+	iv[0] = add(pl, mul(sub(T[o1][ax], pl), r));
+#pragma unroll
+	for (int c = 0; c < 3; c++)
+		p0[c] = add(mul(sub(T[o1][c], A[c]), r), A[c]);
+	r = dvd(D[lone], sub(D[lone], D[o2]));
+	iv[1] = add(pl, mul(sub(T[o2][ax], pl), r));
+#pragma unroll
+	for (int c = 0; c < 3; c++)
+		p1[c] = add(A[c], mul(sub(T[o2][c], A[c]), r));
+}
+
+// Test with the intersection segment (Moeller's 2001 extension).  Points are
+// zero for misses and coplanar pairs.
+PW_HD int tri_tri_isect(const double *V0, const double *V1, const double *V2,
+                        const double *U0, const double *U1, const double *U2, double eps,
+                        int *coplanar, double *pt1, double *pt2)
+{
+	const double *V[3] = { V0, V1, V2 };
+	const double *U[3] = { U0, U1, U2 };
+	double N1[3], N2[3], du[3], dv[3];
+	*coplanar = 0;
+	for (int c = 0; c < 3; c++) { pt1[c] = 0.0; pt2[c] = 0.0; }
+	plane_dists(V, U, eps, N1, du);
+	if (mul(du[0], du[1]) > 0.0 && mul(du[0], du[2]) > 0.0)
+		return 0;
+	plane_dists(U, V, eps, N2, dv);
+	if (mul(dv[0], dv[1]) > 0.0 && mul(dv[0], dv[2]) > 0.0)
+		return 0;
+	double Dl[3];
+	cross3(N1, N2, Dl);
+	const int ax = max_axis(Dl);
+	const int lv = lone_vertex(dv);
+	if (lv < 0) {
+		*coplanar = 1;
+		return coplanar_test(N1, V, U);
+	}
+	const int lu = lone_vertex(du);
+	if (lu < 0) {
+		*coplanar = 1;
+		return coplanar_test(N1, V, U);
+	}
+	double iv[2], iu[2], a1[3], a2[3], b1[3], b2[3];
+	interval_pts(V, dv, lv, ax, iv, a1, a2);
+	interval_pts(U, du, lu, ax, iu, b1, b2);
+	int sv = 0, su = 0;
+	if (iv[0] > iv[1]) { const double c = iv[0]; iv[0] = iv[1]; iv[1] = c; sv = 1; }
+	if (iu[0] > iu[1]) { const double c = iu[0]; iu[0] = iu[1]; iu[1] = c; su = 1; }
+	if (iv[1] < iu[0] || iu[1] < iv[0])
+		return 0;
+	const double *s, *e;
+	if (iu[0] < iv[0]) {
+		s = sv ? a2 : a1;
+		if (iu[1] < iv[1]) e = su ? b1 : b2;
+		else               e = sv ? a1 : a2;
+	} else {
+		s = su ? b2 : b1;
+		if (iu[1] > iv[1]) e = sv ? a1 : a2;
+		else               e = su ? b1 : b2;
+	}
+	for (int c = 0; c < 3; c++) { pt1[c] = s[c]; pt2[c] = e[c]; }
+	return 1;
+}
+
+// ---------------------------------------------------------------- boxes
+
+// Separating-axis test of an axis-aligned box (half-extents ea) against a box
+// with axes = columns of R, half-extents eb, centre offset T; AR = |R| + slack.
+// 1 = a separating axis exists (strict), 0 = overlap or touch.
+PW_HD int sat_disjoint(const double *ea, const double *eb, const double *T, const double *R, const double *AR)
+{
+	for (int i = 0; i < 3; i++) {
+		const double rb = add(add(mul(eb[0], AR[3 * i + 0]), mul(eb[1], AR[3 * i + 1])), mul(eb[2], AR[3 * i + 2]));
+		if (dabs(T[i]) > add(ea[i], rb)) return 1;
+	}
+	for (int j = 0; j < 3; j++) {
+		const double tl = add(add(mul(T[0], R[0 + j]), mul(T[1], R[3 + j])), mul(T[2], R[6 + j]));
+		const double ra = add(add(mul(ea[0], AR[0 + j]), mul(ea[1], AR[3 + j])), mul(ea[2], AR[6 + j]));
+		if (dabs(tl) > add(ra, eb[j])) return 1;
+	}
+	for (int i = 0; i < 3; i++) {
+		const int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+		for (int j = 0; j < 3; j++) {
+			const int j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+			const double tl = sub(mul(T[i2], R[3 * i1 + j]), mul(T[i1], R[3 * i2 + j]));
+			const double ra = add(mul(ea[i1], AR[3 * i2 + j]), mul(ea[i2], AR[3 * i1 + j]));
+			const double rb = add(mul(eb[j1], AR[3 * i + j2]), mul(eb[j2], AR[3 * i + j1]));
+			if (dabs(tl) > add(ra, rb)) return 1;
+		}
+	}
+	return 0;
+}
+
+// isDisentangled box test: robot local AABB box (rc, rh) placed by the state,
+// env box (ec, eh) placed by the perturbation transform (Re, te).
+PW_HD int boxes_disjoint(const double *q, const double *rc, const double *rh,
+                         const double *Re, const double *te, const double *ec, const double *eh)
+{
+	double R[9], t[3], cr[3], ce[3], d[3], Rr[9], T[3], AR[9];
+	state_transform(q, R, t);
+	xform_point(R, t, rc, cr);
+	xform_point(Re, te, ec, ce);
+	for (int c = 0; c < 3; c++) d[c] = sub(cr[c], ce[c]);
+	for (int i = 0; i < 3; i++) {
+		T[i] = add(add(mul(Re[0 + i], d[0]), mul(Re[3 + i], d[1])), mul(Re[6 + i], d[2]));
+		for (int j = 0; j < 3; j++)
+			Rr[3 * i + j] = add(add(mul(Re[0 + i], R[0 + j]), mul(Re[3 + i], R[3 + j])), mul(Re[6 + i], R[6 + j]));
+	}
+	for (int i = 0; i < 9; i++) AR[i] = dabs(Rr[i]);
+	return sat_disjoint(eh, rh, T, Rr, AR);
+}
+
+} // namespace pwm

@@ -1,0 +1,910 @@
+// pw_world.cu -- world life cycle, the unit-world recipe and the GPU LBVH build.
+//
+// The unit-world recipe restates lib/osr/unit_world.cc:94-161 (load,
+// scaleToUnit, angleModel), lib/osr/scene.cc:141-145,211-229 (vertex mean,
+// moveToCenter, scale), lib/osr/bbox.h:21-51 (bounding box seeded at the
+// origin) and lib/osr/cdmodel.cc:120-160 (the float xform applied in double).
+// The BVH replaces FCL's BVHModel<OBBRSS> (cdmodel.cc:17-18,85-114) with a
+// linear BVH built on the device: 30-bit Morton codes of triangle centroids,
+// a radix sort, Karras' 2012 parallel hierarchy construction and a bottom-up
+// refit of conservative FP32 boxes.
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "pw_internal.cuh"
+#include "pw_math.cuh"
+
+static thread_local std::string g_last_error;
+
+int pw_fail(int code, const std::string &msg)
+{
+	g_last_error = msg;
+	return code;
+}
+
+int pw_cuda_fail(cudaError_t e, const char *what)
+{
+	g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+	if (e == cudaErrorMemoryAllocation)
+		return PW_ERR_OUT_OF_MEMORY;
+	return PW_ERR_CUDA;
+}
+
+cudaError_t DeviceBuffer::reserve(size_t need)
+{
+	if (need <= bytes && ptr)
+		return cudaSuccess;
+	release();
+	size_t n = need < 256 ? 256 : need;
+	cudaError_t e = cudaMalloc(&ptr, n);
+	if (e != cudaSuccess) {
+		ptr = nullptr;
+		bytes = 0;
+		return e;
+	}
+	bytes = n;
+	return cudaSuccess;
+}
+
+void DeviceBuffer::release()
+{
+	if (ptr)
+		cudaFree(ptr);
+	ptr = nullptr;
+	bytes = 0;
+}
+
+extern "C" const char *pw_last_error(void) { return g_last_error.c_str(); }
+
+// ------------------------------------------------------------------ life cycle
+
+extern "C" int pw_world_create(pw_world **out, int device)
+{
+	if (!out)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_create: out is NULL");
+	int ndev = 0;
+	PW_CUDA(cudaGetDeviceCount(&ndev));
+	if (device < 0 || device >= ndev)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_create: no such CUDA device");
+	PW_CUDA(cudaSetDevice(device));
+	pw_world *w = new pw_world();
+	w->device = device;
+	pwm::state_transform(w->pert, w->pertR, w->pert_t);
+	cudaDeviceGetAttribute(&w->num_sms, cudaDevAttrMultiProcessorCount, device);
+	*out = w;
+	return PW_OK;
+}
+
+void pw_free_mesh_device(pw_world *w)
+{
+	for (void *p : w->mesh_allocs)
+		cudaFree(p);
+	w->mesh_allocs.clear();
+	w->dev.env = MeshDev();
+	w->dev.rob = MeshDev();
+}
+
+extern "C" int pw_world_destroy(pw_world *w)
+{
+	if (!w)
+		return PW_OK;
+	cudaSetDevice(w->device);
+	pw_free_mesh_device(w);
+	for (cudaEvent_t &e : w->ev)
+		if (e)
+			cudaEventDestroy(e);
+	delete w;
+	return PW_OK;
+}
+
+static int check_mesh(const float *V, int64_t nv, const uint32_t *F, int64_t nf, const char *who)
+{
+	if (nv < 0 || nf < 0 || (nv > 0 && !V) || (nf > 0 && !F))
+		return pw_fail(PW_ERR_INVALID_ARG, std::string(who) + ": bad mesh pointers or sizes");
+	if (nv > (int64_t(1) << 30) || nf > (int64_t(1) << 29))
+		return pw_fail(PW_ERR_INVALID_ARG, std::string(who) + ": mesh too large");
+	for (int64_t i = 0; i < 3 * nf; i++)
+		if (F[i] >= (uint64_t)nv)
+			return pw_fail(PW_ERR_INVALID_ARG, std::string(who) + ": face index out of range");
+	for (int64_t i = 0; i < 3 * nv; i++)
+		if (!std::isfinite(V[i]))
+			return pw_fail(PW_ERR_INVALID_ARG, std::string(who) + ": non-finite vertex");
+	return PW_OK;
+}
+
+// Float mean of the vertices, summed in order (the OMPL centre, scene.cc:40-50,141-145).
+static void float_mean(const std::vector<float> &V, float out[3])
+{
+	float acc[3] = { 0.f, 0.f, 0.f };
+	const size_t n = V.size() / 3;
+	for (size_t i = 0; i < n; i++)
+		for (int c = 0; c < 3; c++)
+			acc[c] = acc[c] + V[3 * i + c];
+	for (int c = 0; c < 3; c++)
+		out[c] = n ? acc[c] / (float)n : 0.0f;
+}
+
+extern "C" int pw_world_load_env(pw_world *w, const float *V, int64_t nv, const uint32_t *F, int64_t nf)
+{
+	if (!w)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_load_env: world is NULL");
+	int rc = check_mesh(V, nv, F, nf, "pw_world_load_env");
+	if (rc)
+		return rc;
+	w->Ve.assign(V, V + 3 * nv);
+	w->Fe.assign(F, F + 3 * nf);
+	w->has_env = true;
+	w->ready = false;
+	return PW_OK;
+}
+
+extern "C" int pw_world_load_robot(pw_world *w, const float *V, int64_t nv, const uint32_t *F, int64_t nf)
+{
+	if (!w)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_load_robot: world is NULL");
+	int rc = check_mesh(V, nv, F, nf, "pw_world_load_robot");
+	if (rc)
+		return rc;
+	w->Vr.assign(V, V + 3 * nv);
+	w->Fr.assign(F, F + 3 * nf);
+	w->has_rob = true;
+	w->ready = false;
+	float_mean(w->Vr, w->ompl_center);
+	for (int c = 0; c < 3; c++)
+		w->center[c] = w->ompl_center[c];
+	return PW_OK;
+}
+
+extern "C" int pw_world_enforce_robot_center(pw_world *w, const double c[3])
+{
+	if (!w || !c)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_enforce_robot_center: NULL argument");
+	if (!w->has_rob)
+		return pw_fail(PW_ERR_NO_MODEL, "pw_world_enforce_robot_center: robot not loaded");
+	for (int k = 0; k < 3; k++)
+		w->center[k] = (float)c[k];
+	return PW_OK;
+}
+
+// Bounding box seeded at the origin (bbox.h:21-51): the span includes the origin.
+static float span_of(const std::vector<float> &V)
+{
+	float lo[3] = { 0.f, 0.f, 0.f }, hi[3] = { 0.f, 0.f, 0.f };
+	const size_t n = V.size() / 3;
+	for (size_t i = 0; i < n; i++)
+		for (int c = 0; c < 3; c++) {
+			const float x = V[3 * i + c];
+			hi[c] = std::max(x, hi[c]);
+			lo[c] = std::min(x, lo[c]);
+		}
+	return std::max(std::max(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+}
+
+extern "C" int pw_world_scale_to_unit(pw_world *w)
+{
+	if (!w)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_scale_to_unit: world is NULL");
+	if (!w->has_env)
+		return pw_fail(PW_ERR_NO_MODEL, "pw_world_scale_to_unit: environment not loaded");
+	const float se = span_of(w->Ve);
+	const float sr = w->has_rob ? span_of(w->Vr) : 1.0f;
+	w->scale = (float)(1.0 / (double)std::max(se, sr));
+	w->scaled = true;
+	return PW_OK;
+}
+
+static void apply_perturbation_to_env(pw_world *w)
+{
+	const size_t n = w->env_local.size() / 3;
+	w->env_world.resize(w->env_local.size());
+	for (size_t i = 0; i < n; i++)
+		pwm::xform_point(w->pertR, w->pert_t, &w->env_local[3 * i], &w->env_world[3 * i]);
+}
+
+static void local_box(const std::vector<double> &V, double c[3], double h[3])
+{
+	double lo[3] = { INFINITY, INFINITY, INFINITY }, hi[3] = { -INFINITY, -INFINITY, -INFINITY };
+	const size_t n = V.size() / 3;
+	for (size_t i = 0; i < n; i++)
+		for (int k = 0; k < 3; k++) {
+			lo[k] = std::min(lo[k], V[3 * i + k]);
+			hi[k] = std::max(hi[k], V[3 * i + k]);
+		}
+	for (int k = 0; k < 3; k++) {
+		c[k] = n ? (lo[k] + hi[k]) * 0.5 : 0.0;
+		h[k] = n ? (hi[k] - lo[k]) * 0.5 : 0.0;
+	}
+}
+
+extern "C" int pw_world_angle_model(pw_world *w, float latitude, float longitude)
+{
+	if (!w)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_angle_model: world is NULL");
+	if (latitude != 0.0f || longitude != 0.0f)
+		return pw_fail(PW_ERR_INVALID_ARG,
+		               "The arguments of UnitWorld::angleModel are reserved for compatibility; both must be 0.");
+	if (!w->has_env || !w->has_rob)
+		return pw_fail(PW_ERR_NO_MODEL, "pw_world_angle_model: environment and robot must both be loaded");
+	if (!w->scaled)
+		return pw_fail(PW_ERR_NO_MODEL, "pw_world_angle_model: call scale_to_unit first");
+	PW_CUDA(cudaSetDevice(w->device));
+	const double s = (double)w->scale;
+	// env: xform = S(s); robot: xform = S(s) T(-c), translation column fl32(s * -c)
+	w->env_local.resize(w->Ve.size());
+	for (size_t i = 0; i < w->Ve.size(); i++)
+		w->env_local[i] = s * (double)w->Ve[i];
+	float tr[3];
+	for (int c = 0; c < 3; c++)
+		tr[c] = w->scale * (-w->center[c]);
+	w->rob_local.resize(w->Vr.size());
+	for (size_t i = 0; i < w->Vr.size() / 3; i++)
+		for (int c = 0; c < 3; c++)
+			w->rob_local[3 * i + c] = s * (double)w->Vr[3 * i + c] + (double)tr[c];
+	local_box(w->env_local, w->env_box_c, w->env_box_h);
+	local_box(w->rob_local, w->rob_box_c, w->rob_box_h);
+	apply_perturbation_to_env(w);
+	pw_free_mesh_device(w);
+	w->ready = false;
+	int rc = pw_build_mesh_device(w, w->dev.env, w->env_world, w->Fe);
+	if (rc)
+		return rc;
+	rc = pw_build_mesh_device(w, w->dev.rob, w->rob_local, w->Fr);
+	if (rc)
+		return rc;
+	w->dev.del_env = 5.9604645e-08f * w->dev.env.emax * 1.0001f;
+	w->ready = true;
+	return PW_OK;
+}
+
+extern "C" int pw_world_set_perturbation(pw_world *w, const double q[7])
+{
+	if (!w || !q)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_set_perturbation: NULL argument");
+	for (int i = 0; i < 7; i++)
+		if (!std::isfinite(q[i]))
+			return pw_fail(PW_ERR_INVALID_ARG, "pw_world_set_perturbation: non-finite state");
+	memcpy(w->pert, q, sizeof(double) * 7);
+	pwm::state_transform(w->pert, w->pertR, w->pert_t);
+	if (w->ready) {
+		PW_CUDA(cudaSetDevice(w->device));
+		apply_perturbation_to_env(w);
+		// rebuild only the env mesh; keep the robot
+		MeshDev rob = w->dev.rob;
+		std::vector<void *> keep;
+		for (void *p : w->mesh_allocs) {
+			bool robp = p == rob.nodeA || p == rob.nodeB || p == rob.triA || p == rob.triB || p == rob.triC ||
+			            p == rob.V64 || p == rob.F;
+			if (robp)
+				keep.push_back(p);
+			else
+				cudaFree(p);
+		}
+		w->mesh_allocs = keep;
+		w->ready = false;
+		int rc = pw_build_mesh_device(w, w->dev.env, w->env_world, w->Fe);
+		if (rc)
+			return rc;
+		w->dev.del_env = 5.9604645e-08f * w->dev.env.emax * 1.0001f;
+		w->ready = true;
+	}
+	return PW_OK;
+}
+
+extern "C" int pw_world_get_perturbation(const pw_world *w, double q[7])
+{
+	if (!w || !q)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_get_perturbation: NULL argument");
+	memcpy(q, w->pert, sizeof(double) * 7);
+	return PW_OK;
+}
+
+extern "C" int pw_world_info_get(const pw_world *w, pw_world_info *o)
+{
+	if (!w || !o)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_info_get: NULL argument");
+	memset(o, 0, sizeof(*o));
+	o->scene_scale = (double)w->scale;
+	for (int c = 0; c < 3; c++) {
+		o->robot_center[c] = w->center[c];
+		o->robot_ompl_center[c] = w->ompl_center[c];
+	}
+	// scene xform S(s); robot xform S(s) T(-c), both float, as row-major doubles
+	for (int i = 0; i < 16; i++) {
+		o->scene_matrix[i] = 0.0;
+		o->robot_matrix[i] = 0.0;
+	}
+	for (int i = 0; i < 3; i++) {
+		o->scene_matrix[5 * i] = (double)w->scale;
+		o->robot_matrix[5 * i] = (double)w->scale;
+		o->robot_matrix[4 * i + 3] = (double)(w->scale * (-w->center[i]));
+	}
+	o->scene_matrix[15] = 1.0;
+	o->robot_matrix[15] = 1.0;
+	o->env_vertices = (int64_t)(w->Ve.size() / 3);
+	o->env_faces = (int64_t)(w->Fe.size() / 3);
+	o->robot_vertices = (int64_t)(w->Vr.size() / 3);
+	o->robot_faces = (int64_t)(w->Fr.size() / 3);
+	o->env_bvh_depth = w->dev.env.depth;
+	o->robot_bvh_depth = w->dev.rob.depth;
+	o->ready = w->ready ? 1 : 0;
+	o->device = w->device;
+	return PW_OK;
+}
+
+extern "C" int pw_world_cd_vertices(const pw_world *w, int geo, double *out)
+{
+	if (!w || !out || (geo != PW_GEO_ENV && geo != PW_GEO_ROB))
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_cd_vertices: bad argument");
+	if (!w->ready)
+		return pw_fail(PW_ERR_NO_MODEL, "pw_world_cd_vertices: world not set up");
+	const std::vector<double> &V = geo == PW_GEO_ENV ? w->env_world : w->rob_local;
+	memcpy(out, V.data(), sizeof(double) * V.size());
+	return PW_OK;
+}
+
+extern "C" int pw_world_cd_faces(const pw_world *w, int geo, int32_t *out)
+{
+	if (!w || !out || (geo != PW_GEO_ENV && geo != PW_GEO_ROB))
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_cd_faces: bad argument");
+	const std::vector<uint32_t> &F = geo == PW_GEO_ENV ? w->Fe : w->Fr;
+	for (size_t i = 0; i < F.size(); i++)
+		out[i] = (int32_t)F[i];
+	return PW_OK;
+}
+
+// ------------------------------------------------------------------ frames
+
+// Hamilton product a * b, quaternions (w, x, y, z).
+static void quat_mul(const double *a, const double *b, double *o)
+{
+	using namespace pwm;
+	o[0] = sub(sub(sub(mul(a[0], b[0]), mul(a[1], b[1])), mul(a[2], b[2])), mul(a[3], b[3]));
+	o[1] = sub(add(add(mul(a[0], b[1]), mul(a[1], b[0])), mul(a[2], b[3])), mul(a[3], b[2]));
+	o[2] = add(add(sub(mul(a[0], b[2]), mul(a[1], b[3])), mul(a[2], b[0])), mul(a[3], b[1]));
+	o[3] = add(sub(add(mul(a[0], b[3]), mul(a[1], b[2])), mul(a[2], b[1])), mul(a[3], b[0]));
+}
+
+static void mat_vec(const double *R, const double *v, double *o)
+{
+	for (int i = 0; i < 3; i++)
+		o[i] = pwm::add(pwm::add(pwm::mul(R[3 * i], v[0]), pwm::mul(R[3 * i + 1], v[1])), pwm::mul(R[3 * i + 2], v[2]));
+}
+
+// decompose (osr_state.cc:85-92): translation and normalised rotation.
+static void decompose(const double *q, double *t, double *rot)
+{
+	t[0] = q[0]; t[1] = q[1]; t[2] = q[2];
+	const double r[4] = { q[3], q[4], q[5], q[6] };
+	pwm::quat_normalize(r, rot);
+}
+
+// compose (osr_state.cc:107-119): the rotation is normalised again.
+static void compose(const double *t, const double *rot, double *q)
+{
+	double r[4];
+	pwm::quat_normalize(rot, r);
+	q[0] = t[0]; q[1] = t[1]; q[2] = t[2];
+	q[3] = r[0]; q[4] = r[1]; q[5] = r[2]; q[6] = r[3];
+}
+
+// applyPertubation (unit_world.cc:713-724).
+static void apply_pert(const pw_world *w, const double *in, double *out)
+{
+	double t[3], rot[4], pt[3], prot[4], qret[4], R[9], Rt[3], tret[3];
+	decompose(in, t, rot);
+	decompose(w->pert, pt, prot);
+	quat_mul(prot, rot, qret);
+	pwm::quat_to_matrix(prot, R);
+	mat_vec(R, t, Rt);
+	for (int c = 0; c < 3; c++) tret[c] = pwm::add(pt[c], Rt[c]);
+	compose(tret, qret, out);
+}
+
+// unapplyPertubation (unit_world.cc:726-737).
+static void unapply_pert(const pw_world *w, const double *in, double *out)
+{
+	double t[3], rot[4], pt[3], prot[4], inv[4], R[9], d[3], tret[3], qret[4];
+	decompose(in, t, rot);
+	decompose(w->pert, pt, prot);
+	const double n2 = pwm::add(pwm::add(pwm::add(pwm::mul(prot[1], prot[1]), pwm::mul(prot[2], prot[2])),
+	                                    pwm::mul(prot[3], prot[3])), pwm::mul(prot[0], prot[0]));
+	inv[0] = prot[0] / n2; inv[1] = -prot[1] / n2; inv[2] = -prot[2] / n2; inv[3] = -prot[3] / n2;
+	pwm::quat_to_matrix(inv, R);
+	for (int c = 0; c < 3; c++) d[c] = pwm::add(-pt[c], t[c]);
+	mat_vec(R, d, tret);
+	quat_mul(inv, rot, qret);
+	compose(tret, qret, out);
+}
+
+static void to_unit(const pw_world *w, const double *in, double *out)
+{
+	double tmp[7];
+	const double s = (double)w->scale;
+	for (int c = 0; c < 3; c++) tmp[c] = pwm::mul(s, in[c]);
+	for (int c = 3; c < 7; c++) tmp[c] = in[c];
+	apply_pert(w, tmp, out);
+}
+
+static void from_unit(const pw_world *w, const double *in, double *out)
+{
+	double tmp[7];
+	unapply_pert(w, in, tmp);
+	const double inv = 1.0 / (double)w->scale;
+	for (int c = 0; c < 3; c++) out[c] = pwm::mul(inv, tmp[c]);
+	for (int c = 3; c < 7; c++) out[c] = tmp[c];
+}
+
+static int check_conv(const pw_world *w, const double *in, int64_t n, const double *out, const char *who)
+{
+	if (!w || (n > 0 && (!in || !out)) || n < 0)
+		return pw_fail(PW_ERR_INVALID_ARG, std::string(who) + ": bad argument");
+	if (!w->scaled)
+		return pw_fail(PW_ERR_NO_MODEL, std::string(who) + ": world not scaled");
+	return PW_OK;
+}
+
+extern "C" int pw_world_translate_to_unit(const pw_world *w, const double *in, int64_t n, double *out)
+{
+	int rc = check_conv(w, in, n, out, "pw_world_translate_to_unit");
+	if (rc) return rc;
+	for (int64_t i = 0; i < n; i++)
+		to_unit(w, in + 7 * i, out + 7 * i);
+	return PW_OK;
+}
+
+extern "C" int pw_world_translate_from_unit(const pw_world *w, const double *in, int64_t n, double *out)
+{
+	int rc = check_conv(w, in, n, out, "pw_world_translate_from_unit");
+	if (rc) return rc;
+	for (int64_t i = 0; i < n; i++)
+		from_unit(w, in + 7 * i, out + 7 * i);
+	return PW_OK;
+}
+
+// translateOMPLStateToUnitState (unit_world.cc:689-711): w-last -> w-first, to unit,
+// then t' = t - R(q) * (ompl_centre - centre) * scale.
+extern "C" int pw_world_translate_ompl_to_unit(const pw_world *w, const double *in, int64_t n, double *out)
+{
+	int rc = check_conv(w, in, n, out, "pw_world_translate_ompl_to_unit");
+	if (rc) return rc;
+	double dc[3];
+	for (int c = 0; c < 3; c++)
+		dc[c] = (double)(w->ompl_center[c] - w->center[c]) * (double)w->scale;
+	for (int64_t i = 0; i < n; i++) {
+		const double *p = in + 7 * i;
+		const double wf[7] = { p[0], p[1], p[2], p[6], p[3], p[4], p[5] };
+		double u[7], t[3], rot[4], R[9], Rd[3], t2[3];
+		to_unit(w, wf, u);
+		decompose(u, t, rot);
+		pwm::quat_to_matrix(rot, R);
+		mat_vec(R, dc, Rd);
+		for (int c = 0; c < 3; c++) t2[c] = pwm::sub(t[c], Rd[c]);
+		compose(t2, rot, out + 7 * i);
+	}
+	return PW_OK;
+}
+
+// translateUnitStateToOMPLState (unit_world.cc:556-590).
+extern "C" int pw_world_translate_unit_to_ompl(const pw_world *w, const double *in, int64_t n, double *out,
+                                               int to_angle_axis)
+{
+	int rc = check_conv(w, in, n, out, "pw_world_translate_unit_to_ompl");
+	if (rc) return rc;
+	double dc[3];
+	for (int c = 0; c < 3; c++)
+		dc[c] = (double)(w->ompl_center[c] - w->center[c]) * (double)w->scale;
+	for (int64_t i = 0; i < n; i++) {
+		double t[3], rot[4], R[9], Rd[3], t2[3], c7[7], o[7];
+		decompose(in + 7 * i, t, rot);
+		pwm::quat_to_matrix(rot, R);
+		mat_vec(R, dc, Rd);
+		for (int c = 0; c < 3; c++) t2[c] = pwm::add(t[c], Rd[c]);
+		compose(t2, rot, c7);
+		from_unit(w, c7, o);
+		double *dst = out + 7 * i;
+		dst[0] = o[0]; dst[1] = o[1]; dst[2] = o[2];
+		if (to_angle_axis) {
+			// angle-axis of the w-first quaternion: angle = 2 atan2(|v|, |w|) with the axis
+			// sign following w, as Eigen::AngleAxis does from a quaternion
+			const double vn = std::sqrt(o[4] * o[4] + o[5] * o[5] + o[6] * o[6]);
+			double ang = 2.0 * std::atan2(vn, std::fabs(o[3]));
+			double ax[3] = { 1.0, 0.0, 0.0 };
+			if (vn > 0.0) {
+				const double sgn = o[3] < 0.0 ? -1.0 : 1.0;
+				for (int c = 0; c < 3; c++) ax[c] = sgn * o[4 + c] / vn;
+			}
+			dst[3] = ang; dst[4] = ax[0]; dst[5] = ax[1]; dst[6] = ax[2];
+		} else {
+			dst[3] = o[4]; dst[4] = o[5]; dst[5] = o[6]; dst[6] = o[3];
+		}
+	}
+	return PW_OK;
+}
+
+// ------------------------------------------------------------------ host state math
+
+extern "C" int pw_state_distance(const double a[7], const double b[7], double *out)
+{
+	if (!a || !b || !out)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_state_distance: NULL argument");
+	*out = pwm::distance(a, b);
+	return PW_OK;
+}
+
+extern "C" int pw_state_interpolate(const double a[7], const double b[7], double tau, double out[7])
+{
+	if (!a || !b || !out)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_state_interpolate: NULL argument");
+	pwm::interpolate(a, b, tau, out);
+	return PW_OK;
+}
+
+extern "C" int pw_segment_step_state(const double from[7], const double to[7], double verify_delta, int64_t k,
+                                     double out[7], double *tau, int64_t *num_steps)
+{
+	if (!from || !to || !out || !tau || !num_steps)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_segment_step_state: NULL argument");
+	const double dist = pwm::distance(from, to);
+	if (!(verify_delta >= dist) && dist == dist && (!(verify_delta > 0.0) || dist / verify_delta > 1073741824.0))
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_segment_step_state: verify_delta must be > 0 and dist/verify_delta < 2^30");
+	int64_t K = 0;
+	if (!(verify_delta >= dist) && dist == dist) {
+		double delta = verify_delta;
+		while (delta <= dist) {
+			delta = pwm::advance_delta(delta, dist, verify_delta);
+			K++;
+		}
+	}
+	*num_steps = K;
+	if (k < 0 || k >= K)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_segment_step_state: step index out of range");
+	double delta = verify_delta;
+	for (int64_t j = 0; j < k; j++)
+		delta = pwm::advance_delta(delta, dist, verify_delta);
+	const double inv = pwm::dvd(1.0, dist);
+	*tau = pwm::mul(delta, inv);
+	pwm::interpolate(from, to, *tau, out);
+	return PW_OK;
+}
+
+// ------------------------------------------------------------------ LBVH build
+
+// Per triangle: FP32 vertices (nearest), conservative box (directed rounding), centroid.
+__global__ void k_tri_prep(const double *V, const int32_t *F, int n, float4 *ta, float4 *tb, float4 *tc,
+                           float *lo, float *hi, float *cen)
+{
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= n)
+		return;
+	double p[3][3];
+	for (int k = 0; k < 3; k++)
+		for (int c = 0; c < 3; c++)
+			p[k][c] = V[3 * F[3 * t + k] + c];
+	ta[t] = make_float4(__double2float_rn(p[0][0]), __double2float_rn(p[0][1]), __double2float_rn(p[0][2]),
+	                    __int_as_float(t));
+	tb[t] = make_float4(__double2float_rn(p[1][0]), __double2float_rn(p[1][1]), __double2float_rn(p[1][2]), 0.f);
+	tc[t] = make_float4(__double2float_rn(p[2][0]), __double2float_rn(p[2][1]), __double2float_rn(p[2][2]), 0.f);
+	for (int c = 0; c < 3; c++) {
+		const double mn = fmin(fmin(p[0][c], p[1][c]), p[2][c]);
+		const double mx = fmax(fmax(p[0][c], p[1][c]), p[2][c]);
+		const float l = __double2float_rd(mn), h = __double2float_ru(mx);
+		lo[3 * t + c] = l;
+		hi[3 * t + c] = h;
+		cen[3 * t + c] = 0.5f * (l + h);
+	}
+}
+
+// Single-block min/max of the centroids: out = (min.xyz, max.xyz).
+__global__ void k_bounds(const float *cen, int n, float *out)
+{
+	__shared__ float smin[3][256], smax[3][256];
+	float mn[3] = { INFINITY, INFINITY, INFINITY }, mx[3] = { -INFINITY, -INFINITY, -INFINITY };
+	for (int i = threadIdx.x; i < n; i += blockDim.x)
+		for (int c = 0; c < 3; c++) {
+			mn[c] = fminf(mn[c], cen[3 * i + c]);
+			mx[c] = fmaxf(mx[c], cen[3 * i + c]);
+		}
+	for (int c = 0; c < 3; c++) {
+		smin[c][threadIdx.x] = mn[c];
+		smax[c][threadIdx.x] = mx[c];
+	}
+	__syncthreads();
+	for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+		if (threadIdx.x < s)
+			for (int c = 0; c < 3; c++) {
+				smin[c][threadIdx.x] = fminf(smin[c][threadIdx.x], smin[c][threadIdx.x + s]);
+				smax[c][threadIdx.x] = fmaxf(smax[c][threadIdx.x], smax[c][threadIdx.x + s]);
+			}
+		__syncthreads();
+	}
+	if (threadIdx.x == 0)
+		for (int c = 0; c < 3; c++) {
+			out[c] = smin[c][0];
+			out[3 + c] = smax[c][0];
+		}
+}
+
+__device__ __forceinline__ uint32_t expand_bits10(uint32_t v)
+{
+	v = (v * 0x00010001u) & 0xFF0000FFu;
+	v = (v * 0x00000101u) & 0x0F00F00Fu;
+	v = (v * 0x00000011u) & 0xC30C30C3u;
+	v = (v * 0x00000005u) & 0x49249249u;
+	return v;
+}
+
+__global__ void k_morton(const float *cen, int n, const float *bounds, uint32_t *keys, uint32_t *vals)
+{
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= n)
+		return;
+	uint32_t code = 0;
+	uint32_t q[3];
+	for (int c = 0; c < 3; c++) {
+		const float ext = bounds[3 + c] - bounds[c];
+		float f = ext > 0.f ? (cen[3 * t + c] - bounds[c]) / ext : 0.5f;
+		f = fminf(fmaxf(f * 1024.f, 0.f), 1023.f);
+		q[c] = (uint32_t)f;
+	}
+	code = (expand_bits10(q[0]) << 2) | (expand_bits10(q[1]) << 1) | expand_bits10(q[2]);
+	keys[t] = code;
+	vals[t] = (uint32_t)t;
+}
+
+__device__ __forceinline__ int lcp_delta(const uint32_t *keys, int n, int i, int j)
+{
+	if (j < 0 || j >= n)
+		return -1;
+	const uint32_t a = keys[i], b = keys[j];
+	if (a == b)
+		return 32 + __clz((uint32_t)i ^ (uint32_t)j);
+	return __clz(a ^ b);
+}
+
+// Karras 2012: internal node i covers a key range; children are internal or leaf nodes.
+__global__ void k_karras(const uint32_t *keys, int n, int32_t *left, int32_t *right, int32_t *parent)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n - 1)
+		return;
+	const int d = (lcp_delta(keys, n, i, i + 1) - lcp_delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+	const int dmin = lcp_delta(keys, n, i, i - d);
+	int lmax = 2;
+	while (lcp_delta(keys, n, i, i + lmax * d) > dmin)
+		lmax *= 2;
+	int l = 0;
+	for (int t = lmax / 2; t >= 1; t /= 2)
+		if (lcp_delta(keys, n, i, i + (l + t) * d) > dmin)
+			l += t;
+	const int j = i + l * d;
+	const int dnode = lcp_delta(keys, n, i, j);
+	int s = 0;
+	int t = l;
+	do {
+		t = (t + 1) >> 1;
+		if (lcp_delta(keys, n, i, i + (s + t) * d) > dnode)
+			s += t;
+	} while (t > 1);
+	const int gamma = i + s * d + min(d, 0);
+	const int leaf_base = n - 1;
+	const int lc = (min(i, j) == gamma) ? leaf_base + gamma : gamma;
+	const int rc = (max(i, j) == gamma + 1) ? leaf_base + gamma + 1 : gamma + 1;
+	left[i] = lc;
+	right[i] = rc;
+	parent[lc] = i;
+	parent[rc] = i;
+}
+
+// Leaves: permute triangles into slot order and write leaf boxes, then refit
+// the ancestors bottom-up (the second child to arrive computes the union).
+__global__ void k_refit(const uint32_t *order, int n, const float *tlo, const float *thi, const float4 *ta,
+                        const float4 *tb, const float4 *tc, float4 *sa, float4 *sb, float4 *sc, float *blo,
+                        float *bhi, const int32_t *left, const int32_t *right, const int32_t *parent,
+                        unsigned int *flags)
+{
+	const int j = blockIdx.x * blockDim.x + threadIdx.x;
+	if (j >= n)
+		return;
+	const int leaf_base = n - 1;
+	const uint32_t t = order[j];
+	sa[j] = ta[t];
+	sb[j] = tb[t];
+	sc[j] = tc[t];
+	int node = leaf_base + j;
+	for (int c = 0; c < 3; c++) {
+		blo[3 * node + c] = tlo[3 * t + c];
+		bhi[3 * node + c] = thi[3 * t + c];
+	}
+	__threadfence();
+	int p = node == 0 ? -1 : parent[node];
+	while (p >= 0) {
+		if (atomicAdd(&flags[p], 1u) == 0)
+			return;
+		__threadfence();
+		const int l = left[p], r = right[p];
+		for (int c = 0; c < 3; c++) {
+			const float lo = fminf(__ldcg(&blo[3 * l + c]), __ldcg(&blo[3 * r + c]));
+			const float hi = fmaxf(__ldcg(&bhi[3 * l + c]), __ldcg(&bhi[3 * r + c]));
+			blo[3 * p + c] = lo;
+			bhi[3 * p + c] = hi;
+		}
+		__threadfence();
+		p = p == 0 ? -1 : parent[p];
+	}
+}
+
+// Boxes to (centre, half-extent) with [c - h, c + h] containing [lo, hi]; child links.
+__global__ void k_finalize(int nnodes, int n, const float *blo, const float *bhi, const int32_t *left,
+                           const int32_t *right, const float4 *sa, float4 *na, float4 *nb)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= nnodes)
+		return;
+	float c[3], h[3];
+	for (int k = 0; k < 3; k++) {
+		const double lo = blo[3 * i + k], hi = bhi[3 * i + k];
+		const float cf = __double2float_rn(0.5 * (lo + hi));
+		const double hh = fmax(hi - (double)cf, (double)cf - lo);
+		c[k] = cf;
+		h[k] = __double2float_ru(hh);
+	}
+	const int leaf_base = n - 1;
+	int l = -1, r = -1;
+	if (i < leaf_base) {
+		l = left[i];
+		r = right[i];
+	} else {
+		l = __float_as_int(sa[i - leaf_base].w);
+	}
+	na[i] = make_float4(c[0], c[1], c[2], __int_as_float(l));
+	nb[i] = make_float4(h[0], h[1], h[2], __int_as_float(r));
+}
+
+__global__ void k_depth(int n, const int32_t *parent, int *maxdepth)
+{
+	const int j = blockIdx.x * blockDim.x + threadIdx.x;
+	if (j >= n)
+		return;
+	int node = (n - 1) + j;
+	int d = 0;
+	while (node != 0 && d < 4096) {
+		node = parent[node];
+		d++;
+	}
+	atomicMax(maxdepth, d);
+}
+
+template <typename T>
+static cudaError_t walloc(pw_world *w, T **p, size_t count)
+{
+	cudaError_t e = cudaMalloc((void **)p, sizeof(T) * (count ? count : 1));
+	if (e == cudaSuccess)
+		w->mesh_allocs.push_back((void *)*p);
+	return e;
+}
+
+int pw_build_mesh_device(pw_world *w, MeshDev &m, const std::vector<double> &V64, const std::vector<uint32_t> &F)
+{
+	m = MeshDev();
+	const int n = (int)(F.size() / 3);
+	const int nv = (int)(V64.size() / 3);
+	m.ntri = n;
+	m.nvert = nv;
+	m.leaf_base = n > 0 ? n - 1 : 0;
+	// host-side magnitudes
+	double emax = 0.0;
+	for (double x : V64)
+		emax = std::max(emax, std::fabs(x));
+	m.emax = (float)emax * 1.0001f + 1e-30f;
+	PW_CUDA(walloc(w, &m.V64, V64.size()));
+	PW_CUDA(walloc(w, &m.F, F.size()));
+	PW_CUDA(cudaMemcpy(m.V64, V64.data(), sizeof(double) * V64.size(), cudaMemcpyHostToDevice));
+	PW_CUDA(cudaMemcpy(m.F, F.data(), sizeof(int32_t) * F.size(), cudaMemcpyHostToDevice));
+	if (n == 0)
+		return PW_OK;
+	const int nnodes = 2 * n - 1;
+	PW_CUDA(walloc(w, &m.nodeA, nnodes));
+	PW_CUDA(walloc(w, &m.nodeB, nnodes));
+	PW_CUDA(walloc(w, &m.triA, n));
+	PW_CUDA(walloc(w, &m.triB, n));
+	PW_CUDA(walloc(w, &m.triC, n));
+
+	// temporaries
+	float4 *ta, *tb, *tc;
+	float *tlo, *thi, *cen, *bounds, *blo, *bhi;
+	uint32_t *keys, *vals, *keys2, *vals2;
+	int32_t *left, *right, *parent;
+	unsigned int *flags;
+	int *maxdepth;
+	std::vector<void *> tmp;
+	auto tal = [&](void **p, size_t bytes) -> cudaError_t {
+		cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+		if (e == cudaSuccess)
+			tmp.push_back(*p);
+		return e;
+	};
+	auto cleanup = [&]() {
+		for (void *p : tmp)
+			cudaFree(p);
+		tmp.clear();
+	};
+#define TAL(ptr, bytes)                                     \
+	do {                                                    \
+		cudaError_t e__ = tal((void **)&(ptr), (bytes));    \
+		if (e__ != cudaSuccess) {                           \
+			cleanup();                                      \
+			return pw_cuda_fail(e__, "BVH temporaries");    \
+		}                                                   \
+	} while (0)
+	TAL(ta, sizeof(float4) * n);
+	TAL(tb, sizeof(float4) * n);
+	TAL(tc, sizeof(float4) * n);
+	TAL(tlo, sizeof(float) * 3 * n);
+	TAL(thi, sizeof(float) * 3 * n);
+	TAL(cen, sizeof(float) * 3 * n);
+	TAL(bounds, sizeof(float) * 6);
+	TAL(blo, sizeof(float) * 3 * nnodes);
+	TAL(bhi, sizeof(float) * 3 * nnodes);
+	TAL(keys, sizeof(uint32_t) * n);
+	TAL(vals, sizeof(uint32_t) * n);
+	TAL(keys2, sizeof(uint32_t) * n);
+	TAL(vals2, sizeof(uint32_t) * n);
+	TAL(left, sizeof(int32_t) * nnodes);
+	TAL(right, sizeof(int32_t) * nnodes);
+	TAL(parent, sizeof(int32_t) * nnodes);
+	TAL(flags, sizeof(unsigned int) * nnodes);
+	TAL(maxdepth, sizeof(int));
+	const int B = 256;
+	const int G = (n + B - 1) / B;
+	cudaMemset(flags, 0, sizeof(unsigned int) * nnodes);
+	cudaMemset(maxdepth, 0, sizeof(int));
+	cudaMemset(parent, 0xff, sizeof(int32_t) * nnodes);
+	k_tri_prep<<<G, B>>>(m.V64, m.F, n, ta, tb, tc, tlo, thi, cen);
+	k_bounds<<<1, 256>>>(cen, n, bounds);
+	k_morton<<<G, B>>>(cen, n, bounds, keys, vals);
+	size_t tmp_bytes = 0;
+	cudaError_t se = cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys2, vals, vals2, n, 0, 30);
+	if (se != cudaSuccess) {
+		cleanup();
+		return pw_cuda_fail(se, "BVH sort (size query)");
+	}
+	void *cub_tmp = nullptr;
+	TAL(cub_tmp, tmp_bytes);
+	se = cub::DeviceRadixSort::SortPairs(cub_tmp, tmp_bytes, keys, keys2, vals, vals2, n, 0, 30);
+	if (se != cudaSuccess) {
+		cleanup();
+		return pw_cuda_fail(se, "BVH sort");
+	}
+	if (n > 1)
+		k_karras<<<(n - 1 + B - 1) / B, B>>>(keys2, n, left, right, parent);
+	k_refit<<<G, B>>>(vals2, n, tlo, thi, ta, tb, tc, m.triA, m.triB, m.triC, blo, bhi, left, right, parent, flags);
+	k_finalize<<<(nnodes + B - 1) / B, B>>>(nnodes, n, blo, bhi, left, right, m.triA, m.nodeA, m.nodeB);
+	k_depth<<<G, B>>>(n, parent, maxdepth);
+	cudaError_t e = cudaGetLastError();
+	if (e == cudaSuccess)
+		e = cudaDeviceSynchronize();
+	if (e != cudaSuccess) {
+		cleanup();
+		return pw_cuda_fail(e, "BVH build");
+	}
+	int depth = 0;
+	float rootlo[3], roothi[3];
+	cudaMemcpy(&depth, maxdepth, sizeof(int), cudaMemcpyDeviceToHost);
+	cudaMemcpy(rootlo, blo, sizeof(float) * 3, cudaMemcpyDeviceToHost);
+	cudaMemcpy(roothi, bhi, sizeof(float) * 3, cudaMemcpyDeviceToHost);
+	m.depth = depth;
+	double r1 = 0.0;
+	for (int c = 0; c < 3; c++)
+		r1 += std::max(std::fabs((double)rootlo[c]), std::fabs((double)roothi[c]));
+	m.r1 = (float)r1 * 1.0001f + 1e-30f;
+	cleanup();
+#undef TAL
+	if (depth >= 4096)
+		return pw_fail(PW_ERR_INTERNAL, "BVH build: hierarchy deeper than 4096 levels");
+	return PW_OK;
+}

@@ -1,0 +1,456 @@
+"""UnitWorld -- pyosr's collision-query API on the GB300 engine.
+
+Mirrors ``py::class_<UnitWorld>`` of lib/pyosr/module.cc:127-250: the same
+method names, argument meaning, return shapes and error behaviour
+(``RuntimeError`` where the reference throws).  Single-state methods run the
+batch kernels with one row.  Batched methods take torch tensors on the CUDA
+device (float64, [N, 7]) and return device tensors; the numpy-level methods
+(``calculate_visibility_*``) copy through pinned host memory.
+
+Every query goes through libpwcollide.so; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+from . import objio
+from ._lib import PwError, check
+
+GEO_ENV = _lib.PW_GEO_ENV
+GEO_ROB = _lib.PW_GEO_ROB
+STATE_DIMENSION = 7
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_lib.dp)
+
+
+def _states_np(q) -> np.ndarray:
+    q = np.ascontiguousarray(np.asarray(q, dtype=np.float64))
+    if q.ndim == 1:
+        q = q.reshape(1, -1)
+    if q.shape[-1] != 7:
+        raise ValueError("states must have 7 columns [x, y, z, w, qx, qy, qz]")
+    return q
+
+
+def _stream_ptr(device) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+class UnitWorld:
+    """World of an environment and a robot mesh in the normalised unit frame."""
+
+    GEO_ENV = GEO_ENV
+    GEO_ROB = GEO_ROB
+
+    def __init__(self, device: int = 0):
+        L = _lib.load()
+        if not torch.cuda.is_available():
+            raise RuntimeError("UnitWorld needs a CUDA device (there is no CPU fallback)")
+        self._L = L
+        self._device = torch.device("cuda", device)
+        h = _lib.vp()
+        check(L.pw_world_create(ctypes.byref(h), int(device)), "pw_world_create")
+        self._h = h
+        self._robot_state = np.array([0, 0, 0, 1, 0, 0, 0], dtype=np.float64)
+        self._recommended_cres = 0.001
+        self._meshes = [None, None]
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                self._L.pw_world_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    # ----------------------------------------------------------- set-up
+    def load_env_mesh(self, V, F):
+        V = np.ascontiguousarray(V, dtype=np.float32)
+        F = np.ascontiguousarray(F, dtype=np.uint32)
+        self._meshes[0] = (V, F)
+        check(self._L.pw_world_load_env(self._h, V.ctypes.data_as(_lib.fp), V.shape[0],
+                                        F.ctypes.data_as(_lib.u32p), F.shape[0]), "loadModelFromFile")
+
+    def load_robot_mesh(self, V, F):
+        V = np.ascontiguousarray(V, dtype=np.float32)
+        F = np.ascontiguousarray(F, dtype=np.uint32)
+        self._meshes[1] = (V, F)
+        self._robot_state = np.array([0, 0, 0, 1, 0, 0, 0], dtype=np.float64)
+        check(self._L.pw_world_load_robot(self._h, V.ctypes.data_as(_lib.fp), V.shape[0],
+                                          F.ctypes.data_as(_lib.u32p), F.shape[0]), "loadRobotFromFile")
+
+    def loadModelFromFile(self, fn: str):
+        self.load_env_mesh(*objio.load_obj(fn))
+
+    def loadRobotFromFile(self, fn: str):
+        self.load_robot_mesh(*objio.load_obj(fn))
+
+    def enforceRobotCenter(self, center):
+        c = np.ascontiguousarray(center, dtype=np.float64).reshape(3)
+        check(self._L.pw_world_enforce_robot_center(self._h, _dp(c)), "enforceRobotCenter")
+
+    def scaleToUnit(self):
+        check(self._L.pw_world_scale_to_unit(self._h), "scaleToUnit")
+
+    def angleModel(self, latitude: float, longitude: float):
+        check(self._L.pw_world_angle_model(self._h, float(latitude), float(longitude)), "angleModel")
+
+    def setupFrom(self, other: "UnitWorld"):
+        """Share the other world's meshes and scale (UnitWorld::copyFrom, unit_world.cc:76-92)."""
+        if other._meshes[0] is not None:
+            self.load_env_mesh(*other._meshes[0])
+        if other._meshes[1] is not None:
+            self.load_robot_mesh(*other._meshes[1])
+        info = other._info()
+        self.scaleToUnit()
+        if other._meshes[1] is not None:
+            self.enforceRobotCenter(np.array(info.robot_center[:]))
+        self.angleModel(0.0, 0.0)
+        self.set_perturbation(other.perturbation)
+
+    def set_perturbation(self, q):
+        q = np.ascontiguousarray(q, dtype=np.float64).reshape(7)
+        check(self._L.pw_world_set_perturbation(self._h, _dp(q)), "set_perturbation")
+
+    @property
+    def perturbation(self):
+        q = np.zeros(7)
+        check(self._L.pw_world_get_perturbation(self._h, _dp(q)), "perturbation")
+        return q
+
+    @property
+    def state(self):
+        return self._robot_state.copy()
+
+    @state.setter
+    def state(self, q):
+        self._robot_state = np.asarray(q, dtype=np.float64).reshape(7).copy()
+
+    def _info(self) -> _lib.WorldInfo:
+        info = _lib.WorldInfo()
+        check(self._L.pw_world_info_get(self._h, ctypes.byref(info)), "info")
+        return info
+
+    @property
+    def scene_scale(self) -> float:
+        return float(self._info().scene_scale)
+
+    @property
+    def scene_matrix(self):
+        return np.array(self._info().scene_matrix[:]).reshape(4, 4)
+
+    @property
+    def robot_matrix(self):
+        return np.array(self._info().robot_matrix[:]).reshape(4, 4)
+
+    @property
+    def recommended_cres(self) -> float:
+        return self._recommended_cres
+
+    @recommended_cres.setter
+    def recommended_cres(self, v: float):
+        self._recommended_cres = float(v)
+
+    def get_ompl_center(self, geo: int = GEO_ROB):
+        info = self._info()
+        if geo == GEO_ROB:
+            return np.array(info.robot_ompl_center[:])
+        return np.zeros(3)
+
+    def info(self) -> dict:
+        i = self._info()
+        return {"scene_scale": i.scene_scale, "robot_center": np.array(i.robot_center[:]),
+                "robot_ompl_center": np.array(i.robot_ompl_center[:]), "env_vertices": i.env_vertices,
+                "env_faces": i.env_faces, "robot_vertices": i.robot_vertices, "robot_faces": i.robot_faces,
+                "env_bvh_depth": i.env_bvh_depth, "robot_bvh_depth": i.robot_bvh_depth, "ready": bool(i.ready)}
+
+    # ----------------------------------------------------------- batched device API
+    def _dev_states(self, q: torch.Tensor) -> torch.Tensor:
+        if not isinstance(q, torch.Tensor):
+            q = torch.as_tensor(np.asarray(q, dtype=np.float64))
+        if q.dim() == 1:
+            q = q.reshape(1, -1)
+        if q.shape[-1] != 7:
+            raise ValueError("states must have 7 columns")
+        return q.to(device=self._device, dtype=torch.float64).contiguous()
+
+    def is_valid_states(self, q: torch.Tensor) -> torch.Tensor:
+        """isValid for a batch: bool tensor [N] on the device (True = collision free)."""
+        q = self._dev_states(q)
+        out = torch.empty(q.shape[0], dtype=torch.uint8, device=self._device)
+        check(self._L.pw_states_valid(self._h, q.data_ptr(), q.shape[0], out.data_ptr(),
+                                      _stream_ptr(self._device)), "is_valid_state")
+        return out.bool()
+
+    def is_disentangled_states(self, q: torch.Tensor) -> torch.Tensor:
+        q = self._dev_states(q)
+        out = torch.empty(q.shape[0], dtype=torch.uint8, device=self._device)
+        rc = self._L.pw_states_disentangled(self._h, q.data_ptr(), q.shape[0], out.data_ptr(),
+                                            _stream_ptr(self._device))
+        if rc == _lib.PW_ERR_NO_MODEL:
+            raise RuntimeError("Pain in the ass: models not loaded")
+        check(rc, "is_disentangled")
+        return out.bool()
+
+    def first_contact_steps(self, q0: torch.Tensor, q1: torch.Tensor, verify_delta: float,
+                            mode: int = _lib.PW_SEG_TRANSIT) -> torch.Tensor:
+        """First colliding step of every segment (int32 [N]): >= 0 step index, -1 all free,
+        -2 no step taken (verify_delta >= distance), -3 more than 2^30 steps."""
+        q0 = self._dev_states(q0)
+        q1 = self._dev_states(q1)
+        if q0.shape != q1.shape:
+            raise ValueError("from/to batches differ in shape")
+        out = torch.empty(q0.shape[0], dtype=torch.int32, device=self._device)
+        check(self._L.pw_segments_first_contact(self._h, q0.data_ptr(), q1.data_ptr(), q0.shape[0],
+                                                float(verify_delta), int(mode), out.data_ptr(),
+                                                _stream_ptr(self._device)), "first_contact_steps")
+        return out
+
+    def is_valid_transitions(self, q0: torch.Tensor, q1: torch.Tensor, initial_verify_delta: float) -> torch.Tensor:
+        """isValidTransition for a batch of aligned pairs (bool [N])."""
+        return self.first_contact_steps(q0, q1, initial_verify_delta, _lib.PW_SEG_TRANSITION) == _lib.PW_STEP_FREE
+
+    def last_stats(self) -> dict:
+        st = _lib.QueryStats()
+        check(self._L.pw_world_last_stats(self._h, ctypes.byref(st)), "last_stats")
+        return st.as_dict()
+
+    # ----------------------------------------------------------- pyosr single-state API
+    def is_valid_state(self, q) -> bool:
+        return bool(self.is_valid_states(_states_np(q)).cpu()[0])
+
+    def is_disentangled(self, q) -> bool:
+        return bool(self.is_disentangled_states(_states_np(q)).cpu()[0])
+
+    def transit_state_to_with_contact(self, from_state, to_state, verify_delta):
+        """(last_free, colliding_or_last, done, last_tau, tau) of unit_world.cc:405-474."""
+        a = _states_np(from_state)[0]
+        b = _states_np(to_state)[0]
+        dist = distance(a, b)
+        if verify_delta >= dist:
+            return a.copy(), b.copy(), False, np.float32(0.0), np.float32(1.0)
+        if dist != dist:
+            return a.copy(), a.copy(), False, np.float32(0.0), np.float32(0.0)
+        k = int(self.first_contact_steps(a, b, verify_delta, _lib.PW_SEG_TRANSIT).cpu()[0])
+        if k == _lib.PW_STEP_INVALID:
+            raise RuntimeError("transit_state_to: more than 2^30 steps at this verify_delta")
+        if k >= 0:
+            st, tau, _ = segment_step_state(a, b, verify_delta, k)
+            if k > 0:
+                lf, ltau, _ = segment_step_state(a, b, verify_delta, k - 1)
+            else:
+                lf, ltau = a.copy(), 0.0
+            return lf, st, False, np.float32(ltau), np.float32(tau)
+        # every step free: the loop's last state, `done` true, and the reference's outer tau (0)
+        _, _, K = segment_step_state(a, b, verify_delta, 0)
+        lf, ltau, _ = segment_step_state(a, b, verify_delta, K - 1)
+        return lf, lf.copy(), True, np.float32(ltau), np.float32(0.0)
+
+    def transit_state_to(self, from_state, to_state, verify_delta):
+        """(free state, done, progress) of unit_world.cc:395-402."""
+        tup = self.transit_state_to_with_contact(from_state, to_state, verify_delta)
+        return tup[0], tup[2], tup[3]
+
+    def is_valid_transition(self, from_state, to_state, initial_verify_delta) -> bool:
+        a = _states_np(from_state)
+        b = _states_np(to_state)
+        return bool(self.is_valid_transitions(a, b, initial_verify_delta).cpu()[0])
+
+    # ----------------------------------------------------------- frames
+    def _convert(self, fn, q, *extra):
+        q = _states_np(q)
+        out = np.zeros_like(q)
+        check(fn(self._h, _dp(q), q.shape[0], _dp(out), *extra), "state conversion")
+        return out
+
+    def translate_to_unit_state(self, q):
+        single = np.ndim(q) == 1
+        out = self._convert(self._L.pw_world_translate_to_unit, q)
+        return out[0] if single else out
+
+    def translate_from_unit_state(self, q):
+        single = np.ndim(q) == 1
+        out = self._convert(self._L.pw_world_translate_from_unit, q)
+        return out[0] if single else out
+
+    def translate_ompl_to_unit(self, Q):
+        return self._convert(self._L.pw_world_translate_ompl_to_unit, Q)
+
+    def translate_unit_to_ompl(self, Q, to_angle_axis: bool = False):
+        return self._convert(self._L.pw_world_translate_unit_to_ompl, Q, int(bool(to_angle_axis)))
+
+    # ----------------------------------------------------------- visibility batches
+    def _pairs_first(self, qs0, qs1, verify_magnitude):
+        a = torch.from_numpy(qs0).pin_memory().to(self._device, non_blocking=True)
+        b = torch.from_numpy(qs1).pin_memory().to(self._device, non_blocking=True)
+        k = self.first_contact_steps(a, b, verify_magnitude, _lib.PW_SEG_TRANSITION)
+        return (k == _lib.PW_STEP_FREE).to(torch.int8).cpu().numpy()
+
+    def _maybe_unit(self, qs, is_unit):
+        qs = _states_np(qs)
+        return qs if is_unit else self.translate_to_unit_state(qs)
+
+    def calculate_visibility_pair(self, qs0, qs0_are_unit_states, qs1, qs1_are_unit_states, verify_magnitude,
+                                  enable_mt=True):
+        """int8 [max(M, N)]: isValidTransition(qs0[i], qs1[i]) (unit_world.cc:799-840)."""
+        a = self._maybe_unit(qs0, qs0_are_unit_states)
+        b = self._maybe_unit(qs1, qs1_are_unit_states)
+        if a.shape[0] != b.shape[0]:
+            raise ValueError("calculate_visibility_pair: qs0 and qs1 must have the same number of rows")
+        return self._pairs_first(a, b, verify_magnitude)
+
+    def calculate_visibility_matrix2(self, qs0, qs0_are_unit_states, qs1, qs1_are_unit_states, verify_magnitude,
+                                     enable_mt=True):
+        """int8 [M, N] of isValidTransition(qs0[i], qs1[j]) (unit_world.cc:761-797)."""
+        a = self._maybe_unit(qs0, qs0_are_unit_states)
+        b = self._maybe_unit(qs1, qs1_are_unit_states)
+        M, N = a.shape[0], b.shape[0]
+        out = np.zeros((M, N), dtype=np.int8)
+        rows = max(1, (1 << 22) // max(N, 1))
+        for r0 in range(0, M, rows):
+            r1 = min(M, r0 + rows)
+            A = np.repeat(a[r0:r1], N, axis=0)
+            B = np.tile(b, (r1 - r0, 1))
+            out[r0:r1] = self._pairs_first(A, B, verify_magnitude).reshape(r1 - r0, N)
+        return out
+
+    def calculate_visibility_matrix(self, qs, is_unit_states, verify_magnitude):
+        """Symmetric int8 [N, N] over pairs i < j (unit_world.cc:740-759); the diagonal is 0."""
+        q = self._maybe_unit(qs, is_unit_states)
+        N = q.shape[0]
+        iu, ju = np.triu_indices(N, k=1)
+        out = np.zeros((N, N), dtype=np.int8)
+        if iu.size:
+            v = self._pairs_first(np.ascontiguousarray(q[iu]), np.ascontiguousarray(q[ju]), verify_magnitude)
+            out[iu, ju] = v
+            out[ju, iu] = v
+        return out
+
+    # ----------------------------------------------------------- contacts and geometry
+    def intersecting_segments(self, unitq):
+        """(begins m x 3, ends m x 3, lengths m, face pairs m x 2 [env, robot]) of
+        unit_world.cc:959-1012, rows sorted by (env face, robot face)."""
+        q = np.ascontiguousarray(unitq, dtype=np.float64).reshape(7)
+        cap = 1024
+        while True:
+            b = np.zeros((cap, 3))
+            e = np.zeros((cap, 3))
+            m = np.zeros(cap)
+            p = np.zeros((cap, 2), dtype=np.int32)
+            c = np.zeros(cap, dtype=np.int32)
+            cnt = ctypes.c_int64(0)
+            rc = self._L.pw_intersecting_segments(self._h, _dp(q), cap, _dp(b), _dp(e), _dp(m),
+                                                  p.ctypes.data_as(_lib.i32p), c.ctypes.data_as(_lib.i32p),
+                                                  ctypes.byref(cnt))
+            if rc == _lib.PW_ERR_CAPACITY and cnt.value > cap:
+                cap = int(cnt.value)
+                continue
+            check(rc, "intersecting_segments")
+            n = int(cnt.value)
+            self._last_coplanar = c[:n].copy()
+            return b[:n].copy(), e[:n].copy(), m[:n].copy(), p[:n].copy()
+
+    def _cd(self, geo):
+        info = self._info()
+        nv = info.env_vertices if geo == GEO_ENV else info.robot_vertices
+        nf = info.env_faces if geo == GEO_ENV else info.robot_faces
+        V = np.zeros((nv, 3))
+        F = np.zeros((nf, 3), dtype=np.int32)
+        check(self._L.pw_world_cd_vertices(self._h, geo, _dp(V)), "cd_vertices")
+        check(self._L.pw_world_cd_faces(self._h, geo, F.ctypes.data_as(_lib.i32p)), "cd_faces")
+        return V, F
+
+    def get_robot_geometry(self, q, q_is_unit: bool = True):
+        """Robot CD vertices placed at q (unit_world.cc:1102-1116)."""
+        qu = _states_np(q)[0] if q_is_unit else self.translate_to_unit_state(_states_np(q)[0])
+        V, F = self._cd(GEO_ROB)
+        R, t = state_transform(qu)
+        return V @ R.T + t, F
+
+    def get_scene_geometry(self, q, q_is_unit: bool = True):
+        V, F = self._cd(GEO_ENV)
+        return V, F
+
+
+# ------------------------------------------------------------------- module-level state math
+
+def get_identity_state_vector():
+    return np.array([0, 0, 0, 1, 0, 0, 0], dtype=np.float64)
+
+
+def distance(a, b) -> float:
+    """osr::distance (osr_state.cc:130-154) with the engine's deterministic FP64 math."""
+    L = _lib.load()
+    a = np.ascontiguousarray(a, dtype=np.float64).reshape(7)
+    b = np.ascontiguousarray(b, dtype=np.float64).reshape(7)
+    out = np.zeros(1)
+    check(L.pw_state_distance(_dp(a), _dp(b), _dp(out)), "distance")
+    return float(out[0])
+
+
+def multi_distance(origin, targets):
+    targets = _states_np(targets)
+    return np.array([distance(origin, t) for t in targets])
+
+
+def interpolate(a, b, tau: float):
+    """osr::interpolate (osr_state.cc:27-44)."""
+    L = _lib.load()
+    a = np.ascontiguousarray(a, dtype=np.float64).reshape(7)
+    b = np.ascontiguousarray(b, dtype=np.float64).reshape(7)
+    out = np.zeros(7)
+    check(L.pw_state_interpolate(_dp(a), _dp(b), float(tau), _dp(out)), "interpolate")
+    return out
+
+
+def segment_step_state(a, b, verify_delta: float, k: int):
+    """(state, tau, number of steps) of step k of the reference stepping loop."""
+    L = _lib.load()
+    a = np.ascontiguousarray(a, dtype=np.float64).reshape(7)
+    b = np.ascontiguousarray(b, dtype=np.float64).reshape(7)
+    out = np.zeros(7)
+    tau = np.zeros(1)
+    n = ctypes.c_int64(0)
+    rc = L.pw_segment_step_state(_dp(a), _dp(b), float(verify_delta), int(k), _dp(out), _dp(tau), ctypes.byref(n))
+    if rc != _lib.PW_OK and not (rc == _lib.PW_ERR_INVALID_ARG and n.value > 0 and (k < 0 or k >= n.value)):
+        check(rc, "segment_step_state")
+    return out, float(tau[0]), int(n.value)
+
+
+def state_transform(q):
+    """Rotation (raw-quaternion formula) and translation of a state, numpy float64."""
+    q = np.asarray(q, dtype=np.float64).reshape(7)
+    w, x, y, z = q[3:7]
+    tx, ty, tz = 2 * x, 2 * y, 2 * z
+    R = np.array([[1 - (ty * y + tz * z), ty * x - tz * w, tz * x + ty * w],
+                  [ty * x + tz * w, 1 - (tx * x + tz * z), tz * y - tx * w],
+                  [tz * x - ty * w, tz * y + tx * w, 1 - (tx * x + ty * y)]])
+    return R, q[:3].copy()
+
+
+def apply(from_state, tr, aa):
+    """osr::apply (osr_state.cc:244-259): translate, then rotate by angle-axis on the left."""
+    q = np.asarray(from_state, dtype=np.float64).reshape(7)
+    rot = q[3:7] / np.linalg.norm(q[3:7])
+    t = q[:3] + np.asarray(tr, dtype=np.float64)
+    aa = np.asarray(aa, dtype=np.float64)
+    ang = float(np.linalg.norm(aa))
+    axis = np.array([1.0, 0.0, 0.0]) if ang == 0.0 else aa / ang
+    dq = np.concatenate([[math.cos(ang / 2)], math.sin(ang / 2) * axis])
+    w1, x1, y1, z1 = dq
+    w2, x2, y2, z2 = rot
+    r = np.array([w1 * w2 - x1 * x2 - y1 * y2 - z1 * z2, w1 * x2 + x1 * w2 + y1 * z2 - z1 * y2,
+                  w1 * y2 - x1 * z2 + y1 * w2 + z1 * x2, w1 * z2 + x1 * y2 - y1 * x2 + z1 * w2])
+    r /= np.linalg.norm(r)
+    return np.concatenate([t, r])
+
+
+__all__ = ["UnitWorld", "GEO_ENV", "GEO_ROB", "STATE_DIMENSION", "PwError", "distance", "multi_distance",
+           "interpolate", "segment_step_state", "apply", "get_identity_state_vector", "state_transform"]

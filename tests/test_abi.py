@@ -1,0 +1,75 @@
+"""The C ABI library loads, exports every declared entry point, and its host-only
+helpers agree bit for bit with the oracle (CPU; no GPU compute)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "pw_collide.h")).read()
+    return set(re.findall(r"PW_API[^;]*?\b(pw_[a-z0-9_]+)\s*\(", src, flags=re.S))
+
+
+def test_header_and_binding_agree():
+    from puzzletunneldiscovery_gb300 import _lib
+    assert _declared() == set(_lib.EXPORTS)
+
+
+def test_library_exports_every_symbol(built_lib):
+    L = ctypes.CDLL(built_lib)
+    for name in _declared():
+        assert hasattr(L, name), name
+
+
+def test_host_state_math_bit_exact(built_lib, oracle_mod):
+    import puzzletunneldiscovery_gb300 as pw
+    from puzzletunneldiscovery_gb300 import workloads as W
+    q0, q1 = W.segment_batch(200, -2, 2, 0.4, seed=5)
+    for a, b in zip(q0, q1):
+        assert pw.distance(a, b) == oracle_mod.distance(a, b)
+        for tau in (0.0, 0.25, 0.999, 1.0):
+            assert (pw.interpolate(a, b, tau) == oracle_mod.interpolate(a, b, tau)).all()
+    a, b = q0[0], q1[0]
+    K = oracle_mod.segment_steps(a, b, 0.001)
+    for k in (0, 1, K // 2, K - 1):
+        s, tau, n = pw.segment_step_state(a, b, 0.001, k)
+        s2, tau2 = oracle_mod.segment_state(a, b, 0.001, k)
+        assert n == K and (s == s2).all() and tau == tau2
+
+
+def test_nearly_identical_rotations_take_linear_branch(built_lib, oracle_mod):
+    import puzzletunneldiscovery_gb300 as pw
+    a = np.array([0.1, 0.2, 0.3, 1.0, 0.0, 0.0, 0.0])
+    b = np.array([0.2, 0.2, 0.3, 1.0, 1e-17, 0.0, 0.0])
+    for tau in (0.3, 0.7):
+        assert (pw.interpolate(a, b, tau) == oracle_mod.interpolate(a, b, tau)).all()
+    c = b.copy()
+    c[3:] = -c[3:]                         # the same rotation, opposite sign: d < 0 path
+    assert (pw.interpolate(a, c, 0.4) == oracle_mod.interpolate(a, c, 0.4)).all()
+
+
+def test_world_create_reports_errors_without_device(built_lib):
+    import torch
+    from puzzletunneldiscovery_gb300 import _lib
+    L = _lib.load()
+    h = ctypes.c_void_p()
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    rc = L.pw_world_create(ctypes.byref(h), 0)
+    assert rc in (_lib.PW_ERR_CUDA, _lib.PW_ERR_INVALID_ARG)
+    assert L.pw_last_error()
+    assert L.pw_world_destroy(None) == _lib.PW_OK
+
+
+def test_unitworld_refuses_cpu(built_lib):
+    import torch
+    import puzzletunneldiscovery_gb300 as pw
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(RuntimeError):
+        pw.UnitWorld()

@@ -1,0 +1,231 @@
+"""GPU path vs the CPU oracle: verdicts and first-contact steps must be identical.
+
+All queries go through libpwcollide.so (UnitWorld -> C ABI).  Sizes are ones
+the oracle finishes in seconds; the full-size workloads are covered by
+size-independent properties in test_gpu_properties.py.
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden
+from puzzletunneldiscovery_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(O, Ve, Fe, Vr, Fr, center=None):
+    import puzzletunneldiscovery_gb300 as pw
+    uw = pw.UnitWorld()
+    uw.load_env_mesh(Ve, Fe)
+    uw.load_robot_mesh(Vr, Fr)
+    if center is not None:
+        uw.enforceRobotCenter(center)
+    uw.scaleToUnit()
+    uw.angleModel(0.0, 0.0)
+    ow = O.OracleWorld(Ve, Fe, Vr, Fr, center=None if center is None else np.asarray(center, dtype=np.float32))
+    return uw, ow
+
+
+@pytest.fixture(scope="module")
+def tori(oracle_mod, built_lib):
+    return _pair(oracle_mod, *W.cfg_interlocking_tori())
+
+
+@pytest.fixture(scope="module")
+def alpha(oracle_mod, built_lib):
+    g = golden("alpha_puzzle.npz")
+    uw, ow = _pair(oracle_mod, g["Ve"], g["Fe"], g["Vr"], g["Fr"], center=g["center"].astype(np.float32))
+    return uw, ow, g
+
+
+def test_cd_vertices_and_scale_match(tori):
+    uw, ow = tori
+    assert uw.scene_scale == ow.scene_scale
+    V, _ = uw._cd(0)
+    assert (V == ow.vertices(0)).all()
+    V, _ = uw._cd(1)
+    assert (V == ow.vertices(1)).all()
+
+
+def test_states_regression_vectors(tori):
+    uw, ow = tori
+    g = golden("torus_regression.npz")
+    v = uw.is_valid_states(torch.from_numpy(g["states"])).cpu().numpy()
+    assert (v == g["valid"]).all()
+    d = uw.is_disentangled_states(torch.from_numpy(g["states"])).cpu().numpy()
+    assert (d == g["disentangled"]).all()
+
+
+def test_states_cfg0_parity(tori):
+    """The interlocking-tori state workload (100k states) against the oracle."""
+    uw, ow = tori
+    q = W.uniform_states(100_000, -2.0, 2.0, ow.scene_scale, seed=0)
+    gpu = uw.is_valid_states(torch.from_numpy(q)).cpu().numpy()
+    cpu = ow.is_valid(q)
+    assert (gpu == cpu).all(), int((gpu != cpu).sum())
+    st = uw.last_stats()
+    assert st["queries"] == q.shape[0]
+    d = uw.is_disentangled_states(torch.from_numpy(q)).cpu().numpy()
+    assert (d == ow.is_disentangled(q)).all()
+
+
+def test_segments_regression_vectors(tori):
+    uw, ow = tori
+    g = golden("torus_regression.npz")
+    f = uw.first_contact_steps(torch.from_numpy(g["seg_from"]), torch.from_numpy(g["seg_to"]),
+                               float(g["delta"])).cpu().numpy()
+    assert (f == g["first"]).all()
+    t = uw.first_contact_steps(torch.from_numpy(g["seg_from"]), torch.from_numpy(g["seg_to"]),
+                               float(g["delta"]), mode=1).cpu().numpy()
+    assert (t == g["transition_first"]).all()
+
+
+def test_segments_cfg1_sample_parity(tori):
+    uw, ow = tori
+    q0, q1 = W.segment_batch(1500, -2.0, 2.0, ow.scene_scale, seed=7)
+    gpu = uw.first_contact_steps(torch.from_numpy(q0), torch.from_numpy(q1), 0.001).cpu().numpy()
+    cpu, _ = ow.segments_first_contact(q0, q1, 0.001)
+    assert (gpu == cpu).all(), int((gpu != cpu).sum())
+
+
+def test_near_contact_states(tori, oracle_mod):
+    """States at and just before each segment's first contact: the FP32 band's hardest inputs."""
+    uw, ow = tori
+    q0, q1 = W.segment_batch(400, -2.0, 2.0, ow.scene_scale, seed=11)
+    first, _ = ow.segments_first_contact(q0, q1, 0.001)
+    rows = []
+    for a, b, k in zip(q0, q1, first):
+        if k > 0:
+            for kk in (k - 1, k):
+                s, _ = oracle_mod.segment_state(a, b, 0.001, kk)
+                rows.append(s)
+    rows = np.array(rows)
+    # bisect each contact to ~1e-12 in tau to get states within rounding of touching
+    fine = []
+    for a, b, k in list(zip(q0, q1, first))[:120]:
+        if k <= 0:
+            continue
+        lo, _ = oracle_mod.segment_state(a, b, 0.001, k - 1)
+        hi, _ = oracle_mod.segment_state(a, b, 0.001, k)
+        for _ in range(40):
+            mid = oracle_mod.interpolate(lo, hi, 0.5)
+            if ow.is_valid(mid)[0]:
+                lo = mid
+            else:
+                hi = mid
+        fine += [lo, hi]
+    rows = np.concatenate([rows, np.array(fine)]) if fine else rows
+    gpu = uw.is_valid_states(torch.from_numpy(rows)).cpu().numpy()
+    cpu = ow.is_valid(rows)
+    assert (gpu == cpu).all(), int((gpu != cpu).sum())
+    assert uw.last_stats()["retests"] > 0   # the band was exercised
+
+
+def test_alpha_puzzle_states_and_path(alpha):
+    uw, ow, g = alpha
+    s = uw.scene_scale
+    U = []
+    for p in g["keys_wfirst"]:
+        U.append(np.concatenate([p[:3] * s, p[3:7] / np.linalg.norm(p[3:7])]))
+    U = np.array(U)
+    assert uw.is_valid_states(torch.from_numpy(U)).cpu().numpy().all()
+    f = uw.first_contact_steps(torch.from_numpy(U[:-1]), torch.from_numpy(U[1:]), 0.0005).cpu().numpy()
+    assert (f == -1).all()
+    # random states around the puzzle
+    q = W.uniform_states(20_000, -60.0, 60.0, s, seed=2)
+    q[:, :3] += ow.vertices(0).mean(axis=0)
+    assert (uw.is_valid_states(torch.from_numpy(q)).cpu().numpy() == ow.is_valid(q)).all()
+
+
+def test_ompl_conversion_matches_unit_recipe(alpha):
+    """translateOMPLStateToUnitState (unit_world.cc:689-711): w-last -> w-first, scale, then
+    t' = t - R(q) (ompl_centre - centre) * scale, where the enforced centre differs from the
+    vertex mean."""
+    import puzzletunneldiscovery_gb300 as pw
+    uw, ow, g = alpha
+    U = uw.translate_ompl_to_unit(g["path_wlast"])
+    info = uw.info()
+    s = uw.scene_scale
+    dc = (info["robot_ompl_center"].astype(np.float32) - info["robot_center"].astype(np.float32)).astype(np.float64) * s
+    for p, u in zip(g["path_wlast"], U):
+        q = np.array([p[6], p[3], p[4], p[5]])
+        q = q / np.linalg.norm(q)
+        R, _ = pw.state_transform(np.concatenate([[0, 0, 0], q]))
+        np.testing.assert_allclose(u[:3], p[:3] * s - R @ dc, rtol=1e-10, atol=1e-13)
+        np.testing.assert_allclose(u[3:], q, rtol=1e-12, atol=1e-15)
+    # the reference's own scripts place the w-first keys with translate_to_unit_state
+    K = uw.translate_to_unit_state(g["keys_wfirst"])
+    assert uw.is_valid_states(torch.from_numpy(K)).cpu().numpy().all()
+    back = uw.translate_from_unit_state(K)
+    np.testing.assert_allclose(back[:, :3], g["keys_wfirst"][:, :3], rtol=1e-6)
+
+
+def test_edge_cases(tori, oracle_mod):
+    uw, ow = tori
+    empty = torch.zeros((0, 7), dtype=torch.float64)
+    assert uw.is_valid_states(empty).numel() == 0
+    assert uw.first_contact_steps(empty, empty, 0.01).numel() == 0
+    # non-unit quaternions are used raw, as translate_state_to_transform does
+    q = W.uniform_states(3000, -2.0, 2.0, ow.scene_scale, seed=4)
+    q[:, 3:] *= np.random.default_rng(0).uniform(0.5, 1.5, size=(3000, 1))
+    assert (uw.is_valid_states(torch.from_numpy(q)).cpu().numpy() == ow.is_valid(q)).all()
+    assert (uw.is_disentangled_states(torch.from_numpy(q)).cpu().numpy() == ow.is_disentangled(q)).all()
+    # far away, identical endpoints, delta >= dist
+    a = np.array([[4.0, 4.0, 4.0, 1, 0, 0, 0]])
+    b = a.copy()
+    b[0, 0] += 0.0001
+    f = uw.first_contact_steps(torch.from_numpy(a), torch.from_numpy(b), 0.001).cpu().numpy()
+    assert f[0] == -2
+    f = uw.first_contact_steps(torch.from_numpy(a), torch.from_numpy(a), 0.001, mode=1).cpu().numpy()
+    assert f[0] == -2
+    with pytest.raises(RuntimeError):
+        uw.first_contact_steps(torch.from_numpy(a), torch.from_numpy(b), 0.0)
+
+
+def test_transit_tuple_matches_oracle(tori, oracle_mod):
+    uw, ow = tori
+    q0, q1 = W.segment_batch(40, -2.0, 2.0, ow.scene_scale, seed=9)
+    for a, b in zip(q0, q1):
+        got = uw.transit_state_to_with_contact(a, b, 0.002)
+        exp, _, _ = ow.transit_state_to_with_contact(a, b, 0.002)
+        assert (got[0] == exp[0]).all() and (got[1] == exp[1]).all()
+        assert got[2] == exp[2] and got[3] == exp[3] and got[4] == exp[4]
+        assert uw.is_valid_transition(a, b, 0.002) == (ow.segments_first_contact(a, b, 0.002, mode=1)[0][0] == -1)
+
+
+def test_perturbation(tori, oracle_mod):
+    uw, ow = tori
+    p = np.array([0.05, -0.02, 0.01, 0.9, 0.1, 0.3, -0.2])
+    p[3:] /= np.linalg.norm(p[3:])
+    uw.set_perturbation(p)
+    ow.set_perturbation(p)
+    try:
+        q = W.uniform_states(5000, -2.0, 2.0, ow.scene_scale, seed=6)
+        assert (uw.is_valid_states(torch.from_numpy(q)).cpu().numpy() == ow.is_valid(q)).all()
+        assert (uw.is_disentangled_states(torch.from_numpy(q)).cpu().numpy() == ow.is_disentangled(q)).all()
+    finally:
+        ident = np.array([0, 0, 0, 1, 0, 0, 0.0])
+        uw.set_perturbation(ident)
+        ow.set_perturbation(ident)
+
+
+def test_intersecting_segments_match(tori):
+    uw, ow = tori
+    for q in (np.array([0.0, 0.0, 0.0, 1, 0, 0, 0]), np.array([0.1, 0.05, 0.0, 0.96, 0.2, 0.1, 0.17]),
+              np.array([5.0, 5.0, 5.0, 1, 0, 0, 0])):
+        b, e, m, p = uw.intersecting_segments(q)
+        b2, e2, m2, p2, c2 = ow.intersecting_segments(q)
+        assert (p == p2).all()
+        assert (b == b2).all() and (e == e2).all() and (m == m2).all()
+
+
+def test_single_triangle_meshes(oracle_mod, built_lib):
+    """The fclcontacts pair as one-triangle meshes: BVHs with a single leaf."""
+    k = golden("fcl_kat.npz")
+    Ve = k["tri_h"].astype(np.float32)
+    Vr = k["tri_v"].astype(np.float32)
+    F = np.array([[0, 1, 2]], dtype=np.uint32)
+    uw, ow = _pair(oracle_mod, Ve, F, Vr, F)
+    q = W.uniform_states(2000, -1.0, 1.0, ow.scene_scale, seed=1)
+    assert (uw.is_valid_states(torch.from_numpy(q)).cpu().numpy() == ow.is_valid(q)).all()
