@@ -1,0 +1,26 @@
+"""Small, fixed workloads for ncu captures (not collected by pytest).
+
+python tests/profile_targets.py states|segments [n]
+"""
+import sys, os
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+import torch
+import puzzletunneldiscovery_gb300 as pw
+from puzzletunneldiscovery_gb300 import workloads as W
+what = sys.argv[1]
+n = int(sys.argv[2]) if len(sys.argv) > 2 else 1_000_000
+Ve, Fe, Vr, Fr = W.cfg_interlocking_tori()
+uw = pw.UnitWorld(0)
+uw.load_env_mesh(Ve, Fe); uw.load_robot_mesh(Vr, Fr); uw.scaleToUnit(); uw.angleModel(0, 0)
+s = uw.scene_scale
+if what == "states":
+    q = torch.from_numpy(W.uniform_states(n, -2, 2, s, seed=0)).cuda()
+    for _ in range(3):
+        v = uw.is_valid_states(q)
+else:
+    q0, q1 = W.segment_batch(n, -2, 2, s, seed=0)
+    a = torch.from_numpy(q0).cuda(); b = torch.from_numpy(q1).cuda()
+    for _ in range(3):
+        f = uw.first_contact_steps(a, b, 0.001)
+torch.cuda.synchronize()
+print("done", uw.last_stats())
