@@ -113,6 +113,18 @@ PW_API int pw_world_cd_faces(const pw_world *w, int geo, int32_t *out);
  * valid[i] = 1 when the robot at states[i] touches no env triangle. */
 PW_API int pw_states_valid(pw_world *w, const double *states, int64_t n, uint8_t *valid, void *stream);
 
+/* device, async: the verdicts of pw_states_valid without allocating any device memory.
+ * No counterpart in the reference.  For callers that may not allocate once running (a
+ * host framework whose pool allocator owns the device heap, or a loop that cannot take
+ * cudaMalloc's implicit synchronisation): the scratch lives in a fixed array inside the
+ * library (about 16 MiB per GPU that loads it, held until exit).  At most 1048576 states
+ * per call; larger batches are rejected with PW_ERR_INVALID_ARG.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) and should come
+ * before any stream capture.  All calls share the array, so calls whose work overlaps on
+ * the GPU (different streams, different worlds on the same device) race; order them on
+ * one stream.  pw_world_last_stats does not report on this entry point. */
+PW_API int pw_states_valid_noalloc(pw_world *w, const double *states, int64_t n, uint8_t *valid, void *stream);
+
 /* device, async: UnitWorld::isDisentangled (unit_world.cc:249-264) for n states. */
 PW_API int pw_states_disentangled(pw_world *w, const double *states, int64_t n, uint8_t *disentangled, void *stream);
 

@@ -35,7 +35,7 @@ EXPORTS = (
     "pw_world_cd_faces", "pw_states_valid", "pw_states_disentangled", "pw_segments_first_contact",
     "pw_intersecting_segments", "pw_world_translate_to_unit", "pw_world_translate_from_unit",
     "pw_world_translate_ompl_to_unit", "pw_world_translate_unit_to_ompl", "pw_world_last_stats",
-    "pw_state_distance", "pw_state_interpolate", "pw_segment_step_state",
+    "pw_state_distance", "pw_state_interpolate", "pw_segment_step_state", "pw_states_valid_noalloc",
 )
 
 
@@ -106,6 +106,7 @@ def load():
         "pw_world_cd_vertices": (ctypes.c_int, [vp, ctypes.c_int, dp]),
         "pw_world_cd_faces": (ctypes.c_int, [vp, ctypes.c_int, i32p]),
         "pw_states_valid": (ctypes.c_int, [vp, vp, i64, vp, vp]),
+        "pw_states_valid_noalloc": (ctypes.c_int, [vp, vp, i64, vp, vp]),
         "pw_states_disentangled": (ctypes.c_int, [vp, vp, i64, vp, vp]),
         "pw_segments_first_contact": (ctypes.c_int, [vp, vp, vp, i64, ctypes.c_double, ctypes.c_int, vp, vp]),
         "pw_intersecting_segments": (ctypes.c_int, [vp, dp, i64, dp, dp, dp, i32p, i32p, i64p]),

@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <climits>
 #include <cstring>
+#include <mutex>
 
 #include "pw_internal.cuh"
 #include "pw_math.cuh"
@@ -326,8 +327,9 @@ struct LaneStats {
 	unsigned long long node = 0, leaf = 0, inl = 0;
 };
 
-// Hand the buffered uncertain pairs to the FP64 queue.  When the queue is full
-// the pairs are re-tested here; returns true if one of those hit.
+// Hand the buffered uncertain pairs to the FP64 queue (CAP entries).  When the
+// queue is full the pairs are re-tested here; returns true if one of those hit.
+template <uint64_t CAP>
 __device__ bool flush_unc(const WarpSmem &sm, int nunc, int lane, uint32_t query, uint32_t step,
                           QueryCounters *ctr, RetestEntry *rq, const WorldDev &W, const StateSrc &src,
                           LaneStats &st)
@@ -343,7 +345,7 @@ __device__ bool flush_unc(const WarpSmem &sm, int nunc, int lane, uint32_t query
 		e.step = step;
 		e.env_tri = sm.unc[lane].x;
 		e.rob_tri = sm.unc[lane].y;
-		if (base + lane < RETEST_CAP) {
+		if (base + lane < CAP) {
 			rq[base + lane] = e;
 		} else {
 			st.inl++;
@@ -355,6 +357,7 @@ __device__ bool flush_unc(const WarpSmem &sm, int nunc, int lane, uint32_t query
 
 // Warp-cooperative traversal of one query; returns true on a certified hit
 // (or an inline FP64 hit).  Uncertain pairs of a query without a hit are queued.
+template <uint64_t CAP>
 __device__ bool traverse(const WorldDev &W, const QF &f, WarpSmem &sm, int lane, int soft_cap, uint32_t query,
                          uint32_t step, QueryCounters *ctr, RetestEntry *rq, const StateSrc &src, LaneStats &st)
 {
@@ -415,7 +418,7 @@ __device__ bool traverse(const WorldDev &W, const QF &f, WarpSmem &sm, int lane,
 		if (um) {
 			const int cnt = __popc(um);
 			if (nunc + cnt > UNC_CAP) {
-				if (flush_unc(sm, nunc, lane, query, step, ctr, rq, W, src, st)) {
+				if (flush_unc<CAP>(sm, nunc, lane, query, step, ctr, rq, W, src, st)) {
 					hit = true;
 					nunc = 0;
 					break;
@@ -438,7 +441,7 @@ __device__ bool traverse(const WorldDev &W, const QF &f, WarpSmem &sm, int lane,
 	}
 	__syncwarp();
 	if (!hit && nunc > 0)
-		hit = flush_unc(sm, nunc, lane, query, step, ctr, rq, W, src, st);
+		hit = flush_unc<CAP>(sm, nunc, lane, query, step, ctr, rq, W, src, st);
 	__syncwarp();
 	return hit;
 }
@@ -463,6 +466,7 @@ __device__ void flush_stats(QueryCounters *ctr, const LaneStats &st, unsigned lo
 
 // ------------------------------------------------------------------ states
 
+template <uint64_t CAP>
 __global__ void __launch_bounds__(WARPS * 32) k_states(WorldDev W, const double *states, int64_t n,
                                                        uint8_t *out, QueryCounters *ctr, RetestEntry *rq,
                                                        int soft_cap)
@@ -490,7 +494,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_states(WorldDev W, const double 
 		__syncwarp();
 		for (int j = 0; j < cnt; j++) {
 			const QF f = sm.qf[j];
-			const bool hit = traverse(W, f, sm, lane, soft_cap, (uint32_t)(base + j), 0u, ctr, rq, src, st);
+			const bool hit = traverse<CAP>(W, f, sm, lane, soft_cap, (uint32_t)(base + j), 0u, ctr, rq, src, st);
 			if (lane == 0)
 				out[base + j] = hit ? 0 : 1;
 		}
@@ -501,10 +505,11 @@ __global__ void __launch_bounds__(WARPS * 32) k_states(WorldDev W, const double 
 	flush_stats(ctr, st, queries, items, lane);
 }
 
+template <uint64_t CAP>
 __global__ void k_retest(WorldDev W, StateSrc src, uint8_t *valid_out, int32_t *first_out, QueryCounters *ctr,
                          const RetestEntry *rq)
 {
-	const unsigned long long cnt = min((unsigned long long)RETEST_CAP, ctr->retest_count);
+	const unsigned long long cnt = min((unsigned long long)CAP, ctr->retest_count);
 	unsigned long long hits = 0;
 	for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < cnt;
 	     i += (unsigned long long)gridDim.x * blockDim.x) {
@@ -733,7 +738,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_segments(WorldDev W, StateSrc sr
 				break;
 			const QF f = sm.qf[kk];
 			queries++;
-			const bool hit = traverse(W, f, sm, lane, soft_cap, s, (uint32_t)k, ctr, rq, src, st);
+			const bool hit = traverse<RETEST_CAP>(W, f, sm, lane, soft_cap, s, (uint32_t)k, ctr, rq, src, st);
 			if (hit) {
 				if (lane == 0)
 					atomicMin(&first[s], k);
@@ -954,18 +959,18 @@ extern "C" int pw_states_valid(pw_world *w, const double *states, int64_t n, uin
 		return PW_OK;
 	}
 	const size_t smem = warp_smem_bytes() * WARPS;
-	rc = set_smem_attr((const void *)k_states, smem);
+	rc = set_smem_attr((const void *)k_states<RETEST_CAP>, smem);
 	if (rc)
 		return rc;
-	const int grid = persistent_grid(w, (const void *)k_states, smem);
+	const int grid = persistent_grid(w, (const void *)k_states<RETEST_CAP>, smem);
 	RetestEntry *rq = (RetestEntry *)w->retest.ptr;
 	rc = mark(w, 0, st);
 	if (rc)
 		return rc;
-	k_states<<<grid, WARPS * 32, smem, st>>>(w->dev, states, n, valid, ctr, rq, soft_cap_of(w));
+	k_states<RETEST_CAP><<<grid, WARPS * 32, smem, st>>>(w->dev, states, n, valid, ctr, rq, soft_cap_of(w));
 	mark(w, 1, st);
 	StateSrc src{ states, nullptr, nullptr, nullptr, nullptr };
-	k_retest<<<w->num_sms * 4, 256, 0, st>>>(w->dev, src, valid, nullptr, ctr, rq);
+	k_retest<RETEST_CAP><<<w->num_sms * 4, 256, 0, st>>>(w->dev, src, valid, nullptr, ctr, rq);
 	mark(w, 2, st);
 	w->timed = true;
 	PW_CUDA(cudaGetLastError());
@@ -1094,7 +1099,7 @@ extern "C" int pw_segments_first_contact(pw_world *w, const double *from, const 
 	k_segments<<<grid, WARPS * 32, smem, st>>>(w->dev, src, vals2, round_off, max_rounds, first_step, ctr, rq,
 	                                           soft_cap_of(w));
 	mark(w, 1, st);
-	k_retest<<<w->num_sms * 4, 256, 0, st>>>(w->dev, src, nullptr, first_step, ctr, rq);
+	k_retest<RETEST_CAP><<<w->num_sms * 4, 256, 0, st>>>(w->dev, src, nullptr, first_step, ctr, rq);
 	mark(w, 2, st);
 	w->timed = true;
 	k_seg_finalize<<<G, B, 0, st>>>(first_step, params, n, ctr);
@@ -1211,5 +1216,86 @@ extern "C" int pw_world_last_stats(pw_world *w, pw_query_stats *out)
 		out->traverse_ms = a;
 		out->retest_ms = b;
 	}
+	return PW_OK;
+}
+
+// ------------------------------------------------------------------ allocation-free variant
+//
+// Some callers must not allocate device memory once they are running: a planner
+// or simulator that embeds this library inside a framework whose pool allocator
+// owns the whole device heap, or a latency-critical loop that cannot afford the
+// implicit device synchronisation of cudaMalloc/cudaFree.  For them,
+// pw_states_valid_noalloc keeps its scratch (query counters and the FP64
+// re-test queue) in the fixed device array below instead of the world's
+// buffers.  The array is part of the library image: every GPU that loads the
+// library holds it (NOALLOC_BYTES, about 16 MiB) until the process exits.
+
+namespace {
+constexpr uint64_t NOALLOC_RETEST_CAP = uint64_t(1) << 20;   // queued FP64 re-tests
+constexpr int64_t NOALLOC_MAX_STATES = int64_t(1) << 20;     // states per call
+constexpr size_t NOALLOC_CTR_BYTES = 256;                     // QueryCounters, padded
+static_assert(sizeof(QueryCounters) <= NOALLOC_CTR_BYTES, "counters do not fit their slot");
+constexpr size_t NOALLOC_BYTES = NOALLOC_CTR_BYTES + sizeof(RetestEntry) * NOALLOC_RETEST_CAP;
+} // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+// Host code cannot use the name g_noalloc_scratch as a device address; the real
+// address is looked up once per device, with that device current.
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_ptr[128];
+
+static int noalloc_scratch(int device, void **out)
+{
+	if (device < 0 || device >= 128)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_states_valid_noalloc: device ordinal out of range");
+	std::lock_guard<std::mutex> lock(g_noalloc_mu);
+	if (!g_noalloc_ptr[device]) {
+		void *p = nullptr;
+		const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+		if (e != cudaSuccess)
+			return pw_cuda_fail(e, "pw_states_valid_noalloc: cudaGetSymbolAddress");
+		g_noalloc_ptr[device] = p;
+	}
+	*out = g_noalloc_ptr[device];
+	return PW_OK;
+}
+
+extern "C" int pw_states_valid_noalloc(pw_world *w, const double *states, int64_t n, uint8_t *valid, void *stream)
+{
+	int rc = check_ready(w, "pw_states_valid_noalloc");
+	if (rc)
+		return rc;
+	if (n < 0 || (n > 0 && (!states || !valid)))
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_states_valid_noalloc: bad pointers or size");
+	if (n > NOALLOC_MAX_STATES)
+		return pw_fail(PW_ERR_INVALID_ARG,
+		               "pw_states_valid_noalloc: at most 1048576 states per call (split the batch or use "
+		               "pw_states_valid)");
+	PW_CUDA(cudaSetDevice(w->device));
+	void *scratch = nullptr;
+	rc = noalloc_scratch(w->device, &scratch);
+	if (rc)
+		return rc;
+	cudaStream_t st = (cudaStream_t)stream;
+	QueryCounters *ctr = (QueryCounters *)scratch;
+	RetestEntry *rq = (RetestEntry *)((unsigned char *)scratch + NOALLOC_CTR_BYTES);
+	// the array keeps the previous call's contents: the counters must start at zero
+	PW_CUDA(cudaMemsetAsync(ctr, 0, sizeof(QueryCounters), st));
+	if (n == 0)
+		return PW_OK;
+	if (w->dev.env.ntri == 0 || w->dev.rob.ntri == 0) {
+		PW_CUDA(cudaMemsetAsync(valid, 1, (size_t)n, st));
+		return PW_OK;
+	}
+	const size_t smem = warp_smem_bytes() * WARPS;
+	rc = set_smem_attr((const void *)k_states<NOALLOC_RETEST_CAP>, smem);
+	if (rc)
+		return rc;
+	const int grid = persistent_grid(w, (const void *)k_states<NOALLOC_RETEST_CAP>, smem);
+	k_states<NOALLOC_RETEST_CAP><<<grid, WARPS * 32, smem, st>>>(w->dev, states, n, valid, ctr, rq, soft_cap_of(w));
+	StateSrc src{ states, nullptr, nullptr, nullptr, nullptr };
+	k_retest<NOALLOC_RETEST_CAP><<<w->num_sms * 4, 256, 0, st>>>(w->dev, src, valid, nullptr, ctr, rq);
+	PW_CUDA(cudaGetLastError());
 	return PW_OK;
 }
