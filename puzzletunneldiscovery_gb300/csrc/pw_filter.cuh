@@ -1,0 +1,290 @@
+// pw_filter.cuh -- FP32 box and triangle tests with certified error bounds.
+//
+// Host and device: the device kernels use these, and host-side tests drive
+// the same code against the FP64 triangle test on adversarial inputs.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "pw_math.cuh"
+
+namespace pwf {
+
+constexpr float U32 = 5.9604645e-08f;     // 2^-24
+
+// Per-query FP32 transform and error bounds: five float4 per query slot in
+// shared memory (80-byte stride, so lanes reading different slots hit
+// different banks; lanes reading the same slot get a broadcast).
+//   q[0] = (R00, R01, R02, t0)   q[1] = (R10, R11, R12, t1)   q[2] = (R20, R21, R22, t2)
+//   q[3] = (er, margin, dx, W)   q[4] = (eg, 0, 0, 0)
+// er:     entrywise bound on |R32 - Q|, Q the exact rotation closest to the state's (box tests)
+// margin: absolute slack added to every separating-axis inequality
+// dx:     per-coordinate bound on |(robot vertex - env vertex) in FP32 - the same in FP64|
+// W:      bound on any coordinate magnitude (for the FP64 side's own rounding)
+// eg:     a robot edge g rotates with error <= eg * |g|_1
+struct QFs {
+	float4 q[5];
+};
+
+PW_HD void make_qf(const double *q, float r1_rob, float emax_env, float del_env, QFs &o)
+{
+	const float x = (float)q[4], y = (float)q[5], z = (float)q[6], w = (float)q[3];
+	const float tx = 2.f * x, ty = 2.f * y, tz = 2.f * z;
+	const float twx = tx * w, twy = ty * w, twz = tz * w;
+	const float txx = tx * x, txy = ty * x, txz = tz * x;
+	const float tyy = ty * y, tyz = tz * y, tzz = tz * z;
+	const float t0 = (float)q[0], t1 = (float)q[1], t2 = (float)q[2];
+	o.q[0] = make_float4(1.f - (tyy + tzz), txy - twz, txz + twy, t0);
+	o.q[1] = make_float4(txy + twz, 1.f - (txx + tzz), tyz - twx, t1);
+	o.q[2] = make_float4(txz - twy, tyz + twx, 1.f - (txx + tyy), t2);
+	const float s = x * x + y * y + z * z + w * w;
+	const float dev = fabsf(1.f - s) + 8.f * U32 * s;        // |1 - |q|^2| for the FP64 quaternion
+	const float epsR = (10.f * s + 4.f) * U32;                // |R32 - R(q64)| entrywise
+	const float r1 = r1_rob;                                  // |x|_1 of any robot point (local frame)
+	const float tinf = fmaxf(fmaxf(fabsf(t0), fabsf(t1)), fabsf(t2));
+	const float rs = (1.f + 2.f * dev) * r1;                  // bound of |R x|_inf
+	// robot vertex: rotation error, vertex rounding, three FMA roundings, t rounding, FP64 side
+	const float del_r = epsR * r1 + U32 * rs + 3.f * U32 * (tinf + rs) + U32 * tinf + 1e-15f * (r1 + tinf);
+	const float Wm = tinf + r1 + emax_env;
+	const float er = epsR + 2.f * dev;
+	const float margin = del_r + er * (3.f * r1 + 4.f * Wm) + 32.f * U32 * Wm;
+	o.q[3] = make_float4(er, margin, del_r + del_env, Wm);
+	o.q[4] = make_float4(epsR + 5.f * U32 * (1.f + 2.f * dev), 0.f, 0.f, 0.f);
+}
+
+// Separating-axis test of an env node box (centre A0, half-extents A1) and a
+// robot node box (local centre B0, half-extents B1) placed by the slot's
+// transform.  Returns a lower bound on the distance between the boxes when a
+// separating axis is certified (> 0), or -1 when they may overlap.  The slack
+// covers FP32 placement and arithmetic error and the distance of R32 from a
+// rotation; the result is scaled down for axes whose length may exceed 1.
+PW_HD float sat_sep32(const float4 &A0, const float4 &A1, const float4 &B0, const float4 &B1, const float4 &Q0,
+                      const float4 &Q1, const float4 &Q2, const float4 &Q3)
+{
+	const float R00 = Q0.x, R01 = Q0.y, R02 = Q0.z, R10 = Q1.x, R11 = Q1.y, R12 = Q1.z;
+	const float R20 = Q2.x, R21 = Q2.y, R22 = Q2.z;
+	const float T0 = fmaf(R00, B0.x, fmaf(R01, B0.y, fmaf(R02, B0.z, Q0.w))) - A0.x;
+	const float T1 = fmaf(R10, B0.x, fmaf(R11, B0.y, fmaf(R12, B0.z, Q1.w))) - A0.y;
+	const float T2 = fmaf(R20, B0.x, fmaf(R21, B0.y, fmaf(R22, B0.z, Q2.w))) - A0.z;
+	const float a0 = A1.x, a1 = A1.y, a2 = A1.z, b0 = B1.x, b1 = B1.y, b2 = B1.z;
+	const float m = fmaf(Q3.x, (a0 + a1 + a2) + (b0 + b1 + b2), Q3.y);
+	const float shrink = 1.f - 4.f * Q3.x;
+	const float aR00 = fabsf(R00), aR01 = fabsf(R01), aR02 = fabsf(R02);
+	const float aR10 = fabsf(R10), aR11 = fabsf(R11), aR12 = fabsf(R12);
+	const float aR20 = fabsf(R20), aR21 = fabsf(R21), aR22 = fabsf(R22);
+	float g;
+	// env axes (unit length)
+	if ((g = fabsf(T0) - (a0 + fmaf(b0, aR00, fmaf(b1, aR01, fmaf(b2, aR02, m))))) > 0.f) return g;
+	if ((g = fabsf(T1) - (a1 + fmaf(b0, aR10, fmaf(b1, aR11, fmaf(b2, aR12, m))))) > 0.f) return g;
+	if ((g = fabsf(T2) - (a2 + fmaf(b0, aR20, fmaf(b1, aR21, fmaf(b2, aR22, m))))) > 0.f) return g;
+	// robot axes
+	if ((g = fabsf(fmaf(T0, R00, fmaf(T1, R10, T2 * R20))) - (b0 + fmaf(a0, aR00, fmaf(a1, aR10, fmaf(a2, aR20, m))))) > 0.f) return g * shrink;
+	if ((g = fabsf(fmaf(T0, R01, fmaf(T1, R11, T2 * R21))) - (b1 + fmaf(a0, aR01, fmaf(a1, aR11, fmaf(a2, aR21, m))))) > 0.f) return g * shrink;
+	if ((g = fabsf(fmaf(T0, R02, fmaf(T1, R12, T2 * R22))) - (b2 + fmaf(a0, aR02, fmaf(a1, aR12, fmaf(a2, aR22, m))))) > 0.f) return g * shrink;
+	// cross axes e_i x (column j of R), length at most that of the column
+	if ((g = fabsf(T2 * R10 - T1 * R20) - fmaf(a1, aR20, fmaf(a2, aR10, fmaf(b1, aR02, fmaf(b2, aR01, m))))) > 0.f) return g * shrink;
+	if ((g = fabsf(T2 * R11 - T1 * R21) - fmaf(a1, aR21, fmaf(a2, aR11, fmaf(b0, aR02, fmaf(b2, aR00, m))))) > 0.f) return g * shrink;
+	if ((g = fabsf(T2 * R12 - T1 * R22) - fmaf(a1, aR22, fmaf(a2, aR12, fmaf(b0, aR01, fmaf(b1, aR00, m))))) > 0.f) return g * shrink;
+	if ((g = fabsf(T0 * R20 - T2 * R00) - fmaf(a0, aR20, fmaf(a2, aR00, fmaf(b1, aR12, fmaf(b2, aR11, m))))) > 0.f) return g * shrink;
+	if ((g = fabsf(T0 * R21 - T2 * R01) - fmaf(a0, aR21, fmaf(a2, aR01, fmaf(b0, aR12, fmaf(b2, aR10, m))))) > 0.f) return g * shrink;
+	if ((g = fabsf(T0 * R22 - T2 * R02) - fmaf(a0, aR22, fmaf(a2, aR02, fmaf(b0, aR11, fmaf(b1, aR10, m))))) > 0.f) return g * shrink;
+	if ((g = fabsf(T1 * R00 - T0 * R10) - fmaf(a0, aR10, fmaf(a1, aR00, fmaf(b1, aR22, fmaf(b2, aR21, m))))) > 0.f) return g * shrink;
+	if ((g = fabsf(T1 * R01 - T0 * R11) - fmaf(a0, aR11, fmaf(a1, aR01, fmaf(b0, aR22, fmaf(b2, aR20, m))))) > 0.f) return g * shrink;
+	if ((g = fabsf(T1 * R02 - T0 * R12) - fmaf(a0, aR12, fmaf(a1, aR02, fmaf(b0, aR21, fmaf(b1, aR20, m))))) > 0.f) return g * shrink;
+	return -1.f;
+}
+
+PW_HD bool sat_disjoint32(const float4 &A0, const float4 &A1, const float4 &B0, const float4 &B1, const float4 &Q0,
+                          const float4 &Q1, const float4 &Q2, const float4 &Q3)
+{
+	return sat_sep32(A0, A1, B0, B1, Q0, Q1, Q2, Q3) > 0.f;
+}
+
+PW_HD float3 f3(float4 a) { return make_float3(a.x, a.y, a.z); }
+PW_HD float3 f3add(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+PW_HD float3 f3sub(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+PW_HD float3 f3neg(float3 a) { return make_float3(-a.x, -a.y, -a.z); }
+PW_HD float3 f3cross(float3 a, float3 b)
+{
+	return make_float3(fmaf(a.y, b.z, -a.z * b.y), fmaf(a.z, b.x, -a.x * b.z), fmaf(a.x, b.y, -a.y * b.x));
+}
+PW_HD float f3dot(float3 a, float3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
+PW_HD float f3inf(float3 a) { return fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fabsf(a.z)); }
+PW_HD float f3l1(float3 a) { return fabsf(a.x) + fabsf(a.y) + fabsf(a.z); }
+PW_HD float f3get(float3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
+
+// Signed distances of three points (given relative to the plane's first vertex,
+// w[k] with per-coordinate error ew[k]) to the plane with normal N = e1 x e2,
+// and a bound b[k] on |FP32 value - FP64 value (Moeller's formula)|.
+struct PlaneRes {
+	float3 N;
+	float etaN, NL1;
+	float d[3], b[3];
+};
+
+PW_HD void plane_bounds(float3 e1, float3 e2, float ee1, float ee2, const float3 *w,
+                                             const float *ew, float M, PlaneRes &r)
+{
+	r.N = f3cross(e1, e2);
+	const float A1 = f3inf(e1), A2 = f3inf(e2);
+	r.etaN = 2.f * (A1 * ee2 + ee1 * A2 + ee1 * ee2) + 3.f * U32 * A1 * A2;
+	const float NL1 = f3l1(r.N) + 3.f * r.etaN;
+	r.NL1 = NL1;
+	const float b64 = 4e-15f * (NL1 + 4.f * A1 * A2) * M;
+#pragma unroll
+	for (int k = 0; k < 3; k++) {
+		const float Wi = f3inf(w[k]), W1 = f3l1(w[k]);
+		r.d[k] = f3dot(r.N, w[k]);
+		r.b[k] = 2.f * (NL1 * ew[k] + r.etaN * (W1 + 3.f * ew[k]) + 3.f * U32 * NL1 * Wi + b64);
+	}
+}
+
+// -1 / +1 certified sign, 0 uncertain.
+PW_HD int csign(float d, float b) { return d > b ? 1 : (d < -b ? -1 : 0); }
+
+// Lone vertex from certified nonzero signs (mirrors the FP64 dispatch).
+PW_HD int lone3(const int *s)
+{
+	if (s[0] * s[1] > 0) return 2;
+	if (s[0] * s[2] > 0) return 1;
+	return 0;
+}
+
+// Interval on the projection axis: endpoints p_l + (p_o - p_l) d_l / (d_l - d_o)
+// with p relative to a common origin.  ea[k]: error of p[k]; ei[k]: the part of
+// it that does not cancel in differences.  Returns the endpoints and a bound.
+PW_HD void interval_bounds(const float *p, const float *ea, const float *ei, const float *d,
+                                                const float *b, int lone, float *lo, float *hi, float *err)
+{
+	const int o1 = lone == 0 ? 1 : 0;
+	const int o2 = lone == 2 ? 1 : 2;
+	const int oo[2] = { o1, o2 };
+	float e[2], E = 0.f;
+#pragma unroll
+	for (int k = 0; k < 2; k++) {
+		const int o = oo[k];
+		const float den = fabsf(d[lone]) + fabsf(d[o]);
+		const float bb = b[lone] + b[o];
+		const float r = d[lone] / (d[lone] - d[o]);
+		const float dr = bb / fmaxf(den - bb, 1e-37f) + 3.f * U32;
+		const float pd = p[o] - p[lone];
+		e[k] = fmaf(pd, r, p[lone]);
+		const float epd = ei[o] + ei[lone] + U32 * fabsf(pd);
+		const float ek = ea[lone] + epd + fabsf(pd) * dr + U32 * (fabsf(p[lone]) + 2.f * fabsf(pd));
+		E = fmaxf(E, ek);
+	}
+	*lo = fminf(e[0], e[1]);
+	*hi = fmaxf(e[0], e[1]);
+	*err = E;
+}
+
+// Lower bound on the distance between a triangle and the points of a plane
+// test whose signs are all certified equal: min (|d| - b) / |N|_1.
+PW_HD float plane_gap(const PlaneRes &r)
+{
+	float g = fabsf(r.d[0]) - r.b[0];
+	g = fminf(g, fabsf(r.d[1]) - r.b[1]);
+	g = fminf(g, fabsf(r.d[2]) - r.b[2]);
+	return fmaxf(g, 0.f) / r.NL1;
+}
+
+// FP32 Moeller filter of env triangle (V0, edges e1, e2) against robot triangle
+// (local vertex x0, local edges g1, g2) placed by the slot's transform.
+// 0 = certified separate, 1 = certified intersecting, 2 = uncertain.
+// *gap: a lower bound on the distance between the triangles (0 when unknown).
+PW_HD int tri_filter(float3 V0, float3 e1, float3 e2, float3 x0, float3 g1, float3 g2, const float4 &Q0,
+                     const float4 &Q1, const float4 &Q2, const float4 &Q3, float eg, float *gap)
+{
+	*gap = 0.f;
+	const float dx = Q3.z, M = Q3.w;
+	const float3 U0 = make_float3(fmaf(Q0.x, x0.x, fmaf(Q0.y, x0.y, fmaf(Q0.z, x0.z, Q0.w))),
+	                              fmaf(Q1.x, x0.x, fmaf(Q1.y, x0.y, fmaf(Q1.z, x0.z, Q1.w))),
+	                              fmaf(Q2.x, x0.x, fmaf(Q2.y, x0.y, fmaf(Q2.z, x0.z, Q2.w))));
+	const float3 f1 = make_float3(fmaf(Q0.x, g1.x, fmaf(Q0.y, g1.y, Q0.z * g1.z)),
+	                              fmaf(Q1.x, g1.x, fmaf(Q1.y, g1.y, Q1.z * g1.z)),
+	                              fmaf(Q2.x, g1.x, fmaf(Q2.y, g1.y, Q2.z * g1.z)));
+	const float3 f2 = make_float3(fmaf(Q0.x, g2.x, fmaf(Q0.y, g2.y, Q0.z * g2.z)),
+	                              fmaf(Q1.x, g2.x, fmaf(Q1.y, g2.y, Q1.z * g2.z)),
+	                              fmaf(Q2.x, g2.x, fmaf(Q2.y, g2.y, Q2.z * g2.z)));
+	const float G1 = eg * f3l1(g1) + 1e-15f * M, G2 = eg * f3l1(g2) + 1e-15f * M;   // errors of f1, f2
+	const float A1 = f3inf(e1), A2 = f3inf(e2);
+	const float3 w0 = f3sub(U0, V0);                       // U0 - V0
+	const float ew0 = dx + U32 * f3inf(w0);
+	// robot vertices relative to V0: du = N1 . (U_k - V0)
+	float3 w[3];
+	float ew[3], eiu[3];
+	w[0] = w0;
+	w[1] = f3add(w0, f1);
+	w[2] = f3add(w0, f2);
+	ew[0] = ew0;
+	ew[1] = ew0 + G1 + U32 * f3inf(w[1]);
+	ew[2] = ew0 + G2 + U32 * f3inf(w[2]);
+	PlaneRes pv;
+	plane_bounds(e1, e2, U32 * A1, U32 * A2, w, ew, M, pv);
+	int su[3];
+#pragma unroll
+	for (int k = 0; k < 3; k++) su[k] = csign(pv.d[k], pv.b[k]);
+	if (su[0] == 0 || su[1] == 0 || su[2] == 0)
+		return 2;
+	if (su[0] == su[1] && su[0] == su[2]) {
+		*gap = plane_gap(pv);
+		return 0;
+	}
+	// env vertices relative to U0: dv = N2 . (V_i - U0)
+	float3 v[3];
+	float evv[3];
+	v[0] = f3neg(w0);
+	v[1] = f3add(v[0], e1);
+	v[2] = f3add(v[0], e2);
+	evv[0] = ew0;
+	evv[1] = ew0 + U32 * A1 + U32 * f3inf(v[1]);
+	evv[2] = ew0 + U32 * A2 + U32 * f3inf(v[2]);
+	PlaneRes pu;
+	plane_bounds(f1, f2, G1, G2, v, evv, M, pu);
+	int sv[3];
+#pragma unroll
+	for (int k = 0; k < 3; k++) sv[k] = csign(pu.d[k], pu.b[k]);
+	if (sv[0] == 0 || sv[1] == 0 || sv[2] == 0)
+		return 2;
+	if (sv[0] == sv[1] && sv[0] == sv[2]) {
+		*gap = plane_gap(pu);
+		return 0;
+	}
+	// direction of the intersection line and the FP64 axis choice
+	const float3 Dl = f3cross(pv.N, pu.N);
+	const float n1 = f3inf(pv.N), n2 = f3inf(pu.N);
+	const float etaD = 2.f * (2.f * (n1 * pu.etaN + pv.etaN * n2 + pv.etaN * pu.etaN) + 3.f * U32 * n1 * n2 +
+	                          3e-14f * n1 * n2);
+	const float a0 = fabsf(Dl.x), a1 = fabsf(Dl.y), a2 = fabsf(Dl.z);
+	int ax = 0;
+	float mx = a0;
+	if (a1 > mx) { mx = a1; ax = 1; }
+	if (a2 > mx) { mx = a2; ax = 2; }
+	const float o_a = ax == 0 ? a1 : a0;
+	const float o_b = ax == 2 ? a1 : a2;
+	if (mx - o_a <= 2.f * etaD || mx - o_b <= 2.f * etaD)
+		return 2;
+	// projections relative to V0 on the chosen axis
+	const float pvv[3] = { 0.f, f3get(e1, ax), f3get(e2, ax) };
+	const float eav[3] = { 0.f, U32 * A1, U32 * A2 };
+	const float puu[3] = { f3get(w[0], ax), f3get(w[1], ax), f3get(w[2], ax) };
+	const float eau[3] = { ew[0], ew[1], ew[2] };
+	eiu[0] = U32 * fabsf(puu[0]);
+	eiu[1] = G1 + U32 * fabsf(puu[1]);
+	eiu[2] = G2 + U32 * fabsf(puu[2]);
+	float vlo, vhi, verr, ulo, uhi, uerr;
+	interval_bounds(pvv, eav, eav, pu.d, pu.b, lone3(sv), &vlo, &vhi, &verr);
+	interval_bounds(puu, eau, eiu, pv.d, pv.b, lone3(su), &ulo, &uhi, &uerr);
+	const float B = 2.f * (verr + uerr + 1e-14f * M);
+	const float s1 = ulo - vhi, s2 = vlo - uhi;
+	if (s1 > B || s2 > B)
+		return 0;
+	if (s1 < -B && s2 < -B)
+		return 1;
+	return 2;
+}
+
+
+} // namespace pwf

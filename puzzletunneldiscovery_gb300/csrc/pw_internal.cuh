@@ -12,7 +12,8 @@
 // Morton order of the build); FP64 data stays in the original face order.
 //   nodeA[i] = (centre.xyz, left child)   nodeB[i] = (half-extent.xyz, right child)
 //   internal nodes 0 .. ntri-2 (root 0), leaves ntri-1 .. 2*ntri-2 (slot = i - leaf_base).
-//   triA/B/C[slot] = FP32 vertices 0/1/2 (w of triA = original face id).
+//   triA/B/C[slot] = FP32 vertex 0, edge 1-0, edge 2-0, each rounded once from FP64
+//   (w of triA = original face id).
 // Boxes are conservative: they contain the FP64 vertices exactly.
 struct MeshDev {
 	int32_t ntri = 0;
@@ -24,6 +25,7 @@ struct MeshDev {
 	double *V64 = nullptr;   // nvert x 3 (env: perturbation frame; robot: local frame)
 	int32_t *F = nullptr;    // ntri x 3
 	float r1 = 0.f;          // L1 bound of any point of any node box (robot: local frame)
+	double r2 = 0.0;         // max Euclidean norm of a vertex (robot: local frame)
 	float emax = 0.f;        // max |coordinate| of any vertex
 };
 
@@ -62,10 +64,10 @@ struct RetestEntry {
 
 // Per-segment constants of the stepping loop, built on the device.
 struct SegParams {
-	double a[7], b[7];        // from / to states (as given)
 	double qa[4], qb[4];      // normalised rotations
 	double d, theta, stheta;  // slerp constants
 	double dist, inv_dist, step;
+	double skip_scale;        // bound on the motion of any robot point from one step to the next
 	int32_t linear;
 	int32_t nsteps;           // steps the reference loop takes (0: none)
 	int64_t ckpt_base;        // first checkpoint slot

@@ -26,30 +26,28 @@
 
 #include "pw_internal.cuh"
 #include "pw_math.cuh"
+#include "pw_filter.cuh"
 
 namespace {
+
+using namespace pwf;
 
 constexpr int WARPS = 4;                  // warps per block
 constexpr int STACK_CAP = 1024;           // node-pair stack entries per warp
 constexpr int UNC_CAP = 32;               // uncertain pairs buffered per warp
-constexpr float U32 = 5.9604645e-08f;     // 2^-24
 constexpr unsigned FULL = 0xffffffffu;
 constexpr uint64_t RETEST_CAP = 1u << 22; // queued FP64 re-tests per query batch
 
-// Per-query FP32 transform and error bounds.
-struct QF {
-	float R[9];
-	float AR[9];    // |R| + slack
-	float t[3];
-	float del;      // bound on |difference of two FP32 vertices - FP64 difference| per coordinate
-	float margin;   // absolute slack of every separating-axis test
-	float W;        // magnitude bound of any coordinate (scene extent)
-};
+constexpr int SLOT_SHIFT = 27;                       // stack entry: (env node, robot node | slot << 27)
+constexpr uint32_t NODE_MASK = (1u << SLOT_SHIFT) - 1u;
 
 struct WarpSmem {
 	uint2 stack[STACK_CAP];
 	uint2 unc[UNC_CAP];
-	QF qf[32];
+	QFs qf[32];
+	uint32_t slot_query[32];   // state or segment index of each slot
+	uint32_t slot_step[32];    // segment step of each slot (0 for states)
+	uint8_t unc_slot[UNC_CAP];
 };
 
 // Where the FP64 state of a query comes from when a pair must be re-tested.
@@ -60,214 +58,9 @@ struct StateSrc {
 	const double *ckpt;
 };
 
-__device__ __forceinline__ void make_qf(const double *q, const WorldDev &W, QF &o)
+__device__ __forceinline__ void make_qf(const double *q, const WorldDev &W, QFs &o)
 {
-	const float x = (float)q[4], y = (float)q[5], z = (float)q[6], w = (float)q[3];
-	const float tx = 2.f * x, ty = 2.f * y, tz = 2.f * z;
-	const float twx = tx * w, twy = ty * w, twz = tz * w;
-	const float txx = tx * x, txy = ty * x, txz = tz * x;
-	const float tyy = ty * y, tyz = tz * y, tzz = tz * z;
-	o.R[0] = 1.f - (tyy + tzz); o.R[1] = txy - twz;         o.R[2] = txz + twy;
-	o.R[3] = txy + twz;         o.R[4] = 1.f - (txx + tzz); o.R[5] = tyz - twx;
-	o.R[6] = txz - twy;         o.R[7] = tyz + twx;         o.R[8] = 1.f - (txx + tyy);
-	o.t[0] = (float)q[0]; o.t[1] = (float)q[1]; o.t[2] = (float)q[2];
-	const float s = x * x + y * y + z * z + w * w;
-	const float dev = fabsf(1.f - s) + 8.f * U32 * s;
-	const float epsR = 16.f * U32 * (1.f + s);
-	const float r1 = W.rob.r1;
-	const float tinf = fmaxf(fmaxf(fabsf(o.t[0]), fabsf(o.t[1])), fabsf(o.t[2]));
-	const float del_r = epsR * r1 + 8.f * U32 * ((1.f + 2.f * s) * r1 + tinf) + 1e-30f;
-	const float Wm = tinf + r1 + W.env.emax;
-	const float er = epsR + 2.f * dev;
-#pragma unroll
-	for (int i = 0; i < 9; i++)
-		o.AR[i] = fabsf(o.R[i]) + er;
-	o.W = Wm;
-	o.margin = del_r + er * (3.f * r1 + 4.f * Wm) + 128.f * U32 * Wm;
-	o.del = 2.f * fmaxf(del_r, W.del_env);
-}
-
-// Separating-axis test of env node box (ca, ea) and robot node box (cb local, eb);
-// true when provably disjoint.
-__device__ __forceinline__ bool sat_disjoint32(const float4 &A0, const float4 &A1, const float4 &B0,
-                                               const float4 &B1, const QF &f)
-{
-	const float *R = f.R, *AR = f.AR;
-	const float T0 = fmaf(R[0], B0.x, fmaf(R[1], B0.y, fmaf(R[2], B0.z, f.t[0]))) - A0.x;
-	const float T1 = fmaf(R[3], B0.x, fmaf(R[4], B0.y, fmaf(R[5], B0.z, f.t[1]))) - A0.y;
-	const float T2 = fmaf(R[6], B0.x, fmaf(R[7], B0.y, fmaf(R[8], B0.z, f.t[2]))) - A0.z;
-	const float ea0 = A1.x, ea1 = A1.y, ea2 = A1.z;
-	const float eb0 = B1.x, eb1 = B1.y, eb2 = B1.z;
-	const float m = f.margin;
-	// env axes
-	if (fabsf(T0) > ea0 + fmaf(eb0, AR[0], fmaf(eb1, AR[1], eb2 * AR[2])) + m) return true;
-	if (fabsf(T1) > ea1 + fmaf(eb0, AR[3], fmaf(eb1, AR[4], eb2 * AR[5])) + m) return true;
-	if (fabsf(T2) > ea2 + fmaf(eb0, AR[6], fmaf(eb1, AR[7], eb2 * AR[8])) + m) return true;
-	// robot axes
-	if (fabsf(fmaf(T0, R[0], fmaf(T1, R[3], T2 * R[6]))) > fmaf(ea0, AR[0], fmaf(ea1, AR[3], ea2 * AR[6])) + eb0 + m) return true;
-	if (fabsf(fmaf(T0, R[1], fmaf(T1, R[4], T2 * R[7]))) > fmaf(ea0, AR[1], fmaf(ea1, AR[4], ea2 * AR[7])) + eb1 + m) return true;
-	if (fabsf(fmaf(T0, R[2], fmaf(T1, R[5], T2 * R[8]))) > fmaf(ea0, AR[2], fmaf(ea1, AR[5], ea2 * AR[8])) + eb2 + m) return true;
-	// cross axes A_i x B_j
-#define PW_CROSS(i1, i2, ti1, ti2, ea_i1, ea_i2, j, j1, j2, eb_j1, eb_j2, i)                                      \
-	if (fabsf(ti2 * R[3 * i1 + j] - ti1 * R[3 * i2 + j]) >                                                        \
-	    ea_i1 * AR[3 * i2 + j] + ea_i2 * AR[3 * i1 + j] + eb_j1 * AR[3 * i + j2] + eb_j2 * AR[3 * i + j1] + m)   \
-		return true;
-	PW_CROSS(1, 2, T1, T2, ea1, ea2, 0, 1, 2, eb1, eb2, 0)
-	PW_CROSS(1, 2, T1, T2, ea1, ea2, 1, 2, 0, eb2, eb0, 0)
-	PW_CROSS(1, 2, T1, T2, ea1, ea2, 2, 0, 1, eb0, eb1, 0)
-	PW_CROSS(2, 0, T2, T0, ea2, ea0, 0, 1, 2, eb1, eb2, 1)
-	PW_CROSS(2, 0, T2, T0, ea2, ea0, 1, 2, 0, eb2, eb0, 1)
-	PW_CROSS(2, 0, T2, T0, ea2, ea0, 2, 0, 1, eb0, eb1, 1)
-	PW_CROSS(0, 1, T0, T1, ea0, ea1, 0, 1, 2, eb1, eb2, 2)
-	PW_CROSS(0, 1, T0, T1, ea0, ea1, 1, 2, 0, eb2, eb0, 2)
-	PW_CROSS(0, 1, T0, T1, ea0, ea1, 2, 0, 1, eb0, eb1, 2)
-#undef PW_CROSS
-	return false;
-}
-
-__device__ __forceinline__ float3 f3sub(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ float3 f3cross(float3 a, float3 b)
-{
-	return make_float3(fmaf(a.y, b.z, -a.z * b.y), fmaf(a.z, b.x, -a.x * b.z), fmaf(a.x, b.y, -a.y * b.x));
-}
-__device__ __forceinline__ float f3dot(float3 a, float3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
-__device__ __forceinline__ float f3inf(float3 a) { return fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fabsf(a.z)); }
-__device__ __forceinline__ float f3l1(float3 a) { return fabsf(a.x) + fabsf(a.y) + fabsf(a.z); }
-__device__ __forceinline__ float f3get(float3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
-
-// Plane of S against the vertices of T: signed distances with error bounds.
-// D = per-coordinate error of any vertex difference; M = coordinate magnitude.
-struct PlaneRes {
-	float3 N;
-	float etaN;
-	float d[3], b[3];
-};
-
-__device__ __forceinline__ void plane_bounds(float3 S0, float3 S1, float3 S2, float3 T0, float3 T1, float3 T2,
-                                             float D, float M, PlaneRes &r)
-{
-	const float3 e1 = f3sub(S1, S0), e2 = f3sub(S2, S0);
-	r.N = f3cross(e1, e2);
-	const float A1 = f3inf(e1), A2 = f3inf(e2);
-	const float ee1 = D + U32 * A1, ee2 = D + U32 * A2;
-	r.etaN = 2.f * (A1 * ee2 + ee1 * A2 + ee1 * ee2) + 3.f * U32 * A1 * A2;
-	const float NL1 = f3l1(r.N) + 3.f * r.etaN;
-	const float b64 = 4e-15f * (NL1 + 4.f * A1 * A2) * M;
-	const float3 T[3] = { T0, T1, T2 };
-#pragma unroll
-	for (int k = 0; k < 3; k++) {
-		const float3 w = f3sub(T[k], S0);
-		const float Wi = f3inf(w), W1 = f3l1(w);
-		const float ew = D + U32 * Wi;
-		r.d[k] = f3dot(r.N, w);
-		r.b[k] = 2.f * (NL1 * ew + r.etaN * (W1 + 3.f * ew) + 3.f * U32 * NL1 * Wi + b64);
-	}
-}
-
-// -1 / +1 certified sign, 0 uncertain.
-__device__ __forceinline__ int csign(float d, float b) { return d > b ? 1 : (d < -b ? -1 : 0); }
-
-// Lone vertex from certified nonzero signs (mirrors the FP64 dispatch).
-__device__ __forceinline__ int lone3(const int *s)
-{
-	if (s[0] * s[1] > 0) return 2;
-	if (s[0] * s[2] > 0) return 1;
-	return 0;
-}
-
-// Interval endpoints on axis `ax` relative to origin O, with an error bound.
-__device__ __forceinline__ void interval_bounds(const float *p, const float *d, const float *b, int lone,
-                                                float etap, float *lo, float *hi, float *err)
-{
-	const int o1 = lone == 0 ? 1 : 0;
-	const int o2 = lone == 2 ? 1 : 2;
-	float e[2], E = 0.f;
-	const int oo[2] = { o1, o2 };
-#pragma unroll
-	for (int k = 0; k < 2; k++) {
-		const int o = oo[k];
-		const float den = fabsf(d[lone]) + fabsf(d[o]);
-		const float bb = b[lone] + b[o];
-		const float r = d[lone] / (d[lone] - d[o]);
-		const float dr = bb / fmaxf(den - bb, 1e-37f) + 3.f * U32;
-		const float pd = p[o] - p[lone];
-		e[k] = fmaf(pd, r, p[lone]);
-		const float ek = etap + (2.f * etap + U32 * fabsf(pd)) + fabsf(pd) * dr + U32 * (fabsf(p[lone]) + fabsf(pd));
-		E = fmaxf(E, ek);
-	}
-	*lo = fminf(e[0], e[1]);
-	*hi = fmaxf(e[0], e[1]);
-	*err = E;
-}
-
-// FP32 Moeller filter.  0 = certified separate, 1 = certified intersecting, 2 = uncertain.
-__device__ __noinline__ int tri_filter(float3 V0, float3 V1, float3 V2, float3 U0, float3 U1, float3 U2, float D,
-                                       float M)
-{
-	PlaneRes pv, pu;
-	plane_bounds(V0, V1, V2, U0, U1, U2, D, M, pv);   // du
-	int su[3];
-#pragma unroll
-	for (int k = 0; k < 3; k++) su[k] = csign(pv.d[k], pv.b[k]);
-	if (su[0] == 0 || su[1] == 0 || su[2] == 0)
-		return 2;
-	if (su[0] == su[1] && su[0] == su[2])
-		return 0;
-	plane_bounds(U0, U1, U2, V0, V1, V2, D, M, pu);   // dv
-	int sv[3];
-#pragma unroll
-	for (int k = 0; k < 3; k++) sv[k] = csign(pu.d[k], pu.b[k]);
-	if (sv[0] == 0 || sv[1] == 0 || sv[2] == 0)
-		return 2;
-	if (sv[0] == sv[1] && sv[0] == sv[2])
-		return 0;
-	// direction of the intersection line and the FP64 axis choice
-	const float3 Dl = f3cross(pv.N, pu.N);
-	const float n1 = f3inf(pv.N), n2 = f3inf(pu.N);
-	const float etaD = 2.f * (2.f * (n1 * pu.etaN + pv.etaN * n2 + pv.etaN * pu.etaN) + 3.f * U32 * n1 * n2 +
-	                          3e-14f * n1 * n2);
-	const float a0 = fabsf(Dl.x), a1 = fabsf(Dl.y), a2 = fabsf(Dl.z);
-	int ax = 0;
-	float mx = a0;
-	if (a1 > mx) { mx = a1; ax = 1; }
-	if (a2 > mx) { mx = a2; ax = 2; }
-	const float o_a = ax == 0 ? a1 : a0;
-	const float o_b = ax == 2 ? a1 : a2;
-	if (mx - o_a <= 2.f * etaD || mx - o_b <= 2.f * etaD)
-		return 2;
-	const float O = f3get(V0, ax);
-	const float pvv[3] = { 0.f, f3get(V1, ax) - O, f3get(V2, ax) - O };
-	const float puu[3] = { f3get(U0, ax) - O, f3get(U1, ax) - O, f3get(U2, ax) - O };
-	const float P = fmaxf(fmaxf(fmaxf(fabsf(pvv[1]), fabsf(pvv[2])), fmaxf(fabsf(puu[0]), fabsf(puu[1]))),
-	                      fabsf(puu[2]));
-	const float etap = D + U32 * P;
-	float vlo, vhi, verr, ulo, uhi, uerr;
-	interval_bounds(pvv, pu.d, pu.b, lone3(sv), etap, &vlo, &vhi, &verr);
-	interval_bounds(puu, pv.d, pv.b, lone3(su), etap, &ulo, &uhi, &uerr);
-	const float B = 2.f * (verr + uerr + 1e-14f * M);
-	const float s1 = ulo - vhi, s2 = vlo - uhi;
-	if (s1 > B || s2 > B)
-		return 0;
-	if (s1 < -B && s2 < -B)
-		return 1;
-	return 2;
-}
-
-__device__ __forceinline__ float3 xf(const QF &f, float4 p)
-{
-	return make_float3(fmaf(f.R[0], p.x, fmaf(f.R[1], p.y, fmaf(f.R[2], p.z, f.t[0]))),
-	                   fmaf(f.R[3], p.x, fmaf(f.R[4], p.y, fmaf(f.R[5], p.z, f.t[1]))),
-	                   fmaf(f.R[6], p.x, fmaf(f.R[7], p.y, fmaf(f.R[8], p.z, f.t[2]))));
-}
-
-__device__ int leaf_test(const WorldDev &W, const QF &f, int es, int rs, uint32_t *et, uint32_t *rt)
-{
-	const float4 a = __ldg(W.env.triA + es), b = __ldg(W.env.triB + es), c = __ldg(W.env.triC + es);
-	const float4 ra = __ldg(W.rob.triA + rs), rb = __ldg(W.rob.triB + rs), rc = __ldg(W.rob.triC + rs);
-	*et = (uint32_t)__float_as_int(a.w);
-	*rt = (uint32_t)__float_as_int(ra.w);
-	return tri_filter(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(c.x, c.y, c.z),
-	                  xf(f, ra), xf(f, rb), xf(f, rc), f.del, f.W);
+	pwf::make_qf(q, W.rob.r1, W.env.emax, W.del_env, o);
 }
 
 // FP64 re-test of one triangle pair at state q: exactly the oracle's arithmetic.
@@ -327,121 +120,323 @@ struct LaneStats {
 	unsigned long long node = 0, leaf = 0, inl = 0;
 };
 
-// Hand the buffered uncertain pairs to the FP64 queue (CAP entries).  When the
-// queue is full the pairs are re-tested here; returns true if one of those hit.
+// Queue the buffered uncertain pairs whose slot is not in `skip`.  When the
+// queue (CAP entries) is full the pair is re-tested here; returns the mask of
+// slots such an inline FP64 re-test found in contact.
 template <uint64_t CAP>
-__device__ bool flush_unc(const WarpSmem &sm, int nunc, int lane, uint32_t query, uint32_t step,
-                          QueryCounters *ctr, RetestEntry *rq, const WorldDev &W, const StateSrc &src,
-                          LaneStats &st)
+__device__ uint32_t flush_unc(const WarpSmem &sm, int nunc, uint32_t skip, int lane, QueryCounters *ctr,
+                              RetestEntry *rq, const WorldDev &W, const StateSrc &src, LaneStats &st)
 {
+	const int slot = lane < nunc ? (int)sm.unc_slot[lane] : 0;
+	const bool mine = lane < nunc && !((skip >> slot) & 1u);
+	const unsigned mm = __ballot_sync(FULL, mine);
+	if (!mm)
+		return 0u;
 	unsigned long long base = 0;
 	if (lane == 0)
-		base = atomicAdd(&ctr->retest_count, (unsigned long long)nunc);
+		base = atomicAdd(&ctr->retest_count, (unsigned long long)__popc(mm));
 	base = __shfl_sync(FULL, base, 0);
-	bool hit = false;
-	if (lane < nunc) {
+	uint32_t hits = 0u;
+	if (mine) {
+		const unsigned long long idx = base + __popc(mm & ((1u << lane) - 1u));
 		RetestEntry e;
-		e.query = query;
-		e.step = step;
+		e.query = sm.slot_query[slot];
+		e.step = sm.slot_step[slot];
 		e.env_tri = sm.unc[lane].x;
 		e.rob_tri = sm.unc[lane].y;
-		if (base + lane < CAP) {
-			rq[base + lane] = e;
+		if (idx < CAP) {
+			rq[idx] = e;
 		} else {
 			st.inl++;
-			hit = retest_entry(W, src, e);
+			if (retest_entry(W, src, e))
+				hits = 1u << slot;
 		}
 	}
-	return __any_sync(FULL, hit);
+	return __reduce_or_sync(FULL, hits);
 }
 
-// Warp-cooperative traversal of one query; returns true on a certified hit
-// (or an inline FP64 hit).  Uncertain pairs of a query without a hit are queued.
+// One warp answers up to 32 queries at once (slots = set bits of `open`;
+// sm.qf, sm.slot_query and sm.slot_step describe them): every stack entry
+// carries its slot, lanes test pairs of any open slot, and a slot closes at its
+// first certified contact.  Returns the mask of slots in contact.  Uncertain
+// pairs of slots still open at the end go to the FP64 queue.
 template <uint64_t CAP>
-__device__ bool traverse(const WorldDev &W, const QF &f, WarpSmem &sm, int lane, int soft_cap, uint32_t query,
-                         uint32_t step, QueryCounters *ctr, RetestEntry *rq, const StateSrc &src, LaneStats &st)
+__device__ uint32_t traverse_batch(const WorldDev &W, WarpSmem &sm, int lane, uint32_t open, int soft_cap,
+                                   QueryCounters *ctr, RetestEntry *rq, const StateSrc &src, LaneStats &st)
 {
 	const uint32_t ebase = (uint32_t)W.env.leaf_base, rbase = (uint32_t)W.rob.leaf_base;
 	const unsigned lt_mask = (1u << lane) - 1u;
-	if (lane == 0)
-		sm.stack[0] = make_uint2(0u, 0u);
+	const unsigned gt_mask = ~(lt_mask | (1u << lane));
+	const int nroot = __popc(open);
+	if ((open >> lane) & 1u)
+		sm.stack[nroot - 1 - __popc(open & lt_mask)] = make_uint2(0u, (uint32_t)lane << SLOT_SHIFT);
 	__syncwarp();
-	int top = 1, nunc = 0;
-	bool hit = false;
-	while (top > 0) {
+	int top = nroot, nunc = 0;
+	uint32_t done = ~open, hit = 0u;
+	while (top > 0 && done != FULL) {
 		int p = min(top, 32);
 		const int room = soft_cap - top;
 		if (room < p)
 			p = max(1, room);
-		const bool active = lane < p;
+		bool active = lane < p;
 		uint2 pr = make_uint2(0u, 0u);
 		if (active)
-			pr = sm.stack[top - p + lane];
+			pr = sm.stack[top - 1 - lane];
 		__syncwarp();
 		top -= p;
+		const int slot = (int)(pr.y >> SLOT_SHIFT);
+		const uint32_t rn = pr.y & NODE_MASK;
+		if ((done >> slot) & 1u)
+			active = false;
 		bool push = false, lhit = false, unc = false;
 		uint2 c0 = make_uint2(0u, 0u), c1 = make_uint2(0u, 0u), up = make_uint2(0u, 0u);
 		if (active) {
 			const float4 A0 = __ldg(W.env.nodeA + pr.x), A1 = __ldg(W.env.nodeB + pr.x);
-			const float4 B0 = __ldg(W.rob.nodeA + pr.y), B1 = __ldg(W.rob.nodeB + pr.y);
+			const float4 B0 = __ldg(W.rob.nodeA + rn), B1 = __ldg(W.rob.nodeB + rn);
+			const QFs &Q = sm.qf[slot];
+			const float4 Q0 = Q.q[0], Q1 = Q.q[1], Q2 = Q.q[2], Q3 = Q.q[3];
 			st.node++;
-			if (!sat_disjoint32(A0, A1, B0, B1, f)) {
-				const bool la = pr.x >= ebase, lb = pr.y >= rbase;
+			if (!sat_disjoint32(A0, A1, B0, B1, Q0, Q1, Q2, Q3)) {
+				const bool la = pr.x >= ebase, lb = rn >= rbase;
 				if (la && lb) {
 					st.leaf++;
-					uint32_t et, rt;
-					const int r = leaf_test(W, f, (int)(pr.x - ebase), (int)(pr.y - rbase), &et, &rt);
+					const int es = (int)(pr.x - ebase), rs = (int)(rn - rbase);
+					const float4 ta = __ldg(W.env.triA + es), tb = __ldg(W.env.triB + es),
+					             tc = __ldg(W.env.triC + es);
+					const float4 ra = __ldg(W.rob.triA + rs), rb = __ldg(W.rob.triB + rs),
+					             rc = __ldg(W.rob.triC + rs);
+					float gap;
+					const int r = tri_filter(f3(ta), f3(tb), f3(tc), f3(ra), f3(rb), f3(rc), Q0, Q1, Q2, Q3,
+					                         Q.q[4].x, &gap);
 					if (r == 1) {
 						lhit = true;
 					} else if (r == 2) {
 						unc = true;
-						up = make_uint2(et, rt);
+						up = make_uint2((uint32_t)__float_as_int(ta.w), (uint32_t)__float_as_int(ra.w));
 					}
 				} else {
+					const uint32_t sbits = (uint32_t)slot << SLOT_SHIFT;
 					const bool da = !la && (lb || (A1.x + A1.y + A1.z) >= (B1.x + B1.y + B1.z));
 					if (da) {
 						c0 = make_uint2((uint32_t)__float_as_int(A0.w), pr.y);
 						c1 = make_uint2((uint32_t)__float_as_int(A1.w), pr.y);
 					} else {
-						c0 = make_uint2(pr.x, (uint32_t)__float_as_int(B0.w));
-						c1 = make_uint2(pr.x, (uint32_t)__float_as_int(B1.w));
+						c0 = make_uint2(pr.x, (uint32_t)__float_as_int(B0.w) | sbits);
+						c1 = make_uint2(pr.x, (uint32_t)__float_as_int(B1.w) | sbits);
 					}
 					push = true;
 				}
 			}
 		}
-		if (__any_sync(FULL, lhit)) {
-			hit = true;
-			break;
+		const uint32_t hm = __reduce_or_sync(FULL, lhit ? (1u << slot) : 0u);
+		if (hm) {
+			hit |= hm;
+			done |= hm;
+			if (done == FULL)
+				break;
 		}
-		const unsigned um = __ballot_sync(FULL, unc);
+		unc = unc && !((done >> slot) & 1u);
+		unsigned um = __ballot_sync(FULL, unc);
 		if (um) {
-			const int cnt = __popc(um);
-			if (nunc + cnt > UNC_CAP) {
-				if (flush_unc<CAP>(sm, nunc, lane, query, step, ctr, rq, W, src, st)) {
-					hit = true;
-					nunc = 0;
-					break;
-				}
+			if (nunc + __popc(um) > UNC_CAP) {
+				const uint32_t ih = flush_unc<CAP>(sm, nunc, done, lane, ctr, rq, W, src, st);
 				nunc = 0;
 				__syncwarp();
+				if (ih) {
+					hit |= ih;
+					done |= ih;
+					if (done == FULL)
+						break;
+					unc = unc && !((done >> slot) & 1u);
+					um = __ballot_sync(FULL, unc);
+				}
 			}
-			if (unc)
-				sm.unc[nunc + __popc(um & lt_mask)] = up;
-			nunc += cnt;
+			if (unc) {
+				const int o = nunc + __popc(um & lt_mask);
+				sm.unc[o] = up;
+				sm.unc_slot[o] = (uint8_t)slot;
+			}
+			nunc += __popc(um);
 		}
+		push = push && !((done >> slot) & 1u);
 		const unsigned pm = __ballot_sync(FULL, push);
 		if (push) {
-			const int o = top + 2 * __popc(pm & lt_mask);
-			sm.stack[o] = c0;
-			sm.stack[o + 1] = c1;
+			// lane 0's children end on top
+			const int o = top + 2 * __popc(pm & gt_mask);
+			sm.stack[o] = c1;
+			sm.stack[o + 1] = c0;
 		}
 		top += 2 * __popc(pm);
 		__syncwarp();
 	}
 	__syncwarp();
-	if (!hit && nunc > 0)
-		hit = flush_unc<CAP>(sm, nunc, lane, query, step, ctr, rq, W, src, st);
+	if (nunc > 0 && done != FULL) {
+		const uint32_t ih = flush_unc<CAP>(sm, nunc, done, lane, ctr, rq, W, src, st);
+		hit |= ih;
+		done |= ih;
+	}
+	__syncwarp();
+	return hit;
+}
+
+// Stack entry of a chunk traversal: (env node, robot node | s0 << 22 | s1 << 27),
+// the consecutive steps s0..s1 of one segment sharing the node pair.
+constexpr int S0_SHIFT = 22, S1_SHIFT = 27;
+constexpr uint32_t RNODE_MASK = (1u << S0_SHIFT) - 1u;
+
+__device__ __forceinline__ uint32_t range_bits(int s0, int s1)
+{
+	return ((uint32_t)s0 << S0_SHIFT) | ((uint32_t)s1 << S1_SHIFT);
+}
+
+// Traversal of the steps 0..nopen-1 of one segment chunk (slots = steps in
+// order; sm.qf, sm.slot_query, sm.slot_step describe them).  A node pair is
+// tested once for a whole range of steps: with the transform of the middle
+// step and the slack widened by the range's motion bound (`motion` per step),
+// so a pair separated from the swept robot node is pruned for every step of
+// the range at once.  Ranges split in halves where the motion is comparable to
+// the node size, and always before leaf tests, which are per step.  Returns the
+// lowest step in contact as a one-bit mask (0 when none).
+template <uint64_t CAP>
+__device__ uint32_t traverse_chunk(const WorldDev &W, WarpSmem &sm, int lane, int nopen, float motion, int soft_cap,
+                                   QueryCounters *ctr, RetestEntry *rq, const StateSrc &src, LaneStats &st)
+{
+	const uint32_t ebase = (uint32_t)W.env.leaf_base, rbase = (uint32_t)W.rob.leaf_base;
+	const unsigned lt_mask = (1u << lane) - 1u;
+	const unsigned gt_mask = ~(lt_mask | (1u << lane));
+	if (lane == 0)
+		sm.stack[0] = make_uint2(0u, range_bits(0, nopen - 1));
+	__syncwarp();
+	int top = 1, nunc = 0;
+	uint32_t done = nopen >= 32 ? 0u : ~((1u << nopen) - 1u), hit = 0u;
+	while (top > 0 && done != FULL) {
+		int p = min(top, 32);
+		const int room = soft_cap - top;
+		if (room < p)
+			p = max(1, room);
+		bool active = lane < p;
+		uint2 pr = make_uint2(0u, 0u);
+		if (active)
+			pr = sm.stack[top - 1 - lane];
+		__syncwarp();
+		top -= p;
+		const int s0 = (int)((pr.y >> S0_SHIFT) & 31u);
+		int s1 = (int)(pr.y >> S1_SHIFT);
+		const uint32_t rn = pr.y & RNODE_MASK;
+		if (active) {
+			// steps from the lowest contact upwards are settled
+			const uint32_t above = done >> s0;
+			if (above & 1u)
+				active = false;
+			else if (above)
+				s1 = min(s1, s0 + __ffs(above) - 2);
+		}
+		bool push = false, lhit = false, unc = false;
+		uint2 c0 = make_uint2(0u, 0u), c1 = make_uint2(0u, 0u), up = make_uint2(0u, 0u);
+		if (active) {
+			const float4 A0 = __ldg(W.env.nodeA + pr.x), A1 = __ldg(W.env.nodeB + pr.x);
+			const float4 B0 = __ldg(W.rob.nodeA + rn), B1 = __ldg(W.rob.nodeB + rn);
+			const int sm_ = (s0 + s1) >> 1;
+			const QFs &Q = sm.qf[sm_];
+			const float4 Q0 = Q.q[0], Q1 = Q.q[1], Q2 = Q.q[2];
+			float4 Q3 = Q.q[3];
+			float infl = 0.f;
+			if (s1 > s0) {
+				infl = (float)max(sm_ - s0, s1 - sm_) * motion + 1e-9f * (1.f + Q3.w);
+				Q3.y += infl;
+			}
+			st.node++;
+			if (!(sat_sep32(A0, A1, B0, B1, Q0, Q1, Q2, Q3) > 0.f)) {
+				const bool la = pr.x >= ebase, lb = rn >= rbase;
+				const float ext = fmaxf(fmaxf(fmaxf(A1.x, A1.y), A1.z), fmaxf(fmaxf(B1.x, B1.y), B1.z));
+				if (s1 > s0 && ((la && lb) || infl > 0.5f * ext)) {
+					// split the step range; the lower half ends on top
+					c0 = make_uint2(pr.x, rn | range_bits(s0, sm_));
+					c1 = make_uint2(pr.x, rn | range_bits(sm_ + 1, s1));
+					push = true;
+				} else if (la && lb) {
+					st.leaf++;
+					const int es = (int)(pr.x - ebase), rs = (int)(rn - rbase);
+					const float4 ta = __ldg(W.env.triA + es), tb = __ldg(W.env.triB + es),
+					             tc = __ldg(W.env.triC + es);
+					const float4 ra = __ldg(W.rob.triA + rs), rb = __ldg(W.rob.triB + rs),
+					             rc = __ldg(W.rob.triC + rs);
+					float gap;
+					const int r = tri_filter(f3(ta), f3(tb), f3(tc), f3(ra), f3(rb), f3(rc), Q0, Q1, Q2, Q.q[3],
+					                         Q.q[4].x, &gap);
+					if (r == 1) {
+						lhit = true;
+					} else if (r == 2) {
+						unc = true;
+						up = make_uint2((uint32_t)__float_as_int(ta.w), (uint32_t)__float_as_int(ra.w));
+					}
+				} else {
+					const uint32_t rb_ = range_bits(s0, s1);
+					const bool da = !la && (lb || (A1.x + A1.y + A1.z) >= (B1.x + B1.y + B1.z));
+					if (da) {
+						c0 = make_uint2((uint32_t)__float_as_int(A0.w), rn | rb_);
+						c1 = make_uint2((uint32_t)__float_as_int(A1.w), rn | rb_);
+					} else {
+						c0 = make_uint2(pr.x, (uint32_t)__float_as_int(B0.w) | rb_);
+						c1 = make_uint2(pr.x, (uint32_t)__float_as_int(B1.w) | rb_);
+					}
+					push = true;
+				}
+			}
+		}
+		const uint32_t hm = __reduce_or_sync(FULL, lhit ? (1u << s0) : 0u);
+		if (hm) {
+			const uint32_t low = hm & (~hm + 1u);
+			if (!hit || low < hit)
+				hit = low;
+			done |= ~(hit - 1u);
+			if (done == FULL)
+				break;
+		}
+		unc = unc && !((done >> s0) & 1u);
+		unsigned um = __ballot_sync(FULL, unc);
+		if (um) {
+			if (nunc + __popc(um) > UNC_CAP) {
+				const uint32_t ih = flush_unc<CAP>(sm, nunc, done, lane, ctr, rq, W, src, st);
+				nunc = 0;
+				__syncwarp();
+				if (ih) {
+					const uint32_t low = ih & (~ih + 1u);
+					if (!hit || low < hit)
+						hit = low;
+					done |= ~(hit - 1u);
+					if (done == FULL)
+						break;
+					unc = unc && !((done >> s0) & 1u);
+					um = __ballot_sync(FULL, unc);
+				}
+			}
+			if (unc) {
+				const int o = nunc + __popc(um & lt_mask);
+				sm.unc[o] = up;
+				sm.unc_slot[o] = (uint8_t)s0;
+			}
+			nunc += __popc(um);
+		}
+		push = push && !((done >> s0) & 1u);
+		const unsigned pm = __ballot_sync(FULL, push);
+		if (push) {
+			const int o = top + 2 * __popc(pm & gt_mask);
+			sm.stack[o] = c1;
+			sm.stack[o + 1] = c0;
+		}
+		top += 2 * __popc(pm);
+		__syncwarp();
+	}
+	__syncwarp();
+	if (nunc > 0 && done != FULL) {
+		const uint32_t ih = flush_unc<CAP>(sm, nunc, done, lane, ctr, rq, W, src, st);
+		if (ih) {
+			const uint32_t low = ih & (~ih + 1u);
+			if (!hit || low < hit)
+				hit = low;
+		}
+	}
 	__syncwarp();
 	return hit;
 }
@@ -474,7 +469,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_states(WorldDev W, const double 
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	WarpSmem &sm = reinterpret_cast<WarpSmem *>(smem_raw)[warp];
-	StateSrc src{ states, nullptr, nullptr, nullptr, nullptr };
+	const StateSrc src{ states, nullptr, nullptr, nullptr, nullptr };
 	LaneStats st;
 	unsigned long long queries = 0, items = 0;
 	for (;;) {
@@ -490,14 +485,14 @@ __global__ void __launch_bounds__(WARPS * 32) k_states(WorldDev W, const double 
 			for (int i = 0; i < 7; i++)
 				q[i] = states[7 * (base + lane) + i];
 			make_qf(q, W, sm.qf[lane]);
+			sm.slot_query[lane] = (uint32_t)(base + lane);
+			sm.slot_step[lane] = 0u;
 		}
 		__syncwarp();
-		for (int j = 0; j < cnt; j++) {
-			const QF f = sm.qf[j];
-			const bool hit = traverse<CAP>(W, f, sm, lane, soft_cap, (uint32_t)(base + j), 0u, ctr, rq, src, st);
-			if (lane == 0)
-				out[base + j] = hit ? 0 : 1;
-		}
+		const uint32_t open = cnt == 32 ? FULL : ((1u << cnt) - 1u);
+		const uint32_t hit = traverse_batch<CAP>(W, sm, lane, open, soft_cap, ctr, rq, src, st);
+		if (lane < cnt)
+			out[base + lane] = ((hit >> lane) & 1u) ? 0 : 1;
 		queries += cnt;
 		items++;
 		__syncwarp();
@@ -574,7 +569,7 @@ __global__ void k_seg_bound(const double *from, const double *to, int64_t n, dou
 // Per-segment constants, exact step count and delta checkpoints every 32 steps.
 __global__ void k_seg_setup(const double *from, const double *to, int64_t n, double vdelta, int mode,
                             const int64_t *slots, const int64_t *slot_base, SegParams *params, double *ckpt,
-                            int32_t *first, uint32_t *keys, uint32_t *vals, QueryCounters *ctr)
+                            int32_t *first, uint32_t *keys, uint32_t *vals, QueryCounters *ctr, double rob_r2)
 {
 	const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
 	if (s >= n)
@@ -596,6 +591,15 @@ __global__ void k_seg_setup(const double *from, const double *to, int64_t n, dou
 	P.dist = dist;
 	P.inv_dist = pwm::dvd(1.0, dist);
 	P.step = step;
+	{
+		// motion of any robot point per unit tau: |p1 - p0| + (rotation angle 2 theta) * r2;
+		// the linear slerp branch turns by less than 1e-7 rad over the whole segment
+		const double dx = b[0] - a[0], dy = b[1] - a[1], dz = b[2] - a[2];
+		const double lin = sqrt(dx * dx + dy * dy + dz * dz);
+		const double ang = S.linear ? 1e-7 : 2.0 * S.theta;
+		const double motion = (lin * (1.0 + 1e-12) + ang * rob_r2 * (1.0 + 1e-12)) * (1.0 + 1e-6) + 1e-15;
+		P.skip_scale = step * P.inv_dist * (1.0 + 1e-6) * motion + 1e-300;
+	}
 	P.ckpt_base = slot_base[s];
 	int32_t code = INT_MAX;
 	int64_t K = 0;
@@ -671,6 +675,10 @@ __global__ void __launch_bounds__(1024) k_rounds(const uint32_t *sorted_keys, in
 	}
 }
 
+// Work item = (segment, 32-step chunk) in chunk-major order, so that early
+// contacts prune later chunks.  A warp computes the chunk's FP64 states lane-
+// parallel, then answers its steps with one swept traversal and records the
+// first step in contact with atomicMin.
 __global__ void __launch_bounds__(WARPS * 32) k_segments(WorldDev W, StateSrc src, const uint32_t *order,
                                                          const int64_t *round_off, int64_t nrounds, int32_t *first,
                                                          QueryCounters *ctr, RetestEntry *rq, int soft_cap)
@@ -688,10 +696,9 @@ __global__ void __launch_bounds__(WARPS * 32) k_segments(WorldDev W, StateSrc sr
 		item = __shfl_sync(FULL, item, 0);
 		if (item >= total)
 			break;
-		// round j: largest j with round_off[j] <= item (lane 0 searches, then broadcast)
 		int64_t j = 0;
 		if (lane == 0) {
-			// round_off[0] = 0 <= item < total = round_off[R]; round_off is non-decreasing
+			// round_off[0] = 0 <= item < total = round_off[nrounds]; round_off is non-decreasing
 			int64_t lo = 0, hi = nrounds;
 			while (hi - lo > 1) {
 				const int64_t mid = (lo + hi) >> 1;
@@ -727,24 +734,17 @@ __global__ void __launch_bounds__(WARPS * 32) k_segments(WorldDev W, StateSrc sr
 			double q[7];
 			pwm::interpolate_p(src.from + 7 * (size_t)s, src.to + 7 * (size_t)s, S, tau, q);
 			make_qf(q, W, sm.qf[lane]);
+			sm.slot_query[lane] = s;
+			sm.slot_step[lane] = (uint32_t)(k0 + lane);
 		}
 		__syncwarp();
-		for (int kk = 0; kk < cnt; kk++) {
-			const int32_t k = k0 + kk;
-			if (lane == 0)
-				cur = *(volatile int32_t *)&first[s];
-			cur = __shfl_sync(FULL, cur, 0);
-			if (cur <= k)
-				break;
-			const QF f = sm.qf[kk];
-			queries++;
-			const bool hit = traverse<RETEST_CAP>(W, f, sm, lane, soft_cap, s, (uint32_t)k, ctr, rq, src, st);
-			if (hit) {
-				if (lane == 0)
-					atomicMin(&first[s], k);
-				break;
-			}
-		}
+		// steps at or after the segment's current first contact are not needed
+		const int lim = (int)min((int64_t)cnt, (int64_t)cur - k0);
+		queries += lim;
+		const float motion = __double2float_ru(P.skip_scale);
+		const uint32_t hit = traverse_chunk<RETEST_CAP>(W, sm, lane, lim, motion, soft_cap, ctr, rq, src, st);
+		if (hit && lane == 0)
+			atomicMin(&first[s], k0 + (__ffs(hit) - 1));
 		__syncwarp();
 	}
 	flush_stats(ctr, st, queries, items, lane);
@@ -778,17 +778,24 @@ __global__ void k_seg_finalize(int32_t *first, const SegParams *params, int64_t 
 
 constexpr int ISECT_CAP = 1 << 20;
 
-// One warp enumerates every leaf pair that is not certified separate.
-__global__ void k_isect_collect(WorldDev W, QF f, uint2 *cand, unsigned int *ncand, int soft_cap)
+// One warp enumerates every leaf pair of state q that is not certified separate.
+__global__ void k_isect_collect(WorldDev W, const double *q, uint2 *cand, unsigned int *ncand, int soft_cap)
 {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	const int lane = threadIdx.x & 31;
 	WarpSmem &sm = reinterpret_cast<WarpSmem *>(smem_raw)[0];
 	const uint32_t ebase = (uint32_t)W.env.leaf_base, rbase = (uint32_t)W.rob.leaf_base;
-	const unsigned lt_mask = (1u << lane) - 1u;
-	if (lane == 0)
+	const unsigned gt_mask = ~(((1u << lane) - 1u) | (1u << lane));
+	if (lane == 0) {
+		double s[7];
+		for (int i = 0; i < 7; i++)
+			s[i] = q[i];
+		make_qf(s, W, sm.qf[0]);
 		sm.stack[0] = make_uint2(0u, 0u);
+	}
 	__syncwarp();
+	const float4 Q0 = sm.qf[0].q[0], Q1 = sm.qf[0].q[1], Q2 = sm.qf[0].q[2], Q3 = sm.qf[0].q[3];
+	const float eg = sm.qf[0].q[4].x;
 	int top = 1;
 	while (top > 0) {
 		int p = min(top, 32);
@@ -798,7 +805,7 @@ __global__ void k_isect_collect(WorldDev W, QF f, uint2 *cand, unsigned int *nca
 		const bool active = lane < p;
 		uint2 pr = make_uint2(0u, 0u);
 		if (active)
-			pr = sm.stack[top - p + lane];
+			pr = sm.stack[top - 1 - lane];
 		__syncwarp();
 		top -= p;
 		bool push = false;
@@ -806,15 +813,20 @@ __global__ void k_isect_collect(WorldDev W, QF f, uint2 *cand, unsigned int *nca
 		if (active) {
 			const float4 A0 = __ldg(W.env.nodeA + pr.x), A1 = __ldg(W.env.nodeB + pr.x);
 			const float4 B0 = __ldg(W.rob.nodeA + pr.y), B1 = __ldg(W.rob.nodeB + pr.y);
-			if (!sat_disjoint32(A0, A1, B0, B1, f)) {
+			if (!sat_disjoint32(A0, A1, B0, B1, Q0, Q1, Q2, Q3)) {
 				const bool la = pr.x >= ebase, lb = pr.y >= rbase;
 				if (la && lb) {
-					uint32_t et, rt;
-					const int r = leaf_test(W, f, (int)(pr.x - ebase), (int)(pr.y - rbase), &et, &rt);
+					const int es = (int)(pr.x - ebase), rs = (int)(pr.y - rbase);
+					const float4 ta = __ldg(W.env.triA + es), tb = __ldg(W.env.triB + es),
+					             tc = __ldg(W.env.triC + es);
+					const float4 ra = __ldg(W.rob.triA + rs), rb = __ldg(W.rob.triB + rs),
+					             rc = __ldg(W.rob.triC + rs);
+					float gap;
+					const int r = tri_filter(f3(ta), f3(tb), f3(tc), f3(ra), f3(rb), f3(rc), Q0, Q1, Q2, Q3, eg, &gap);
 					if (r != 0) {
 						const unsigned idx = atomicAdd(ncand, 1u);
 						if (idx < ISECT_CAP)
-							cand[idx] = make_uint2(et, rt);
+							cand[idx] = make_uint2((uint32_t)__float_as_int(ta.w), (uint32_t)__float_as_int(ra.w));
 					}
 				} else {
 					const bool da = !la && (lb || (A1.x + A1.y + A1.z) >= (B1.x + B1.y + B1.z));
@@ -831,9 +843,9 @@ __global__ void k_isect_collect(WorldDev W, QF f, uint2 *cand, unsigned int *nca
 		}
 		const unsigned pm = __ballot_sync(FULL, push);
 		if (push) {
-			const int o = top + 2 * __popc(pm & lt_mask);
-			sm.stack[o] = c0;
-			sm.stack[o + 1] = c1;
+			const int o = top + 2 * __popc(pm & gt_mask);
+			sm.stack[o] = c1;
+			sm.stack[o + 1] = c0;
 		}
 		top += 2 * __popc(pm);
 		__syncwarp();
@@ -883,7 +895,7 @@ size_t warp_smem_bytes() { return sizeof(WarpSmem); }
 
 int soft_cap_of(const pw_world *w)
 {
-	const int slack = w->dev.env.depth + w->dev.rob.depth + 8;
+	const int slack = w->dev.env.depth + w->dev.rob.depth + 5 + 8;   // 5: step-range splits
 	return STACK_CAP - slack;
 }
 
@@ -895,6 +907,8 @@ int check_ready(pw_world *w, const char *who)
 		return pw_fail(PW_ERR_NO_MODEL, std::string(who) + ": call load_env/load_robot, scale_to_unit and angle_model first");
 	if (soft_cap_of(w) < 64)
 		return pw_fail(PW_ERR_INTERNAL, std::string(who) + ": BVH too deep for the traversal stack");
+	if (2 * (int64_t)w->dev.rob.ntri - 1 > (int64_t)NODE_MASK)
+		return pw_fail(PW_ERR_INVALID_ARG, std::string(who) + ": robot mesh above 2^26 triangles");
 	return PW_OK;
 }
 
@@ -1021,6 +1035,8 @@ extern "C" int pw_segments_first_contact(pw_world *w, const double *from, const 
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_segments_first_contact: bad pointers or size");
 	if (mode != PW_SEG_TRANSIT && mode != PW_SEG_TRANSITION)
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_segments_first_contact: unknown mode");
+	if (2 * (int64_t)w->dev.rob.ntri - 1 > (int64_t)RNODE_MASK)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_segments_first_contact: robot mesh above 2^21 triangles");
 	if (!(verify_delta > 0.0) || !(verify_delta < INFINITY))
 		return pw_fail(PW_ERR_INVALID_ARG,
 		               "pw_segments_first_contact: verify_delta must be finite and > 0 (the reference loop never ends otherwise)");
@@ -1068,19 +1084,14 @@ extern "C" int pw_segments_first_contact(pw_world *w, const double *from, const 
 	uint32_t *keys = (uint32_t *)w->seg_keys.ptr, *vals = (uint32_t *)w->seg_order.ptr;
 	uint32_t *keys2 = (uint32_t *)w->seg_keys2.ptr, *vals2 = (uint32_t *)w->seg_order2.ptr;
 	k_seg_setup<<<G, B, 0, st>>>(from, to, n, verify_delta, mode, slots, slot_base, params, ckpt, first_step, keys,
-	                             vals, ctr);
+	                             vals, ctr, w->dev.rob.r2);
 	PW_CUDA(cudaGetLastError());
 	PW_CUDA(cub::DeviceRadixSort::SortPairsDescending(w->cub_tmp.ptr, t2, keys, keys2, vals, vals2, (int)n, 0, 32, st));
-	// rounds: at most max(slots) + 1 offsets
-	int64_t max_rounds = 0;
-	{
-		// bound the round count by the largest slot bound (copy of the sorted maximum needs the sort;
-		// use the slot total as a safe bound when it is small, else read the maximum back)
-		uint32_t mx = 0;
-		PW_CUDA(cudaMemcpyAsync(&mx, keys2, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-		PW_CUDA(cudaStreamSynchronize(st));
-		max_rounds = mx;
-	}
+	// rounds: as many as the longest segment has chunks
+	uint32_t max_chunks = 0;
+	PW_CUDA(cudaMemcpyAsync(&max_chunks, keys2, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+	PW_CUDA(cudaStreamSynchronize(st));
+	const int64_t max_rounds = max_chunks;
 	if ((rc = grow<int64_t>(w->round_off, (size_t)max_rounds + 2)))
 		return rc;
 	int64_t *round_off = (int64_t *)w->round_off.ptr;
@@ -1127,38 +1138,12 @@ extern "C" int pw_intersecting_segments(pw_world *w, const double q[7], int64_t 
 	PW_CUDA(drows.reserve(sizeof(IsectRow) * ISECT_CAP));
 	PW_CUDA(cudaMemcpy(dq.ptr, q, sizeof(double) * 7, cudaMemcpyHostToDevice));
 	PW_CUDA(cudaMemset(dn.ptr, 0, sizeof(unsigned int) * 2));
-	QF f;
-	{
-		// the same FP32 set-up the kernels use, evaluated on the host
-		const float x = (float)q[4], y = (float)q[5], z = (float)q[6], ww = (float)q[3];
-		const float tx = 2.f * x, ty = 2.f * y, tz = 2.f * z;
-		const float twx = tx * ww, twy = ty * ww, twz = tz * ww;
-		const float txx = tx * x, txy = ty * x, txz = tz * x;
-		const float tyy = ty * y, tyz = tz * y, tzz = tz * z;
-		const float R[9] = { 1.f - (tyy + tzz), txy - twz, txz + twy, txy + twz, 1.f - (txx + tzz), tyz - twx,
-		                     txz - twy, tyz + twx, 1.f - (txx + tyy) };
-		for (int i = 0; i < 9; i++) f.R[i] = R[i];
-		f.t[0] = (float)q[0]; f.t[1] = (float)q[1]; f.t[2] = (float)q[2];
-		const float s = x * x + y * y + z * z + ww * ww;
-		const float dev = fabsf(1.f - s) + 8.f * U32 * s;
-		const float epsR = 16.f * U32 * (1.f + s);
-		const float r1 = w->dev.rob.r1;
-		const float tinf = std::max(std::max(fabsf(f.t[0]), fabsf(f.t[1])), fabsf(f.t[2]));
-		const float del_r = epsR * r1 + 8.f * U32 * ((1.f + 2.f * s) * r1 + tinf) + 1e-30f;
-		const float Wm = tinf + r1 + w->dev.env.emax;
-		const float er = epsR + 2.f * dev;
-		for (int i = 0; i < 9; i++) f.AR[i] = fabsf(f.R[i]) + er;
-		f.W = Wm;
-		// a wider slack on the host side costs nothing here and covers host/device rounding differences
-		f.margin = 2.f * (del_r + er * (3.f * r1 + 4.f * Wm) + 128.f * U32 * Wm);
-		f.del = 4.f * std::max(del_r, w->dev.del_env);
-	}
 	const size_t smem = warp_smem_bytes();
 	rc = set_smem_attr((const void *)k_isect_collect, smem);
 	if (rc)
 		return rc;
 	unsigned int *ncand = (unsigned int *)dn.ptr;
-	k_isect_collect<<<1, 32, smem>>>(w->dev, f, (uint2 *)dcand.ptr, ncand, soft_cap_of(w));
+	k_isect_collect<<<1, 32, smem>>>(w->dev, (const double *)dq.ptr, (uint2 *)dcand.ptr, ncand, soft_cap_of(w));
 	k_isect_eval<<<w->num_sms, 256>>>(w->dev, (const double *)dq.ptr, (const uint2 *)dcand.ptr, ncand,
 	                                  (IsectRow *)drows.ptr, ncand + 1);
 	PW_CUDA(cudaGetLastError());

@@ -585,10 +585,13 @@ __global__ void k_tri_prep(const double *V, const int32_t *F, int n, float4 *ta,
 	for (int k = 0; k < 3; k++)
 		for (int c = 0; c < 3; c++)
 			p[k][c] = V[3 * F[3 * t + k] + c];
+	// vertex 0 and the two edges from it, each rounded once from FP64
 	ta[t] = make_float4(__double2float_rn(p[0][0]), __double2float_rn(p[0][1]), __double2float_rn(p[0][2]),
 	                    __int_as_float(t));
-	tb[t] = make_float4(__double2float_rn(p[1][0]), __double2float_rn(p[1][1]), __double2float_rn(p[1][2]), 0.f);
-	tc[t] = make_float4(__double2float_rn(p[2][0]), __double2float_rn(p[2][1]), __double2float_rn(p[2][2]), 0.f);
+	tb[t] = make_float4(__double2float_rn(__dsub_rn(p[1][0], p[0][0])), __double2float_rn(__dsub_rn(p[1][1], p[0][1])),
+	                    __double2float_rn(__dsub_rn(p[1][2], p[0][2])), 0.f);
+	tc[t] = make_float4(__double2float_rn(__dsub_rn(p[2][0], p[0][0])), __double2float_rn(__dsub_rn(p[2][1], p[0][1])),
+	                    __double2float_rn(__dsub_rn(p[2][2], p[0][2])), 0.f);
 	for (int c = 0; c < 3; c++) {
 		const double mn = fmin(fmin(p[0][c], p[1][c]), p[2][c]);
 		const double mx = fmax(fmax(p[0][c], p[1][c]), p[2][c]);
@@ -797,10 +800,13 @@ int pw_build_mesh_device(pw_world *w, MeshDev &m, const std::vector<double> &V64
 	m.nvert = nv;
 	m.leaf_base = n > 0 ? n - 1 : 0;
 	// host-side magnitudes
-	double emax = 0.0;
+	double emax = 0.0, r2 = 0.0;
 	for (double x : V64)
 		emax = std::max(emax, std::fabs(x));
+	for (size_t i = 0; i + 2 < V64.size(); i += 3)
+		r2 = std::max(r2, std::sqrt(V64[i] * V64[i] + V64[i + 1] * V64[i + 1] + V64[i + 2] * V64[i + 2]));
 	m.emax = (float)emax * 1.0001f + 1e-30f;
+	m.r2 = r2 * (1.0 + 1e-12) + 1e-300;
 	PW_CUDA(walloc(w, &m.V64, V64.size()));
 	PW_CUDA(walloc(w, &m.F, F.size()));
 	PW_CUDA(cudaMemcpy(m.V64, V64.data(), sizeof(double) * V64.size(), cudaMemcpyHostToDevice));
