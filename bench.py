@@ -296,6 +296,7 @@ def run_ours(args):
                        "leaf_tests": last["leaf_tests"], "fp64_retests": last["retests"],
                        "fp64_retest_rate_per_leaf": last["retests"] / max(1, last["leaf_tests"]),
                        "inline_retests": last["inline_retests"], "retest_ms": last["retest_ms"],
+                       "detailed_chunk_fraction": last["detailed_chunks"] / max(1, last["work_items"]),
                        "segments_per_s": args.n * ws / (tot_ms / args.steps / 1e3),
                        "free_fraction": float((fc == -1).mean()), "step_ms": step_ms}}
     print(json.dumps(line))

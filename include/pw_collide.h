@@ -71,6 +71,7 @@ typedef struct pw_query_stats {
 	int64_t inline_retests;      /* FP64 re-tests done in the traversal kernel (queue full) */
 	int64_t work_items;          /* work items the persistent kernel executed */
 	int64_t reference_checks;    /* isValid calls the sequential reference loop makes for the same batch */
+	int64_t detailed_chunks;     /* 32-step segment chunks that needed a transform per step */
 	double traverse_ms;          /* device time of the traversal kernel (CUDA events on the query stream) */
 	double retest_ms;            /* device time of the FP64 re-test kernel */
 } pw_query_stats;

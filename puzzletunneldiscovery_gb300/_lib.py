@@ -60,7 +60,8 @@ class QueryStats(ctypes.Structure):
     _fields_ = [("queries", ctypes.c_int64), ("node_tests", ctypes.c_int64), ("leaf_tests", ctypes.c_int64),
                 ("retests", ctypes.c_int64), ("retest_hits", ctypes.c_int64),
                 ("inline_retests", ctypes.c_int64), ("work_items", ctypes.c_int64),
-                ("reference_checks", ctypes.c_int64), ("traverse_ms", ctypes.c_double),
+                ("reference_checks", ctypes.c_int64), ("detailed_chunks", ctypes.c_int64),
+                ("traverse_ms", ctypes.c_double),
                 ("retest_ms", ctypes.c_double)]
 
     def as_dict(self):

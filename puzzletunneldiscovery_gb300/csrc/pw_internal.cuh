@@ -38,7 +38,7 @@ struct WorldDev {
 struct QueryCounters {
 	unsigned long long work;        // next work item of the persistent kernels
 	unsigned long long retest_count;
-	unsigned long long stat[8];     // see STAT_* below
+	unsigned long long stat[10];    // see STAT_* below
 	unsigned long long ref_checks;  // isValid calls of the sequential reference loop
 	unsigned int error;             // device-side consistency failure (PW_ERR_INTERNAL)
 	unsigned int pad;
@@ -52,6 +52,7 @@ enum {
 	STAT_INLINE = 5,
 	STAT_ITEMS = 6,
 	STAT_TOTAL_ITEMS = 7,
+	STAT_DETAILED = 8,   // segment chunks that needed per-step transforms
 };
 
 // A triangle pair whose FP32 verdict fell inside the error band.
@@ -100,7 +101,7 @@ struct pw_world {
 	DeviceBuffer counters;     // QueryCounters
 	DeviceBuffer retest;       // RetestEntry[retest_cap]
 	uint64_t retest_cap = 0;
-	DeviceBuffer seg_params, seg_ckpt, seg_keys, seg_order, seg_keys2, seg_order2, round_off, cub_tmp, misc;
+	DeviceBuffer seg_params, seg_ckpt, seg_anchor, seg_keys, seg_order, seg_keys2, seg_order2, round_off, cub_tmp, misc;
 	cudaStream_t last_stream = nullptr;
 	cudaEvent_t ev[4] = { nullptr, nullptr, nullptr, nullptr }; // traversal start/end, re-test start/end
 	bool timed = false;

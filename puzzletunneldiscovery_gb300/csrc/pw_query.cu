@@ -56,6 +56,7 @@ struct StateSrc {
 	const double *from, *to;   // segments kernel
 	const SegParams *seg;
 	const double *ckpt;
+	const QFs *anchors;        // per chunk: FP32 transform of the anchor step
 };
 
 __device__ __forceinline__ void make_qf(const double *q, const WorldDev &W, QFs &o)
@@ -289,17 +290,41 @@ __device__ __forceinline__ uint32_t range_bits(int s0, int s1)
 	return ((uint32_t)s0 << S0_SHIFT) | ((uint32_t)s1 << S1_SHIFT);
 }
 
-// Traversal of the steps 0..nopen-1 of one segment chunk (slots = steps in
-// order; sm.qf, sm.slot_query, sm.slot_step describe them).  A node pair is
-// tested once for a whole range of steps: with the transform of the middle
-// step and the slack widened by the range's motion bound (`motion` per step),
-// so a pair separated from the swept robot node is pruned for every step of
-// the range at once.  Ranges split in halves where the motion is comparable to
-// the node size, and always before leaf tests, which are per step.  Returns the
-// lowest step in contact as a one-bit mask (0 when none).
+// FP64 state of step k0 + lane of segment s (delta walked from the chunk's
+// checkpoint) reduced to the slot's FP32 transform and bounds.
+__device__ __noinline__ void chunk_step_qf(const WorldDev &W, const StateSrc &src, uint32_t s, int64_t ckslot,
+                                           int lane, QFs &o)
+{
+	const SegParams &P = src.seg[s];
+	double delta = src.ckpt[ckslot];
+	for (int t = 0; t < lane; t++)
+		delta = pwm::advance_delta(delta, P.dist, P.step);
+	const double tau = pwm::mul(delta, P.inv_dist);
+	pwm::SlerpParams S;
+	seg_slerp(P, S);
+	double q[7];
+	pwm::interpolate_p(src.from + 7 * (size_t)s, src.to + 7 * (size_t)s, S, tau, q);
+	make_qf(q, W, o);
+}
+
+// Traversal of the steps 0..nopen-1 of one segment chunk of cnt steps (slots =
+// steps in order; sm.slot_query / sm.slot_step describe them).  A node pair is
+// tested once for a whole range of steps, with one step's transform and the
+// slack widened by the motion bound (`motion` per step) to the farthest step of
+// the range, so a pair separated from the swept robot node is pruned for the
+// whole range at once.
+//   Phase A uses only the anchor step's transform (sm.qf[anchor], exact, from
+//   the set-up kernel) and never splits a range.  The first pair that needs a
+//   finer look (a leaf pair, or motion comparable to the node size) switches
+//   the warp to phase B: the FP64 state of every step is computed lane-parallel
+//   and ranges split in halves around their middle step down to single steps,
+//   which take the per-step leaf tests.
+// Returns the lowest step in contact as a one-bit mask (0 when none).
 template <uint64_t CAP>
-__device__ uint32_t traverse_chunk(const WorldDev &W, WarpSmem &sm, int lane, int nopen, float motion, int soft_cap,
-                                   QueryCounters *ctr, RetestEntry *rq, const StateSrc &src, LaneStats &st)
+__device__ uint32_t traverse_chunk(const WorldDev &W, WarpSmem &sm, int lane, int nopen, int cnt, int anchor,
+                                   float motion, int soft_cap, QueryCounters *ctr, RetestEntry *rq,
+                                   const StateSrc &src, LaneStats &st, uint32_t seg, int64_t ckslot,
+                                   unsigned long long &ndetailed)
 {
 	const uint32_t ebase = (uint32_t)W.env.leaf_base, rbase = (uint32_t)W.rob.leaf_base;
 	const unsigned lt_mask = (1u << lane) - 1u;
@@ -308,6 +333,7 @@ __device__ uint32_t traverse_chunk(const WorldDev &W, WarpSmem &sm, int lane, in
 		sm.stack[0] = make_uint2(0u, range_bits(0, nopen - 1));
 	__syncwarp();
 	int top = 1, nunc = 0;
+	bool detailed = false;
 	uint32_t done = nopen >= 32 ? 0u : ~((1u << nopen) - 1u), hit = 0u;
 	while (top > 0 && done != FULL) {
 		int p = min(top, 32);
@@ -331,29 +357,36 @@ __device__ uint32_t traverse_chunk(const WorldDev &W, WarpSmem &sm, int lane, in
 			else if (above)
 				s1 = min(s1, s0 + __ffs(above) - 2);
 		}
-		bool push = false, lhit = false, unc = false;
+		bool push2 = false, push1 = false, lhit = false, unc = false, need = false;
 		uint2 c0 = make_uint2(0u, 0u), c1 = make_uint2(0u, 0u), up = make_uint2(0u, 0u);
 		if (active) {
 			const float4 A0 = __ldg(W.env.nodeA + pr.x), A1 = __ldg(W.env.nodeB + pr.x);
 			const float4 B0 = __ldg(W.rob.nodeA + rn), B1 = __ldg(W.rob.nodeB + rn);
-			const int sm_ = (s0 + s1) >> 1;
-			const QFs &Q = sm.qf[sm_];
+			const int ref = detailed ? (s0 + s1) >> 1 : anchor;
+			const int reach = max(abs(s0 - ref), abs(s1 - ref));
+			const QFs &Q = sm.qf[ref];
 			const float4 Q0 = Q.q[0], Q1 = Q.q[1], Q2 = Q.q[2];
 			float4 Q3 = Q.q[3];
 			float infl = 0.f;
-			if (s1 > s0) {
-				infl = (float)max(sm_ - s0, s1 - sm_) * motion + 1e-9f * (1.f + Q3.w);
+			if (reach > 0) {
+				infl = (float)reach * motion + 1e-9f * (1.f + Q3.w);
 				Q3.y += infl;
 			}
 			st.node++;
 			if (!(sat_sep32(A0, A1, B0, B1, Q0, Q1, Q2, Q3) > 0.f)) {
 				const bool la = pr.x >= ebase, lb = rn >= rbase;
 				const float ext = fmaxf(fmaxf(fmaxf(A1.x, A1.y), A1.z), fmaxf(fmaxf(B1.x, B1.y), B1.z));
-				if (s1 > s0 && ((la && lb) || infl > 0.5f * ext)) {
+				const bool fine = (la && lb) || infl > 0.5f * ext;
+				if (!detailed && fine) {
+					// hand the pair back for phase B
+					need = true;
+					push1 = true;
+					c0 = make_uint2(pr.x, rn | range_bits(s0, s1));
+				} else if (s1 > s0 && fine) {
 					// split the step range; the lower half ends on top
-					c0 = make_uint2(pr.x, rn | range_bits(s0, sm_));
-					c1 = make_uint2(pr.x, rn | range_bits(sm_ + 1, s1));
-					push = true;
+					c0 = make_uint2(pr.x, rn | range_bits(s0, ref));
+					c1 = make_uint2(pr.x, rn | range_bits(ref + 1, s1));
+					push2 = true;
 				} else if (la && lb) {
 					st.leaf++;
 					const int es = (int)(pr.x - ebase), rs = (int)(rn - rbase);
@@ -380,7 +413,7 @@ __device__ uint32_t traverse_chunk(const WorldDev &W, WarpSmem &sm, int lane, in
 						c0 = make_uint2(pr.x, (uint32_t)__float_as_int(B0.w) | rb_);
 						c1 = make_uint2(pr.x, (uint32_t)__float_as_int(B1.w) | rb_);
 					}
-					push = true;
+					push2 = true;
 				}
 			}
 		}
@@ -418,14 +451,25 @@ __device__ uint32_t traverse_chunk(const WorldDev &W, WarpSmem &sm, int lane, in
 			}
 			nunc += __popc(um);
 		}
-		push = push && !((done >> s0) & 1u);
-		const unsigned pm = __ballot_sync(FULL, push);
-		if (push) {
-			const int o = top + 2 * __popc(pm & gt_mask);
+		const bool settled = (done >> s0) & 1u;
+		push2 = push2 && !settled;
+		push1 = push1 && !settled;
+		const unsigned pm2 = __ballot_sync(FULL, push2), pm1 = __ballot_sync(FULL, push1);
+		// lane 0's entries end on top
+		const int o = top + 2 * __popc(pm2 & gt_mask) + __popc(pm1 & gt_mask);
+		if (push2) {
 			sm.stack[o] = c1;
 			sm.stack[o + 1] = c0;
+		} else if (push1) {
+			sm.stack[o] = c0;
 		}
-		top += 2 * __popc(pm);
+		top += 2 * __popc(pm2) + __popc(pm1);
+		if (!detailed && __any_sync(FULL, need)) {
+			if (lane < cnt)
+				chunk_step_qf(W, src, seg, ckslot, lane, sm.qf[lane]);
+			detailed = true;
+			ndetailed++;
+		}
 		__syncwarp();
 	}
 	__syncwarp();
@@ -469,7 +513,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_states(WorldDev W, const double 
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	WarpSmem &sm = reinterpret_cast<WarpSmem *>(smem_raw)[warp];
-	const StateSrc src{ states, nullptr, nullptr, nullptr, nullptr };
+	const StateSrc src{ states, nullptr, nullptr, nullptr, nullptr, nullptr };
 	LaneStats st;
 	unsigned long long queries = 0, items = 0;
 	for (;;) {
@@ -567,10 +611,26 @@ __global__ void k_seg_bound(const double *from, const double *to, int64_t n, dou
 }
 
 // Per-segment constants, exact step count and delta checkpoints every 32 steps.
-__global__ void k_seg_setup(const double *from, const double *to, int64_t n, double vdelta, int mode,
-                            const int64_t *slots, const int64_t *slot_base, SegParams *params, double *ckpt,
-                            int32_t *first, uint32_t *keys, uint32_t *vals, QueryCounters *ctr, double rob_r2)
+// Anchor step of a chunk of cnt steps: the middle step of a full chunk.
+__device__ __forceinline__ int anchor_of(int cnt) { return cnt >= 16 ? 15 : (cnt - 1) / 2; }
+
+// FP32 transform (QFs) of the step whose delta is given, from its FP64 state.
+__device__ __forceinline__ void seg_step_qf(const WorldDev &W, const double *a, const double *b, const SegParams &P,
+                                            double delta, QFs &o)
 {
+	const double tau = pwm::mul(delta, P.inv_dist);
+	pwm::SlerpParams S;
+	seg_slerp(P, S);
+	double q[7];
+	pwm::interpolate_p(a, b, S, tau, q);
+	make_qf(q, W, o);
+}
+
+__global__ void k_seg_setup(WorldDev W, const double *from, const double *to, int64_t n, double vdelta, int mode,
+                            const int64_t *slots, const int64_t *slot_base, SegParams *params, double *ckpt,
+                            QFs *anchors, int32_t *first, uint32_t *keys, uint32_t *vals, QueryCounters *ctr)
+{
+	const double rob_r2 = W.rob.r2;
 	const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
 	if (s >= n)
 		return;
@@ -621,8 +681,19 @@ __global__ void k_seg_setup(const double *from, const double *to, int64_t n, dou
 				}
 				ckpt[P.ckpt_base + (K >> 5)] = delta;
 			}
+			if ((K & 31) == 15)   // the chunk has at least 16 steps: its anchor is step 15
+				seg_step_qf(W, a, b, P, delta, anchors[P.ckpt_base + (K >> 5)]);
 			delta = pwm::advance_delta(delta, dist, step);
 			K++;
+		}
+		const int last = (int)(K & 31);
+		if (K > 0 && last > 0 && last < 16) {
+			// short last chunk: its anchor is its middle step
+			const int64_t c = (K - 1) >> 5;
+			double d = ckpt[P.ckpt_base + c];
+			for (int i = 0; i < anchor_of(last); i++)
+				d = pwm::advance_delta(d, dist, step);
+			seg_step_qf(W, a, b, P, d, anchors[P.ckpt_base + c]);
 		}
 	}
 	P.nsteps = (int32_t)K;
@@ -687,7 +758,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_segments(WorldDev W, StateSrc sr
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	WarpSmem &sm = reinterpret_cast<WarpSmem *>(smem_raw)[warp];
 	LaneStats st;
-	unsigned long long queries = 0, items = 0;
+	unsigned long long queries = 0, items = 0, detailed = 0;
 	const unsigned long long total = ctr->stat[STAT_TOTAL_ITEMS];
 	for (;;) {
 		unsigned long long item = 0;
@@ -724,29 +795,27 @@ __global__ void __launch_bounds__(WARPS * 32) k_segments(WorldDev W, StateSrc sr
 		cur = __shfl_sync(FULL, cur, 0);
 		if (cur <= k0)
 			continue;
+		const int anchor = anchor_of(cnt);
+		const int64_t ckslot = P.ckpt_base + j;
 		if (lane < cnt) {
-			double delta = src.ckpt[P.ckpt_base + j];
-			for (int t = 0; t < lane; t++)
-				delta = pwm::advance_delta(delta, P.dist, P.step);
-			const double tau = pwm::mul(delta, P.inv_dist);
-			pwm::SlerpParams S;
-			seg_slerp(P, S);
-			double q[7];
-			pwm::interpolate_p(src.from + 7 * (size_t)s, src.to + 7 * (size_t)s, S, tau, q);
-			make_qf(q, W, sm.qf[lane]);
 			sm.slot_query[lane] = s;
 			sm.slot_step[lane] = (uint32_t)(k0 + lane);
 		}
+		if (lane < 5)
+			sm.qf[anchor].q[lane] = src.anchors[ckslot].q[lane];
 		__syncwarp();
 		// steps at or after the segment's current first contact are not needed
 		const int lim = (int)min((int64_t)cnt, (int64_t)cur - k0);
 		queries += lim;
 		const float motion = __double2float_ru(P.skip_scale);
-		const uint32_t hit = traverse_chunk<RETEST_CAP>(W, sm, lane, lim, motion, soft_cap, ctr, rq, src, st);
+		const uint32_t hit = traverse_chunk<RETEST_CAP>(W, sm, lane, lim, cnt, anchor, motion, soft_cap, ctr, rq, src,
+		                                                st, s, ckslot, detailed);
 		if (hit && lane == 0)
 			atomicMin(&first[s], k0 + (__ffs(hit) - 1));
 		__syncwarp();
 	}
+	if (lane == 0 && detailed)
+		atomicAdd(&ctr->stat[STAT_DETAILED], detailed);
 	flush_stats(ctr, st, queries, items, lane);
 }
 
@@ -983,7 +1052,7 @@ extern "C" int pw_states_valid(pw_world *w, const double *states, int64_t n, uin
 		return rc;
 	k_states<RETEST_CAP><<<grid, WARPS * 32, smem, st>>>(w->dev, states, n, valid, ctr, rq, soft_cap_of(w));
 	mark(w, 1, st);
-	StateSrc src{ states, nullptr, nullptr, nullptr, nullptr };
+	StateSrc src{ states, nullptr, nullptr, nullptr, nullptr, nullptr };
 	k_retest<RETEST_CAP><<<w->num_sms * 4, 256, 0, st>>>(w->dev, src, valid, nullptr, ctr, rq);
 	mark(w, 2, st);
 	w->timed = true;
@@ -1077,14 +1146,16 @@ extern "C" int pw_segments_first_contact(pw_world *w, const double *from, const 
 	int64_t total_slots = 0;
 	PW_CUDA(cudaMemcpyAsync(&total_slots, slot_base + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
 	PW_CUDA(cudaStreamSynchronize(st));
-	if ((rc = grow<double>(w->seg_ckpt, (size_t)total_slots + 1)))
+	if ((rc = grow<double>(w->seg_ckpt, (size_t)total_slots + 1)) ||
+	    (rc = grow<QFs>(w->seg_anchor, (size_t)total_slots + 1)))
 		return rc;
+	QFs *anchors = (QFs *)w->seg_anchor.ptr;
 	SegParams *params = (SegParams *)w->seg_params.ptr;
 	double *ckpt = (double *)w->seg_ckpt.ptr;
 	uint32_t *keys = (uint32_t *)w->seg_keys.ptr, *vals = (uint32_t *)w->seg_order.ptr;
 	uint32_t *keys2 = (uint32_t *)w->seg_keys2.ptr, *vals2 = (uint32_t *)w->seg_order2.ptr;
-	k_seg_setup<<<G, B, 0, st>>>(from, to, n, verify_delta, mode, slots, slot_base, params, ckpt, first_step, keys,
-	                             vals, ctr, w->dev.rob.r2);
+	k_seg_setup<<<G, B, 0, st>>>(w->dev, from, to, n, verify_delta, mode, slots, slot_base, params, ckpt, anchors,
+	                             first_step, keys, vals, ctr);
 	PW_CUDA(cudaGetLastError());
 	PW_CUDA(cub::DeviceRadixSort::SortPairsDescending(w->cub_tmp.ptr, t2, keys, keys2, vals, vals2, (int)n, 0, 32, st));
 	// rounds: as many as the longest segment has chunks
@@ -1103,7 +1174,7 @@ extern "C" int pw_segments_first_contact(pw_world *w, const double *from, const 
 		return rc;
 	const int grid = persistent_grid(w, (const void *)k_segments, smem);
 	RetestEntry *rq = (RetestEntry *)w->retest.ptr;
-	StateSrc src{ nullptr, from, to, params, ckpt };
+	StateSrc src{ nullptr, from, to, params, ckpt, anchors };
 	rc = mark(w, 0, st);
 	if (rc)
 		return rc;
@@ -1194,6 +1265,7 @@ extern "C" int pw_world_last_stats(pw_world *w, pw_query_stats *out)
 	out->inline_retests = (int64_t)c.stat[STAT_INLINE];
 	out->work_items = (int64_t)c.stat[STAT_ITEMS];
 	out->reference_checks = w->last_states >= 0 ? w->last_states : (int64_t)c.ref_checks;
+	out->detailed_chunks = (int64_t)c.stat[STAT_DETAILED];
 	if (w->timed) {
 		float a = 0.f, b = 0.f;
 		PW_CUDA(cudaEventElapsedTime(&a, w->ev[0], w->ev[1]));
@@ -1279,7 +1351,7 @@ extern "C" int pw_states_valid_noalloc(pw_world *w, const double *states, int64_
 		return rc;
 	const int grid = persistent_grid(w, (const void *)k_states<NOALLOC_RETEST_CAP>, smem);
 	k_states<NOALLOC_RETEST_CAP><<<grid, WARPS * 32, smem, st>>>(w->dev, states, n, valid, ctr, rq, soft_cap_of(w));
-	StateSrc src{ states, nullptr, nullptr, nullptr, nullptr };
+	StateSrc src{ states, nullptr, nullptr, nullptr, nullptr, nullptr };
 	k_retest<NOALLOC_RETEST_CAP><<<w->num_sms * 4, 256, 0, st>>>(w->dev, src, valid, nullptr, ctr, rq);
 	PW_CUDA(cudaGetLastError());
 	return PW_OK;
