@@ -266,9 +266,9 @@ def run_ours(args):
     achieved = alg_bytes / (trav_ms / 1e3) / 1e9
     peak, peak_kind = _peaks()
     traffic = None
-    tpq = _traffic_per_query()
-    if tpq is not None:
-        traffic = tpq * sum(s["queries"] for s in stats) / len(stats)
+    tps = _traffic_per_segment()
+    if tps is not None:
+        traffic = tps * args.n
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "kernel": "k_segments", "kernel_ms": trav_ms,
             "peak_source": peak_kind, "algorithmic_bytes": alg_bytes}
@@ -305,12 +305,12 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def _traffic_per_query():
-    """DRAM bytes per (segment, step) query of the traversal kernel from the committed ncu summary."""
+def _traffic_per_segment():
+    """DRAM bytes per segment of the traversal kernel, from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "k_segments_traffic.txt")
     try:
         for line in open(path):
-            if line.startswith("dram_bytes_per_query"):
+            if line.startswith("dram_bytes_per_segment"):
                 return float(line.split("=")[1])
     except Exception:
         pass
