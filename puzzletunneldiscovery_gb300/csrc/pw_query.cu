@@ -33,7 +33,7 @@ namespace {
 using namespace pwf;
 
 constexpr int WARPS = 4;                  // warps per block
-constexpr int STACK_CAP = 1024;           // node-pair stack entries per warp
+constexpr int STACK_CAP = 896;            // node-pair stack entries per warp
 constexpr int UNC_CAP = 32;               // uncertain pairs buffered per warp
 constexpr unsigned FULL = 0xffffffffu;
 constexpr uint64_t RETEST_CAP = 1u << 22; // queued FP64 re-tests per query batch
@@ -41,13 +41,17 @@ constexpr uint64_t RETEST_CAP = 1u << 22; // queued FP64 re-tests per query batc
 constexpr int SLOT_SHIFT = 27;                       // stack entry: (env node, robot node | slot << 27)
 constexpr uint32_t NODE_MASK = (1u << SLOT_SHIFT) - 1u;
 
+constexpr int LEAFQ_CAP = 64;  // leaf pairs waiting for a 32-wide triangle-filter batch
+
 struct WarpSmem {
 	uint2 stack[STACK_CAP];
 	uint2 unc[UNC_CAP];
 	QFs qf[32];
+	uint2 leafq[LEAFQ_CAP];    // (env slot, robot slot) of queued leaf pairs
 	uint32_t slot_query[32];   // state or segment index of each slot
 	uint32_t slot_step[32];    // segment step of each slot (0 for states)
 	uint8_t unc_slot[UNC_CAP];
+	uint8_t leafq_slot[LEAFQ_CAP];
 };
 
 // Where the FP64 state of a query comes from when a pair must be re-tested.
@@ -172,9 +176,70 @@ __device__ uint32_t traverse_batch(const WorldDev &W, WarpSmem &sm, int lane, ui
 	if ((open >> lane) & 1u)
 		sm.stack[nroot - 1 - __popc(open & lt_mask)] = make_uint2(0u, (uint32_t)lane << SLOT_SHIFT);
 	__syncwarp();
-	int top = nroot, nunc = 0;
+	int top = nroot, nunc = 0, nleaf = 0;
 	uint32_t done = ~open, hit = 0u;
-	while (top > 0 && done != FULL) {
+
+	auto add_unc = [&](bool unc, uint2 up, int slot) {
+		unc = unc && !((done >> slot) & 1u);
+		unsigned um = __ballot_sync(FULL, unc);
+		if (!um)
+			return;
+		if (nunc + __popc(um) > UNC_CAP) {
+			const uint32_t ih = flush_unc<CAP>(sm, nunc, done, lane, ctr, rq, W, src, st);
+			nunc = 0;
+			__syncwarp();
+			if (ih) {
+				hit |= ih;
+				done |= ih;
+				unc = unc && !((done >> slot) & 1u);
+				um = __ballot_sync(FULL, unc);
+			}
+		}
+		if (unc) {
+			const int o = nunc + __popc(um & lt_mask);
+			sm.unc[o] = up;
+			sm.unc_slot[o] = (uint8_t)slot;
+		}
+		nunc += __popc(um);
+	};
+	auto run_leaves = [&](int k) {
+		bool lh = false, lu = false;
+		uint2 up = make_uint2(0u, 0u);
+		int ls = 0;
+		if (lane < k) {
+			const int i = nleaf - k + lane;
+			const uint2 e = sm.leafq[i];
+			ls = sm.leafq_slot[i];
+			if (!((done >> ls) & 1u)) {
+				st.leaf++;
+				const QFs &Q = sm.qf[ls];
+				const float4 ta = __ldg(W.env.triA + e.x), tb = __ldg(W.env.triB + e.x), tc = __ldg(W.env.triC + e.x);
+				const float4 ra = __ldg(W.rob.triA + e.y), rb = __ldg(W.rob.triB + e.y), rc = __ldg(W.rob.triC + e.y);
+				float gap;
+				const int r = tri_filter(f3(ta), f3(tb), f3(tc), f3(ra), f3(rb), f3(rc), Q.q[0], Q.q[1], Q.q[2],
+				                         Q.q[3], Q.q[4].x, &gap);
+				if (r == 1) {
+					lh = true;
+				} else if (r == 2) {
+					lu = true;
+					up = make_uint2((uint32_t)__float_as_int(ta.w), (uint32_t)__float_as_int(ra.w));
+				}
+			}
+		}
+		nleaf -= k;
+		__syncwarp();
+		const uint32_t hm = __reduce_or_sync(FULL, lh ? (1u << ls) : 0u);
+		hit |= hm;
+		done |= hm;
+		if (done != FULL)
+			add_unc(lu, up, ls);
+	};
+
+	while ((top > 0 || nleaf > 0) && done != FULL) {
+		if (top == 0) {
+			run_leaves(nleaf);
+			continue;
+		}
 		int p = min(top, 32);
 		const int room = soft_cap - top;
 		if (room < p)
@@ -189,32 +254,18 @@ __device__ uint32_t traverse_batch(const WorldDev &W, WarpSmem &sm, int lane, ui
 		const uint32_t rn = pr.y & NODE_MASK;
 		if ((done >> slot) & 1u)
 			active = false;
-		bool push = false, lhit = false, unc = false;
-		uint2 c0 = make_uint2(0u, 0u), c1 = make_uint2(0u, 0u), up = make_uint2(0u, 0u);
+		bool push = false, leaf = false;
+		uint2 c0 = make_uint2(0u, 0u), c1 = make_uint2(0u, 0u);
 		if (active) {
 			const float4 A0 = __ldg(W.env.nodeA + pr.x), A1 = __ldg(W.env.nodeB + pr.x);
 			const float4 B0 = __ldg(W.rob.nodeA + rn), B1 = __ldg(W.rob.nodeB + rn);
 			const QFs &Q = sm.qf[slot];
-			const float4 Q0 = Q.q[0], Q1 = Q.q[1], Q2 = Q.q[2], Q3 = Q.q[3];
 			st.node++;
-			if (!sat_disjoint32(A0, A1, B0, B1, Q0, Q1, Q2, Q3)) {
+			if (!sat_disjoint32(A0, A1, B0, B1, Q.q[0], Q.q[1], Q.q[2], Q.q[3])) {
 				const bool la = pr.x >= ebase, lb = rn >= rbase;
 				if (la && lb) {
-					st.leaf++;
-					const int es = (int)(pr.x - ebase), rs = (int)(rn - rbase);
-					const float4 ta = __ldg(W.env.triA + es), tb = __ldg(W.env.triB + es),
-					             tc = __ldg(W.env.triC + es);
-					const float4 ra = __ldg(W.rob.triA + rs), rb = __ldg(W.rob.triB + rs),
-					             rc = __ldg(W.rob.triC + rs);
-					float gap;
-					const int r = tri_filter(f3(ta), f3(tb), f3(tc), f3(ra), f3(rb), f3(rc), Q0, Q1, Q2, Q3,
-					                         Q.q[4].x, &gap);
-					if (r == 1) {
-						lhit = true;
-					} else if (r == 2) {
-						unc = true;
-						up = make_uint2((uint32_t)__float_as_int(ta.w), (uint32_t)__float_as_int(ra.w));
-					}
+					leaf = true;
+					c0 = make_uint2(pr.x - ebase, rn - rbase);
 				} else {
 					const uint32_t sbits = (uint32_t)slot << SLOT_SHIFT;
 					const bool da = !la && (lb || (A1.x + A1.y + A1.z) >= (B1.x + B1.y + B1.z));
@@ -229,37 +280,13 @@ __device__ uint32_t traverse_batch(const WorldDev &W, WarpSmem &sm, int lane, ui
 				}
 			}
 		}
-		const uint32_t hm = __reduce_or_sync(FULL, lhit ? (1u << slot) : 0u);
-		if (hm) {
-			hit |= hm;
-			done |= hm;
-			if (done == FULL)
-				break;
+		const unsigned lm = __ballot_sync(FULL, leaf);
+		if (leaf) {
+			const int o = nleaf + __popc(lm & lt_mask);
+			sm.leafq[o] = c0;
+			sm.leafq_slot[o] = (uint8_t)slot;
 		}
-		unc = unc && !((done >> slot) & 1u);
-		unsigned um = __ballot_sync(FULL, unc);
-		if (um) {
-			if (nunc + __popc(um) > UNC_CAP) {
-				const uint32_t ih = flush_unc<CAP>(sm, nunc, done, lane, ctr, rq, W, src, st);
-				nunc = 0;
-				__syncwarp();
-				if (ih) {
-					hit |= ih;
-					done |= ih;
-					if (done == FULL)
-						break;
-					unc = unc && !((done >> slot) & 1u);
-					um = __ballot_sync(FULL, unc);
-				}
-			}
-			if (unc) {
-				const int o = nunc + __popc(um & lt_mask);
-				sm.unc[o] = up;
-				sm.unc_slot[o] = (uint8_t)slot;
-			}
-			nunc += __popc(um);
-		}
-		push = push && !((done >> slot) & 1u);
+		nleaf += __popc(lm);
 		const unsigned pm = __ballot_sync(FULL, push);
 		if (push) {
 			// lane 0's children end on top
@@ -269,6 +296,8 @@ __device__ uint32_t traverse_batch(const WorldDev &W, WarpSmem &sm, int lane, ui
 		}
 		top += 2 * __popc(pm);
 		__syncwarp();
+		if (nleaf >= 32)
+			run_leaves(32);
 	}
 	__syncwarp();
 	if (nunc > 0 && done != FULL) {
@@ -332,10 +361,79 @@ __device__ uint32_t traverse_chunk(const WorldDev &W, WarpSmem &sm, int lane, in
 	if (lane == 0)
 		sm.stack[0] = make_uint2(0u, range_bits(0, nopen - 1));
 	__syncwarp();
-	int top = 1, nunc = 0;
+	int top = 1, nunc = 0, nleaf = 0;
 	bool detailed = false;
 	uint32_t done = nopen >= 32 ? 0u : ~((1u << nopen) - 1u), hit = 0u;
-	while (top > 0 && done != FULL) {
+
+	// contact at the steps in hm: keep the lowest; every step from it upwards is settled
+	auto settle = [&](uint32_t hm) {
+		const uint32_t low = hm & (~hm + 1u);
+		if (!hit || low < hit)
+			hit = low;
+		done |= ~(hit - 1u);
+	};
+	// buffer the uncertain pairs of this round (at most one per lane), flushing when full
+	auto add_unc = [&](bool unc, uint2 up, int slot) {
+		unc = unc && !((done >> slot) & 1u);
+		unsigned um = __ballot_sync(FULL, unc);
+		if (!um)
+			return;
+		if (nunc + __popc(um) > UNC_CAP) {
+			const uint32_t ih = flush_unc<CAP>(sm, nunc, done, lane, ctr, rq, W, src, st);
+			nunc = 0;
+			__syncwarp();
+			if (ih) {
+				settle(ih);
+				unc = unc && !((done >> slot) & 1u);
+				um = __ballot_sync(FULL, unc);
+			}
+		}
+		if (unc) {
+			const int o = nunc + __popc(um & lt_mask);
+			sm.unc[o] = up;
+			sm.unc_slot[o] = (uint8_t)slot;
+		}
+		nunc += __popc(um);
+	};
+	// run the triangle filter on the newest k queued leaf pairs, one per lane
+	auto run_leaves = [&](int k) {
+		bool lh = false, lu = false;
+		uint2 up = make_uint2(0u, 0u);
+		int ls = 0;
+		if (lane < k) {
+			const int i = nleaf - k + lane;
+			const uint2 e = sm.leafq[i];
+			ls = sm.leafq_slot[i];
+			if (!((done >> ls) & 1u)) {
+				st.leaf++;
+				const QFs &Q = sm.qf[ls];
+				const float4 ta = __ldg(W.env.triA + e.x), tb = __ldg(W.env.triB + e.x), tc = __ldg(W.env.triC + e.x);
+				const float4 ra = __ldg(W.rob.triA + e.y), rb = __ldg(W.rob.triB + e.y), rc = __ldg(W.rob.triC + e.y);
+				float gap;
+				const int r = tri_filter(f3(ta), f3(tb), f3(tc), f3(ra), f3(rb), f3(rc), Q.q[0], Q.q[1], Q.q[2],
+				                         Q.q[3], Q.q[4].x, &gap);
+				if (r == 1) {
+					lh = true;
+				} else if (r == 2) {
+					lu = true;
+					up = make_uint2((uint32_t)__float_as_int(ta.w), (uint32_t)__float_as_int(ra.w));
+				}
+			}
+		}
+		nleaf -= k;
+		__syncwarp();
+		const uint32_t hm = __reduce_or_sync(FULL, lh ? (1u << ls) : 0u);
+		if (hm)
+			settle(hm);
+		if (done != FULL)
+			add_unc(lu, up, ls);
+	};
+
+	while ((top > 0 || nleaf > 0) && done != FULL) {
+		if (top == 0) {
+			run_leaves(nleaf);
+			continue;
+		}
 		int p = min(top, 32);
 		const int room = soft_cap - top;
 		if (room < p)
@@ -357,8 +455,8 @@ __device__ uint32_t traverse_chunk(const WorldDev &W, WarpSmem &sm, int lane, in
 			else if (above)
 				s1 = min(s1, s0 + __ffs(above) - 2);
 		}
-		bool push2 = false, push1 = false, lhit = false, unc = false, need = false;
-		uint2 c0 = make_uint2(0u, 0u), c1 = make_uint2(0u, 0u), up = make_uint2(0u, 0u);
+		bool push2 = false, push1 = false, leaf = false, need = false;
+		uint2 c0 = make_uint2(0u, 0u), c1 = make_uint2(0u, 0u);
 		if (active) {
 			const float4 A0 = __ldg(W.env.nodeA + pr.x), A1 = __ldg(W.env.nodeB + pr.x);
 			const float4 B0 = __ldg(W.rob.nodeA + rn), B1 = __ldg(W.rob.nodeB + rn);
@@ -388,21 +486,8 @@ __device__ uint32_t traverse_chunk(const WorldDev &W, WarpSmem &sm, int lane, in
 					c1 = make_uint2(pr.x, rn | range_bits(ref + 1, s1));
 					push2 = true;
 				} else if (la && lb) {
-					st.leaf++;
-					const int es = (int)(pr.x - ebase), rs = (int)(rn - rbase);
-					const float4 ta = __ldg(W.env.triA + es), tb = __ldg(W.env.triB + es),
-					             tc = __ldg(W.env.triC + es);
-					const float4 ra = __ldg(W.rob.triA + rs), rb = __ldg(W.rob.triB + rs),
-					             rc = __ldg(W.rob.triC + rs);
-					float gap;
-					const int r = tri_filter(f3(ta), f3(tb), f3(tc), f3(ra), f3(rb), f3(rc), Q0, Q1, Q2, Q.q[3],
-					                         Q.q[4].x, &gap);
-					if (r == 1) {
-						lhit = true;
-					} else if (r == 2) {
-						unc = true;
-						up = make_uint2((uint32_t)__float_as_int(ta.w), (uint32_t)__float_as_int(ra.w));
-					}
+					leaf = true;
+					c0 = make_uint2(pr.x - ebase, rn - rbase);
 				} else {
 					const uint32_t rb_ = range_bits(s0, s1);
 					const bool da = !la && (lb || (A1.x + A1.y + A1.z) >= (B1.x + B1.y + B1.z));
@@ -417,43 +502,14 @@ __device__ uint32_t traverse_chunk(const WorldDev &W, WarpSmem &sm, int lane, in
 				}
 			}
 		}
-		const uint32_t hm = __reduce_or_sync(FULL, lhit ? (1u << s0) : 0u);
-		if (hm) {
-			const uint32_t low = hm & (~hm + 1u);
-			if (!hit || low < hit)
-				hit = low;
-			done |= ~(hit - 1u);
-			if (done == FULL)
-				break;
+		// queue leaf pairs; filter them 32 at a time
+		const unsigned lm = __ballot_sync(FULL, leaf);
+		if (leaf) {
+			const int o = nleaf + __popc(lm & lt_mask);
+			sm.leafq[o] = c0;
+			sm.leafq_slot[o] = (uint8_t)s0;
 		}
-		unc = unc && !((done >> s0) & 1u);
-		unsigned um = __ballot_sync(FULL, unc);
-		if (um) {
-			if (nunc + __popc(um) > UNC_CAP) {
-				const uint32_t ih = flush_unc<CAP>(sm, nunc, done, lane, ctr, rq, W, src, st);
-				nunc = 0;
-				__syncwarp();
-				if (ih) {
-					const uint32_t low = ih & (~ih + 1u);
-					if (!hit || low < hit)
-						hit = low;
-					done |= ~(hit - 1u);
-					if (done == FULL)
-						break;
-					unc = unc && !((done >> s0) & 1u);
-					um = __ballot_sync(FULL, unc);
-				}
-			}
-			if (unc) {
-				const int o = nunc + __popc(um & lt_mask);
-				sm.unc[o] = up;
-				sm.unc_slot[o] = (uint8_t)s0;
-			}
-			nunc += __popc(um);
-		}
-		const bool settled = (done >> s0) & 1u;
-		push2 = push2 && !settled;
-		push1 = push1 && !settled;
+		nleaf += __popc(lm);
 		const unsigned pm2 = __ballot_sync(FULL, push2), pm1 = __ballot_sync(FULL, push1);
 		// lane 0's entries end on top
 		const int o = top + 2 * __popc(pm2 & gt_mask) + __popc(pm1 & gt_mask);
@@ -471,15 +527,14 @@ __device__ uint32_t traverse_chunk(const WorldDev &W, WarpSmem &sm, int lane, in
 			ndetailed++;
 		}
 		__syncwarp();
+		if (nleaf >= 32)
+			run_leaves(32);
 	}
 	__syncwarp();
 	if (nunc > 0 && done != FULL) {
 		const uint32_t ih = flush_unc<CAP>(sm, nunc, done, lane, ctr, rq, W, src, st);
-		if (ih) {
-			const uint32_t low = ih & (~ih + 1u);
-			if (!hit || low < hit)
-				hit = low;
-		}
+		if (ih)
+			settle(ih);
 	}
 	__syncwarp();
 	return hit;
