@@ -31,7 +31,6 @@ sys.path.insert(0, ROOT)
 
 from puzzletunneldiscovery_gb300 import workloads as W  # noqa: E402
 
-METRIC = "collision checks/sec (first-contact segment queries, interlocking tori)"
 UNIT = "checks/s"
 DELTA = 0.001
 # per-unit algorithmic bytes of the traversal kernel (roofline section)
@@ -56,11 +55,22 @@ def _dist_env():
     return ws, rank, local
 
 
-def _meshes():
-    return W.cfg_interlocking_tori()
+WORKLOADS = {
+    # name: (metric, meshes, default units per GPU)
+    "segments": ("collision checks/sec (first-contact segment queries, interlocking tori)",
+                 W.cfg_interlocking_tori, 1_000_000),
+    "plate": ("collision checks/sec (is_valid_state, perforated plate vs torus knot)", W.cfg_plate_knot, 20_000_000),
+}
 
 
-def _batch(n, scale, seed):
+def _meshes(workload="segments"):
+    return WORKLOADS[workload][1]()
+
+
+def _batch(n, scale, seed, workload="segments", Ve=None):
+    if workload == "plate":
+        lo, hi = Ve.min(0) - 0.5, Ve.max(0) + 0.5
+        return W.uniform_states(n, lo, hi, scale, seed=seed), None
     return W.segment_batch(n, -2.0, 2.0, scale, seed=seed)
 
 
@@ -115,26 +125,55 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_baseline(q0, q1, target_s=12.0, max_n=None):
+class Work:
+    """One workload: its meshes, per-rank batch, GPU call and CPU-oracle call."""
+
+    def __init__(self, name, n, seed, scale, Ve):
+        self.name = name
+        self.n = n
+        self.metric = WORKLOADS[name][0]
+        self.q0, self.q1 = _batch(n, scale, seed, name, Ve)
+
+    def gpu(self, uw, a, b):
+        if self.name == "plate":
+            return uw.is_valid_states(a)
+        return uw.first_contact_steps(a, b, DELTA)
+
+    def cpu(self, ow, lo, hi, threads):
+        """(reference checks, seconds) of the oracle on units lo..hi."""
+        t0 = time.perf_counter()
+        if self.name == "plate":
+            ow.is_valid(self.q0[lo:hi], nthreads=threads)
+            checks = hi - lo
+        else:
+            _, c = ow.segments_first_contact(self.q0[lo:hi], self.q1[lo:hi], DELTA, mode=0, nthreads=threads)
+            checks = int(c.sum())
+        return checks, time.perf_counter() - t0
+
+    def bytes_in(self):
+        return self.n * 56 * (1 if self.name == "plate" else 2)
+
+    def bytes_out(self):
+        return self.n * (1 if self.name == "plate" else 4)
+
+
+def cpu_baseline(work, target_s=12.0):
     """The oracle (CPU restatement of the reference path) on a bounded sample, all host threads."""
     from oracle import oracle as O
     O.build()
-    Ve, Fe, Vr, Fr = _meshes()
+    Ve, Fe, Vr, Fr = _meshes(work.name)
     ow = O.OracleWorld(Ve, Fe, Vr, Fr)
     cores = os.cpu_count() or 1
-    n = 128
-    total = len(q0) if max_n is None else min(len(q0), max_n)
+    n = 128 if work.name == "segments" else 8192
     while True:
-        n = min(n, total)
-        t0 = time.perf_counter()
-        _, checks = ow.segments_first_contact(q0[:n], q1[:n], DELTA, mode=0, nthreads=cores)
-        dt = time.perf_counter() - t0
-        if dt >= target_s or n >= total:
+        n = min(n, work.n)
+        checks, dt = work.cpu(ow, 0, n, cores)
+        if dt >= target_s or n >= work.n:
             break
-        n = min(total, max(n * 2, int(n * target_s / max(dt, 1e-3) * 1.1)))
-    return {"value": float(checks.sum()) / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "first %d segments of the rank-0 batch (%d reference checks, %.1f s)"
-                      % (n, int(checks.sum()), dt)}
+        n = min(work.n, max(n * 2, int(n * target_s / max(dt, 1e-3) * 1.1)))
+    unit_name = "segments" if work.name == "segments" else "states"
+    return {"value": float(checks) / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "first %d %s of the rank-0 batch (%d reference checks, %.1f s)" % (n, unit_name, checks, dt)}
 
 
 def run_reference(args):
@@ -144,29 +183,27 @@ def run_reference(args):
         return
     from oracle import oracle as O
     O.build()
-    Ve, Fe, Vr, Fr = _meshes()
+    Ve, Fe, Vr, Fr = _meshes(args.workload)
     ow = O.OracleWorld(Ve, Fe, Vr, Fr)
     cores = os.cpu_count() or 1
-    q0, q1 = _batch(args.n, ow.scene_scale, seed=0)
-    sample = args.ref_sample
+    work = Work(args.workload, args.n, 0, ow.scene_scale, Ve)
+    sample = args.ref_sample if args.workload == "segments" else 100 * args.ref_sample
     times, checks = [], []
     for it in range(args.warmup + args.steps):
-        lo = (it * sample) % max(1, len(q0) - sample)
-        t0 = time.perf_counter()
-        _, c = ow.segments_first_contact(q0[lo:lo + sample], q1[lo:lo + sample], DELTA, mode=0, nthreads=cores)
-        dt = time.perf_counter() - t0
+        lo = (it * sample) % max(1, work.n - sample)
+        c, dt = work.cpu(ow, lo, lo + sample, cores)
         if it >= args.warmup:
             times.append(dt)
-            checks.append(int(c.sum()))
+            checks.append(c)
     value = sum(checks) / sum(times)
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+    line = {"impl": "reference", "metric": work.metric, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded interlocking-tori segments)",
-            "config": {"workload": "segments_first_contact/interlocking_tori", "n_segments": args.n,
-                       "verify_delta": DELTA, "sample_per_step": sample},
+            "data": "synthetic (seeded, same batch as the GPU arm)",
+            "config": {"workload": args.workload, "units_per_gpu": args.n, "verify_delta": DELTA,
+                       "sample_per_step": sample},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": "%d segments per step of the %d-segment batch" % (sample, args.n)},
+                             "sample": "%d units per step of the %d-unit batch" % (sample, args.n)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -182,15 +219,15 @@ def run_ours(args):
         dist.init_process_group("nccl", init_method="env://")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    Ve, Fe, Vr, Fr = _meshes()
+    Ve, Fe, Vr, Fr = _meshes(args.workload)
     uw = pw.UnitWorld(local)
     uw.load_env_mesh(Ve, Fe)
     uw.load_robot_mesh(Vr, Fr)
     uw.scaleToUnit()
     uw.angleModel(0.0, 0.0)
-    q0, q1 = _batch(args.n, uw.scene_scale, seed=rank)
-    a = torch.from_numpy(q0).to(dev)
-    b = torch.from_numpy(q1).to(dev)
+    work = Work(args.workload, args.n, rank, uw.scene_scale, Ve)
+    a = torch.from_numpy(work.q0).to(dev)
+    b = torch.from_numpy(work.q1).to(dev) if work.q1 is not None else None
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     def barrier():
@@ -199,7 +236,7 @@ def run_ours(args):
         torch.cuda.synchronize(dev)
 
     for _ in range(args.warmup):
-        uw.first_contact_steps(a, b, DELTA)
+        work.gpu(uw, a, b)
     barrier()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     stats = []
@@ -209,7 +246,7 @@ def run_ours(args):
         for i in range(args.steps):
             flush.zero_()                      # L2 flush between timed steps (not timed)
             ev[i][0].record(stream)
-            f = uw.first_contact_steps(a, b, DELTA)
+            f = work.gpu(uw, a, b)
             ev[i][1].record(stream)
             stats.append(uw.last_stats())      # synchronises; outside the event pair
         barrier()
@@ -227,9 +264,9 @@ def run_ours(args):
     value = tot_checks / (tot_ms / 1e3)
 
     # end to end through the public API with host buffers (pinned), copies inside the timed region
-    ha = torch.from_numpy(q0).pin_memory()
-    hb = torch.from_numpy(q1).pin_memory()
-    hout = torch.empty(args.n, dtype=torch.int32).pin_memory()
+    ha = torch.from_numpy(work.q0).pin_memory()
+    hb = torch.from_numpy(work.q1).pin_memory() if work.q1 is not None else None
+    hout = torch.empty(args.n, dtype=f.dtype).pin_memory()
     e2e_ms, e2e_checks = 0.0, 0
     barrier()
     for i in range(args.steps):
@@ -237,8 +274,8 @@ def run_ours(args):
         s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s0.record(stream)
         da = ha.to(dev, non_blocking=True)
-        db = hb.to(dev, non_blocking=True)
-        f = uw.first_contact_steps(da, db, DELTA)
+        db = hb.to(dev, non_blocking=True) if hb is not None else None
+        f = work.gpu(uw, da, db)
         hout.copy_(f, non_blocking=True)
         s1.record(stream)
         torch.cuda.synchronize(dev)
@@ -262,43 +299,53 @@ def run_ours(args):
     trav_ms = sum(s["traverse_ms"] for s in stats) / len(stats)
     node = sum(s["node_tests"] for s in stats) / len(stats)
     leaf = sum(s["leaf_tests"] for s in stats) / len(stats)
-    alg_bytes = node * BYTES_NODE_PAIR + leaf * BYTES_LEAF_PAIR + args.n * BYTES_SEGMENT
+    io = work.bytes_in() + work.bytes_out()
+    alg_bytes = node * BYTES_NODE_PAIR + leaf * BYTES_LEAF_PAIR + io
     achieved = alg_bytes / (trav_ms / 1e3) / 1e9
     peak, peak_kind = _peaks()
     traffic = None
     tps = _traffic_per_segment()
-    if tps is not None:
+    if tps is not None and args.workload == "segments":
         traffic = tps * args.n
+    kernel = "k_segments" if args.workload == "segments" else "k_states"
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": traffic, "kernel": "k_segments", "kernel_ms": trav_ms,
+            "traffic": traffic, "kernel": kernel, "kernel_ms": trav_ms,
             "peak_source": peak_kind, "algorithmic_bytes": alg_bytes}
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(q0, q1, target_s=args.cpu_seconds)
+        cpu = cpu_baseline(work, target_s=args.cpu_seconds)
     last = stats[-1]
     fc = f.cpu().numpy()
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+    if args.workload == "segments":
+        config = {"workload": "segments_first_contact/interlocking_tori",
+                  "meshes": "torus R=1 r=0.25 64x32 (4096 tris) x2, interlocked",
+                  "n_segments_per_gpu": args.n, "verify_delta": DELTA, "mode": "transit_state_to"}
+        extra = {"segments_per_s": args.n * ws / (tot_ms / args.steps / 1e3),
+                 "free_fraction": float((fc == -1).mean()),
+                 "detailed_chunk_fraction": last["detailed_chunks"] / max(1, last["work_items"])}
+    else:
+        config = {"workload": "is_valid_state/perforated_plate_vs_torus_knot",
+                  "meshes": "plate 400x400 grid over [-2,2]^2 with 25 holes (%d tris), (2,3) knot 256x16 (8192 tris)"
+                            % len(Fe),
+                  "n_states_per_gpu": args.n}
+        extra = {"free_fraction": float(fc.astype(bool).mean())}
+    config.update({"l2": "flushed (256 MB write) between timed steps; per-step working set > L2",
+                   "parallelism": "replicas" if ws == 1 else "shard-per-rank (weak)"})
+    line = {"metric": work.metric, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 traversal + f64 state math/re-tests",
-            "data": "synthetic (seeded interlocking-tori segments; no published data set for this path)",
-            "config": {"workload": "segments_first_contact/interlocking_tori",
-                       "meshes": "torus R=1 r=0.25 64x32 (4096 tris) x2, interlocked",
-                       "n_segments_per_gpu": args.n, "verify_delta": DELTA, "mode": "transit_state_to",
-                       "l2": "flushed (256 MB write) between timed steps; per-step working set > L2",
-                       "parallelism": "replicas" if ws == 1 else "shard-per-rank (weak)"},
-            "roofline": roof, "cpu_baseline": cpu,
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(2 * args.n * 56 * ws),
-                    "d2h_bytes_per_step": int(4 * args.n * ws)},
+            "data": "synthetic (seeded; no published data set for this path)",
+            "config": config, "roofline": roof, "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(work.bytes_in() * ws),
+                    "d2h_bytes_per_step": int(work.bytes_out() * ws)},
             "clocks": clk.summary(),
-            "gpu_launches": 6 * args.steps,
-            "detail": {"reference_checks_per_step": tot_checks / args.steps,
-                       "gpu_queries_per_step": last["queries"], "node_tests": last["node_tests"],
-                       "leaf_tests": last["leaf_tests"], "fp64_retests": last["retests"],
-                       "fp64_retest_rate_per_leaf": last["retests"] / max(1, last["leaf_tests"]),
-                       "inline_retests": last["inline_retests"], "retest_ms": last["retest_ms"],
-                       "detailed_chunk_fraction": last["detailed_chunks"] / max(1, last["work_items"]),
-                       "segments_per_s": args.n * ws / (tot_ms / args.steps / 1e3),
-                       "free_fraction": float((fc == -1).mean()), "step_ms": step_ms}}
+            "gpu_launches": (6 if args.workload == "segments" else 2) * args.steps,
+            "detail": dict({"reference_checks_per_step": tot_checks / args.steps,
+                            "gpu_queries_per_step": last["queries"], "node_tests": last["node_tests"],
+                            "leaf_tests": last["leaf_tests"], "fp64_retests": last["retests"],
+                            "fp64_retest_rate_per_leaf": last["retests"] / max(1, last["leaf_tests"]),
+                            "inline_retests": last["inline_retests"], "retest_ms": last["retest_ms"],
+                            "step_ms": step_ms}, **extra)}
     print(json.dumps(line))
     if ws > 1:
         dist.barrier()
@@ -323,11 +370,14 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--n", type=int, default=1_000_000, help="segments per GPU")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="segments")
+    ap.add_argument("--n", type=int, default=None, help="units (segments or states) per GPU")
     ap.add_argument("--ref-sample", type=int, default=400, help="segments per reference-arm step")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
+    if args.n is None:
+        args.n = WORKLOADS[args.workload][2]
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -229,3 +229,32 @@ def test_single_triangle_meshes(oracle_mod, built_lib):
     uw, ow = _pair(oracle_mod, Ve, F, Vr, F)
     q = W.uniform_states(2000, -1.0, 1.0, ow.scene_scale, seed=1)
     assert (uw.is_valid_states(torch.from_numpy(q)).cpu().numpy() == ow.is_valid(q)).all()
+
+
+@pytest.fixture(scope="module")
+def plate(oracle_mod, built_lib):
+    """Perforated plate (269k triangles) and a (2,3) torus knot (8192 triangles)."""
+    return _pair(oracle_mod, *W.cfg_plate_knot())
+
+
+def test_plate_knot_states_parity(plate):
+    uw, ow = plate
+    Ve = ow.Ve
+    lo, hi = Ve.min(0) - 0.5, Ve.max(0) + 0.5
+    q = W.uniform_states(60_000, lo, hi, ow.scene_scale, seed=5)
+    gpu = uw.is_valid_states(torch.from_numpy(q)).cpu().numpy()
+    cpu = ow.is_valid(q)
+    assert (gpu == cpu).all(), int((gpu != cpu).sum())
+    assert 0.01 < cpu.mean() < 0.99
+    info = uw.info()
+    assert info["env_faces"] == ow.info()["nf_env"] and info["env_bvh_depth"] > 15
+
+
+def test_plate_knot_segments_parity(plate):
+    uw, ow = plate
+    Ve = ow.Ve
+    lo, hi = Ve.min(0) - 0.5, Ve.max(0) + 0.5
+    q0, q1 = W.segment_batch(600, lo, hi, ow.scene_scale, sigma_t=0.3, seed=8)
+    gpu = uw.first_contact_steps(torch.from_numpy(q0), torch.from_numpy(q1), 0.001).cpu().numpy()
+    cpu, _ = ow.segments_first_contact(q0, q1, 0.001)
+    assert (gpu == cpu).all(), int((gpu != cpu).sum())
