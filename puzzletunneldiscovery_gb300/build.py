@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 LIB_NAME = "libpwcollide.so"
 LIB_PATH = os.path.join(HERE, LIB_NAME)
-SOURCES = ["pw_world.cu", "pw_query.cu"]
+SOURCES = ["pw_world.cu", "pw_query.cu", "pw_mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -36,7 +36,7 @@ def _flags():
 
 def _deps():
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
-    files.append(os.path.join(INCLUDE, "pw_collide.h"))
+    files += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
     files.append(os.path.abspath(__file__))
     return files
 

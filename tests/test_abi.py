@@ -11,8 +11,11 @@ from conftest import ROOT
 
 
 def _declared():
-    src = open(os.path.join(ROOT, "include", "pw_collide.h")).read()
-    return set(re.findall(r"PW_API[^;]*?\b(pw_[a-z0-9_]+)\s*\(", src, flags=re.S))
+    names = set()
+    for h in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        src = open(os.path.join(ROOT, "include", h)).read()
+        names |= set(re.findall(r"PW_API[^;]*?\b(pw_[a-z0-9_]+)\s*\(", src, flags=re.S))
+    return names
 
 
 def test_header_and_binding_agree():

@@ -1,0 +1,126 @@
+"""The learned proposal on the GPU: forward, gradients and Adam against the CPU
+oracle (oracle/mlp_oracle.py), and a trained network that beats uniform
+sampling at finding free states.  Everything runs through libpwcollide.so.
+
+Tolerances.  The device accumulates in FP32 in a different order from the
+FP64 oracle, and a BF16 rounding of an activation can land on the other side
+of a tie; both are far below these bounds:
+  * probabilities: |p_dev - p_oracle| <= 2e-3 (absolute);
+  * loss: relative 1e-3;
+  * gradients: per parameter tensor, ||g_dev - g_oracle|| <= 2e-2 ||g_oracle||;
+  * Adam: parameters after the step within 1e-6 relative of the oracle step
+    applied to the device gradient.
+"""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mo():
+    from oracle import mlp_oracle
+    return mlp_oracle
+
+
+def _net(seed=1):
+    from puzzletunneldiscovery_gb300.surrogate import Surrogate
+    return Surrogate(0, seed)
+
+
+def _states(n, seed):
+    from puzzletunneldiscovery_gb300 import workloads as W
+    return W.uniform_states(n, -2.0, 2.0, 0.4, seed=seed)
+
+
+def _tensors(mo, p):
+    layers, ow5, ob5, n = mo.layout()
+    out = []
+    for l, (o, fin, ob) in enumerate(layers):
+        out.append(("W%d" % (l + 1), slice(o, o + mo.H * fin)))
+        out.append(("b%d" % (l + 1), slice(ob, ob + mo.H)))
+    out.append(("w5", slice(ow5, ow5 + mo.H)))
+    out.append(("b5", slice(ob5, ob5 + 1)))
+    return out
+
+
+def test_parameter_block_layout(built_lib, mo):
+    net = _net()
+    assert net.num_params == mo.layout()[3]
+    p = net.params()
+    W1 = p[:mo.H * mo.KIN].reshape(mo.H, mo.KIN)
+    assert (W1[:, 9:] == 0).all() and np.abs(W1[:, :9]).max() > 0
+    p2 = np.random.default_rng(0).normal(0, 0.05, p.shape).astype(np.float32)
+    net.set_params(p2)
+    assert (net.params() == p2).all()
+
+
+@pytest.mark.parametrize("n", [1, 127, 4096, 70001])
+def test_predict_matches_oracle(built_lib, mo, n):
+    net = _net(2)
+    q = _states(n, 10 + n)
+    p = net.params().astype(np.float64)
+    want = mo.predict(p, q)
+    got = net.predict(torch.from_numpy(q).cuda()).cpu().numpy()
+    assert got.shape == (n,)
+    assert np.abs(got - want).max() <= 2e-3
+
+
+@pytest.mark.parametrize("n", [1000, 65536])
+def test_gradients_match_oracle(built_lib, mo, n):
+    net = _net(3)
+    q = _states(n, 20)
+    y = (np.linalg.norm(q[:, :3], axis=1) > 0.5).astype(np.uint8)
+    p = net.params().astype(np.float64)
+    loss = net.gradients(torch.from_numpy(q).cuda(), torch.from_numpy(y).cuda())
+    L, g = mo.gradients(p, q, y)
+    assert abs(loss - L) <= 1e-3 * abs(L)
+    gd = net.grads().astype(np.float64)
+    for name, sl in _tensors(mo, p):
+        ref = g[sl]
+        err = np.linalg.norm(gd[sl] - ref)
+        assert err <= 2e-2 * np.linalg.norm(ref) + 1e-9, (name, err, np.linalg.norm(ref))
+
+
+def test_adam_step_matches_oracle(built_lib, mo):
+    net = _net(4)
+    q = torch.from_numpy(_states(4096, 30)).cuda()
+    y = (torch.rand(4096, device="cuda") < 0.5).to(torch.uint8)
+    p0 = net.params().astype(np.float64)
+    net.gradients(q, y)
+    g = net.grads().astype(np.float64)
+    net.train_step(q, y, 1e-3)
+    p1 = net.params().astype(np.float64)
+    want, _, _ = mo.adam(p0, g, np.zeros_like(p0), np.zeros_like(p0), 1, 1e-3)
+    assert np.abs(p1 - want).max() <= 1e-6 * max(1.0, np.abs(want).max())
+
+
+def test_training_beats_uniform_sampling(built_lib):
+    """The gain the network brings: after online training on exact labels, the
+    top 10% of candidates it ranks are free far more often than uniform
+    candidates, and every accepted sample is exactly free."""
+    import puzzletunneldiscovery_gb300 as pw
+    from puzzletunneldiscovery_gb300 import surrogate as S
+    from puzzletunneldiscovery_gb300 import workloads as W
+    Ve, Fe, Vr, Fr = W.cfg_interlocking_tori()
+    uw = pw.UnitWorld(0)
+    uw.load_env_mesh(Ve, Fe)
+    uw.load_robot_mesh(Vr, Fr)
+    uw.scaleToUnit()
+    uw.angleModel(0.0, 0.0)
+    dev = torch.device("cuda", 0)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(0)
+    draw = lambda n: S.uniform_states_device(n, -2.0, 2.0, uw.scene_scale, gen, dev)  # noqa: E731
+    net = _net(5)
+    rep = S.train_online(uw, net, draw, 4 << 20, batch=65536, lr=1e-3, log_every=16)
+    assert rep.losses[-1][1] < 0.6 * rep.losses[0][1]
+    cand = draw(1 << 22)
+    exact = uw.is_valid_states(cand)
+    base = float(exact.float().mean())
+    acc, g = S.guided_free_samples(uw, net, cand, top_frac=0.1)
+    assert uw.is_valid_states(acc).all()          # no false-free sample
+    assert g.precision >= min(0.99, base + 0.3)
+    prec, rec = S.precision_recall(net.predict(cand), exact)
+    assert prec > base + 0.2 and rec > 0.8
