@@ -47,8 +47,19 @@ PW_API int pw_mlp_set_params(pw_mlp *m, const float *host_in);
 /* host: the gradient block of the last pw_mlp_gradients / pw_mlp_train_step. */
 PW_API int pw_mlp_get_grads(const pw_mlp *m, float *host_out);
 
-/* P(collision free) of n states (device float64 [n x 7] -> device float32 [n]). */
+/* P(collision free) of n states (device float64 [n x 7] -> device float32 [n]):
+ * one fused, persistent kernel on the tcgen05 tensor cores (weights streamed by
+ * bulk copies, accumulators in tensor memory).  Its waits are bounded;
+ * pw_mlp_check reports whether one gave up. */
 PW_API int pw_mlp_predict(pw_mlp *m, const double *states, int64_t n, float *prob, void *stream);
+
+/* The same prediction through the mma.sync GEMM kernels that training uses
+ * (a cross-check of pw_mlp_predict; layer by layer, activations through HBM). */
+PW_API int pw_mlp_predict_mma(pw_mlp *m, const double *states, int64_t n, float *prob, void *stream);
+
+/* host: synchronises the device; PW_ERR_INTERNAL if a bounded device wait of an
+ * earlier pw_mlp_predict gave up (its probabilities are then invalid). */
+PW_API int pw_mlp_check(pw_mlp *m);
 
 /* Gradients of the mean binary cross-entropy over one batch (device states,
  * device uint8 labels, 1 = free) into the gradient block; no update.

@@ -38,7 +38,8 @@ EXPORTS = (
     "pw_state_distance", "pw_state_interpolate", "pw_segment_step_state", "pw_states_valid_noalloc",
     # include/pw_mlp.h
     "pw_mlp_create", "pw_mlp_destroy", "pw_mlp_num_params", "pw_mlp_get_params", "pw_mlp_set_params",
-    "pw_mlp_get_grads", "pw_mlp_predict", "pw_mlp_gradients", "pw_mlp_train_step",
+    "pw_mlp_get_grads", "pw_mlp_predict", "pw_mlp_gradients", "pw_mlp_train_step", "pw_mlp_predict_mma",
+    "pw_mlp_check",
 )
 
 
@@ -129,6 +130,8 @@ def load():
         "pw_mlp_set_params": (ctypes.c_int, [vp, fp]),
         "pw_mlp_get_grads": (ctypes.c_int, [vp, fp]),
         "pw_mlp_predict": (ctypes.c_int, [vp, vp, i64, vp, vp]),
+        "pw_mlp_predict_mma": (ctypes.c_int, [vp, vp, i64, vp, vp]),
+        "pw_mlp_check": (ctypes.c_int, [vp]),
         "pw_mlp_gradients": (ctypes.c_int, [vp, vp, vp, i64, fp, vp]),
         "pw_mlp_train_step": (ctypes.c_int, [vp, vp, vp, i64, ctypes.c_float, fp, vp]),
     }

@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstring>
 #include <random>
+#include <string>
 #include <vector>
 
 #include "pw_internal.cuh"
@@ -94,10 +95,23 @@ __device__ __forceinline__ void mma_bf16(float *d, unsigned a0, unsigned a1, uns
 	             : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
-__device__ __forceinline__ float silu(float z) { return z / (1.f + __expf(-z)); }
+// SiLU through one hardware tanh: silu(z) = z sigmoid(z) = h + h tanh(h), h = z / 2.
+// tanh.approx.f32 has a relative error near 2^-11, below the BF16 rounding that follows.
+__device__ __forceinline__ float tanh_fast(float x)
+{
+	float y;
+	asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+	return y;
+}
+__device__ __forceinline__ float silu(float z)
+{
+	const float h = 0.5f * z;
+	return fmaf(h, tanh_fast(h), h);
+}
+// d silu / dz = s (1 + z (1 - s)), s = sigmoid(z) = (1 + tanh(z / 2)) / 2
 __device__ __forceinline__ float dsilu(float z)
 {
-	const float s = 1.f / (1.f + __expf(-z));
+	const float s = fmaf(0.5f, tanh_fast(0.5f * z), 0.5f);
 	return s * (1.f + z * (1.f - s));
 }
 
@@ -383,6 +397,8 @@ __global__ void k_to_bf16(const float *w, int64_t n, bf16 *wb, bf16 *wbt, int ro
 	}
 }
 
+#include "pw_mlp_tc.cuh"
+
 } // namespace
 
 // ------------------------------------------------------------------ the network object
@@ -395,6 +411,9 @@ struct pw_mlp {
 	DeviceBuffer wbf, wbft;      // BF16 weights and transposes (hidden layers)
 	size_t off_wb[NLAYER];
 	DeviceBuffer acts, zs, gbuf, gbuf2, head, misc;
+	DeviceBuffer wimg;           // swizzled BF16 weight images of the tcgen05 forward kernel
+	bool wimg_dirty = true;
+	int num_sms = 1;
 	int64_t cap = 0;             // rows the activation buffers hold
 	int64_t step = 0;
 	float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
@@ -456,6 +475,8 @@ extern "C" int pw_mlp_create(pw_mlp **out, int device, uint64_t seed)
 	chk(m->wbf.reserve(sizeof(bf16) * ob));
 	chk(m->wbft.reserve(sizeof(bf16) * ob));
 	chk(m->misc.reserve(64));
+	chk(cudaMemset(m->misc.ptr, 0, 64));
+	chk(cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, device));
 	if (rc) {
 		delete m;
 		return rc;
@@ -521,6 +542,7 @@ extern "C" int pw_mlp_set_params(pw_mlp *m, const float *host_in)
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_mlp_set_params: NULL argument");
 	PW_CUDA(cudaSetDevice(m->device));
 	PW_CUDA(cudaMemcpy(m->params.ptr, host_in, sizeof(float) * m->nparam, cudaMemcpyHostToDevice));
+	m->wimg_dirty = true;
 	for (int l = 0; l < NLAYER; l++) {
 		const int64_t nw = (int64_t)H * in_dim(l);
 		k_to_bf16<<<(unsigned)((nw + 255) / 256), 256>>>((float *)m->params.ptr + m->off_w[l], nw,
@@ -569,15 +591,73 @@ static int mlp_forward(pw_mlp *m, const double *states, int64_t n, cudaStream_t 
 	return PW_OK;
 }
 
-// P(free) of n states (device pointers), on the stream.
+static int *mlp_err(pw_mlp *m) { return (int *)((char *)m->misc.ptr + 16); }
+
+// P(free) of n states on the tcgen05 tensor cores (one fused persistent kernel).
 extern "C" int pw_mlp_predict(pw_mlp *m, const double *states, int64_t n, float *prob, void *stream)
 {
 	if (!m || n < 0 || (n > 0 && (!states || !prob)))
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_mlp_predict: bad argument");
 	if (n == 0)
 		return PW_OK;
-	if (n > (int64_t(1) << 31) - BM)
-		return pw_fail(PW_ERR_INVALID_ARG, "pw_mlp_predict: at most 2^31 - 128 states per call");
+	PW_CUDA(cudaSetDevice(m->device));
+	cudaStream_t st = (cudaStream_t)stream;
+	if (m->wimg_dirty) {
+		PW_CUDA(m->wimg.reserve((size_t)tc::NWBLOCK * tc::WBLOCK_BYTES));
+		const int64_t nchunk = (int64_t)tc::NWBLOCK * H * 8;
+		tc::k_weight_image<<<(unsigned)((nchunk + 255) / 256), 256, 0, st>>>(
+		    (const float *)m->params.ptr, (int64_t)m->off_w[0], (int64_t)m->off_w[1], (int64_t)m->off_w[2],
+		    (int64_t)m->off_w[3], (bf16 *)m->wimg.ptr);
+		PW_CUDA(cudaGetLastError());
+		m->wimg_dirty = false;
+	}
+	static bool attr_set = false;
+	if (!attr_set) {
+		PW_CUDA(cudaFuncSetAttribute(tc::k_mlp_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                             tc::SMEM_BYTES));
+		attr_set = true;
+	}
+	tc::FwdArgs a;
+	a.states = states;
+	a.n = n;
+	a.wimg = (const bf16 *)m->wimg.ptr;
+	a.params = (const float *)m->params.ptr;
+	for (int l = 0; l < NLAYER; l++)
+		a.off_b[l] = (int64_t)m->off_b[l];
+	a.off_w5 = (int64_t)m->off_w5;
+	a.off_b5 = (int64_t)m->off_b5;
+	a.prob = prob;
+	a.err = mlp_err(m);
+	const int64_t ntiles = (n + tc::TILE_M - 1) / tc::TILE_M;
+	const unsigned grid = (unsigned)std::min<int64_t>(ntiles, m->num_sms);
+	tc::k_mlp_forward_tc<<<grid, tc::NTHREADS, tc::SMEM_BYTES, st>>>(a);
+	PW_CUDA(cudaGetLastError());
+	return PW_OK;
+}
+
+extern "C" int pw_mlp_check(pw_mlp *m)
+{
+	if (!m)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_mlp_check: NULL network");
+	PW_CUDA(cudaSetDevice(m->device));
+	PW_CUDA(cudaDeviceSynchronize());
+	int err = 0;
+	PW_CUDA(cudaMemcpy(&err, mlp_err(m), sizeof(int), cudaMemcpyDeviceToHost));
+	if (err) {
+		PW_CUDA(cudaMemset(mlp_err(m), 0, sizeof(int)));
+		return pw_fail(PW_ERR_INTERNAL, "pw_mlp: a device wait of the tcgen05 forward kernel gave up (site " +
+		                                    std::to_string(err) + ")");
+	}
+	return PW_OK;
+}
+
+// The same network through the mma.sync GEMM kernels that training uses.
+extern "C" int pw_mlp_predict_mma(pw_mlp *m, const double *states, int64_t n, float *prob, void *stream)
+{
+	if (!m || n < 0 || (n > 0 && (!states || !prob)))
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_mlp_predict_mma: bad argument");
+	if (n == 0)
+		return PW_OK;
 	PW_CUDA(cudaSetDevice(m->device));
 	cudaStream_t st = (cudaStream_t)stream;
 	const int64_t chunk = int64_t(1) << 22;
@@ -688,6 +768,7 @@ extern "C" int pw_mlp_train_step(pw_mlp *m, const double *states, const uint8_t 
 		return rc;
 	cudaStream_t st = (cudaStream_t)stream;
 	m->step++;
+	m->wimg_dirty = true;
 	const float c1 = 1.f - std::pow(m->b1, (float)m->step), c2 = 1.f - std::pow(m->b2, (float)m->step);
 	float *P = (float *)m->params.ptr, *G = (float *)m->grads.ptr, *M1 = (float *)m->m1.ptr, *M2 = (float *)m->m2.ptr;
 	for (int l = 0; l < NLAYER; l++) {

@@ -88,6 +88,21 @@ class Surrogate:
                                           _stream(q.device)), "pw_mlp_predict")
         return out
 
+    def predict_mma(self, q: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        """The same prediction through the mma.sync GEMM kernels that training uses."""
+        q = self._states(q)
+        n = q.shape[0]
+        if out is None:
+            out = torch.empty(n, dtype=torch.float32, device=q.device)
+        _lib.check(self._L.pw_mlp_predict_mma(self._h, ctypes.c_void_p(q.data_ptr()), n,
+                                              ctypes.c_void_p(out.data_ptr()), _stream(q.device)),
+                   "pw_mlp_predict_mma")
+        return out
+
+    def check(self) -> None:
+        """Synchronise; raise if a bounded device wait of an earlier predict gave up."""
+        _lib.check(self._L.pw_mlp_check(self._h), "pw_mlp_check")
+
     def _labels(self, y, n):
         if not (isinstance(y, torch.Tensor) and y.is_cuda and y.shape == (n,)):
             raise TypeError("labels must be a CUDA tensor of shape [n]")

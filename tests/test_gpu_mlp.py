@@ -67,6 +67,38 @@ def test_predict_matches_oracle(built_lib, mo, n):
     assert np.abs(got - want).max() <= 2e-3
 
 
+@pytest.mark.parametrize("n", [1, 128, 129, 300000])
+def test_tcgen05_forward_matches_mma_forward(built_lib, mo, n):
+    """The fused tcgen05 kernel (pw_mlp_predict) and the layer-by-layer mma.sync
+    kernels (pw_mlp_predict_mma) compute the same network: both against the
+    oracle, and against each other, on tile-aligned and ragged batch sizes."""
+    net = _net(7)
+    q = _states(n, 40 + n)
+    dq = torch.from_numpy(q).cuda()
+    a = net.predict(dq)
+    net.check()
+    b = net.predict_mma(dq)
+    a, b = a.cpu().numpy(), b.cpu().numpy()
+    assert np.abs(a - b).max() <= 2e-3
+    k = min(n, 2048)
+    want = mo.predict(net.params().astype(np.float64), q[:k])
+    assert np.abs(a[:k] - want).max() <= 2e-3
+
+
+def test_tcgen05_forward_after_training_step(built_lib, mo):
+    """Adam updates reach the swizzled weight images the tcgen05 kernel reads."""
+    net = _net(8)
+    q = torch.from_numpy(_states(65536, 50)).cuda()
+    y = (q[:, :3].norm(dim=1) > 0.5).to(torch.uint8)
+    net.predict(q)
+    for _ in range(3):
+        net.train_step(q, y, 1e-3)
+    a = net.predict(q[:4096]).cpu().numpy()
+    net.check()
+    want = mo.predict(net.params().astype(np.float64), q[:4096].cpu().numpy())
+    assert np.abs(a - want).max() <= 2e-3
+
+
 @pytest.mark.parametrize("n", [1000, 65536])
 def test_gradients_match_oracle(built_lib, mo, n):
     net = _net(3)
