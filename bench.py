@@ -60,7 +60,11 @@ WORKLOADS = {
     "segments": ("collision checks/sec (first-contact segment queries, interlocking tori)",
                  W.cfg_interlocking_tori, 1_000_000),
     "plate": ("collision checks/sec (is_valid_state, perforated plate vs torus knot)", W.cfg_plate_knot, 20_000_000),
+    "surrogate": ("verified collision-free samples/sec (surrogate-guided, interlocking tori)",
+                  W.cfg_interlocking_tori, 200_000_000),
 }
+# proposal network: FLOPs per scored state (9 -> 256 x4 -> 1; the padded input columns are not counted)
+MLP_FLOP_PER_ROW = 2 * (9 * 256 + 3 * 256 * 256 + 256)
 
 
 def _meshes(workload="segments"):
@@ -352,6 +356,243 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_surrogate(args):
+    """Learned proposal on the interlocking tori: train on exact labels, then
+    per step rank `n` uniform candidates with the network, check the top
+    fraction exactly and count the verified free samples.  The plain arm
+    checks every candidate exactly."""
+    import torch
+
+    import puzzletunneldiscovery_gb300 as pw
+    from puzzletunneldiscovery_gb300 import surrogate as S
+
+    ws, rank, local = _dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    Ve, Fe, Vr, Fr = _meshes("surrogate")
+    uw = pw.UnitWorld(local)
+    uw.load_env_mesh(Ve, Fe)
+    uw.load_robot_mesh(Vr, Fr)
+    uw.scaleToUnit()
+    uw.angleModel(0.0, 0.0)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(1000 + rank)
+    draw = lambda n: S.uniform_states_device(n, -2.0, 2.0, uw.scene_scale, gen, dev)  # noqa: E731
+    stream = torch.cuda.current_stream(dev)
+
+    # training on exact labels (timed as its own phase)
+    net = S.Surrogate(local, seed=rank)
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    t0.record(stream)
+    rep = S.train_online(uw, net, draw, args.train_labels, batch=65536, lr=1e-3, log_every=100)
+    t1.record(stream)
+    torch.cuda.synchronize(dev)
+    train_ms = t0.elapsed_time(t1)
+
+    cand = draw(args.n)                       # resident candidates (not timed)
+    prob = torch.empty(args.n, dtype=torch.float32, device=dev)
+    # exact labels of a 4M sample: precision / recall of the network as a free-space predictor
+    sample = cand[: 1 << 22]
+    exact = uw.is_valid_states(sample)
+    prec, rec = S.precision_recall(net.predict(sample), exact)
+    net.check()
+
+    def guided(frac=args.top_frac):
+        net.score(cand, out=prob)
+        m1.record(stream)
+        sel = S.select_top(prob, cand, int(round(frac * args.n)))
+        ok = uw.is_valid_states(sel)
+        return sel, ok
+
+    def plain():
+        return uw.is_valid_states(cand)
+
+    m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(args.warmup):
+        guided()
+        plain()
+    torch.cuda.synchronize(dev)
+    g_ms, p_ms, mlp_ms, g_free, p_free, g_checked, false_free = [], [], [], 0, 0, 0, 0
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            m0.record(stream)
+            sel, ok = guided()
+            nfree = ok.sum()
+            s1.record(stream)
+            torch.cuda.synchronize(dev)
+            g_ms.append(s0.elapsed_time(s1))
+            mlp_ms.append(m0.elapsed_time(m1))
+            g_free += int(nfree)
+            g_checked += int(sel.shape[0])
+            if i == 0:
+                # every accepted sample was checked exactly; re-check the accepted set once
+                false_free = int((~uw.is_valid_states(sel[ok])).sum())
+            s0.record(stream)
+            okp = plain()
+            nfree = okp.sum()
+            s1.record(stream)
+            torch.cuda.synchronize(dev)
+            p_ms.append(s0.elapsed_time(s1))
+            p_free += int(nfree)
+    value = g_free / (sum(g_ms) / 1e3)
+    plain_value = p_free / (sum(p_ms) / 1e3)
+    # the same pipeline at larger checked fractions (one timed step each)
+    sweep = {}
+    for frac in args.sweep:
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        s0.record(stream)
+        m0.record(stream)
+        sel, ok = guided(frac)
+        nfree = ok.sum()
+        s1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = s0.elapsed_time(s1)
+        sweep["%.2f" % frac] = {"verified_free_per_s": int(nfree) / (ms / 1e3), "ms": ms,
+                                "precision": int(nfree) / max(1, sel.shape[0]),
+                                "over_plain": int(nfree) / (ms / 1e3) / plain_value}
+
+    # end to end: candidates from pinned host memory, accepted states back to the host
+    hc = cand[: args.e2e_n].cpu().pin_memory()
+    e2e_ms, e2e_free, h2d, d2h = 0.0, 0, 0, 0
+    for i in range(args.steps):
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        dc = hc.to(dev, non_blocking=True)
+        pr = net.score(dc)
+        sel = S.select_top(pr, dc, int(round(args.top_frac * dc.shape[0])))
+        acc = sel[uw.is_valid_states(sel)]
+        hacc = acc.cpu()
+        s1.record(stream)
+        torch.cuda.synchronize(dev)
+        e2e_ms += s0.elapsed_time(s1)
+        e2e_free += hacc.shape[0]
+        h2d, d2h = hc.numel() * 8, hacc.numel() * 8
+    e2e_value = e2e_free / (e2e_ms / 1e3)
+    if rank != 0:
+        return
+
+    mlp_kernel_ms = sum(mlp_ms) / len(mlp_ms)
+    achieved = MLP_FLOP_PER_ROW * args.n / (mlp_kernel_ms / 1e3) / 1e12
+    peak, peak_kind = _bf16_peak()
+    traffic = None
+    tpr = _profile_value("k_mlp_forward_tc_traffic.txt", "dram_bytes_per_row")
+    if tpr is not None:
+        traffic = tpr * args.n
+    roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "traffic": traffic, "kernel": "k_mlp_forward_tc", "kernel_ms": mlp_kernel_ms,
+            "peak_source": peak_kind, "algorithmic_flop": MLP_FLOP_PER_ROW * args.n}
+    cpu = None
+    if ws == 1 and not args.no_cpu_baseline:
+        cpu = _cpu_plain_sampling(uw.scene_scale, args.cpu_seconds)
+    line = {"metric": WORKLOADS["surrogate"][0], "value": value, "unit": "samples/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(g_ms) / len(g_ms),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 network (f32 accumulate) + f32/f64 exact checks",
+            "data": "synthetic (seeded uniform states on the device)",
+            "config": {"workload": "surrogate_guided_sampling/interlocking_tori", "candidates_per_step": args.n,
+                       "top_fraction": args.top_frac, "train_labels": args.train_labels, "batch": 65536,
+                       "lr": 1e-3, "network": "9 -> 256x4 SiLU -> 1 sigmoid, BF16",
+                       "l2": "per-step working set (11 GB of candidates) > L2",
+                       "parallelism": "replicas" if ws == 1 else "independent replicas"},
+            "roofline": roof, "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "candidates_per_step": args.e2e_n},
+            "clocks": clk.summary(),
+            "gpu_launches": 7 * args.steps,
+            "detail": {"plain_verified_free_per_s": plain_value, "guided_over_plain": value / plain_value,
+                       "plain_ms_per_step": sum(p_ms) / len(p_ms), "guided_ms_per_step": sum(g_ms) / len(g_ms),
+                       "mlp_ms_per_step": mlp_kernel_ms, "mlp_rows_per_s": args.n / (mlp_kernel_ms / 1e3),
+                       "checked_per_step": g_checked / args.steps,
+                       "precision_top_fraction": g_free / max(1, g_checked),
+                       "plain_free_fraction": p_free / (args.n * args.steps),
+                       "precision_at_0.5": prec, "recall_at_0.5": rec, "false_free_accepted": false_free,
+                       "train_ms": train_ms, "train_steps": rep.steps,
+                       "train_labels_per_s": rep.labels / (train_ms / 1e3),
+                       "train_loss_first_last": [rep.losses[0][1], rep.losses[-1][1]] if rep.losses else None,
+                       "top_fraction_sweep": sweep}}
+    print(json.dumps(line))
+
+
+def _bf16_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            p = json.load(fh)
+        return float(p["bf16_tflops_sustained"]), "measured (sustained)"
+    except Exception:
+        return 1700.0, "fallback (sustained)"
+
+
+def _cpu_plain_sampling(scale, target_s):
+    """Plain uniform sampling on the host cores: the oracle's isValid on uniform
+    states, counting the free ones (the reference's sampler has no surrogate)."""
+    from oracle import oracle as O
+    O.build()
+    Ve, Fe, Vr, Fr = _meshes("surrogate")
+    ow = O.OracleWorld(Ve, Fe, Vr, Fr)
+    cores = os.cpu_count() or 1
+    n = 65536
+    while True:
+        q = W.uniform_states(n, -2.0, 2.0, scale, seed=77)
+        t0 = time.perf_counter()
+        v = ow.is_valid(q, nthreads=cores)
+        dt = time.perf_counter() - t0
+        if dt >= target_s or n >= 1 << 26:
+            break
+        n = min(1 << 26, max(n * 2, int(n * target_s / max(dt, 1e-3) * 1.1)))
+    return {"value": float(v.sum()) / dt, "unit": "samples/s", "cores": cores, "kind": "port",
+            "sample": "%d uniform states checked, %d free, %.1f s" % (n, int(v.sum()), dt)}
+
+
+def run_surrogate_reference(args):
+    """--impl reference for the surrogate workload: plain uniform sampling with the
+    CPU restatement of the reference's isValid on all host cores."""
+    ws, rank, _ = _dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    Ve, Fe, Vr, Fr = _meshes("surrogate")
+    ow = O.OracleWorld(Ve, Fe, Vr, Fr)
+    cores = os.cpu_count() or 1
+    sample = 200 * args.ref_sample
+    times, free = [], 0
+    for it in range(args.warmup + args.steps):
+        q = W.uniform_states(sample, -2.0, 2.0, ow.scene_scale, seed=500 + it)
+        t0 = time.perf_counter()
+        v = ow.is_valid(q, nthreads=cores)
+        dt = time.perf_counter() - t0
+        if it >= args.warmup:
+            times.append(dt)
+            free += int(v.sum())
+    value = free / sum(times)
+    line = {"impl": "reference", "metric": WORKLOADS["surrogate"][0], "value": value, "unit": "samples/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform states)",
+            "config": {"workload": "surrogate_guided_sampling/interlocking_tori", "candidates_per_step": sample,
+                       "method": "plain uniform sampling (the reference has no surrogate)"},
+            "cpu_baseline": {"value": value, "unit": "samples/s", "cores": cores, "kind": "port",
+                             "sample": "%d uniform states per step" % sample},
+            "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def _profile_value(name, key):
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(path):
+            if line.startswith(key):
+                return float(line.split("=")[1])
+    except Exception:
+        pass
+    return None
+
+
 def _traffic_per_segment():
     """DRAM bytes per segment of the traversal kernel, from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "k_segments_traffic.txt")
@@ -375,10 +616,18 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=400, help="segments per reference-arm step")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--train-labels", type=int, default=50_000_000, help="surrogate: exact labels to train on")
+    ap.add_argument("--top-frac", type=float, default=0.1, help="surrogate: fraction of candidates checked")
+    ap.add_argument("--e2e-n", type=int, default=20_000_000, help="surrogate: candidates per end-to-end step")
+    ap.add_argument("--sweep", type=lambda v: [float(x) for x in v.split(",") if x], default=[0.25, 0.5, 0.6],
+                    help="surrogate: further checked fractions reported in detail")
     args = ap.parse_args()
     if args.n is None:
         args.n = WORKLOADS[args.workload][2]
-    if args.impl == "reference":
+    if args.workload == "surrogate":
+        args.e2e_n = min(args.e2e_n, args.n)
+        run_surrogate_reference(args) if args.impl == "reference" else run_surrogate(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

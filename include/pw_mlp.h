@@ -53,6 +53,10 @@ PW_API int pw_mlp_get_grads(const pw_mlp *m, float *host_out);
  * pw_mlp_check reports whether one gave up. */
 PW_API int pw_mlp_predict(pw_mlp *m, const double *states, int64_t n, float *prob, void *stream);
 
+/* The logit of the same network (the score before the sigmoid): a ranking
+ * score that does not saturate, for pw_select_top.  Same kernel as pw_mlp_predict. */
+PW_API int pw_mlp_score(pw_mlp *m, const double *states, int64_t n, float *logit, void *stream);
+
 /* The same prediction through the mma.sync GEMM kernels that training uses
  * (a cross-check of pw_mlp_predict; layer by layer, activations through HBM). */
 PW_API int pw_mlp_predict_mma(pw_mlp *m, const double *states, int64_t n, float *prob, void *stream);
@@ -60,6 +64,14 @@ PW_API int pw_mlp_predict_mma(pw_mlp *m, const double *states, int64_t n, float 
 /* host: synchronises the device; PW_ERR_INTERNAL if a bounded device wait of an
  * earlier pw_mlp_predict gave up (its probabilities are then invalid). */
 PW_API int pw_mlp_check(pw_mlp *m);
+
+/* host: the states whose score is at or above the k-th largest score (any
+ * finite floats, e.g. pw_mlp_score output), gathered into out_states (device,
+ * [capacity x 7], in no particular order); *out_count = how many (k plus ties
+ * at the threshold).  PW_ERR_CAPACITY if that exceeds capacity.  Synchronises
+ * the stream. */
+PW_API int pw_select_top(const float *score, const double *states, int64_t n, int64_t k, double *out_states,
+                         int64_t capacity, int64_t *out_count, void *stream);
 
 /* Gradients of the mean binary cross-entropy over one batch (device states,
  * device uint8 labels, 1 = free) into the gradient block; no update.

@@ -399,6 +399,62 @@ __global__ void k_to_bf16(const float *w, int64_t n, bf16 *wb, bf16 *wbt, int ro
 
 #include "pw_mlp_tc.cuh"
 
+// ------------------------------------------------------------------ top-k selection
+//
+// Scores are floats mapped to 32-bit keys that order like the values (sign
+// bit flipped for non-negative values, all bits flipped for negative ones).
+// Three histogram passes over 11, 11 and 10 bits of the key (block-private
+// shared-memory counters) find the key of the k-th largest score exactly; a
+// compaction pass gathers the states at or above it.
+__device__ __forceinline__ uint32_t score_key(float v)
+{
+	const uint32_t b = __float_as_uint(v);
+	return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+constexpr int SEL_BITS[3] = { 11, 11, 10 };
+constexpr int SEL_SHIFT[3] = { 21, 10, 0 };
+
+__global__ void k_score_hist(const float *score, int64_t n, int shift, int bits, uint32_t prefix, int prefix_shift,
+                             unsigned long long *hist)
+{
+	__shared__ unsigned int sh[2048];
+	const int nb = 1 << bits;
+	for (int i = threadIdx.x; i < nb; i += blockDim.x)
+		sh[i] = 0;
+	__syncthreads();
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const uint32_t b = score_key(score[i]);
+		if (prefix_shift >= 32 || (b >> prefix_shift) == prefix)
+			atomicAdd(&sh[(b >> shift) & (nb - 1)], 1u);
+	}
+	__syncthreads();
+	for (int i = threadIdx.x; i < nb; i += blockDim.x)
+		if (sh[i])
+			atomicAdd(&hist[i], (unsigned long long)sh[i]);
+}
+
+__global__ void k_select_states(const float *score, const double *states, int64_t n, uint32_t thr_bits,
+                                double *out, int64_t capacity, unsigned long long *count)
+{
+	const int lane = threadIdx.x & 31;
+	for (int64_t base = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) - lane; base < n;
+	     base += (int64_t)gridDim.x * blockDim.x) {
+		const int64_t i = base + lane;
+		const bool take = i < n && score_key(score[i]) >= thr_bits;
+		const unsigned mask = __ballot_sync(0xffffffffu, take);
+		unsigned long long at = 0;
+		if (lane == 0 && mask)
+			at = atomicAdd(count, (unsigned long long)__popc(mask));
+		at = __shfl_sync(0xffffffffu, at, 0);
+		if (take) {
+			const int64_t o = (int64_t)at + __popc(mask & ((1u << lane) - 1));
+			if (o < capacity)
+				for (int c = 0; c < 7; c++)
+					out[7 * o + c] = states[7 * i + c];
+		}
+	}
+}
+
 } // namespace
 
 // ------------------------------------------------------------------ the network object
@@ -593,11 +649,23 @@ static int mlp_forward(pw_mlp *m, const double *states, int64_t n, cudaStream_t 
 
 static int *mlp_err(pw_mlp *m) { return (int *)((char *)m->misc.ptr + 16); }
 
-// P(free) of n states on the tcgen05 tensor cores (one fused persistent kernel).
+static int mlp_forward_tc(pw_mlp *m, const double *states, int64_t n, float *prob, int logits, void *stream);
+
 extern "C" int pw_mlp_predict(pw_mlp *m, const double *states, int64_t n, float *prob, void *stream)
 {
+	return mlp_forward_tc(m, states, n, prob, 0, stream);
+}
+
+extern "C" int pw_mlp_score(pw_mlp *m, const double *states, int64_t n, float *logit, void *stream)
+{
+	return mlp_forward_tc(m, states, n, logit, 1, stream);
+}
+
+// P(free) (or the logit) of n states on the tcgen05 tensor cores (one fused persistent kernel).
+static int mlp_forward_tc(pw_mlp *m, const double *states, int64_t n, float *prob, int logits, void *stream)
+{
 	if (!m || n < 0 || (n > 0 && (!states || !prob)))
-		return pw_fail(PW_ERR_INVALID_ARG, "pw_mlp_predict: bad argument");
+		return pw_fail(PW_ERR_INVALID_ARG, logits ? "pw_mlp_score: bad argument" : "pw_mlp_predict: bad argument");
 	if (n == 0)
 		return PW_OK;
 	PW_CUDA(cudaSetDevice(m->device));
@@ -627,11 +695,65 @@ extern "C" int pw_mlp_predict(pw_mlp *m, const double *states, int64_t n, float 
 	a.off_w5 = (int64_t)m->off_w5;
 	a.off_b5 = (int64_t)m->off_b5;
 	a.prob = prob;
+	a.logits = logits;
 	a.err = mlp_err(m);
 	const int64_t ntiles = (n + tc::TILE_M - 1) / tc::TILE_M;
 	const unsigned grid = (unsigned)std::min<int64_t>(ntiles, m->num_sms);
 	tc::k_mlp_forward_tc<<<grid, tc::NTHREADS, tc::SMEM_BYTES, st>>>(a);
 	PW_CUDA(cudaGetLastError());
+	return PW_OK;
+}
+
+extern "C" int pw_select_top(const float *score, const double *states, int64_t n, int64_t k, double *out_states,
+                             int64_t capacity, int64_t *out_count, void *stream)
+{
+	if (n < 0 || k < 0 || capacity < 0 || !out_count || (n > 0 && (!score || !states)) ||
+	    (capacity > 0 && !out_states))
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_select_top: bad argument");
+	*out_count = 0;
+	if (n == 0 || k == 0)
+		return PW_OK;
+	k = std::min(k, n);
+	cudaStream_t st = (cudaStream_t)stream;
+	int dev = 0, sms = 1;
+	PW_CUDA(cudaGetDevice(&dev));
+	PW_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+	DeviceBuffer hist;
+	PW_CUDA(hist.reserve(sizeof(unsigned long long) * (2048 + 1)));
+	unsigned long long *dh = (unsigned long long *)hist.ptr;
+	std::vector<unsigned long long> h(2048);
+	const unsigned grid = (unsigned)std::min<int64_t>((n + 255) / 256, (int64_t)sms * 8);
+	uint32_t prefix = 0;   // bits of the k-th largest score found so far
+	int64_t above = 0;     // scores strictly above the current prefix range
+	for (int pass = 0; pass < 3; pass++) {
+		const int nb = 1 << SEL_BITS[pass];
+		const int pshift = SEL_SHIFT[pass] + SEL_BITS[pass];   // bits above this pass
+		PW_CUDA(cudaMemsetAsync(dh, 0, sizeof(unsigned long long) * nb, st));
+		k_score_hist<<<grid, 256, 0, st>>>(score, n, SEL_SHIFT[pass], SEL_BITS[pass], prefix, pass == 0 ? 32 : pshift,
+		                                   dh);
+		PW_CUDA(cudaGetLastError());
+		PW_CUDA(cudaMemcpyAsync(h.data(), dh, sizeof(unsigned long long) * nb, cudaMemcpyDeviceToHost, st));
+		PW_CUDA(cudaStreamSynchronize(st));
+		int b = nb - 1;
+		for (; b > 0; b--) {
+			if (above + (int64_t)h[b] >= k)
+				break;
+			above += (int64_t)h[b];
+		}
+		prefix = (prefix << SEL_BITS[pass]) | (uint32_t)b;
+	}
+	const uint32_t thr = prefix;
+	unsigned long long *dc = dh + 2048;
+	PW_CUDA(cudaMemsetAsync(dc, 0, sizeof(unsigned long long), st));
+	k_select_states<<<grid, 256, 0, st>>>(score, states, n, thr, out_states, capacity, dc);
+	PW_CUDA(cudaGetLastError());
+	unsigned long long cnt = 0;
+	PW_CUDA(cudaMemcpyAsync(&cnt, dc, sizeof(cnt), cudaMemcpyDeviceToHost, st));
+	PW_CUDA(cudaStreamSynchronize(st));
+	*out_count = (int64_t)cnt;
+	if ((int64_t)cnt > capacity)
+		return pw_fail(PW_ERR_CAPACITY, "pw_select_top: " + std::to_string(cnt) + " states tie at or above the "
+		                                    "k-th score; capacity " + std::to_string(capacity));
 	return PW_OK;
 }
 

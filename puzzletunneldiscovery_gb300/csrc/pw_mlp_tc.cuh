@@ -1,19 +1,22 @@
 // pw_mlp_tc.cuh -- fused forward pass of the proposal network on the 5th-generation
 // tensor cores (tcgen05 + tensor memory), sm_103a.  Included by pw_mlp.cu inside
-// its anonymous namespace (uses H, KIN, bf16, silu, feature_row).
+// its anonymous namespace (uses H, KIN, bf16, tanh_fast, feature_row).
 //
-// One persistent CTA per SM walks 128-row tiles of states.  Per tile:
-//   features -> act (smem, BF16)            epilogue warps
-//   L1: act x W1^T -> acc0 (TMEM, FP32)     MMA thread, 1 instruction (K = 16)
-//   E1: acc0 + b1, SiLU -> act              epilogue warps, 64 columns at a time
-//   L2: act x W2^T -> acc1                  MMA thread, K-block j starts as soon as
-//   E2 ...                                  E1 has written K-block j of act
-//   L4 -> acc1; E4: SiLU, dot with w5, sigmoid -> prob
-// Layers alternate between two 256-column accumulators so that the MMAs of
-// layer l+1 run while the epilogue still reads layer l's accumulator.
-// Weights stream through a 4-stage ring of 32 KB K-blocks (256 rows x 64 k),
-// each a single bulk copy of an image that is already in the 128-byte-swizzle
-// layout the MMA reads (built by k_weight_image).
+// One persistent CTA per SM walks pairs of 128-row tiles of states (slots A
+// and B).  Each slot owns one 64 KB activation buffer (shared memory, BF16,
+// 128-byte swizzle) and one 256-column FP32 accumulator in tensor memory.
+// Per slot and layer l:
+//   MMA thread: act x W_l^T -> acc (K-blocks of 64, streamed weight blocks)
+//   epilogue warps: acc + b_l -> SiLU -> act (BF16), for layers 1..3;
+//                   layer 4: SiLU, dot with w5, + b5 -> logit or sigmoid
+// The MMA thread issues A(l), B(l), A(l+1), B(l+1), ... so the epilogue of one
+// slot runs while the tensor cores work on the other.
+// Weights are stored pre-scaled by 1/2 (exact in BF16 and FP32), so the
+// accumulator holds h = z / 2 and SiLU(z) = h + h tanh(h) costs one FADD (bias),
+// one MUFU and one FFMA per element.
+// Weights stream through a 3-stage ring of 32 KB blocks (256 rows x 64 k), each
+// one bulk copy of an image already in the swizzled layout the MMA reads
+// (built by k_weight_image).
 //
 // Roles (576 threads): warp 0 = weight producer and TMEM owner, warp 1 = MMA
 // issuer, warps 2..17 = epilogue (warp w reads TMEM lanes 32 (w % 4) ..).
@@ -25,28 +28,27 @@ namespace tc {
 
 constexpr int TILE_M = 128;
 constexpr int KB = 64;                        // k per weight block / act K-block
-constexpr int NSTAGE = 4;
+constexpr int NSTAGE = 3;
 constexpr int WBLOCK_BYTES = H * KB * 2;      // 32 KB: 256 rows x 128 bytes
 constexpr int NWBLOCK = 1 + 3 * (H / KB);     // W1 (one block) + 4 blocks for each of W2..W4
 constexpr int ACT_KB_BYTES = TILE_M * KB * 2; // 16 KB per act K-block
+constexpr int ACT_BYTES = 4 * ACT_KB_BYTES;   // 64 KB per slot
 constexpr int NEPI_WARPS = 16;
 constexpr int NTHREADS = (2 + NEPI_WARPS) * 32;
 constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;   // 2 s per wait
 
 // shared-memory map (offsets from a 1024-byte aligned base)
-constexpr int SM_ACT = 0;                                        // 4 x 16 KB
-constexpr int SM_W = SM_ACT + 4 * ACT_KB_BYTES;                  // NSTAGE x 32 KB
-constexpr int SM_BIAS = SM_W + NSTAGE * WBLOCK_BYTES;            // 4 x 256 floats
-constexpr int SM_W5 = SM_BIAS + 4 * H * 4;                       // 256 floats + b5
-constexpr int SM_PART = SM_W5 + (H + 4) * 4;                     // 4 x 128 floats (head partial sums)
-constexpr int SM_BAR = SM_PART + 4 * TILE_M * 4;                 // mbarriers
-constexpr int NBAR = 2 * NSTAGE + 4 + 2 + 1 + 1;                 // full, empty, act, done, head, final
+constexpr int SM_ACT = 0;                                        // 2 slots x 64 KB
+constexpr int SM_W = SM_ACT + 2 * ACT_BYTES;                     // NSTAGE x 32 KB
+constexpr int SM_BAR = SM_W + NSTAGE * WBLOCK_BYTES;             // mbarriers
+constexpr int NBAR = 2 * NSTAGE + 2 + 2 + 2 + 1;                 // full, empty, act, done, head, final
 constexpr int SM_MISC = SM_BAR + NBAR * 8;                       // tmem base, abort flag
 constexpr int SMEM_BYTES = SM_MISC + 16 + 1024;                  // + alignment slack
+static_assert(SMEM_BYTES <= 232448, "shared memory budget of one CTA");
 
-// barrier indices
-constexpr int B_FULL = 0, B_EMPTY = NSTAGE, B_ACT = 2 * NSTAGE, B_DONE = B_ACT + 4, B_HEAD = B_DONE + 2,
-              B_FINAL = B_HEAD + 1;
+// barrier indices (act, done, head: one per slot)
+constexpr int B_FULL = 0, B_EMPTY = NSTAGE, B_ACT = 2 * NSTAGE, B_DONE = B_ACT + 2, B_HEAD = B_DONE + 2,
+              B_FINAL = B_HEAD + 2;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -171,11 +173,12 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b)
 struct FwdArgs {
 	const double *states;
 	int64_t n;
-	const bf16 *wimg;        // NWBLOCK images of WBLOCK_BYTES
+	const bf16 *wimg;        // NWBLOCK images of WBLOCK_BYTES (weights scaled by 1/2)
 	const float *params;     // FP32 parameter block
 	int64_t off_b[4];
 	int64_t off_w5, off_b5;
 	float *prob;
+	int logits;              // 1: write the logit (a ranking score that does not saturate) instead of P(free)
 	int *err;
 };
 
@@ -184,30 +187,24 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 	extern __shared__ uint8_t smem_raw[];
 	uint8_t *sm = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
 	const uint32_t sbase = smem_u32(sm);
-	float *s_bias = (float *)(sm + SM_BIAS);
-	float *s_w5 = (float *)(sm + SM_W5);
-	float *s_part = (float *)(sm + SM_PART);
 	uint32_t *s_tmem = (uint32_t *)(sm + SM_MISC);
 	volatile int *s_abort = (volatile int *)(sm + SM_MISC + 4);
 	auto bar = [&](int i) { return sbase + SM_BAR + 8 * i; };
 
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	const int64_t ntiles = (a.n + TILE_M - 1) / TILE_M;
+	const int64_t G = gridDim.x;
 
-	for (int i = threadIdx.x; i < 4 * H; i += NTHREADS)
-		s_bias[i] = a.params[a.off_b[i / H] + (i % H)];
-	for (int i = threadIdx.x; i < H + 1; i += NTHREADS)
-		s_w5[i] = i < H ? a.params[a.off_w5 + i] : a.params[a.off_b5];
 	if (threadIdx.x == 0) {
 		for (int s = 0; s < NSTAGE; s++) {
 			mbar_init(bar(B_FULL + s), 1);
 			mbar_init(bar(B_EMPTY + s), 1);
 		}
-		for (int j = 0; j < 4; j++)
-			mbar_init(bar(B_ACT + j), NEPI_WARPS);
-		mbar_init(bar(B_DONE + 0), 1);
-		mbar_init(bar(B_DONE + 1), 1);
-		mbar_init(bar(B_HEAD), NEPI_WARPS);
+		for (int sl = 0; sl < 2; sl++) {
+			mbar_init(bar(B_ACT + sl), NEPI_WARPS);
+			mbar_init(bar(B_DONE + sl), 1);
+			mbar_init(bar(B_HEAD + sl), NEPI_WARPS);
+		}
 		mbar_init(bar(B_FINAL), 1);
 		*s_abort = 0;
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -223,25 +220,31 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 	const uint32_t tmem = *s_tmem;
 
 	if (warp == 0) {
-		// ---------------- weight producer
+		// ---------------- weight producer: per pair, per layer, per live slot, the layer's blocks
 		if (lane == 0) {
 			uint32_t it = 0;
 			int64_t last_it[NSTAGE];
 			for (int s = 0; s < NSTAGE; s++)
 				last_it[s] = -1;
 			bool ok = true;
-			for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-				for (int b = 0; b < NWBLOCK; b++, it++) {
-					const int s = it % NSTAGE;
-					if (!mbar_wait(bar(B_EMPTY + s), ((it / NSTAGE) & 1) ^ 1, s_abort, a.err, 1)) {
-						ok = false;
-						break;
+			for (int64_t tA = blockIdx.x; tA < ntiles && ok; tA += 2 * G) {
+				const int nslot = tA + G < ntiles ? 2 : 1;
+				for (int layer = 0; layer < 4 && ok; layer++)
+					for (int sl = 0; sl < nslot && ok; sl++) {
+						const int b0 = layer == 0 ? 0 : 1 + 4 * (layer - 1), nb = layer == 0 ? 1 : 4;
+						for (int b = b0; b < b0 + nb; b++, it++) {
+							const int s = it % NSTAGE;
+							if (!mbar_wait(bar(B_EMPTY + s), ((it / NSTAGE) & 1) ^ 1, s_abort, a.err, 1)) {
+								ok = false;
+								break;
+							}
+							mbar_expect_tx(bar(B_FULL + s), WBLOCK_BYTES);
+							bulk_g2s(sbase + SM_W + s * WBLOCK_BYTES,
+							         (const uint8_t *)a.wimg + (size_t)b * WBLOCK_BYTES, WBLOCK_BYTES,
+							         bar(B_FULL + s));
+							last_it[s] = it;
+						}
 					}
-					mbar_expect_tx(bar(B_FULL + s), WBLOCK_BYTES);
-					bulk_g2s(sbase + SM_W + s * WBLOCK_BYTES, (const uint8_t *)a.wimg + (size_t)b * WBLOCK_BYTES,
-					         WBLOCK_BYTES, bar(B_FULL + s));
-					last_it[s] = it;
-				}
 			}
 			// copies in flight must land before the CTA leaves
 			for (int s = 0; s < NSTAGE; s++)
@@ -251,31 +254,39 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 	} else if (warp == 1) {
 		// ---------------- MMA issuer
 		if (lane == 0) {
-			uint32_t it = 0, act_ph[4] = { 0, 0, 0, 0 };
+			uint32_t it = 0, act_ph[2] = { 0, 0 };
 			bool ok = true;
-			for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-				for (int layer = 0; layer < 4 && ok; layer++) {
-					const uint32_t acc = tmem + (uint32_t)((layer & 1) * 256);
-					const int nkb = layer == 0 ? 1 : 4;
-					for (int j = 0; j < nkb; j++, it++) {
-						const int s = it % NSTAGE;
-						if (!mbar_wait(bar(B_FULL + s), (it / NSTAGE) & 1, s_abort, a.err, 2) ||
-						    !mbar_wait(bar(B_ACT + j), act_ph[j], s_abort, a.err, 3)) {
+			for (int64_t tA = blockIdx.x; tA < ntiles && ok; tA += 2 * G) {
+				const int nslot = tA + G < ntiles ? 2 : 1;
+				for (int layer = 0; layer < 4 && ok; layer++)
+					for (int sl = 0; sl < nslot && ok; sl++) {
+						// the slot's activations of this layer are in shared memory
+						if (!mbar_wait(bar(B_ACT + sl), act_ph[sl], s_abort, a.err, 3)) {
 							ok = false;
 							break;
 						}
-						act_ph[j] ^= 1;
+						act_ph[sl] ^= 1;
 						tc_fence_after();
-						const uint32_t abase = sbase + SM_ACT + j * ACT_KB_BYTES;
-						const uint32_t bbase = sbase + SM_W + s * WBLOCK_BYTES;
-						const int nk = layer == 0 ? 1 : KB / 16;
-						for (int k = 0; k < nk; k++)
-							mma_bf16_ss(acc, sdesc(abase + 32 * k), sdesc(bbase + 32 * k), (j | k) != 0);
-						mma_commit(bar(B_EMPTY + s));
+						const uint32_t acc = tmem + (uint32_t)(sl * 256);
+						const uint32_t act = sbase + SM_ACT + sl * ACT_BYTES;
+						const int nkb = layer == 0 ? 1 : 4;
+						for (int j = 0; j < nkb; j++, it++) {
+							const int s = it % NSTAGE;
+							if (!mbar_wait(bar(B_FULL + s), (it / NSTAGE) & 1, s_abort, a.err, 2)) {
+								ok = false;
+								break;
+							}
+							tc_fence_after();
+							const uint32_t abase = act + j * ACT_KB_BYTES;
+							const uint32_t bbase = sbase + SM_W + s * WBLOCK_BYTES;
+							const int nk = layer == 0 ? 1 : KB / 16;
+							for (int k = 0; k < nk; k++)
+								mma_bf16_ss(acc, sdesc(abase + 32 * k), sdesc(bbase + 32 * k), (j | k) != 0);
+							mma_commit(bar(B_EMPTY + s));
+						}
+						if (ok)
+							mma_commit(bar(B_DONE + sl));
 					}
-					if (ok)
-						mma_commit(bar(B_DONE + (layer & 1)));
-				}
 			}
 			// every MMA issued so far completes before the tensor memory is freed
 			mma_commit(bar(B_FINAL));
@@ -288,90 +299,103 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 		const int g = e >> 2;
 		const int r = q * 32 + lane;                  // tile row of this thread
 		const uint32_t lane_off = (uint32_t)(q * 32) << 16;
-		uint32_t done_ph[2] = { 0, 0 }, head_ph = 0;
+		uint32_t done_ph[2] = { 0, 0 }, head_ph[2] = { 0, 0 };
+		const float b5 = a.params[a.off_b5];
 		bool ok = true;
-		for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-			const int64_t row = t * TILE_M + r;
-			// features of this tile into act K-block 0 (chunks 0 and 1 of each row)
-			if (g == 0) {
-				uint4 c0 = make_uint4(0, 0, 0, 0), c1 = c0;
-				if (row < a.n) {
-					__align__(16) bf16 f[16];
-					feature_row(a.states + 7 * row, f);
-					c0 = *reinterpret_cast<uint4 *>(f);
-					c1 = *reinterpret_cast<uint4 *>(f + 8);
-				}
-				*reinterpret_cast<uint4 *>(sm + SM_ACT + swz(r, 0)) = c0;
-				*reinterpret_cast<uint4 *>(sm + SM_ACT + swz(r, 1)) = c1;
-			}
-			fence_async_smem();
-			__syncwarp();
-			if (lane == 0)
-				mbar_arrive(bar(B_ACT + 0));
-			float head = 0.f;
-			for (int layer = 0; layer < 4; layer++) {
-				const int ai = layer & 1;
-				if (!mbar_wait(bar(B_DONE + ai), done_ph[ai], s_abort, a.err, 4)) {
-					ok = false;
-					break;
-				}
-				done_ph[ai] ^= 1;
-				tc_fence_after();
-				const float *bias = s_bias + layer * H;
-				for (int j = 0; j < 4; j++) {
-					const int col = j * KB + g * 16;
-					float v[16];
-					tmem_ld16(tmem + lane_off + (uint32_t)(ai * 256 + col), v);
-					uint32_t pk[8];
-#pragma unroll
-					for (int i = 0; i < 16; i += 2) {
-						const float h0 = silu(v[i] + bias[col + i]);
-						const float h1 = silu(v[i + 1] + bias[col + i + 1]);
-						pk[i / 2] = pack_bf16x2(h0, h1);
+		for (int64_t tA = blockIdx.x; tA < ntiles && ok; tA += 2 * G) {
+			const int nslot = tA + G < ntiles ? 2 : 1;
+			// features of both tiles into act K-block 0 (chunks 0 and 1 of each row)
+			for (int sl = 0; sl < nslot; sl++) {
+				const int64_t row = (tA + sl * G) * TILE_M + r;
+				if (g == 0) {
+					uint4 c0 = make_uint4(0, 0, 0, 0), c1 = c0;
+					if (row < a.n) {
+						__align__(16) bf16 f[16];
+						feature_row(a.states + 7 * row, f);
+						c0 = *reinterpret_cast<uint4 *>(f);
+						c1 = *reinterpret_cast<uint4 *>(f + 8);
 					}
-					if (layer < 3) {
-						uint8_t *kb = sm + SM_ACT + j * ACT_KB_BYTES;
-						*reinterpret_cast<uint4 *>(kb + swz(r, 2 * g)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-						*reinterpret_cast<uint4 *>(kb + swz(r, 2 * g + 1)) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
-						fence_async_smem();
-						tc_fence_before();
-						__syncwarp();
-						if (lane == 0)
-							mbar_arrive(bar(B_ACT + j));
-					} else {
+					uint8_t *act = sm + SM_ACT + sl * ACT_BYTES;
+					*reinterpret_cast<uint4 *>(act + swz(r, 0)) = c0;
+					*reinterpret_cast<uint4 *>(act + swz(r, 1)) = c1;
+				}
+				fence_async_smem();
+				__syncwarp();
+				if (lane == 0)
+					mbar_arrive(bar(B_ACT + sl));
+			}
+			for (int layer = 0; layer < 4 && ok; layer++) {
+				const float *bias = a.params + a.off_b[layer];
+				for (int sl = 0; sl < nslot; sl++) {
+					if (!mbar_wait(bar(B_DONE + sl), done_ph[sl], s_abort, a.err, 4)) {
+						ok = false;
+						break;
+					}
+					done_ph[sl] ^= 1;
+					tc_fence_after();
+					uint8_t *act = sm + SM_ACT + sl * ACT_BYTES;
+					float head = 0.f;
+					for (int j = 0; j < 4; j++) {
+						const int col = j * KB + g * 16;
+						float v[16];
+						tmem_ld16(tmem + lane_off + (uint32_t)(sl * 256 + col), v);
+						uint32_t pk[8];
 #pragma unroll
-						for (int i = 0; i < 8; i++) {
-							const __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162 *>(&pk[i]);
-							head = fmaf(__low2float(h), s_w5[col + 2 * i], head);
-							head = fmaf(__high2float(h), s_w5[col + 2 * i + 1], head);
+						for (int i = 0; i < 16; i += 2) {
+							const float h0 = v[i] + 0.5f * __ldg(bias + col + i);
+							const float h1 = v[i + 1] + 0.5f * __ldg(bias + col + i + 1);
+							pk[i / 2] = pack_bf16x2(fmaf(h0, tanh_fast(h0), h0), fmaf(h1, tanh_fast(h1), h1));
+						}
+						if (layer < 3) {
+							uint8_t *kb = act + j * ACT_KB_BYTES;
+							*reinterpret_cast<uint4 *>(kb + swz(r, 2 * g)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+							*reinterpret_cast<uint4 *>(kb + swz(r, 2 * g + 1)) =
+							    make_uint4(pk[4], pk[5], pk[6], pk[7]);
+						} else {
+							const float *w5 = a.params + a.off_w5 + col;
+#pragma unroll
+							for (int i = 0; i < 8; i++) {
+								const __nv_bfloat162 hh = *reinterpret_cast<__nv_bfloat162 *>(&pk[i]);
+								head = fmaf(__low2float(hh), __ldg(w5 + 2 * i), head);
+								head = fmaf(__high2float(hh), __ldg(w5 + 2 * i + 1), head);
+							}
 						}
 					}
+					tc_fence_before();
+					if (layer < 3) {
+						// the whole accumulator is read and the next layer's input written
+						fence_async_smem();
+						__syncwarp();
+						if (lane == 0)
+							mbar_arrive(bar(B_ACT + sl));
+						continue;
+					}
+					// head: the accumulator is read and the act buffer is free (all MMAs of the
+					// slot are complete), so its first 2 KB hold the column-group partial sums
+					float *part = (float *)act;
+					part[g * TILE_M + r] = head;
+					__syncwarp();
+					if (lane == 0)
+						mbar_arrive(bar(B_HEAD + sl));
+					if (g == 0) {
+						if (!mbar_wait(bar(B_HEAD + sl), head_ph[sl], s_abort, a.err, 5)) {
+							ok = false;
+							break;
+						}
+						const float s = part[r] + part[TILE_M + r] + part[2 * TILE_M + r] + part[3 * TILE_M + r] + b5;
+						const int64_t row = (tA + sl * G) * TILE_M + r;
+						if (row < a.n)
+							a.prob[row] = a.logits ? s : 1.f / (1.f + __expf(-s));
+					}
+					head_ph[sl] ^= 1;
 				}
 			}
-			if (!ok)
-				break;
-			// head: sum the four column groups of each row, add b5, sigmoid
-			tc_fence_before();
-			s_part[g * TILE_M + r] = head;
-			__syncwarp();
-			if (lane == 0)
-				mbar_arrive(bar(B_HEAD));
-			if (g == 0) {
-				if (!mbar_wait(bar(B_HEAD), head_ph, s_abort, a.err, 5)) {
-					ok = false;
-					break;
-				}
-				const float s = s_part[r] + s_part[TILE_M + r] + s_part[2 * TILE_M + r] + s_part[3 * TILE_M + r] +
-				                s_w5[H];
-				if (row < a.n)
-					a.prob[row] = 1.f / (1.f + __expf(-s));
-			}
-			head_ph ^= 1;
 		}
 	}
 	tc_fence_before();
 	__syncthreads();
 	if (warp == 0) {
+		__syncwarp();
 		tc_fence_after();
 		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
 	}
@@ -379,7 +403,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 
 // Weight images for the kernel above: block 0 = W1 (256 x 16, zero-padded to
 // k = 64), blocks 1 + 4 (l - 1) + j = K-block j of W_{l+1}.  Each block is
-// 256 rows x 128 bytes in the 128-byte swizzle layout.
+// 256 rows x 128 bytes in the 128-byte swizzle layout.  Values are BF16(w) / 2
+// (= BF16(w / 2) exactly), so the accumulator holds z / 2.
 __global__ void k_weight_image(const float *params, int64_t off_w1, int64_t off_w2, int64_t off_w3, int64_t off_w4,
                                bf16 *img)
 {
@@ -402,7 +427,7 @@ __global__ void k_weight_image(const float *params, int64_t off_w1, int64_t off_
 			const int64_t off = l == 0 ? off_w2 : (l == 1 ? off_w3 : off_w4);
 			w = params[off + (int64_t)n * H + j * KB + c * 8 + e];
 		}
-		v[e] = __float2bfloat16_rn(w);
+		v[e] = __float2bfloat16_rn(0.5f * w);
 	}
 	uint8_t *dst = (uint8_t *)img + (size_t)b * WBLOCK_BYTES + swz(n, c);
 	*reinterpret_cast<uint4 *>(dst) = *reinterpret_cast<uint4 *>(v);

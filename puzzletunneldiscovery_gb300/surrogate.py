@@ -88,6 +88,16 @@ class Surrogate:
                                           _stream(q.device)), "pw_mlp_predict")
         return out
 
+    def score(self, q: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        """The logit of P(free) (no sigmoid), float32 [n]: a ranking score that does not saturate."""
+        q = self._states(q)
+        n = q.shape[0]
+        if out is None:
+            out = torch.empty(n, dtype=torch.float32, device=q.device)
+        _lib.check(self._L.pw_mlp_score(self._h, ctypes.c_void_p(q.data_ptr()), n, ctypes.c_void_p(out.data_ptr()),
+                                        _stream(q.device)), "pw_mlp_score")
+        return out
+
     def predict_mma(self, q: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         """The same prediction through the mma.sync GEMM kernels that training uses."""
         q = self._states(q)
@@ -188,25 +198,39 @@ class GuidedReport:
     precision: float = 0.0      # accepted / checked: exact-free among the top fraction
 
 
-def guided_free_samples(world, net: Surrogate, q: torch.Tensor, top_frac: float = 0.1,
-                        chunk: int = 1 << 23):
-    """Rank candidates by the network and check the top `top_frac` of each chunk
-    exactly; returns (accepted free states, GuidedReport).  Every returned state
-    passed pw_states_valid."""
+def select_top(score: torch.Tensor, q: torch.Tensor, k: int, slack: int = 1 << 16) -> torch.Tensor:
+    """The states whose score is at or above the k-th largest (pw_select_top),
+    in no particular order; ties at the threshold are all kept."""
+    L = _lib.load()
+    if not (isinstance(score, torch.Tensor) and score.dtype == torch.float32 and score.is_cuda
+            and score.shape == (q.shape[0],)):
+        raise TypeError("score must be a CUDA float32 tensor with one value per state")
+    q = q.contiguous()
+    cap = min(q.shape[0], k + slack)
+    while True:
+        out = torch.empty((cap, 7), dtype=torch.float64, device=q.device)
+        cnt = ctypes.c_int64()
+        rc = L.pw_select_top(ctypes.c_void_p(score.data_ptr()), ctypes.c_void_p(q.data_ptr()), q.shape[0], int(k),
+                             ctypes.c_void_p(out.data_ptr()), cap, ctypes.byref(cnt), _stream(q.device))
+        if rc == _lib.PW_ERR_CAPACITY:
+            cap = int(cnt.value)
+            continue
+        _lib.check(rc, "pw_select_top")
+        return out[:cnt.value]
+
+
+def guided_free_samples(world, net: Surrogate, q: torch.Tensor, top_frac: float = 0.1, score=None):
+    """Rank candidates by the network's logit and check the top `top_frac`
+    exactly; returns (accepted free states, GuidedReport).  Every returned
+    state passed pw_states_valid."""
     rep = GuidedReport()
-    out = []
-    prob = None
-    for s in range(0, q.shape[0], chunk):
-        c = q[s:s + chunk]
-        prob = net.predict(c, out=prob[:c.shape[0]] if prob is not None and prob.shape[0] >= c.shape[0] else None)
-        k = max(1, int(round(top_frac * c.shape[0])))
-        idx = torch.topk(prob[:c.shape[0]], k, sorted=False).indices
-        cand = c.index_select(0, idx)
-        ok = world.is_valid_states(cand)
-        out.append(cand[ok])
-        rep.candidates += c.shape[0]
-        rep.checked += k
-    acc = torch.cat(out) if out else q[:0]
+    score = net.score(q, out=score)
+    k = max(1, int(round(top_frac * q.shape[0])))
+    cand = select_top(score, q, k)
+    ok = world.is_valid_states(cand)
+    acc = cand[ok]
+    rep.candidates = int(q.shape[0])
+    rep.checked = int(cand.shape[0])
     rep.accepted = int(acc.shape[0])
     rep.precision = rep.accepted / max(rep.checked, 1)
     return acc, rep

@@ -1,6 +1,6 @@
 """Small, fixed workloads for ncu captures (not collected by pytest).
 
-python tests/profile_targets.py states|segments [n]
+python tests/profile_targets.py states|segments|mlp|train [n]
 """
 import sys, os
 sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
@@ -13,6 +13,23 @@ Ve, Fe, Vr, Fr = W.cfg_interlocking_tori()
 uw = pw.UnitWorld(0)
 uw.load_env_mesh(Ve, Fe); uw.load_robot_mesh(Vr, Fr); uw.scaleToUnit(); uw.angleModel(0, 0)
 s = uw.scene_scale
+if what in ("mlp", "train"):
+    from puzzletunneldiscovery_gb300.surrogate import Surrogate, uniform_states_device
+    net = Surrogate(0, 1)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(0)
+    q = uniform_states_device(n, -2, 2, s, g, torch.device("cuda", 0))
+    if what == "mlp":
+        for _ in range(3):
+            p = net.predict(q)
+        net.check()
+    else:
+        y = uw.is_valid_states(q[:65536])
+        for _ in range(3):
+            net.train_step(q[:65536], y, 1e-3)
+    torch.cuda.synchronize()
+    print("done")
+    sys.exit(0)
 if what == "states":
     q = torch.from_numpy(W.uniform_states(n, -2, 2, s, seed=0)).cuda()
     for _ in range(3):

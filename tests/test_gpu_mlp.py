@@ -78,8 +78,10 @@ def test_tcgen05_forward_matches_mma_forward(built_lib, mo, n):
     a = net.predict(dq)
     net.check()
     b = net.predict_mma(dq)
+    logit = net.score(dq).cpu().numpy()
     a, b = a.cpu().numpy(), b.cpu().numpy()
     assert np.abs(a - b).max() <= 2e-3
+    assert np.abs(1.0 / (1.0 + np.exp(-logit.astype(np.float64))) - a).max() <= 1e-6
     k = min(n, 2048)
     want = mo.predict(net.params().astype(np.float64), q[:k])
     assert np.abs(a[:k] - want).max() <= 2e-3
@@ -156,3 +158,23 @@ def test_training_beats_uniform_sampling(built_lib):
     assert g.precision >= min(0.99, base + 0.3)
     prec, rec = S.precision_recall(net.predict(cand), exact)
     assert prec > base + 0.2 and rec > 0.8
+
+
+@pytest.mark.parametrize("n,k,lo", [(1, 1, 0.0), (1000, 100, 0.0), (1 << 20, 104857, 0.0), (300000, 300000, 0.0),
+                                    (200000, 77777, -8.0), (65536, 3, -1.0)])
+def test_select_top_is_exact(built_lib, n, k, lo):
+    """pw_select_top keeps exactly the states scored at or above the k-th
+    largest score, ties included (scores quantised so that ties occur;
+    negative scores where lo < 0)."""
+    from puzzletunneldiscovery_gb300.surrogate import select_top
+    g = torch.Generator(device="cuda")
+    g.manual_seed(n)
+    score = lo + (torch.rand(n, device="cuda", generator=g) * 4096).floor() / 4096 * (1.0 - 2 * lo)
+    q = torch.zeros((n, 7), dtype=torch.float64, device="cuda")
+    q[:, 0] = torch.arange(n, device="cuda", dtype=torch.float64)
+    out = select_top(score, q, k)
+    kth = torch.topk(score, k).values.min()
+    want = torch.nonzero(score >= kth).flatten()
+    got = torch.sort(out[:, 0].long()).values
+    assert got.shape[0] >= k
+    assert torch.equal(got, want)
