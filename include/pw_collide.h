@@ -145,6 +145,17 @@ PW_API int pw_intersecting_segments(pw_world *w, const double q[7], int64_t capa
                              double *ends, double *mags, int32_t *face_pairs, int32_t *coplanar,
                              int64_t *count);
 
+/* The result tuple of transit_state_to_with_contact (unit_world.cc:405-474) for n
+ * segments, from the codes pw_segments_first_contact(PW_SEG_TRANSIT) wrote for
+ * the same segments and verify_delta (device arrays): last_free [n x 7],
+ * contact [n x 7] (first colliding state, or the last state when done), done
+ * [n] (1 = every step free), last_tau [n], tau [n].  *err_flag (device int,
+ * zeroed by the caller) becomes non-zero if a code was PW_STEP_INVALID.
+ * Used by touch sampling (src/GP/pipeline/touchq_util.py:8-27). */
+PW_API int pw_segments_contact_states(const double *from, const double *to, const int32_t *first_step, int64_t n,
+                                      double verify_delta, double *last_free, double *contact, uint8_t *done,
+                                      float *last_tau, float *tau, int *err_flag, void *stream);
+
 /* host: state-frame conversions (unit_world.cc:526-539, 689-711, 713-737). */
 PW_API int pw_world_translate_to_unit(const pw_world *w, const double *in, int64_t n, double *out);
 PW_API int pw_world_translate_from_unit(const pw_world *w, const double *in, int64_t n, double *out);

@@ -36,6 +36,7 @@ EXPORTS = (
     "pw_intersecting_segments", "pw_world_translate_to_unit", "pw_world_translate_from_unit",
     "pw_world_translate_ompl_to_unit", "pw_world_translate_unit_to_ompl", "pw_world_last_stats",
     "pw_state_distance", "pw_state_interpolate", "pw_segment_step_state", "pw_states_valid_noalloc",
+    "pw_segments_contact_states",
     # include/pw_mlp.h
     "pw_mlp_create", "pw_mlp_destroy", "pw_mlp_num_params", "pw_mlp_get_params", "pw_mlp_set_params",
     "pw_mlp_get_grads", "pw_mlp_predict", "pw_mlp_gradients", "pw_mlp_train_step", "pw_mlp_predict_mma",
@@ -123,6 +124,8 @@ def load():
         "pw_state_distance": (ctypes.c_int, [dp, dp, dp]),
         "pw_state_interpolate": (ctypes.c_int, [dp, dp, ctypes.c_double, dp]),
         "pw_segment_step_state": (ctypes.c_int, [dp, dp, ctypes.c_double, i64, dp, dp, i64p]),
+        "pw_segments_contact_states": (ctypes.c_int, [vp, vp, vp, i64, ctypes.c_double, vp, vp, vp, vp, vp, vp,
+                                                      vp]),
         "pw_mlp_create": (ctypes.c_int, [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_uint64]),
         "pw_mlp_destroy": (ctypes.c_int, [vp]),
         "pw_mlp_num_params": (ctypes.c_int64, [vp]),

@@ -651,6 +651,11 @@ static int *mlp_err(pw_mlp *m) { return (int *)((char *)m->misc.ptr + 16); }
 
 static int mlp_forward_tc(pw_mlp *m, const double *states, int64_t n, float *prob, int logits, void *stream);
 
+static float *mlp_head_table(pw_mlp *m)
+{
+	return (float *)((char *)m->wimg.ptr + (size_t)tc::NWBLOCK * tc::WBLOCK_BYTES);
+}
+
 extern "C" int pw_mlp_predict(pw_mlp *m, const double *states, int64_t n, float *prob, void *stream)
 {
 	return mlp_forward_tc(m, states, n, prob, 0, stream);
@@ -671,11 +676,14 @@ static int mlp_forward_tc(pw_mlp *m, const double *states, int64_t n, float *pro
 	PW_CUDA(cudaSetDevice(m->device));
 	cudaStream_t st = (cudaStream_t)stream;
 	if (m->wimg_dirty) {
-		PW_CUDA(m->wimg.reserve((size_t)tc::NWBLOCK * tc::WBLOCK_BYTES));
+		PW_CUDA(m->wimg.reserve((size_t)tc::NWBLOCK * tc::WBLOCK_BYTES + sizeof(float) * tc::HT_FLOATS));
 		const int64_t nchunk = (int64_t)tc::NWBLOCK * H * 8;
 		tc::k_weight_image<<<(unsigned)((nchunk + 255) / 256), 256, 0, st>>>(
 		    (const float *)m->params.ptr, (int64_t)m->off_w[0], (int64_t)m->off_w[1], (int64_t)m->off_w[2],
 		    (int64_t)m->off_w[3], (bf16 *)m->wimg.ptr);
+		tc::k_head_table<<<(tc::HT_FLOATS + 255) / 256, 256, 0, st>>>(
+		    (const float *)m->params.ptr, (int64_t)m->off_b[0], (int64_t)m->off_b[1], (int64_t)m->off_b[2],
+		    (int64_t)m->off_b[3], (int64_t)m->off_w5, (int64_t)m->off_b5, mlp_head_table(m));
 		PW_CUDA(cudaGetLastError());
 		m->wimg_dirty = false;
 	}
@@ -689,11 +697,7 @@ static int mlp_forward_tc(pw_mlp *m, const double *states, int64_t n, float *pro
 	a.states = states;
 	a.n = n;
 	a.wimg = (const bf16 *)m->wimg.ptr;
-	a.params = (const float *)m->params.ptr;
-	for (int l = 0; l < NLAYER; l++)
-		a.off_b[l] = (int64_t)m->off_b[l];
-	a.off_w5 = (int64_t)m->off_w5;
-	a.off_b5 = (int64_t)m->off_b5;
+	a.ht = mlp_head_table(m);
 	a.prob = prob;
 	a.logits = logits;
 	a.err = mlp_err(m);

@@ -170,13 +170,15 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b)
 	return *reinterpret_cast<uint32_t *>(&h);
 }
 
+// Per-column constants of the epilogue, after the weight images:
+// [4][256] biases b_l / 2, [256] w5, b5 (16-byte aligned rows).
+constexpr int HT_W5 = 4 * H, HT_B5 = 5 * H, HT_FLOATS = 5 * H + 4;
+
 struct FwdArgs {
 	const double *states;
 	int64_t n;
 	const bf16 *wimg;        // NWBLOCK images of WBLOCK_BYTES (weights scaled by 1/2)
-	const float *params;     // FP32 parameter block
-	int64_t off_b[4];
-	int64_t off_w5, off_b5;
+	const float *ht;         // epilogue constants (HT_*)
 	float *prob;
 	int logits;              // 1: write the logit (a ranking score that does not saturate) instead of P(free)
 	int *err;
@@ -300,7 +302,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 		const int r = q * 32 + lane;                  // tile row of this thread
 		const uint32_t lane_off = (uint32_t)(q * 32) << 16;
 		uint32_t done_ph[2] = { 0, 0 }, head_ph[2] = { 0, 0 };
-		const float b5 = a.params[a.off_b5];
+		const float b5 = a.ht[HT_B5];
 		bool ok = true;
 		for (int64_t tA = blockIdx.x; tA < ntiles && ok; tA += 2 * G) {
 			const int nslot = tA + G < ntiles ? 2 : 1;
@@ -325,7 +327,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 					mbar_arrive(bar(B_ACT + sl));
 			}
 			for (int layer = 0; layer < 4 && ok; layer++) {
-				const float *bias = a.params + a.off_b[layer];
+				const float *bias = a.ht + layer * H;   // b_l / 2
 				for (int sl = 0; sl < nslot; sl++) {
 					if (!mbar_wait(bar(B_DONE + sl), done_ph[sl], s_abort, a.err, 4)) {
 						ok = false;
@@ -335,15 +337,20 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 					tc_fence_after();
 					uint8_t *act = sm + SM_ACT + sl * ACT_BYTES;
 					float head = 0.f;
+					// per K-block j of act: this warp's 16 columns j*64 + g*16 .. +15
 					for (int j = 0; j < 4; j++) {
 						const int col = j * KB + g * 16;
-						float v[16];
+						float v[16], bv[16];
+#pragma unroll
+						for (int i = 0; i < 4; i++)
+							*reinterpret_cast<float4 *>(bv + 4 * i) =
+							    __ldg(reinterpret_cast<const float4 *>(bias + col) + i);
 						tmem_ld16(tmem + lane_off + (uint32_t)(sl * 256 + col), v);
 						uint32_t pk[8];
 #pragma unroll
 						for (int i = 0; i < 16; i += 2) {
-							const float h0 = v[i] + 0.5f * __ldg(bias + col + i);
-							const float h1 = v[i + 1] + 0.5f * __ldg(bias + col + i + 1);
+							const float h0 = v[i] + bv[i];
+							const float h1 = v[i + 1] + bv[i + 1];
 							pk[i / 2] = pack_bf16x2(fmaf(h0, tanh_fast(h0), h0), fmaf(h1, tanh_fast(h1), h1));
 						}
 						if (layer < 3) {
@@ -352,12 +359,15 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 							*reinterpret_cast<uint4 *>(kb + swz(r, 2 * g + 1)) =
 							    make_uint4(pk[4], pk[5], pk[6], pk[7]);
 						} else {
-							const float *w5 = a.params + a.off_w5 + col;
+#pragma unroll
+							for (int i = 0; i < 4; i++)
+								*reinterpret_cast<float4 *>(bv + 4 * i) =
+								    __ldg(reinterpret_cast<const float4 *>(a.ht + HT_W5 + col) + i);
 #pragma unroll
 							for (int i = 0; i < 8; i++) {
 								const __nv_bfloat162 hh = *reinterpret_cast<__nv_bfloat162 *>(&pk[i]);
-								head = fmaf(__low2float(hh), __ldg(w5 + 2 * i), head);
-								head = fmaf(__high2float(hh), __ldg(w5 + 2 * i + 1), head);
+								head = fmaf(__low2float(hh), bv[2 * i], head);
+								head = fmaf(__high2float(hh), bv[2 * i + 1], head);
 							}
 						}
 					}
@@ -399,6 +409,25 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 		tc_fence_after();
 		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
 	}
+}
+
+__global__ void k_head_table(const float *params, int64_t off_b1, int64_t off_b2, int64_t off_b3, int64_t off_b4,
+                             int64_t off_w5, int64_t off_b5, float *ht)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= HT_FLOATS)
+		return;
+	float v = 0.f;
+	if (i < HT_W5) {
+		const int l = i / H, c = i % H;
+		const int64_t off = l == 0 ? off_b1 : (l == 1 ? off_b2 : (l == 2 ? off_b3 : off_b4));
+		v = 0.5f * params[off + c];
+	} else if (i < HT_B5) {
+		v = params[off_w5 + (i - HT_W5)];
+	} else if (i == HT_B5) {
+		v = params[off_b5];
+	}
+	ht[i] = v;
 }
 
 // Weight images for the kernel above: block 0 = W1 (256 x 16, zero-padded to

@@ -1,0 +1,115 @@
+// pw_touch.cu -- the result tuple of UnitWorld::transitStateToWithContact
+// (lib/osr/unit_world.cc:405-474) for a batch of segments, from their
+// first-contact codes.  This is what the touch-configuration sampler
+// (src/GP/pipeline/touchq_util.py:8-27, calc_touch) consumes: the last free
+// state, the first colliding state (or the last state), `done`, and the two
+// taus, for thousands of random segments from one root.
+#include <cuda_runtime.h>
+
+#include "pw_internal.cuh"
+#include "pw_math.cuh"
+
+namespace {
+
+// One thread per segment.  The taus come from the reference's delta loop
+// restated in FP64 (advance_delta), so states are bit-identical to
+// pw_segment_step_state and to the oracle.
+__global__ void k_contact_states(const double *from, const double *to, const int32_t *first, int64_t n,
+                                 double verify_delta, double *last_free, double *contact, uint8_t *done,
+                                 float *last_tau, float *tau, int *err)
+{
+	const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+	if (i >= n)
+		return;
+	const double *a = from + 7 * i, *b = to + 7 * i;
+	double *lf = last_free + 7 * i, *st = contact + 7 * i;
+	const double dist = pwm::distance(a, b);
+	if (verify_delta >= dist) {
+		// unit_world.cc:445-447: nothing checked, the target returned
+		for (int c = 0; c < 7; c++) {
+			lf[c] = a[c];
+			st[c] = b[c];
+		}
+		done[i] = 0;
+		last_tau[i] = 0.f;
+		tau[i] = 1.f;
+		return;
+	}
+	if (dist != dist) {
+		for (int c = 0; c < 7; c++)
+			lf[c] = st[c] = a[c];
+		done[i] = 0;
+		last_tau[i] = tau[i] = 0.f;
+		return;
+	}
+	const int32_t k = first[i];
+	if (k < -1) {
+		// PW_STEP_INVALID (or a code that does not belong to this delta)
+		atomicCAS(err, 0, 1);
+		for (int c = 0; c < 7; c++)
+			lf[c] = st[c] = a[c];
+		done[i] = 0;
+		last_tau[i] = tau[i] = 0.f;
+		return;
+	}
+	const double inv = pwm::dvd(1.0, dist);
+	pwm::SlerpParams P;
+	pwm::slerp_setup(a, b, P);
+	// delta of step j is the value after j updates of the loop (step 0: verify_delta)
+	double prev = 0.0, delta = verify_delta;
+	int64_t j = 0;
+	if (k >= 0) {
+		for (; j < k; j++) {
+			prev = delta;
+			delta = pwm::advance_delta(delta, dist, verify_delta);
+		}
+		const double t = pwm::mul(delta, inv);
+		pwm::interpolate_p(a, b, P, t, st);
+		tau[i] = (float)t;
+		if (k == 0) {
+			for (int c = 0; c < 7; c++)
+				lf[c] = a[c];
+			last_tau[i] = 0.f;
+		} else {
+			const double lt = pwm::mul(prev, inv);
+			pwm::interpolate_p(a, b, P, lt, lf);
+			last_tau[i] = (float)lt;
+		}
+		done[i] = 0;
+		return;
+	}
+	// every step free: the last state the loop checked, done = true, outer tau 0
+	while (true) {
+		const double next = pwm::advance_delta(delta, dist, verify_delta);
+		if (!(next <= dist))
+			break;
+		delta = next;
+	}
+	const double lt = pwm::mul(delta, inv);
+	pwm::interpolate_p(a, b, P, lt, lf);
+	for (int c = 0; c < 7; c++)
+		st[c] = lf[c];
+	done[i] = 1;
+	last_tau[i] = (float)lt;
+	tau[i] = 0.f;
+}
+
+} // namespace
+
+extern "C" int pw_segments_contact_states(const double *from, const double *to, const int32_t *first_step, int64_t n,
+                                          double verify_delta, double *last_free, double *contact, uint8_t *done,
+                                          float *last_tau, float *tau, int *err_flag, void *stream)
+{
+	if (n < 0 || (n > 0 && (!from || !to || !first_step || !last_free || !contact || !done || !last_tau || !tau ||
+	                        !err_flag)))
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_segments_contact_states: bad pointers or size");
+	if (!(verify_delta > 0.0))
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_segments_contact_states: verify_delta must be > 0");
+	if (n == 0)
+		return PW_OK;
+	cudaStream_t st = (cudaStream_t)stream;
+	k_contact_states<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(from, to, first_step, n, verify_delta, last_free,
+	                                                               contact, done, last_tau, tau, err_flag);
+	PW_CUDA(cudaGetLastError());
+	return PW_OK;
+}

@@ -253,6 +253,31 @@ class UnitWorld:
         lf, ltau, _ = segment_step_state(a, b, verify_delta, K - 1)
         return lf, lf.copy(), True, np.float32(ltau), np.float32(0.0)
 
+    def transit_states_to_with_contact(self, q0, q1, verify_delta: float):
+        """transit_state_to_with_contact for a batch (device tensors): returns
+        (last_free [N,7], contact [N,7], done [N] bool, last_tau [N] f32, tau [N] f32),
+        each row the tuple of unit_world.cc:405-474 for that segment."""
+        q0 = self._dev_states(q0)
+        q1 = self._dev_states(q1)
+        if q0.shape != q1.shape:
+            raise ValueError("from/to batches differ in shape")
+        n = q0.shape[0]
+        steps = self.first_contact_steps(q0, q1, verify_delta, _lib.PW_SEG_TRANSIT)
+        dev = self._device
+        lf = torch.empty((n, 7), dtype=torch.float64, device=dev)
+        st = torch.empty((n, 7), dtype=torch.float64, device=dev)
+        done = torch.empty(n, dtype=torch.uint8, device=dev)
+        lt = torch.empty(n, dtype=torch.float32, device=dev)
+        tt = torch.empty(n, dtype=torch.float32, device=dev)
+        err = torch.zeros(1, dtype=torch.int32, device=dev)
+        check(self._L.pw_segments_contact_states(q0.data_ptr(), q1.data_ptr(), steps.data_ptr(), n,
+                                                 float(verify_delta), lf.data_ptr(), st.data_ptr(), done.data_ptr(),
+                                                 lt.data_ptr(), tt.data_ptr(), err.data_ptr(),
+                                                 _stream_ptr(dev)), "transit_states_to_with_contact")
+        if int(err.item()) != 0:
+            raise RuntimeError("transit_state_to: more than 2^30 steps at this verify_delta")
+        return lf, st, done.bool(), lt, tt
+
     def transit_state_to(self, from_state, to_state, verify_delta):
         """(free state, done, progress) of unit_world.cc:395-402."""
         tup = self.transit_state_to_with_contact(from_state, to_state, verify_delta)

@@ -1,0 +1,112 @@
+"""Host logic of the batched samplers (puzzletunneldiscovery_gb300/sampling.py),
+on the CPU with a stand-in world whose verdicts are scripted."""
+import math
+
+import numpy as np
+import torch
+
+from conftest import ROOT  # noqa: F401
+
+
+class ScriptedWorld:
+    """Answers is_valid_states from a fixed pattern, in call order."""
+
+    def __init__(self, pattern):
+        self.pattern = np.asarray(pattern, bool).ravel()
+        self._device = torch.device("cpu")
+        self.calls = []
+
+    def is_valid_states(self, q):
+        self.calls.append(q.shape[0])
+        assert q.shape[0] == self.pattern.shape[0]
+        return torch.from_numpy(self.pattern.copy())
+
+
+def _S():
+    from puzzletunneldiscovery_gb300 import sampling
+    return sampling
+
+
+def test_quat_between_and_rotate():
+    S = _S()
+    rng = np.random.default_rng(0)
+    a = rng.normal(size=(100, 3))
+    b = rng.normal(size=(100, 3))
+    b[0] = -a[0]                     # opposite directions
+    b[1] = 2.0 * a[1]                # same direction
+    q = S.quat_between(a, b)
+    assert np.allclose(np.linalg.norm(q, axis=1), 1.0)
+    ra = S.quat_rotate(q, a / np.linalg.norm(a, axis=1, keepdims=True))
+    assert np.allclose(ra, b / np.linalg.norm(b, axis=1, keepdims=True), atol=1e-12)
+
+
+def test_touch_states_place_points_with_opposed_normals():
+    S = _S()
+    rng = np.random.default_rng(1)
+    P, A = 5, 7
+    rp, ep = rng.normal(size=(P, 3)), rng.normal(size=(P, 3))
+    rn = rng.normal(size=(P, 3))
+    en = rng.normal(size=(P, 3))
+    rn /= np.linalg.norm(rn, axis=1, keepdims=True)
+    en /= np.linalg.norm(en, axis=1, keepdims=True)
+    ang = rng.uniform(0, 2 * math.pi, (P, A))
+    qs = S._touch_states(rp, rn, ep, en, 0.01, ang)
+    for p in range(P):
+        for i in range(A):
+            q = qs[p, i]
+            rob_o = rp[p] + 0.01 * rn[p]
+            placed = S.quat_rotate(q[3:], rob_o) + q[:3]
+            assert np.allclose(placed, ep[p] + 0.01 * en[p], atol=1e-12)
+            assert np.allclose(S.quat_rotate(q[3:], rn[p]), -en[p], atol=1e-12)
+
+
+def test_enum_free_configuration_median_runs():
+    S = _S()
+    # runs of free spins: [1..3] -> 2, [5] -> 5, trailing [8, 9] is not reported (reference quirk)
+    pattern = np.array([0, 1, 1, 1, 0, 1, 0, 0, 1, 1], bool)
+    uw = ScriptedWorld(pattern)
+    z = np.zeros(3)
+    n = np.array([0.0, 0.0, 1.0])
+    all_free = S.enum_free_configuration(uw, z, n, z, n, 0.0, 10, only_median=False)
+    assert all_free.shape == (6, 7)
+    med = S.enum_free_configuration(uw, z, n, z, n, 0.0, 10, only_median=True)
+    qs = S._touch_states(z, n, z, n, 0.0, (np.arange(10) * (2 * math.pi / 10))[None, :])[0]
+    assert np.array_equal(med, qs[[2, 5]])
+
+
+def test_sample_free_configuration_first_free_or_last_tried():
+    S = _S()
+    pattern = np.array([[0, 0, 1, 1], [0, 0, 0, 0]], bool)
+    uw = ScriptedWorld(pattern)
+    pts = np.zeros((2, 3))
+    nrm = np.tile([0.0, 1.0, 0.0], (2, 1))
+    rng = np.random.default_rng(3)
+    q, found = S.sample_free_configurations(uw, pts, nrm, pts, nrm, 0.0, max_trials=3, rng=rng)
+    assert list(found) == [True, False]
+    rng = np.random.default_rng(3)
+    ang = rng.uniform(0.0, 2 * math.pi, (2, 4))
+    qs = S._touch_states(pts, nrm, pts, nrm, 0.0, ang)
+    assert np.array_equal(q[0], qs[0, 2]) and np.array_equal(q[1], qs[1, 3])
+
+
+def test_apply_batch_matches_single_apply():
+    S = _S()
+    from puzzletunneldiscovery_gb300.unit_world import apply
+    rng = np.random.default_rng(4)
+    q0 = np.array([0.1, -0.2, 0.3, 0.5, 0.5, -0.5, 0.5])
+    tr = rng.normal(size=(20, 3))
+    aa = rng.normal(size=(20, 3))
+    aa[0] = 0.0
+    out = S.apply_batch(q0, tr, aa)
+    for i in range(20):
+        assert np.allclose(out[i], apply(q0, tr[i], aa[i]), atol=1e-15)
+
+
+def test_random_directions():
+    S = _S()
+    rng = np.random.default_rng(5)
+    s = S.random_on_sphere(1000, 1.0, rng)
+    assert np.allclose(np.linalg.norm(s, axis=1), 1.0)
+    b = S.random_within_sphere(1000, 2 * math.pi, rng)
+    assert (np.linalg.norm(b, axis=1) <= 2 * math.pi + 1e-12).all()
+    assert abs(s.mean(axis=0)).max() < 0.1
