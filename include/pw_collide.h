@@ -74,6 +74,8 @@ typedef struct pw_query_stats {
 	int64_t detailed_chunks;     /* 32-step segment chunks that needed a transform per step */
 	double traverse_ms;          /* device time of the traversal kernel (CUDA events on the query stream) */
 	double retest_ms;            /* device time of the FP64 re-test kernel */
+	int64_t device_errors;       /* non-zero: a device-side capacity or consistency check failed; the
+	                                affected segments carry PW_STEP_INVALID */
 } pw_query_stats;
 
 /* Thread-local message for the last failing call on this thread. */
@@ -144,6 +146,25 @@ PW_API int pw_segments_first_contact(pw_world *w, const double *from, const doub
 PW_API int pw_intersecting_segments(pw_world *w, const double q[7], int64_t capacity, double *begins,
                              double *ends, double *mags, int32_t *face_pairs, int32_t *coplanar,
                              int64_t *count);
+
+/* Graph mode (on != 0): pw_segments_first_contact makes no host synchronisation
+ * and no device allocation, so a caller can capture it into a CUDA graph and
+ * replay it.  It then runs within the scratch sized by pw_segments_reserve or
+ * by the last call made with graph mode off; segments that do not fit get
+ * PW_STEP_INVALID and pw_world_last_stats reports device_errors.  Off by default. */
+PW_API int pw_world_set_graph_mode(pw_world *w, int on);
+
+/* host: size the segment-query scratch for up to n segments with, in total, up
+ * to total_chunks 32-step chunks and at most max_chunks chunks in one segment. */
+PW_API int pw_segments_reserve(pw_world *w, int64_t n, int64_t total_chunks, int64_t max_chunks);
+
+/* Launch configuration of the persistent traversal kernels (kernel 0: states,
+ * 1: segments): width = queries a warp takes per grab (1..32, states only),
+ * soft_cap = traversal stack entries before the warp narrows to depth-first
+ * (>= 64, clamped to the stack), blocks = resident blocks per SM (clamped to
+ * occupancy).  0 keeps the default.  Verdicts do not depend on it. */
+PW_API int pw_world_set_launch_config(pw_world *w, int kernel, int width, int soft_cap, int blocks);
+PW_API int pw_world_get_launch_config(pw_world *w, int kernel, int *width, int *soft_cap, int *blocks);
 
 /* The result tuple of transit_state_to_with_contact (unit_world.cc:405-474) for n
  * segments, from the codes pw_segments_first_contact(PW_SEG_TRANSIT) wrote for

@@ -107,6 +107,18 @@ struct pw_world {
 	bool timed = false;
 	int64_t last_states = -1;   // size of the last state batch (-1: the last query was segments)
 	int num_sms = 0;
+	// graph mode: segment queries make no host synchronisation and no allocation;
+	// they run within the scratch capacities below (set by pw_segments_reserve or
+	// by the last segment query made outside graph mode)
+	bool graph_mode = false;
+	int64_t cap_chunks = 0;     // checkpoint / anchor slots (32-step chunks) of one call
+	int64_t cap_rounds = 0;     // chunks of the longest segment of one call
+	int64_t cap_segments = 0;   // segments of one call
+	// launch configuration (pw_world_set_launch_config; 0 = default)
+	int launch_width[2] = { 0, 0 };     // queries a warp takes per grab (states kernel only)
+	int launch_soft_cap[2] = { 0, 0 };  // traversal stack soft cap
+	int launch_blocks[2] = { 0, 0 };    // resident blocks per SM of the persistent kernel
+	int grid_cache[2] = { 0, 0 };       // grid of the persistent kernels under that configuration
 };
 
 // error plumbing (pw_world.cu)

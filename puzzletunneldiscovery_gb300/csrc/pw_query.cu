@@ -563,7 +563,7 @@ __device__ void flush_stats(QueryCounters *ctr, const LaneStats &st, unsigned lo
 template <uint64_t CAP>
 __global__ void __launch_bounds__(WARPS * 32) k_states(WorldDev W, const double *states, int64_t n,
                                                        uint8_t *out, QueryCounters *ctr, RetestEntry *rq,
-                                                       int soft_cap)
+                                                       int soft_cap, int width)
 {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -574,11 +574,11 @@ __global__ void __launch_bounds__(WARPS * 32) k_states(WorldDev W, const double 
 	for (;;) {
 		unsigned long long base = 0;
 		if (lane == 0)
-			base = atomicAdd(&ctr->work, 32ull);
+			base = atomicAdd(&ctr->work, (unsigned long long)width);
 		base = __shfl_sync(FULL, base, 0);
 		if (base >= (unsigned long long)n)
 			break;
-		const int cnt = (int)min((unsigned long long)32, (unsigned long long)n - base);
+		const int cnt = (int)min((unsigned long long)width, (unsigned long long)n - base);
 		if (lane < cnt) {
 			double q[7];
 			for (int i = 0; i < 7; i++)
@@ -683,7 +683,8 @@ __device__ __forceinline__ void seg_step_qf(const WorldDev &W, const double *a, 
 
 __global__ void k_seg_setup(WorldDev W, const double *from, const double *to, int64_t n, double vdelta, int mode,
                             const int64_t *slots, const int64_t *slot_base, SegParams *params, double *ckpt,
-                            QFs *anchors, int32_t *first, uint32_t *keys, uint32_t *vals, QueryCounters *ctr)
+                            QFs *anchors, int32_t *first, uint32_t *keys, uint32_t *vals, QueryCounters *ctr,
+                            int64_t ckpt_cap)
 {
 	const double rob_r2 = W.rob.r2;
 	const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -721,6 +722,10 @@ __global__ void k_seg_setup(WorldDev W, const double *from, const double *to, in
 	if (step >= dist || dist != dist) {
 		code = PW_STEP_NONE;
 	} else if (!(step > 0.0) || dist / step > MAX_STEPS) {
+		code = -3;
+	} else if (P.ckpt_base + slots[s] > ckpt_cap) {
+		// graph mode: the reserved checkpoint slots do not hold this segment
+		atomicExch(&ctr->error, 2u);
 		code = -3;
 	} else {
 		double delta = step;
@@ -762,12 +767,21 @@ __global__ void k_seg_setup(WorldDev W, const double *from, const double *to, in
 // than j chunks (segments sorted by chunk count, descending).  Computes the
 // exclusive offsets of the rounds and the total number of work items.
 __global__ void __launch_bounds__(1024) k_rounds(const uint32_t *sorted_keys, int64_t n, int64_t *round_off,
-                                                 QueryCounters *ctr)
+                                                 int64_t round_cap, int32_t *first, QueryCounters *ctr)
 {
 	typedef cub::BlockScan<long long, 1024> Scan;
 	__shared__ typename Scan::TempStorage tmp;
 	__shared__ long long carry;
-	const int64_t R = n > 0 ? (int64_t)sorted_keys[0] : 0;
+	int64_t R = n > 0 ? (int64_t)sorted_keys[0] : 0;
+	if (R > round_cap) {
+		// graph mode: the longest segment has more chunks than reserved; no work runs
+		// and every segment reports PW_STEP_INVALID
+		for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
+			first[i] = -3;
+		if (threadIdx.x == 0)
+			atomicExch(&ctr->error, 3u);
+		R = 0;
+	}
 	if (threadIdx.x == 0)
 		carry = 0;
 	__syncthreads();
@@ -797,6 +811,7 @@ __global__ void __launch_bounds__(1024) k_rounds(const uint32_t *sorted_keys, in
 	}
 	if (threadIdx.x == 0) {
 		round_off[R] = carry;
+		round_off[round_cap + 1] = R;      // the round count, read by k_segments
 		ctr->stat[STAT_TOTAL_ITEMS] = (unsigned long long)carry;
 	}
 }
@@ -806,9 +821,11 @@ __global__ void __launch_bounds__(1024) k_rounds(const uint32_t *sorted_keys, in
 // parallel, then answers its steps with one swept traversal and records the
 // first step in contact with atomicMin.
 __global__ void __launch_bounds__(WARPS * 32) k_segments(WorldDev W, StateSrc src, const uint32_t *order,
-                                                         const int64_t *round_off, int64_t nrounds, int32_t *first,
-                                                         QueryCounters *ctr, RetestEntry *rq, int soft_cap)
+                                                         const int64_t *round_off, const int64_t *nrounds_p,
+                                                         int32_t *first, QueryCounters *ctr, RetestEntry *rq,
+                                                         int soft_cap)
 {
+	const int64_t nrounds = *nrounds_p;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	WarpSmem &sm = reinterpret_cast<WarpSmem *>(smem_raw)[warp];
@@ -1052,6 +1069,33 @@ int persistent_grid(pw_world *w, const void *kernel, size_t smem)
 	return per_sm * (w->num_sms > 0 ? w->num_sms : 1);
 }
 
+// Launch configuration of kernel 0 (states) / 1 (segments), as set by pw_world_set_launch_config.
+int launch_grid(pw_world *w, int kernel, const void *fn, size_t smem)
+{
+	if (w->grid_cache[kernel] > 0)
+		return w->grid_cache[kernel];
+	int per_sm = 0;
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, WARPS * 32, smem);
+	if (per_sm < 1)
+		per_sm = 1;
+	if (w->launch_blocks[kernel] > 0 && w->launch_blocks[kernel] < per_sm)
+		per_sm = w->launch_blocks[kernel];
+	w->grid_cache[kernel] = per_sm * (w->num_sms > 0 ? w->num_sms : 1);
+	return w->grid_cache[kernel];
+}
+
+int launch_soft_cap(const pw_world *w, int kernel)
+{
+	const int hard = soft_cap_of(w);
+	const int c = w->launch_soft_cap[kernel];
+	return c > 0 && c < hard ? c : hard;
+}
+
+int launch_width(const pw_world *w, int kernel)
+{
+	return kernel == 0 && w->launch_width[0] > 0 ? w->launch_width[0] : 32;
+}
+
 // Event i (0: before the traversal, 1: between traversal and re-test, 2: after) on stream st.
 int mark(pw_world *w, int i, cudaStream_t st)
 {
@@ -1097,20 +1141,22 @@ extern "C" int pw_states_valid(pw_world *w, const double *states, int64_t n, uin
 		return PW_OK;
 	}
 	const size_t smem = warp_smem_bytes() * WARPS;
-	rc = set_smem_attr((const void *)k_states<RETEST_CAP>, smem);
-	if (rc)
+	if (!w->graph_mode && (rc = set_smem_attr((const void *)k_states<RETEST_CAP>, smem)))
 		return rc;
-	const int grid = persistent_grid(w, (const void *)k_states<RETEST_CAP>, smem);
+	const int grid = launch_grid(w, 0, (const void *)k_states<RETEST_CAP>, smem);
 	RetestEntry *rq = (RetestEntry *)w->retest.ptr;
-	rc = mark(w, 0, st);
-	if (rc)
+	if (!w->graph_mode && (rc = mark(w, 0, st)))
 		return rc;
-	k_states<RETEST_CAP><<<grid, WARPS * 32, smem, st>>>(w->dev, states, n, valid, ctr, rq, soft_cap_of(w));
-	mark(w, 1, st);
+	k_states<RETEST_CAP><<<grid, WARPS * 32, smem, st>>>(w->dev, states, n, valid, ctr, rq, launch_soft_cap(w, 0),
+	                                                     launch_width(w, 0));
+	if (!w->graph_mode)
+		mark(w, 1, st);
 	StateSrc src{ states, nullptr, nullptr, nullptr, nullptr, nullptr };
 	k_retest<RETEST_CAP><<<w->num_sms * 4, 256, 0, st>>>(w->dev, src, valid, nullptr, ctr, rq);
-	mark(w, 2, st);
-	w->timed = true;
+	if (!w->graph_mode) {
+		mark(w, 2, st);
+		w->timed = true;
+	}
 	PW_CUDA(cudaGetLastError());
 	return PW_OK;
 }
@@ -1143,9 +1189,13 @@ extern "C" int pw_states_disentangled(pw_world *w, const double *states, int64_t
 }
 
 template <typename T>
-static int grow(DeviceBuffer &b, size_t count)
+static int grow(DeviceBuffer &b, size_t count, bool may_allocate = true)
 {
-	PW_CUDA(b.reserve(sizeof(T) * (count ? count : 1)));
+	const size_t need = sizeof(T) * (count ? count : 1);
+	if (!may_allocate && b.bytes < need)
+		return pw_fail(PW_ERR_CAPACITY, "graph mode: scratch not reserved for this batch (call pw_segments_reserve "
+		                                "or run the batch once with graph mode off)");
+	PW_CUDA(b.reserve(need));
 	return PW_OK;
 }
 
@@ -1179,9 +1229,10 @@ extern "C" int pw_segments_first_contact(pw_world *w, const double *from, const 
 	if (n == 0)
 		return PW_OK;
 	// scratch: params, slot bounds/base, keys/vals (x2), cub temp
-	if ((rc = grow<SegParams>(w->seg_params, n)) || (rc = grow<int64_t>(w->misc, 2 * n + 2)) ||
-	    (rc = grow<uint32_t>(w->seg_keys, n)) || (rc = grow<uint32_t>(w->seg_order, n)) ||
-	    (rc = grow<uint32_t>(w->seg_keys2, n)) || (rc = grow<uint32_t>(w->seg_order2, n)))
+	const bool alloc = !w->graph_mode;
+	if ((rc = grow<SegParams>(w->seg_params, n, alloc)) || (rc = grow<int64_t>(w->misc, 2 * n + 2, alloc)) ||
+	    (rc = grow<uint32_t>(w->seg_keys, n, alloc)) || (rc = grow<uint32_t>(w->seg_order, n, alloc)) ||
+	    (rc = grow<uint32_t>(w->seg_keys2, n, alloc)) || (rc = grow<uint32_t>(w->seg_order2, n, alloc)))
 		return rc;
 	int64_t *slots = (int64_t *)w->misc.ptr;
 	int64_t *slot_base = slots + n + 1;
@@ -1193,54 +1244,135 @@ extern "C" int pw_segments_first_contact(pw_world *w, const double *from, const 
 	PW_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, t1, slots, slot_base, (int)(n + 1), st));
 	PW_CUDA(cub::DeviceRadixSort::SortPairsDescending(nullptr, t2, (uint32_t *)nullptr, (uint32_t *)nullptr,
 	                                                  (uint32_t *)nullptr, (uint32_t *)nullptr, (int)n, 0, 32, st));
-	PW_CUDA(w->cub_tmp.reserve(std::max(t1, t2)));
+	if ((rc = grow<char>(w->cub_tmp, std::max(t1, t2), alloc)))
+		return rc;
 	// slots[n] = 0 so that slot_base[n] is the total
 	PW_CUDA(cudaMemsetAsync(slots + n, 0, sizeof(int64_t), st));
 	PW_CUDA(cub::DeviceScan::ExclusiveSum(w->cub_tmp.ptr, t1, slots, slot_base, (int)(n + 1), st));
-	// the checkpoint array needs the total: read it back (one small synchronous copy)
-	int64_t total_slots = 0;
-	PW_CUDA(cudaMemcpyAsync(&total_slots, slot_base + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-	PW_CUDA(cudaStreamSynchronize(st));
-	if ((rc = grow<double>(w->seg_ckpt, (size_t)total_slots + 1)) ||
-	    (rc = grow<QFs>(w->seg_anchor, (size_t)total_slots + 1)))
-		return rc;
+	if (!w->graph_mode) {
+		// size the checkpoint arrays by the total (one small synchronous copy)
+		int64_t total_slots = 0;
+		PW_CUDA(cudaMemcpyAsync(&total_slots, slot_base + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+		PW_CUDA(cudaStreamSynchronize(st));
+		if ((rc = grow<double>(w->seg_ckpt, (size_t)total_slots + 1)) ||
+		    (rc = grow<QFs>(w->seg_anchor, (size_t)total_slots + 1)))
+			return rc;
+	}
+	const int64_t ckpt_cap = (int64_t)std::min(w->seg_ckpt.bytes / sizeof(double), w->seg_anchor.bytes / sizeof(QFs));
 	QFs *anchors = (QFs *)w->seg_anchor.ptr;
 	SegParams *params = (SegParams *)w->seg_params.ptr;
 	double *ckpt = (double *)w->seg_ckpt.ptr;
 	uint32_t *keys = (uint32_t *)w->seg_keys.ptr, *vals = (uint32_t *)w->seg_order.ptr;
 	uint32_t *keys2 = (uint32_t *)w->seg_keys2.ptr, *vals2 = (uint32_t *)w->seg_order2.ptr;
 	k_seg_setup<<<G, B, 0, st>>>(w->dev, from, to, n, verify_delta, mode, slots, slot_base, params, ckpt, anchors,
-	                             first_step, keys, vals, ctr);
+	                             first_step, keys, vals, ctr, ckpt_cap);
 	PW_CUDA(cudaGetLastError());
 	PW_CUDA(cub::DeviceRadixSort::SortPairsDescending(w->cub_tmp.ptr, t2, keys, keys2, vals, vals2, (int)n, 0, 32, st));
-	// rounds: as many as the longest segment has chunks
-	uint32_t max_chunks = 0;
-	PW_CUDA(cudaMemcpyAsync(&max_chunks, keys2, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-	PW_CUDA(cudaStreamSynchronize(st));
-	const int64_t max_rounds = max_chunks;
-	if ((rc = grow<int64_t>(w->round_off, (size_t)max_rounds + 2)))
-		return rc;
+	if (!w->graph_mode) {
+		// rounds: as many as the longest segment has chunks
+		uint32_t max_chunks = 0;
+		PW_CUDA(cudaMemcpyAsync(&max_chunks, keys2, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+		PW_CUDA(cudaStreamSynchronize(st));
+		if ((int64_t)max_chunks + 2 > (int64_t)(w->round_off.bytes / sizeof(int64_t)) &&
+		    (rc = grow<int64_t>(w->round_off, (size_t)max_chunks + 2)))
+			return rc;
+	}
+	if (w->round_off.bytes < 3 * sizeof(int64_t))
+		return pw_fail(PW_ERR_CAPACITY, "graph mode: scratch not reserved for this batch");
+	const int64_t round_cap = (int64_t)(w->round_off.bytes / sizeof(int64_t)) - 2;
 	int64_t *round_off = (int64_t *)w->round_off.ptr;
-	k_rounds<<<1, 1024, 0, st>>>(keys2, n, round_off, ctr);
+	k_rounds<<<1, 1024, 0, st>>>(keys2, n, round_off, round_cap, first_step, ctr);
 	PW_CUDA(cudaGetLastError());
 	const size_t smem = warp_smem_bytes() * WARPS;
-	rc = set_smem_attr((const void *)k_segments, smem);
-	if (rc)
+	if (!w->graph_mode && (rc = set_smem_attr((const void *)k_segments, smem)))
 		return rc;
-	const int grid = persistent_grid(w, (const void *)k_segments, smem);
+	const int grid = launch_grid(w, 1, (const void *)k_segments, smem);
 	RetestEntry *rq = (RetestEntry *)w->retest.ptr;
 	StateSrc src{ nullptr, from, to, params, ckpt, anchors };
-	rc = mark(w, 0, st);
-	if (rc)
+	if (!w->graph_mode && (rc = mark(w, 0, st)))
 		return rc;
-	k_segments<<<grid, WARPS * 32, smem, st>>>(w->dev, src, vals2, round_off, max_rounds, first_step, ctr, rq,
-	                                           soft_cap_of(w));
-	mark(w, 1, st);
+	k_segments<<<grid, WARPS * 32, smem, st>>>(w->dev, src, vals2, round_off, round_off + round_cap + 1, first_step,
+	                                           ctr, rq, launch_soft_cap(w, 1));
+	if (!w->graph_mode)
+		mark(w, 1, st);
 	k_retest<RETEST_CAP><<<w->num_sms * 4, 256, 0, st>>>(w->dev, src, nullptr, first_step, ctr, rq);
-	mark(w, 2, st);
-	w->timed = true;
+	if (!w->graph_mode) {
+		mark(w, 2, st);
+		w->timed = true;
+	}
 	k_seg_finalize<<<G, B, 0, st>>>(first_step, params, n, ctr);
 	PW_CUDA(cudaGetLastError());
+	return PW_OK;
+}
+
+extern "C" int pw_world_set_graph_mode(pw_world *w, int on)
+{
+	if (!w)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_set_graph_mode: world is NULL");
+	if (on && w->ready) {
+		// the attributes and occupancy queries the launches need, outside any capture
+		PW_CUDA(cudaSetDevice(w->device));
+		int rc = ensure_query_scratch(w);
+		if (rc || (rc = set_smem_attr((const void *)k_segments, warp_smem_bytes() * WARPS)) ||
+		    (rc = set_smem_attr((const void *)k_states<RETEST_CAP>, warp_smem_bytes() * WARPS)))
+			return rc;
+		launch_grid(w, 0, (const void *)k_states<RETEST_CAP>, warp_smem_bytes() * WARPS);
+		launch_grid(w, 1, (const void *)k_segments, warp_smem_bytes() * WARPS);
+	}
+	w->graph_mode = on != 0;
+	return PW_OK;
+}
+
+extern "C" int pw_segments_reserve(pw_world *w, int64_t n, int64_t total_chunks, int64_t max_chunks)
+{
+	int rc = check_ready(w, "pw_segments_reserve");
+	if (rc)
+		return rc;
+	if (n < 0 || total_chunks < 0 || max_chunks < 0 || n > (int64_t(1) << 31) - 1)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_segments_reserve: bad sizes");
+	PW_CUDA(cudaSetDevice(w->device));
+	if ((rc = ensure_query_scratch(w)) || (rc = grow<SegParams>(w->seg_params, n)) ||
+	    (rc = grow<int64_t>(w->misc, 2 * n + 2)) || (rc = grow<uint32_t>(w->seg_keys, n)) ||
+	    (rc = grow<uint32_t>(w->seg_order, n)) || (rc = grow<uint32_t>(w->seg_keys2, n)) ||
+	    (rc = grow<uint32_t>(w->seg_order2, n)) || (rc = grow<double>(w->seg_ckpt, total_chunks + 1)) ||
+	    (rc = grow<QFs>(w->seg_anchor, total_chunks + 1)) || (rc = grow<int64_t>(w->round_off, max_chunks + 2)))
+		return rc;
+	size_t t1 = 0, t2 = 0;
+	PW_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, t1, (int64_t *)nullptr, (int64_t *)nullptr, (int)(n + 1)));
+	PW_CUDA(cub::DeviceRadixSort::SortPairsDescending(nullptr, t2, (uint32_t *)nullptr, (uint32_t *)nullptr,
+	                                                  (uint32_t *)nullptr, (uint32_t *)nullptr, (int)n, 0, 32));
+	PW_CUDA(w->cub_tmp.reserve(std::max(t1, t2)));
+	return PW_OK;
+}
+
+extern "C" int pw_world_set_launch_config(pw_world *w, int kernel, int width, int soft_cap, int blocks)
+{
+	if (!w || kernel < 0 || kernel > 1 || width < 0 || width > 32 || soft_cap < 0 || blocks < 0)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_set_launch_config: bad argument");
+	if (soft_cap > 0 && soft_cap < 64)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_set_launch_config: soft_cap below 64");
+	w->launch_width[kernel] = width;
+	w->launch_soft_cap[kernel] = soft_cap;
+	w->launch_blocks[kernel] = blocks;
+	w->grid_cache[kernel] = 0;
+	return PW_OK;
+}
+
+extern "C" int pw_world_get_launch_config(pw_world *w, int kernel, int *width, int *soft_cap, int *blocks)
+{
+	if (!w || kernel < 0 || kernel > 1 || !width || !soft_cap || !blocks)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_get_launch_config: bad argument");
+	*width = launch_width(w, kernel);
+	*soft_cap = w->ready ? launch_soft_cap(w, kernel) : w->launch_soft_cap[kernel];
+	*blocks = w->launch_blocks[kernel];
+	if (*blocks == 0 && w->ready) {
+		const void *k = kernel == 0 ? (const void *)k_states<RETEST_CAP> : (const void *)k_segments;
+		PW_CUDA(cudaSetDevice(w->device));
+		int rc = set_smem_attr(k, warp_smem_bytes() * WARPS);
+		if (rc)
+			return rc;
+		*blocks = launch_grid(w, kernel, k, warp_smem_bytes() * WARPS) / (w->num_sms > 0 ? w->num_sms : 1);
+	}
 	return PW_OK;
 }
 
@@ -1321,6 +1453,7 @@ extern "C" int pw_world_last_stats(pw_world *w, pw_query_stats *out)
 	out->work_items = (int64_t)c.stat[STAT_ITEMS];
 	out->reference_checks = w->last_states >= 0 ? w->last_states : (int64_t)c.ref_checks;
 	out->detailed_chunks = (int64_t)c.stat[STAT_DETAILED];
+	out->device_errors = (int64_t)c.error;
 	if (w->timed) {
 		float a = 0.f, b = 0.f;
 		PW_CUDA(cudaEventElapsedTime(&a, w->ev[0], w->ev[1]));
@@ -1405,7 +1538,8 @@ extern "C" int pw_states_valid_noalloc(pw_world *w, const double *states, int64_
 	if (rc)
 		return rc;
 	const int grid = persistent_grid(w, (const void *)k_states<NOALLOC_RETEST_CAP>, smem);
-	k_states<NOALLOC_RETEST_CAP><<<grid, WARPS * 32, smem, st>>>(w->dev, states, n, valid, ctr, rq, soft_cap_of(w));
+	k_states<NOALLOC_RETEST_CAP><<<grid, WARPS * 32, smem, st>>>(w->dev, states, n, valid, ctr, rq, soft_cap_of(w),
+	                                                             32);
 	StateSrc src{ states, nullptr, nullptr, nullptr, nullptr, nullptr };
 	k_retest<NOALLOC_RETEST_CAP><<<w->num_sms * 4, 256, 0, st>>>(w->dev, src, valid, nullptr, ctr, rq);
 	PW_CUDA(cudaGetLastError());

@@ -217,6 +217,25 @@ class UnitWorld:
         """isValidTransition for a batch of aligned pairs (bool [N])."""
         return self.first_contact_steps(q0, q1, initial_verify_delta, _lib.PW_SEG_TRANSITION) == _lib.PW_STEP_FREE
 
+    # graph mode and launch configuration -------------------------------------
+    def set_graph_mode(self, on: bool) -> None:
+        """Segment queries without host synchronisation or allocation (CUDA-graph capturable)."""
+        check(self._L.pw_world_set_graph_mode(self._h, 1 if on else 0), "set_graph_mode")
+
+    def segments_reserve(self, n: int, total_chunks: int, max_chunks: int) -> None:
+        check(self._L.pw_segments_reserve(self._h, int(n), int(total_chunks), int(max_chunks)), "segments_reserve")
+
+    def set_launch_config(self, kernel: int, width: int = 0, soft_cap: int = 0, blocks: int = 0) -> None:
+        """kernel 0 = states, 1 = segments; 0 keeps a field's default."""
+        check(self._L.pw_world_set_launch_config(self._h, int(kernel), int(width), int(soft_cap), int(blocks)),
+              "set_launch_config")
+
+    def get_launch_config(self, kernel: int) -> dict:
+        w, c, b = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        check(self._L.pw_world_get_launch_config(self._h, int(kernel), ctypes.byref(w), ctypes.byref(c),
+                                                 ctypes.byref(b)), "get_launch_config")
+        return {"width": w.value, "soft_cap": c.value, "blocks": b.value}
+
     def last_stats(self) -> dict:
         st = _lib.QueryStats()
         check(self._L.pw_world_last_stats(self._h, ctypes.byref(st)), "last_stats")
