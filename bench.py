@@ -62,6 +62,8 @@ WORKLOADS = {
     "plate": ("collision checks/sec (is_valid_state, perforated plate vs torus knot)", W.cfg_plate_knot, 20_000_000),
     "surrogate": ("verified collision-free samples/sec (surrogate-guided, interlocking tori)",
                   W.cfg_interlocking_tori, 200_000_000),
+    "narrow": ("escapes through a plate hole/sec (surrogate-guided narrow-passage search, plate vs torus knot)",
+               W.cfg_plate_knot, 4_000_000),
 }
 # proposal network: FLOPs per scored state (9 -> 256 x4 -> 1; the padded input columns are not counted)
 MLP_FLOP_PER_ROW = 2 * (9 * 256 + 3 * 256 * 256 + 256)
@@ -239,6 +241,17 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize(dev)
 
+    tuned = None
+    if not args.no_autotune:
+        # launch configuration picked by the autotuner on a sample of this rank's own batch
+        from puzzletunneldiscovery_gb300.autotune import tune_segments, tune_states
+        if args.workload == "plate":
+            r = tune_states(uw, a[: min(args.n, 2_000_000)], reps=1)
+        else:
+            m = min(args.n, 100_000)
+            r = tune_segments(uw, a[:m], b[:m], DELTA, reps=1)
+        tuned = {"kernel": r.kernel, "config": r.best, "default_ms": r.default_ms, "best_ms": r.best_ms,
+                 "configs_tried": len(r.table)}
     for _ in range(args.warmup):
         work.gpu(uw, a, b)
     barrier()
@@ -266,6 +279,26 @@ def run_ours(args):
     else:
         tot_ms, tot_checks = my_ms, float(my_checks)
     value = tot_checks / (tot_ms / 1e3)
+
+    # the same query replayed as one CUDA graph (graph mode: no host synchronisation inside the step)
+    graph_ms = None
+    if args.workload == "segments":
+        from puzzletunneldiscovery_gb300.autotune import SegmentGraph
+        g = SegmentGraph(uw, a, b, DELTA)
+        g.replay()
+        gms = []
+        for i in range(args.steps):
+            flush.zero_()
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            gout = g.replay()
+            s1.record(stream)
+            torch.cuda.synchronize(dev)
+            gms.append(s0.elapsed_time(s1))
+        if not torch.equal(gout, f):
+            raise RuntimeError("graph replay changed first-contact steps")
+        graph_ms = sum(gms) / len(gms)
+        del g
 
     # end to end through the public API with host buffers (pinned), copies inside the timed region
     ha = torch.from_numpy(work.q0).pin_memory()
@@ -349,7 +382,8 @@ def run_ours(args):
                             "leaf_tests": last["leaf_tests"], "fp64_retests": last["retests"],
                             "fp64_retest_rate_per_leaf": last["retests"] / max(1, last["leaf_tests"]),
                             "inline_retests": last["inline_retests"], "retest_ms": last["retest_ms"],
-                            "step_ms": step_ms}, **extra)}
+                            "step_ms": step_ms, "autotune": tuned, "graph_replay_ms_per_step": graph_ms},
+                           **extra)}
     print(json.dumps(line))
     if ws > 1:
         dist.barrier()
@@ -518,6 +552,119 @@ def run_surrogate(args):
     print(json.dumps(line))
 
 
+def run_narrow(args):
+    """Narrow-passage search on the plate / torus-knot meshes: per step, every
+    root is expanded 64 times, expansions that carry the knot through the
+    plate plane are ranked by the network (guided) or drawn at random (plain),
+    and the top k per round are validated exactly as segments in one graph
+    replay.  Value = escapes (exactly free crossing motions) per second."""
+    import torch
+
+    import puzzletunneldiscovery_gb300 as pw
+    from puzzletunneldiscovery_gb300 import narrow as N
+    from puzzletunneldiscovery_gb300 import surrogate as S
+
+    ws, rank, local = _dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    Ve, Fe, Vr, Fr = _meshes("narrow")
+    uw = pw.UnitWorld(local)
+    uw.load_env_mesh(Ve, Fe)
+    uw.load_robot_mesh(Vr, Fr)
+    uw.scaleToUnit()
+    uw.angleModel(0.0, 0.0)
+    s = uw.scene_scale
+    lo, hi = Ve.min(0) - 0.5, Ve.max(0) + 0.5
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(2000 + rank)
+    roots = N.draw_free_roots(uw, args.n, lo, hi, gen)
+    probes = N.centre_line_probes(uw, 256, 16, every=8)
+    extent = float(np.abs(Ve[:, :2]).max()) * s
+    net = S.Surrogate(local, seed=rank)
+    search = N.NarrowPassageSearch(uw, net, probes, 0.0, extent, per_root=64, sigma_t=0.05, sigma_rot=0.1,
+                                   k=args.narrow_k, verify_delta=DELTA, retrain_labels=10_000_000, seed=rank)
+    # initial training: exact labels of the crossing expansions of separate free roots
+    t0 = time.perf_counter()
+    warm_roots = N.draw_free_roots(uw, min(args.n, 1 << 21), lo, hi, gen)
+    train_steps = search.pretrain(warm_roots, args.narrow_train_labels)
+    torch.cuda.synchronize(dev)
+    train_s = time.perf_counter() - t0
+    # the plain arm gets its own world, so that the two searches' captured graphs
+    # never invalidate each other's scratch
+    uw_plain = pw.UnitWorld(local)
+    uw_plain.load_env_mesh(Ve, Fe)
+    uw_plain.load_robot_mesh(Vr, Fr)
+    uw_plain.scaleToUnit()
+    uw_plain.angleModel(0.0, 0.0)
+    plain = N.NarrowPassageSearch(uw_plain, None, probes, 0.0, extent, per_root=64, sigma_t=0.05, sigma_rot=0.1,
+                                  k=args.narrow_k, verify_delta=DELTA, seed=rank)
+    for _ in range(args.warmup):
+        search.run(roots, guided=True)
+        plain.run(roots, guided=False)
+    g_reps, p_reps = [], []
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            g_reps.append(search.run(roots, guided=True, keep_escapes=(i == 0)))
+            p_reps.append(plain.run(roots, guided=False))
+    g_esc = sum(r.escapes for r in g_reps)
+    g_s = sum(r.seconds for r in g_reps)
+    p_esc = sum(r.escapes for r in p_reps)
+    p_s = sum(r.seconds for r in p_reps)
+    value = g_esc / g_s
+    plain_value = p_esc / p_s
+    # every escape of the first guided step again, outside the graph: false-free must be 0
+    false_free = 0
+    for frm, to in g_reps[0].escape_states:
+        if frm.shape[0]:
+            false_free += int((uw.first_contact_steps(frm, to, DELTA, 1) != -1).sum())
+    # end to end: roots from pinned host memory, escapes back to the host
+    hroots = roots.cpu().pin_memory()
+    e2e_esc, e2e_s, d2h = 0, 0.0, 0
+    for i in range(args.steps):
+        torch.cuda.synchronize(dev)
+        t = time.perf_counter()
+        droots = hroots.to(dev, non_blocking=True)
+        r = search.run(droots, guided=True, keep_escapes=True)
+        host = [(f.cpu(), t_.cpu()) for f, t_ in r.escape_states]
+        torch.cuda.synchronize(dev)
+        e2e_s += time.perf_counter() - t
+        e2e_esc += r.escapes
+        d2h = sum(f.numel() * 8 * 2 for f, _ in host)
+    if rank != 0:
+        return
+    last = g_reps[-1]
+    line = {"metric": WORKLOADS["narrow"][0], "value": value, "unit": "escapes/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * g_s / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 network (f32 accumulate) + f32/f64 exact segment checks",
+            "data": "synthetic (seeded free roots over the plate's box padded by 0.5)",
+            "config": {"workload": "narrow_passage_search/perforated_plate_vs_torus_knot", "roots": args.n,
+                       "expansions_per_root": 64, "sigma_t": 0.05, "sigma_rot": 0.1,
+                       "validated_per_round": args.narrow_k, "roots_per_round": 1 << 20,
+                       "verify_delta": DELTA, "initial_train_labels": args.narrow_train_labels,
+                       "score": "min of the network's logits at the motion's midpoint and endpoint",
+                       "retrain_every_labels": 10_000_000,
+                       "escape": "an exactly free segment along which a knot centre-line point crosses the "
+                                 "plate plane inside the plate (hence through a hole)",
+                       "l2": "per-step working set (roots and 64x expansions, GBs) > L2",
+                       "parallelism": "replicas"},
+            "roofline": None, "cpu_baseline": None,
+            "e2e": {"value": e2e_esc / e2e_s, "unit": "escapes/s", "h2d_bytes_per_step": int(hroots.numel() * 8),
+                    "d2h_bytes_per_step": int(d2h)},
+            "clocks": clk.summary(),
+            "gpu_launches": None,
+            "detail": {"plain_escapes_per_s": plain_value, "guided_over_plain": value / max(plain_value, 1e-12),
+                       "guided_yield": g_esc / max(1, sum(r.validated for r in g_reps)),
+                       "plain_yield": p_esc / max(1, sum(r.validated for r in p_reps)),
+                       "escapes_per_step": g_esc / args.steps, "plain_escapes_per_step": p_esc / args.steps,
+                       "crossing_fraction": last.crossing / max(1, last.candidates),
+                       "validated_per_step": last.validated, "rounds_per_step": last.rounds,
+                       "false_free_escapes": false_free, "retrains": sum(r.retrains for r in g_reps),
+                       "initial_train_s": train_s, "initial_train_steps": train_steps,
+                       "plain_ms_per_step": 1e3 * p_s / args.steps}}
+    print(json.dumps(line))
+
+
 def _bf16_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -616,6 +763,10 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=400, help="segments per reference-arm step")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
+    ap.add_argument("--narrow-k", type=int, default=65536, help="narrow: segments validated per round")
+    ap.add_argument("--narrow-train-labels", type=int, default=10_000_000,
+                    help="narrow: exact labels of the initial training")
     ap.add_argument("--train-labels", type=int, default=50_000_000, help="surrogate: exact labels to train on")
     ap.add_argument("--top-frac", type=float, default=0.1, help="surrogate: fraction of candidates checked")
     ap.add_argument("--e2e-n", type=int, default=20_000_000, help="surrogate: candidates per end-to-end step")
@@ -624,7 +775,13 @@ def main():
     args = ap.parse_args()
     if args.n is None:
         args.n = WORKLOADS[args.workload][2]
-    if args.workload == "surrogate":
+    if args.workload == "narrow":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no narrow-passage search with a "
+                              "learned proposal; its CPU path is timed in the plate workload"}))
+        else:
+            run_narrow(args)
+    elif args.workload == "surrogate":
         args.e2e_n = min(args.e2e_n, args.n)
         run_surrogate_reference(args) if args.impl == "reference" else run_surrogate(args)
     elif args.impl == "reference":

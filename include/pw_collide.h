@@ -154,6 +154,12 @@ PW_API int pw_intersecting_segments(pw_world *w, const double q[7], int64_t capa
  * PW_STEP_INVALID and pw_world_last_stats reports device_errors.  Off by default. */
 PW_API int pw_world_set_graph_mode(pw_world *w, int on);
 
+/* host: an identifier of the world's current query scratch (its buffers'
+ * addresses and sizes).  A call made outside graph mode may grow, and so move,
+ * the scratch: a CUDA graph captured earlier is valid only while the epoch it
+ * was captured under is unchanged. */
+PW_API int pw_world_scratch_epoch(pw_world *w, uint64_t *out);
+
 /* host: size the segment-query scratch for up to n segments with, in total, up
  * to total_chunks 32-step chunks and at most max_chunks chunks in one segment. */
 PW_API int pw_segments_reserve(pw_world *w, int64_t n, int64_t total_chunks, int64_t max_chunks);
@@ -176,6 +182,17 @@ PW_API int pw_world_get_launch_config(pw_world *w, int kernel, int *width, int *
 PW_API int pw_segments_contact_states(const double *from, const double *to, const int32_t *first_step, int64_t n,
                                       double verify_delta, double *last_free, double *contact, uint8_t *done,
                                       float *last_tau, float *tau, int *err_flag, void *stream);
+
+/* Plate crossings of expansions (narrow-passage search): for candidate i (ends
+ * [n x 7], device) from root i / per_root (roots, device), out[i] = 1 if some
+ * probe point (robot-local unit frame, probes [nprobe <= 64 x 3], device) is on
+ * different sides of the plane z = plane_z at the root and at the end, with
+ * the straight-line crossing inside |x|, |y| <= extent.  Geometry only, FP32
+ * (a candidate filter, not a verdict); no reference counterpart (the reference
+ * has no narrow-passage expansion). */
+PW_API int pw_expansion_crossings(const double *roots, const double *ends, int64_t n, int per_root,
+                                  const double *probes, int nprobe, double plane_z, double extent, uint8_t *out,
+                                  void *stream);
 
 /* host: state-frame conversions (unit_world.cc:526-539, 689-711, 713-737). */
 PW_API int pw_world_translate_to_unit(const pw_world *w, const double *in, int64_t n, double *out);

@@ -107,33 +107,48 @@ def autotune(uw, states: torch.Tensor | None = None, segments=None, verify_delta
 class SegmentGraph:
     """pw_segments_first_contact over a resident batch, captured into a CUDA graph.
 
-    The first call runs the batch normally (sizing the scratch), then the world
+    The batch first runs normally (sizing the world's scratch), then the world
     switches to graph mode and one call is captured.  ``replay()`` re-runs the
     whole query as one graph launch on the current stream and returns the
     output tensor (overwritten in place).  Inputs must stay at the same
     addresses; their contents may change if the scratch still fits (otherwise
     the affected segments report PW_STEP_INVALID and ``errors()`` is non-zero).
+
+    The graph holds the addresses of the world's scratch buffers.  Any query
+    made on the same world outside graph mode may grow (move) them, so every
+    replay first compares the world's scratch epoch with the one captured and
+    captures again when it changed.
     """
 
     def __init__(self, uw, q0: torch.Tensor, q1: torch.Tensor, verify_delta: float, mode: int = _lib.PW_SEG_TRANSIT):
         self.uw = uw
         self.q0, self.q1 = uw._dev_states(q0), uw._dev_states(q1)
         self.delta, self.mode = float(verify_delta), int(mode)
+        self.captures = 0
+        self._capture()
+
+    def _capture(self):
+        uw = self.uw
+        dev = self.q0.device
         uw.first_contact_steps(self.q0, self.q1, self.delta, self.mode)      # sizes the scratch
-        torch.cuda.synchronize(self.q0.device)
+        torch.cuda.synchronize(dev)
         uw.set_graph_mode(True)
         self.graph = torch.cuda.CUDAGraph()
-        side = torch.cuda.Stream(self.q0.device)
-        side.wait_stream(torch.cuda.current_stream(self.q0.device))
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
         try:
             with torch.cuda.stream(side):
                 with torch.cuda.graph(self.graph, stream=side):
                     self.out = uw.first_contact_steps(self.q0, self.q1, self.delta, self.mode)
         finally:
             uw.set_graph_mode(False)
-        torch.cuda.current_stream(self.q0.device).wait_stream(side)
+        torch.cuda.current_stream(dev).wait_stream(side)
+        self.epoch = uw.scratch_epoch()
+        self.captures += 1
 
     def replay(self) -> torch.Tensor:
+        if self.uw.scratch_epoch() != self.epoch:
+            self._capture()
         self.graph.replay()
         return self.out
 

@@ -1323,6 +1323,27 @@ extern "C" int pw_world_set_graph_mode(pw_world *w, int on)
 	return PW_OK;
 }
 
+extern "C" int pw_world_scratch_epoch(pw_world *w, uint64_t *out)
+{
+	if (!w || !out)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_scratch_epoch: NULL argument");
+	// FNV-1a over the addresses and sizes of every buffer a segment or state query uses
+	const DeviceBuffer *bufs[] = { &w->counters, &w->retest, &w->seg_params, &w->seg_ckpt, &w->seg_anchor,
+	                               &w->seg_keys, &w->seg_order, &w->seg_keys2, &w->seg_order2, &w->round_off,
+	                               &w->cub_tmp, &w->misc };
+	uint64_t h = 1469598103934665603ull;
+	for (const DeviceBuffer *b : bufs) {
+		const uint64_t v[2] = { (uint64_t)(uintptr_t)b->ptr, (uint64_t)b->bytes };
+		for (uint64_t x : v)
+			for (int i = 0; i < 8; i++) {
+				h ^= (x >> (8 * i)) & 0xff;
+				h *= 1099511628211ull;
+			}
+	}
+	*out = h;
+	return PW_OK;
+}
+
 extern "C" int pw_segments_reserve(pw_world *w, int64_t n, int64_t total_chunks, int64_t max_chunks)
 {
 	int rc = check_ready(w, "pw_segments_reserve");

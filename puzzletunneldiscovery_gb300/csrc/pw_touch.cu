@@ -113,3 +113,72 @@ extern "C" int pw_segments_contact_states(const double *from, const double *to, 
 	PW_CUDA(cudaGetLastError());
 	return PW_OK;
 }
+
+// ------------------------------------------------------------------ plane crossings of expansions
+//
+// Narrow-passage search on a plate: root r is expanded to `per_root`
+// endpoints (ends[r * per_root + j]).  A candidate crosses the plate if some
+// probe point of the robot (robot-local unit frame, e.g. points of a knot's
+// centre line) lies on different sides of the plane z = plane_z at the root
+// and at the endpoint, and the straight-line crossing point of that probe
+// lies within |x|, |y| <= extent.  A collision-free segment with such a
+// crossing passes the robot through a hole of the plate.  Geometry only, in
+// FP32: it selects candidates; the exact segment query decides whether the
+// motion is free.
+
+namespace {
+
+// Probe point p placed by state q, in FP32 (a candidate filter, not a verdict).
+__device__ __forceinline__ void place(const double *q, const float *p, float *o)
+{
+	const float w = (float)q[3], x = (float)q[4], y = (float)q[5], z = (float)q[6];
+	const float R[9] = { 1.f - 2.f * (y * y + z * z), 2.f * (x * y - w * z), 2.f * (x * z + w * y),
+	                     2.f * (x * y + w * z), 1.f - 2.f * (x * x + z * z), 2.f * (y * z - w * x),
+	                     2.f * (x * z - w * y), 2.f * (y * z + w * x), 1.f - 2.f * (x * x + y * y) };
+	for (int i = 0; i < 3; i++)
+		o[i] = R[3 * i] * p[0] + R[3 * i + 1] * p[1] + R[3 * i + 2] * p[2] + (float)q[i];
+}
+
+__global__ void k_expansion_crossings(const double *roots, const double *ends, int64_t n, int per_root,
+                                      const double *probes, int nprobe, float plane_z, float extent, uint8_t *out)
+{
+	__shared__ float sp[3 * 64];
+	const int np = min(nprobe, 64);
+	for (int k = threadIdx.x; k < 3 * np; k += blockDim.x)
+		sp[k] = (float)probes[k];
+	__syncthreads();
+	const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+	if (i >= n)
+		return;
+	const double *a = roots + 7 * (i / per_root), *b = ends + 7 * i;
+	uint8_t hit = 0;
+	for (int k = 0; k < np && !hit; k++) {
+		float pa[3], pb[3];
+		place(a, sp + 3 * k, pa);
+		place(b, sp + 3 * k, pb);
+		const float za = pa[2] - plane_z, zb = pb[2] - plane_z;
+		if ((za < 0.f) != (zb < 0.f) && za != zb) {
+			const float t = za / (za - zb);
+			const float x = pa[0] + t * (pb[0] - pa[0]), y = pa[1] + t * (pb[1] - pa[1]);
+			hit = fabsf(x) <= extent && fabsf(y) <= extent;
+		}
+	}
+	out[i] = hit;
+}
+
+} // namespace
+
+extern "C" int pw_expansion_crossings(const double *roots, const double *ends, int64_t n, int per_root,
+                                      const double *probes, int nprobe, double plane_z, double extent, uint8_t *out,
+                                      void *stream)
+{
+	if (n < 0 || per_root <= 0 || nprobe < 0 || nprobe > 64 ||
+	    (n > 0 && (!roots || !ends || !out || (nprobe > 0 && !probes))))
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_expansion_crossings: bad pointers or sizes (at most 64 probes)");
+	if (n == 0)
+		return PW_OK;
+	k_expansion_crossings<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+	    roots, ends, n, per_root, probes, nprobe, (float)plane_z, (float)extent, out);
+	PW_CUDA(cudaGetLastError());
+	return PW_OK;
+}

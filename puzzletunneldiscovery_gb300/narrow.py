@@ -1,0 +1,260 @@
+"""Surrogate-guided narrow-passage search: escapes of a robot through the holes
+of a plate.
+
+Free roots are expanded into perturbed endpoints (Gaussian translation,
+Gaussian rotation vector applied on the left, as osr::apply does).  A
+geometric filter (``pw_expansion_crossings``) keeps the expansions along
+which some point of the robot's centre line crosses the plate plane inside
+the plate; a collision-free such motion passes the robot through a hole.  The
+proposal network scores the endpoints of those candidates, the top k of each
+round are validated exactly as segments (``pw_segments_first_contact`` in
+is_valid_transition mode, replayed as one CUDA graph), and the free ones are
+the escapes.  Endpoint labels of the validated candidates feed the network,
+which is retrained every ``retrain_labels`` labels.  The plain search
+validates k random candidates instead.
+
+An escape is only ever counted after the exact segment query found the
+motion free, so the set of escapes holds no false-free motion whatever the
+network scores.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+from .autotune import SegmentGraph
+from .surrogate import Surrogate, uniform_states_device
+
+
+def _stream(dev):
+    return ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+
+
+def centre_line_probes(uw, rings: int, ring_size: int, every: int = 8) -> np.ndarray:
+    """Points of a tube robot's centre line in its local unit frame: the means of
+    every `every`-th ring of `ring_size` vertices (vertex i * ring_size + j)."""
+    V, _ = uw._cd(1)
+    V = V[: rings * ring_size].reshape(rings, ring_size, 3)
+    return V[::every].mean(axis=1)
+
+
+def expand(roots: torch.Tensor, per_root: int, sigma_t: float, sigma_rot: float, gen: torch.Generator):
+    """per_root endpoints per root: t + N(0, sigma_t^2 I), and the rotation by a
+    rotation vector ~ N(0, sigma_rot^2 I) applied on the left (osr_state.cc:244-259)."""
+    n = roots.shape[0] * per_root
+    dev = roots.device
+    base = roots.repeat_interleave(per_root, dim=0)
+    noise = torch.randn((n, 6), dtype=torch.float64, device=dev, generator=gen)
+    out = torch.empty_like(base)
+    out[:, :3] = base[:, :3] + sigma_t * noise[:, :3]
+    rv = sigma_rot * noise[:, 3:]
+    ang = torch.linalg.vector_norm(rv, dim=1, keepdim=True)
+    axis = torch.where(ang > 0, rv / torch.where(ang > 0, ang, torch.ones_like(ang)),
+                       torch.tensor([1.0, 0.0, 0.0], dtype=torch.float64, device=dev))
+    h = 0.5 * ang
+    w1, v1 = torch.cos(h), torch.sin(h) * axis
+    q = base[:, 3:] / torch.linalg.vector_norm(base[:, 3:], dim=1, keepdim=True)
+    w2, v2 = q[:, :1], q[:, 1:]
+    w = w1 * w2 - (v1 * v2).sum(dim=1, keepdim=True)
+    v = w1 * v2 + w2 * v1 + torch.cross(v1, v2, dim=1)
+    r = torch.cat([w, v], dim=1)
+    out[:, 3:] = r / torch.linalg.vector_norm(r, dim=1, keepdim=True)
+    return out
+
+
+def crossings(roots, ends, per_root: int, probes: torch.Tensor, plane_z: float, extent: float) -> torch.Tensor:
+    L = _lib.load()
+    out = torch.empty(ends.shape[0], dtype=torch.uint8, device=ends.device)
+    _lib.check(L.pw_expansion_crossings(ctypes.c_void_p(roots.data_ptr()), ctypes.c_void_p(ends.data_ptr()),
+                                        ends.shape[0], int(per_root), ctypes.c_void_p(probes.data_ptr()),
+                                        probes.shape[0], float(plane_z), float(extent),
+                                        ctypes.c_void_p(out.data_ptr()), _stream(ends.device)),
+               "pw_expansion_crossings")
+    return out.bool()
+
+
+def midpoints(frm: torch.Tensor, to: torch.Tensor) -> torch.Tensor:
+    """interpolate(frm, to, 1/2): the translation average and the slerp midpoint,
+    which is the normalised sum of the two unit quaternions (sign-aligned)."""
+    out = torch.empty_like(to)
+    out[:, :3] = 0.5 * (frm[:, :3] + to[:, :3])
+    qa = frm[:, 3:] / torch.linalg.vector_norm(frm[:, 3:], dim=1, keepdim=True)
+    qb = to[:, 3:] / torch.linalg.vector_norm(to[:, 3:], dim=1, keepdim=True)
+    sgn = torch.where((qa * qb).sum(dim=1, keepdim=True) < 0, -1.0, 1.0)
+    m = qa + sgn * qb
+    out[:, 3:] = m / torch.linalg.vector_norm(m, dim=1, keepdim=True)
+    return out
+
+
+def draw_free_roots(uw, n: int, lo, hi, gen: torch.Generator, chunk: int = 1 << 22) -> torch.Tensor:
+    """n collision-free states, translation uniform in the box [lo, hi] (world
+    units, scaled to the unit frame), uniform rotation."""
+    dev = uw._device
+    got, total = [], 0
+    lo = np.asarray(lo, np.float64)
+    hi = np.asarray(hi, np.float64)
+    while total < n:
+        q = uniform_states_device(chunk, 0.0, 1.0, 1.0, gen, dev)
+        q[:, :3] = (torch.from_numpy(lo).to(dev) + q[:, :3] * torch.from_numpy(hi - lo).to(dev)) * uw.scene_scale
+        q = q[uw.is_valid_states(q)]
+        got.append(q)
+        total += q.shape[0]
+    return torch.cat(got)[:n].contiguous()
+
+
+@dataclass
+class SearchReport:
+    rounds: int = 0
+    candidates: int = 0
+    crossing: int = 0
+    validated: int = 0
+    escapes: int = 0
+    labels: int = 0
+    retrains: int = 0
+    seconds: float = 0.0
+    escape_states: list = field(default_factory=list)   # (from, to) device tensors of the escapes
+
+    @property
+    def escapes_per_s(self):
+        return self.escapes / self.seconds if self.seconds > 0 else 0.0
+
+    @property
+    def yield_(self):
+        return self.escapes / max(1, self.validated)
+
+
+class NarrowPassageSearch:
+    """One world (plate + robot), one network; rounds of expansion, filter,
+    ranking and exact validation."""
+
+    def __init__(self, uw, net: Surrogate | None, probes: np.ndarray, plane_z: float, extent: float,
+                 per_root: int = 64, sigma_t: float = 0.05, sigma_rot: float = 0.1, k: int = 65536,
+                 verify_delta: float = 0.001, retrain_labels: int = 10_000_000, seed: int = 0):
+        self.uw, self.net = uw, net
+        self.dev = uw._device
+        self.probes = torch.from_numpy(np.ascontiguousarray(probes, np.float64)).to(self.dev)
+        self.plane_z, self.extent = float(plane_z), float(extent)
+        self.per_root, self.k = int(per_root), int(k)
+        self.sigma_t = float(sigma_t) * uw.scene_scale      # world units -> unit frame
+        self.sigma_rot = float(sigma_rot)
+        self.delta = float(verify_delta)
+        self.retrain_labels = int(retrain_labels)
+        self.gen = torch.Generator(device=self.dev)
+        self.gen.manual_seed(seed)
+        self._lab_q, self._lab_y, self._nlab = [], [], 0
+        # static segment buffers, validated by one captured graph per round
+        self.a = torch.zeros((self.k, 7), dtype=torch.float64, device=self.dev)
+        self.b = torch.zeros((self.k, 7), dtype=torch.float64, device=self.dev)
+        self.a[:, 3] = 1.0
+        self.b[:, 3] = 1.0
+        self.graph = None
+
+    def _validate(self, frm, to):
+        """First-contact codes (is_valid_transition mode) of up to k segments via the graph."""
+        m = frm.shape[0]
+        self.a[:m].copy_(frm)
+        self.b[:m].copy_(to)
+        if m < self.k:
+            self.a[m:].copy_(self.a[:1].expand(self.k - m, 7))   # zero-length fillers: no step is checked
+            self.b[m:].copy_(self.a[:1].expand(self.k - m, 7))
+        if self.graph is None:
+            # the first batch sizes the scratch; the graph then replays within it
+            self.graph = SegmentGraph(self.uw, self.a, self.b, self.delta, _lib.PW_SEG_TRANSITION)
+        out = self.graph.replay()
+        if bool((out == _lib.PW_STEP_INVALID).any()):
+            # longer segments than the captured scratch holds: size again and re-capture
+            self.graph._capture()
+            out = self.graph.replay()
+        return out[:m]
+
+    def _label(self, q, y):
+        if self.net is None:
+            return 0
+        self._lab_q.append(q)
+        self._lab_y.append(y.to(torch.uint8))
+        self._nlab += q.shape[0]
+        if self._nlab < self.retrain_labels:
+            return 0
+        Q, Y = torch.cat(self._lab_q), torch.cat(self._lab_y)
+        perm = torch.randperm(Q.shape[0], device=self.dev, generator=self.gen)
+        for s in range(0, Q.shape[0] - 65535, 65536):
+            idx = perm[s:s + 65536]
+            self.net.train_step(Q[idx], Y[idx], 1e-3)
+        self._lab_q, self._lab_y, self._nlab = [], [], 0
+        return 1
+
+    def pretrain(self, roots: torch.Tensor, labels: int, roots_per_round: int = 1 << 20, batch: int = 65536,
+                 lr: float = 1e-3) -> int:
+        """Train the network on exact labels of the midpoints and endpoints of the
+        crossing expansions of `roots` (the search's own candidate distribution);
+        returns the number of Adam steps."""
+        steps, seen = 0, 0
+        while seen < labels:
+            for r0 in range(0, roots.shape[0], roots_per_round):
+                R = roots[r0:r0 + roots_per_round]
+                ends = expand(R, self.per_root, self.sigma_t, self.sigma_rot, self.gen)
+                idx = torch.nonzero(crossings(R, ends, self.per_root, self.probes, self.plane_z,
+                                              self.extent)).flatten()
+                if idx.shape[0] == 0:
+                    continue
+                ct = ends.index_select(0, idx)
+                q = torch.cat([midpoints(R.index_select(0, idx // self.per_root), ct), ct])
+                y = self.uw.is_valid_states(q)
+                perm = torch.randperm(q.shape[0], device=self.dev, generator=self.gen)
+                for s in range(0, q.shape[0] - batch + 1, batch):
+                    sel = perm[s:s + batch]
+                    self.net.train_step(q[sel], y[sel], lr)
+                    steps += 1
+                seen += q.shape[0]
+                if seen >= labels:
+                    break
+        return steps
+
+    def run(self, roots: torch.Tensor, guided: bool, roots_per_round: int = 1 << 20,
+            keep_escapes: bool = False) -> SearchReport:
+        rep = SearchReport()
+        torch.cuda.synchronize(self.dev)
+        t0 = time.perf_counter()
+        for r0 in range(0, roots.shape[0], roots_per_round):
+            R = roots[r0:r0 + roots_per_round]
+            ends = expand(R, self.per_root, self.sigma_t, self.sigma_rot, self.gen)
+            cross = crossings(R, ends, self.per_root, self.probes, self.plane_z, self.extent)
+            idx = torch.nonzero(cross).flatten()
+            rep.candidates += ends.shape[0]
+            rep.crossing += int(idx.shape[0])
+            if idx.shape[0] == 0:
+                rep.rounds += 1
+                continue
+            k = min(self.k, int(idx.shape[0]))
+            if guided and self.net is not None:
+                # a crossing motion is free only if the robot threads the hole: score the
+                # motion's midpoint and its endpoint, and rank by the weaker of the two
+                cf = R.index_select(0, idx // self.per_root)
+                ct = ends.index_select(0, idx)
+                score = torch.minimum(self.net.score(midpoints(cf, ct)), self.net.score(ct))
+                pick = idx[torch.topk(score, k, sorted=False).indices]
+            else:
+                pick = idx[torch.randperm(idx.shape[0], device=self.dev, generator=self.gen)[:k]]
+            frm = R.index_select(0, pick // self.per_root)
+            to = ends.index_select(0, pick)
+            codes = self._validate(frm, to)
+            free = codes == _lib.PW_STEP_FREE
+            rep.validated += k
+            rep.escapes += int(free.sum())
+            if keep_escapes:
+                rep.escape_states.append((frm[free].clone(), to[free].clone()))
+            # exact labels of the validated motions' midpoints train the network
+            if guided and self.net is not None:
+                mid = midpoints(frm, to)
+                rep.retrains += self._label(mid, self.uw.is_valid_states(mid))
+                rep.labels += k
+            rep.rounds += 1
+        torch.cuda.synchronize(self.dev)
+        rep.seconds = time.perf_counter() - t0
+        return rep

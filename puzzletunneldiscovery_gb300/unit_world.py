@@ -222,6 +222,12 @@ class UnitWorld:
         """Segment queries without host synchronisation or allocation (CUDA-graph capturable)."""
         check(self._L.pw_world_set_graph_mode(self._h, 1 if on else 0), "set_graph_mode")
 
+    def scratch_epoch(self) -> int:
+        """Identifier of the current query scratch; a captured graph is valid while it is unchanged."""
+        e = ctypes.c_uint64()
+        check(self._L.pw_world_scratch_epoch(self._h, ctypes.byref(e)), "scratch_epoch")
+        return int(e.value)
+
     def segments_reserve(self, n: int, total_chunks: int, max_chunks: int) -> None:
         check(self._L.pw_segments_reserve(self._h, int(n), int(total_chunks), int(max_chunks)), "segments_reserve")
 

@@ -32,9 +32,16 @@ def test_segment_graph_replay_matches_direct_call(built_lib):
         torch.cuda.synchronize()
         assert torch.equal(got, want)
     assert g.errors() == 0
-    # graph mode is off again: ordinary calls still size their own scratch
-    q0b, q1b = W.segment_batch(30000, -2.0, 2.0, uw.scene_scale, seed=42)
+    # graph mode is off again: ordinary calls still size their own scratch, and a
+    # call that grows (moves) it makes the next replay capture again
+    q0b, q1b = W.segment_batch(60000, -2.0, 2.0, uw.scene_scale, seed=42)
+    e0 = uw.scratch_epoch()
     uw.first_contact_steps(torch.from_numpy(q0b).cuda(), torch.from_numpy(q1b).cuda(), 0.001)
+    assert uw.scratch_epoch() != e0
+    got = g.replay()
+    torch.cuda.synchronize()
+    assert g.captures == 2
+    assert torch.equal(got, want)
 
 
 def test_graph_mode_over_capacity_reports_invalid(built_lib):

@@ -110,3 +110,13 @@ def test_random_directions():
     b = S.random_within_sphere(1000, 2 * math.pi, rng)
     assert (np.linalg.norm(b, axis=1) <= 2 * math.pi + 1e-12).all()
     assert abs(s.mean(axis=0)).max() < 0.1
+
+
+def test_narrow_midpoint_is_the_slerp_midpoint(oracle_mod):
+    """narrow.midpoints equals interpolate(a, b, 1/2) (osr_state.cc:27-44) to rounding."""
+    from puzzletunneldiscovery_gb300 import narrow as N
+    from puzzletunneldiscovery_gb300 import workloads as W
+    q0, q1 = W.segment_batch(300, -2, 2, 0.4, seed=3)
+    m = N.midpoints(torch.from_numpy(q0), torch.from_numpy(q1)).numpy()
+    for i in range(300):
+        assert np.abs(m[i] - oracle_mod.interpolate(q0[i], q1[i], 0.5)).max() < 1e-14
