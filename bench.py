@@ -760,7 +760,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="segments")
     ap.add_argument("--n", type=int, default=None, help="units (segments or states) per GPU")
-    ap.add_argument("--ref-sample", type=int, default=400, help="segments per reference-arm step")
+    ap.add_argument("--ref-sample", type=int, default=2000, help="segments per reference-arm step")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")

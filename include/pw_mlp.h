@@ -80,6 +80,11 @@ PW_API int pw_select_top(const float *score, const double *states, int64_t n, in
 PW_API int pw_mlp_gradients(pw_mlp *m, const double *states, const uint8_t *labels, int64_t n, float *loss_out,
                             void *stream);
 
+/* Kernels of the training step: 0 (default) = tcgen05 GEMMs (TMA-loaded
+ * operands, accumulators in tensor memory); 1 = the mma.sync GEMMs (a
+ * cross-check of the same step). */
+PW_API int pw_mlp_set_training_kernels(pw_mlp *m, int use_mma);
+
 /* pw_mlp_gradients followed by one Adam step (beta1 0.9, beta2 0.999, eps 1e-8). */
 PW_API int pw_mlp_train_step(pw_mlp *m, const double *states, const uint8_t *labels, int64_t n, float lr,
                              float *loss_out, void *stream);

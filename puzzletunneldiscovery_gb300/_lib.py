@@ -41,7 +41,7 @@ EXPORTS = (
     # include/pw_mlp.h
     "pw_mlp_create", "pw_mlp_destroy", "pw_mlp_num_params", "pw_mlp_get_params", "pw_mlp_set_params",
     "pw_mlp_get_grads", "pw_mlp_predict", "pw_mlp_gradients", "pw_mlp_train_step", "pw_mlp_predict_mma",
-    "pw_mlp_check", "pw_select_top", "pw_mlp_score",
+    "pw_mlp_check", "pw_select_top", "pw_mlp_score", "pw_mlp_set_training_kernels",
 )
 
 
@@ -144,6 +144,7 @@ def load():
         "pw_mlp_predict_mma": (ctypes.c_int, [vp, vp, i64, vp, vp]),
         "pw_mlp_check": (ctypes.c_int, [vp]),
         "pw_mlp_score": (ctypes.c_int, [vp, vp, i64, vp, vp]),
+        "pw_mlp_set_training_kernels": (ctypes.c_int, [vp, ctypes.c_int]),
         "pw_select_top": (ctypes.c_int, [vp, vp, i64, i64, vp, i64, i64p, vp]),
         "pw_mlp_gradients": (ctypes.c_int, [vp, vp, vp, i64, fp, vp]),
         "pw_mlp_train_step": (ctypes.c_int, [vp, vp, vp, i64, ctypes.c_float, fp, vp]),

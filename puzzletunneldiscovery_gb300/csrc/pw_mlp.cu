@@ -8,6 +8,8 @@
 // Training: binary cross-entropy, Adam; master weights and moments FP32.
 // GEMMs are hand-written tensor-core kernels (mma.sync BF16 m16n8k16 with FP32
 // accumulation) with fused bias + SiLU epilogues.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -326,7 +328,7 @@ __global__ void k_head_loss(const float *logit, const uint8_t *label, int64_t n,
 
 // dW5 += g . h4, db5 += sum g, and G4 = (g w5^T) * SiLU'(Z4) in BF16.
 __global__ void k_head_backward(const bf16 *H4, const float *Z4, const float *g, const float *w5, int64_t n,
-                                float *dw5, float *db5, bf16 *G4)
+                                float *dw5, float *db5, bf16 *G4, bf16 *G4t = nullptr, int64_t ldt = 0)
 {
 	__shared__ float sw[H];
 	for (int k = threadIdx.x; k < H; k += blockDim.x)
@@ -341,7 +343,10 @@ __global__ void k_head_backward(const bf16 *H4, const float *Z4, const float *g,
 		for (int k = lane; k < H; k += 32) {
 			const size_t o = (size_t)row * H + k;
 			atomicAdd(&sw[k], gi * __bfloat162float(H4[o]));
-			G4[o] = __float2bfloat16_rn(gi * w5[k] * dsilu(Z4[o]));
+			const bf16 gk = __float2bfloat16_rn(gi * w5[k] * dsilu(Z4[o]));
+			G4[o] = gk;
+			if (G4t)
+				G4t[(size_t)k * ldt + row] = gk;
 		}
 	}
 	__syncthreads();
@@ -398,6 +403,35 @@ __global__ void k_to_bf16(const float *w, int64_t n, bf16 *wb, bf16 *wbt, int ro
 }
 
 #include "pw_mlp_tc.cuh"
+#include "pw_mlp_train.cuh"
+
+// Zero-padded 64-wide input rows (the tcgen05 GEMM reads K-blocks of 64) and
+// the transposed 16-wide features (the B operand of the first weight gradient).
+__global__ void k_features64(const double *states, int64_t n, bf16 *X64, bf16 *Xt, int64_t ldt)
+{
+	const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+	if (i >= n)
+		return;
+	__align__(16) bf16 f[KIN];
+	feature_row(states + 7 * i, f);
+	uint4 *o = reinterpret_cast<uint4 *>(X64 + i * 64);
+	o[0] = *reinterpret_cast<uint4 *>(f);
+	o[1] = *reinterpret_cast<uint4 *>(f + 8);
+	for (int c = 2; c < 8; c++)
+		o[c] = make_uint4(0, 0, 0, 0);
+	for (int k = 0; k < KIN; k++)
+		Xt[(size_t)k * ldt + i] = f[k];
+}
+
+// W1 [256][16] -> BF16 [256][64], zero-padded.
+__global__ void k_w1_pad(const float *W1, bf16 *out)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= H * 64)
+		return;
+	const int r = i / 64, c = i % 64;
+	out[i] = __float2bfloat16_rn(c < KIN ? W1[r * KIN + c] : 0.f);
+}
 
 // ------------------------------------------------------------------ top-k selection
 //
@@ -468,6 +502,10 @@ struct pw_mlp {
 	size_t off_wb[NLAYER];
 	DeviceBuffer acts, zs, gbuf, gbuf2, head, misc;
 	DeviceBuffer wimg;           // swizzled BF16 weight images of the tcgen05 forward kernel
+	// tcgen05 training: padded inputs, transposed activations / gradients, split-K partials
+	DeviceBuffer x64, xt, ht, gt, w1p, dw_ws;
+	int64_t tcap = 0;            // rows (multiple of 128) of the training buffers above
+	bool mma_training = false;   // train with the mma.sync kernels instead
 	bool wimg_dirty = true;
 	int num_sms = 1;
 	int64_t cap = 0;             // rows the activation buffers hold
@@ -805,9 +843,194 @@ extern "C" int pw_mlp_predict_mma(pw_mlp *m, const double *states, int64_t n, fl
 
 // Gradients of the mean binary cross-entropy of one batch into the grads block
 // (no update); *loss_out gets the loss (synchronises the stream).
+// ------------------------------------------------------------------ tcgen05 training step
+
+typedef PFN_cuTensorMapEncodeTiled_v12000 EncodeFn;
+
+static EncodeFn encode_fn()
+{
+	static EncodeFn fn = nullptr;
+	if (!fn) {
+		void *p = nullptr;
+		cudaDriverEntryPointQueryResult q;
+		if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+		        cudaSuccess &&
+		    q == cudaDriverEntryPointSuccess)
+			fn = (EncodeFn)p;
+	}
+	return fn;
+}
+
+// Tensor map of a row-major BF16 matrix [rows][cols] with row pitch `ld` elements,
+// box = 64 columns x box_rows rows, 128-byte swizzle.
+static int make_map(CUtensorMap *map, const bf16 *base, int64_t rows, int64_t cols, int64_t ld, int box_rows)
+{
+	EncodeFn enc = encode_fn();
+	if (!enc)
+		return pw_fail(PW_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+	if (((uintptr_t)base & 15) || ((ld * 2) & 15))
+		return pw_fail(PW_ERR_INTERNAL, "tensor map: base or row pitch not 16-byte aligned");
+	const cuuint64_t dims[2] = { (cuuint64_t)cols, (cuuint64_t)rows };
+	const cuuint64_t strides[1] = { (cuuint64_t)(ld * 2) };
+	const cuuint32_t box[2] = { 64u, (cuuint32_t)box_rows };
+	const cuuint32_t estr[2] = { 1u, 1u };
+	const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)base, dims, strides, box, estr,
+	                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+	                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+	if (r != CUDA_SUCCESS)
+		return pw_fail(PW_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+	return PW_OK;
+}
+
+template <int NT, int EPI, int STAGES>
+static int run_gemm(const CUtensorMap &ta, const CUtensorMap &tb, const tt::Args &a, int splits, cudaStream_t st)
+{
+	typedef tt::Cfg<NT, STAGES> C;
+	static bool attr = false;
+	if (!attr) {
+		PW_CUDA(cudaFuncSetAttribute(tt::k_gemm_tc<NT, EPI, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                             C::SMEM));
+		attr = true;
+	}
+	dim3 grid((unsigned)((a.M + tt::BM - 1) / tt::BM), (unsigned)((a.N + NT - 1) / NT), (unsigned)splits);
+	tt::k_gemm_tc<NT, EPI, STAGES><<<grid, tt::NTHREADS, C::SMEM, st>>>(ta, tb, a);
+	PW_CUDA(cudaGetLastError());
+	return PW_OK;
+}
+
+// Bias gradient: column sums of G [n][256].
+static void colsum(const bf16 *G, int64_t n, float *out, int num_sms, cudaStream_t st)
+{
+	const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)num_sms * 4));
+	const int64_t rows = (n + blocks - 1) / blocks;
+	tt::k_colsum_v<<<(unsigned)blocks, 256, 0, st>>>(G, n, rows, out);
+}
+
+static int tc_reserve(pw_mlp *m, int64_t rows)
+{
+	if (rows <= m->tcap)
+		return PW_OK;
+	const int64_t r = ((rows + 127) / 128) * 128;
+	PW_CUDA(m->x64.reserve(sizeof(bf16) * (size_t)r * 64));
+	PW_CUDA(m->xt.reserve(sizeof(bf16) * (size_t)r * KIN));
+	PW_CUDA(m->ht.reserve(sizeof(bf16) * (size_t)r * H * 3));    // H1t, H2t, H3t
+	PW_CUDA(m->gt.reserve(sizeof(bf16) * (size_t)r * H));
+	m->tcap = r;
+	return PW_OK;
+}
+
+static int mlp_backward_tc(pw_mlp *m, const double *states, const uint8_t *labels, int64_t n, cudaStream_t st,
+                           float *loss_out)
+{
+	int rc = mlp_reserve(m, n);
+	if (rc || (rc = tc_reserve(m, n)))
+		return rc;
+	const int64_t ldt = m->tcap;
+	float *P = (float *)m->params.ptr, *G = (float *)m->grads.ptr;
+	float *logit = (float *)m->head.ptr, *gs = logit + m->cap;
+	float *loss = (float *)m->misc.ptr;
+	int *err = mlp_err(m);
+	bf16 *x64 = (bf16 *)m->x64.ptr, *xt = (bf16 *)m->xt.ptr, *ht = (bf16 *)m->ht.ptr, *gt = (bf16 *)m->gt.ptr;
+	auto Ht = [&](int l) { return ht + (size_t)(l - 1) * H * ldt; };   // H_l^T, l = 1..3
+	PW_CUDA(m->w1p.reserve(sizeof(bf16) * H * 64));
+	k_w1_pad<<<(H * 64 + 255) / 256, 256, 0, st>>>(P + m->off_w[0], (bf16 *)m->w1p.ptr);
+	k_features64<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(states, n, x64, xt, ldt);
+	PW_CUDA(cudaGetLastError());
+	// forward: Z_{l+1}, H_{l+1} (row-major), H_{l+1}^T
+	for (int l = 0; l < NLAYER; l++) {
+		CUtensorMap ta, tb;
+		const int K = l == 0 ? 64 : H;
+		const bf16 *A = l == 0 ? x64 : act(m, l);
+		const bf16 *B = l == 0 ? (const bf16 *)m->w1p.ptr : (const bf16 *)m->wbf.ptr + m->off_wb[l];
+		if ((rc = make_map(&ta, A, n, K, K, tt::BM)) || (rc = make_map(&tb, B, H, K, K, 256)))
+			return rc;
+		tt::Args a;
+		memset(&a, 0, sizeof(a));
+		a.M = (int)n;
+		a.N = H;
+		a.K = K;
+		a.k_split = K;
+		a.bias = P + m->off_b[l];
+		a.Z = zbuf(m, l + 1);
+		a.Y = act(m, l + 1);
+		a.Yt = l + 1 < NLAYER ? Ht(l + 1) : nullptr;
+		a.ldt = ldt;
+		a.err = err;
+		if ((rc = run_gemm<256, tt::E_FWD, 2>(ta, tb, a, 1, st)))
+			return rc;
+	}
+	PW_CUDA(cudaMemsetAsync(G, 0, sizeof(float) * m->nparam, st));
+	PW_CUDA(cudaMemsetAsync(loss, 0, sizeof(float), st));
+	k_head_forward<<<(unsigned)((n * 32 + 255) / 256), 256, 0, st>>>(act(m, NLAYER), P + m->off_w5, P + m->off_b5, n,
+	                                                                  logit, nullptr);
+	k_head_loss<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(logit, labels, n, gs, loss);
+	bf16 *Gcur = (bf16 *)m->gbuf.ptr, *Gnext = (bf16 *)m->gbuf2.ptr;
+	tt::k_head_backward_t<<<(unsigned)std::min<int64_t>((n + 63) / 64, (int64_t)m->num_sms * 8), 256, 0, st>>>(
+	    act(m, NLAYER), zbuf(m, NLAYER), gs, P + m->off_w5, n, G + m->off_w5, G + m->off_b5, Gcur, gt, ldt);
+	PW_CUDA(cudaGetLastError());
+	// split the batch so that the weight-gradient GEMMs fill the GPU (2 M tiles each)
+	const int64_t kblocks = (n + 63) / 64;
+	const int64_t splits = std::max<int64_t>(1, std::min<int64_t>(kblocks, (int64_t)m->num_sms / 2));
+	const int k_split = (int)(((kblocks + splits - 1) / splits) * 64);
+	const int nsplit = (int)((n + k_split - 1) / k_split);
+	PW_CUDA(m->dw_ws.reserve(sizeof(float) * (size_t)nsplit * H * H));
+	for (int l = NLAYER - 1; l >= 0; l--) {
+		// dW_l = G^T X_l: A = G^T [256][n], B = X_l^T [in][n], K = batch
+		const int in = l == 0 ? KIN : H;
+		CUtensorMap ta, tb;
+		if ((rc = make_map(&ta, gt, H, n, ldt, tt::BM)) ||
+		    (rc = make_map(&tb, l == 0 ? xt : Ht(l), in, n, ldt, in == H ? 256 : 16)))
+			return rc;
+		tt::Args a;
+		memset(&a, 0, sizeof(a));
+		a.M = H;
+		a.N = in;
+		a.K = (int)n;
+		a.k_split = k_split;
+		a.C = (float *)m->dw_ws.ptr;
+		a.err = err;
+		if ((rc = in == H ? run_gemm<256, tt::E_DW, 4>(ta, tb, a, nsplit, st)
+		                  : run_gemm<16, tt::E_DW, 4>(ta, tb, a, nsplit, st)))
+			return rc;
+		const int64_t cnt = (int64_t)H * in;
+		tt::k_reduce_splits<<<(unsigned)((cnt + 255) / 256), 256, 0, st>>>((const float *)m->dw_ws.ptr, nsplit, cnt,
+		                                                                  G + m->off_w[l]);
+		colsum(Gcur, n, G + m->off_b[l], m->num_sms, st);
+		PW_CUDA(cudaGetLastError());
+		if (l == 0)
+			break;
+		// G_l = (G W_l) * SiLU'(Z_l): A = G [n][256], B = W_l^T [in][out]
+		if ((rc = make_map(&ta, Gcur, n, H, H, tt::BM)) ||
+		    (rc = make_map(&tb, (const bf16 *)m->wbft.ptr + m->off_wb[l], H, H, H, 256)))
+			return rc;
+		memset(&a, 0, sizeof(a));
+		a.M = (int)n;
+		a.N = H;
+		a.K = H;
+		a.k_split = H;
+		a.Z = zbuf(m, l);
+		a.Y = Gnext;
+		a.Yt = gt;
+		a.ldt = ldt;
+		a.err = err;
+		if ((rc = run_gemm<256, tt::E_DX, 2>(ta, tb, a, 1, st)))
+			return rc;
+		bf16 *t = Gcur;
+		Gcur = Gnext;
+		Gnext = t;
+	}
+	if (loss_out) {
+		PW_CUDA(cudaMemcpyAsync(loss_out, loss, sizeof(float), cudaMemcpyDeviceToHost, st));
+		PW_CUDA(cudaStreamSynchronize(st));
+	}
+	return PW_OK;
+}
+
 static int mlp_backward(pw_mlp *m, const double *states, const uint8_t *labels, int64_t n, cudaStream_t st,
                         float *loss_out)
 {
+	if (!m->mma_training)
+		return mlp_backward_tc(m, states, labels, n, st, loss_out);
 	int rc = mlp_reserve(m, n);
 	if (rc)
 		return rc;
@@ -886,6 +1109,14 @@ extern "C" int pw_mlp_gradients(pw_mlp *m, const double *states, const uint8_t *
 }
 
 // One Adam step on a batch (device states and 0/1 labels, 1 = free).
+extern "C" int pw_mlp_set_training_kernels(pw_mlp *m, int use_mma)
+{
+	if (!m)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_mlp_set_training_kernels: NULL network");
+	m->mma_training = use_mma != 0;
+	return PW_OK;
+}
+
 extern "C" int pw_mlp_train_step(pw_mlp *m, const double *states, const uint8_t *labels, int64_t n, float lr,
                                  float *loss_out, void *stream)
 {

@@ -109,6 +109,10 @@ class Surrogate:
                    "pw_mlp_predict_mma")
         return out
 
+    def set_training_kernels(self, use_mma: bool) -> None:
+        """Train with the mma.sync GEMMs (True) or the tcgen05 GEMMs (False, default)."""
+        _lib.check(self._L.pw_mlp_set_training_kernels(self._h, 1 if use_mma else 0), "pw_mlp_set_training_kernels")
+
     def check(self) -> None:
         """Synchronise; raise if a bounded device wait of an earlier predict gave up."""
         _lib.check(self._L.pw_mlp_check(self._h), "pw_mlp_check")

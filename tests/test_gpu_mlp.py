@@ -101,9 +101,13 @@ def test_tcgen05_forward_after_training_step(built_lib, mo):
     assert np.abs(a - want).max() <= 2e-3
 
 
+@pytest.mark.parametrize("kernels", ["tcgen05", "mma"])
 @pytest.mark.parametrize("n", [1000, 65536])
-def test_gradients_match_oracle(built_lib, mo, n):
+def test_gradients_match_oracle(built_lib, mo, n, kernels):
+    """Both training paths (tcgen05 GEMMs with TMA-loaded operands, and the
+    mma.sync GEMMs) give the oracle's gradients."""
     net = _net(3)
+    net.set_training_kernels(kernels == "mma")
     q = _states(n, 20)
     y = (np.linalg.norm(q[:, :3], axis=1) > 0.5).astype(np.uint8)
     p = net.params().astype(np.float64)
@@ -115,6 +119,23 @@ def test_gradients_match_oracle(built_lib, mo, n):
         ref = g[sl]
         err = np.linalg.norm(gd[sl] - ref)
         assert err <= 2e-2 * np.linalg.norm(ref) + 1e-9, (name, err, np.linalg.norm(ref))
+
+
+def test_training_kernels_agree(built_lib, mo):
+    """The two training paths give the same gradient, tensor by tensor, to
+    BF16-rounding accuracy (ragged batch: 30000 rows is no multiple of 128)."""
+    q = torch.from_numpy(_states(30000, 60)).cuda()
+    y = (q[:, :3].norm(dim=1) > 0.45).to(torch.uint8)
+    grads = []
+    for mma in (False, True):
+        net = _net(6)
+        net.set_training_kernels(mma)
+        net.gradients(q, y)
+        grads.append(net.grads().astype(np.float64))
+    p = _net(6).params().astype(np.float64)
+    for name, sl in _tensors(mo, p):
+        a, b = grads[0][sl], grads[1][sl]
+        assert np.linalg.norm(a - b) <= 2e-2 * np.linalg.norm(b) + 1e-9, name
 
 
 def test_adam_step_matches_oracle(built_lib, mo):
