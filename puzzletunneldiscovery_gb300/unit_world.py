@@ -407,6 +407,42 @@ class UnitWorld:
             self._last_coplanar = c[:n].copy()
             return b[:n].copy(), e[:n].copy(), m[:n].copy(), p[:n].copy()
 
+    # contact forces (unit_world.cc:1015-1057) ---------------------------------
+    def _face_normals(self, geo):
+        """Per-face unit normals of the CD mesh in its own frame (igl::per_face_normals:
+        (v1 - v0) x (v2 - v0) normalised; a degenerate face gives the zero vector)."""
+        cache = self.__dict__.setdefault("_fn_cache", {})
+        if geo not in cache:
+            V, F = self._cd(geo)
+            n = np.cross(V[F[:, 1]] - V[F[:, 0]], V[F[:, 2]] - V[F[:, 0]])
+            r = np.linalg.norm(n, axis=1, keepdims=True)
+            cache[geo] = np.where(r > 0, n / np.where(r > 0, r, 1.0), 0.0)
+        return cache[geo]
+
+    def robot_face_normals_from_indices(self, faces):
+        return self._face_normals(GEO_ROB)[np.asarray(faces, dtype=np.int64).reshape(-1)]
+
+    def scene_face_normals_from_indices(self, faces):
+        return self._face_normals(GEO_ENV)[np.asarray(faces, dtype=np.int64).reshape(-1)]
+
+    def robot_face_normals_from_index_pairs(self, faces):
+        return self.robot_face_normals_from_indices(np.asarray(faces).reshape(-1, 2)[:, 1])
+
+    def scene_face_normals_from_index_pairs(self, faces):
+        return self.scene_face_normals_from_indices(np.asarray(faces).reshape(-1, 2)[:, 0])
+
+    def force_direction_from_intersecting_segments(self, sbegins, sends, faces):
+        """(force positions, force directions) of unit_world.cc:1038-1057: the
+        segment midpoints, and (end - begin) x robot face normal, flipped to
+        agree with the environment face normal.  As in the reference, the robot
+        normal is taken in the robot's own frame."""
+        b = np.asarray(sbegins, dtype=np.float64).reshape(-1, 3)
+        e = np.asarray(sends, dtype=np.float64).reshape(-1, 3)
+        pos = (b + e) * 0.5
+        d = np.cross(e - b, self.robot_face_normals_from_index_pairs(faces))
+        dots = np.sign(np.sum(d * self.scene_face_normals_from_index_pairs(faces), axis=1))
+        return pos, d * dots[:, None]
+
     def _cd(self, geo):
         info = self._info()
         nv = info.env_vertices if geo == GEO_ENV else info.robot_vertices

@@ -258,3 +258,30 @@ def test_plate_knot_segments_parity(plate):
     gpu = uw.first_contact_steps(torch.from_numpy(q0), torch.from_numpy(q1), 0.001).cpu().numpy()
     cpu, _ = ow.segments_first_contact(q0, q1, 0.001)
     assert (gpu == cpu).all(), int((gpu != cpu).sum())
+
+
+def test_force_directions_from_contacts(tori):
+    """force_direction_from_intersecting_segments (unit_world.cc:1038-1057) on the
+    contacts of a colliding state: midpoints, and directions built from the
+    oracle's vertices."""
+    uw, ow = tori
+    q = np.array([0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0])       # robot ring through the env ring
+    b, e, mag, faces = uw.intersecting_segments(q)
+    assert len(b) > 0
+    pos, d = uw.force_direction_from_intersecting_segments(b, e, faces)
+    assert np.allclose(pos, 0.5 * (b + e))
+    Ve, Vr = ow.vertices(0), ow.vertices(1)
+    _, Fe = uw._cd(0)
+    _, Fr = uw._cd(1)
+
+    def normals(V, F, idx):
+        n = np.cross(V[F[idx, 1]] - V[F[idx, 0]], V[F[idx, 2]] - V[F[idx, 0]])
+        return n / np.linalg.norm(n, axis=1, keepdims=True)
+
+    nr = normals(Vr, Fr, faces[:, 1])
+    ne = normals(Ve, Fe, faces[:, 0])
+    want = np.cross(e - b, nr)
+    want *= np.sign(np.sum(want * ne, axis=1))[:, None]
+    assert np.allclose(d, want, atol=1e-12)
+    assert np.allclose(uw.robot_face_normals_from_index_pairs(faces), nr)
+    assert np.allclose(uw.scene_face_normals_from_indices(faces[:, 0]), ne)
