@@ -689,6 +689,73 @@ static int *mlp_err(pw_mlp *m) { return (int *)((char *)m->misc.ptr + 16); }
 
 static int mlp_forward_tc(pw_mlp *m, const double *states, int64_t n, float *prob, int logits, void *stream);
 
+// The weight-block schedule of a pair of tiles (see tc::Sched): the sequence of
+// block uses, with stages chosen by Belady's rule (evict the content whose next
+// use is farthest away); every content is released by its last use within the
+// pair, so each pair starts with an empty ring.
+static void build_schedule(int nslot, int &count, uint16_t *out)
+{
+	struct Use {
+		int block, kb;
+	};
+	std::vector<Use> uses;
+	for (int layer = 0; layer < NLAYER; layer++)
+		for (int sl = 0; sl < nslot; sl++) {
+			if (layer == 0) {
+				uses.push_back({ 0, 0 });
+				continue;
+			}
+			for (int u = 0; u < 4; u++) {
+				const int j = sl == 0 ? u : 3 - u;
+				uses.push_back({ 1 + 4 * (layer - 1) + j, j });
+			}
+		}
+	const int U = (int)uses.size();
+	std::vector<int> stage(U), load(U);
+	int content[tc::NSTAGE] = { -1, -1, -1 }, last_used[tc::NSTAGE] = { -1, -1, -1 };
+	auto next_use = [&](int block, int from) {
+		for (int k = from; k < U; k++)
+			if (uses[k].block == block)
+				return k;
+		return U + 1;
+	};
+	for (int i = 0; i < U; i++) {
+		int s = -1;
+		for (int t = 0; t < tc::NSTAGE; t++)
+			if (content[t] == uses[i].block)
+				s = t;
+		load[i] = s < 0;
+		if (s < 0) {
+			// a stage whose content is dead, the least recently used first (so that loads
+			// rotate through the ring and prefetch); else the farthest next use
+			long best = -1;
+			for (int t = 0; t < tc::NSTAGE; t++) {
+				const int nu = content[t] < 0 ? U + 1 : next_use(content[t], i);
+				const long key = nu > U ? 4L * U + (U - last_used[t]) : nu;
+				if (key > best) {
+					best = key;
+					s = t;
+				}
+			}
+			content[s] = uses[i].block;
+		}
+		stage[i] = s;
+		last_used[s] = i;
+	}
+	for (int i = 0; i < U; i++) {
+		// last use of this content: the next event on the stage is a load, or there is none
+		bool last = true;
+		for (int k = i + 1; k < U; k++)
+			if (stage[k] == stage[i]) {
+				last = load[k] != 0;
+				break;
+			}
+		out[i] = (uint16_t)(uses[i].block | (stage[i] << 4) | (load[i] << 6) | ((last ? 1 : 0) << 7) |
+		                    (uses[i].kb << 8));
+	}
+	count = U;
+}
+
 static float *mlp_head_table(pw_mlp *m)
 {
 	return (float *)((char *)m->wimg.ptr + (size_t)tc::NWBLOCK * tc::WBLOCK_BYTES);
@@ -732,6 +799,9 @@ static int mlp_forward_tc(pw_mlp *m, const double *states, int64_t n, float *pro
 		attr_set = true;
 	}
 	tc::FwdArgs a;
+	memset(&a, 0, sizeof(a));
+	build_schedule(1, a.sched.n[0], a.sched.e[0]);
+	build_schedule(2, a.sched.n[1], a.sched.e[1]);
 	a.states = states;
 	a.n = n;
 	a.wimg = (const bf16 *)m->wimg.ptr;

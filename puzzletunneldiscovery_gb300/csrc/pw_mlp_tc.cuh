@@ -16,7 +16,9 @@
 // one MUFU and one FFMA per element.
 // Weights stream through a 3-stage ring of 32 KB blocks (256 rows x 64 k), each
 // one bulk copy of an image already in the swizzled layout the MMA reads
-// (built by k_weight_image).
+// (built by k_weight_image).  The ring is used as a cache: slot B takes each
+// layer's K-blocks in reverse order, so three of the four blocks slot A used
+// are still resident (a pair loads 16 blocks instead of 26; schedule below).
 //
 // Roles (576 threads): warp 0 = weight producer and TMEM owner, warp 1 = MMA
 // issuer, warps 2..17 = epilogue (warp w reads TMEM lanes 32 (w % 4) ..).
@@ -146,6 +148,17 @@ __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence:
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
+__device__ __forceinline__ void tmem_ld16_nw(uint32_t taddr, uint32_t r[16])
+{
+	asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+	             "[%16];"
+	             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+	               "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+	               "=r"(r[15])
+	             : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16])
 {
 	uint32_t r[16];
@@ -174,7 +187,24 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b)
 // [4][256] biases b_l / 2, [256] w5, b5 (16-byte aligned rows).
 constexpr int HT_W5 = 4 * H, HT_B5 = 5 * H, HT_FLOATS = 5 * H + 4;
 
+// Weight-block schedule of one pair of tiles (entry i = i-th use of a block by
+// the MMA thread), built on the host by pw_mlp.cu: slot B walks the K-blocks of
+// each layer in reverse, so the blocks slot A left in the ring are used again
+// without a reload.  Entry bits: 0-3 block, 4-5 stage, 6 load before use,
+// 7 last use of the stage's content (release it), 8-9 K-block j of the act.
+constexpr int SCHED_MAX = 2 + 3 * 8;
+struct Sched {
+	int n[2];                          // uses of a pair with 1 / 2 live slots
+	uint16_t e[2][SCHED_MAX];
+};
+__device__ __forceinline__ int se_block(uint16_t e) { return e & 15; }
+__device__ __forceinline__ int se_stage(uint16_t e) { return (e >> 4) & 3; }
+__device__ __forceinline__ bool se_load(uint16_t e) { return (e >> 6) & 1; }
+__device__ __forceinline__ bool se_last(uint16_t e) { return (e >> 7) & 1; }
+__device__ __forceinline__ int se_kb(uint16_t e) { return (e >> 8) & 3; }
+
 struct FwdArgs {
+	Sched sched;
 	const double *states;
 	int64_t n;
 	const bf16 *wimg;        // NWBLOCK images of WBLOCK_BYTES (weights scaled by 1/2)
@@ -222,44 +252,44 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 	const uint32_t tmem = *s_tmem;
 
 	if (warp == 0) {
-		// ---------------- weight producer: per pair, per layer, per live slot, the layer's blocks
+		// ---------------- weight producer: the loads of the pair's schedule, in order
 		if (lane == 0) {
-			uint32_t it = 0;
-			int64_t last_it[NSTAGE];
-			for (int s = 0; s < NSTAGE; s++)
-				last_it[s] = -1;
+			uint32_t loads[NSTAGE] = { 0, 0, 0 };
 			bool ok = true;
 			for (int64_t tA = blockIdx.x; tA < ntiles && ok; tA += 2 * G) {
 				const int nslot = tA + G < ntiles ? 2 : 1;
-				for (int layer = 0; layer < 4 && ok; layer++)
-					for (int sl = 0; sl < nslot && ok; sl++) {
-						const int b0 = layer == 0 ? 0 : 1 + 4 * (layer - 1), nb = layer == 0 ? 1 : 4;
-						for (int b = b0; b < b0 + nb; b++, it++) {
-							const int s = it % NSTAGE;
-							if (!mbar_wait(bar(B_EMPTY + s), ((it / NSTAGE) & 1) ^ 1, s_abort, a.err, 1)) {
-								ok = false;
-								break;
-							}
-							mbar_expect_tx(bar(B_FULL + s), WBLOCK_BYTES);
-							bulk_g2s(sbase + SM_W + s * WBLOCK_BYTES,
-							         (const uint8_t *)a.wimg + (size_t)b * WBLOCK_BYTES, WBLOCK_BYTES,
-							         bar(B_FULL + s));
-							last_it[s] = it;
-						}
+				const uint16_t *E = a.sched.e[nslot - 1];
+				for (int i = 0; i < a.sched.n[nslot - 1]; i++) {
+					const uint16_t e = E[i];
+					if (!se_load(e))
+						continue;
+					const int s = se_stage(e);
+					// the stage's previous content has been released by its last use
+					if (!mbar_wait(bar(B_EMPTY + s), (loads[s] & 1) ^ 1, s_abort, a.err, 1)) {
+						ok = false;
+						break;
 					}
+					mbar_expect_tx(bar(B_FULL + s), WBLOCK_BYTES);
+					bulk_g2s(sbase + SM_W + s * WBLOCK_BYTES,
+					         (const uint8_t *)a.wimg + (size_t)se_block(e) * WBLOCK_BYTES, WBLOCK_BYTES,
+					         bar(B_FULL + s));
+					loads[s]++;
+				}
 			}
 			// copies in flight must land before the CTA leaves
 			for (int s = 0; s < NSTAGE; s++)
-				if (last_it[s] >= 0)
-					mbar_drain(bar(B_FULL + s), (uint32_t)((last_it[s] / NSTAGE) & 1));
+				if (loads[s] > 0)
+					mbar_drain(bar(B_FULL + s), (loads[s] - 1) & 1);
 		}
 	} else if (warp == 1) {
-		// ---------------- MMA issuer
+		// ---------------- MMA issuer: the pair's schedule, slot by slot within each layer
 		if (lane == 0) {
-			uint32_t it = 0, act_ph[2] = { 0, 0 };
+			uint32_t loads[NSTAGE] = { 0, 0, 0 }, act_ph[2] = { 0, 0 };
 			bool ok = true;
 			for (int64_t tA = blockIdx.x; tA < ntiles && ok; tA += 2 * G) {
 				const int nslot = tA + G < ntiles ? 2 : 1;
+				const uint16_t *E = a.sched.e[nslot - 1];
+				int i = 0;
 				for (int layer = 0; layer < 4 && ok; layer++)
 					for (int sl = 0; sl < nslot && ok; sl++) {
 						// the slot's activations of this layer are in shared memory
@@ -272,19 +302,24 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 						const uint32_t acc = tmem + (uint32_t)(sl * 256);
 						const uint32_t act = sbase + SM_ACT + sl * ACT_BYTES;
 						const int nkb = layer == 0 ? 1 : 4;
-						for (int j = 0; j < nkb; j++, it++) {
-							const int s = it % NSTAGE;
-							if (!mbar_wait(bar(B_FULL + s), (it / NSTAGE) & 1, s_abort, a.err, 2)) {
-								ok = false;
-								break;
+						for (int u = 0; u < nkb; u++, i++) {
+							const uint16_t e = E[i];
+							const int s = se_stage(e), j = se_kb(e);
+							if (se_load(e)) {
+								if (!mbar_wait(bar(B_FULL + s), loads[s] & 1, s_abort, a.err, 2)) {
+									ok = false;
+									break;
+								}
+								loads[s]++;
 							}
 							tc_fence_after();
 							const uint32_t abase = act + j * ACT_KB_BYTES;
 							const uint32_t bbase = sbase + SM_W + s * WBLOCK_BYTES;
 							const int nk = layer == 0 ? 1 : KB / 16;
 							for (int k = 0; k < nk; k++)
-								mma_bf16_ss(acc, sdesc(abase + 32 * k), sdesc(bbase + 32 * k), (j | k) != 0);
-							mma_commit(bar(B_EMPTY + s));
+								mma_bf16_ss(acc, sdesc(abase + 32 * k), sdesc(bbase + 32 * k), (u | k) != 0);
+							if (se_last(e))
+								mma_commit(bar(B_EMPTY + s));
 						}
 						if (ok)
 							mma_commit(bar(B_DONE + sl));
@@ -337,37 +372,44 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 					tc_fence_after();
 					uint8_t *act = sm + SM_ACT + sl * ACT_BYTES;
 					float head = 0.f;
-					// per K-block j of act: this warp's 16 columns j*64 + g*16 .. +15
-					for (int j = 0; j < 4; j++) {
-						const int col = j * KB + g * 16;
-						float v[16], bv[16];
+					// K-blocks of act two at a time: this warp's 16 columns j*64 + g*16 .. +15
+					for (int j0 = 0; j0 < 4; j0 += 2) {
+						uint32_t rv[2][16];
+						tmem_ld16_nw(tmem + lane_off + (uint32_t)(sl * 256 + j0 * KB + g * 16), rv[0]);
+						tmem_ld16_nw(tmem + lane_off + (uint32_t)(sl * 256 + (j0 + 1) * KB + g * 16), rv[1]);
+						tmem_wait_ld();
 #pragma unroll
-						for (int i = 0; i < 4; i++)
-							*reinterpret_cast<float4 *>(bv + 4 * i) =
-							    __ldg(reinterpret_cast<const float4 *>(bias + col) + i);
-						tmem_ld16(tmem + lane_off + (uint32_t)(sl * 256 + col), v);
-						uint32_t pk[8];
-#pragma unroll
-						for (int i = 0; i < 16; i += 2) {
-							const float h0 = v[i] + bv[i];
-							const float h1 = v[i + 1] + bv[i + 1];
-							pk[i / 2] = pack_bf16x2(fmaf(h0, tanh_fast(h0), h0), fmaf(h1, tanh_fast(h1), h1));
-						}
-						if (layer < 3) {
-							uint8_t *kb = act + j * ACT_KB_BYTES;
-							*reinterpret_cast<uint4 *>(kb + swz(r, 2 * g)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-							*reinterpret_cast<uint4 *>(kb + swz(r, 2 * g + 1)) =
-							    make_uint4(pk[4], pk[5], pk[6], pk[7]);
-						} else {
+						for (int jj = 0; jj < 2; jj++) {
+							const int j = j0 + jj;
+							const int col = j * KB + g * 16;
+							float bv[16];
 #pragma unroll
 							for (int i = 0; i < 4; i++)
 								*reinterpret_cast<float4 *>(bv + 4 * i) =
-								    __ldg(reinterpret_cast<const float4 *>(a.ht + HT_W5 + col) + i);
+								    __ldg(reinterpret_cast<const float4 *>(bias + col) + i);
+							uint32_t pk[8];
 #pragma unroll
-							for (int i = 0; i < 8; i++) {
-								const __nv_bfloat162 hh = *reinterpret_cast<__nv_bfloat162 *>(&pk[i]);
-								head = fmaf(__low2float(hh), bv[2 * i], head);
-								head = fmaf(__high2float(hh), bv[2 * i + 1], head);
+							for (int i = 0; i < 16; i += 2) {
+								const float h0 = __uint_as_float(rv[jj][i]) + bv[i];
+								const float h1 = __uint_as_float(rv[jj][i + 1]) + bv[i + 1];
+								pk[i / 2] = pack_bf16x2(fmaf(h0, tanh_fast(h0), h0), fmaf(h1, tanh_fast(h1), h1));
+							}
+							if (layer < 3) {
+								uint8_t *kb = act + j * ACT_KB_BYTES;
+								*reinterpret_cast<uint4 *>(kb + swz(r, 2 * g)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+								*reinterpret_cast<uint4 *>(kb + swz(r, 2 * g + 1)) =
+								    make_uint4(pk[4], pk[5], pk[6], pk[7]);
+							} else {
+#pragma unroll
+								for (int i = 0; i < 4; i++)
+									*reinterpret_cast<float4 *>(bv + 4 * i) =
+									    __ldg(reinterpret_cast<const float4 *>(a.ht + HT_W5 + col) + i);
+#pragma unroll
+								for (int i = 0; i < 8; i++) {
+									const __nv_bfloat162 hh = *reinterpret_cast<__nv_bfloat162 *>(&pk[i]);
+									head = fmaf(__low2float(hh), bv[2 * i], head);
+									head = fmaf(__high2float(hh), bv[2 * i + 1], head);
+								}
 							}
 						}
 					}
