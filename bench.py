@@ -652,7 +652,10 @@ def run_narrow(args):
             "e2e": {"value": e2e_esc / e2e_s, "unit": "escapes/s", "h2d_bytes_per_step": int(hroots.numel() * 8),
                     "d2h_bytes_per_step": int(d2h)},
             "clocks": clk.summary(),
-            "gpu_launches": None,
+            # this project's kernels per guided round: crossing filter 1, network scores 2, the
+            # replayed validation graph 6 (bounds, set-up, rounds, traversal, re-test, finalise;
+            # its CUB scan and sort kernels not counted), endpoint labels 2 (traversal, re-test)
+            "gpu_launches": 11 * sum(r.rounds for r in g_reps),
             "detail": {"plain_escapes_per_s": plain_value, "guided_over_plain": value / max(plain_value, 1e-12),
                        "guided_yield": g_esc / max(1, sum(r.validated for r in g_reps)),
                        "plain_yield": p_esc / max(1, sum(r.validated for r in p_reps)),

@@ -310,19 +310,4 @@ __global__ void __launch_bounds__(256) k_colsum_v(const bf16 *G, int64_t n, int6
 	atomicAdd(&out[threadIdx.x], s);
 }
 
-// Input features in both layouts: X0 [n][16] and X0t [16][ldt].
-__global__ void k_features_t(const double *states, int64_t n, bf16 *X, bf16 *Xt, int64_t ldt)
-{
-	const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-	if (i >= n)
-		return;
-	__align__(16) bf16 f[KIN];
-	feature_row(states + 7 * i, f);
-	uint4 *o = reinterpret_cast<uint4 *>(X + i * KIN);
-	o[0] = *reinterpret_cast<uint4 *>(f);
-	o[1] = *reinterpret_cast<uint4 *>(f + 8);
-	for (int k = 0; k < KIN; k++)
-		Xt[(size_t)k * ldt + i] = f[k];
-}
-
 } // namespace tt
