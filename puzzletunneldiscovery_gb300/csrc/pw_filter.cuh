@@ -152,6 +152,10 @@ PW_HD int lone3(const int *s)
 	return 0;
 }
 
+// a[i] for a runtime i in {0, 1, 2}, by selects: the arrays stay in registers
+// (indexing them with a runtime value would move them to local memory).
+PW_HD float sel3(const float *a, int i) { return i == 0 ? a[0] : (i == 1 ? a[1] : a[2]); }
+
 // Interval on the projection axis: endpoints p_l + (p_o - p_l) d_l / (d_l - d_o)
 // with p relative to a common origin.  ea[k]: error of p[k]; ei[k]: the part of
 // it that does not cancel in differences.  Returns the endpoints and a bound.
@@ -160,19 +164,21 @@ PW_HD void interval_bounds(const float *p, const float *ea, const float *ei, con
 {
 	const int o1 = lone == 0 ? 1 : 0;
 	const int o2 = lone == 2 ? 1 : 2;
-	const int oo[2] = { o1, o2 };
+	const float pl = sel3(p, lone), eal = sel3(ea, lone), eil = sel3(ei, lone);
+	const float dl = sel3(d, lone), bl = sel3(b, lone);
 	float e[2], E = 0.f;
 #pragma unroll
 	for (int k = 0; k < 2; k++) {
-		const int o = oo[k];
-		const float den = fabsf(d[lone]) + fabsf(d[o]);
-		const float bb = b[lone] + b[o];
-		const float r = d[lone] / (d[lone] - d[o]);
+		const int o = k == 0 ? o1 : o2;
+		const float d_o = sel3(d, o), b_o = sel3(b, o), p_o = sel3(p, o), ei_o = sel3(ei, o);
+		const float den = fabsf(dl) + fabsf(d_o);
+		const float bb = bl + b_o;
+		const float r = dl / (dl - d_o);
 		const float dr = bb / fmaxf(den - bb, 1e-37f) + 3.f * U32;
-		const float pd = p[o] - p[lone];
-		e[k] = fmaf(pd, r, p[lone]);
-		const float epd = ei[o] + ei[lone] + U32 * fabsf(pd);
-		const float ek = ea[lone] + epd + fabsf(pd) * dr + U32 * (fabsf(p[lone]) + 2.f * fabsf(pd));
+		const float pd = p_o - pl;
+		e[k] = fmaf(pd, r, pl);
+		const float epd = ei_o + eil + U32 * fabsf(pd);
+		const float ek = eal + epd + fabsf(pd) * dr + U32 * (fabsf(pl) + 2.f * fabsf(pd));
 		E = fmaxf(E, ek);
 	}
 	*lo = fminf(e[0], e[1]);
