@@ -285,3 +285,25 @@ def test_force_directions_from_contacts(tori):
     assert np.allclose(d, want, atol=1e-12)
     assert np.allclose(uw.robot_face_normals_from_index_pairs(faces), nr)
     assert np.allclose(uw.scene_face_normals_from_indices(faces[:, 0]), ne)
+
+
+def test_ompl_screening_of_the_alpha_path(alpha):
+    """validate_states / validate_motion_pairs (ompldriver.cc:566-621) on the alpha
+    puzzle's OMPL solution path: every waypoint and every edge is valid; shifted
+    into the puzzle, waypoints collide exactly where the oracle says."""
+    from puzzletunneldiscovery_gb300 import ompl_compat as OC
+    uw, ow, g = alpha
+    P = g["path_wlast"]
+    v = OC.validate_states(uw, P)
+    assert v.dtype == np.int32 and v.shape == (len(P),) and v.all()
+    m = OC.validate_motion_pairs(uw, P[:-1], P[1:], 0.0005)
+    assert m.shape == (len(P) - 1,) and m.all()
+    # shorter second batch: trailing rows stay 0, as in the reference
+    m2 = OC.validate_motion_pairs(uw, P[:10], P[1:6], 0.0005)
+    assert m2.shape == (10,) and m2[:5].all() and not m2[5:].any()
+    # perturbed waypoints: verdicts equal the oracle's on the converted states
+    rng = np.random.default_rng(4)
+    Q = P[rng.integers(0, len(P), 2000)].copy()
+    Q[:, :3] += rng.normal(0, 3.0, (2000, 3))
+    U = uw.translate_ompl_to_unit(Q)
+    assert (OC.validate_states(uw, Q) == ow.is_valid(U).astype(np.int32)).all()
