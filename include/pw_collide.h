@@ -194,6 +194,14 @@ PW_API int pw_expansion_crossings(const double *roots, const double *ends, int64
                                   const double *probes, int nprobe, double plane_z, double extent, uint8_t *out,
                                   void *stream);
 
+/* per_root perturbed copies of each of nroots states (device, [nroots x 7] ->
+ * out [nroots * per_root x 7]): translation + N(0, sigma_t^2 I) and a rotation
+ * vector ~ N(0, sigma_rot^2 I) applied on the left (as osr::apply,
+ * osr_state.cc:244-259).  Counter-based random numbers: the same seed gives
+ * the same candidates.  For narrow-passage expansion; no reference counterpart. */
+PW_API int pw_expand_states(const double *roots, int64_t nroots, int per_root, double sigma_t, double sigma_rot,
+                            uint64_t seed, double *out, void *stream);
+
 /* host: state-frame conversions (unit_world.cc:526-539, 689-711, 713-737). */
 PW_API int pw_world_translate_to_unit(const pw_world *w, const double *in, int64_t n, double *out);
 PW_API int pw_world_translate_from_unit(const pw_world *w, const double *in, int64_t n, double *out);

@@ -182,3 +182,95 @@ extern "C" int pw_expansion_crossings(const double *roots, const double *ends, i
 	PW_CUDA(cudaGetLastError());
 	return PW_OK;
 }
+
+// ------------------------------------------------------------------ expansions
+//
+// per_root perturbed copies of each root: translation + N(0, sigma_t^2 I),
+// and the rotation by a rotation vector ~ N(0, sigma_rot^2 I) applied on the
+// left (as osr::apply does, osr_state.cc:244-259), the result normalised.
+// Normals from a counter-based generator (SplitMix64 finaliser over
+// (seed, candidate, draw)) and the Box-Muller transform with 24-bit uniforms,
+// so a (seed, index) pair always gives the same candidate.
+
+namespace {
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z)
+{
+	z += 0x9E3779B97F4A7C15ull;
+	z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+	z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+	return z ^ (z >> 31);
+}
+
+// Two independent N(0, 1) values from one 64-bit draw, in FP32 (sampling
+// noise, not a verdict: FP32 keeps the transcendentals off GB300's narrow
+// FP64 pipe).
+__device__ __forceinline__ void normal2(uint64_t bits, float &a, float &b)
+{
+	const float u1 = ((float)(uint32_t)(bits >> 40) + 0.5f) * (1.0f / 16777216.0f);   // (0, 1)
+	const float u2 = ((float)(uint32_t)((bits >> 16) & 0xFFFFFFu) + 0.5f) * (1.0f / 16777216.0f);
+	const float r = sqrtf(-2.0f * logf(u1));
+	float s, c;
+	sincospif(2.0f * u2, &s, &c);
+	a = r * c;
+	b = r * s;
+}
+
+__global__ void k_expand(const double *roots, int64_t n, int per_root, double sigma_t, double sigma_rot,
+                         uint64_t seed, double *out)
+{
+	const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+	if (i >= n)
+		return;
+	const double *q = roots + 7 * (i / per_root);
+	const uint64_t base = mix64(seed ^ mix64((uint64_t)i));
+	float g[6];
+	normal2(mix64(base + 1), g[0], g[1]);
+	normal2(mix64(base + 2), g[2], g[3]);
+	normal2(mix64(base + 3), g[4], g[5]);
+	double *o = out + 7 * i;
+	for (int c = 0; c < 3; c++)
+		o[c] = q[c] + sigma_t * (double)g[c];
+	const float sr = (float)sigma_rot;
+	const float rx = sr * g[3], ry = sr * g[4], rz = sr * g[5];
+	const float ang = sqrtf(rx * rx + ry * ry + rz * rz);
+	float w1 = 1.f, x1 = 0.f, y1 = 0.f, z1 = 0.f;
+	if (ang > 0.f) {
+		float sh, ch;
+		sincosf(0.5f * ang, &sh, &ch);
+		sh /= ang;
+		w1 = ch;
+		x1 = rx * sh;
+		y1 = ry * sh;
+		z1 = rz * sh;
+	}
+	// the endpoint's rotation in FP32 (it is a random perturbation; the segment query
+	// normalises and interpolates it in FP64 from the stored value)
+	const float w2 = (float)q[3], x2 = (float)q[4], y2 = (float)q[5], z2 = (float)q[6];
+	const float w = w1 * w2 - x1 * x2 - y1 * y2 - z1 * z2;
+	const float x = w1 * x2 + x1 * w2 + y1 * z2 - z1 * y2;
+	const float y = w1 * y2 - x1 * z2 + y1 * w2 + z1 * x2;
+	const float z = w1 * z2 + x1 * y2 - y1 * x2 + z1 * w2;
+	const float im = rsqrtf(w * w + x * x + y * y + z * z);
+	o[3] = (double)(w * im);
+	o[4] = (double)(x * im);
+	o[5] = (double)(y * im);
+	o[6] = (double)(z * im);
+}
+
+} // namespace
+
+extern "C" int pw_expand_states(const double *roots, int64_t nroots, int per_root, double sigma_t, double sigma_rot,
+                                uint64_t seed, double *out, void *stream)
+{
+	if (nroots < 0 || per_root <= 0 || !(sigma_t >= 0.0) || !(sigma_rot >= 0.0) ||
+	    (nroots > 0 && (!roots || !out)))
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_expand_states: bad pointers, sizes or deviations");
+	const int64_t n = nroots * per_root;
+	if (n == 0)
+		return PW_OK;
+	k_expand<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(roots, n, per_root, sigma_t, sigma_rot,
+	                                                                      seed, out);
+	PW_CUDA(cudaGetLastError());
+	return PW_OK;
+}

@@ -44,27 +44,16 @@ def centre_line_probes(uw, rings: int, ring_size: int, every: int = 8) -> np.nda
     return V[::every].mean(axis=1)
 
 
-def expand(roots: torch.Tensor, per_root: int, sigma_t: float, sigma_rot: float, gen: torch.Generator):
-    """per_root endpoints per root: t + N(0, sigma_t^2 I), and the rotation by a
-    rotation vector ~ N(0, sigma_rot^2 I) applied on the left (osr_state.cc:244-259)."""
-    n = roots.shape[0] * per_root
-    dev = roots.device
-    base = roots.repeat_interleave(per_root, dim=0)
-    noise = torch.randn((n, 6), dtype=torch.float64, device=dev, generator=gen)
-    out = torch.empty_like(base)
-    out[:, :3] = base[:, :3] + sigma_t * noise[:, :3]
-    rv = sigma_rot * noise[:, 3:]
-    ang = torch.linalg.vector_norm(rv, dim=1, keepdim=True)
-    axis = torch.where(ang > 0, rv / torch.where(ang > 0, ang, torch.ones_like(ang)),
-                       torch.tensor([1.0, 0.0, 0.0], dtype=torch.float64, device=dev))
-    h = 0.5 * ang
-    w1, v1 = torch.cos(h), torch.sin(h) * axis
-    q = base[:, 3:] / torch.linalg.vector_norm(base[:, 3:], dim=1, keepdim=True)
-    w2, v2 = q[:, :1], q[:, 1:]
-    w = w1 * w2 - (v1 * v2).sum(dim=1, keepdim=True)
-    v = w1 * v2 + w2 * v1 + torch.cross(v1, v2, dim=1)
-    r = torch.cat([w, v], dim=1)
-    out[:, 3:] = r / torch.linalg.vector_norm(r, dim=1, keepdim=True)
+def expand(roots: torch.Tensor, per_root: int, sigma_t: float, sigma_rot: float, seed: int) -> torch.Tensor:
+    """per_root endpoints per root (pw_expand_states): t + N(0, sigma_t^2 I), and the
+    rotation by a rotation vector ~ N(0, sigma_rot^2 I) applied on the left
+    (osr_state.cc:244-259).  The same seed gives the same endpoints."""
+    L = _lib.load()
+    roots = roots.contiguous()
+    out = torch.empty((roots.shape[0] * per_root, 7), dtype=torch.float64, device=roots.device)
+    _lib.check(L.pw_expand_states(ctypes.c_void_p(roots.data_ptr()), roots.shape[0], int(per_root),
+                                  float(sigma_t), float(sigma_rot), ctypes.c_uint64(seed & (2**64 - 1)),
+                                  ctypes.c_void_p(out.data_ptr()), _stream(roots.device)), "pw_expand_states")
     return out
 
 
@@ -147,6 +136,7 @@ class NarrowPassageSearch:
         self.retrain_labels = int(retrain_labels)
         self.gen = torch.Generator(device=self.dev)
         self.gen.manual_seed(seed)
+        self.seed, self.calls = int(seed), 0
         self._lab_q, self._lab_y, self._nlab = [], [], 0
         # static segment buffers, validated by one captured graph per round
         self.a = torch.zeros((self.k, 7), dtype=torch.float64, device=self.dev)
@@ -154,6 +144,10 @@ class NarrowPassageSearch:
         self.a[:, 3] = 1.0
         self.b[:, 3] = 1.0
         self.graph = None
+
+    def _next_seed(self) -> int:
+        self.calls += 1
+        return (self.seed * 0x9E3779B97F4A7C15 + self.calls) & (2**64 - 1)
 
     def _validate(self, frm, to):
         """First-contact codes (is_valid_transition mode) of up to k segments via the graph."""
@@ -164,14 +158,31 @@ class NarrowPassageSearch:
             self.a[m:].copy_(self.a[:1].expand(self.k - m, 7))   # zero-length fillers: no step is checked
             self.b[m:].copy_(self.a[:1].expand(self.k - m, 7))
         if self.graph is None:
-            # the first batch sizes the scratch; the graph then replays within it
+            # size the scratch for this batch with headroom, so that later batches of the
+            # same distribution replay without a new capture
+            self._reserve(1.5)
             self.graph = SegmentGraph(self.uw, self.a, self.b, self.delta, _lib.PW_SEG_TRANSITION)
         out = self.graph.replay()
         if bool((out == _lib.PW_STEP_INVALID).any()):
-            # longer segments than the captured scratch holds: size again and re-capture
+            # longer segments than the reserved scratch holds: reserve more and capture again
+            self._reserve(2.0)
             self.graph._capture()
             out = self.graph.replay()
         return out[:m]
+
+    def _reserve(self, headroom: float):
+        """Reserve segment scratch for the current k buffers times `headroom`: chunk
+        counts bounded from the distances (translation norm + rotation angle,
+        the engine's metric) of the segments in the buffers."""
+        qa = self.a[:, 3:] / torch.linalg.vector_norm(self.a[:, 3:], dim=1, keepdim=True)
+        qb = self.b[:, 3:] / torch.linalg.vector_norm(self.b[:, 3:], dim=1, keepdim=True)
+        ang = 2.0 * torch.acos(torch.clamp((qa * qb).sum(dim=1).abs(), max=1.0))
+        dist = torch.linalg.vector_norm(self.b[:, :3] - self.a[:, :3], dim=1) + ang
+        # is_valid_transition steps at min(dist / 2, delta): at least 2 steps per segment
+        chunks = torch.ceil((torch.ceil(dist / self.delta) + 2.0) / 32.0) + 1.0
+        total = int(chunks.sum().item() * headroom) + 1024
+        longest = int(chunks.max().item() * headroom) + 8
+        self.uw.segments_reserve(self.k, total, longest)
 
     def _label(self, q, y):
         if self.net is None:
@@ -198,7 +209,7 @@ class NarrowPassageSearch:
         while seen < labels:
             for r0 in range(0, roots.shape[0], roots_per_round):
                 R = roots[r0:r0 + roots_per_round]
-                ends = expand(R, self.per_root, self.sigma_t, self.sigma_rot, self.gen)
+                ends = expand(R, self.per_root, self.sigma_t, self.sigma_rot, self._next_seed())
                 idx = torch.nonzero(crossings(R, ends, self.per_root, self.probes, self.plane_z,
                                               self.extent)).flatten()
                 if idx.shape[0] == 0:
@@ -223,7 +234,7 @@ class NarrowPassageSearch:
         t0 = time.perf_counter()
         for r0 in range(0, roots.shape[0], roots_per_round):
             R = roots[r0:r0 + roots_per_round]
-            ends = expand(R, self.per_root, self.sigma_t, self.sigma_rot, self.gen)
+            ends = expand(R, self.per_root, self.sigma_t, self.sigma_rot, self._next_seed())
             cross = crossings(R, ends, self.per_root, self.probes, self.plane_z, self.extent)
             idx = torch.nonzero(cross).flatten()
             rep.candidates += ends.shape[0]

@@ -64,3 +64,60 @@ def test_small_search_escapes_are_free(built_lib, oracle_mod):
             assert done
             checked += 1
     assert rep.escapes == 0 or checked > 0
+
+
+def _mix64(z):
+    M = (1 << 64) - 1
+    z = (z + 0x9E3779B97F4A7C15) & M
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M
+    return z ^ (z >> 31)
+
+
+def _expand_ref(root, i, per_root, st, sr, seed):
+    """A restatement of pw_expand_states for one candidate (FP32 noise, FP64 product)."""
+    f32 = np.float32
+    base = _mix64(seed ^ _mix64(i))
+    g = []
+    for k in (1, 2, 3):
+        bits = _mix64((base + k) & ((1 << 64) - 1))
+        u1 = (f32(bits >> 40) + f32(0.5)) * f32(1.0 / 16777216.0)
+        u2 = (f32((bits >> 16) & 0xFFFFFF) + f32(0.5)) * f32(1.0 / 16777216.0)
+        r = np.sqrt(f32(-2.0) * np.log(u1))
+        g += [r * np.cos(f32(2.0) * np.pi * u2), r * np.sin(f32(2.0) * np.pi * u2)]
+    g = np.asarray(g, dtype=np.float64)
+    t = [root[c] + st * g[c] for c in range(3)]
+    rv = sr * g[3:6]
+    ang = np.linalg.norm(rv)
+    w1, v1 = (np.cos(ang / 2), rv * np.sin(ang / 2) / ang) if ang > 0 else (1.0, np.zeros(3))
+    q = np.asarray(root[3:], dtype=np.float64)
+    q = q / np.linalg.norm(q)
+    w2, v2 = q[0], q[1:]
+    w = w1 * w2 - np.dot(v1, v2)
+    v = w1 * v2 + w2 * v1 + np.cross(v1, v2)
+    r4 = np.concatenate([[w], v])
+    return np.concatenate([t, r4 / np.linalg.norm(r4)])
+
+
+def test_expansion_kernel(built_lib):
+    """pw_expand_states: deterministic per seed, matches a restatement of its
+    generator and rotation, and has the requested spreads."""
+    from puzzletunneldiscovery_gb300 import narrow as N
+    from puzzletunneldiscovery_gb300 import workloads as W
+    roots = torch.from_numpy(W.uniform_states(2000, -1.0, 1.0, 0.3, seed=8)).cuda()
+    a = N.expand(roots, 64, 0.02, 0.1, 77)
+    b = N.expand(roots, 64, 0.02, 0.1, 77)
+    c = N.expand(roots, 64, 0.02, 0.1, 78)
+    assert torch.equal(a, b) and not torch.equal(a, c)
+    A = a.cpu().numpy()
+    R = roots.cpu().numpy()
+    for i in (0, 1, 63, 64, 5000, 127999):
+        # FP32 noise and rotation: agreement to FP32 rounding
+        np.testing.assert_allclose(A[i], _expand_ref(R[i // 64], i, 64, 0.02, 0.1, 77), rtol=0, atol=2e-6)
+    d = A[:, :3] - np.repeat(R[:, :3], 64, axis=0)
+    assert abs(d.std() - 0.02) < 0.001 and abs(d.mean()) < 0.001
+    assert np.allclose(np.linalg.norm(A[:, 3:], axis=1), 1.0, atol=1e-6)
+    qr = np.repeat(R[:, 3:] / np.linalg.norm(R[:, 3:], axis=1, keepdims=True), 64, axis=0)
+    ang = 2 * np.arccos(np.clip(np.abs(np.sum(A[:, 3:] * qr, axis=1)), 0, 1))
+    # |rotation vector| of a 3-D N(0, 0.1^2 I) draw: mean 0.1 * sqrt(8 / pi)
+    assert abs(ang.mean() - 0.1 * np.sqrt(8 / np.pi)) < 0.005

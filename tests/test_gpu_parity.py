@@ -288,12 +288,16 @@ def test_force_directions_from_contacts(tori):
 
 
 def test_ompl_screening_of_the_alpha_path(alpha):
-    """validate_states / validate_motion_pairs (ompldriver.cc:566-621) on the alpha
-    puzzle's OMPL solution path: every waypoint and every edge is valid; shifted
-    into the puzzle, waypoints collide exactly where the oracle says."""
+    """validate_states / validate_motion_pairs (ompldriver.cc:566-621) on OMPL-frame
+    states made from the alpha puzzle's free keys (translate_unit_to_ompl, the
+    inverse of the translateOMPLStateToUnitState rule they are checked with):
+    every key and every edge between consecutive keys is valid; perturbed
+    states collide exactly where the oracle says."""
     from puzzletunneldiscovery_gb300 import ompl_compat as OC
     uw, ow, g = alpha
-    P = g["path_wlast"]
+    K = uw.translate_to_unit_state(g["keys_wfirst"])
+    P = uw.translate_unit_to_ompl(K)
+    np.testing.assert_allclose(uw.translate_ompl_to_unit(P), K, rtol=1e-9, atol=1e-12)
     v = OC.validate_states(uw, P)
     assert v.dtype == np.int32 and v.shape == (len(P),) and v.all()
     m = OC.validate_motion_pairs(uw, P[:-1], P[1:], 0.0005)
@@ -301,9 +305,11 @@ def test_ompl_screening_of_the_alpha_path(alpha):
     # shorter second batch: trailing rows stay 0, as in the reference
     m2 = OC.validate_motion_pairs(uw, P[:10], P[1:6], 0.0005)
     assert m2.shape == (10,) and m2[:5].all() and not m2[5:].any()
-    # perturbed waypoints: verdicts equal the oracle's on the converted states
+    # perturbed states: verdicts equal the oracle's on the converted states
     rng = np.random.default_rng(4)
     Q = P[rng.integers(0, len(P), 2000)].copy()
     Q[:, :3] += rng.normal(0, 3.0, (2000, 3))
     U = uw.translate_ompl_to_unit(Q)
-    assert (OC.validate_states(uw, Q) == ow.is_valid(U).astype(np.int32)).all()
+    got = OC.validate_states(uw, Q)
+    assert 0 < got.sum() < len(Q)
+    assert (got == ow.is_valid(U).astype(np.int32)).all()
