@@ -6,7 +6,7 @@
  * engine's own: it scores SE(3) states by their probability of being
  * collision free so that samplers spend exact checks (pw_states_valid,
  * pw_segments_first_contact) where free space is likely.  The exact queries
- * stay the judge: a score is never a verdict.
+ * stay the arbiter: a score is never a verdict.
  *
  * Network: features f(q) = [x, y, z, R(q)[:,0], R(q)[:,1]] (9 values, padded
  * to 16 with zeros), 4 hidden layers of width 256 with SiLU, one sigmoid

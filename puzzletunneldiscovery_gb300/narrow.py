@@ -20,7 +20,6 @@ network scores.
 from __future__ import annotations
 
 import ctypes
-import math
 import time
 from dataclasses import dataclass, field
 
