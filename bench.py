@@ -214,6 +214,20 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def max_time_sum_units(ms, units, world, device):
+    """Whole-job figures over the ranks: the slowest rank's time and the units all
+    ranks processed (weak scaling: each rank times its own batch)."""
+    if world <= 1:
+        return float(ms), float(units)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    c = torch.tensor([float(units)], device=device, dtype=torch.float64)
+    dist.all_reduce(c, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(c.item())
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -270,14 +284,7 @@ def run_ours(args):
     step_ms = [s.elapsed_time(e) for s, e in ev]
     my_ms = sum(step_ms)
     my_checks = sum(s["reference_checks"] for s in stats)
-    if ws > 1:
-        t = torch.tensor([my_ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        c = torch.tensor([my_checks], device=dev, dtype=torch.float64)
-        dist.all_reduce(c, op=dist.ReduceOp.SUM)
-        tot_ms, tot_checks = float(t.item()), float(c.item())
-    else:
-        tot_ms, tot_checks = my_ms, float(my_checks)
+    tot_ms, tot_checks = max_time_sum_units(my_ms, my_checks, ws, dev)
     value = tot_checks / (tot_ms / 1e3)
 
     # the same query replayed as one CUDA graph (graph mode: no host synchronisation inside the step)
@@ -318,12 +325,7 @@ def run_ours(args):
         torch.cuda.synchronize(dev)
         e2e_ms += s0.elapsed_time(s1)
         e2e_checks += uw.last_stats()["reference_checks"]
-    if ws > 1:
-        t = torch.tensor([e2e_ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        c = torch.tensor([e2e_checks], device=dev, dtype=torch.float64)
-        dist.all_reduce(c, op=dist.ReduceOp.SUM)
-        e2e_ms, e2e_checks = float(t.item()), float(c.item())
+    e2e_ms, e2e_checks = max_time_sum_units(e2e_ms, e2e_checks, ws, dev)
     e2e_value = e2e_checks / (e2e_ms / 1e3)
 
     if rank != 0:

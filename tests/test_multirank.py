@@ -61,3 +61,27 @@ def test_two_gloo_ranks_match_single_process(tmp_path, oracle_mod):
     ow = oracle_mod.OracleWorld(Ve, Fe, Vr, Fr)
     q = W.uniform_states(1001, -2.0, 2.0, ow.scene_scale, seed=3)
     assert (np.load(out).astype(bool) == ow.is_valid(q)).all()
+
+
+def _bench_rank(rank, world, port, out_path):
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import torch
+    import torch.distributed as dist
+    import bench
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    ms, units = bench.max_time_sum_units(100.0 + 50.0 * rank, 1000 * (rank + 1), world, torch.device("cpu"))
+    if rank == 0:
+        np.save(out_path, np.array([ms, units]))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_bench_reduces_over_ranks(tmp_path):
+    """bench.py's whole-job figures at N > 1: the slowest rank's time, all ranks' units."""
+    out = str(tmp_path / "agg.npy")
+    mp.spawn(_bench_rank, args=(2, _free_port(), out), nprocs=2, join=True)
+    ms, units = np.load(out)
+    assert ms == 150.0 and units == 3000.0
