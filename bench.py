@@ -347,9 +347,13 @@ def run_ours(args):
     if tps is not None and args.workload == "segments":
         traffic = tps * args.n
     kernel = "k_segments" if args.workload == "segments" else "k_states"
+    issue = _profile_value("k_segments_traffic.txt" if args.workload == "segments" else "k_states_plate_traffic.txt",
+                           "smsp_issue_active_pct")
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "kernel": kernel, "kernel_ms": trav_ms,
-            "peak_source": peak_kind, "algorithmic_bytes": alg_bytes}
+            "peak_source": peak_kind, "algorithmic_bytes": alg_bytes,
+            "served_from": "L1/L2 (BVHs resident); DRAM moves only the inputs",
+            "sm_issue_active_pct_ncu": issue}
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(work, target_s=args.cpu_seconds)
