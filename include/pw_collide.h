@@ -183,6 +183,16 @@ PW_API int pw_segments_contact_states(const double *from, const double *to, cons
                                       double verify_delta, double *last_free, double *contact, uint8_t *done,
                                       float *last_tau, float *tau, int *err_flag, void *stream);
 
+/* pw_segments_contact_states for the batch of this world's last
+ * pw_segments_first_contact(PW_SEG_TRANSIT) call (same from, to, n and
+ * verify_delta): starts each state from that call's 32-step checkpoints
+ * instead of re-running the delta loop.  Any other batch takes the
+ * pw_segments_contact_states path; the results are the same. */
+PW_API int pw_world_segments_contact_states(pw_world *w, const double *from, const double *to,
+                                            const int32_t *first_step, int64_t n, double verify_delta,
+                                            double *last_free, double *contact, uint8_t *done, float *last_tau,
+                                            float *tau, int *err_flag, void *stream);
+
 /* Plate crossings of expansions (narrow-passage search): for candidate i (ends
  * [n x 7], device) from root i / per_root (roots, device), out[i] = 1 if some
  * probe point (robot-local unit frame, probes [nprobe <= 64 x 3], device) is on

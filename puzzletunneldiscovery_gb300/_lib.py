@@ -36,7 +36,8 @@ EXPORTS = (
     "pw_intersecting_segments", "pw_world_translate_to_unit", "pw_world_translate_from_unit",
     "pw_world_translate_ompl_to_unit", "pw_world_translate_unit_to_ompl", "pw_world_last_stats",
     "pw_state_distance", "pw_state_interpolate", "pw_segment_step_state", "pw_states_valid_noalloc",
-    "pw_segments_contact_states", "pw_world_set_graph_mode", "pw_segments_reserve", "pw_world_set_launch_config",
+    "pw_segments_contact_states", "pw_world_segments_contact_states", "pw_world_set_graph_mode",
+    "pw_segments_reserve", "pw_world_set_launch_config",
     "pw_world_get_launch_config", "pw_expansion_crossings", "pw_world_scratch_epoch", "pw_expand_states",
     # include/pw_mlp.h
     "pw_mlp_create", "pw_mlp_destroy", "pw_mlp_num_params", "pw_mlp_get_params", "pw_mlp_set_params",
@@ -126,6 +127,8 @@ def load():
         "pw_state_interpolate": (ctypes.c_int, [dp, dp, ctypes.c_double, dp]),
         "pw_segment_step_state": (ctypes.c_int, [dp, dp, ctypes.c_double, i64, dp, dp, i64p]),
         "pw_world_set_graph_mode": (ctypes.c_int, [vp, ctypes.c_int]),
+        "pw_world_segments_contact_states": (ctypes.c_int, [vp, vp, vp, vp, i64, ctypes.c_double, vp, vp, vp, vp,
+                                                            vp, vp, vp]),
         "pw_world_scratch_epoch": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_uint64)]),
         "pw_expand_states": (ctypes.c_int, [vp, i64, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                             ctypes.c_uint64, vp, vp]),

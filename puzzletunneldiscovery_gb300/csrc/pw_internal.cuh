@@ -119,6 +119,12 @@ struct pw_world {
 	int launch_soft_cap[2] = { 0, 0 };  // traversal stack soft cap
 	int launch_blocks[2] = { 0, 0 };    // resident blocks per SM of the persistent kernel
 	int grid_cache[2] = { 0, 0 };       // grid of the persistent kernels under that configuration
+	// the last segment query's inputs: its parameters and checkpoints stay in the
+	// scratch, so the transit tuples of the same batch can start from them
+	const double *last_seg_from = nullptr, *last_seg_to = nullptr;
+	int64_t last_seg_n = -1;
+	double last_seg_delta = 0.0;
+	int last_seg_mode = -1;
 };
 
 // error plumbing (pw_world.cu)

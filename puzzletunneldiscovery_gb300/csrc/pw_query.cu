@@ -1225,6 +1225,7 @@ extern "C" int pw_segments_first_contact(pw_world *w, const double *from, const 
 	QueryCounters *ctr = (QueryCounters *)w->counters.ptr;
 	w->timed = false;
 	w->last_states = -1;
+	w->last_seg_n = -1;
 	PW_CUDA(cudaMemsetAsync(ctr, 0, sizeof(QueryCounters), st));
 	if (n == 0)
 		return PW_OK;
@@ -1301,6 +1302,101 @@ extern "C" int pw_segments_first_contact(pw_world *w, const double *from, const 
 		w->timed = true;
 	}
 	k_seg_finalize<<<G, B, 0, st>>>(first_step, params, n, ctr);
+	PW_CUDA(cudaGetLastError());
+	w->last_seg_from = from;
+	w->last_seg_to = to;
+	w->last_seg_n = n;
+	w->last_seg_delta = verify_delta;
+	w->last_seg_mode = mode;
+	return PW_OK;
+}
+
+// Transit tuples from the set-up kernel's checkpoints (the same batch as the
+// last pw_segments_first_contact(PW_SEG_TRANSIT) call): at most 31 delta updates
+// per state instead of the whole loop up to the first contact.
+__global__ void k_contact_states_ckpt(const double *from, const double *to, const SegParams *params,
+                                      const double *ckpt, const int32_t *first, int64_t n, double *last_free,
+                                      double *contact, uint8_t *done, float *last_tau, float *tau, int *err)
+{
+	const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+	if (i >= n)
+		return;
+	const double *a = from + 7 * i, *b = to + 7 * i;
+	double *lf = last_free + 7 * i, *st = contact + 7 * i;
+	const SegParams &P = params[i];
+	const int32_t k = first[i];
+	auto state_at = [&](int64_t j, double *q) {
+		double d = ckpt[P.ckpt_base + (j >> 5)];
+		for (int64_t r = 0; r < (j & 31); r++)
+			d = pwm::advance_delta(d, P.dist, P.step);
+		const double t = pwm::mul(d, P.inv_dist);
+		pwm::SlerpParams S;
+		seg_slerp(P, S);
+		pwm::interpolate_p(a, b, S, t, q);
+		return t;
+	};
+	if (k == PW_STEP_NONE) {
+		const bool nan = P.dist != P.dist;
+		for (int c = 0; c < 7; c++) {
+			lf[c] = a[c];
+			st[c] = nan ? a[c] : b[c];
+		}
+		done[i] = 0;
+		last_tau[i] = 0.f;
+		tau[i] = nan ? 0.f : 1.f;
+		return;
+	}
+	if (k < PW_STEP_NONE || (k == PW_STEP_FREE && P.nsteps <= 0)) {
+		atomicCAS(err, 0, 1);
+		for (int c = 0; c < 7; c++)
+			lf[c] = st[c] = a[c];
+		done[i] = 0;
+		last_tau[i] = tau[i] = 0.f;
+		return;
+	}
+	if (k >= 0) {
+		tau[i] = (float)state_at(k, st);
+		if (k == 0) {
+			for (int c = 0; c < 7; c++)
+				lf[c] = a[c];
+			last_tau[i] = 0.f;
+		} else {
+			last_tau[i] = (float)state_at(k - 1, lf);
+		}
+		done[i] = 0;
+		return;
+	}
+	const float lt = (float)state_at(P.nsteps - 1, lf);
+	for (int c = 0; c < 7; c++)
+		st[c] = lf[c];
+	done[i] = 1;
+	last_tau[i] = lt;
+	tau[i] = 0.f;
+}
+
+extern "C" int pw_segments_contact_states(const double *from, const double *to, const int32_t *first_step, int64_t n,
+                                          double verify_delta, double *last_free, double *contact, uint8_t *done,
+                                          float *last_tau, float *tau, int *err_flag, void *stream);
+
+extern "C" int pw_world_segments_contact_states(pw_world *w, const double *from, const double *to,
+                                                const int32_t *first_step, int64_t n, double verify_delta,
+                                                double *last_free, double *contact, uint8_t *done, float *last_tau,
+                                                float *tau, int *err_flag, void *stream)
+{
+	if (!w)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_segments_contact_states: world is NULL");
+	const bool same = w->last_seg_n == n && w->last_seg_from == from && w->last_seg_to == to &&
+	                  w->last_seg_delta == verify_delta && w->last_seg_mode == PW_SEG_TRANSIT &&
+	                  w->seg_params.ptr && n > 0;
+	if (!same)
+		return pw_segments_contact_states(from, to, first_step, n, verify_delta, last_free, contact, done, last_tau,
+		                                  tau, err_flag, stream);
+	if (!last_free || !contact || !done || !last_tau || !tau || !err_flag || !first_step)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_segments_contact_states: bad pointers");
+	PW_CUDA(cudaSetDevice(w->device));
+	k_contact_states_ckpt<<<(unsigned)((n + 127) / 128), 128, 0, (cudaStream_t)stream>>>(
+	    from, to, (const SegParams *)w->seg_params.ptr, (const double *)w->seg_ckpt.ptr, first_step, n, last_free,
+	    contact, done, last_tau, tau, err_flag);
 	PW_CUDA(cudaGetLastError());
 	return PW_OK;
 }

@@ -295,10 +295,10 @@ class UnitWorld:
         lt = torch.empty(n, dtype=torch.float32, device=dev)
         tt = torch.empty(n, dtype=torch.float32, device=dev)
         err = torch.zeros(1, dtype=torch.int32, device=dev)
-        check(self._L.pw_segments_contact_states(q0.data_ptr(), q1.data_ptr(), steps.data_ptr(), n,
-                                                 float(verify_delta), lf.data_ptr(), st.data_ptr(), done.data_ptr(),
-                                                 lt.data_ptr(), tt.data_ptr(), err.data_ptr(),
-                                                 _stream_ptr(dev)), "transit_states_to_with_contact")
+        check(self._L.pw_world_segments_contact_states(self._h, q0.data_ptr(), q1.data_ptr(), steps.data_ptr(), n,
+                                                       float(verify_delta), lf.data_ptr(), st.data_ptr(),
+                                                       done.data_ptr(), lt.data_ptr(), tt.data_ptr(), err.data_ptr(),
+                                                       _stream_ptr(dev)), "transit_states_to_with_contact")
         if int(err.item()) != 0:
             raise RuntimeError("transit_state_to: more than 2^30 steps at this verify_delta")
         return lf, st, done.bool(), lt, tt

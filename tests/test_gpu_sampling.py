@@ -78,3 +78,29 @@ def test_enum_free_configuration_verdicts_match_oracle(tori):
         assert np.array_equal(got[p], qs[p][valid[p]])
     q, found = S.sample_free_configurations(uw, rp, rn, ep, en, 1e-3, max_trials=15, rng=np.random.default_rng(2))
     assert ow.is_valid(q[found]).all()
+
+
+def test_checkpointed_transit_tuples_equal_full_loop(tori):
+    """pw_world_segments_contact_states (from the set-up kernel's checkpoints) and
+    pw_segments_contact_states (the delta loop from step 0) give identical tuples."""
+    from puzzletunneldiscovery_gb300 import _lib
+    uw, _ = tori
+    q0, q1 = W.segment_batch(20000, -2.0, 2.0, uw.scene_scale, seed=33)
+    q1[:10] = q0[:10]
+    a, b = torch.from_numpy(q0).cuda(), torch.from_numpy(q1).cuda()
+    fast = uw.transit_states_to_with_contact(a, b, 0.001)      # checkpoint path (same batch as its query)
+    steps = uw.first_contact_steps(a, b, 0.001)
+    L = _lib.load()
+    n = a.shape[0]
+    outs = [torch.empty((n, 7), dtype=torch.float64, device="cuda"), torch.empty((n, 7), dtype=torch.float64,
+                                                                                device="cuda"),
+            torch.empty(n, dtype=torch.uint8, device="cuda"), torch.empty(n, dtype=torch.float32, device="cuda"),
+            torch.empty(n, dtype=torch.float32, device="cuda")]
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    _lib.check(L.pw_segments_contact_states(a.data_ptr(), b.data_ptr(), steps.data_ptr(), n, 0.001,
+                                            *[o.data_ptr() for o in outs], err.data_ptr(),
+                                            torch.cuda.current_stream().cuda_stream), "contact states")
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    for x, y in zip(fast, outs):
+        assert torch.equal(x.to(y.dtype), y)
