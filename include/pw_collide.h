@@ -47,6 +47,13 @@ extern "C" {
 /* First-contact codes written by pw_segments_first_contact (>= 0: step index). */
 #define PW_STEP_FREE (-1)      /* every step free: the reference's `done` is true */
 #define PW_STEP_NONE (-2)      /* verify_delta >= dist: no step checked, `done` false (unit_world.cc:445-447) */
+#define PW_STEP_INVALID (-3)   /* not answered: a device-side capacity or step-bound check failed */
+
+/* Bits of pw_query_stats.device_errors. */
+#define PW_DEVERR_STEP_BOUND 1 /* a segment had more steps than its bound (never expected) */
+#define PW_DEVERR_CKPT_CAP 2   /* graph mode: reserved checkpoint slots too few for a segment */
+#define PW_DEVERR_ROUND_CAP 4  /* graph mode: the longest segment has more chunks than reserved */
+#define PW_DEVERR_NONFINITE 8  /* a state had a NaN / infinite component; its verdict is 0 (not free) */
 
 typedef struct pw_world pw_world;
 
@@ -74,8 +81,9 @@ typedef struct pw_query_stats {
 	int64_t detailed_chunks;     /* 32-step segment chunks that needed a transform per step */
 	double traverse_ms;          /* device time of the traversal kernel (CUDA events on the query stream) */
 	double retest_ms;            /* device time of the FP64 re-test kernel */
-	int64_t device_errors;       /* non-zero: a device-side capacity or consistency check failed; the
-	                                affected segments carry PW_STEP_INVALID */
+	int64_t device_errors;       /* PW_DEVERR_* bits: a device-side capacity or consistency check
+	                                failed (the affected segments carry PW_STEP_INVALID), or a
+	                                state was not finite */
 } pw_query_stats;
 
 /* Thread-local message for the last failing call on this thread. */
@@ -113,7 +121,9 @@ PW_API int pw_world_cd_vertices(const pw_world *w, int geo, double *out);
 PW_API int pw_world_cd_faces(const pw_world *w, int geo, int32_t *out);
 
 /* device, async: UnitWorld::isValid (unit_world.cc:215-247) for n states.
- * valid[i] = 1 when the robot at states[i] touches no env triangle. */
+ * valid[i] = 1 when the robot at states[i] touches no env triangle.  A state
+ * with a non-finite component gets 0 and sets PW_DEVERR_NONFINITE (the
+ * reference hands such a transform to FCL, whose answer is unspecified). */
 PW_API int pw_states_valid(pw_world *w, const double *states, int64_t n, uint8_t *valid, void *stream);
 
 /* device, async: the verdicts of pw_states_valid without allocating any device memory.

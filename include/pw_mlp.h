@@ -46,6 +46,11 @@ PW_API int pw_mlp_get_params(const pw_mlp *m, float *host_out);
 PW_API int pw_mlp_set_params(pw_mlp *m, const float *host_in);
 /* host: the gradient block of the last pw_mlp_gradients / pw_mlp_train_step. */
 PW_API int pw_mlp_get_grads(const pw_mlp *m, float *host_out);
+/* host: the Adam state (first and second moments, num_params floats each, and the
+ * step count), so that a checkpoint taken between steps resumes with the same
+ * next update. Either moment pointer may be NULL to skip it; set validates step >= 0. */
+PW_API int pw_mlp_get_adam(const pw_mlp *m, float *m1_out, float *m2_out, int64_t *step_out);
+PW_API int pw_mlp_set_adam(pw_mlp *m, const float *m1_in, const float *m2_in, int64_t step);
 
 /* P(collision free) of n states (device float64 [n x 7] -> device float32 [n]):
  * one fused, persistent kernel on the tcgen05 tensor cores (weights streamed by

@@ -1,6 +1,7 @@
 // pw_internal.cuh -- data layout shared by the world set-up and the query kernels.
 #pragma once
 
+#include "pw_trace.h"
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>

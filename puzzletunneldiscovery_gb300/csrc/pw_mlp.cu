@@ -657,6 +657,37 @@ extern "C" int pw_mlp_get_grads(const pw_mlp *m, float *host_out)
 	return PW_OK;
 }
 
+extern "C" int pw_mlp_get_adam(const pw_mlp *m, float *m1_out, float *m2_out, int64_t *step_out)
+{
+	if (!m)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_mlp_get_adam: NULL network");
+	PW_CUDA(cudaSetDevice(m->device));
+	PW_CUDA(cudaDeviceSynchronize());
+	if (m1_out)
+		PW_CUDA(cudaMemcpy(m1_out, m->m1.ptr, sizeof(float) * m->nparam, cudaMemcpyDeviceToHost));
+	if (m2_out)
+		PW_CUDA(cudaMemcpy(m2_out, m->m2.ptr, sizeof(float) * m->nparam, cudaMemcpyDeviceToHost));
+	if (step_out)
+		*step_out = m->step;
+	return PW_OK;
+}
+
+extern "C" int pw_mlp_set_adam(pw_mlp *m, const float *m1_in, const float *m2_in, int64_t step)
+{
+	if (!m)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_mlp_set_adam: NULL network");
+	if (step < 0)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_mlp_set_adam: negative step count");
+	PW_CUDA(cudaSetDevice(m->device));
+	PW_CUDA(cudaDeviceSynchronize());
+	if (m1_in)
+		PW_CUDA(cudaMemcpy(m->m1.ptr, m1_in, sizeof(float) * m->nparam, cudaMemcpyHostToDevice));
+	if (m2_in)
+		PW_CUDA(cudaMemcpy(m->m2.ptr, m2_in, sizeof(float) * m->nparam, cudaMemcpyHostToDevice));
+	m->step = step;
+	return PW_OK;
+}
+
 static void launch_gemm_fwd(pw_mlp *m, int l, int64_t n, cudaStream_t st, bool keep_z)
 {
 	GemmArgs p;
@@ -763,11 +794,13 @@ static float *mlp_head_table(pw_mlp *m)
 
 extern "C" int pw_mlp_predict(pw_mlp *m, const double *states, int64_t n, float *prob, void *stream)
 {
+	PW_TRACE("pw_mlp_predict");
 	return mlp_forward_tc(m, states, n, prob, 0, stream);
 }
 
 extern "C" int pw_mlp_score(pw_mlp *m, const double *states, int64_t n, float *logit, void *stream)
 {
+	PW_TRACE("pw_mlp_score");
 	return mlp_forward_tc(m, states, n, logit, 1, stream);
 }
 
@@ -819,6 +852,7 @@ static int mlp_forward_tc(pw_mlp *m, const double *states, int64_t n, float *pro
 extern "C" int pw_select_top(const float *score, const double *states, int64_t n, int64_t k, double *out_states,
                              int64_t capacity, int64_t *out_count, void *stream)
 {
+	PW_TRACE("pw_select_top");
 	if (n < 0 || k < 0 || capacity < 0 || !out_count || (n > 0 && (!score || !states)) ||
 	    (capacity > 0 && !out_states))
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_select_top: bad argument");
@@ -888,6 +922,7 @@ extern "C" int pw_mlp_check(pw_mlp *m)
 // The same network through the mma.sync GEMM kernels that training uses.
 extern "C" int pw_mlp_predict_mma(pw_mlp *m, const double *states, int64_t n, float *prob, void *stream)
 {
+	PW_TRACE("pw_mlp_predict_mma");
 	if (!m || n < 0 || (n > 0 && (!states || !prob)))
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_mlp_predict_mma: bad argument");
 	if (n == 0)
@@ -1170,6 +1205,7 @@ static int mlp_backward(pw_mlp *m, const double *states, const uint8_t *labels, 
 extern "C" int pw_mlp_gradients(pw_mlp *m, const double *states, const uint8_t *labels, int64_t n, float *loss_out,
                                 void *stream)
 {
+	PW_TRACE("pw_mlp_gradients");
 	if (!m || n <= 0 || !states || !labels)
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_mlp_gradients: bad argument");
 	if (n > (int64_t(1) << 24))
@@ -1190,6 +1226,7 @@ extern "C" int pw_mlp_set_training_kernels(pw_mlp *m, int use_mma)
 extern "C" int pw_mlp_train_step(pw_mlp *m, const double *states, const uint8_t *labels, int64_t n, float lr,
                                  float *loss_out, void *stream)
 {
+	PW_TRACE("pw_mlp_train_step");
 	int rc = pw_mlp_gradients(m, states, labels, n, loss_out, stream);
 	if (rc)
 		return rc;

@@ -579,17 +579,24 @@ __global__ void __launch_bounds__(WARPS * 32) k_states(WorldDev W, const double 
 		if (base >= (unsigned long long)n)
 			break;
 		const int cnt = (int)min((unsigned long long)width, (unsigned long long)n - base);
+		bool finite = true;
 		if (lane < cnt) {
 			double q[7];
-			for (int i = 0; i < 7; i++)
+			for (int i = 0; i < 7; i++) {
 				q[i] = states[7 * (base + lane) + i];
+				finite = finite && isfinite(q[i]);
+			}
 			make_qf(q, W, sm.qf[lane]);
 			sm.slot_query[lane] = (uint32_t)(base + lane);
 			sm.slot_step[lane] = 0u;
 		}
+		// a non-finite state is answered "not free" without a traversal
+		const uint32_t bad = __ballot_sync(FULL, !finite);
+		if (bad && lane == 0)
+			atomicOr(&ctr->error, (unsigned)PW_DEVERR_NONFINITE);
 		__syncwarp();
-		const uint32_t open = cnt == 32 ? FULL : ((1u << cnt) - 1u);
-		const uint32_t hit = traverse_batch<CAP>(W, sm, lane, open, soft_cap, ctr, rq, src, st);
+		const uint32_t open = (cnt == 32 ? FULL : ((1u << cnt) - 1u)) & ~bad;
+		const uint32_t hit = traverse_batch<CAP>(W, sm, lane, open, soft_cap, ctr, rq, src, st) | bad;
 		if (lane < cnt)
 			out[base + lane] = ((hit >> lane) & 1u) ? 0 : 1;
 		queries += cnt;
@@ -720,12 +727,15 @@ __global__ void k_seg_setup(WorldDev W, const double *from, const double *to, in
 	int32_t code = INT_MAX;
 	int64_t K = 0;
 	if (step >= dist || dist != dist) {
+		// a NaN distance: the reference loop (delta <= dist) checks no step
+		if (dist != dist)
+			atomicOr(&ctr->error, (unsigned)PW_DEVERR_NONFINITE);
 		code = PW_STEP_NONE;
 	} else if (!(step > 0.0) || dist / step > MAX_STEPS) {
 		code = -3;
 	} else if (P.ckpt_base + slots[s] > ckpt_cap) {
 		// graph mode: the reserved checkpoint slots do not hold this segment
-		atomicExch(&ctr->error, 2u);
+		atomicOr(&ctr->error, (unsigned)PW_DEVERR_CKPT_CAP);
 		code = -3;
 	} else {
 		double delta = step;
@@ -734,7 +744,7 @@ __global__ void k_seg_setup(WorldDev W, const double *from, const double *to, in
 			if ((K & 31) == 0) {
 				if ((K >> 5) >= nslots) {
 					// the step bound was too small: never write past this segment's slots
-					atomicExch(&ctr->error, 1u);
+					atomicOr(&ctr->error, (unsigned)PW_DEVERR_STEP_BOUND);
 					code = -3;
 					K = 0;
 					break;
@@ -777,9 +787,9 @@ __global__ void __launch_bounds__(1024) k_rounds(const uint32_t *sorted_keys, in
 		// graph mode: the longest segment has more chunks than reserved; no work runs
 		// and every segment reports PW_STEP_INVALID
 		for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
-			first[i] = -3;
+			first[i] = PW_STEP_INVALID;
 		if (threadIdx.x == 0)
-			atomicExch(&ctr->error, 3u);
+			atomicOr(&ctr->error, (unsigned)PW_DEVERR_ROUND_CAP);
 		R = 0;
 	}
 	if (threadIdx.x == 0)
@@ -1117,6 +1127,7 @@ int set_smem_attr(const void *kernel, size_t smem)
 
 extern "C" int pw_states_valid(pw_world *w, const double *states, int64_t n, uint8_t *valid, void *stream)
 {
+	PW_TRACE("pw_states_valid");
 	int rc = check_ready(w, "pw_states_valid");
 	if (rc)
 		return rc;
@@ -1163,6 +1174,7 @@ extern "C" int pw_states_valid(pw_world *w, const double *states, int64_t n, uin
 
 extern "C" int pw_states_disentangled(pw_world *w, const double *states, int64_t n, uint8_t *out, void *stream)
 {
+	PW_TRACE("pw_states_disentangled");
 	if (!w)
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_states_disentangled: world is NULL");
 	if (!w->ready)
@@ -1202,6 +1214,7 @@ static int grow(DeviceBuffer &b, size_t count, bool may_allocate = true)
 extern "C" int pw_segments_first_contact(pw_world *w, const double *from, const double *to, int64_t n,
                                          double verify_delta, int mode, int32_t *first_step, void *stream)
 {
+	PW_TRACE("pw_segments_first_contact");
 	int rc = check_ready(w, "pw_segments_first_contact");
 	if (rc)
 		return rc;
@@ -1383,6 +1396,7 @@ extern "C" int pw_world_segments_contact_states(pw_world *w, const double *from,
                                                 double *last_free, double *contact, uint8_t *done, float *last_tau,
                                                 float *tau, int *err_flag, void *stream)
 {
+	PW_TRACE("pw_world_segments_contact_states");
 	if (!w)
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_segments_contact_states: world is NULL");
 	const bool same = w->last_seg_n == n && w->last_seg_from == from && w->last_seg_to == to &&
@@ -1442,6 +1456,7 @@ extern "C" int pw_world_scratch_epoch(pw_world *w, uint64_t *out)
 
 extern "C" int pw_segments_reserve(pw_world *w, int64_t n, int64_t total_chunks, int64_t max_chunks)
 {
+	PW_TRACE("pw_segments_reserve");
 	int rc = check_ready(w, "pw_segments_reserve");
 	if (rc)
 		return rc;
@@ -1497,6 +1512,7 @@ extern "C" int pw_intersecting_segments(pw_world *w, const double q[7], int64_t 
                                         double *ends, double *mags, int32_t *face_pairs, int32_t *coplanar,
                                         int64_t *count)
 {
+	PW_TRACE("pw_intersecting_segments");
 	int rc = check_ready(w, "pw_intersecting_segments");
 	if (rc)
 		return rc;
@@ -1625,6 +1641,7 @@ static int noalloc_scratch(int device, void **out)
 
 extern "C" int pw_states_valid_noalloc(pw_world *w, const double *states, int64_t n, uint8_t *valid, void *stream)
 {
+	PW_TRACE("pw_states_valid_noalloc");
 	int rc = check_ready(w, "pw_states_valid_noalloc");
 	if (rc)
 		return rc;

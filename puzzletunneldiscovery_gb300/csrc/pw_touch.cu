@@ -100,6 +100,7 @@ extern "C" int pw_segments_contact_states(const double *from, const double *to, 
                                           double verify_delta, double *last_free, double *contact, uint8_t *done,
                                           float *last_tau, float *tau, int *err_flag, void *stream)
 {
+	PW_TRACE("pw_segments_contact_states");
 	if (n < 0 || (n > 0 && (!from || !to || !first_step || !last_free || !contact || !done || !last_tau || !tau ||
 	                        !err_flag)))
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_segments_contact_states: bad pointers or size");
@@ -172,6 +173,7 @@ extern "C" int pw_expansion_crossings(const double *roots, const double *ends, i
                                       const double *probes, int nprobe, double plane_z, double extent, uint8_t *out,
                                       void *stream)
 {
+	PW_TRACE("pw_expansion_crossings");
 	if (n < 0 || per_root <= 0 || nprobe < 0 || nprobe > 64 ||
 	    (n > 0 && (!roots || !ends || !out || (nprobe > 0 && !probes))))
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_expansion_crossings: bad pointers or sizes (at most 64 probes)");
@@ -263,6 +265,7 @@ __global__ void k_expand(const double *roots, int64_t n, int per_root, double si
 extern "C" int pw_expand_states(const double *roots, int64_t nroots, int per_root, double sigma_t, double sigma_rot,
                                 uint64_t seed, double *out, void *stream)
 {
+	PW_TRACE("pw_expand_states");
 	if (nroots < 0 || per_root <= 0 || !(sigma_t >= 0.0) || !(sigma_rot >= 0.0) ||
 	    (nroots > 0 && (!roots || !out)))
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_expand_states: bad pointers, sizes or deviations");

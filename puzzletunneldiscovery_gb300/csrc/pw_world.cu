@@ -187,6 +187,7 @@ static float span_of(const std::vector<float> &V)
 
 extern "C" int pw_world_scale_to_unit(pw_world *w)
 {
+	PW_TRACE("pw_world_scale_to_unit");
 	if (!w)
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_scale_to_unit: world is NULL");
 	if (!w->has_env)
@@ -223,6 +224,7 @@ static void local_box(const std::vector<double> &V, double c[3], double h[3])
 
 extern "C" int pw_world_angle_model(pw_world *w, float latitude, float longitude)
 {
+	PW_TRACE("pw_world_angle_model");
 	if (!w)
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_angle_model: world is NULL");
 	if (latitude != 0.0f || longitude != 0.0f)

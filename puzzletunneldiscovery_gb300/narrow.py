@@ -148,6 +148,33 @@ class NarrowPassageSearch:
         self.calls += 1
         return (self.seed * 0x9E3779B97F4A7C15 + self.calls) & (2**64 - 1)
 
+    def state_dict(self, include_network: bool = True) -> dict:
+        """Search progress as seeded counters: the expansion seed and call count
+        (a round's endpoints are a pure function of the two), the generator
+        state behind the shuffles and the plain arm's picks, the labels waiting
+        for the next retraining (CPU copies), and the network with its Adam
+        state.  Taken between rounds; a search restored from it draws the same
+        next round."""
+        sd = {"format": "pw_narrow/1", "seed": self.seed, "calls": self.calls,
+              "gen": self.gen.get_state(),
+              "pending_q": [q.cpu() for q in self._lab_q], "pending_y": [y.cpu() for y in self._lab_y]}
+        if include_network and self.net is not None:
+            sd["net"] = self.net.state_dict()
+        return sd
+
+    def load_state_dict(self, sd: dict) -> None:
+        if sd.get("format") != "pw_narrow/1":
+            raise ValueError("not a narrow-passage search checkpoint (format %r)" % sd.get("format"))
+        self.seed, self.calls = int(sd["seed"]), int(sd["calls"])
+        self.gen.set_state(sd["gen"])
+        self._lab_q = [q.to(self.dev) for q in sd["pending_q"]]
+        self._lab_y = [y.to(self.dev) for y in sd["pending_y"]]
+        self._nlab = sum(int(q.shape[0]) for q in self._lab_q)
+        if "net" in sd:
+            if self.net is None:
+                raise ValueError("checkpoint holds a network but this search has none")
+            self.net.load_state_dict(sd["net"])
+
     def _validate(self, frm, to):
         """First-contact codes (is_valid_transition mode) of up to k segments via the graph."""
         m = frm.shape[0]

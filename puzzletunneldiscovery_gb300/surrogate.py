@@ -65,11 +65,47 @@ class Surrogate:
         _lib.check(self._L.pw_mlp_get_grads(self._h, out.ctypes.data_as(_lib.fp)), "pw_mlp_get_grads")
         return out
 
+    def adam_state(self) -> dict:
+        """Adam's first / second moments (float32 [num_params]) and step count."""
+        m1 = np.empty(self.num_params, np.float32)
+        m2 = np.empty(self.num_params, np.float32)
+        step = ctypes.c_int64()
+        _lib.check(self._L.pw_mlp_get_adam(self._h, m1.ctypes.data_as(_lib.fp), m2.ctypes.data_as(_lib.fp),
+                                           ctypes.byref(step)), "pw_mlp_get_adam")
+        return {"m1": m1, "m2": m2, "step": int(step.value)}
+
+    def set_adam_state(self, state: dict) -> None:
+        m1 = np.ascontiguousarray(state["m1"], np.float32)
+        m2 = np.ascontiguousarray(state["m2"], np.float32)
+        if m1.shape != (self.num_params,) or m2.shape != (self.num_params,):
+            raise ValueError("expected Adam moments of %d values" % self.num_params)
+        _lib.check(self._L.pw_mlp_set_adam(self._h, m1.ctypes.data_as(_lib.fp), m2.ctypes.data_as(_lib.fp),
+                                           int(state["step"])), "pw_mlp_set_adam")
+
+    def state_dict(self) -> dict:
+        """Everything a resumed run needs for the same next training step:
+        parameters, Adam moments and step count (CPU tensors)."""
+        a = self.adam_state()
+        return {"format": "pw_mlp/1", "params": torch.from_numpy(self.params()),
+                "m1": torch.from_numpy(a["m1"]), "m2": torch.from_numpy(a["m2"]), "step": a["step"]}
+
+    def load_state_dict(self, sd: dict) -> None:
+        if sd.get("format") != "pw_mlp/1":
+            raise ValueError("not a pw_mlp checkpoint (format %r)" % sd.get("format"))
+        self.set_params(sd["params"].numpy())
+        self.set_adam_state({"m1": sd["m1"].numpy(), "m2": sd["m2"].numpy(), "step": sd["step"]})
+
     def save(self, path: str) -> None:
-        np.save(path, self.params())
+        """Checkpoint with torch.save: parameters and Adam state."""
+        torch.save(self.state_dict(), path)
 
     def load(self, path: str) -> None:
-        self.set_params(np.load(path))
+        """Restore a torch.save checkpoint, or a bare float32 parameter array
+        saved with numpy (Adam state then left as it is)."""
+        if str(path).endswith(".npy"):
+            self.set_params(np.load(path))
+            return
+        self.load_state_dict(torch.load(path, map_location="cpu", weights_only=True))
 
     # device calls -----------------------------------------------------------
     def _states(self, q):

@@ -76,3 +76,48 @@ def test_unitworld_refuses_cpu(built_lib):
         pytest.skip("a GPU is present")
     with pytest.raises(RuntimeError):
         pw.UnitWorld()
+
+
+_NULL_OK = {"pw_last_error", "pw_world_destroy", "pw_mlp_destroy", "pw_mlp_num_params"}
+
+_NULL_PROBE = r"""
+import ctypes, json, sys
+sys.path.insert(0, sys.argv[1])
+from puzzletunneldiscovery_gb300 import _lib
+L = _lib.load()
+out = {}
+for name in _lib.EXPORTS:
+    if name in %r:
+        continue
+    fn = getattr(L, name)
+    args = []
+    for t in fn.argtypes:
+        if t in (ctypes.c_int, ctypes.c_int64, ctypes.c_uint64, ctypes.c_int32):
+            args.append(t(1))
+        elif t in (ctypes.c_double, ctypes.c_float):
+            args.append(t(1.0))
+        else:
+            args.append(None)
+    rc = fn(*args)
+    out[name] = [int(rc), (L.pw_last_error() or b"").decode()]
+print(json.dumps(out))
+"""
+
+
+def test_every_entry_point_rejects_null_arguments(built_lib):
+    """Host-side fault injection without a device: every entry point, called with
+    NULL for each pointer and size 1, returns an error status and leaves a
+    message in pw_last_error instead of dereferencing anything.  Runs in a child
+    process so that a missing check shows as a failed test, not a crashed run."""
+    import json
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, "-c", _NULL_PROBE % (_NULL_OK,), ROOT], capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0, r.stderr[-2000:]
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    from puzzletunneldiscovery_gb300 import _lib
+    assert set(res) == set(_lib.EXPORTS) - _NULL_OK
+    for name, (rc, msg) in res.items():
+        assert rc != _lib.PW_OK, name
+        assert msg, name

@@ -151,6 +151,43 @@ def test_adam_step_matches_oracle(built_lib, mo):
     assert np.abs(p1 - want).max() <= 1e-6 * max(1.0, np.abs(want).max())
 
 
+def test_checkpoint_resume_gives_the_same_next_step(built_lib, mo, tmp_path):
+    """A torch.save checkpoint (parameters, Adam moments, step count) restores
+    into a fresh network exactly, and the resumed network's next Adam step is
+    the oracle step from the restored state (1e-6 relative, as above).  The
+    moments matter: restoring the parameters alone gives a different step."""
+    lr = 1e-3
+    a = _net(11)
+    for s in range(3):
+        q = torch.from_numpy(_states(8192, 80 + s)).cuda()
+        a.train_step(q, (q[:, :3].norm(dim=1) > 0.45).to(torch.uint8), lr)
+    path = str(tmp_path / "net.pt")
+    a.save(path)
+    ck = torch.load(path, weights_only=True)
+    assert ck["step"] == 3 and ck["m2"].abs().sum() > 0
+    b = _net(99)
+    b.load(path)
+    assert np.array_equal(b.params(), ck["params"].numpy())
+    st = b.adam_state()
+    assert st["step"] == 3 and np.array_equal(st["m1"], ck["m1"].numpy()) and np.array_equal(st["m2"], ck["m2"].numpy())
+    q = torch.from_numpy(_states(8192, 90)).cuda()
+    y = (q[:, :3].norm(dim=1) > 0.45).to(torch.uint8)
+    b.train_step(q, y, lr)
+    pb = b.params().astype(np.float64)
+    want, _, _ = mo.adam(ck["params"].numpy().astype(np.float64), b.grads().astype(np.float64),
+                         ck["m1"].numpy().astype(np.float64), ck["m2"].numpy().astype(np.float64), 4, lr)
+    tol = 1e-6 * max(1.0, np.abs(want).max())
+    assert np.abs(pb - want).max() <= tol
+    a.train_step(q, y, lr)
+    assert np.abs(a.params().astype(np.float64) - pb).max() <= 2 * tol
+    c = _net(99)
+    c.set_params(ck["params"].numpy())
+    c.train_step(q, y, lr)
+    assert np.abs(c.params().astype(np.float64) - pb).max() > 100 * tol
+    with pytest.raises(ValueError):
+        b.load_state_dict({"format": "something else"})
+
+
 def test_training_beats_uniform_sampling(built_lib):
     """The gain the network brings: after online training on exact labels, the
     top 10% of candidates it ranks are free far more often than uniform

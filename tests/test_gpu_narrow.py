@@ -121,3 +121,41 @@ def test_expansion_kernel(built_lib):
     ang = 2 * np.arccos(np.clip(np.abs(np.sum(A[:, 3:] * qr, axis=1)), 0, 1))
     # |rotation vector| of a 3-D N(0, 0.1^2 I) draw: mean 0.1 * sqrt(8 / pi)
     assert abs(ang.mean() - 0.1 * np.sqrt(8 / np.pi)) < 0.005
+
+
+def test_search_checkpoint_resumes_the_same_rounds(built_lib):
+    """A narrow-passage search checkpointed between rounds (seeded counters,
+    generator state, pending labels, network) and restored into a new search
+    with a differently seeded network draws the same next rounds: same
+    candidates, crossings and escapes.  Retraining is off during the compared
+    rounds, so the network's scores are the restored ones."""
+    import puzzletunneldiscovery_gb300 as pw
+    from puzzletunneldiscovery_gb300 import narrow as N
+    from puzzletunneldiscovery_gb300.surrogate import Surrogate
+    Ve, Fe, Vr, Fr = W.cfg_plate_knot(n=120)
+    uw = pw.UnitWorld(0)
+    uw.load_env_mesh(Ve, Fe)
+    uw.load_robot_mesh(Vr, Fr)
+    uw.scaleToUnit()
+    uw.angleModel(0.0, 0.0)
+    s = uw.scene_scale
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(5)
+    lo, hi = Ve.min(0) - 0.5, Ve.max(0) + 0.5
+    roots = N.draw_free_roots(uw, 10000, lo, hi, gen)
+    probes = N.centre_line_probes(uw, 256, 16, every=8)
+    extent = float(np.abs(Ve[:, :2]).max()) * s
+    kw = dict(k=2048, retrain_labels=10**9)
+    first = N.NarrowPassageSearch(uw, Surrogate(0, 3), probes, 0.0, extent, seed=7, **kw)
+    first.pretrain(roots, 65536 * 2, roots_per_round=5000)
+    first.run(roots[:5000], guided=True, roots_per_round=5000)
+    sd = first.state_dict()
+    assert sd["calls"] == first.calls and sd["net"]["step"] >= 1
+    second = N.NarrowPassageSearch(uw, Surrogate(0, 4), probes, 0.0, extent, seed=0, **kw)
+    second.load_state_dict(sd)
+    for guided in (True, False):
+        r1 = first.run(roots, guided=guided, roots_per_round=5000)
+        r2 = second.run(roots, guided=guided, roots_per_round=5000)
+        assert (r1.candidates, r1.crossing, r1.validated, r1.escapes) == (r2.candidates, r2.crossing, r2.validated,
+                                                                          r2.escapes)
+    assert first.calls == second.calls and first._nlab == second._nlab
