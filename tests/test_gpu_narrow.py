@@ -147,7 +147,7 @@ def test_search_checkpoint_resumes_the_same_rounds(built_lib):
     extent = float(np.abs(Ve[:, :2]).max()) * s
     kw = dict(k=2048, retrain_labels=10**9)
     first = N.NarrowPassageSearch(uw, Surrogate(0, 3), probes, 0.0, extent, seed=7, **kw)
-    first.pretrain(roots, 65536 * 2, roots_per_round=5000)
+    assert first.pretrain(roots, 20000, roots_per_round=5000, batch=1024) >= 1
     first.run(roots[:5000], guided=True, roots_per_round=5000)
     sd = first.state_dict()
     assert sd["calls"] == first.calls and sd["net"]["step"] >= 1
