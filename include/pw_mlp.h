@@ -70,6 +70,13 @@ PW_API int pw_mlp_predict_mma(pw_mlp *m, const double *states, int64_t n, float 
  * earlier pw_mlp_predict gave up (its probabilities are then invalid). */
 PW_API int pw_mlp_check(pw_mlp *m);
 
+/* host, test of the bounded waits: the next pw_mlp_predict / pw_mlp_score
+ * launch issues no weight copies, so its MMA issuer's wait for a weight stage
+ * runs out after the limit (about 2 s).  Every role then stops, the kernel
+ * frees its tensor memory and returns; pw_mlp_check reports PW_ERR_INTERNAL
+ * and the following launches run normally.  Nothing faults or hangs. */
+PW_API int pw_mlp_withhold_next_weights(pw_mlp *m);
+
 /* host: the states whose score is at or above the k-th largest score (any
  * finite floats, e.g. pw_mlp_score output), gathered into out_states (device,
  * [capacity x 7], in no particular order); *out_count = how many (k plus ties

@@ -43,7 +43,7 @@ EXPORTS = (
     "pw_mlp_create", "pw_mlp_destroy", "pw_mlp_num_params", "pw_mlp_get_params", "pw_mlp_set_params",
     "pw_mlp_get_grads", "pw_mlp_predict", "pw_mlp_gradients", "pw_mlp_train_step", "pw_mlp_predict_mma",
     "pw_mlp_check", "pw_select_top", "pw_mlp_score", "pw_mlp_set_training_kernels", "pw_mlp_get_adam",
-    "pw_mlp_set_adam",
+    "pw_mlp_set_adam", "pw_mlp_withhold_next_weights",
 )
 
 
@@ -148,6 +148,7 @@ def load():
         "pw_mlp_get_grads": (ctypes.c_int, [vp, fp]),
         "pw_mlp_get_adam": (ctypes.c_int, [vp, vp, vp, vp]),
         "pw_mlp_set_adam": (ctypes.c_int, [vp, vp, vp, i64]),
+        "pw_mlp_withhold_next_weights": (ctypes.c_int, [vp]),
         "pw_mlp_predict": (ctypes.c_int, [vp, vp, i64, vp, vp]),
         "pw_mlp_predict_mma": (ctypes.c_int, [vp, vp, i64, vp, vp]),
         "pw_mlp_check": (ctypes.c_int, [vp]),

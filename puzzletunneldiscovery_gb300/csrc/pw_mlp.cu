@@ -506,6 +506,7 @@ struct pw_mlp {
 	DeviceBuffer x64, xt, ht, gt, w1p, dw_ws;
 	int64_t tcap = 0;            // rows (multiple of 128) of the training buffers above
 	bool mma_training = false;   // train with the mma.sync kernels instead
+	bool withhold_next = false;  // the next tcgen05 forward launch issues no weight copies
 	bool wimg_dirty = true;
 	int num_sms = 1;
 	int64_t cap = 0;             // rows the activation buffers hold
@@ -841,6 +842,8 @@ static int mlp_forward_tc(pw_mlp *m, const double *states, int64_t n, float *pro
 	a.ht = mlp_head_table(m);
 	a.prob = prob;
 	a.logits = logits;
+	a.withhold = m->withhold_next ? 1 : 0;
+	m->withhold_next = false;
 	a.err = mlp_err(m);
 	const int64_t ntiles = (n + tc::TILE_M - 1) / tc::TILE_M;
 	const unsigned grid = (unsigned)std::min<int64_t>(ntiles, m->num_sms);
@@ -920,6 +923,14 @@ extern "C" int pw_mlp_check(pw_mlp *m)
 }
 
 // The same network through the mma.sync GEMM kernels that training uses.
+extern "C" int pw_mlp_withhold_next_weights(pw_mlp *m)
+{
+	if (!m)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_mlp_withhold_next_weights: NULL network");
+	m->withhold_next = true;
+	return PW_OK;
+}
+
 extern "C" int pw_mlp_predict_mma(pw_mlp *m, const double *states, int64_t n, float *prob, void *stream)
 {
 	PW_TRACE("pw_mlp_predict_mma");

@@ -211,6 +211,7 @@ struct FwdArgs {
 	const float *ht;         // epilogue constants (HT_*)
 	float *prob;
 	int logits;              // 1: write the logit (a ranking score that does not saturate) instead of P(free)
+	int withhold;            // 1: issue no weight copies (the test of the bounded waits: they run out)
 	int *err;
 };
 
@@ -255,7 +256,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 		// ---------------- weight producer: the loads of the pair's schedule, in order
 		if (lane == 0) {
 			uint32_t loads[NSTAGE] = { 0, 0, 0 };
-			bool ok = true;
+			bool ok = !a.withhold;
 			for (int64_t tA = blockIdx.x; tA < ntiles && ok; tA += 2 * G) {
 				const int nslot = tA + G < ntiles ? 2 : 1;
 				const uint16_t *E = a.sched.e[nslot - 1];

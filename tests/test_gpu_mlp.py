@@ -188,6 +188,29 @@ def test_checkpoint_resume_gives_the_same_next_step(built_lib, mo, tmp_path):
         b.load_state_dict({"format": "something else"})
 
 
+def test_bounded_wait_runs_out_and_is_reported(built_lib):
+    """The tcgen05 forward kernel's waits are bounded: a launch whose weight
+    copies are withheld (nothing ever completes the stage it waits for) gives
+    up after the limit, frees its tensor memory and returns; pw_mlp_check
+    reports it, and the next launch gives the same probabilities as before."""
+    import time
+    from puzzletunneldiscovery_gb300 import _lib
+    net = _net(2)
+    q = torch.from_numpy(_states(4096, 70)).cuda()
+    want = net.predict(q).clone()
+    net.check()
+    assert net._L.pw_mlp_withhold_next_weights(net._h) == _lib.PW_OK
+    t0 = time.perf_counter()
+    net.predict(q)
+    with pytest.raises(_lib.PwError) as e:
+        net.check()
+    assert e.value.code == _lib.PW_ERR_INTERNAL and "gave up" in str(e.value)
+    assert time.perf_counter() - t0 < 30.0
+    got = net.predict(q)
+    net.check()
+    assert torch.equal(got, want)
+
+
 def test_training_beats_uniform_sampling(built_lib):
     """The gain the network brings: after online training on exact labels, the
     top 10% of candidates it ranks are free far more often than uniform
