@@ -1,0 +1,79 @@
+"""Host logic of the planner's screening stages against the reference's own
+task partitioner and disjoint set (tests/golden/screening_golden.npz, made by
+tests/golden/make_screening_golden.py from partt.py and disjoint_set.py)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+GOLDEN = os.path.join(ROOT, "tests", "golden", "screening_golden.npz")
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return np.load(GOLDEN)
+
+
+def test_partition_matches_the_reference_partitioner(golden):
+    from puzzletunneldiscovery_gb300 import screening as S
+    meta = golden["part_meta"]
+    assert len(meta) >= 10
+    for i, (nkey_total, quota, gran, total, task) in enumerate(meta):
+        assert S.partition_screening(int(nkey_total), int(quota), int(gran)) == total
+        f, t = S.partition_screening(int(nkey_total), int(quota), int(gran), index=int(task))
+        assert np.array_equal(f, golden["part_from_%d" % i]), i
+        assert np.array_equal(t, golden["part_to_%d" % i]), i
+
+
+def test_chunks_tile_the_task_range():
+    from puzzletunneldiscovery_gb300 import screening as S
+    for ntask, num in [(1, 1), (10, 3), (1540, 15), (5050, 37), (7, 7), (1000003, 1000)]:
+        b = S.chunk_bounds(ntask, num)
+        assert b.shape == (num, 2)
+        assert b[0, 0] == 0 and b[-1, 1] == ntask
+        assert (b[1:, 0] == b[:-1, 1]).all() and (b[:, 1] >= b[:, 0]).all()
+
+
+def test_tril_pairs_decode_flat_indices():
+    from puzzletunneldiscovery_gb300 import screening as S
+    for n in (1, 2, 3, 17, 300):
+        r, c = np.tril_indices(n)
+        i, j = S.tril_pairs(np.arange(r.shape[0]))
+        assert np.array_equal(i, r) and np.array_equal(j, c)
+    # far beyond float32 / at the float64 rounding edges: exact integer identities
+    i0 = np.array([10**6, 3 * 10**6 + 7, 2**26 + 3], dtype=np.int64)
+    base = i0 * (i0 + 1) // 2
+    for off in (0, 1, -1):
+        k = base + off
+        i, j = S.tril_pairs(k)
+        assert (i * (i + 1) // 2 + j == k).all() and (j >= 0).all() and (j <= i).all()
+
+
+def test_root_selection_matches_the_reference_disjoint_set(golden):
+    from puzzletunneldiscovery_gb300 import screening as S
+    for c in range(int(golden["root_count"])):
+        nkey = int(golden["root_%d_nkey" % c])
+        keys = np.repeat(np.arange(nkey, dtype=np.float64)[:, None], 7, axis=1)
+        out = S.assemble_roots(None, keys, golden["root_%d_bases" % c], golden["root_%d_from" % c],
+                               golden["root_%d_to" % c], disentangled=golden["root_%d_dis" % c])
+        assert set(out) == {"ge", "nt", "nn", "cmb"}
+        for s, got in out.items():
+            want = golden["root_%d_%s" % (c, s)]
+            assert np.array_equal(got[:, 0].astype(np.int64), want), (c, s)
+
+
+def test_edge_files_round_trip(tmp_path):
+    from puzzletunneldiscovery_gb300 import screening as S
+    rng = np.random.default_rng(0)
+    parts = []
+    for t in range(3):
+        f = rng.integers(2, 50, size=10 + t)
+        g = rng.integers(2, 50, size=10 + t)
+        np.savez_compressed(tmp_path / ("edge_batch-%d.npz" % t), EDGE_FROM=f, EDGE_TO=g)
+        parts.append((f, g))
+    ef, et = S.load_edges(str(tmp_path))
+    assert ef.shape == (33,) and et.shape == (33,)
+    want = sorted(zip(np.concatenate([p[0] for p in parts]), np.concatenate([p[1] for p in parts])))
+    assert sorted(zip(ef, et)) == want
