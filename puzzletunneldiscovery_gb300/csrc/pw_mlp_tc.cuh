@@ -183,6 +183,26 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b)
 	return *reinterpret_cast<uint32_t *>(&h);
 }
 
+// SiLU of two pre-activations (accumulator + bias, both halved by the weight
+// scaling), packed to BF16: with h = x / 2, SiLU(x) = h + h tanh(h).  The add and
+// the fma run as packed f32x2 instructions (two lanes per instruction, each
+// rounded as its scalar form).
+__device__ __forceinline__ uint32_t silu_pair(uint32_t acc0, uint32_t acc1, float b0, float b1)
+{
+	uint64_t h, b, t, y;
+	asm("mov.b64 %0, {%1, %2};" : "=l"(h) : "r"(acc0), "r"(acc1));
+	asm("mov.b64 %0, {%1, %2};" : "=l"(b) : "f"(b0), "f"(b1));
+	asm("add.rn.f32x2 %0, %1, %2;" : "=l"(h) : "l"(h), "l"(b));
+	float h0, h1;
+	asm("mov.b64 {%0, %1}, %2;" : "=f"(h0), "=f"(h1) : "l"(h));
+	const float t0 = tanh_fast(h0), t1 = tanh_fast(h1);
+	asm("mov.b64 %0, {%1, %2};" : "=l"(t) : "f"(t0), "f"(t1));
+	asm("fma.rn.f32x2 %0, %1, %2, %1;" : "=l"(y) : "l"(h), "l"(t));
+	float y0, y1;
+	asm("mov.b64 {%0, %1}, %2;" : "=f"(y0), "=f"(y1) : "l"(y));
+	return pack_bf16x2(y0, y1);
+}
+
 // Per-column constants of the epilogue, after the weight images:
 // [4][256] biases b_l / 2, [256] w5, b5 (16-byte aligned rows).
 constexpr int HT_W5 = 4 * H, HT_B5 = 5 * H, HT_FLOATS = 5 * H + 4;
@@ -373,46 +393,44 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 					tc_fence_after();
 					uint8_t *act = sm + SM_ACT + sl * ACT_BYTES;
 					float head = 0.f;
-					// K-blocks of act two at a time: this warp's 16 columns j*64 + g*16 .. +15
-					for (int j0 = 0; j0 < 4; j0 += 2) {
-						uint32_t rv[2][16];
-						tmem_ld16_nw(tmem + lane_off + (uint32_t)(sl * 256 + j0 * KB + g * 16), rv[0]);
-						tmem_ld16_nw(tmem + lane_off + (uint32_t)(sl * 256 + (j0 + 1) * KB + g * 16), rv[1]);
-						tmem_wait_ld();
+					// this warp's 16 columns j*64 + g*16 .. +15 of each K-block j; the tensor-memory
+					// load of block j + 1 is in flight while block j is computed
+					uint32_t rv[2][16];
+					tmem_ld16_nw(tmem + lane_off + (uint32_t)(sl * 256 + g * 16), rv[0]);
+					tmem_wait_ld();
 #pragma unroll
-						for (int jj = 0; jj < 2; jj++) {
-							const int j = j0 + jj;
-							const int col = j * KB + g * 16;
-							float bv[16];
+					for (int j = 0; j < 4; j++) {
+						if (j < 3)
+							tmem_ld16_nw(tmem + lane_off + (uint32_t)(sl * 256 + (j + 1) * KB + g * 16),
+							             rv[(j + 1) & 1]);
+						const int col = j * KB + g * 16;
+						float bv[16];
+#pragma unroll
+						for (int i = 0; i < 4; i++)
+							*reinterpret_cast<float4 *>(bv + 4 * i) = __ldg(reinterpret_cast<const float4 *>(bias + col) + i);
+						const uint32_t *cur = rv[j & 1];
+						uint32_t pk[8];
+#pragma unroll
+						for (int i = 0; i < 16; i += 2)
+							pk[i / 2] = silu_pair(cur[i], cur[i + 1], bv[i], bv[i + 1]);
+						if (layer < 3) {
+							uint8_t *kb = act + j * ACT_KB_BYTES;
+							*reinterpret_cast<uint4 *>(kb + swz(r, 2 * g)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+							*reinterpret_cast<uint4 *>(kb + swz(r, 2 * g + 1)) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+						} else {
 #pragma unroll
 							for (int i = 0; i < 4; i++)
 								*reinterpret_cast<float4 *>(bv + 4 * i) =
-								    __ldg(reinterpret_cast<const float4 *>(bias + col) + i);
-							uint32_t pk[8];
+								    __ldg(reinterpret_cast<const float4 *>(a.ht + HT_W5 + col) + i);
 #pragma unroll
-							for (int i = 0; i < 16; i += 2) {
-								const float h0 = __uint_as_float(rv[jj][i]) + bv[i];
-								const float h1 = __uint_as_float(rv[jj][i + 1]) + bv[i + 1];
-								pk[i / 2] = pack_bf16x2(fmaf(h0, tanh_fast(h0), h0), fmaf(h1, tanh_fast(h1), h1));
-							}
-							if (layer < 3) {
-								uint8_t *kb = act + j * ACT_KB_BYTES;
-								*reinterpret_cast<uint4 *>(kb + swz(r, 2 * g)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-								*reinterpret_cast<uint4 *>(kb + swz(r, 2 * g + 1)) =
-								    make_uint4(pk[4], pk[5], pk[6], pk[7]);
-							} else {
-#pragma unroll
-								for (int i = 0; i < 4; i++)
-									*reinterpret_cast<float4 *>(bv + 4 * i) =
-									    __ldg(reinterpret_cast<const float4 *>(a.ht + HT_W5 + col) + i);
-#pragma unroll
-								for (int i = 0; i < 8; i++) {
-									const __nv_bfloat162 hh = *reinterpret_cast<__nv_bfloat162 *>(&pk[i]);
-									head = fmaf(__low2float(hh), bv[2 * i], head);
-									head = fmaf(__high2float(hh), bv[2 * i + 1], head);
-								}
+							for (int i = 0; i < 8; i++) {
+								const __nv_bfloat162 hh = *reinterpret_cast<__nv_bfloat162 *>(&pk[i]);
+								head = fmaf(__low2float(hh), bv[2 * i], head);
+								head = fmaf(__high2float(hh), bv[2 * i + 1], head);
 							}
 						}
+						if (j < 3)
+							tmem_wait_ld();
 					}
 					tc_fence_before();
 					if (layer < 3) {
