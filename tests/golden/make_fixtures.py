@@ -11,6 +11,7 @@ files this script writes.
   (alpha-1.2.org.w-first.npz) and the tunnel vertices (alpha-1.2.org.tunnel*.npz).
   Every one of those states is collision-free in the reference (it is a
   planner's solution), so they pin the oracle's "free" verdicts.
+* alpha_rl.npz -- the mesh pair and states of src/RL/test_collide.py (see alpha_rl).
 * fcl_kat.npz -- the triangle pair of sancheck/fclcontacts/main.cc:17-64
   (expected: collision) and the analytic intersection segment of that pair.
 * torus_regression.npz -- seeded interlocking-tori states and segments with
@@ -47,6 +48,24 @@ def alpha():
                         path_wlast=path, keys_wfirst=keys, tunnel=tun, tunnel_more=tun_more)
 
 
+def alpha_rl():
+    """res/alpha/env-1.2.obj + robot.obj and the states src/RL/test_collide.py:39-53
+    checks on them (float32 as the script builds them): [0.04, 0, 0, .5, .5, .5, .5]
+    and [0.7, 0, 0, .5, .5, .5, .5], both printed with "Expecting True", plus the
+    script's x sweep [-0.8, 0.8) step 0.02 with the oracle's verdicts (a regression
+    pin; the reference prints the sweep without expectations)."""
+    A = os.path.join(REF, "res", "alpha")
+    Ve, Fe = objio.load_obj(os.path.join(A, "env-1.2.obj"))
+    Vr, Fr = objio.load_obj(os.path.join(A, "robot.obj"))
+    expect_free = np.array([[0.04, 0, 0, 0.5, 0.5, 0.5, 0.5], [0.7, 0, 0, 0.5, 0.5, 0.5, 0.5]],
+                           dtype=np.float32).astype(np.float64)
+    sweep = np.array([[x, 0, 0, 0.5, 0.5, 0.5, 0.5] for x in np.arange(-0.8, 0.8, 0.02)],
+                     dtype=np.float32).astype(np.float64)
+    w = O.OracleWorld(Ve, Fe, Vr, Fr)
+    np.savez_compressed(os.path.join(HERE, "alpha_rl.npz"), Ve=Ve, Fe=Fe, Vr=Vr, Fr=Fr, expect_free=expect_free,
+                        sweep=sweep, sweep_valid=w.is_valid(sweep))
+
+
 def fcl_kat():
     h = np.array([[0, 0, 0], [1, 0, 0], [0, 0, 1]], dtype=np.float64)
     v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], dtype=np.float64) + np.array([-0.49, -0.5, 0.5])
@@ -70,7 +89,7 @@ def torus_regression():
 
 
 if __name__ == "__main__":
-    alpha()
-    fcl_kat()
-    torus_regression()
+    makers = {"alpha": alpha, "alpha_rl": alpha_rl, "fcl_kat": fcl_kat, "torus_regression": torus_regression}
+    for name in (sys.argv[1:] or list(makers)):
+        makers[name]()
     print("fixtures written to", HERE)

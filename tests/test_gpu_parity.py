@@ -122,6 +122,24 @@ def test_near_contact_states(tori, oracle_mod):
     assert uw.last_stats()["retests"] > 0   # the band was exercised
 
 
+def test_rl_alpha_states_expected_free(built_lib):
+    """src/RL/test_collide.py:39-53 (env-1.2.obj + robot.obj): the two states the
+    reference expects free are free on the engine, and the script's x sweep
+    gives the oracle's committed verdicts, through is_valid_state and the batch."""
+    import puzzletunneldiscovery_gb300 as pw
+    from conftest import golden
+    g = golden("alpha_rl.npz")
+    uw = pw.UnitWorld(0)
+    uw.load_env_mesh(g["Ve"], g["Fe"])
+    uw.load_robot_mesh(g["Vr"], g["Fr"])
+    uw.scaleToUnit()
+    uw.angleModel(0.0, 0.0)
+    for q in g["expect_free"]:
+        assert uw.is_valid_state(q) is True
+    v = uw.is_valid_states(torch.from_numpy(g["sweep"])).cpu().numpy()
+    assert (v == g["sweep_valid"]).all()
+
+
 def test_alpha_puzzle_states_and_path(alpha):
     uw, ow, g = alpha
     s = uw.scene_scale

@@ -35,6 +35,18 @@ def _to_unit(states, s, wlast):
     return np.array(out)
 
 
+def test_rl_alpha_states_expected_free(oracle_mod):
+    """src/RL/test_collide.py:39-53 on res/alpha/env-1.2.obj + robot.obj: the two
+    states it prints with "Expecting True" are free; the oracle's x sweep matches
+    the committed regression vector and is free at both ends of the sweep."""
+    g = golden("alpha_rl.npz")
+    w = oracle_mod.OracleWorld(g["Ve"], g["Fe"], g["Vr"], g["Fr"])
+    assert w.is_valid(g["expect_free"]).all()
+    v = w.is_valid(g["sweep"])
+    assert (v == g["sweep_valid"]).all()
+    assert v[:5].all() and v[-5:].all() and not v.all()
+
+
 def test_alpha_solution_path_is_free(oracle_mod):
     """Every state of the reference's alpha-puzzle OMPL solution is collision-free."""
     w, g = _alpha_world(oracle_mod)
