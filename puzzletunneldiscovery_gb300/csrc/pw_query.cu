@@ -750,6 +750,19 @@ __global__ void k_seg_setup(WorldDev W, const double *from, const double *to, in
 					break;
 				}
 				ckpt[P.ckpt_base + (K >> 5)] = delta;
+				// a chunk that ends well below dist (room counted in FP32, 8 steps of
+				// margin) takes every branch of the loop the same way: its deltas are the
+				// plain sums, so only the adds run (same FP64 values, bit for bit)
+				const float room = __fdiv_rn((float)pwm::sub(dist, delta), (float)step);
+				if (room > 40.f) {
+					for (int i = 0; i < 32; i++) {
+						if (i == 15)
+							seg_step_qf(W, a, b, P, delta, anchors[P.ckpt_base + (K >> 5)]);
+						delta = pwm::add(delta, step);
+					}
+					K += 32;
+					continue;
+				}
 			}
 			if ((K & 31) == 15)   // the chunk has at least 16 steps: its anchor is step 15
 				seg_step_qf(W, a, b, P, delta, anchors[P.ckpt_base + (K >> 5)]);
