@@ -145,6 +145,13 @@ class Work:
             return uw.is_valid_states(a)
         return uw.first_contact_steps(a, b, DELTA)
 
+    def gpu_host(self, uw, ha, hb):
+        """The same call on host batches (the public host-array entry points: the
+        copies of one chunk overlap the checks of the previous one)."""
+        if self.name == "plate":
+            return uw.is_valid_states_host(ha)
+        return uw.first_contact_steps_host(ha, hb, DELTA)
+
     def cpu(self, ow, lo, hi, threads):
         """(reference checks, seconds) of the oracle on units lo..hi."""
         t0 = time.perf_counter()
@@ -307,24 +314,24 @@ def run_ours(args):
         graph_ms = sum(gms) / len(gms)
         del g
 
-    # end to end through the public API with host buffers (pinned), copies inside the timed region
+    # end to end through the public host-array API with pinned host buffers: every
+    # step copies its inputs in and its results out inside the timed region
     ha = torch.from_numpy(work.q0).pin_memory()
     hb = torch.from_numpy(work.q1).pin_memory() if work.q1 is not None else None
-    hout = torch.empty(args.n, dtype=f.dtype).pin_memory()
+    checks_per_step = stats[0]["reference_checks"]   # the same batch as the timed device steps
     e2e_ms, e2e_checks = 0.0, 0
     barrier()
     for i in range(args.steps):
         flush.zero_()
         s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s0.record(stream)
-        da = ha.to(dev, non_blocking=True)
-        db = hb.to(dev, non_blocking=True) if hb is not None else None
-        f = work.gpu(uw, da, db)
-        hout.copy_(f, non_blocking=True)
+        hout = work.gpu_host(uw, ha, hb)
         s1.record(stream)
         torch.cuda.synchronize(dev)
         e2e_ms += s0.elapsed_time(s1)
-        e2e_checks += uw.last_stats()["reference_checks"]
+        e2e_checks += checks_per_step
+    if not torch.equal(hout.to(dev), f):
+        raise RuntimeError("host-array path disagrees with the device path")
     e2e_ms, e2e_checks = max_time_sum_units(e2e_ms, e2e_checks, ws, dev)
     e2e_value = e2e_checks / (e2e_ms / 1e3)
 

@@ -189,6 +189,70 @@ class UnitWorld:
                                       _stream_ptr(self._device)), "is_valid_state")
         return out.bool()
 
+    # host batches, streamed ------------------------------------------------------
+    def _host_stream(self, run, hosts, out_dtype, chunk: int) -> torch.Tensor:
+        """Runs `run(device inputs..., device out)` over host batches in chunks of
+        `chunk` rows: the host-to-device copy of chunk i + 1 runs on a copy stream
+        while chunk i is checked on the current stream, and each chunk's result is
+        copied back behind it.  Returns the results in pinned host memory."""
+        hs = []
+        for h in hosts:
+            t = h if isinstance(h, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(h, dtype=np.float64))
+            if t.dtype != torch.float64 or t.dim() != 2 or t.shape[1] != 7:
+                raise ValueError("host states must be float64 [n, 7]")
+            t = t.contiguous()
+            hs.append(t if t.is_pinned() else t.pin_memory())
+        n = hs[0].shape[0]
+        if any(h.shape[0] != n for h in hs):
+            raise ValueError("host batches differ in length")
+        out = torch.empty(n, dtype=out_dtype, pin_memory=True)
+        if n == 0:
+            return out
+        host_out = out.view(torch.uint8) if out_dtype == torch.bool else out
+        dev_dtype = torch.uint8 if out_dtype == torch.bool else out_dtype
+        dev = self._device
+        chunk = max(1, min(int(chunk), n))
+        comp = torch.cuda.current_stream(dev)
+        copy = getattr(self, "_copy_stream", None)
+        if copy is None:
+            copy = self._copy_stream = torch.cuda.Stream(dev)
+        bufs = [[torch.empty((chunk, 7), dtype=torch.float64, device=dev) for _ in hs] for _ in range(2)]
+        obufs = [torch.empty(chunk, dtype=dev_dtype, device=dev) for _ in range(2)]
+        ready = [torch.cuda.Event() for _ in range(2)]
+        free = [torch.cuda.Event() for _ in range(2)]
+        for k, s0 in enumerate(range(0, n, chunk)):
+            m = min(chunk, n - s0)
+            b = k & 1
+            with torch.cuda.stream(copy):
+                if k >= 2:
+                    copy.wait_event(free[b])        # chunk k - 2 is done with buffer b
+                for h, d in zip(hs, bufs[b]):
+                    d[:m].copy_(h[s0:s0 + m], non_blocking=True)
+                ready[b].record(copy)
+            comp.wait_event(ready[b])
+            run(*[d[:m] for d in bufs[b]], obufs[b][:m])
+            host_out[s0:s0 + m].copy_(obufs[b][:m], non_blocking=True)
+            free[b].record(comp)
+        comp.synchronize()
+        return out
+
+    def is_valid_states_host(self, q, chunk: int = 1 << 21) -> torch.Tensor:
+        """isValid for a host batch (numpy or CPU tensor, float64 [N, 7]): bool [N] in
+        pinned host memory.  Pinned input avoids a staging copy."""
+        def run(d, o):
+            check(self._L.pw_states_valid(self._h, d.data_ptr(), d.shape[0], o.data_ptr(), _stream_ptr(self._device)),
+                  "is_valid_state")
+        return self._host_stream(run, [q], torch.bool, chunk)
+
+    def first_contact_steps_host(self, q0, q1, verify_delta: float, mode: int = _lib.PW_SEG_TRANSIT,
+                                 chunk: int = 1 << 22) -> torch.Tensor:
+        """first_contact_steps for host batches: int32 [N] in pinned host memory."""
+        def run(a, b, o):
+            check(self._L.pw_segments_first_contact(self._h, a.data_ptr(), b.data_ptr(), a.shape[0], float(verify_delta),
+                                                    int(mode), o.data_ptr(), _stream_ptr(self._device)),
+                  "first_contact_steps")
+        return self._host_stream(run, [q0, q1], torch.int32, chunk)
+
     def is_disentangled_states(self, q: torch.Tensor) -> torch.Tensor:
         q = self._dev_states(q)
         out = torch.empty(q.shape[0], dtype=torch.uint8, device=self._device)

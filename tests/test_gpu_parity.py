@@ -39,6 +39,28 @@ def alpha(oracle_mod, built_lib):
     return uw, ow, g
 
 
+def test_host_array_entry_points_match_device(tori):
+    """is_valid_states_host / first_contact_steps_host (host batches streamed in
+    chunks, copies overlapping checks) give the device path's answers, for numpy
+    and pinned inputs and a batch that is no multiple of the chunk."""
+    uw, ow = tori
+    q = W.uniform_states(100_003, -2.0, 2.0, uw.scene_scale, seed=31)
+    want = uw.is_valid_states(torch.from_numpy(q)).cpu()
+    for src in (q, torch.from_numpy(q).pin_memory()):
+        got = uw.is_valid_states_host(src, chunk=7_919)
+        assert got.is_pinned() and got.dtype == torch.bool and torch.equal(got, want)
+    q0, q1 = W.segment_batch(20_001, -2.0, 2.0, uw.scene_scale, seed=32)
+    f = uw.first_contact_steps(torch.from_numpy(q0), torch.from_numpy(q1), 0.001).cpu()
+    for chunk in (1 << 22, 4_999):
+        got = uw.first_contact_steps_host(q0, q1, 0.001, chunk=chunk)
+        assert got.dtype == torch.int32 and torch.equal(got, f)
+    e, _ = ow.segments_first_contact(q0[:300], q1[:300], 0.001)
+    assert (f[:300].numpy() == e).all()
+    assert uw.is_valid_states_host(np.zeros((0, 7))).shape == (0,)
+    with pytest.raises(ValueError):
+        uw.first_contact_steps_host(q0, q1[:-1], 0.001)
+
+
 def test_cd_vertices_and_scale_match(tori):
     uw, ow = tori
     assert uw.scene_scale == ow.scene_scale
