@@ -6,7 +6,8 @@ launch configurations (queries a warp takes per grab, traversal stack soft cap
 resident blocks per SM) on a sample of the caller's own workload, checks that
 every configuration returns the same verdicts, and keeps the fastest
 (pw_world_set_launch_config).  The best configuration depends on the meshes
-(BVH depth, how often queries collide), so it is chosen per world.
+(BVH depth, how often queries collide), so it is chosen per world and can be
+cached per (mesh pair, GPU model) in a JSON file (``TuneCache``).
 
 ``SegmentGraph`` captures one ``pw_segments_first_contact`` call over a
 resident batch into a CUDA graph (graph mode: no host synchronisation, no
@@ -16,9 +17,14 @@ launch.
 """
 from __future__ import annotations
 
+import hashlib
 import itertools
+import json
+import os
+import tempfile
 from dataclasses import dataclass, field
 
+import numpy as np
 import torch
 
 from . import _lib
@@ -94,13 +100,98 @@ def tune_segments(uw, q0: torch.Tensor, q1: torch.Tensor, verify_delta: float, s
     return TuneReport("segments", cfg, default_ms, ms, table)
 
 
-def autotune(uw, states: torch.Tensor | None = None, segments=None, verify_delta: float = 0.001, **kw):
-    """Tune both kernels on samples of the caller's workload; returns the reports."""
+def tune_key(meshes, device_name: str, num_sms: int, kernel: str, extra: str = "") -> str:
+    """Cache key of a tuned configuration: the mesh pair's arrays (env and robot
+    vertices and faces as loaded), the GPU model and SM count, and the kernel."""
+    h = hashlib.sha256()
+    for m in meshes:
+        if m is None:
+            h.update(b"none")
+            continue
+        for a in m:
+            a = np.ascontiguousarray(a)
+            h.update(str((a.dtype.str, a.shape)).encode())
+            h.update(a.tobytes())
+    h.update(("%s|%d|%s|%s" % (device_name, num_sms, kernel, extra)).encode())
+    return h.hexdigest()
+
+
+class TuneCache:
+    """Tuned configurations per (mesh pair, GPU), in a JSON file.  The default
+    file is $PW_AUTOTUNE_CACHE, else ~/.cache/puzzletunneldiscovery_gb300/autotune.json.
+    Writes go through a temporary file and a rename, so a reader never sees a
+    partial file."""
+
+    def __init__(self, path: str | None = None):
+        self.path = path or os.environ.get("PW_AUTOTUNE_CACHE") or os.path.join(
+            os.path.expanduser("~"), ".cache", "puzzletunneldiscovery_gb300", "autotune.json")
+
+    def load(self) -> dict:
+        try:
+            with open(self.path) as fh:
+                d = json.load(fh)
+            return d if isinstance(d, dict) else {}
+        except (OSError, ValueError):
+            return {}
+
+    def get(self, key: str):
+        return self.load().get(key)
+
+    def put(self, key: str, value: dict) -> None:
+        d = self.load()
+        d[key] = value
+        os.makedirs(os.path.dirname(os.path.abspath(self.path)), exist_ok=True)
+        fd, tmp = tempfile.mkstemp(dir=os.path.dirname(os.path.abspath(self.path)), suffix=".tmp")
+        with os.fdopen(fd, "w") as fh:
+            json.dump(d, fh, indent=1, sort_keys=True)
+        os.replace(tmp, self.path)
+
+
+def _world_key(uw, kernel: str) -> str:
+    props = torch.cuda.get_device_properties(uw._device)
+    return tune_key(uw._meshes, props.name, props.multi_processor_count, kernel, "%.17g" % uw.scene_scale)
+
+
+def _apply(uw, kernel: str, cfg: dict) -> None:
+    if kernel == "states":
+        uw.set_launch_config(0, cfg.get("width", 0), cfg.get("soft_cap", 0), cfg.get("blocks", 0))
+    else:
+        uw.set_launch_config(1, 0, cfg.get("soft_cap", 0), cfg.get("blocks", 0))
+
+
+def autotune(uw, states: torch.Tensor | None = None, segments=None, verify_delta: float = 0.001,
+             cache: "TuneCache | str | bool | None" = None, **kw):
+    """Tune both kernels on samples of the caller's workload; returns the reports.
+
+    With a cache (True for the default file, a path, or a TuneCache) a
+    configuration already tuned for the same mesh pair on the same GPU model is
+    applied without timing anything (its report has an empty table); a new one
+    is stored after tuning."""
+    tc = None
+    if cache is True:
+        tc = TuneCache()
+    elif isinstance(cache, str):
+        tc = TuneCache(cache)
+    elif isinstance(cache, TuneCache):
+        tc = cache
     out = {}
+    jobs = []
     if states is not None:
-        out["states"] = tune_states(uw, states, **kw)
+        jobs.append(("states", lambda: tune_states(uw, states, **kw)))
     if segments is not None:
-        out["segments"] = tune_segments(uw, segments[0], segments[1], verify_delta, **kw)
+        jobs.append(("segments", lambda: tune_segments(uw, segments[0], segments[1], verify_delta, **kw)))
+    for kernel, run in jobs:
+        key = _world_key(uw, kernel) if tc is not None else None
+        hit = tc.get(key) if tc is not None else None
+        if hit is not None:
+            _apply(uw, kernel, hit["config"])
+            out[kernel] = TuneReport(kernel, dict(hit["config"]), float(hit["default_ms"]), float(hit["best_ms"]))
+            continue
+        r = run()
+        if tc is not None:
+            tc.put(key, {"config": r.best, "default_ms": r.default_ms, "best_ms": r.best_ms,
+                         "configs_tried": len(r.table)})
+        out[kernel] = r
     return out
 
 

@@ -98,3 +98,31 @@ def test_autotune_keeps_verdicts(built_lib, oracle_mod):
     ow = oracle_mod.OracleWorld(*W.cfg_interlocking_tori())
     qs = q[:5000].cpu().numpy()
     assert (uw.is_valid_states(torch.from_numpy(qs).cuda()).cpu().numpy() == ow.is_valid(qs)).all()
+
+
+def test_autotune_cache_reapplies_a_tuned_configuration(built_lib, tmp_path):
+    """A configuration tuned for a mesh pair on this GPU is stored; a second world
+    with the same meshes gets it from the cache without timing anything, and a
+    different mesh pair misses the cache."""
+    import puzzletunneldiscovery_gb300 as pw
+    from puzzletunneldiscovery_gb300.autotune import TuneCache, autotune
+    path = str(tmp_path / "tune.json")
+    uw = _world()
+    q = torch.from_numpy(W.uniform_states(100000, -2.0, 2.0, uw.scene_scale, seed=47)).cuda()
+    first = autotune(uw, states=q, cache=path, soft_caps=(128, 0), blocks=(0, 2), reps=1)["states"]
+    assert len(first.table) == 3 * 2 * 2
+    applied = uw.get_launch_config(0)
+    second_world = _world()
+    again = autotune(second_world, states=q, cache=path, soft_caps=(128, 0), blocks=(0, 2), reps=1)["states"]
+    assert again.table == [] and again.best == first.best
+    assert second_world.get_launch_config(0) == applied
+    assert torch.equal(second_world.is_valid_states(q), uw.is_valid_states(q))
+    Ve, Fe, Vr, Fr = W.interlocking_tori(1.0, 0.25, 48, 24)
+    other = pw.UnitWorld(0)
+    other.load_env_mesh(Ve, Fe)
+    other.load_robot_mesh(Vr, Fr)
+    other.scaleToUnit()
+    other.angleModel(0.0, 0.0)
+    miss = autotune(other, states=q, cache=TuneCache(path), soft_caps=(0,), blocks=(0,), reps=1)["states"]
+    assert len(miss.table) == 3
+    assert len(TuneCache(path).load()) == 2

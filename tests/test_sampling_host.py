@@ -120,3 +120,24 @@ def test_narrow_midpoint_is_the_slerp_midpoint(oracle_mod):
     m = N.midpoints(torch.from_numpy(q0), torch.from_numpy(q1)).numpy()
     for i in range(300):
         assert np.abs(m[i] - oracle_mod.interpolate(q0[i], q1[i], 0.5)).max() < 1e-14
+
+
+def test_autotune_cache_keys_and_file(tmp_path):
+    """The tuned-configuration cache: keys separate mesh pairs, GPU models and
+    kernels; the JSON file round-trips and is replaced atomically."""
+    from puzzletunneldiscovery_gb300.autotune import TuneCache, tune_key
+    V = np.zeros((3, 3), np.float32)
+    F = np.array([[0, 1, 2]], np.uint32)
+    V2 = V.copy()
+    V2[1, 0] = 1.0
+    k = tune_key([(V, F), (V, F)], "GB300", 152, "states")
+    assert k == tune_key([(V.copy(), F.copy()), (V, F)], "GB300", 152, "states")
+    assert k != tune_key([(V2, F), (V, F)], "GB300", 152, "states")
+    assert k != tune_key([(V, F), (V, F)], "GB300", 148, "states")
+    assert k != tune_key([(V, F), (V, F)], "GB300", 152, "segments")
+    c = TuneCache(str(tmp_path / "sub" / "tune.json"))
+    assert c.get(k) is None
+    c.put(k, {"config": {"width": 16, "soft_cap": 0, "blocks": 0}, "default_ms": 2.0, "best_ms": 1.5})
+    c.put("other", {"config": {}, "default_ms": 1.0, "best_ms": 1.0})
+    assert TuneCache(str(tmp_path / "sub" / "tune.json")).get(k)["config"]["width"] == 16
+    assert sorted(p.name for p in (tmp_path / "sub").iterdir()) == ["tune.json"]
