@@ -372,6 +372,49 @@ class UnitWorld:
         tup = self.transit_state_to_with_contact(from_state, to_state, verify_delta)
         return tup[0], tup[2], tup[3]
 
+    def transit_state(self, state, action: int, transit_magnitude: float, verify_delta: float):
+        """UnitWorld::transitState (unit_world.cc:268-330): one of the 12 discrete
+        actions (translation / rotation, +- x, y, z) by the verify step (twice it
+        for rotations, as float32), then transit_state_to, halving the float32
+        verify step while no progress is made.  An invalid action or start state
+        returns (state, False, 0.0).  transit_magnitude is unused, as in the
+        reference's active branch."""
+        from . import state_ops as so
+        q = _states_np(state)[0]
+        if action < 0 or action >= 12 or not self.is_valid_state(q):
+            return q, False, 0.0
+        action_type = 0 if action < 6 else 1
+        deltacap = np.float32(verify_delta) if action_type == 0 else np.float32(verify_delta * 2.0)
+        sym = np.float32(1.0 if action % 2 == 0 else -1.0)
+        axis = np.zeros(3)
+        axis[(action - 6 * action_type) // 2] = 1.0
+        trans, rot = so.decompose(q)
+        if action_type == 0:
+            trans = trans + float(deltacap) * axis * float(sym)
+        else:
+            rot = so.quat_mul(so.quat_from_angleaxis(float(np.float32(deltacap * sym)), axis), rot)
+        to = so.compose(trans, rot)
+        cvd = np.float32(verify_delta)
+        while True:
+            free, done, prog = self.transit_state_to(q, to, float(cvd))
+            if not self.is_valid_state(free):
+                raise RuntimeError("SAN check failed, invalid state from transitStateTo")
+            if prog > 0.0 or cvd == 0.0:
+                return free, done, prog
+            cvd = np.float32(cvd / 2.0)
+
+    def transit_state_by(self, from_state, tr, aav, verify_delta: float):
+        """UnitWorld::transitStateBy (unit_world.cc:490-507): the target is the start
+        translated by tr and rotated on the left by the angle-axis vector aav (the
+        start's quaternion as given, not normalised)."""
+        from . import state_ops as so
+        a = _states_np(from_state)[0]
+        aav = np.asarray(aav, dtype=np.float64).reshape(3)
+        n = float(np.linalg.norm(aav))
+        rot = so.quat_mul(so.quat_from_angleaxis(n, aav / n if n > 0 else aav), a[3:7])
+        to = np.concatenate([a[:3] + np.asarray(tr, dtype=np.float64).reshape(3), rot])
+        return self.transit_state_to(a, to, verify_delta)
+
     def is_valid_transition(self, from_state, to_state, initial_verify_delta) -> bool:
         a = _states_np(from_state)
         b = _states_np(to_state)
@@ -399,6 +442,102 @@ class UnitWorld:
 
     def translate_unit_to_ompl(self, Q, to_angle_axis: bool = False):
         return self._convert(self._L.pw_world_translate_unit_to_ompl, Q, int(bool(to_angle_axis)))
+
+    def _vanilla_offset(self, qs, sign: float):
+        from . import state_ops as so
+        qs = _states_np(qs)
+        oc = self.get_ompl_center(GEO_ROB)
+        out = qs.copy()
+        for i, q in enumerate(qs):
+            # vanilla and OMPL states are both w-last
+            r = np.array([q[6], q[3], q[4], q[5]])
+            out[i, :3] = q[:3] + sign * (so.quat_to_matrix(r / np.linalg.norm(r)) @ oc)
+        return out
+
+    def translate_vanilla_to_ompl(self, qs):
+        """t_ompl = t_vanilla + R O, O the robot's OMPL centre (unit_world.cc:600-638)."""
+        return self._vanilla_offset(qs, 1.0)
+
+    def translate_ompl_to_vanilla(self, qs):
+        """t_vanilla = t_ompl - R O (unit_world.cc:640-661)."""
+        return self._vanilla_offset(qs, -1.0)
+
+    def translate_vanilla_to_unit(self, qs):
+        """unit_world.cc:663-667."""
+        return self.translate_ompl_to_unit(self.translate_vanilla_to_ompl(qs))
+
+    def translate_vanilla_pts_to_unit(self, geo: int, pts):
+        """Points of a mesh's own frame to the unit frame: the scene's calibration
+        transform, after the OMPL centre is taken off robot points
+        (unit_world.cc:669-688)."""
+        pts = np.asarray(pts, dtype=np.float64)
+        if pts.ndim != 2 or pts.shape[0] == 0:
+            return np.zeros((0, 3))
+        p = pts[:, :3] if geo == GEO_ENV else pts[:, :3] - self.get_ompl_center(GEO_ROB)
+        h = np.concatenate([p, np.ones((p.shape[0], 1))], axis=1)
+        return (self.scene_matrix @ h.T).T[:, :3]
+
+    # kinetic-energy metric (unit_world.cc:1567-1596) -------------------------------
+    def _robot_mass_properties(self):
+        """Volume and inertia tensor of the robot's CD mesh: the divergence-theorem
+        sums over the tetrahedra (origin, triangle) -- signed volume det / 6 and
+        the covariance det * A^T C0 A, C0 the unit tetrahedron's (1/60 on the
+        diagonal, 1/120 off it), inertia = trace(C) I - C -- rebased to the robot
+        scene's centre as cdmodel.cc:60-80 does."""
+        cache = self.__dict__.get("_mass_cache")
+        key = (id(self._meshes[1][0]) if self._meshes[1] is not None else None, self.scene_scale)
+        if cache is not None and cache[0] == key:
+            return cache[1], cache[2]
+        V, F = self._cd(GEO_ROB)
+        A = V[F]                                     # [m, 3 vertices, 3 coords]: rows are the vertices
+        det = np.einsum("ij,ij->i", np.cross(A[:, 0], A[:, 1]), A[:, 2])
+        C0 = np.full((3, 3), 1.0 / 120.0) + np.eye(3) * (1.0 / 120.0)
+        C = np.einsum("m,mki,kl,mlj->ij", det, A, C0, A)
+        vol = float(det.sum()) / 6.0
+        mi = np.trace(C) * np.eye(3) - C
+        c = np.array(self._info().robot_center[:])
+        off = np.outer(c, c)
+        rebased = mi + vol * off
+        for k in range(3):
+            rebased[k, k] = mi[k, k] - vol * (float(c @ c) - c[k] * c[k])
+        self._mass_cache = (key, rebased, vol)
+        return rebased, vol
+
+    def kinetic_energy_distance(self, q0, q1) -> float:
+        """|dt|^2 + 4 dr_v^T I dr_v / volume, dr = rot1 rot0^-1 (unit_world.cc:1567-1582)."""
+        from . import state_ops as so
+        t0, r0 = so.decompose(q0)
+        t1, r1 = so.decompose(q1)
+        dt = t1 - t0
+        dr = so.quat_mul(r1, so.quat_inverse(r0))
+        inertia, vol = self._robot_mass_properties()
+        return float(dt @ dt) + float(dr[1:] @ inertia @ dr[1:]) * 4.0 / vol
+
+    def multi_kinetic_energy_distance(self, origin, targets):
+        targets = _states_np(targets)
+        return np.array([self.kinetic_energy_distance(origin, t) for t in targets])
+
+    # free-configuration samplers with pyosr's method names (module.cc:211-226) -------
+    def sample_free_configuration(self, rob_surface_point, rob_surface_normal, env_surface_point,
+                                  env_surface_normal, margin: float, max_trials: int = -1):
+        """UnitWorld::sampleFreeConfiguration; max_trials < 0 tries until a free
+        spin is found, as the reference does."""
+        from . import sampling
+        if max_trials >= 0:
+            return sampling.sample_free_configuration(self, rob_surface_point, rob_surface_normal, env_surface_point,
+                                                      env_surface_normal, margin, max_trials)
+        while True:
+            q, found = sampling.sample_free_configurations(self, rob_surface_point, rob_surface_normal,
+                                                           env_surface_point, env_surface_normal, margin, 255)
+            if bool(found[0]):
+                return q[0]
+
+    def enum_free_configuration(self, rob_surface_point, rob_surface_normal, env_surface_point, env_surface_normal,
+                                margin: float, denominator: int, only_median: bool = False):
+        """UnitWorld::enumFreeConfiguration (all spins checked as one batch)."""
+        from . import sampling
+        return sampling.enum_free_configuration(self, rob_surface_point, rob_surface_normal, env_surface_point,
+                                                env_surface_normal, margin, denominator, only_median)
 
     # ----------------------------------------------------------- visibility batches
     def _pairs_first(self, qs0, qs1, verify_magnitude):
