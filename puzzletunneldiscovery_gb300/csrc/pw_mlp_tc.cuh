@@ -384,6 +384,15 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 			}
 			for (int layer = 0; layer < 4 && ok; layer++) {
 				const float *bias = a.ht + layer * H;   // b_l / 2
+				if (layer == 2 && g == 0) {
+					// the next pair's state rows into L2 while this pair finishes, so that its
+					// features do not wait on HBM at the pair boundary
+					for (int sl = 0; sl < 2; sl++) {
+						const int64_t row = (tA + 2 * G + sl * G) * TILE_M + r;
+						if (row < a.n)
+							asm volatile("prefetch.global.L2 [%0];" ::"l"(a.states + 7 * row));
+					}
+				}
 				for (int sl = 0; sl < nslot; sl++) {
 					if (!mbar_wait(bar(B_DONE + sl), done_ph[sl], s_abort, a.err, 4)) {
 						ok = false;
