@@ -120,7 +120,7 @@ class TuneCache:
     """Tuned configurations per (mesh pair, GPU), in a JSON file.  The default
     file is $PW_AUTOTUNE_CACHE, else ~/.cache/puzzletunneldiscovery_gb300/autotune.json.
     Writes go through a temporary file and a rename, so a reader never sees a
-    partial file."""
+    partial file; two processes writing at once keep the last writer's entries."""
 
     def __init__(self, path: str | None = None):
         self.path = path or os.environ.get("PW_AUTOTUNE_CACHE") or os.path.join(

@@ -198,6 +198,8 @@ class UnitWorld:
         hs = []
         for h in hosts:
             t = h if isinstance(h, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(h, dtype=np.float64))
+            if t.is_cuda:
+                raise TypeError("host entry points take host batches; use the device methods for CUDA tensors")
             if t.dtype != torch.float64 or t.dim() != 2 or t.shape[1] != 7:
                 raise ValueError("host states must be float64 [n, 7]")
             t = t.contiguous()
