@@ -33,7 +33,10 @@ namespace {
 using namespace pwf;
 
 constexpr int WARPS = 4;                  // warps per block
-constexpr int STACK_CAP = 896;            // node-pair stack entries per warp
+// node-pair stack entries per warp: 384 keeps a warp's shared memory at 6.6 KB, so
+// that 8 blocks of 4 warps are resident per SM (measured: 5 blocks with 896
+// entries, 7 with 512, 8 with 384 took the 1M-segment step from 336 to 299 ms)
+constexpr int STACK_CAP = 384;
 constexpr int UNC_CAP = 32;               // uncertain pairs buffered per warp
 constexpr unsigned FULL = 0xffffffffu;
 constexpr uint64_t RETEST_CAP = 1u << 22; // queued FP64 re-tests per query batch
@@ -561,7 +564,7 @@ __device__ void flush_stats(QueryCounters *ctr, const LaneStats &st, unsigned lo
 // ------------------------------------------------------------------ states
 
 template <uint64_t CAP>
-__global__ void __launch_bounds__(WARPS * 32) k_states(WorldDev W, const double *states, int64_t n,
+__global__ void __launch_bounds__(WARPS * 32, 8) k_states(WorldDev W, const double *states, int64_t n,
                                                        uint8_t *out, QueryCounters *ctr, RetestEntry *rq,
                                                        int soft_cap, int width)
 {
@@ -843,7 +846,7 @@ __global__ void __launch_bounds__(1024) k_rounds(const uint32_t *sorted_keys, in
 // contacts prune later chunks.  A warp computes the chunk's FP64 states lane-
 // parallel, then answers its steps with one swept traversal and records the
 // first step in contact with atomicMin.
-__global__ void __launch_bounds__(WARPS * 32) k_segments(WorldDev W, StateSrc src, const uint32_t *order,
+__global__ void __launch_bounds__(WARPS * 32, 8) k_segments(WorldDev W, StateSrc src, const uint32_t *order,
                                                          const int64_t *round_off, const int64_t *nrounds_p,
                                                          int32_t *first, QueryCounters *ctr, RetestEntry *rq,
                                                          int soft_cap)
