@@ -487,17 +487,18 @@ class UnitWorld:
         diagonal, 1/120 off it), inertia = trace(C) I - C -- rebased to the robot
         scene's centre as cdmodel.cc:60-80 does."""
         cache = self.__dict__.get("_mass_cache")
-        key = (id(self._meshes[1][0]) if self._meshes[1] is not None else None, self.scene_scale)
+        V, F = self._cd(GEO_ROB)
+        c = np.array(self._info().robot_center[:])
+        # keyed by what the result depends on: the CD mesh as placed and the rebase centre
+        key = (V.tobytes(), F.tobytes(), c.tobytes())
         if cache is not None and cache[0] == key:
             return cache[1], cache[2]
-        V, F = self._cd(GEO_ROB)
         A = V[F]                                     # [m, 3 vertices, 3 coords]: rows are the vertices
         det = np.einsum("ij,ij->i", np.cross(A[:, 0], A[:, 1]), A[:, 2])
         C0 = np.full((3, 3), 1.0 / 120.0) + np.eye(3) * (1.0 / 120.0)
         C = np.einsum("m,mki,kl,mlj->ij", det, A, C0, A)
         vol = float(det.sum()) / 6.0
         mi = np.trace(C) * np.eye(3) - C
-        c = np.array(self._info().robot_center[:])
         off = np.outer(c, c)
         rebased = mi + vol * off
         for k in range(3):
