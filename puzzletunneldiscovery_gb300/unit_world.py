@@ -517,8 +517,19 @@ class UnitWorld:
         return float(dt @ dt) + float(dr[1:] @ inertia @ dr[1:]) * 4.0 / vol
 
     def multi_kinetic_energy_distance(self, origin, targets):
+        """kinetic_energy_distance(origin, targets[i]) for every row (unit_world.cc:1584-1596)."""
+        from . import state_ops as so
         targets = _states_np(targets)
-        return np.array([self.kinetic_energy_distance(origin, t) for t in targets])
+        inertia, vol = self._robot_mass_properties()
+        t0, r0 = so.decompose(origin)
+        inv0 = so.quat_inverse(r0)
+        out = np.empty(targets.shape[0])
+        for i, q in enumerate(targets):
+            t1, r1 = so.decompose(q)
+            dt = t1 - t0
+            dv = so.quat_mul(r1, inv0)[1:]
+            out[i] = float(dt @ dt) + float(dv @ inertia @ dv) * 4.0 / vol
+        return out
 
     # free-configuration samplers with pyosr's method names (module.cc:211-226) -------
     def sample_free_configuration(self, rob_surface_point, rob_surface_normal, env_surface_point,
