@@ -32,6 +32,39 @@ def build(force: bool = False) -> str:
     return _LIB_PATH
 
 
+_REF_SRC = "/root/reference/lib/tritri/Moller97d.cc"
+_REF_LIB = os.path.join(_HERE, "_ref", "libref_tritri.so")
+_ref = None
+
+
+def build_ref() -> str | None:
+    """Compile the reference's own Moller test (its source where it lies) into
+    _ref/ when the reference checkout is present; None otherwise."""
+    if not os.path.exists(_REF_SRC):
+        return _REF_LIB if os.path.exists(_REF_LIB) else None
+    if not os.path.exists(_REF_LIB) or os.path.getmtime(_REF_LIB) < os.path.getmtime(
+            os.path.join(_HERE, "ref_tritri_shim.cc")):
+        subprocess.run(["make", "-s", "-C", _HERE, "_ref/libref_tritri.so"], check=True)
+    return _REF_LIB
+
+
+def ref_lib():
+    """The reference's triangle test (ref_tri_tri, ref_tri_tri_isect), or None."""
+    global _ref
+    if _ref is None:
+        path = build_ref()
+        if path is None or not os.path.exists(path):
+            return None
+        try:
+            L = ctypes.CDLL(path)
+        except OSError:
+            return None
+        L.ref_tri_tri.argtypes = [c_double_p] * 6
+        L.ref_tri_tri_isect.argtypes = [c_double_p] * 6 + [ctypes.POINTER(ctypes.c_int), c_double_p, c_double_p]
+        _ref = L
+    return _ref
+
+
 def lib():
     global _lib
     if _lib is None:

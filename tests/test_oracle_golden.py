@@ -160,3 +160,71 @@ def test_intersecting_segments_oracle(oracle_mod):
     np.testing.assert_allclose(m, np.linalg.norm(e - b, axis=1), rtol=1e-12, atol=1e-15)
     b, e, m, p, c = w.intersecting_segments(np.array([5.0, 5.0, 5.0, 1, 0, 0, 0]))
     assert len(m) == 0
+
+
+def _tri_cases(seed):
+    """Random pairs, pairs sharing a vertex or an edge, coplanar pairs, pairs with a
+    vertex on the other's plane, pairs nudged around touching, and tiny pairs."""
+    rng = np.random.default_rng(seed)
+    out = [(rng.uniform(-1, 1, (3, 3)), rng.uniform(-1, 1, (3, 3))) for _ in range(3000)]
+    for _ in range(500):
+        V = rng.uniform(-1, 1, (3, 3))
+        U = rng.uniform(-1, 1, (3, 3))
+        U[0] = V[rng.integers(0, 3)]
+        out.append((V, U.copy()))
+        U[1] = V[(rng.integers(0, 3))]
+        out.append((V, U.copy()))
+        Vc, Uc = V.copy(), U.copy()
+        Vc[:, 2] = 0.0
+        Uc[:, 2] = 0.0
+        out.append((Vc, Uc))
+        n = np.cross(V[1] - V[0], V[2] - V[0])
+        n /= np.linalg.norm(n)
+        W = U.copy()
+        W[0] -= np.dot(W[0] - V[0], n) * n          # a vertex on V's plane (to rounding)
+        out.append((V, W))
+        for eps in (1e-9, 1e-7, 1e-5):
+            out.append((V, W + eps * rng.normal(size=(3, 3))))
+    for _ in range(500):
+        s = 0.0025
+        out.append((rng.uniform(-1, 1, (3, 3)) * s, rng.uniform(-1, 1, (3, 3)) * s))
+    return out
+
+
+def test_moller_restatement_matches_the_reference_source(oracle_mod):
+    """The oracle's Moller test with the reference's 1e-6 snap against the
+    reference's own lib/tritri/Moller97d.cc (built from its source by
+    oracle/Makefile): verdict, coplanarity and intersection-line endpoints bit
+    for bit, on random and near-degenerate pairs."""
+    import ctypes
+    ref = oracle_mod.ref_lib()
+    if ref is None:
+        pytest.skip("the reference checkout is not present (its Moller source cannot be built here)")
+    p = lambda a: np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+    cases = _tri_cases(8)
+    hits = cops = 0
+    random_diffs = tiny_diffs = 0
+    for i, (V, U) in enumerate(cases):
+        args = [p(v) for v in V] + [p(u) for u in U]
+        want = bool(ref.ref_tri_tri(*args))
+        assert oracle_mod.tri_tri(list(V), list(U), eps=1e-6) is want
+        cop = ctypes.c_int(0)
+        r1, r2 = np.zeros(3), np.zeros(3)
+        wi = bool(ref.ref_tri_tri_isect(*args, ctypes.byref(cop), p(r1), p(r2)))
+        hit, coplanar, q1, q2 = oracle_mod.tri_tri_isect(list(V), list(U), eps=1e-6)
+        assert hit is wi and coplanar is bool(cop.value)
+        if wi and not cop.value:
+            assert np.array_equal(q1, r1) and np.array_equal(q2, r2)
+        hits += wi
+        cops += bool(cop.value)
+        # the engine's verdict takes no snap: on generic pairs it agrees with the
+        # snapped one; on 0.0025-unit triangles (plate cells) the absolute 1e-6
+        # snap of unnormalised plane distances swallows real separations
+        diff = oracle_mod.tri_tri(list(V), list(U), eps=0.0) is not want
+        if i < 3000:
+            random_diffs += diff
+        elif i >= len(cases) - 500:
+            tiny_diffs += diff
+    assert hits > 500 and cops > 100
+    assert random_diffs == 0
+    assert tiny_diffs > 0
