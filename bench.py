@@ -22,6 +22,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -33,7 +34,9 @@ from puzzletunneldiscovery_gb300 import workloads as W  # noqa: E402
 
 UNIT = "checks/s"
 DELTA = 0.001
-# per-unit algorithmic bytes of the traversal kernel (roofline section)
+# per-unit algorithmic bytes of the traversal kernel: each node-pair test reads two
+# FP32 boxes, each leaf test two FP32 triangles, each segment its two states and
+# writes its first-contact step
 BYTES_NODE_PAIR = 2 * 32      # env node + robot node (two float4 each)
 BYTES_LEAF_PAIR = 2 * 48      # env triangle + robot triangle (three float4 each)
 BYTES_SEGMENT = 2 * 56 + 4    # two states in, one int32 out
@@ -86,7 +89,10 @@ class ClockSampler:
     def __init__(self, device):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks_%d.csv" % os.getpid())
+        # samples go to a temporary file (override with PW_BENCH_CLOCKS_DIR); the
+        # JSON line carries their summary
+        self.path = os.path.join(os.environ.get("PW_BENCH_CLOCKS_DIR", tempfile.gettempdir()),
+                                 "bench_clocks_%d.csv" % os.getpid())
 
     def __enter__(self):
         try:
