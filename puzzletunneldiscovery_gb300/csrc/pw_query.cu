@@ -33,10 +33,11 @@ namespace {
 using namespace pwf;
 
 constexpr int WARPS = 4;                  // warps per block
-// node-pair stack entries per warp: 384 keeps a warp's shared memory at 6.6 KB, so
-// that 8 blocks of 4 warps are resident per SM (measured: 5 blocks with 896
-// entries, 7 with 512, 8 with 384 took the 1M-segment step from 336 to 299 ms)
-constexpr int STACK_CAP = 384;
+// node-pair stack entries per warp: 416 keeps a warp's shared memory at 6.8 KB, so
+// that 8 blocks of 4 warps (with the 1 KB the runtime reserves per block) fit in
+// the SM's 228 KB (measured: 5 blocks with 896 entries, 7 with 512, 8 with 384
+// took the 1M-segment step from 336 to 299 ms; 416 gained another 1 % on the plate)
+constexpr int STACK_CAP = 416;
 constexpr int UNC_CAP = 32;               // uncertain pairs buffered per warp
 constexpr unsigned FULL = 0xffffffffu;
 constexpr uint64_t RETEST_CAP = 1u << 22; // queued FP64 re-tests per query batch
