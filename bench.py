@@ -395,7 +395,9 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(work.bytes_in() * ws),
                     "d2h_bytes_per_step": int(work.bytes_out() * ws)},
             "clocks": clk.summary(),
-            "gpu_launches": (6 if args.workload == "segments" else 2) * args.steps,
+            # segments: bounds, set-up, anchors, rounds, traversal, re-test, finalise (CUB's scan and
+            # sort not counted); states: traversal, re-test
+            "gpu_launches": (7 if args.workload == "segments" else 2) * args.steps,
             "detail": dict({"reference_checks_per_step": tot_checks / args.steps,
                             "gpu_queries_per_step": last["queries"], "node_tests": last["node_tests"],
                             "leaf_tests": last["leaf_tests"], "fp64_retests": last["retests"],
@@ -672,9 +674,9 @@ def run_narrow(args):
                     "d2h_bytes_per_step": int(d2h)},
             "clocks": clk.summary(),
             # this project's kernels per guided round: crossing filter 1, network scores 2, the
-            # replayed validation graph 6 (bounds, set-up, rounds, traversal, re-test, finalise;
-            # its CUB scan and sort kernels not counted), endpoint labels 2 (traversal, re-test)
-            "gpu_launches": 11 * sum(r.rounds for r in g_reps),
+            # replayed validation graph 7 (bounds, set-up, anchors, rounds, traversal, re-test,
+            # finalise; its CUB scan and sort kernels not counted), endpoint labels 2 (traversal, re-test)
+            "gpu_launches": 12 * sum(r.rounds for r in g_reps),
             "detail": {"plain_escapes_per_s": plain_value, "guided_over_plain": value / max(plain_value, 1e-12),
                        "guided_yield": g_esc / max(1, sum(r.validated for r in g_reps)),
                        "plain_yield": p_esc / max(1, sum(r.validated for r in p_reps)),

@@ -692,10 +692,43 @@ __device__ __forceinline__ void seg_step_qf(const WorldDev &W, const double *a, 
 	make_qf(q, W, o);
 }
 
+// The anchor frame of every chunk (k_seg_setup's checkpoints and step counts
+// in place), one thread per checkpoint slot over a grid-stride loop: the
+// chunk's segment by binary search of the slot offsets, its anchor step's
+// delta walked from the chunk's checkpoint with the reference's update, the
+// FP64 state interpolated and reduced to the FP32 frame.  Kept apart from the
+// sequential per-segment loop so that segments of very different lengths do
+// not leave the FP64 lanes of a warp idle.
+__global__ void k_seg_anchors(WorldDev W, const double *from, const double *to, int64_t n, const int64_t *slot_base,
+                              const SegParams *params, const double *ckpt, QFs *anchors)
+{
+	const int64_t total = slot_base[n];
+	for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < total;
+	     c += (int64_t)gridDim.x * blockDim.x) {
+		int64_t lo = 0, hi = n;          // slot_base[lo] <= c < slot_base[hi]
+		while (hi - lo > 1) {
+			const int64_t mid = (lo + hi) >> 1;
+			if (slot_base[mid] <= c)
+				lo = mid;
+			else
+				hi = mid;
+		}
+		const SegParams &P = params[lo];
+		const int64_t j = c - slot_base[lo];
+		const int64_t K = P.nsteps;
+		if (j >= (K + 31) / 32)
+			continue;                    // a slot past the segment's chunks (or no steps)
+		const int cnt = (int)min((int64_t)32, K - 32 * j);
+		double d = ckpt[c];
+		for (int i = 0; i < anchor_of(cnt); i++)
+			d = pwm::advance_delta(d, P.dist, P.step);
+		seg_step_qf(W, from + 7 * lo, to + 7 * lo, P, d, anchors[c]);
+	}
+}
+
 __global__ void k_seg_setup(WorldDev W, const double *from, const double *to, int64_t n, double vdelta, int mode,
                             const int64_t *slots, const int64_t *slot_base, SegParams *params, double *ckpt,
-                            QFs *anchors, int32_t *first, uint32_t *keys, uint32_t *vals, QueryCounters *ctr,
-                            int64_t ckpt_cap)
+                            int32_t *first, uint32_t *keys, uint32_t *vals, QueryCounters *ctr, int64_t ckpt_cap)
 {
 	const double rob_r2 = W.rob.r2;
 	const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -759,28 +792,14 @@ __global__ void k_seg_setup(WorldDev W, const double *from, const double *to, in
 				// plain sums, so only the adds run (same FP64 values, bit for bit)
 				const float room = __fdiv_rn((float)pwm::sub(dist, delta), (float)step);
 				if (room > 40.f) {
-					for (int i = 0; i < 32; i++) {
-						if (i == 15)
-							seg_step_qf(W, a, b, P, delta, anchors[P.ckpt_base + (K >> 5)]);
+					for (int i = 0; i < 32; i++)
 						delta = pwm::add(delta, step);
-					}
 					K += 32;
 					continue;
 				}
 			}
-			if ((K & 31) == 15)   // the chunk has at least 16 steps: its anchor is step 15
-				seg_step_qf(W, a, b, P, delta, anchors[P.ckpt_base + (K >> 5)]);
 			delta = pwm::advance_delta(delta, dist, step);
 			K++;
-		}
-		const int last = (int)(K & 31);
-		if (K > 0 && last > 0 && last < 16) {
-			// short last chunk: its anchor is its middle step
-			const int64_t c = (K - 1) >> 5;
-			double d = ckpt[P.ckpt_base + c];
-			for (int i = 0; i < anchor_of(last); i++)
-				d = pwm::advance_delta(d, dist, step);
-			seg_step_qf(W, a, b, P, d, anchors[P.ckpt_base + c]);
 		}
 	}
 	P.nsteps = (int32_t)K;
@@ -1295,8 +1314,9 @@ extern "C" int pw_segments_first_contact(pw_world *w, const double *from, const 
 	double *ckpt = (double *)w->seg_ckpt.ptr;
 	uint32_t *keys = (uint32_t *)w->seg_keys.ptr, *vals = (uint32_t *)w->seg_order.ptr;
 	uint32_t *keys2 = (uint32_t *)w->seg_keys2.ptr, *vals2 = (uint32_t *)w->seg_order2.ptr;
-	k_seg_setup<<<G, B, 0, st>>>(w->dev, from, to, n, verify_delta, mode, slots, slot_base, params, ckpt, anchors,
+	k_seg_setup<<<G, B, 0, st>>>(w->dev, from, to, n, verify_delta, mode, slots, slot_base, params, ckpt,
 	                             first_step, keys, vals, ctr, ckpt_cap);
+	k_seg_anchors<<<(unsigned)(w->num_sms * 8), 256, 0, st>>>(w->dev, from, to, n, slot_base, params, ckpt, anchors);
 	PW_CUDA(cudaGetLastError());
 	PW_CUDA(cub::DeviceRadixSort::SortPairsDescending(w->cub_tmp.ptr, t2, keys, keys2, vals, vals2, (int)n, 0, 32, st));
 	if (!w->graph_mode) {
