@@ -134,12 +134,14 @@ def screen_pairs(uw, keys, from_indices, to_indices, verify_magnitude: float | N
 
 
 def screen_keyconf(uw, keys, max_chunk_number: int = 1, minimal_chunk_size: int = 1, out_dir: str | None = None,
-                   verify_magnitude: float | None = None, batch: int = 1 << 22):
+                   verify_magnitude: float | None = None, batch: int = 1 << 22, resume: bool = False):
     """The whole screening stage: every task of partition_screening checked on
     the device (pairs decoded from flat indices there, nothing per pair on the
     host).  Returns (EDGE_FROM, EDGE_TO) over all tasks in task order; with
     out_dir, also writes edge_batch-<task>.npz per task as the reference's
-    workers do (solve2.py:226)."""
+    workers do (solve2.py:226).  With resume, a task whose file already exists
+    is read back instead of checked again, as the reference's rerun mode
+    recomputes only the missing task outputs (solve2.py:168-187)."""
     vm = uw.recommended_cres if verify_magnitude is None else float(verify_magnitude)
     keys = np.asarray(keys, dtype=np.float64)
     nkey = keys.shape[0] - RESERVED
@@ -152,6 +154,12 @@ def screen_keyconf(uw, keys, max_chunk_number: int = 1, minimal_chunk_size: int 
     dev = uw._device
     all_f, all_t = [], []
     for task, (s, e) in enumerate(bounds):
+        fn = os.path.join(out_dir, "edge_batch-{}.npz".format(task)) if out_dir is not None else None
+        if resume and fn is not None and os.path.isfile(fn):
+            d = np.load(fn)
+            all_f.append(np.asarray(d["EDGE_FROM"], dtype=np.int64))
+            all_t.append(np.asarray(d["EDGE_TO"], dtype=np.int64))
+            continue
         ef, et = [], []
         for s0 in range(int(s), int(e), batch):
             k = torch.arange(s0, min(int(e), s0 + batch), dtype=torch.int64, device=dev)
@@ -162,9 +170,9 @@ def screen_keyconf(uw, keys, max_chunk_number: int = 1, minimal_chunk_size: int 
             et.append(c[vis].cpu().numpy())
         f = np.concatenate(ef) if ef else np.zeros(0, np.int64)
         t = np.concatenate(et) if et else np.zeros(0, np.int64)
-        if out_dir is not None:
+        if fn is not None:
             os.makedirs(out_dir, exist_ok=True)
-            np.savez_compressed(os.path.join(out_dir, "edge_batch-{}.npz".format(task)), EDGE_FROM=f, EDGE_TO=t)
+            np.savez_compressed(fn, EDGE_FROM=f, EDGE_TO=t)
         all_f.append(f)
         all_t.append(t)
     return np.concatenate(all_f), np.concatenate(all_t)

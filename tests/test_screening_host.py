@@ -77,3 +77,49 @@ def test_edge_files_round_trip(tmp_path):
     assert ef.shape == (33,) and et.shape == (33,)
     want = sorted(zip(np.concatenate([p[0] for p in parts]), np.concatenate([p[1] for p in parts])))
     assert sorted(zip(ef, et)) == want
+
+
+class _FakeWorld:
+    """A stand-in for UnitWorld on the CPU: key i is visible from key j unless
+    i + j is a multiple of 3; counts the pairs it is asked about."""
+    recommended_cres = 0.01
+    _device = "cpu"
+
+    def __init__(self):
+        self.pairs = 0
+
+    def translate_to_unit_state(self, q):
+        return np.array(q, dtype=np.float64)
+
+    def first_contact_steps(self, A, B, vm, kind):
+        import torch
+        from puzzletunneldiscovery_gb300 import _lib
+        assert kind == _lib.PW_SEG_TRANSITION and vm == self.recommended_cres
+        self.pairs += A.shape[0]
+        s = (A[:, 0] + B[:, 0]).round().to(torch.int64)
+        return torch.where(s % 3 != 0, torch.full_like(s, _lib.PW_STEP_FREE), torch.full_like(s, 4))
+
+
+def test_screening_resume_checks_only_missing_tasks(tmp_path):
+    from puzzletunneldiscovery_gb300 import screening as S
+    n = 22
+    keys = np.zeros((n, 7))
+    keys[:, 0] = np.arange(n)
+    keys[:, 3] = 1.0
+    w = _FakeWorld()
+    ef, et = S.screen_keyconf(w, keys, max_chunk_number=4, minimal_chunk_size=1, out_dir=str(tmp_path), batch=7)
+    ntask = (n - S.RESERVED) * (n - S.RESERVED + 1) // 2
+    assert w.pairs == ntask
+    r, c = np.tril_indices(n - S.RESERVED)
+    r, c = r + S.RESERVED, c + S.RESERVED
+    m = (r + c) % 3 != 0
+    assert np.array_equal(ef, r[m]) and np.array_equal(et, c[m])
+    # a worker lost task 2: only its pairs are checked again
+    b = S.chunk_bounds(ntask, 4)
+    os.remove(tmp_path / "edge_batch-2.npz")
+    w2 = _FakeWorld()
+    ef2, et2 = S.screen_keyconf(w2, keys, max_chunk_number=4, minimal_chunk_size=1, out_dir=str(tmp_path),
+                                batch=7, resume=True)
+    assert w2.pairs == b[2, 1] - b[2, 0]
+    assert np.array_equal(ef2, ef) and np.array_equal(et2, et)
+    assert (tmp_path / "edge_batch-2.npz").exists()
