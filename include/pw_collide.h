@@ -229,6 +229,28 @@ PW_API int pw_world_translate_ompl_to_unit(const pw_world *w, const double *in, 
 PW_API int pw_world_translate_unit_to_ompl(const pw_world *w, const double *in, int64_t n, double *out,
                                     int to_angle_axis);
 
+/* device in, synchronous: OmplDriver::validateMotionPairs (lib/pyse3ompl/ompldriver.cc:597-621)
+ * with OMPL's discrete motion validator, for n OMPL-frame motions from[i] -> to[i]
+ * (x, y, z, qx, qy, qz, qw).  The state space is OMPL.app's SE(3) with the translation bounded
+ * by lo / hi and the longest valid segment a fraction cdres of each component's extent
+ * (setStateValidityCheckingResolution, ompldriver.cc:676-677).  valid[i] = 1 when to[i] and
+ * every state interpolate(from[i], to[i], k / nd), k = 1 .. nd - 1, are collision free;
+ * from[i] itself is not checked, as in OMPL.  A motion with a non-finite component gets 0.
+ * *states_checked (may be NULL) = the states checked over the batch.  Rejects cdres outside
+ * (0, 1), bounds with lo > hi or no extent, and motions of more than 2^31 - 1 segments. */
+PW_API int pw_ompl_check_motions(pw_world *w, const double *from, const double *to, int64_t n,
+                                 const double lo[3], const double hi[3], double cdres, uint8_t *valid,
+                                 int64_t *states_checked, void *stream);
+
+/* device in, synchronous: the states pw_ompl_check_motions checks, in the unit frame.
+ * Motion i's states are rows offsets[i] .. offsets[i + 1] - 1 of `states`: first to[i], then the
+ * interpolated states k = 1 .. nd - 1.  offsets (device, n + 1 entries) may be NULL.  *total = the
+ * number of states; PW_ERR_CAPACITY (with *total set and nothing written) when it exceeds
+ * capacity.  No counterpart in the reference: it exposes what the check looks at. */
+PW_API int pw_ompl_motion_states(pw_world *w, const double *from, const double *to, int64_t n,
+                                 const double lo[3], const double hi[3], double cdres, int64_t capacity,
+                                 double *states, int64_t *offsets, int64_t *total, void *stream);
+
 /* host: statistics of the last query on this world (synchronises its stream). */
 PW_API int pw_world_last_stats(pw_world *w, pw_query_stats *out);
 

@@ -103,6 +103,12 @@ def lib():
             getattr(L, name).argtypes = [ctypes.c_double]
         L.or_atan2q.restype = ctypes.c_double
         L.or_atan2q.argtypes = [ctypes.c_double, ctypes.c_double]
+        L.or_ompl_lvs.argtypes = [c_double_p, c_double_p, ctypes.c_double, c_double_p]
+        L.or_ompl_segment_count.restype = ctypes.c_int64
+        L.or_ompl_segment_count.argtypes = [c_double_p, c_double_p, c_double_p]
+        L.or_ompl_interpolate.argtypes = [c_double_p, c_double_p, ctypes.c_double, c_double_p]
+        L.or_ompl_motion_states.restype = ctypes.c_int64
+        L.or_ompl_motion_states.argtypes = [c_double_p, c_double_p, c_double_p, ctypes.c_int64, c_double_p]
         L.or_tri_tri.restype = ctypes.c_int
         L.or_tri_tri.argtypes = [c_double_p] * 6 + [ctypes.c_double]
         L.or_tri_tri_isect.restype = ctypes.c_int
@@ -281,3 +287,26 @@ def det_acos(x):
 
 def det_atan2(y, x):
     return float(lib().or_atan2q(float(y), float(x)))
+
+
+def ompl_lvs(lo, hi, cdres):
+    """Longest valid segments of OMPL's R^3 and SO(3) components at fraction cdres."""
+    lo = np.ascontiguousarray(lo, dtype=np.float64)
+    hi = np.ascontiguousarray(hi, dtype=np.float64)
+    out = np.zeros(2)
+    lib().or_ompl_lvs(_p(lo, c_double_p), _p(hi, c_double_p), float(cdres), _p(out, c_double_p))
+    return out
+
+
+def ompl_motion_states(a, b, lo, hi, cdres):
+    """The OMPL-frame states OMPL's discrete motion validator checks on the motion
+    a -> b (b first, then interpolate(a, b, k / nd), k = 1 .. nd - 1)."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    lvs = ompl_lvs(lo, hi, cdres)
+    L = lib()
+    m = L.or_ompl_motion_states(_p(a, c_double_p), _p(b, c_double_p), _p(lvs, c_double_p), 0,
+                                _p(np.zeros(7), c_double_p))
+    out = np.zeros((m, 7))
+    L.or_ompl_motion_states(_p(a, c_double_p), _p(b, c_double_p), _p(lvs, c_double_p), m, _p(out, c_double_p))
+    return out

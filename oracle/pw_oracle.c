@@ -1205,3 +1205,85 @@ OR_EXPORT int64_t or_intersecting_segments(const or_world *w, const double q[7],
 	free(qq.pairs);
 	return m;
 }
+
+/* ------------------------------------------------------------------------ */
+/* OMPL's discrete motion check over OMPL.app's SE3StateSpace, the check    */
+/* behind OmplDriver::validateMotionPairs (lib/pyse3ompl/ompldriver.cc:     */
+/* 597-621, resolution set at :676-677).  OMPL is not vendored by the       */
+/* reference (a fork of OMPL 1.x); this restates its published algorithm:   */
+/* SpaceInformation::setStateValidityCheckingResolution sets each           */
+/* component's longest valid segment to extent * fraction (R^3 extent       */
+/* |hi - lo|, SO(3) extent pi/2); the compound validSegmentCount is the     */
+/* largest component count ceil(d / lvs) (R^3 Euclidean distance, SO(3) arc */
+/* length acos|<q1,q2>|, 0 above 1 - 1e-9); DiscreteMotionValidator checks  */
+/* s2 and interpolate(s1, s2, k / nd) for k = 1 .. nd - 1, not s1.          */
+/* OMPL states are (x, y, z, qx, qy, qz, qw).                               */
+/* ------------------------------------------------------------------------ */
+
+static double or_ompl_dot(const double *a, const double *b)
+{
+	return ((a[3] * b[3] + a[4] * b[4]) + a[5] * b[5]) + a[6] * b[6];
+}
+
+static double or_ompl_arc(double dq)
+{
+	const double a = fabs(dq);
+	return a > 1.0 - 1e-9 ? 0.0 : or_acos01(a);
+}
+
+/* Longest valid segments of R^3 and SO(3): out[0], out[1]. */
+OR_EXPORT void or_ompl_lvs(const double lo[3], const double hi[3], double cdres, double out[2])
+{
+	double e = 0.0;
+	for (int c = 0; c < 3; c++) {
+		const double d = hi[c] - lo[c];
+		e = e + d * d;
+	}
+	out[0] = sqrt(e) * cdres;
+	out[1] = OR_PIO2_HI * cdres;
+}
+
+/* The compound space's validSegmentCount(a, b). */
+OR_EXPORT int64_t or_ompl_segment_count(const double a[7], const double b[7], const double lvs[2])
+{
+	const double dx = a[0] - b[0], dy = a[1] - b[1], dz = a[2] - b[2];
+	const double dr = sqrt((dx * dx + dy * dy) + dz * dz);
+	const double ds = or_ompl_arc(or_ompl_dot(a, b));
+	const double nr = ceil(dr / lvs[0]), ns = ceil(ds / lvs[1]);
+	return (int64_t)(nr > ns ? nr : ns);
+}
+
+/* SE3StateSpace::interpolate: R^3 linear, SO(3) slerp with `from` kept below DBL_EPSILON. */
+OR_EXPORT void or_ompl_interpolate(const double a[7], const double b[7], double t, double out[7])
+{
+	for (int c = 0; c < 3; c++)
+		out[c] = a[c] + (b[c] - a[c]) * t;
+	const double dq = or_ompl_dot(a, b);
+	const double theta = or_ompl_arc(dq);
+	if (theta > 2.220446049250313080847e-16) {
+		const double d = 1.0 / or_sin(theta);
+		const double s0 = or_sin((1.0 - t) * theta);
+		double s1 = or_sin(t * theta);
+		if (dq < 0.0)
+			s1 = -s1;
+		for (int c = 3; c < 7; c++)
+			out[c] = (a[c] * s0 + b[c] * s1) * d;
+	} else {
+		for (int c = 3; c < 7; c++)
+			out[c] = a[c];
+	}
+}
+
+/* The states checkMotion(a, b) checks, b first, then k = 1 .. nd - 1; returns their
+ * number and writes at most cap of them. */
+OR_EXPORT int64_t or_ompl_motion_states(const double a[7], const double b[7], const double lvs[2], int64_t cap,
+                                        double *out)
+{
+	const int64_t nd = or_ompl_segment_count(a, b, lvs);
+	const int64_t m = nd >= 2 ? nd : 1;
+	for (int c = 0; c < 7 && cap > 0; c++)
+		out[c] = b[c];
+	for (int64_t k = 1; k < m && k < cap; k++)
+		or_ompl_interpolate(a, b, (double)k / (double)nd, out + 7 * k);
+	return m;
+}

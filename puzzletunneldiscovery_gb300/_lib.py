@@ -39,6 +39,7 @@ EXPORTS = (
     "pw_segments_contact_states", "pw_world_segments_contact_states", "pw_world_set_graph_mode",
     "pw_segments_reserve", "pw_world_set_launch_config",
     "pw_world_get_launch_config", "pw_expansion_crossings", "pw_world_scratch_epoch", "pw_expand_states",
+    "pw_ompl_check_motions", "pw_ompl_motion_states",
     # include/pw_mlp.h
     "pw_mlp_create", "pw_mlp_destroy", "pw_mlp_num_params", "pw_mlp_get_params", "pw_mlp_set_params",
     "pw_mlp_get_grads", "pw_mlp_predict", "pw_mlp_gradients", "pw_mlp_train_step", "pw_mlp_predict_mma",
@@ -124,6 +125,9 @@ def load():
         "pw_world_translate_ompl_to_unit": (ctypes.c_int, [vp, dp, i64, dp]),
         "pw_world_translate_unit_to_ompl": (ctypes.c_int, [vp, dp, i64, dp, ctypes.c_int]),
         "pw_world_last_stats": (ctypes.c_int, [vp, ctypes.POINTER(QueryStats)]),
+        "pw_ompl_check_motions": (ctypes.c_int, [vp, vp, vp, i64, dp, dp, ctypes.c_double, vp, i64p, vp]),
+        "pw_ompl_motion_states": (ctypes.c_int, [vp, vp, vp, i64, dp, dp, ctypes.c_double, i64, vp, vp, i64p,
+                                                 vp]),
         "pw_state_distance": (ctypes.c_int, [dp, dp, dp]),
         "pw_state_interpolate": (ctypes.c_int, [dp, dp, ctypes.c_double, dp]),
         "pw_segment_step_state": (ctypes.c_int, [dp, dp, ctypes.c_double, i64, dp, dp, i64p]),

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 LIB_NAME = "libpwcollide.so"
 LIB_PATH = os.path.join(HERE, LIB_NAME)
-SOURCES = ["pw_world.cu", "pw_query.cu", "pw_mlp.cu", "pw_touch.cu"]
+SOURCES = ["pw_world.cu", "pw_query.cu", "pw_mlp.cu", "pw_touch.cu", "pw_ompl.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

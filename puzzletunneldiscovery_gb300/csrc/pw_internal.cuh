@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "pw_collide.h"
+#include "pw_frames.cuh"
 
 // One mesh on the device.  Triangles and BVH leaves share "slot" order (the
 // Morton order of the build); FP64 data stays in the original face order.
@@ -138,4 +139,7 @@ int pw_cuda_fail(cudaError_t e, const char *what);
 	} while (0)
 
 int pw_build_mesh_device(pw_world *w, MeshDev &m, const std::vector<double> &V64, const std::vector<uint32_t> &F);
+
+// The frame conversions of a world (pw_world.cu).
+pwfr::Frame world_frame(const pw_world *w);
 void pw_free_mesh_device(pw_world *w);

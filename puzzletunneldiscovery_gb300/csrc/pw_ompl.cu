@@ -1,0 +1,317 @@
+// pw_ompl.cu -- OMPL's discrete motion check for batches of motions.
+//
+// pyse3ompl's OmplDriver::validateMotionPairs (lib/pyse3ompl/ompldriver.cc:597-621)
+// calls SpaceInformation::checkMotion once per pair, with OMPL.app's
+// SE3RigidBodyPlanning set up for discrete checking at the puzzle's collision
+// resolution (setStateValidityCheckingResolution(cdres), ompldriver.cc:676-677)
+// and the translation bounded by the puzzle's volume (:679-685).  OMPL is not
+// vendored by the reference (an un-vendored fork of OMPL 1.x); what this file
+// restates is OMPL's published algorithm:
+//   * SE3StateSpace is R^3 x SO(3), both weights 1.  R^3: Euclidean distance,
+//     maximum extent |hi - lo|.  SO(3): arc length acos|<q1, q2>| (0 when
+//     |<q1, q2>| > 1 - 1e-9), maximum extent pi / 2.
+//   * Each component's longest valid segment is its extent times cdres; the
+//     compound space's segment count is the largest component count,
+//     nd = max(ceil(d_R3 / lvs_R3), ceil(d_SO3 / lvs_SO3)).
+//   * DiscreteMotionValidator::checkMotion(s1, s2): s2 is valid and so is
+//     interpolate(s1, s2, k / nd) for k = 1 .. nd - 1.  s1 is assumed valid
+//     and not checked.  The order OMPL checks them in does not change the
+//     answer.
+//   * interpolate: R^3 from + (to - from) t; SO(3) from when the arc length is
+//     at most DBL_EPSILON, else (q1 s0 + q2 s1) / sin(theta) with
+//     s0 = sin((1 - t) theta), s1 = sin(t theta) negated when <q1, q2> < 0.
+// sin and acos are pw_math.cuh's own (a few ulp of libm's), so the states
+// generated here equal the oracle's bit for bit.  The validity of a state is
+// the engine's exact verdict after translateOMPLStateToUnitState
+// (unit_world.cc:689-711), as for validateStates.
+//
+// Layout: one motion's checked states are numbered j = 0 (s2) and j = k
+// (k = 1 .. nd - 1).  A scan of the per-motion counts numbers all states of a
+// batch; they are generated, converted to the unit frame and checked window
+// by window, and a failed state clears its motion's verdict.
+#include <cub/cub.cuh>
+
+#include <cfloat>
+#include <cmath>
+
+#include "pw_internal.cuh"
+#include "pw_math.cuh"
+
+namespace {
+
+constexpr double QUAT_NORM_ERROR = 1e-9;   // OMPL's MAX_QUATERNION_NORM_ERROR
+constexpr double MAX_SEGMENTS = 2147483647.0;
+constexpr int64_t WINDOW = int64_t(1) << 22;   // states generated and checked per pass
+
+struct OmplSpace {
+	double lvs_r3, lvs_so3;   // longest valid segments of the two components
+};
+
+// Raw dot product of the two rotations, in OMPL's storage order (x, y, z, w).
+__device__ __forceinline__ double quat_dot(const double *a, const double *b)
+{
+	using namespace pwm;
+	return add(add(add(mul(a[3], b[3]), mul(a[4], b[4])), mul(a[5], b[5])), mul(a[6], b[6]));
+}
+
+__device__ __forceinline__ double arc_length(double dq)
+{
+	const double a = pwm::dabs(dq);
+	return a > 1.0 - QUAT_NORM_ERROR ? 0.0 : pwm::acos01(a);
+}
+
+__device__ __forceinline__ bool finite7(const double *q)
+{
+	bool ok = true;
+	for (int c = 0; c < 7; c++)
+		ok = ok && isfinite(q[c]);
+	return ok;
+}
+
+// Per motion: how many states checkMotion checks (1, or nd when nd >= 2), and
+// the verdict's starting value (0 for a motion with a non-finite component).
+__global__ void k_ompl_counts(const double *from, const double *to, int64_t n, OmplSpace S, int64_t *count,
+                              uint8_t *valid, int *too_long)
+{
+	const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+	if (i >= n)
+		return;
+	using namespace pwm;
+	const double *a = from + 7 * i, *b = to + 7 * i;
+	if (!finite7(a) || !finite7(b)) {
+		count[i] = 1;
+		valid[i] = 0;
+		return;
+	}
+	const double dx = sub(a[0], b[0]), dy = sub(a[1], b[1]), dz = sub(a[2], b[2]);
+	const double dr = rt(add(add(mul(dx, dx), mul(dy, dy)), mul(dz, dz)));
+	const double ds = arc_length(quat_dot(a, b));
+	const double nr = ceil(dvd(dr, S.lvs_r3)), ns = ceil(dvd(ds, S.lvs_so3));
+	const double nd = nr > ns ? nr : ns;
+	if (nd > MAX_SEGMENTS) {
+		atomicOr(too_long, 1);
+		count[i] = 1;
+		valid[i] = 0;
+		return;
+	}
+	count[i] = nd >= 2.0 ? (int64_t)nd : 1;
+	valid[i] = 1;
+}
+
+// The motion that global state g belongs to: offs[i] <= g < offs[i + 1].
+__device__ __forceinline__ int64_t owner(const int64_t *offs, int64_t n, int64_t g)
+{
+	int64_t lo = 0, hi = n - 1;
+	while (lo < hi) {
+		const int64_t mid = (lo + hi + 1) >> 1;
+		if (offs[mid] <= g)
+			lo = mid;
+		else
+			hi = mid - 1;
+	}
+	return lo;
+}
+
+// OMPL's SE3 interpolate(a, b, t), OMPL states (x, y, z, qx, qy, qz, qw).
+__device__ __forceinline__ void ompl_interpolate(const double *a, const double *b, double t, double *o)
+{
+	using namespace pwm;
+	for (int c = 0; c < 3; c++)
+		o[c] = add(a[c], mul(sub(b[c], a[c]), t));
+	const double dq = quat_dot(a, b);
+	const double theta = arc_length(dq);
+	if (theta > DBL_EPSILON) {
+		const double d = dvd(1.0, sin_q(theta));
+		const double s0 = sin_q(mul(sub(1.0, t), theta));
+		double s1 = sin_q(mul(t, theta));
+		if (dq < 0.0)
+			s1 = -s1;
+		for (int c = 3; c < 7; c++)
+			o[c] = mul(add(mul(a[c], s0), mul(b[c], s1)), d);
+	} else {
+		for (int c = 3; c < 7; c++)
+			o[c] = a[c];
+	}
+}
+
+// Checked states [first, first + cnt) of the batch, in the unit frame.
+__global__ void k_ompl_states(const double *from, const double *to, int64_t n, const int64_t *offs, int64_t first,
+                              int64_t cnt, pwfr::Frame F, double *out)
+{
+	for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < cnt; k += (int64_t)gridDim.x * blockDim.x) {
+		const int64_t g = first + k;
+		const int64_t i = owner(offs, n, g);
+		const int64_t j = g - offs[i];
+		const double *a = from + 7 * i, *b = to + 7 * i;
+		double s[7];
+		if (j == 0) {
+			for (int c = 0; c < 7; c++)
+				s[c] = b[c];
+		} else {
+			const double nd = (double)(offs[i + 1] - offs[i]);
+			ompl_interpolate(a, b, pwm::dvd((double)j, nd), s);
+		}
+		pwfr::ompl_to_unit(F, s, out + 7 * k);
+	}
+}
+
+// A state that collides clears its motion's verdict.
+__global__ void k_ompl_reduce(const uint8_t *state_ok, int64_t first, int64_t cnt, const int64_t *offs, int64_t n,
+                              uint8_t *valid)
+{
+	for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < cnt; k += (int64_t)gridDim.x * blockDim.x)
+		if (!state_ok[k])
+			valid[owner(offs, n, first + k)] = 0;
+}
+
+// The R^3 extent and both longest valid segments, with OMPL's own argument checks
+// (RealVectorBounds::check, StateSpace::setLongestValidSegmentFraction, setup).
+int ompl_space(const double lo[3], const double hi[3], double cdres, OmplSpace &S, const char *who)
+{
+	if (!lo || !hi)
+		return pw_fail(PW_ERR_INVALID_ARG, std::string(who) + ": bounds are NULL");
+	if (!(cdres >= DBL_EPSILON && cdres <= 1.0 - DBL_EPSILON))
+		return pw_fail(PW_ERR_INVALID_ARG, std::string(who) + ": the resolution must lie in (0, 1)");
+	double e = 0.0;
+	for (int c = 0; c < 3; c++) {
+		if (!(std::isfinite(lo[c]) && std::isfinite(hi[c]) && lo[c] <= hi[c]))
+			return pw_fail(PW_ERR_INVALID_ARG, std::string(who) + ": bounds must be finite with lo <= hi");
+		const double d = hi[c] - lo[c];
+		e = e + d * d;
+	}
+	S.lvs_r3 = std::sqrt(e) * cdres;
+	S.lvs_so3 = pwm::PIO2_HI * cdres;
+	if (!(S.lvs_r3 >= DBL_EPSILON))
+		return pw_fail(PW_ERR_INVALID_ARG, std::string(who) + ": the bounds have no extent");
+	return PW_OK;
+}
+
+int blocks_for(const pw_world *w, int64_t cnt)
+{
+	const int64_t want = (cnt + 255) / 256;
+	const int64_t cap = (int64_t)(w->num_sms > 0 ? w->num_sms : 1) * 16;
+	return (int)(want < cap ? (want > 0 ? want : 1) : cap);
+}
+
+// Counts, their scan and the batch's total, on the caller's stream.
+int ompl_prepare(pw_world *w, const double *from, const double *to, int64_t n, const OmplSpace &S, cudaStream_t st,
+                 DeviceBuffer &cnt_buf, DeviceBuffer &off_buf, DeviceBuffer &tmp_buf, DeviceBuffer &flag_buf,
+                 uint8_t *valid, int64_t *total, const char *who)
+{
+	PW_CUDA(cnt_buf.reserve(sizeof(int64_t) * (size_t)n));
+	PW_CUDA(off_buf.reserve(sizeof(int64_t) * (size_t)(n + 1)));
+	PW_CUDA(flag_buf.reserve(sizeof(int)));
+	int64_t *cnt = (int64_t *)cnt_buf.ptr, *offs = (int64_t *)off_buf.ptr;
+	int *flag = (int *)flag_buf.ptr;
+	PW_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
+	PW_CUDA(cudaMemsetAsync(offs, 0, sizeof(int64_t), st));
+	k_ompl_counts<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(from, to, n, S, cnt, valid, flag);
+	size_t tmp_bytes = 0;
+	PW_CUDA(cub::DeviceScan::InclusiveSum(nullptr, tmp_bytes, cnt, offs + 1, n, st));
+	PW_CUDA(tmp_buf.reserve(tmp_bytes > 0 ? tmp_bytes : 1));
+	PW_CUDA(cub::DeviceScan::InclusiveSum(tmp_buf.ptr, tmp_bytes, cnt, offs + 1, n, st));
+	int too_long = 0;
+	PW_CUDA(cudaMemcpyAsync(total, offs + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+	PW_CUDA(cudaMemcpyAsync(&too_long, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+	PW_CUDA(cudaStreamSynchronize(st));
+	if (too_long)
+		return pw_fail(PW_ERR_INVALID_ARG, std::string(who) + ": a motion needs more than 2^31 - 1 segments");
+	return PW_OK;
+}
+
+int check_motion_args(pw_world *w, const double *from, const double *to, int64_t n, const void *out,
+                      const char *who)
+{
+	if (!w)
+		return pw_fail(PW_ERR_INVALID_ARG, std::string(who) + ": world is NULL");
+	if (!w->ready)
+		return pw_fail(PW_ERR_NO_MODEL, std::string(who) + ": world not ready");
+	if (n < 0 || (n > 0 && (!from || !to || !out)))
+		return pw_fail(PW_ERR_INVALID_ARG, std::string(who) + ": bad pointers or size");
+	return PW_OK;
+}
+
+} // namespace
+
+extern "C" int pw_ompl_check_motions(pw_world *w, const double *from, const double *to, int64_t n,
+                                     const double lo[3], const double hi[3], double cdres, uint8_t *valid,
+                                     int64_t *states_checked, void *stream)
+{
+	PW_TRACE("pw_ompl_check_motions");
+	const char *who = "pw_ompl_check_motions";
+	int rc = check_motion_args(w, from, to, n, valid, who);
+	if (rc)
+		return rc;
+	OmplSpace S;
+	if ((rc = ompl_space(lo, hi, cdres, S, who)))
+		return rc;
+	if (states_checked)
+		*states_checked = 0;
+	if (n == 0)
+		return PW_OK;
+	PW_CUDA(cudaSetDevice(w->device));
+	cudaStream_t st = (cudaStream_t)stream;
+	DeviceBuffer cnt_buf, off_buf, tmp_buf, flag_buf, state_buf, ok_buf;
+	int64_t total = 0;
+	if ((rc = ompl_prepare(w, from, to, n, S, st, cnt_buf, off_buf, tmp_buf, flag_buf, valid, &total, who)))
+		return rc;
+	const int64_t win = total < WINDOW ? total : WINDOW;
+	PW_CUDA(state_buf.reserve(sizeof(double) * 7 * (size_t)win));
+	PW_CUDA(ok_buf.reserve((size_t)win));
+	const int64_t *offs = (const int64_t *)off_buf.ptr;
+	double *states = (double *)state_buf.ptr;
+	uint8_t *ok = (uint8_t *)ok_buf.ptr;
+	const pwfr::Frame F = world_frame(w);
+	for (int64_t first = 0; first < total; first += win) {
+		const int64_t cnt = total - first < win ? total - first : win;
+		k_ompl_states<<<blocks_for(w, cnt), 256, 0, st>>>(from, to, n, offs, first, cnt, F, states);
+		PW_CUDA(cudaGetLastError());
+		if ((rc = pw_states_valid(w, states, cnt, ok, stream)))
+			return rc;
+		k_ompl_reduce<<<blocks_for(w, cnt), 256, 0, st>>>(ok, first, cnt, offs, n, valid);
+		PW_CUDA(cudaGetLastError());
+	}
+	// the scratch is freed on return: the batch's work must be done by then
+	PW_CUDA(cudaStreamSynchronize(st));
+	if (states_checked)
+		*states_checked = total;
+	return PW_OK;
+}
+
+extern "C" int pw_ompl_motion_states(pw_world *w, const double *from, const double *to, int64_t n,
+                                     const double lo[3], const double hi[3], double cdres, int64_t capacity,
+                                     double *states, int64_t *offsets, int64_t *total, void *stream)
+{
+	PW_TRACE("pw_ompl_motion_states");
+	const char *who = "pw_ompl_motion_states";
+	int rc = check_motion_args(w, from, to, n, states, who);
+	if (rc)
+		return rc;
+	if (!total || capacity < 0)
+		return pw_fail(PW_ERR_INVALID_ARG, std::string(who) + ": bad capacity or total");
+	OmplSpace S;
+	if ((rc = ompl_space(lo, hi, cdres, S, who)))
+		return rc;
+	*total = 0;
+	if (n == 0)
+		return PW_OK;
+	PW_CUDA(cudaSetDevice(w->device));
+	cudaStream_t st = (cudaStream_t)stream;
+	DeviceBuffer cnt_buf, off_buf, tmp_buf, flag_buf, valid_buf;
+	PW_CUDA(valid_buf.reserve((size_t)n));
+	if ((rc = ompl_prepare(w, from, to, n, S, st, cnt_buf, off_buf, tmp_buf, flag_buf, (uint8_t *)valid_buf.ptr,
+	                       total, who)))
+		return rc;
+	if (offsets)
+		PW_CUDA(cudaMemcpyAsync(offsets, off_buf.ptr, sizeof(int64_t) * (size_t)(n + 1), cudaMemcpyDeviceToDevice,
+		                        st));
+	if (*total > capacity) {
+		PW_CUDA(cudaStreamSynchronize(st));
+		return pw_fail(PW_ERR_CAPACITY, std::string(who) + ": more states than the capacity");
+	}
+	k_ompl_states<<<blocks_for(w, *total), 256, 0, st>>>(from, to, n, (const int64_t *)off_buf.ptr, 0, *total,
+	                                                    world_frame(w), states);
+	PW_CUDA(cudaGetLastError());
+	PW_CUDA(cudaStreamSynchronize(st));
+	return PW_OK;
+}

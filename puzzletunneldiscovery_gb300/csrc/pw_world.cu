@@ -361,84 +361,14 @@ extern "C" int pw_world_cd_faces(const pw_world *w, int geo, int32_t *out)
 
 // ------------------------------------------------------------------ frames
 
-// Hamilton product a * b, quaternions (w, x, y, z).
-static void quat_mul(const double *a, const double *b, double *o)
+// The conversions of one world, in the shared host / device form.
+pwfr::Frame world_frame(const pw_world *w)
 {
-	using namespace pwm;
-	o[0] = sub(sub(sub(mul(a[0], b[0]), mul(a[1], b[1])), mul(a[2], b[2])), mul(a[3], b[3]));
-	o[1] = sub(add(add(mul(a[0], b[1]), mul(a[1], b[0])), mul(a[2], b[3])), mul(a[3], b[2]));
-	o[2] = add(add(sub(mul(a[0], b[2]), mul(a[1], b[3])), mul(a[2], b[0])), mul(a[3], b[1]));
-	o[3] = add(sub(add(mul(a[0], b[3]), mul(a[1], b[2])), mul(a[2], b[1])), mul(a[3], b[0]));
-}
-
-static void mat_vec(const double *R, const double *v, double *o)
-{
-	for (int i = 0; i < 3; i++)
-		o[i] = pwm::add(pwm::add(pwm::mul(R[3 * i], v[0]), pwm::mul(R[3 * i + 1], v[1])), pwm::mul(R[3 * i + 2], v[2]));
-}
-
-// decompose (osr_state.cc:85-92): translation and normalised rotation.
-static void decompose(const double *q, double *t, double *rot)
-{
-	t[0] = q[0]; t[1] = q[1]; t[2] = q[2];
-	const double r[4] = { q[3], q[4], q[5], q[6] };
-	pwm::quat_normalize(r, rot);
-}
-
-// compose (osr_state.cc:107-119): the rotation is normalised again.
-static void compose(const double *t, const double *rot, double *q)
-{
-	double r[4];
-	pwm::quat_normalize(rot, r);
-	q[0] = t[0]; q[1] = t[1]; q[2] = t[2];
-	q[3] = r[0]; q[4] = r[1]; q[5] = r[2]; q[6] = r[3];
-}
-
-// applyPertubation (unit_world.cc:713-724).
-static void apply_pert(const pw_world *w, const double *in, double *out)
-{
-	double t[3], rot[4], pt[3], prot[4], qret[4], R[9], Rt[3], tret[3];
-	decompose(in, t, rot);
-	decompose(w->pert, pt, prot);
-	quat_mul(prot, rot, qret);
-	pwm::quat_to_matrix(prot, R);
-	mat_vec(R, t, Rt);
-	for (int c = 0; c < 3; c++) tret[c] = pwm::add(pt[c], Rt[c]);
-	compose(tret, qret, out);
-}
-
-// unapplyPertubation (unit_world.cc:726-737).
-static void unapply_pert(const pw_world *w, const double *in, double *out)
-{
-	double t[3], rot[4], pt[3], prot[4], inv[4], R[9], d[3], tret[3], qret[4];
-	decompose(in, t, rot);
-	decompose(w->pert, pt, prot);
-	const double n2 = pwm::add(pwm::add(pwm::add(pwm::mul(prot[1], prot[1]), pwm::mul(prot[2], prot[2])),
-	                                    pwm::mul(prot[3], prot[3])), pwm::mul(prot[0], prot[0]));
-	inv[0] = prot[0] / n2; inv[1] = -prot[1] / n2; inv[2] = -prot[2] / n2; inv[3] = -prot[3] / n2;
-	pwm::quat_to_matrix(inv, R);
-	for (int c = 0; c < 3; c++) d[c] = pwm::add(-pt[c], t[c]);
-	mat_vec(R, d, tret);
-	quat_mul(inv, rot, qret);
-	compose(tret, qret, out);
-}
-
-static void to_unit(const pw_world *w, const double *in, double *out)
-{
-	double tmp[7];
-	const double s = (double)w->scale;
-	for (int c = 0; c < 3; c++) tmp[c] = pwm::mul(s, in[c]);
-	for (int c = 3; c < 7; c++) tmp[c] = in[c];
-	apply_pert(w, tmp, out);
-}
-
-static void from_unit(const pw_world *w, const double *in, double *out)
-{
-	double tmp[7];
-	unapply_pert(w, in, tmp);
-	const double inv = 1.0 / (double)w->scale;
-	for (int c = 0; c < 3; c++) out[c] = pwm::mul(inv, tmp[c]);
-	for (int c = 3; c < 7; c++) out[c] = tmp[c];
+	pwfr::Frame F;
+	F.scale = (double)w->scale;
+	for (int c = 0; c < 7; c++) F.pert[c] = w->pert[c];
+	for (int c = 0; c < 3; c++) F.dc[c] = (double)(w->ompl_center[c] - w->center[c]) * (double)w->scale;
+	return F;
 }
 
 static int check_conv(const pw_world *w, const double *in, int64_t n, const double *out, const char *who)
@@ -454,8 +384,9 @@ extern "C" int pw_world_translate_to_unit(const pw_world *w, const double *in, i
 {
 	int rc = check_conv(w, in, n, out, "pw_world_translate_to_unit");
 	if (rc) return rc;
+	const pwfr::Frame F = world_frame(w);
 	for (int64_t i = 0; i < n; i++)
-		to_unit(w, in + 7 * i, out + 7 * i);
+		pwfr::to_unit(F, in + 7 * i, out + 7 * i);
 	return PW_OK;
 }
 
@@ -463,8 +394,9 @@ extern "C" int pw_world_translate_from_unit(const pw_world *w, const double *in,
 {
 	int rc = check_conv(w, in, n, out, "pw_world_translate_from_unit");
 	if (rc) return rc;
+	const pwfr::Frame F = world_frame(w);
 	for (int64_t i = 0; i < n; i++)
-		from_unit(w, in + 7 * i, out + 7 * i);
+		pwfr::from_unit(F, in + 7 * i, out + 7 * i);
 	return PW_OK;
 }
 
@@ -474,20 +406,9 @@ extern "C" int pw_world_translate_ompl_to_unit(const pw_world *w, const double *
 {
 	int rc = check_conv(w, in, n, out, "pw_world_translate_ompl_to_unit");
 	if (rc) return rc;
-	double dc[3];
-	for (int c = 0; c < 3; c++)
-		dc[c] = (double)(w->ompl_center[c] - w->center[c]) * (double)w->scale;
-	for (int64_t i = 0; i < n; i++) {
-		const double *p = in + 7 * i;
-		const double wf[7] = { p[0], p[1], p[2], p[6], p[3], p[4], p[5] };
-		double u[7], t[3], rot[4], R[9], Rd[3], t2[3];
-		to_unit(w, wf, u);
-		decompose(u, t, rot);
-		pwm::quat_to_matrix(rot, R);
-		mat_vec(R, dc, Rd);
-		for (int c = 0; c < 3; c++) t2[c] = pwm::sub(t[c], Rd[c]);
-		compose(t2, rot, out + 7 * i);
-	}
+	const pwfr::Frame F = world_frame(w);
+	for (int64_t i = 0; i < n; i++)
+		pwfr::ompl_to_unit(F, in + 7 * i, out + 7 * i);
 	return PW_OK;
 }
 
@@ -497,17 +418,15 @@ extern "C" int pw_world_translate_unit_to_ompl(const pw_world *w, const double *
 {
 	int rc = check_conv(w, in, n, out, "pw_world_translate_unit_to_ompl");
 	if (rc) return rc;
-	double dc[3];
-	for (int c = 0; c < 3; c++)
-		dc[c] = (double)(w->ompl_center[c] - w->center[c]) * (double)w->scale;
+	const pwfr::Frame F = world_frame(w);
 	for (int64_t i = 0; i < n; i++) {
 		double t[3], rot[4], R[9], Rd[3], t2[3], c7[7], o[7];
-		decompose(in + 7 * i, t, rot);
+		pwfr::decompose(in + 7 * i, t, rot);
 		pwm::quat_to_matrix(rot, R);
-		mat_vec(R, dc, Rd);
+		pwfr::mat_vec(R, F.dc, Rd);
 		for (int c = 0; c < 3; c++) t2[c] = pwm::add(t[c], Rd[c]);
-		compose(t2, rot, c7);
-		from_unit(w, c7, o);
+		pwfr::compose(t2, rot, c7);
+		pwfr::from_unit(F, c7, o);
 		double *dst = out + 7 * i;
 		dst[0] = o[0]; dst[1] = o[1]; dst[2] = o[2];
 		if (to_angle_axis) {

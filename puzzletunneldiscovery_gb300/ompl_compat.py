@@ -20,8 +20,18 @@ call on a world set up for the same puzzle:
   contacts thinner than a step of either rule.
 
 Both return int32 vectors with 1 = valid, as the reference does.
+
+``OmplDriver`` is the validation half of pyse3ompl's driver with OMPL's own
+motion rule: ``set_bb`` / ``set_cdres`` (ompldriver.h:108-116) give the state
+space's translation bounds and collision resolution, and
+``validate_motion_pairs`` checks each motion as OMPL's discrete motion
+validator does (``pw_ompl_check_motions``: the target state and the states
+k / nd along OMPL's SE(3) interpolation, nd from the resolution times each
+component's extent), all motions of a batch in one call.
 """
 from __future__ import annotations
+
+import ctypes
 
 import numpy as np
 import torch
@@ -60,3 +70,92 @@ def validate_motion_pairs(uw: UnitWorld, qs0, qs1, verify_delta: float = 0.001) 
     steps = uw.first_contact_steps(ua, ub, verify_delta, _lib.PW_SEG_TRANSITION).cpu().numpy()
     out[:m] = (steps == _lib.PW_STEP_FREE).astype(np.int32)
     return out
+
+
+def _bb(lo, hi):
+    lo = np.ascontiguousarray(np.asarray(lo, dtype=np.float64).reshape(-1))
+    hi = np.ascontiguousarray(np.asarray(hi, dtype=np.float64).reshape(-1))
+    if lo.shape != (3,) or hi.shape != (3,):
+        raise ValueError("bounds must have 3 entries each")
+    return lo, hi
+
+
+def _motion_args(uw: UnitWorld, qs0, qs1):
+    a, b = _ompl_states(qs0), _ompl_states(qs1)
+    m = min(a.shape[0], b.shape[0])
+    ta = torch.from_numpy(a[:m]).to(uw._device)
+    tb = torch.from_numpy(b[:m]).to(uw._device)
+    return a.shape[0], m, ta, tb
+
+
+def check_motions_discrete(uw: UnitWorld, qs0, qs1, lo, hi, cdres: float):
+    """OMPL's discrete motion check of aligned OMPL-frame motions qs0[i] -> qs1[i]
+    in an SE(3) space bounded by lo / hi at collision resolution cdres.  Returns
+    (int32 verdicts, 1 = the motion is valid, rows beyond the shorter batch 0;
+    the number of states checked)."""
+    lo, hi = _bb(lo, hi)
+    n, m, ta, tb = _motion_args(uw, qs0, qs1)
+    out = np.zeros(n, dtype=np.int32)
+    if m == 0:
+        return out, 0
+    valid = torch.empty(m, dtype=torch.uint8, device=uw._device)
+    checked = ctypes.c_int64()
+    dp = ctypes.POINTER(ctypes.c_double)
+    _lib.check(uw._L.pw_ompl_check_motions(uw._h, ta.data_ptr(), tb.data_ptr(), m, lo.ctypes.data_as(dp),
+                                           hi.ctypes.data_as(dp), float(cdres), valid.data_ptr(),
+                                           ctypes.byref(checked), torch.cuda.current_stream(uw._device).cuda_stream),
+               "check_motions_discrete")
+    out[:m] = valid.cpu().numpy()
+    return out, int(checked.value)
+
+
+def motion_states(uw: UnitWorld, qs0, qs1, lo, hi, cdres: float):
+    """The unit-frame states check_motions_discrete checks: (states [T, 7] on the
+    device, offsets [m + 1]); motion i's rows are offsets[i] .. offsets[i + 1] - 1,
+    its target first."""
+    lo, hi = _bb(lo, hi)
+    _, m, ta, tb = _motion_args(uw, qs0, qs1)
+    dev = uw._device
+    offs = torch.zeros(m + 1, dtype=torch.int64, device=dev)
+    if m == 0:
+        return torch.zeros((0, 7), dtype=torch.float64, device=dev), offs
+    dp = ctypes.POINTER(ctypes.c_double)
+    total = ctypes.c_int64()
+    args = (uw._h, ta.data_ptr(), tb.data_ptr(), m, lo.ctypes.data_as(dp), hi.ctypes.data_as(dp), float(cdres))
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    dummy = torch.zeros((1, 7), dtype=torch.float64, device=dev)
+    rc = uw._L.pw_ompl_motion_states(*args, 0, dummy.data_ptr(), offs.data_ptr(), ctypes.byref(total), stream)
+    if rc not in (_lib.PW_OK, _lib.PW_ERR_CAPACITY):
+        _lib.check(rc, "motion_states")
+    states = torch.empty((max(int(total.value), 1), 7), dtype=torch.float64, device=dev)
+    _lib.check(uw._L.pw_ompl_motion_states(*args, int(total.value), states.data_ptr(), offs.data_ptr(),
+                                           ctypes.byref(total), stream), "motion_states")
+    return states[:int(total.value)], offs
+
+
+class OmplDriver:
+    """The validation calls of pyse3ompl's OmplDriver (ompldriver.h:108-116,
+    ompldriver.cc:566-621) on a UnitWorld loaded with the same puzzle's meshes:
+    set_bb, set_cdres, validate_states and validate_motion_pairs, the last with
+    OMPL's discrete motion rule."""
+
+    def __init__(self, uw: UnitWorld):
+        self.uw = uw
+        self.lo = self.hi = None
+        self.cdres = None
+        self.last_states_checked = 0
+
+    def set_bb(self, mins, maxs) -> None:
+        self.lo, self.hi = _bb(mins, maxs)
+
+    def set_cdres(self, cdres: float) -> None:
+        self.cdres = float(cdres)
+
+    def validate_states(self, qs0) -> np.ndarray:
+        return validate_states(self.uw, qs0)
+
+    def validate_motion_pairs(self, qs0, qs1) -> np.ndarray:
+        if self.lo is None or self.cdres is None:
+            raise RuntimeError("validate_motion_pairs needs set_bb and set_cdres first")
+        out, self.last_states_checked = check_motions_discrete(self.uw, qs0, qs1, self.lo, self.hi, self.cdres)
+        return out

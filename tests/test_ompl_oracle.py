@@ -1,0 +1,89 @@
+"""The oracle's restatement of OMPL's discrete motion check (OMPL 1.x, un-vendored
+by the reference; the check behind OmplDriver::validateMotionPairs,
+lib/pyse3ompl/ompldriver.cc:597-621) against closed forms: the segment count of
+pure translations and pure rotations, and the interpolated states of a rotation
+about one axis.  No device needed."""
+import math
+
+import numpy as np
+import pytest
+
+
+def _rot_z(phi, t=(0.0, 0.0, 0.0)):
+    # OMPL state (x, y, z, qx, qy, qz, qw) of a rotation by phi about z
+    return np.array([t[0], t[1], t[2], 0.0, 0.0, math.sin(phi / 2), math.cos(phi / 2)])
+
+
+def test_segment_lengths(oracle_mod):
+    O = oracle_mod
+    lvs = O.ompl_lvs([-1, -2, -3], [1, 2, 3], 0.01)
+    assert lvs[0] == pytest.approx(math.sqrt(4 + 16 + 36) * 0.01, rel=1e-15)
+    assert lvs[1] == pytest.approx(math.pi / 2 * 0.01, rel=1e-15)
+
+
+@pytest.mark.parametrize("length,cdres", [(0.5, 0.01), (1.0, 0.003), (3.7, 0.05), (0.0, 0.01)])
+def test_translation_counts(oracle_mod, length, cdres):
+    O = oracle_mod
+    lo, hi = [-1, -1, -1], [1, 1, 1]
+    a = _rot_z(0.0)
+    b = _rot_z(0.0, (length, 0.0, 0.0))
+    s = O.ompl_motion_states(a, b, lo, hi, cdres)
+    nd = math.ceil(length / (math.sqrt(12.0) * cdres))
+    assert s.shape[0] == max(nd, 1)
+    assert np.array_equal(s[0], b)
+    if nd >= 2:
+        xs = s[1:, 0]
+        want = np.arange(1, nd) / nd * length
+        assert np.allclose(xs, want, rtol=0, atol=1e-15)
+        # rotations untouched: the arc length is 0, OMPL copies `from`
+        assert (s[1:, 3:] == a[3:]).all()
+
+
+@pytest.mark.parametrize("phi,cdres", [(0.3, 0.01), (2.5, 0.02), (math.pi * 0.99, 0.1)])
+def test_rotation_counts_and_slerp(oracle_mod, phi, cdres):
+    O = oracle_mod
+    a, b = _rot_z(0.0), _rot_z(phi)
+    s = O.ompl_motion_states(a, b, [-1, -1, -1], [1, 1, 1], cdres)
+    # SO(3) arc length of OMPL is acos|<q1, q2>| = phi / 2
+    nd = math.ceil((phi / 2) / (math.pi / 2 * cdres))
+    assert s.shape[0] == max(nd, 1)
+    for k in range(1, nd):
+        want = _rot_z(phi * k / nd)
+        assert np.allclose(s[k], want, rtol=0, atol=1e-13), k
+
+
+def test_long_way_round_takes_the_short_arc(oracle_mod):
+    """q and -q are the same rotation: OMPL's slerp negates s1 for a negative dot,
+    so a motion to -q(phi) rotates by phi, not by 2 pi - phi."""
+    O = oracle_mod
+    a, b = _rot_z(0.0), _rot_z(1.0)
+    b[3:] = -b[3:]
+    s = O.ompl_motion_states(a, b, [-1, -1, -1], [1, 1, 1], 0.05)
+    nd = s.shape[0]
+    assert nd == math.ceil(0.5 / (math.pi / 2 * 0.05))
+    mid = s[nd // 2]
+    angle = 2 * math.atan2(abs(mid[5]), abs(mid[6]))
+    assert angle == pytest.approx(1.0 * (nd // 2) / nd, abs=1e-12)
+
+
+def test_nearly_identical_rotations_are_not_interpolated(oracle_mod):
+    """Above |<q1, q2>| > 1 - 1e-9 OMPL's arc length is 0 and interpolate copies
+    the start rotation."""
+    O = oracle_mod
+    a = _rot_z(0.0)
+    b = _rot_z(1e-5, (0.5, 0.0, 0.0))
+    s = O.ompl_motion_states(a, b, [-1, -1, -1], [1, 1, 1], 0.01)
+    assert s.shape[0] == math.ceil(0.5 / (math.sqrt(12.0) * 0.01))
+    assert (s[1:, 3:] == a[3:]).all()
+
+
+def test_count_is_symmetric(oracle_mod):
+    O = oracle_mod
+    rng = np.random.default_rng(7)
+    lo, hi = [-5, -5, -5], [5, 5, 5]
+    for _ in range(200):
+        a = np.concatenate([rng.uniform(-5, 5, 3), rng.normal(size=4)])
+        b = np.concatenate([rng.uniform(-5, 5, 3), rng.normal(size=4)])
+        a[3:] /= np.linalg.norm(a[3:])
+        b[3:] /= np.linalg.norm(b[3:])
+        assert O.ompl_motion_states(a, b, lo, hi, 0.01).shape[0] == O.ompl_motion_states(b, a, lo, hi, 0.01).shape[0]
