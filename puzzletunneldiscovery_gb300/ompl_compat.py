@@ -88,6 +88,26 @@ def _motion_args(uw: UnitWorld, qs0, qs1):
     return a.shape[0], m, ta, tb
 
 
+def _stream_of(device):
+    d = torch.device(device)
+    return torch.cuda.current_stream(d).cuda_stream if d.type == "cuda" else None
+
+
+def _check_motions_dev(uw: UnitWorld, ta: torch.Tensor, tb: torch.Tensor, lo: np.ndarray, hi: np.ndarray,
+                       cdres: float):
+    """pw_ompl_check_motions on [m, 7] float64 OMPL-frame batches already on the
+    world's device: (uint8 verdicts [m] on the device, states checked)."""
+    m = ta.shape[0]
+    valid = torch.empty(m, dtype=torch.uint8, device=ta.device)
+    checked = ctypes.c_int64()
+    dp = ctypes.POINTER(ctypes.c_double)
+    _lib.check(uw._L.pw_ompl_check_motions(uw._h, ta.data_ptr(), tb.data_ptr(), m, lo.ctypes.data_as(dp),
+                                           hi.ctypes.data_as(dp), float(cdres), valid.data_ptr(),
+                                           ctypes.pointer(checked), _stream_of(ta.device)),
+               "check_motions_discrete")
+    return valid, int(checked.value)
+
+
 def check_motions_discrete(uw: UnitWorld, qs0, qs1, lo, hi, cdres: float):
     """OMPL's discrete motion check of aligned OMPL-frame motions qs0[i] -> qs1[i]
     in an SE(3) space bounded by lo / hi at collision resolution cdres.  Returns
@@ -98,15 +118,9 @@ def check_motions_discrete(uw: UnitWorld, qs0, qs1, lo, hi, cdres: float):
     out = np.zeros(n, dtype=np.int32)
     if m == 0:
         return out, 0
-    valid = torch.empty(m, dtype=torch.uint8, device=uw._device)
-    checked = ctypes.c_int64()
-    dp = ctypes.POINTER(ctypes.c_double)
-    _lib.check(uw._L.pw_ompl_check_motions(uw._h, ta.data_ptr(), tb.data_ptr(), m, lo.ctypes.data_as(dp),
-                                           hi.ctypes.data_as(dp), float(cdres), valid.data_ptr(),
-                                           ctypes.byref(checked), torch.cuda.current_stream(uw._device).cuda_stream),
-               "check_motions_discrete")
+    valid, checked = _check_motions_dev(uw, ta, tb, lo, hi, cdres)
     out[:m] = valid.cpu().numpy()
-    return out, int(checked.value)
+    return out, checked
 
 
 def motion_states(uw: UnitWorld, qs0, qs1, lo, hi, cdres: float):
@@ -154,8 +168,25 @@ class OmplDriver:
     def validate_states(self, qs0) -> np.ndarray:
         return validate_states(self.uw, qs0)
 
-    def validate_motion_pairs(self, qs0, qs1) -> np.ndarray:
+    def _ready(self, what: str) -> None:
         if self.lo is None or self.cdres is None:
-            raise RuntimeError("validate_motion_pairs needs set_bb and set_cdres first")
+            raise RuntimeError("%s needs set_bb and set_cdres first" % what)
+
+    def validate_motion_pairs(self, qs0, qs1) -> np.ndarray:
+        self._ready("validate_motion_pairs")
         out, self.last_states_checked = check_motions_discrete(self.uw, qs0, qs1, self.lo, self.hi, self.cdres)
         return out
+
+    def check_pairs(self, keys: torch.Tensor, from_idx: torch.Tensor, to_idx: torch.Tensor) -> torch.Tensor:
+        """validate_motion_pairs(keys[from_idx], keys[to_idx]) with the keys and
+        the indices already on the device: a bool tensor, no host round trip."""
+        self._ready("check_pairs")
+        if from_idx.shape != to_idx.shape:
+            raise ValueError("from and to indices differ in length")
+        if from_idx.numel() == 0:
+            self.last_states_checked = 0
+            return torch.zeros(0, dtype=torch.bool, device=keys.device)
+        ta = keys.index_select(0, from_idx).contiguous()
+        tb = keys.index_select(0, to_idx).contiguous()
+        valid, self.last_states_checked = _check_motions_dev(self.uw, ta, tb, self.lo, self.hi, self.cdres)
+        return valid.bool()

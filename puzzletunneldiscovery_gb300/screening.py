@@ -134,14 +134,21 @@ def screen_pairs(uw, keys, from_indices, to_indices, verify_magnitude: float | N
 
 
 def screen_keyconf(uw, keys, max_chunk_number: int = 1, minimal_chunk_size: int = 1, out_dir: str | None = None,
-                   verify_magnitude: float | None = None, batch: int = 1 << 22, resume: bool = False):
+                   verify_magnitude: float | None = None, batch: int = 1 << 22, resume: bool = False,
+                   driver=None):
     """The whole screening stage: every task of partition_screening checked on
     the device (pairs decoded from flat indices there, nothing per pair on the
     host).  Returns (EDGE_FROM, EDGE_TO) over all tasks in task order; with
     out_dir, also writes edge_batch-<task>.npz per task as the reference's
     workers do (solve2.py:226).  With resume, a task whose file already exists
     is read back instead of checked again, as the reference's rerun mode
-    recomputes only the missing task outputs (solve2.py:168-187)."""
+    recomputes only the missing task outputs (solve2.py:168-187).
+
+    The pairs are checked as the reference's rerun mode does
+    (calculate_visibility_pair at verify_magnitude, solve2.py:180-183), or,
+    with an ompl_compat.OmplDriver set up for the puzzle, as its workers do:
+    driver.validate_motion_pairs on the OMPL-frame keys (solve2.py:218-219),
+    OMPL's discrete motion rule at the driver's bounds and resolution."""
     vm = uw.recommended_cres if verify_magnitude is None else float(verify_magnitude)
     keys = np.asarray(keys, dtype=np.float64)
     nkey = keys.shape[0] - RESERVED
@@ -150,8 +157,17 @@ def screen_keyconf(uw, keys, max_chunk_number: int = 1, minimal_chunk_size: int 
     ntask = nkey * (nkey + 1) // 2
     total = guess_chunk_number(ntask, max_chunk_number, minimal_chunk_size)
     bounds = chunk_bounds(ntask, total)
-    U = _unit_keys(uw, keys)
     dev = uw._device
+    if driver is None:
+        U = _unit_keys(uw, keys)
+
+        def visible(r, c):
+            return _visible(uw, U, r, c, vm)
+    else:
+        P = torch.from_numpy(np.ascontiguousarray(keys)).to(dev)
+
+        def visible(r, c):
+            return driver.check_pairs(P, r, c)
     all_f, all_t = [], []
     for task, (s, e) in enumerate(bounds):
         fn = os.path.join(out_dir, "edge_batch-{}.npz".format(task)) if out_dir is not None else None
@@ -165,7 +181,7 @@ def screen_keyconf(uw, keys, max_chunk_number: int = 1, minimal_chunk_size: int 
             k = torch.arange(s0, min(int(e), s0 + batch), dtype=torch.int64, device=dev)
             r, c = _tril_pairs_dev(k)
             r, c = r + RESERVED, c + RESERVED
-            vis = _visible(uw, U, r, c, vm)
+            vis = visible(r, c)
             ef.append(r[vis].cpu().numpy())
             et.append(c[vis].cpu().numpy())
         f = np.concatenate(ef) if ef else np.zeros(0, np.int64)

@@ -148,3 +148,22 @@ def test_arguments_and_edge_cases(alpha):
     keep = np.ones(10, bool)
     keep[[4, 7]] = False
     assert nf[4] == 0 and nf[7] == 0 and np.array_equal(nf[keep], full[keep])
+
+
+def test_screening_with_the_ompl_rule(alpha, tmp_path):
+    """screen_keyconf with an OmplDriver (the reference's screening worker,
+    solve2.py:218-219) keeps exactly the lower-triangle pairs that
+    validate_motion_pairs finds valid, across tasks and batches."""
+    from puzzletunneldiscovery_gb300 import ompl_compat as OC
+    from puzzletunneldiscovery_gb300 import screening as S
+    uw, ow, P, lo, hi = alpha
+    keys = P[:40]
+    d = OC.OmplDriver(uw)
+    d.set_bb(lo, hi)
+    d.set_cdres(CDRES)
+    ef, et = S.screen_keyconf(uw, keys, max_chunk_number=4, out_dir=str(tmp_path), batch=100, driver=d)
+    r, c = np.tril_indices(len(keys) - S.RESERVED)
+    r, c = r + S.RESERVED, c + S.RESERVED
+    want = d.validate_motion_pairs(keys[r], keys[c]).astype(bool)
+    assert np.array_equal(ef, r[want]) and np.array_equal(et, c[want])
+    assert 0 < want.sum() <= len(want)

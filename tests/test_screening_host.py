@@ -123,3 +123,64 @@ def test_screening_resume_checks_only_missing_tasks(tmp_path):
     assert w2.pairs == b[2, 1] - b[2, 0]
     assert np.array_equal(ef2, ef) and np.array_equal(et2, et)
     assert (tmp_path / "edge_batch-2.npz").exists()
+
+
+class _FakeOmplLib:
+    """pw_ompl_check_motions over host memory: motion i is valid unless
+    from.x + to.x is a multiple of 3.  Records the arguments it was given."""
+
+    def __init__(self):
+        self.calls = []
+
+    def pw_ompl_check_motions(self, h, pa, pb, m, lo, hi, cdres, pvalid, pchecked, stream):
+        import ctypes
+        A = np.ctypeslib.as_array((ctypes.c_double * (7 * m)).from_address(pa)).reshape(m, 7)
+        B = np.ctypeslib.as_array((ctypes.c_double * (7 * m)).from_address(pb)).reshape(m, 7)
+        self.calls.append((m, [lo[i] for i in range(3)], [hi[i] for i in range(3)], cdres, stream))
+        v = (np.round(A[:, 0] + B[:, 0]).astype(np.int64) % 3 != 0).astype(np.uint8)
+        ctypes.memmove(pvalid, v.ctypes.data, m)
+        pchecked[0] = 5 * m
+        return 0
+
+
+class _FakeOmplWorld:
+    recommended_cres = 0.01
+    _device = "cpu"
+    _h = None
+
+    def __init__(self):
+        self._L = _FakeOmplLib()
+
+
+def test_screening_with_an_ompl_driver_checks_ompl_frame_key_pairs(tmp_path):
+    """screen_keyconf(driver=OmplDriver) asks the driver about every lower-triangle
+    pair (from = row, to = column, the OMPL-frame keys as stored), with the
+    driver's bounds and resolution, in batches; the driver refuses to run
+    before set_bb / set_cdres."""
+    from puzzletunneldiscovery_gb300 import ompl_compat as OC
+    from puzzletunneldiscovery_gb300 import screening as S
+    n = 25
+    keys = np.zeros((n, 7))
+    keys[:, 0] = np.arange(n)
+    keys[:, 6] = 1.0
+    w = _FakeOmplWorld()
+    d = OC.OmplDriver(w)
+    with pytest.raises(RuntimeError):
+        S.screen_keyconf(w, keys, driver=d)
+    d.set_bb([-1, -2, -3], [4, 5, 6])
+    d.set_cdres(0.02)
+    ef, et = S.screen_keyconf(w, keys, max_chunk_number=3, out_dir=str(tmp_path), batch=11, driver=d)
+    r, c = np.tril_indices(n - S.RESERVED)
+    r, c = r + S.RESERVED, c + S.RESERVED
+    m = (r + c) % 3 != 0
+    assert np.array_equal(ef, r[m]) and np.array_equal(et, c[m])
+    calls = w._L.calls
+    assert sum(x[0] for x in calls) == r.shape[0] and max(x[0] for x in calls) <= 11
+    assert all(x[1] == [-1, -2, -3] and x[2] == [4, 5, 6] and x[3] == 0.02 and x[4] is None for x in calls)
+    assert d.last_states_checked == 5 * calls[-1][0]
+    ef2, et2 = S.load_edges(str(tmp_path))
+    assert sorted(zip(ef2, et2)) == sorted(zip(ef, et))
+    # the host-array call goes through the same entry point
+    out, checked = OC.check_motions_discrete(w, keys[2:8], keys[3:7], [-1, -2, -3], [4, 5, 6], 0.02)
+    want = ((np.arange(2, 6) + np.arange(3, 7)) % 3 != 0).astype(np.int32)
+    assert np.array_equal(out, np.concatenate([want, [0, 0]])) and checked == 20
