@@ -67,9 +67,224 @@ WORKLOADS = {
                   W.cfg_interlocking_tori, 200_000_000),
     "narrow": ("escapes through a plate hole/sec (surrogate-guided narrow-passage search, plate vs torus knot)",
                W.cfg_plate_knot, 4_000_000),
+    "ompl": ("motions checked/sec (OMPL discrete motion check, validate_motion_pairs, alpha puzzle)",
+             lambda: _alpha_ompl()[0], 1_000_000),
 }
+# OMPL motion workload: collision resolution and the spread of the motions' targets (OMPL units)
+OMPL_CDRES = 0.01
+OMPL_SIGMA = 2.0
 # proposal network: FLOPs per scored state (9 -> 256 x4 -> 1; the padded input columns are not counted)
 MLP_FLOP_PER_ROW = 2 * (9 * 256 + 3 * 256 * 256 + 256)
+
+
+def _quat_matrix(q):
+    """Rotation matrix of a unit quaternion (w, x, y, z)."""
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                     [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                     [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+
+
+def _alpha_ompl():
+    """The alpha puzzle (its meshes and solution path, tests/golden/alpha_puzzle.npz)
+    with the path's states written in the OMPL frame of a world whose robot centre
+    is enforced to the puzzle's centre c: t_ompl = t + R(q) (m - c), m the robot's
+    float vertex mean, so that translateOMPLStateToUnitState gives back the
+    path's unit-frame states.  Returns ((Ve, Fe, Vr, Fr), c, path in the OMPL frame)."""
+    g = np.load(os.path.join(ROOT, "tests", "golden", "alpha_puzzle.npz"))
+    c = g["center"].astype(np.float32)
+    acc = np.zeros(3, dtype=np.float32)
+    for v in g["Vr"].astype(np.float32):
+        acc = acc + v
+    d = (acc / np.float32(len(g["Vr"])) - c).astype(np.float64)
+    P = g["path_wlast"].astype(np.float64).copy()
+    for i, p in enumerate(P):
+        q = np.array([p[6], p[3], p[4], p[5]])
+        P[i, :3] = p[:3] + _quat_matrix(q / np.linalg.norm(q)) @ d
+    return (g["Ve"], g["Fe"], g["Vr"], g["Fr"]), c, P
+
+
+def _ompl_motions(P, n, seed):
+    """n motions from a path state to another path state displaced by N(0, sigma^2)
+    per axis, in the path's box widened by 20 on every side (the bounds of the
+    state space)."""
+    rng = np.random.default_rng(1000 + seed)
+    i = rng.integers(0, len(P), n)
+    j = rng.integers(0, len(P), n)
+    B = P[j].copy()
+    B[:, :3] += rng.normal(0.0, OMPL_SIGMA, (n, 3))
+    return np.ascontiguousarray(P[i]), B, P[:, :3].min(axis=0) - 20.0, P[:, :3].max(axis=0) + 20.0
+
+
+def _ompl_oracle():
+    from oracle import oracle as O
+    O.build()
+    (Ve, Fe, Vr, Fr), c, P = _alpha_ompl()
+    return O.OracleWorld(Ve, Fe, Vr, Fr, center=c), P
+
+
+def _ompl_cpu(ow, A, B, lo, hi, target_s, start_n=2048):
+    """The oracle's validateMotionPairs (OMPL's early-exit order, all host threads) on a
+    sample of the motions grown until it takes about target_s: (motions/s, sample
+    size, checks per motion, seconds, verdicts)."""
+    cores = os.cpu_count() or 1
+    n = min(start_n, len(A))
+    while True:
+        t0 = time.perf_counter()
+        v, c = ow.ompl_check_motions(A[:n], B[:n], lo, hi, OMPL_CDRES, nthreads=cores)
+        dt = time.perf_counter() - t0
+        if dt >= target_s or n >= len(A):
+            break
+        n = min(len(A), max(n * 2, int(n * target_s / max(dt, 1e-3) * 1.1)))
+    return n / dt, n, float(c.mean()), dt, v
+
+
+def run_ompl(args):
+    """--workload ompl: pw_ompl_check_motions over a resident batch of motions."""
+    import torch
+    import torch.distributed as dist
+
+    import puzzletunneldiscovery_gb300 as pw
+    from puzzletunneldiscovery_gb300 import ompl_compat as OC
+
+    ws, rank, local = _dist_env()
+    if ws > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    (Ve, Fe, Vr, Fr), c, P = _alpha_ompl()
+    uw = pw.UnitWorld(local)
+    uw.load_env_mesh(Ve, Fe)
+    uw.load_robot_mesh(Vr, Fr)
+    uw.enforceRobotCenter(c)
+    uw.scaleToUnit()
+    uw.angleModel(0.0, 0.0)
+    A, B, lo, hi = _ompl_motions(P, args.n, rank)
+    a = torch.from_numpy(A).to(dev)
+    b = torch.from_numpy(B).to(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        if ws > 1:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    for _ in range(args.warmup):
+        OC._check_motions_dev(uw, a, b, lo, hi, OMPL_CDRES)
+    barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    checked = []
+    with ClockSampler(local) as clk:
+        barrier()
+        for i in range(args.steps):
+            flush.zero_()                      # L2 flush between timed steps (not timed)
+            ev[i][0].record(stream)
+            v, n_states = OC._check_motions_dev(uw, a, b, lo, hi, OMPL_CDRES)
+            ev[i][1].record(stream)
+            checked.append(n_states)
+        barrier()
+    step_ms = [s0.elapsed_time(s1) for s0, s1 in ev]
+    tot_ms, tot_motions = max_time_sum_units(sum(step_ms), args.n * args.steps, ws, dev)
+    value = tot_motions / (tot_ms / 1e3)
+    verdicts = v.cpu().numpy()
+
+    # end to end through the public host-array call: motions copied in, verdicts out, every step
+    ha = torch.from_numpy(A).pin_memory().numpy()
+    hb = torch.from_numpy(B).pin_memory().numpy()
+    e2e_ms = 0.0
+    barrier()
+    for i in range(args.steps):
+        flush.zero_()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        hv, _ = OC.check_motions_discrete(uw, ha, hb, lo, hi, OMPL_CDRES)
+        s1.record(stream)
+        torch.cuda.synchronize(dev)
+        e2e_ms += s0.elapsed_time(s1)
+    if not np.array_equal(hv, verdicts.astype(np.int32)):
+        raise RuntimeError("host-array path disagrees with the device path")
+    e2e_ms, e2e_motions = max_time_sum_units(e2e_ms, args.n * args.steps, ws, dev)
+    e2e_value = e2e_motions / (e2e_ms / 1e3)
+
+    if rank != 0:
+        if ws > 1:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    states = checked[-1]
+    windows = -(-states // (1 << 22))
+    ms = tot_ms / args.steps
+    # per checked state: generated and written (56 B), read by the check (56 B), its verdict
+    # written and read (2 B); per motion: both ends read by the count and state kernels
+    # (4 x 56 B), its count and offset (16 B) and verdict (1 B)
+    alg_bytes = states * 114 + args.n * (4 * 56 + 17)
+    peak, peak_kind = _peaks()
+    achieved = alg_bytes / (ms / 1e3) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "kernel": "whole call (k_ompl_counts, k_ompl_states, k_states, k_ompl_reduce)",
+            "peak_source": peak_kind, "algorithmic_bytes": alg_bytes,
+            "note": "the states pass is bound by the traversal's SM issue, as in the plate workload"}
+    cpu = None
+    if ws == 1 and not args.no_cpu_baseline:
+        ow, _ = _ompl_oracle()
+        cv, cn, cpm, cdt, ov = _ompl_cpu(ow, A, B, lo, hi, args.cpu_seconds)
+        if not np.array_equal(ov, verdicts[:cn]):
+            raise RuntimeError("GPU verdicts differ from the oracle's on the CPU sample")
+        cpu = {"value": cv, "unit": "motions/s", "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": "first %d motions of the batch (OMPL's early-exit order, %.2f states checked per "
+                         "motion, %.1f s); verdicts equal the GPU's" % (cn, cpm, cdt)}
+    line = {"metric": WORKLOADS["ompl"][0], "value": value, "unit": "motions/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 state math + f32 traversal",
+            "data": "synthetic (seeded motions between the alpha puzzle's path states)",
+            "config": {"workload": "validate_motion_pairs/alpha_puzzle", "n_motions_per_gpu": args.n,
+                       "cdres": OMPL_CDRES, "target_sigma": OMPL_SIGMA,
+                       "bounds": [lo.tolist(), hi.tolist()],
+                       "l2": "flushed (256 MB write) between timed steps; per-step working set > L2",
+                       "parallelism": "replicas" if ws == 1 else "shard-per-rank (weak)"},
+            "roofline": roof, "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "motions/s", "h2d_bytes_per_step": int(args.n * 112 * ws),
+                    "d2h_bytes_per_step": int(args.n * ws)},
+            "clocks": clk.summary(),
+            # counts, then per window of states: generation, traversal, re-test, reduction
+            "gpu_launches": (1 + 4 * windows) * args.steps,
+            "detail": {"states_checked_per_step": states, "states_per_motion": states / args.n,
+                       "valid_fraction": float(verdicts.mean()), "windows": windows, "step_ms": step_ms}}
+    print(json.dumps(line))
+    if ws > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def run_ompl_reference(args):
+    """--impl reference --workload ompl: the oracle's validateMotionPairs on the host cores."""
+    ws, rank, _ = _dist_env()
+    if rank != 0:
+        return
+    ow, P = _ompl_oracle()
+    A, B, lo, hi = _ompl_motions(P, args.n, 0)
+    cores = os.cpu_count() or 1
+    sample = 50 * args.ref_sample
+    times = []
+    for it in range(args.warmup + args.steps):
+        s0 = (it * sample) % max(1, args.n - sample)
+        t0 = time.perf_counter()
+        ow.ompl_check_motions(A[s0:s0 + sample], B[s0:s0 + sample], lo, hi, OMPL_CDRES, nthreads=cores)
+        if it >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    value = sample * len(times) / sum(times)
+    line = {"impl": "reference", "metric": WORKLOADS["ompl"][0], "value": value, "unit": "motions/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, same motions as the GPU arm)",
+            "config": {"workload": "validate_motion_pairs/alpha_puzzle", "n_motions_per_gpu": args.n,
+                       "cdres": OMPL_CDRES, "sample_per_step": sample},
+            "cpu_baseline": {"value": value, "unit": "motions/s", "cores": cores, "kind": "port",
+                             "sample": "%d motions per step of the %d-motion batch" % (sample, args.n)},
+            "e2e": {"value": value, "unit": "motions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
 
 
 def _meshes(workload="segments"):
@@ -805,6 +1020,8 @@ def main():
                               "learned proposal; its CPU path is timed in the plate workload"}))
         else:
             run_narrow(args)
+    elif args.workload == "ompl":
+        run_ompl_reference(args) if args.impl == "reference" else run_ompl(args)
     elif args.workload == "surrogate":
         args.e2e_n = min(args.e2e_n, args.n)
         run_surrogate_reference(args) if args.impl == "reference" else run_surrogate(args)

@@ -109,6 +109,9 @@ def lib():
         L.or_ompl_interpolate.argtypes = [c_double_p, c_double_p, ctypes.c_double, c_double_p]
         L.or_ompl_motion_states.restype = ctypes.c_int64
         L.or_ompl_motion_states.argtypes = [c_double_p, c_double_p, c_double_p, ctypes.c_int64, c_double_p]
+        L.or_ompl_to_unit.argtypes = [ctypes.c_void_p, c_double_p, c_double_p]
+        L.or_ompl_check_motions.argtypes = [ctypes.c_void_p, c_double_p, c_double_p, ctypes.c_int64, c_double_p,
+                                            c_u8_p, c_i64_p, ctypes.c_int]
         L.or_tri_tri.restype = ctypes.c_int
         L.or_tri_tri.argtypes = [c_double_p] * 6 + [ctypes.c_double]
         L.or_tri_tri_isect.restype = ctypes.c_int
@@ -182,6 +185,26 @@ class OracleWorld:
         fn = self._L.or_states_valid_brute if brute else self._L.or_states_valid
         fn(self._h, _p(q, c_double_p), q.shape[0], _p(out, c_u8_p), nthreads)
         return out.astype(bool)
+
+    def ompl_to_unit(self, P):
+        """translateOMPLStateToUnitState of OMPL-frame states (x, y, z, qx, qy, qz, qw)."""
+        P = _states(P)
+        out = np.zeros_like(P)
+        for i in range(P.shape[0]):
+            self._L.or_ompl_to_unit(self._h, _p(P[i], c_double_p), _p(out[i], c_double_p))
+        return out
+
+    def ompl_check_motions(self, A, B, lo, hi, cdres, nthreads=0):
+        """OmplDriver::validateMotionPairs with OMPL's discrete motion validator (early
+        exit in OMPL's order): (uint8 verdicts, int64 states checked per motion)."""
+        A, B = _states(A), _states(B)
+        assert A.shape == B.shape
+        lvs = ompl_lvs(lo, hi, cdres)
+        valid = np.zeros(A.shape[0], dtype=np.uint8)
+        checks = np.zeros(A.shape[0], dtype=np.int64)
+        self._L.or_ompl_check_motions(self._h, _p(A, c_double_p), _p(B, c_double_p), A.shape[0],
+                                      _p(lvs, c_double_p), _p(valid, c_u8_p), _p(checks, c_i64_p), int(nthreads))
+        return valid, checks
 
     def is_disentangled(self, q, nthreads=0):
         q = _states(q)

@@ -579,6 +579,7 @@ typedef struct or_world {
 	double *env_local; /* env CD vertices before the perturbation transform */
 	float scale;
 	float center[3];
+	float ompl_center[3]; /* float mean of the robot's vertices (scene.cc:40-50,141-145) */
 	double pert[7];
 	double env_box_c[3], env_box_h[3]; /* local AABB box of the env CD model */
 	double rob_box_c[3], rob_box_h[3];
@@ -741,14 +742,13 @@ OR_EXPORT int or_world_set_meshes(or_world *w,
 	const float span_r = or_span(Vr, nvr);
 	const float mx = span_e > span_r ? span_e : span_r;
 	w->scale = (float)(1.0 / (double)mx);
-	if (center) {
-		for (int c = 0; c < 3; c++) w->center[c] = center[c];
-	} else {
+	{
 		float acc[3] = { 0.f, 0.f, 0.f };
 		for (int64_t i = 0; i < nvr; i++)
 			for (int c = 0; c < 3; c++) acc[c] = acc[c] + Vr[3 * i + c];
-		for (int c = 0; c < 3; c++) w->center[c] = nvr > 0 ? acc[c] / (float)nvr : 0.0f;
+		for (int c = 0; c < 3; c++) w->ompl_center[c] = nvr > 0 ? acc[c] / (float)nvr : 0.0f;
 	}
+	for (int c = 0; c < 3; c++) w->center[c] = center ? center[c] : w->ompl_center[c];
 	const double s = (double)w->scale;
 	/* robot xform = S(s) T(-c) in float: translation column fl32(s * -c) */
 	float tr[3];
@@ -1286,4 +1286,124 @@ OR_EXPORT int64_t or_ompl_motion_states(const double a[7], const double b[7], co
 	for (int64_t k = 1; k < m && k < cap; k++)
 		or_ompl_interpolate(a, b, (double)k / (double)nd, out + 7 * k);
 	return m;
+}
+
+/* Hamilton product a * b, quaternions (w, x, y, z). */
+static void or_quat_mul(const double a[4], const double b[4], double o[4])
+{
+	o[0] = ((a[0] * b[0] - a[1] * b[1]) - a[2] * b[2]) - a[3] * b[3];
+	o[1] = ((a[0] * b[1] + a[1] * b[0]) + a[2] * b[3]) - a[3] * b[2];
+	o[2] = ((a[0] * b[2] - a[1] * b[3]) + a[2] * b[0]) + a[3] * b[1];
+	o[3] = ((a[0] * b[3] + a[1] * b[2]) - a[2] * b[1]) + a[3] * b[0];
+}
+
+/* decompose / compose (osr_state.cc:85-119): the rotation normalised each way. */
+static void or_decompose(const double q[7], double t[3], double rot[4])
+{
+	t[0] = q[0]; t[1] = q[1]; t[2] = q[2];
+	const double r[4] = { q[3], q[4], q[5], q[6] };
+	or_quat_normalize(r, rot);
+}
+
+static void or_compose(const double t[3], const double rot[4], double q[7])
+{
+	double r[4];
+	or_quat_normalize(rot, r);
+	q[0] = t[0]; q[1] = t[1]; q[2] = t[2];
+	q[3] = r[0]; q[4] = r[1]; q[5] = r[2]; q[6] = r[3];
+}
+
+static void or_mat_vec(const double R[9], const double v[3], double o[3])
+{
+	for (int i = 0; i < 3; i++)
+		o[i] = (R[3 * i] * v[0] + R[3 * i + 1] * v[1]) + R[3 * i + 2] * v[2];
+}
+
+/* translateOMPLStateToUnitState (unit_world.cc:689-711) of one OMPL state (x, y, z, qx,
+ * qy, qz, qw): w-first, translation scaled, applyPertubation (:713-724), then
+ * t' = t - R(q) (OMPL centre - centre) scale. */
+OR_EXPORT void or_ompl_to_unit(const or_world *w, const double p[7], double u[7])
+{
+	const double s = (double)w->scale;
+	const double tmp[7] = { s * p[0], s * p[1], s * p[2], p[6], p[3], p[4], p[5] };
+	double t[3], rot[4], pt[3], prot[4], qret[4], R[9], Rt[3], tret[3], a[7];
+	or_decompose(tmp, t, rot);
+	or_decompose(w->pert, pt, prot);
+	or_quat_mul(prot, rot, qret);
+	or_quat_to_matrix(prot, R);
+	or_mat_vec(R, t, Rt);
+	for (int c = 0; c < 3; c++) tret[c] = pt[c] + Rt[c];
+	or_compose(tret, qret, a);
+	double dc[3], Rd[3], t2[3];
+	for (int c = 0; c < 3; c++) dc[c] = (double)(w->ompl_center[c] - w->center[c]) * s;
+	or_decompose(a, t, rot);
+	or_quat_to_matrix(rot, R);
+	or_mat_vec(R, dc, Rd);
+	for (int c = 0; c < 3; c++) t2[c] = t[c] - Rd[c];
+	or_compose(t2, rot, u);
+}
+
+static int or_finite7(const double *q)
+{
+	for (int c = 0; c < 7; c++)
+		if (!isfinite(q[c]))
+			return 0;
+	return 1;
+}
+
+/* OmplDriver::validateMotionPairs (ompldriver.cc:597-621) for n OMPL-frame motions, as
+ * OMPL's DiscreteMotionValidator::checkMotion runs it: the target state first, then the
+ * middle state of each index range in a FIFO that starts with [1, nd - 1] and splits each
+ * checked range in two, stopping at the first colliding state.  valid[i] = 1 when none
+ * collides; checks[i] = the states checked.  A motion with a non-finite component gets 0
+ * and no checks. */
+OR_EXPORT void or_ompl_check_motions(const or_world *w, const double *from, const double *to, int64_t n,
+                                     const double lvs[2], uint8_t *valid, int64_t *checks, int nthreads)
+{
+#ifdef _OPENMP
+	if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 16)
+#endif
+	for (int64_t i = 0; i < n; i++) {
+		const double *a = from + 7 * i, *b = to + 7 * i;
+		valid[i] = 0;
+		checks[i] = 0;
+		if (!or_finite7(a) || !or_finite7(b))
+			continue;
+		double u[7], s[7];
+		or_ompl_to_unit(w, b, u);
+		checks[i] = 1;
+		if (!or_is_valid(w, u, 0))
+			continue;
+		const int64_t nd = or_ompl_segment_count(a, b, lvs);
+		int ok = 1;
+		if (nd >= 2) {
+			int64_t *q = (int64_t *)malloc(sizeof(int64_t) * 2 * (size_t)nd);
+			int64_t head = 0, tail = 0;
+			q[0] = 1; q[1] = nd - 1;
+			tail = 1;
+			while (head < tail) {
+				const int64_t f = q[2 * (head % nd)], l = q[2 * (head % nd) + 1];
+				const int64_t mid = (f + l) / 2;
+				or_ompl_interpolate(a, b, (double)mid / (double)nd, s);
+				or_ompl_to_unit(w, s, u);
+				checks[i]++;
+				if (!or_is_valid(w, u, 0)) {
+					ok = 0;
+					break;
+				}
+				head++;
+				if (f < mid) {
+					q[2 * (tail % nd)] = f; q[2 * (tail % nd) + 1] = mid - 1;
+					tail++;
+				}
+				if (l > mid) {
+					q[2 * (tail % nd)] = mid + 1; q[2 * (tail % nd) + 1] = l;
+					tail++;
+				}
+			}
+			free(q);
+		}
+		valid[i] = (uint8_t)ok;
+	}
 }

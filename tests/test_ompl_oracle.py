@@ -4,9 +4,12 @@ lib/pyse3ompl/ompldriver.cc:597-621) against closed forms: the segment count of
 pure translations and pure rotations, and the interpolated states of a rotation
 about one axis.  No device needed."""
 import math
+import os
 
 import numpy as np
 import pytest
+
+from conftest import ROOT
 
 
 def _rot_z(phi, t=(0.0, 0.0, 0.0)):
@@ -87,3 +90,65 @@ def test_count_is_symmetric(oracle_mod):
         a[3:] /= np.linalg.norm(a[3:])
         b[3:] /= np.linalg.norm(b[3:])
         assert O.ompl_motion_states(a, b, lo, hi, 0.01).shape[0] == O.ompl_motion_states(b, a, lo, hi, 0.01).shape[0]
+
+
+@pytest.fixture(scope="module")
+def alpha_ompl(oracle_mod):
+    import bench
+    (Ve, Fe, Vr, Fr), c, P = bench._alpha_ompl()
+    return oracle_mod.OracleWorld(Ve, Fe, Vr, Fr, center=c), P
+
+
+def test_ompl_frame_conversion_closed_form(alpha_ompl):
+    """or_ompl_to_unit (translateOMPLStateToUnitState, unit_world.cc:689-711) is
+    t' = s t - R(q) (m - c) s with the w-first rotation, m the robot's vertex
+    mean and c its enforced centre; the path's OMPL-frame states come back free."""
+    ow, P = alpha_ompl
+    U = ow.ompl_to_unit(P)
+    import bench
+    s = ow.scene_scale
+    g = np.load(os.path.join(ROOT, "tests", "golden", "alpha_puzzle.npz"))
+    acc = np.zeros(3, dtype=np.float32)
+    for v in g["Vr"].astype(np.float32):
+        acc = acc + v
+    # float mean summed in order, minus the float centre, as the world stores them
+    d = (acc / np.float32(len(g["Vr"])) - g["center"].astype(np.float32)).astype(np.float64) * s
+    for p, u in zip(P, U):
+        q = np.array([p[6], p[3], p[4], p[5]])
+        q /= np.linalg.norm(q)
+        assert np.allclose(u[:3], p[:3] * s - bench._quat_matrix(q) @ d, rtol=0, atol=1e-14)
+        assert np.allclose(u[3:], q, rtol=0, atol=1e-15)
+    assert ow.is_valid(U).all()
+
+
+def test_early_exit_check_agrees_with_every_state(alpha_ompl, oracle_mod):
+    """or_ompl_check_motions (OMPL's order, stopping at the first colliding state)
+    gives the verdict of checking every state checkMotion lists, with at most as
+    many checks; the path's own edges are valid."""
+    import bench
+    ow, P = alpha_ompl
+    A, B, lo, hi = bench._ompl_motions(P, 600, seed=5)
+    A = np.concatenate([A, P[:-1]])
+    B = np.concatenate([B, P[1:]])
+    v, checks = ow.ompl_check_motions(A, B, lo, hi, 0.01)
+    for i in range(len(A)):
+        S = oracle_mod.ompl_motion_states(A[i], B[i], lo, hi, 0.01)
+        ok = ow.is_valid(ow.ompl_to_unit(S)).astype(bool)
+        assert v[i] == ok.all(), i
+        assert 1 <= checks[i] <= len(S)
+        if ok.all():
+            assert checks[i] == len(S)
+        elif not ok[0]:
+            assert checks[i] == 1
+    assert v[-(len(P) - 1):].all()
+    assert 0 < v[:600].sum() < 600
+
+
+def test_non_finite_motions_are_invalid(alpha_ompl):
+    ow, P = alpha_ompl
+    A, B = P[:4].copy(), P[1:5].copy()
+    A[1, 0] = np.nan
+    B[2, 5] = np.inf
+    v, checks = ow.ompl_check_motions(A, B, P[:, :3].min(0) - 20, P[:, :3].max(0) + 20, 0.01)
+    assert v[1] == 0 and v[2] == 0 and checks[1] == 0 and checks[2] == 0
+    assert v[0] == 1 and v[3] == 1
