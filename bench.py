@@ -248,8 +248,9 @@ def run_ompl(args):
             "e2e": {"value": e2e_value, "unit": "motions/s", "h2d_bytes_per_step": int(args.n * 112 * ws),
                     "d2h_bytes_per_step": int(args.n * ws)},
             "clocks": clk.summary(),
-            # counts, then per window of states: generation, traversal, re-test, reduction
-            "gpu_launches": (1 + 4 * windows) * args.steps,
+            # segment counts, three pass counts, then per window of a pass's states: generation,
+            # traversal, re-test, reduction (a lower bound: each pass starts its own window)
+            "gpu_launches": (4 + 4 * windows) * args.steps,
             "detail": {"states_checked_per_step": states, "states_per_motion": states / args.n,
                        "valid_fraction": float(verdicts.mean()), "windows": windows, "step_ms": step_ms}}
     print(json.dumps(line))

@@ -25,10 +25,14 @@
 // the engine's exact verdict after translateOMPLStateToUnitState
 // (unit_world.cc:689-711), as for validateStates.
 //
-// Layout: one motion's checked states are numbered j = 0 (s2) and j = k
-// (k = 1 .. nd - 1).  A scan of the per-motion counts numbers all states of a
-// batch; they are generated, converted to the unit frame and checked window
-// by window, and a failed state clears its motion's verdict.
+// The check runs in three passes, each over the motions that are still valid:
+// the targets, then the middle state k = nd / 2 (the first one OMPL's queue
+// checks), then every other k.  A motion's verdict is the AND of all its
+// states either way; the passes only skip the states of motions already
+// known to collide, as OMPL's early exit does.  In a pass, a scan of the
+// per-motion counts numbers the pass's states; they are generated, converted
+// to the unit frame and checked window by window, and a colliding state clears
+// its motion's verdict.
 #include <cub/cub.cuh>
 
 #include <cfloat>
@@ -68,9 +72,12 @@ __device__ __forceinline__ bool finite7(const double *q)
 	return ok;
 }
 
-// Per motion: how many states checkMotion checks (1, or nd when nd >= 2), and
-// the verdict's starting value (0 for a motion with a non-finite component).
-__global__ void k_ompl_counts(const double *from, const double *to, int64_t n, OmplSpace S, int64_t *count,
+// The passes, and the listing of every state a motion's check looks at.
+enum { PASS_ALL = 0, PASS_TARGET = 1, PASS_MID = 2, PASS_REST = 3 };
+
+// Per motion: OMPL's segment count nd, and the verdict's starting value (0, and
+// nd = 0, for a motion with a non-finite component).
+__global__ void k_ompl_counts(const double *from, const double *to, int64_t n, OmplSpace S, int64_t *nd_out,
                               uint8_t *valid, int *too_long)
 {
 	const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -79,7 +86,7 @@ __global__ void k_ompl_counts(const double *from, const double *to, int64_t n, O
 	using namespace pwm;
 	const double *a = from + 7 * i, *b = to + 7 * i;
 	if (!finite7(a) || !finite7(b)) {
-		count[i] = 1;
+		nd_out[i] = 0;
 		valid[i] = 0;
 		return;
 	}
@@ -90,15 +97,49 @@ __global__ void k_ompl_counts(const double *from, const double *to, int64_t n, O
 	const double nd = nr > ns ? nr : ns;
 	if (nd > MAX_SEGMENTS) {
 		atomicOr(too_long, 1);
-		count[i] = 1;
+		nd_out[i] = 0;
 		valid[i] = 0;
 		return;
 	}
-	count[i] = nd >= 2.0 ? (int64_t)nd : 1;
+	nd_out[i] = (int64_t)nd;
 	valid[i] = 1;
 }
 
-// The motion that global state g belongs to: offs[i] <= g < offs[i + 1].
+// States of a motion in a pass: all of them (the target and k = 1 .. nd - 1), the
+// target, the middle one, or the rest; the last three only while the motion is valid.
+__device__ __forceinline__ int64_t pass_count(int pass, int64_t nd, uint8_t valid)
+{
+	switch (pass) {
+	case PASS_ALL: return nd >= 2 ? nd : 1;
+	case PASS_TARGET: return valid ? 1 : 0;
+	case PASS_MID: return valid && nd >= 2 ? 1 : 0;
+	default: return valid && nd >= 3 ? nd - 2 : 0;
+	}
+}
+
+// Index k of the r-th state of a motion in a pass (0: the target).
+__device__ __forceinline__ int64_t pass_index(int pass, int64_t nd, int64_t r)
+{
+	switch (pass) {
+	case PASS_ALL: return r;
+	case PASS_TARGET: return 0;
+	case PASS_MID: return nd / 2;
+	default: {
+		const int64_t k = r + 1;
+		return k >= nd / 2 ? k + 1 : k;
+	}
+	}
+}
+
+__global__ void k_ompl_pass_counts(const int64_t *nd, const uint8_t *valid, int64_t n, int pass, int64_t *cnt)
+{
+	const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+	if (i < n)
+		cnt[i] = pass_count(pass, nd[i], valid[i]);
+}
+
+// The motion that state g of a pass belongs to: the last i with offs[i] <= g, so
+// that motions without states in the pass (offs[i] == offs[i + 1]) are skipped.
 __device__ __forceinline__ int64_t owner(const int64_t *offs, int64_t n, int64_t g)
 {
 	int64_t lo = 0, hi = n - 1;
@@ -134,22 +175,21 @@ __device__ __forceinline__ void ompl_interpolate(const double *a, const double *
 	}
 }
 
-// Checked states [first, first + cnt) of the batch, in the unit frame.
-__global__ void k_ompl_states(const double *from, const double *to, int64_t n, const int64_t *offs, int64_t first,
-                              int64_t cnt, pwfr::Frame F, double *out)
+// States [first, first + cnt) of a pass, in the unit frame.
+__global__ void k_ompl_states(const double *from, const double *to, int64_t n, const int64_t *nd,
+                              const int64_t *offs, int pass, int64_t first, int64_t cnt, pwfr::Frame F, double *out)
 {
 	for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < cnt; k += (int64_t)gridDim.x * blockDim.x) {
 		const int64_t g = first + k;
 		const int64_t i = owner(offs, n, g);
-		const int64_t j = g - offs[i];
+		const int64_t j = pass_index(pass, nd[i], g - offs[i]);
 		const double *a = from + 7 * i, *b = to + 7 * i;
 		double s[7];
 		if (j == 0) {
 			for (int c = 0; c < 7; c++)
 				s[c] = b[c];
 		} else {
-			const double nd = (double)(offs[i + 1] - offs[i]);
-			ompl_interpolate(a, b, pwm::dvd((double)j, nd), s);
+			ompl_interpolate(a, b, pwm::dvd((double)j, (double)nd[i]), s);
 		}
 		pwfr::ompl_to_unit(F, s, out + 7 * k);
 	}
@@ -193,29 +233,73 @@ int blocks_for(const pw_world *w, int64_t cnt)
 	return (int)(want < cap ? (want > 0 ? want : 1) : cap);
 }
 
-// Counts, their scan and the batch's total, on the caller's stream.
-int ompl_prepare(pw_world *w, const double *from, const double *to, int64_t n, const OmplSpace &S, cudaStream_t st,
-                 DeviceBuffer &cnt_buf, DeviceBuffer &off_buf, DeviceBuffer &tmp_buf, DeviceBuffer &flag_buf,
-                 uint8_t *valid, int64_t *total, const char *who)
+// Scratch of one call.
+struct OmplScratch {
+	DeviceBuffer nd, cnt, offs, tmp, flag, states, ok;
+};
+
+// OMPL's segment count of every motion and the verdicts' starting values.
+int ompl_counts(const double *from, const double *to, int64_t n, const OmplSpace &S, cudaStream_t st,
+                OmplScratch &B, uint8_t *valid, const char *who)
 {
-	PW_CUDA(cnt_buf.reserve(sizeof(int64_t) * (size_t)n));
-	PW_CUDA(off_buf.reserve(sizeof(int64_t) * (size_t)(n + 1)));
-	PW_CUDA(flag_buf.reserve(sizeof(int)));
-	int64_t *cnt = (int64_t *)cnt_buf.ptr, *offs = (int64_t *)off_buf.ptr;
-	int *flag = (int *)flag_buf.ptr;
+	PW_CUDA(B.nd.reserve(sizeof(int64_t) * (size_t)n));
+	PW_CUDA(B.flag.reserve(sizeof(int)));
+	int *flag = (int *)B.flag.ptr;
 	PW_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
-	PW_CUDA(cudaMemsetAsync(offs, 0, sizeof(int64_t), st));
-	k_ompl_counts<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(from, to, n, S, cnt, valid, flag);
-	size_t tmp_bytes = 0;
-	PW_CUDA(cub::DeviceScan::InclusiveSum(nullptr, tmp_bytes, cnt, offs + 1, n, st));
-	PW_CUDA(tmp_buf.reserve(tmp_bytes > 0 ? tmp_bytes : 1));
-	PW_CUDA(cub::DeviceScan::InclusiveSum(tmp_buf.ptr, tmp_bytes, cnt, offs + 1, n, st));
+	k_ompl_counts<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(from, to, n, S, (int64_t *)B.nd.ptr, valid, flag);
 	int too_long = 0;
-	PW_CUDA(cudaMemcpyAsync(total, offs + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
 	PW_CUDA(cudaMemcpyAsync(&too_long, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
 	PW_CUDA(cudaStreamSynchronize(st));
 	if (too_long)
 		return pw_fail(PW_ERR_INVALID_ARG, std::string(who) + ": a motion needs more than 2^31 - 1 segments");
+	return PW_OK;
+}
+
+// A pass's per-motion counts, their scan (B.offs, n + 1 entries) and its total.
+int ompl_scan(int64_t n, int pass, const uint8_t *valid, cudaStream_t st, OmplScratch &B, int64_t *total)
+{
+	PW_CUDA(B.cnt.reserve(sizeof(int64_t) * (size_t)n));
+	PW_CUDA(B.offs.reserve(sizeof(int64_t) * (size_t)(n + 1)));
+	int64_t *cnt = (int64_t *)B.cnt.ptr, *offs = (int64_t *)B.offs.ptr;
+	k_ompl_pass_counts<<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const int64_t *)B.nd.ptr, valid, n, pass, cnt);
+	PW_CUDA(cudaMemsetAsync(offs, 0, sizeof(int64_t), st));
+	size_t tmp_bytes = 0;
+	PW_CUDA(cub::DeviceScan::InclusiveSum(nullptr, tmp_bytes, cnt, offs + 1, n, st));
+	PW_CUDA(B.tmp.reserve(tmp_bytes > 0 ? tmp_bytes : 1));
+	PW_CUDA(cub::DeviceScan::InclusiveSum(B.tmp.ptr, tmp_bytes, cnt, offs + 1, n, st));
+	PW_CUDA(cudaMemcpyAsync(total, offs + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+	PW_CUDA(cudaStreamSynchronize(st));
+	return PW_OK;
+}
+
+// One pass of the check: its states, window by window, clear the verdicts of the
+// motions they collide on.
+int ompl_pass(pw_world *w, const double *from, const double *to, int64_t n, int pass, uint8_t *valid,
+              cudaStream_t st, OmplScratch &B, int64_t *checked)
+{
+	int64_t total = 0;
+	int rc = ompl_scan(n, pass, valid, st, B, &total);
+	if (rc)
+		return rc;
+	if (total == 0)
+		return PW_OK;
+	const int64_t win = total < WINDOW ? total : WINDOW;
+	PW_CUDA(B.states.reserve(sizeof(double) * 7 * (size_t)win));
+	PW_CUDA(B.ok.reserve((size_t)win));
+	const int64_t *nd = (const int64_t *)B.nd.ptr, *offs = (const int64_t *)B.offs.ptr;
+	double *states = (double *)B.states.ptr;
+	uint8_t *ok = (uint8_t *)B.ok.ptr;
+	const pwfr::Frame F = world_frame(w);
+	for (int64_t first = 0; first < total; first += win) {
+		const int64_t cnt = total - first < win ? total - first : win;
+		k_ompl_states<<<blocks_for(w, cnt), 256, 0, st>>>(from, to, n, nd, offs, pass, first, cnt, F, states);
+		PW_CUDA(cudaGetLastError());
+		if ((rc = pw_states_valid(w, states, cnt, ok, (void *)st)))
+			return rc;
+		k_ompl_reduce<<<blocks_for(w, cnt), 256, 0, st>>>(ok, first, cnt, offs, n, valid);
+		PW_CUDA(cudaGetLastError());
+	}
+	*checked += total;
 	return PW_OK;
 }
 
@@ -251,30 +335,17 @@ extern "C" int pw_ompl_check_motions(pw_world *w, const double *from, const doub
 		return PW_OK;
 	PW_CUDA(cudaSetDevice(w->device));
 	cudaStream_t st = (cudaStream_t)stream;
-	DeviceBuffer cnt_buf, off_buf, tmp_buf, flag_buf, state_buf, ok_buf;
-	int64_t total = 0;
-	if ((rc = ompl_prepare(w, from, to, n, S, st, cnt_buf, off_buf, tmp_buf, flag_buf, valid, &total, who)))
+	OmplScratch B;
+	if ((rc = ompl_counts(from, to, n, S, st, B, valid, who)))
 		return rc;
-	const int64_t win = total < WINDOW ? total : WINDOW;
-	PW_CUDA(state_buf.reserve(sizeof(double) * 7 * (size_t)win));
-	PW_CUDA(ok_buf.reserve((size_t)win));
-	const int64_t *offs = (const int64_t *)off_buf.ptr;
-	double *states = (double *)state_buf.ptr;
-	uint8_t *ok = (uint8_t *)ok_buf.ptr;
-	const pwfr::Frame F = world_frame(w);
-	for (int64_t first = 0; first < total; first += win) {
-		const int64_t cnt = total - first < win ? total - first : win;
-		k_ompl_states<<<blocks_for(w, cnt), 256, 0, st>>>(from, to, n, offs, first, cnt, F, states);
-		PW_CUDA(cudaGetLastError());
-		if ((rc = pw_states_valid(w, states, cnt, ok, stream)))
+	int64_t checked = 0;
+	for (int pass : { PASS_TARGET, PASS_MID, PASS_REST })
+		if ((rc = ompl_pass(w, from, to, n, pass, valid, st, B, &checked)))
 			return rc;
-		k_ompl_reduce<<<blocks_for(w, cnt), 256, 0, st>>>(ok, first, cnt, offs, n, valid);
-		PW_CUDA(cudaGetLastError());
-	}
 	// the scratch is freed on return: the batch's work must be done by then
 	PW_CUDA(cudaStreamSynchronize(st));
 	if (states_checked)
-		*states_checked = total;
+		*states_checked = checked;
 	return PW_OK;
 }
 
@@ -297,19 +368,23 @@ extern "C" int pw_ompl_motion_states(pw_world *w, const double *from, const doub
 		return PW_OK;
 	PW_CUDA(cudaSetDevice(w->device));
 	cudaStream_t st = (cudaStream_t)stream;
-	DeviceBuffer cnt_buf, off_buf, tmp_buf, flag_buf, valid_buf;
+	OmplScratch B;
+	DeviceBuffer valid_buf;
 	PW_CUDA(valid_buf.reserve((size_t)n));
-	if ((rc = ompl_prepare(w, from, to, n, S, st, cnt_buf, off_buf, tmp_buf, flag_buf, (uint8_t *)valid_buf.ptr,
-	                       total, who)))
+	uint8_t *valid = (uint8_t *)valid_buf.ptr;
+	if ((rc = ompl_counts(from, to, n, S, st, B, valid, who)))
+		return rc;
+	if ((rc = ompl_scan(n, PASS_ALL, valid, st, B, total)))
 		return rc;
 	if (offsets)
-		PW_CUDA(cudaMemcpyAsync(offsets, off_buf.ptr, sizeof(int64_t) * (size_t)(n + 1), cudaMemcpyDeviceToDevice,
+		PW_CUDA(cudaMemcpyAsync(offsets, B.offs.ptr, sizeof(int64_t) * (size_t)(n + 1), cudaMemcpyDeviceToDevice,
 		                        st));
 	if (*total > capacity) {
 		PW_CUDA(cudaStreamSynchronize(st));
 		return pw_fail(PW_ERR_CAPACITY, std::string(who) + ": more states than the capacity");
 	}
-	k_ompl_states<<<blocks_for(w, *total), 256, 0, st>>>(from, to, n, (const int64_t *)off_buf.ptr, 0, *total,
+	k_ompl_states<<<blocks_for(w, *total), 256, 0, st>>>(from, to, n, (const int64_t *)B.nd.ptr,
+	                                                    (const int64_t *)B.offs.ptr, PASS_ALL, 0, *total,
 	                                                    world_frame(w), states);
 	PW_CUDA(cudaGetLastError());
 	PW_CUDA(cudaStreamSynchronize(st));

@@ -58,6 +58,21 @@ def _motions(P, n, seed, sigma=2.0):
     return np.concatenate(A), np.concatenate(B)
 
 
+def _expected_checks(ok, counts):
+    """States the three passes check, given every state's verdict in listing order:
+    each target, the middle state (k = nd // 2) of motions whose target is free,
+    and the rest of the motions whose target and middle state are free."""
+    starts = np.concatenate([[0], np.cumsum(counts)[:-1]])
+    total = 0
+    for s, m in zip(starts, counts):
+        total += 1
+        if m >= 2 and ok[s]:
+            total += 1
+            if m >= 3 and ok[s + m // 2]:
+                total += m - 2
+    return total
+
+
 def _oracle_states(O, uw, A, B, lo, hi, cdres):
     per = [O.ompl_motion_states(a, b, lo, hi, cdres) for a, b in zip(A, B)]
     counts = np.array([p.shape[0] for p in per])
@@ -85,7 +100,7 @@ def test_verdicts_match_the_oracle(alpha, oracle_mod):
     U, counts = _oracle_states(oracle_mod, uw, A, B, lo, hi, CDRES)
     ok = ow.is_valid(U).astype(bool)
     want = np.logical_and.reduceat(ok, np.concatenate([[0], np.cumsum(counts)[:-1]])).astype(np.int32)
-    assert got.dtype == np.int32 and checked == counts.sum()
+    assert got.dtype == np.int32 and checked == _expected_checks(ok, counts) < counts.sum()
     assert np.array_equal(got, want)
     assert 0 < got.sum() < len(got)
     # the driver object gives the same answers once its bounds and resolution are set
@@ -99,9 +114,9 @@ def test_verdicts_match_the_oracle(alpha, oracle_mod):
 
 
 def test_windowed_batch_agrees_with_per_state_verdicts(alpha):
-    """More than one window of states (4M): every motion's verdict is the AND of
-    the engine's verdicts on the states pw_ompl_motion_states lists for it,
-    including motions whose states straddle a window boundary."""
+    """More than one window of states (4M) in the listing: every motion's verdict
+    is the AND of the engine's verdicts on the states pw_ompl_motion_states lists
+    for it, and the passes check exactly the states their early exits leave."""
     from puzzletunneldiscovery_gb300 import ompl_compat as OC
     uw, ow, P, lo, hi = alpha
     A, B = _motions(P, 12000, seed=3, sigma=6.0)
@@ -114,7 +129,7 @@ def test_windowed_batch_agrees_with_per_state_verdicts(alpha):
     bad = torch.zeros(len(A), dtype=torch.int64, device=ok.device).index_add_(0, owner, 1 - ok)
     want = (bad == 0).to(torch.int32).cpu().numpy()
     got, checked = OC.check_motions_discrete(uw, A, B, lo, hi, cdres)
-    assert checked == states.shape[0]
+    assert checked == _expected_checks(ok.cpu().numpy(), counts.cpu().numpy())
     assert np.array_equal(got, want)
     assert 0 < got.sum() < len(got)
 
