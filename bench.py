@@ -407,8 +407,13 @@ def cpu_baseline(work, target_s=12.0):
             break
         n = min(work.n, max(n * 2, int(n * target_s / max(dt, 1e-3) * 1.1)))
     unit_name = "segments" if work.name == "segments" else "states"
+    # the same oracle on one thread, on the sample's first part (about a quarter of target_s)
+    n1 = max(1, min(n, int(n * (target_s / 4.0) / max(dt * cores, 1e-3))))
+    checks1, dt1 = work.cpu(ow, 0, n1, 1)
     return {"value": float(checks) / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "first %d %s of the rank-0 batch (%d reference checks, %.1f s)" % (n, unit_name, checks, dt)}
+            "sample": "first %d %s of the rank-0 batch (%d reference checks, %.1f s)" % (n, unit_name, checks, dt),
+            "single_thread": {"value": float(checks1) / max(dt1, 1e-9), "unit": UNIT, "cores": 1,
+                              "sample": "first %d %s (%d reference checks, %.1f s)" % (n1, unit_name, checks1, dt1)}}
 
 
 def run_reference(args):
