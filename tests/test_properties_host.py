@@ -31,9 +31,19 @@ def _clear(V, U):
     return True
 
 
+def _jitter(V, U):
+    """A deterministic 1e-4 jitter of both triangles: hypothesis favours round
+    coordinates, whose exact touches (an edge meeting an edge, not only a vertex
+    on a plane) have measure zero once the pair is moved off them."""
+    flat = tuple(float(x) for t in (V, U) for p in t for x in p)
+    rng = np.random.default_rng(abs(hash(flat)) % (2 ** 32))
+    return (np.asarray(V) + rng.uniform(-1e-4, 1e-4, (3, 3)), np.asarray(U) + rng.uniform(-1e-4, 1e-4, (3, 3)))
+
+
 @settings(max_examples=300, deadline=None)
 @given(tri, tri)
 def test_tri_tri_symmetric_and_cyclic(oracle_mod, V, U):
+    V, U = _jitter(V, U)
     if not (_generic(V) and _generic(U) and _clear(V, U)):
         return
     V, U = [np.array(v) for v in V], [np.array(u) for u in U]
