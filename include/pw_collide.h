@@ -244,11 +244,12 @@ PW_API int pw_ompl_check_motions(pw_world *w, const double *from, const double *
                                  const double lo[3], const double hi[3], double cdres, uint8_t *valid,
                                  int64_t *states_checked, void *stream);
 
-/* device in, synchronous: the states pw_ompl_check_motions checks, in the unit frame.
+/* device in, synchronous: every state pw_ompl_check_motions may check, in the unit frame.
  * Motion i's states are rows offsets[i] .. offsets[i + 1] - 1 of `states`: first to[i], then the
- * interpolated states k = 1 .. nd - 1.  offsets (device, n + 1 entries) may be NULL.  *total = the
- * number of states; PW_ERR_CAPACITY (with *total set and nothing written) when it exceeds
- * capacity.  No counterpart in the reference: it exposes what the check looks at. */
+ * interpolated states k = 1 .. nd - 1 (the check's passes skip those of motions found colliding
+ * earlier).  offsets (device, n + 1 entries) may be NULL.  *total = the number of states;
+ * PW_ERR_CAPACITY when it exceeds capacity, with *total and offsets written and `states`
+ * untouched.  No counterpart in the reference: it exposes what the check looks at. */
 PW_API int pw_ompl_motion_states(pw_world *w, const double *from, const double *to, int64_t n,
                                  const double lo[3], const double hi[3], double cdres, int64_t capacity,
                                  double *states, int64_t *offsets, int64_t *total, void *stream);
