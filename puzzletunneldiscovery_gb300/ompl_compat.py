@@ -127,9 +127,9 @@ def check_motions_discrete(uw: UnitWorld, qs0, qs1, lo, hi, cdres: float):
 
 
 def motion_states(uw: UnitWorld, qs0, qs1, lo, hi, cdres: float):
-    """The unit-frame states check_motions_discrete checks: (states [T, 7] on the
-    device, offsets [m + 1]); motion i's rows are offsets[i] .. offsets[i + 1] - 1,
-    its target first."""
+    """Every unit-frame state check_motions_discrete may check: (states [T, 7] on
+    the device, offsets [m + 1]); motion i's rows are offsets[i] .. offsets[i + 1] - 1,
+    its target first, then k = 1 .. nd - 1."""
     lo, hi = _bb(lo, hi)
     _, m, ta, tb = _motion_args(uw, qs0, qs1)
     dev = uw._device
@@ -139,14 +139,15 @@ def motion_states(uw: UnitWorld, qs0, qs1, lo, hi, cdres: float):
     dp = ctypes.POINTER(ctypes.c_double)
     total = ctypes.c_int64()
     args = (uw._h, ta.data_ptr(), tb.data_ptr(), m, lo.ctypes.data_as(dp), hi.ctypes.data_as(dp), float(cdres))
-    stream = torch.cuda.current_stream(dev).cuda_stream
+    stream = _stream_of(dev)
     dummy = torch.zeros((1, 7), dtype=torch.float64, device=dev)
-    rc = uw._L.pw_ompl_motion_states(*args, 0, dummy.data_ptr(), offs.data_ptr(), ctypes.byref(total), stream)
+    # first call sizes the listing (PW_ERR_CAPACITY at capacity 0), the second fills it
+    rc = uw._L.pw_ompl_motion_states(*args, 0, dummy.data_ptr(), offs.data_ptr(), ctypes.pointer(total), stream)
     if rc not in (_lib.PW_OK, _lib.PW_ERR_CAPACITY):
         _lib.check(rc, "motion_states")
     states = torch.empty((max(int(total.value), 1), 7), dtype=torch.float64, device=dev)
     _lib.check(uw._L.pw_ompl_motion_states(*args, int(total.value), states.data_ptr(), offs.data_ptr(),
-                                           ctypes.byref(total), stream), "motion_states")
+                                           ctypes.pointer(total), stream), "motion_states")
     return states[:int(total.value)], offs
 
 

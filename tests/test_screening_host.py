@@ -184,3 +184,40 @@ def test_screening_with_an_ompl_driver_checks_ompl_frame_key_pairs(tmp_path):
     out, checked = OC.check_motions_discrete(w, keys[2:8], keys[3:7], [-1, -2, -3], [4, 5, 6], 0.02)
     want = ((np.arange(2, 6) + np.arange(3, 7)) % 3 != 0).astype(np.int32)
     assert np.array_equal(out, np.concatenate([want, [0, 0]])) and checked == 20
+
+
+class _FakeListingLib:
+    """pw_ompl_motion_states over host memory: motion i lists i + 1 states, state r
+    of motion i is filled with 10 i + r; refuses (PW_ERR_CAPACITY) below the total."""
+
+    def __init__(self):
+        self.capacities = []
+
+    def pw_ompl_motion_states(self, h, pa, pb, m, lo, hi, cdres, capacity, pstates, poffs, ptotal, stream):
+        import ctypes
+        counts = np.arange(1, m + 1, dtype=np.int64)
+        offs = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+        ctypes.memmove(poffs, offs.ctypes.data, 8 * (m + 1))
+        ptotal[0] = int(offs[-1])
+        self.capacities.append(capacity)
+        if capacity < offs[-1]:
+            return 5
+        rows = np.zeros((int(offs[-1]), 7))
+        for i in range(m):
+            rows[offs[i]:offs[i + 1], 0] = 10 * i + np.arange(counts[i])
+        ctypes.memmove(pstates, rows.ctypes.data, rows.nbytes)
+        return 0
+
+
+def test_motion_state_listing_sizes_then_fills():
+    from puzzletunneldiscovery_gb300 import ompl_compat as OC
+    w = _FakeOmplWorld()
+    w._L = _FakeListingLib()
+    q = np.zeros((4, 7))
+    q[:, 6] = 1.0
+    states, offs = OC.motion_states(w, q, q, [-1, -1, -1], [1, 1, 1], 0.01)
+    assert w._L.capacities == [0, 10]
+    assert offs.tolist() == [0, 1, 3, 6, 10] and states.shape == (10, 7)
+    assert states[:, 0].tolist() == [0, 10, 11, 20, 21, 22, 30, 31, 32, 33]
+    empty, eoffs = OC.motion_states(w, np.zeros((0, 7)), np.zeros((0, 7)), [-1, -1, -1], [1, 1, 1], 0.01)
+    assert empty.shape == (0, 7) and eoffs.tolist() == [0]
