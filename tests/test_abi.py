@@ -121,3 +121,20 @@ def test_every_entry_point_rejects_null_arguments(built_lib):
     for name, (rc, msg) in res.items():
         assert rc != _lib.PW_OK, name
         assert msg, name
+
+
+@pytest.mark.parametrize("lang,std", [("c", "-std=c99"), ("c++", "-std=c++11")])
+def test_headers_compile_standalone(lang, std, tmp_path):
+    """The C-ABI headers are usable from plain C99 and C++11 callers (a cgo / JNI /
+    ctypes binding compiles against them), with every warning enabled."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc" if lang == "c" else "g++")
+    if cc is None:
+        pytest.skip("no host compiler")
+    src = tmp_path / ("use." + ("c" if lang == "c" else "cc"))
+    src.write_text('#include "pw_collide.h"\n#include "pw_mlp.h"\n'
+                   "int use(void) { return pw_last_error() != 0 ? PW_OK : PW_ERR_INTERNAL; }\n")
+    r = subprocess.run([cc, "-fsyntax-only", std, "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
