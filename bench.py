@@ -375,15 +375,16 @@ class Work:
         return uw.first_contact_steps_host(ha, hb, DELTA)
 
     def cpu(self, ow, lo, hi, threads):
-        """(reference checks, seconds) of the oracle on units lo..hi."""
+        """(reference checks, seconds, result) of the oracle on units lo..hi; the
+        result is in the GPU call's encoding (first-contact steps, or 1 = free)."""
         t0 = time.perf_counter()
         if self.name == "plate":
-            ow.is_valid(self.q0[lo:hi], nthreads=threads)
+            res = ow.is_valid(self.q0[lo:hi], nthreads=threads).astype(np.uint8)
             checks = hi - lo
         else:
-            _, c = ow.segments_first_contact(self.q0[lo:hi], self.q1[lo:hi], DELTA, mode=0, nthreads=threads)
+            res, c = ow.segments_first_contact(self.q0[lo:hi], self.q1[lo:hi], DELTA, mode=0, nthreads=threads)
             checks = int(c.sum())
-        return checks, time.perf_counter() - t0
+        return checks, time.perf_counter() - t0, res
 
     def bytes_in(self):
         return self.n * 56 * (1 if self.name == "plate" else 2)
@@ -392,8 +393,10 @@ class Work:
         return self.n * (1 if self.name == "plate" else 4)
 
 
-def cpu_baseline(work, target_s=12.0):
-    """The oracle (CPU restatement of the reference path) on a bounded sample, all host threads."""
+def cpu_baseline(work, gpu_result, target_s=12.0):
+    """The oracle (CPU restatement of the reference path) on a bounded sample of
+    the timed batch, all host threads, and its results compared with the GPU's
+    on that sample.  Returns (cpu_baseline dict, parity dict)."""
     from oracle import oracle as O
     O.build()
     Ve, Fe, Vr, Fr = _meshes(work.name)
@@ -402,18 +405,26 @@ def cpu_baseline(work, target_s=12.0):
     n = 128 if work.name == "segments" else 8192
     while True:
         n = min(n, work.n)
-        checks, dt = work.cpu(ow, 0, n, cores)
+        checks, dt, res = work.cpu(ow, 0, n, cores)
         if dt >= target_s or n >= work.n:
             break
         n = min(work.n, max(n * 2, int(n * target_s / max(dt, 1e-3) * 1.1)))
     unit_name = "segments" if work.name == "segments" else "states"
     # the same oracle on one thread, on the sample's first part (about a quarter of target_s)
     n1 = max(1, min(n, int(n * (target_s / 4.0) / max(dt * cores, 1e-3))))
-    checks1, dt1 = work.cpu(ow, 0, n1, 1)
-    return {"value": float(checks) / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "first %d %s of the rank-0 batch (%d reference checks, %.1f s)" % (n, unit_name, checks, dt),
-            "single_thread": {"value": float(checks1) / max(dt1, 1e-9), "unit": UNIT, "cores": 1,
-                              "sample": "first %d %s (%d reference checks, %.1f s)" % (n1, unit_name, checks1, dt1)}}
+    checks1, dt1, res1 = work.cpu(ow, 0, n1, 1)
+    g = np.asarray(gpu_result[:n])
+    mism = int((g != res).sum()) + int((g[:n1] != res1).sum())
+    what = ("first-contact step index (or -1) of every segment" if work.name == "segments"
+            else "is_valid_state verdict of every state")
+    parity = {"mismatches": mism, "mismatch_sample": int(n), "compared": what,
+              "sample": "first %d %s of the timed batch (the CPU-baseline sample), against the timed steps' "
+                        "results" % (n, unit_name)}
+    cpu = {"value": float(checks) / dt, "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": "first %d %s of the rank-0 batch (%d reference checks, %.1f s)" % (n, unit_name, checks, dt),
+           "single_thread": {"value": float(checks1) / max(dt1, 1e-9), "unit": UNIT, "cores": 1,
+                             "sample": "first %d %s (%d reference checks, %.1f s)" % (n1, unit_name, checks1, dt1)}}
+    return cpu, parity
 
 
 def run_reference(args):
@@ -431,7 +442,7 @@ def run_reference(args):
     times, checks = [], []
     for it in range(args.warmup + args.steps):
         lo = (it * sample) % max(1, work.n - sample)
-        c, dt = work.cpu(ow, lo, lo + sample, cores)
+        c, dt, _ = work.cpu(ow, lo, lo + sample, cores)
         if it >= args.warmup:
             times.append(dt)
             checks.append(c)
@@ -569,30 +580,20 @@ def run_ours(args):
         return
 
     # roofline of the dominant (traversal) kernel
-    trav_ms = sum(s["traverse_ms"] for s in stats) / len(stats)
-    node = sum(s["node_tests"] for s in stats) / len(stats)
-    leaf = sum(s["leaf_tests"] for s in stats) / len(stats)
-    io = work.bytes_in() + work.bytes_out()
-    alg_bytes = node * BYTES_NODE_PAIR + leaf * BYTES_LEAF_PAIR + io
-    achieved = alg_bytes / (trav_ms / 1e3) / 1e9
-    peak, peak_kind = _peaks()
-    traffic = None
-    tps = _traffic_per_segment()
-    if tps is not None and args.workload == "segments":
-        traffic = tps * args.n
-    kernel = "k_segments" if args.workload == "segments" else "k_states"
-    issue = _profile_value("k_segments_traffic.txt" if args.workload == "segments" else "k_states_plate_traffic.txt",
-                           "smsp_issue_active_pct")
-    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": traffic, "kernel": kernel, "kernel_ms": trav_ms,
-            "peak_source": peak_kind, "algorithmic_bytes": alg_bytes,
-            "served_from": "L1/L2 (BVHs resident); DRAM moves only the inputs",
-            "sm_issue_active_pct_ncu": issue}
-    cpu = None
-    if ws == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(work, target_s=args.cpu_seconds)
-    last = stats[-1]
+    roof = traversal_roofline(stats, work.bytes_in() + work.bytes_out(), args.n, args.workload)
     fc = f.cpu().numpy()
+    cpu, parity = None, None
+    if ws == 1 and not args.no_cpu_baseline:
+        cpu, parity = cpu_baseline(work, fc, target_s=args.cpu_seconds)
+    sur = None
+    if args.workload == "segments" and not args.no_surrogate_arm:
+        # the second half of the metric: verified free samples per second, surrogate-guided
+        # against plain, on the same meshes (config: 50M training labels, 200M candidates, top 10 %)
+        sur = surrogate_measure(args, local, rank, WORKLOADS["surrogate"][2], steps=min(args.steps, 10),
+                                warmup=min(args.warmup, 3), with_cpu=(ws == 1 and not args.no_cpu_baseline),
+                                e2e=False)
+        sur = surrogate_summary(sur)
+    last = stats[-1]
     if args.workload == "segments":
         config = {"workload": "segments_first_contact/interlocking_tori",
                   "meshes": "torus R=1 r=0.25 64x32 (4096 tris) x2, interlocked",
@@ -619,30 +620,83 @@ def run_ours(args):
             # segments: bounds, set-up, anchors, rounds, traversal, re-test, finalise (CUB's scan and
             # sort not counted); states: traversal, re-test
             "gpu_launches": (7 if args.workload == "segments" else 2) * args.steps,
-            "detail": dict({"reference_checks_per_step": tot_checks / args.steps,
+            "detail": dict({"mismatches": parity["mismatches"] if parity else None,
+                            "mismatch_sample": parity["mismatch_sample"] if parity else 0,
+                            "parity": parity,
+                            "reference_checks_per_step": tot_checks / args.steps,
                             "gpu_queries_per_step": last["queries"], "node_tests": last["node_tests"],
                             "leaf_tests": last["leaf_tests"], "fp64_retests": last["retests"],
                             "fp64_retest_rate_per_leaf": last["retests"] / max(1, last["leaf_tests"]),
                             "inline_retests": last["inline_retests"], "retest_ms": last["retest_ms"],
                             "step_ms": step_ms, "autotune": tuned, "graph_replay_ms_per_step": graph_ms},
                            **extra)}
-    print(json.dumps(line))
+    if sur is not None:
+        line["detail"]["surrogate"] = sur
+    print(json.dumps(line), flush=True)
     if ws > 1:
         dist.barrier()
         dist.destroy_process_group()
+    bad = parity["mismatches"] if parity else 0
+    if sur is not None:
+        bad += (sur["mismatches"] or 0) + sur["false_free_accepted"] + (sur["false_free_oracle"] or 0)
+    if bad:
+        print("verdict mismatches against the oracle: %d" % bad, file=sys.stderr)
+        sys.exit(3)
 
 
-def run_surrogate(args):
+def traversal_roofline(stats, io_bytes, n_units, workload):
+    """Roofline record of the traversal kernel.  The algorithmic DRAM bytes are
+    the queries' inputs and results; the BVH nodes and triangles the tests read
+    are L2-resident, so those bytes are reported apart (cache_served), and the
+    binding limit, SM instruction issue, is given with its measured fraction
+    from the committed ncu capture."""
+    trav_ms = sum(s["traverse_ms"] for s in stats) / len(stats)
+    node = sum(s["node_tests"] for s in stats) / len(stats)
+    leaf = sum(s["leaf_tests"] for s in stats) / len(stats)
+    sec = trav_ms / 1e3
+    peak, peak_kind = _peaks()
+    achieved = io_bytes / sec / 1e9
+    seg = workload != "plate"
+    # DRAM traffic per unit from the committed capture of this workload's kernel (none for the
+    # narrow-passage validation, whose segments run on the plate meshes); issue utilisation from
+    # the capture of the same kernel
+    prof = "k_segments_traffic.txt" if seg else "k_states_plate_traffic.txt"
+    per_unit = None
+    if workload == "segments":
+        per_unit = _profile_value(prof, "dram_bytes_per_segment")
+    elif workload == "plate":
+        per_unit = _profile_value(prof, "dram_bytes_per_state")
+    traffic = per_unit * n_units if per_unit is not None else None
+    issue = _profile_value(prof, "smsp_issue_active_pct")
+    cache_bytes = node * BYTES_NODE_PAIR + leaf * BYTES_LEAF_PAIR
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic,
+            "traffic_frac": (traffic / sec / 1e9 / peak) if traffic is not None else None,
+            "kernel": "k_segments" if seg else "k_states", "kernel_ms": trav_ms, "peak_source": peak_kind,
+            "algorithmic_bytes": io_bytes,
+            "algorithmic_bytes_what": "the queries' inputs and results (%s)" %
+                                      ("two 56 B states in, a 4 B step out" if seg else "a 56 B state in, 1 B out"),
+            "limiter": "SM instruction issue: BVH nodes and triangles are L2-resident, DRAM moves only the queries",
+            "limiter_frac": issue / 100.0 if issue is not None else None,
+            "limiter_source": "smsp__issue_active of the committed ncu capture (profiles/)",
+            "cache_served": {"bytes": cache_bytes, "achieved": cache_bytes / sec / 1e9, "unit": "GB/s",
+                             "what": "node-pair tests x %d B + leaf tests x %d B, read from L1/L2"
+                                     % (BYTES_NODE_PAIR, BYTES_LEAF_PAIR)}}
+
+
+def surrogate_measure(args, local, rank, n, steps, warmup, with_cpu, e2e=True):
     """Learned proposal on the interlocking tori: train on exact labels, then
     per step rank `n` uniform candidates with the network, check the top
     fraction exactly and count the verified free samples.  The plain arm
-    checks every candidate exactly."""
+    checks every candidate exactly.  Returns every figure of the measurement;
+    with_cpu adds the oracle on the host cores over a sample of the same
+    candidates, whose verdicts are compared with the plain arm's, and the
+    oracle's re-check of a sample of the accepted set."""
     import torch
 
     import puzzletunneldiscovery_gb300 as pw
     from puzzletunneldiscovery_gb300 import surrogate as S
 
-    ws, rank, local = _dist_env()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     Ve, Fe, Vr, Fr = _meshes("surrogate")
@@ -653,7 +707,7 @@ def run_surrogate(args):
     uw.angleModel(0.0, 0.0)
     gen = torch.Generator(device=dev)
     gen.manual_seed(1000 + rank)
-    draw = lambda n: S.uniform_states_device(n, -2.0, 2.0, uw.scene_scale, gen, dev)  # noqa: E731
+    draw = lambda m: S.uniform_states_device(m, -2.0, 2.0, uw.scene_scale, gen, dev)  # noqa: E731
     stream = torch.cuda.current_stream(dev)
 
     # training on exact labels (timed as its own phase)
@@ -667,32 +721,33 @@ def run_surrogate(args):
     torch.cuda.synchronize(dev)
     train_ms = t0.elapsed_time(t1)
 
-    cand = draw(args.n)                       # resident candidates (not timed)
-    prob = torch.empty(args.n, dtype=torch.float32, device=dev)
+    cand = draw(n)                            # resident candidates (not timed)
+    prob = torch.empty(n, dtype=torch.float32, device=dev)
     # exact labels of a 4M sample: precision / recall of the network as a free-space predictor
     sample = cand[: 1 << 22]
     exact = uw.is_valid_states(sample)
     prec, rec = S.precision_recall(net.predict(sample), exact)
     net.check()
+    m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
     def guided(frac=args.top_frac):
         net.score(cand, out=prob)
         m1.record(stream)
-        sel = S.select_top(prob, cand, int(round(frac * args.n)))
+        sel = S.select_top(prob, cand, int(round(frac * n)))
         ok = uw.is_valid_states(sel)
         return sel, ok
 
     def plain():
         return uw.is_valid_states(cand)
 
-    m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         guided()
         plain()
     torch.cuda.synchronize(dev)
     g_ms, p_ms, mlp_ms, g_free, p_free, g_checked, false_free = [], [], [], 0, 0, 0, 0
+    accepted = None
     with ClockSampler(local) as clk:
-        for i in range(args.steps):
+        for i in range(steps):
             s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             s0.record(stream)
             m0.record(stream)
@@ -706,7 +761,8 @@ def run_surrogate(args):
             g_checked += int(sel.shape[0])
             if i == 0:
                 # every accepted sample was checked exactly; re-check the accepted set once
-                false_free = int((~uw.is_valid_states(sel[ok])).sum())
+                accepted = sel[ok]
+                false_free = int((~uw.is_valid_states(accepted)).sum())
             s0.record(stream)
             okp = plain()
             nfree = okp.sum()
@@ -732,41 +788,85 @@ def run_surrogate(args):
                                 "precision": int(nfree) / max(1, sel.shape[0]),
                                 "over_plain": int(nfree) / (ms / 1e3) / plain_value}
 
-    # end to end: candidates from pinned host memory, accepted states back to the host
-    hc = cand[: args.e2e_n].cpu().pin_memory()
-    e2e_ms, e2e_free, h2d, d2h = 0.0, 0, 0, 0
-    for i in range(args.steps):
-        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s0.record(stream)
-        dc = hc.to(dev, non_blocking=True)
-        pr = net.score(dc)
-        sel = S.select_top(pr, dc, int(round(args.top_frac * dc.shape[0])))
-        acc = sel[uw.is_valid_states(sel)]
-        hacc = acc.cpu()
-        s1.record(stream)
-        torch.cuda.synchronize(dev)
-        e2e_ms += s0.elapsed_time(s1)
-        e2e_free += hacc.shape[0]
-        h2d, d2h = hc.numel() * 8, hacc.numel() * 8
-    e2e_value = e2e_free / (e2e_ms / 1e3)
-    if rank != 0:
-        return
+    out = {"value": value, "plain_value": plain_value, "n": n, "steps": steps, "warmup": warmup,
+           "top_frac": args.top_frac,
+           "g_ms": g_ms, "p_ms": p_ms, "g_free": g_free, "p_free": p_free, "g_checked": g_checked,
+           "precision": prec, "recall": rec, "false_free": false_free, "train_ms": train_ms, "rep": rep,
+           "sweep": sweep, "clocks": clk.summary(), "e2e": None, "cpu": None, "parity": None}
+
+    if e2e:
+        # end to end: candidates from pinned host memory, accepted states back to the host
+        e2e_n = min(args.e2e_n, n)
+        hc = cand[:e2e_n].cpu().pin_memory()
+        e2e_ms, e2e_free, h2d, d2h = 0.0, 0, 0, 0
+        for i in range(steps):
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            dc = hc.to(dev, non_blocking=True)
+            pr = net.score(dc)
+            sel = S.select_top(pr, dc, int(round(args.top_frac * dc.shape[0])))
+            acc = sel[uw.is_valid_states(sel)]
+            hacc = acc.cpu()
+            s1.record(stream)
+            torch.cuda.synchronize(dev)
+            e2e_ms += s0.elapsed_time(s1)
+            e2e_free += hacc.shape[0]
+            h2d, d2h = hc.numel() * 8, hacc.numel() * 8
+        out["e2e"] = {"value": e2e_free / (e2e_ms / 1e3), "unit": "samples/s", "h2d_bytes_per_step": h2d,
+                      "d2h_bytes_per_step": d2h, "candidates_per_step": e2e_n}
 
     mlp_kernel_ms = sum(mlp_ms) / len(mlp_ms)
-    achieved = MLP_FLOP_PER_ROW * args.n / (mlp_kernel_ms / 1e3) / 1e12
+    achieved = MLP_FLOP_PER_ROW * n / (mlp_kernel_ms / 1e3) / 1e12
     peak, peak_kind = _bf16_peak()
-    traffic = None
     tpr = _profile_value("k_mlp_forward_tc_traffic.txt", "dram_bytes_per_row")
-    if tpr is not None:
-        traffic = tpr * args.n
-    roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-            "traffic": traffic, "kernel": "k_mlp_forward_tc", "kernel_ms": mlp_kernel_ms,
-            "peak_source": peak_kind, "algorithmic_flop": MLP_FLOP_PER_ROW * args.n}
-    cpu = None
-    if ws == 1 and not args.no_cpu_baseline:
-        cpu = _cpu_plain_sampling(uw.scene_scale, args.cpu_seconds)
+    out["mlp_ms"] = mlp_kernel_ms
+    out["roof"] = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                   "frac": achieved / peak, "traffic": tpr * n if tpr is not None else None,
+                   "kernel": "k_mlp_forward_tc", "kernel_ms": mlp_kernel_ms, "peak_source": peak_kind,
+                   "algorithmic_flop": MLP_FLOP_PER_ROW * n}
+    if with_cpu:
+        okp_host = okp.cpu().numpy()
+        out["cpu"], out["parity"] = _cpu_plain_sampling(cand, okp_host, args.cpu_seconds)
+        # the oracle re-checks a sample of the accepted set: none may be in collision
+        from oracle import oracle as O
+        ow = O.OracleWorld(Ve, Fe, Vr, Fr)
+        acc = accepted[:200_000].cpu().numpy()
+        out["false_free_oracle"] = int((~ow.is_valid(acc, nthreads=os.cpu_count() or 1)).sum())
+        out["false_free_oracle_sample"] = int(acc.shape[0])
+    return out
+
+
+def surrogate_summary(m):
+    """The surrogate measurement as a compact dict (the headline line's detail)."""
+    b = m["sweep"]
+    return {"metric": WORKLOADS["surrogate"][0], "unit": "samples/s",
+            "config": {"candidates_per_step": m["n"], "top_fraction": m["top_frac"], "train_labels": m["rep"].labels,
+                       "batch": 65536, "lr": 1e-3, "network": "9 -> 256x4 SiLU -> 1 sigmoid, BF16"},
+            "guided_verified_free_per_s": m["value"], "plain_verified_free_per_s": m["plain_value"],
+            "guided_over_plain": m["value"] / m["plain_value"],
+            "guided_ms_per_step": sum(m["g_ms"]) / len(m["g_ms"]),
+            "plain_ms_per_step": sum(m["p_ms"]) / len(m["p_ms"]), "mlp_ms_per_step": m["mlp_ms"],
+            "steps": m["steps"], "precision_at_0.5": m["precision"], "recall_at_0.5": m["recall"],
+            "precision_top_fraction": m["g_free"] / max(1, m["g_checked"]),
+            "false_free_accepted": m["false_free"], "false_free_oracle": m.get("false_free_oracle"),
+            "false_free_oracle_sample": m.get("false_free_oracle_sample", 0),
+            "mismatches": m["parity"]["mismatches"] if m["parity"] else None,
+            "mismatch_sample": m["parity"]["mismatch_sample"] if m["parity"] else 0,
+            "train_ms": m["train_ms"], "roofline": m["roof"], "cpu_baseline": m["cpu"],
+            "top_fraction_sweep": {k: v["over_plain"] for k, v in b.items()}, "clocks": m["clocks"]}
+
+
+def run_surrogate(args):
+    """--workload surrogate: the learned proposal's own line."""
+    ws, rank, local = _dist_env()
+    m = surrogate_measure(args, local, rank, args.n, args.steps, args.warmup,
+                          with_cpu=(ws == 1 and not args.no_cpu_baseline))
+    if rank != 0:
+        return
+    rep = m["rep"]
+    value, plain_value = m["value"], m["plain_value"]
     line = {"metric": WORKLOADS["surrogate"][0], "value": value, "unit": "samples/s", "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(g_ms) / len(g_ms),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(m["g_ms"]) / len(m["g_ms"]),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "bf16 network (f32 accumulate) + f32/f64 exact checks",
             "data": "synthetic (seeded uniform states on the device)",
@@ -775,23 +875,32 @@ def run_surrogate(args):
                        "lr": 1e-3, "network": "9 -> 256x4 SiLU -> 1 sigmoid, BF16",
                        "l2": "per-step working set (11 GB of candidates) > L2",
                        "parallelism": "replicas" if ws == 1 else "independent replicas"},
-            "roofline": roof, "cpu_baseline": cpu,
-            "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "candidates_per_step": args.e2e_n},
-            "clocks": clk.summary(),
+            "roofline": m["roof"], "cpu_baseline": m["cpu"], "e2e": m["e2e"], "clocks": m["clocks"],
+            # per guided step: network scores, 3 histogram passes and the compaction of the
+            # exact top-k, the traversal and re-test of the selected states
             "gpu_launches": 7 * args.steps,
-            "detail": {"plain_verified_free_per_s": plain_value, "guided_over_plain": value / plain_value,
-                       "plain_ms_per_step": sum(p_ms) / len(p_ms), "guided_ms_per_step": sum(g_ms) / len(g_ms),
-                       "mlp_ms_per_step": mlp_kernel_ms, "mlp_rows_per_s": args.n / (mlp_kernel_ms / 1e3),
-                       "checked_per_step": g_checked / args.steps,
-                       "precision_top_fraction": g_free / max(1, g_checked),
-                       "plain_free_fraction": p_free / (args.n * args.steps),
-                       "precision_at_0.5": prec, "recall_at_0.5": rec, "false_free_accepted": false_free,
-                       "train_ms": train_ms, "train_steps": rep.steps,
-                       "train_labels_per_s": rep.labels / (train_ms / 1e3),
+            "detail": {"mismatches": m["parity"]["mismatches"] if m["parity"] else None,
+                       "mismatch_sample": m["parity"]["mismatch_sample"] if m["parity"] else 0,
+                       "parity": m["parity"],
+                       "plain_verified_free_per_s": plain_value, "guided_over_plain": value / plain_value,
+                       "plain_ms_per_step": sum(m["p_ms"]) / len(m["p_ms"]),
+                       "guided_ms_per_step": sum(m["g_ms"]) / len(m["g_ms"]),
+                       "mlp_ms_per_step": m["mlp_ms"], "mlp_rows_per_s": args.n / (m["mlp_ms"] / 1e3),
+                       "checked_per_step": m["g_checked"] / args.steps,
+                       "precision_top_fraction": m["g_free"] / max(1, m["g_checked"]),
+                       "plain_free_fraction": m["p_free"] / (args.n * args.steps),
+                       "precision_at_0.5": m["precision"], "recall_at_0.5": m["recall"],
+                       "false_free_accepted": m["false_free"], "false_free_oracle": m.get("false_free_oracle"),
+                       "false_free_oracle_sample": m.get("false_free_oracle_sample", 0),
+                       "train_ms": m["train_ms"], "train_steps": rep.steps,
+                       "train_labels_per_s": rep.labels / (m["train_ms"] / 1e3),
                        "train_loss_first_last": [rep.losses[0][1], rep.losses[-1][1]] if rep.losses else None,
-                       "top_fraction_sweep": sweep}}
-    print(json.dumps(line))
+                       "top_fraction_sweep": m["sweep"]}}
+    print(json.dumps(line), flush=True)
+    bad = (line["detail"]["mismatches"] or 0) + m["false_free"] + (m.get("false_free_oracle") or 0)
+    if bad:
+        print("verdict mismatches against the oracle: %d" % bad, file=sys.stderr)
+        sys.exit(3)
 
 
 def run_narrow(args):
@@ -846,8 +955,8 @@ def run_narrow(args):
     g_reps, p_reps = [], []
     with ClockSampler(local) as clk:
         for i in range(args.steps):
-            g_reps.append(search.run(roots, guided=True, keep_escapes=(i == 0)))
-            p_reps.append(plain.run(roots, guided=False))
+            g_reps.append(search.run(roots, guided=True, keep_escapes=(i == 0), keep_validated=(i == 0)))
+            p_reps.append(plain.run(roots, guided=False, keep_validated=(i == 0)))
     g_esc = sum(r.escapes for r in g_reps)
     g_s = sum(r.seconds for r in g_reps)
     p_esc = sum(r.escapes for r in p_reps)
@@ -875,6 +984,17 @@ def run_narrow(args):
     if rank != 0:
         return
     last = g_reps[-1]
+    # roofline of the dominant kernel: the first guided round's validated motions once more as a
+    # direct call (the search replays them as a graph), with the traversal's counters and events
+    gf, gt, gcodes = g_reps[0].validated_states
+    uw.first_contact_steps(gf, gt, DELTA, 1)
+    st = uw.last_stats()
+    roof = traversal_roofline([st], gf.shape[0] * (2 * 56 + 4), gf.shape[0], "narrow")
+    roof["kernel_share"] = "exact validation is %.0f %% of a guided round" % (
+        100.0 * st["traverse_ms"] * last.rounds / max(1e-9, 1e3 * g_reps[-1].seconds))
+    cpu, parity = None, None
+    if ws == 1 and not args.no_cpu_baseline:
+        cpu, parity = _cpu_plain_narrow(p_reps[0].validated_states, args.cpu_seconds)
     line = {"metric": WORKLOADS["narrow"][0], "value": value, "unit": "escapes/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * g_s / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -890,7 +1010,7 @@ def run_narrow(args):
                                  "plate plane inside the plate (hence through a hole)",
                        "l2": "per-step working set (roots and 64x expansions, GBs) > L2",
                        "parallelism": "replicas"},
-            "roofline": None, "cpu_baseline": None,
+            "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_esc / e2e_s, "unit": "escapes/s", "h2d_bytes_per_step": int(hroots.numel() * 8),
                     "d2h_bytes_per_step": int(d2h)},
             "clocks": clk.summary(),
@@ -898,7 +1018,9 @@ def run_narrow(args):
             # replayed validation graph 7 (bounds, set-up, anchors, rounds, traversal, re-test,
             # finalise; its CUB scan and sort kernels not counted), endpoint labels 2 (traversal, re-test)
             "gpu_launches": 12 * sum(r.rounds for r in g_reps),
-            "detail": {"plain_escapes_per_s": plain_value, "guided_over_plain": value / max(plain_value, 1e-12),
+            "detail": {"mismatches": parity["mismatches"] if parity else None,
+                       "mismatch_sample": parity["mismatch_sample"] if parity else 0, "parity": parity,
+                       "plain_escapes_per_s": plain_value, "guided_over_plain": value / max(plain_value, 1e-12),
                        "guided_yield": g_esc / max(1, sum(r.validated for r in g_reps)),
                        "plain_yield": p_esc / max(1, sum(r.validated for r in p_reps)),
                        "escapes_per_step": g_esc / args.steps, "plain_escapes_per_step": p_esc / args.steps,
@@ -907,7 +1029,41 @@ def run_narrow(args):
                        "false_free_escapes": false_free, "retrains": sum(r.retrains for r in g_reps),
                        "initial_train_s": train_s, "initial_train_steps": train_steps,
                        "plain_ms_per_step": 1e3 * p_s / args.steps}}
-    print(json.dumps(line))
+    print(json.dumps(line), flush=True)
+    bad = (parity["mismatches"] if parity else 0) + false_free
+    if bad:
+        print("verdict mismatches against the oracle: %d" % bad, file=sys.stderr)
+        sys.exit(3)
+
+
+def _cpu_plain_narrow(validated, target_s):
+    """The plain narrow-passage search's exact validations on the host cores: the
+    oracle's is_valid_transition over the motions of the plain search's first
+    round (grown until it takes about target_s), escapes per second, and its
+    first-contact codes compared with the GPU's.  Returns (cpu_baseline, parity)."""
+    from oracle import oracle as O
+    O.build()
+    Ve, Fe, Vr, Fr = _meshes("narrow")
+    ow = O.OracleWorld(Ve, Fe, Vr, Fr)
+    cores = os.cpu_count() or 1
+    frm, to, codes = (t.cpu().numpy() for t in validated)
+    n = 256
+    while True:
+        n = min(n, frm.shape[0])
+        t0 = time.perf_counter()
+        first, _ = ow.segments_first_contact(frm[:n], to[:n], DELTA, mode=1, nthreads=cores)
+        dt = time.perf_counter() - t0
+        if dt >= target_s or n >= frm.shape[0]:
+            break
+        n = max(n * 2, int(n * target_s / max(dt, 1e-3) * 1.1))
+    esc = int((first == -1).sum())
+    cpu = {"value": esc / dt, "unit": "escapes/s", "cores": cores, "kind": "port",
+           "sample": "the first %d motions the plain search validated in its first round (is_valid_transition, "
+                     "%d escapes, %.1f s; expansion and the crossing filter not counted)" % (n, esc, dt)}
+    parity = {"mismatches": int((first != codes[:n]).sum()), "mismatch_sample": int(n),
+              "compared": "is_valid_transition first-contact code of every motion",
+              "sample": "the CPU-baseline sample, against the plain search's graph-replayed validation"}
+    return cpu, parity
 
 
 def _bf16_peak():
@@ -919,9 +1075,12 @@ def _bf16_peak():
         return 1700.0, "fallback (sustained)"
 
 
-def _cpu_plain_sampling(scale, target_s):
-    """Plain uniform sampling on the host cores: the oracle's isValid on uniform
-    states, counting the free ones (the reference's sampler has no surrogate)."""
+def _cpu_plain_sampling(cand, gpu_valid, target_s):
+    """Plain uniform sampling on the host cores: the oracle's isValid on the
+    first candidates of the GPU's resident batch (grown until it takes about
+    target_s), counting the free ones (the reference's sampler has no
+    surrogate), and its verdicts compared with the GPU plain arm's.
+    Returns (cpu_baseline dict, parity dict)."""
     from oracle import oracle as O
     O.build()
     Ve, Fe, Vr, Fr = _meshes("surrogate")
@@ -929,15 +1088,21 @@ def _cpu_plain_sampling(scale, target_s):
     cores = os.cpu_count() or 1
     n = 65536
     while True:
-        q = W.uniform_states(n, -2.0, 2.0, scale, seed=77)
+        n = min(n, cand.shape[0])
+        q = cand[:n].cpu().numpy()
         t0 = time.perf_counter()
         v = ow.is_valid(q, nthreads=cores)
         dt = time.perf_counter() - t0
-        if dt >= target_s or n >= 1 << 26:
+        if dt >= target_s or n >= min(cand.shape[0], 1 << 26):
             break
-        n = min(1 << 26, max(n * 2, int(n * target_s / max(dt, 1e-3) * 1.1)))
-    return {"value": float(v.sum()) / dt, "unit": "samples/s", "cores": cores, "kind": "port",
-            "sample": "%d uniform states checked, %d free, %.1f s" % (n, int(v.sum()), dt)}
+        n = max(n * 2, int(n * target_s / max(dt, 1e-3) * 1.1))
+    mism = int((v != gpu_valid[:n].astype(bool)).sum())
+    cpu = {"value": float(v.sum()) / dt, "unit": "samples/s", "cores": cores, "kind": "port",
+           "sample": "first %d uniform candidates of the GPU's batch checked, %d free, %.1f s"
+                     % (n, int(v.sum()), dt)}
+    parity = {"mismatches": mism, "mismatch_sample": int(n), "compared": "is_valid_state verdict of every candidate",
+              "sample": "the CPU-baseline sample, against the plain arm's last timed step"}
+    return cpu, parity
 
 
 def run_surrogate_reference(args):
@@ -997,6 +1162,92 @@ def _traffic_per_segment():
     return None
 
 
+def run_profile_case(args):
+    """Small fixed workloads for ncu captures (no JSON line): `states`, `segments`,
+    `mlp`, `train`, `ompl` or `all` (every kernel of the engine once), with
+    --n units, on the interlocking tori (the alpha puzzle for `ompl`)."""
+    import torch
+
+    import puzzletunneldiscovery_gb300 as pw
+    from puzzletunneldiscovery_gb300 import surrogate as S
+
+    what, n = args.profile_case, args.n
+    dev = torch.device("cuda", 0)
+    if what == "ompl":
+        from puzzletunneldiscovery_gb300 import ompl_compat as OC
+        (Ve, Fe, Vr, Fr), c, P = _alpha_ompl()
+        uw = pw.UnitWorld(0)
+        uw.load_env_mesh(Ve, Fe)
+        uw.load_robot_mesh(Vr, Fr)
+        uw.enforceRobotCenter(c)
+        uw.scaleToUnit()
+        uw.angleModel(0.0, 0.0)
+        A, B, lo, hi = _ompl_motions(P, n, 0)
+        a, b = torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev)
+        for _ in range(3):
+            v, states = OC._check_motions_dev(uw, a, b, lo, hi, OMPL_CDRES)
+        torch.cuda.synchronize()
+        print("done", states, float(v.float().mean()))
+        return
+    Ve, Fe, Vr, Fr = W.cfg_interlocking_tori()
+    uw = pw.UnitWorld(0)
+    uw.load_env_mesh(Ve, Fe)
+    uw.load_robot_mesh(Vr, Fr)
+    uw.scaleToUnit()
+    uw.angleModel(0.0, 0.0)
+    s = uw.scene_scale
+    if what == "all":
+        from puzzletunneldiscovery_gb300 import narrow as N
+        q = torch.from_numpy(W.uniform_states(n, -2, 2, s, seed=0)).to(dev)
+        uw.is_valid_states(q)
+        uw.is_disentangled_states(q)
+        q0, q1 = W.segment_batch(max(1, n // 10), -2, 2, s, seed=0)
+        a, b = torch.from_numpy(q0).to(dev), torch.from_numpy(q1).to(dev)
+        uw.transit_states_to_with_contact(a, b, DELTA)
+        uw.intersecting_segments(np.array([0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0]))
+        ends = N.expand(q[:1000], 64, 0.01, 0.1, 5)
+        N.crossings(q[:1000], ends, 64, torch.zeros((4, 3), dtype=torch.float64, device=dev), 0.0, 0.5)
+        net = S.Surrogate(0, 1)
+        sc = net.score(q)
+        S.select_top(sc, q, max(1, n // 10))
+        net.predict_mma(q[:65536])
+        y = uw.is_valid_states(q[:65536])
+        net.train_step(q[:65536], y, 1e-3)
+        net.set_training_kernels(True)
+        net.train_step(q[:65536], y, 1e-3)
+        net.check()
+        torch.cuda.synchronize()
+        print("done")
+        return
+    if what in ("mlp", "train"):
+        net = S.Surrogate(0, 1)
+        g = torch.Generator(device=dev)
+        g.manual_seed(0)
+        q = S.uniform_states_device(n, -2, 2, s, g, dev)
+        if what == "mlp":
+            for _ in range(3):
+                net.predict(q)
+            net.check()
+        else:
+            y = uw.is_valid_states(q[:65536])
+            for _ in range(3):
+                net.train_step(q[:65536], y, 1e-3)
+        torch.cuda.synchronize()
+        print("done")
+        return
+    if what == "states":
+        q = torch.from_numpy(W.uniform_states(n, -2, 2, s, seed=0)).to(dev)
+        for _ in range(3):
+            uw.is_valid_states(q)
+    else:
+        q0, q1 = W.segment_batch(n, -2, 2, s, seed=0)
+        a, b = torch.from_numpy(q0).to(dev), torch.from_numpy(q1).to(dev)
+        for _ in range(3):
+            uw.first_contact_steps(a, b, DELTA)
+    torch.cuda.synchronize()
+    print("done", uw.last_stats())
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -1009,6 +1260,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
+    ap.add_argument("--no-surrogate-arm", action="store_true",
+                    help="segments: skip the surrogate-guided sampling figures in the detail")
     ap.add_argument("--narrow-k", type=int, default=65536, help="narrow: segments validated per round")
     ap.add_argument("--narrow-train-labels", type=int, default=10_000_000,
                     help="narrow: exact labels of the initial training")
@@ -1017,7 +1270,13 @@ def main():
     ap.add_argument("--e2e-n", type=int, default=20_000_000, help="surrogate: candidates per end-to-end step")
     ap.add_argument("--sweep", type=lambda v: [float(x) for x in v.split(",") if x], default=[0.25, 0.5, 0.6],
                     help="surrogate: further checked fractions reported in detail")
+    ap.add_argument("--profile-case", choices=["states", "segments", "mlp", "train", "ompl", "all"], default=None,
+                    help="run a small fixed workload for an ncu capture instead of the benchmark")
     args = ap.parse_args()
+    if args.profile_case:
+        args.n = args.n or 1_000_000
+        run_profile_case(args)
+        return
     if args.n is None:
         args.n = WORKLOADS[args.workload][2]
     if args.workload == "narrow":
@@ -1029,7 +1288,6 @@ def main():
     elif args.workload == "ompl":
         run_ompl_reference(args) if args.impl == "reference" else run_ompl(args)
     elif args.workload == "surrogate":
-        args.e2e_n = min(args.e2e_n, args.n)
         run_surrogate_reference(args) if args.impl == "reference" else run_surrogate(args)
     elif args.impl == "reference":
         run_reference(args)

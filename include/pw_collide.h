@@ -135,7 +135,10 @@ PW_API int pw_states_valid(pw_world *w, const double *states, int64_t n, uint8_t
  * device looks up the array's device address (cudaGetSymbolAddress) and should come
  * before any stream capture.  All calls share the array, so calls whose work overlaps on
  * the GPU (different streams, different worlds on the same device) race; order them on
- * one stream.  pw_world_last_stats does not report on this entry point. */
+ * one stream.  It uses the world's launch configuration (pw_world_set_launch_config) as
+ * pw_states_valid does.  When more pairs need the FP64 re-test than its queue holds
+ * (1048576), the rest are re-tested inline by the traversal, with the same verdicts.
+ * pw_world_last_stats does not report on this entry point. */
 PW_API int pw_states_valid_noalloc(pw_world *w, const double *states, int64_t n, uint8_t *valid, void *stream);
 
 /* device, async: UnitWorld::isDisentangled (unit_world.cc:249-264) for n states. */

@@ -32,7 +32,10 @@ def build(force: bool = False) -> str:
     return _LIB_PATH
 
 
-_REF_SRC = "/root/reference/lib/tritri/Moller97d.cc"
+# the reference checkout: PW_REFERENCE_DIR, by default a sibling of this repository named "reference"
+REFERENCE_DIR = os.environ.get("PW_REFERENCE_DIR",
+                               os.path.join(os.path.dirname(os.path.dirname(_HERE)), "reference"))
+_REF_SRC = os.path.join(REFERENCE_DIR, "lib", "tritri", "Moller97d.cc")
 _REF_LIB = os.path.join(_HERE, "_ref", "libref_tritri.so")
 _ref = None
 
@@ -44,7 +47,8 @@ def build_ref() -> str | None:
         return _REF_LIB if os.path.exists(_REF_LIB) else None
     if not os.path.exists(_REF_LIB) or os.path.getmtime(_REF_LIB) < os.path.getmtime(
             os.path.join(_HERE, "ref_tritri_shim.cc")):
-        subprocess.run(["make", "-s", "-C", _HERE, "_ref/libref_tritri.so"], check=True)
+        subprocess.run(["make", "-s", "-C", _HERE, "_ref/libref_tritri.so", "PW_REFERENCE_DIR=" + REFERENCE_DIR],
+                       check=True)
     return _REF_LIB
 
 

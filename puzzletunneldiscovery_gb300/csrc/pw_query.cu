@@ -1106,15 +1106,6 @@ int ensure_query_scratch(pw_world *w)
 	return PW_OK;
 }
 
-int persistent_grid(pw_world *w, const void *kernel, size_t smem)
-{
-	int per_sm = 0;
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, WARPS * 32, smem);
-	if (per_sm < 1)
-		per_sm = 1;
-	return per_sm * (w->num_sms > 0 ? w->num_sms : 1);
-}
-
 // Launch configuration of kernel 0 (states) / 1 (segments), as set by pw_world_set_launch_config.
 int launch_grid(pw_world *w, int kernel, const void *fn, size_t smem)
 {
@@ -1708,9 +1699,11 @@ extern "C" int pw_states_valid_noalloc(pw_world *w, const double *states, int64_
 	rc = set_smem_attr((const void *)k_states<NOALLOC_RETEST_CAP>, smem);
 	if (rc)
 		return rc;
-	const int grid = persistent_grid(w, (const void *)k_states<NOALLOC_RETEST_CAP>, smem);
-	k_states<NOALLOC_RETEST_CAP><<<grid, WARPS * 32, smem, st>>>(w->dev, states, n, valid, ctr, rq, soft_cap_of(w),
-	                                                             32);
+	// the world's launch configuration, as pw_states_valid uses it (both instances of the
+	// kernel have the same resources, so they share the cached grid)
+	const int grid = launch_grid(w, 0, (const void *)k_states<NOALLOC_RETEST_CAP>, smem);
+	k_states<NOALLOC_RETEST_CAP><<<grid, WARPS * 32, smem, st>>>(w->dev, states, n, valid, ctr, rq,
+	                                                             launch_soft_cap(w, 0), launch_width(w, 0));
 	StateSrc src{ states, nullptr, nullptr, nullptr, nullptr, nullptr };
 	k_retest<NOALLOC_RETEST_CAP><<<w->num_sms * 4, 256, 0, st>>>(w->dev, src, valid, nullptr, ctr, rq);
 	PW_CUDA(cudaGetLastError());

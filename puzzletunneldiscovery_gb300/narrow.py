@@ -107,6 +107,7 @@ class SearchReport:
     retrains: int = 0
     seconds: float = 0.0
     escape_states: list = field(default_factory=list)   # (from, to) device tensors of the escapes
+    validated_states: tuple | None = None   # (from, to, codes) of the first round's validated motions
 
     @property
     def escapes_per_s(self):
@@ -254,7 +255,7 @@ class NarrowPassageSearch:
         return steps
 
     def run(self, roots: torch.Tensor, guided: bool, roots_per_round: int = 1 << 20,
-            keep_escapes: bool = False) -> SearchReport:
+            keep_escapes: bool = False, keep_validated: bool = False) -> SearchReport:
         rep = SearchReport()
         torch.cuda.synchronize(self.dev)
         t0 = time.perf_counter()
@@ -286,6 +287,8 @@ class NarrowPassageSearch:
             rep.escapes += int(free.sum())
             if keep_escapes:
                 rep.escape_states.append((frm[free].clone(), to[free].clone()))
+            if keep_validated and rep.validated_states is None:
+                rep.validated_states = (frm.clone(), to.clone(), codes.clone())
             # exact labels of the validated motions' midpoints train the network
             if guided and self.net is not None:
                 mid = midpoints(frm, to)

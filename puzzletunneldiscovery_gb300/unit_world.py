@@ -43,6 +43,16 @@ def _stream_ptr(device) -> int:
     return torch.cuda.current_stream(device).cuda_stream
 
 
+def _strict_tril_pairs(k: torch.Tensor):
+    """(row, column) of flat index k of the strict lower triangle, row-major:
+    k = row (row - 1) / 2 + column, 0 <= column < row.  Rounding of the square
+    root is corrected by one step either way."""
+    r = torch.floor((torch.sqrt(8.0 * k.to(torch.float64) + 1.0) + 1.0) / 2.0).to(torch.int64)
+    r = torch.where(r * (r - 1) // 2 > k, r - 1, r)
+    r = torch.where((r + 1) * r // 2 <= k, r + 1, r)
+    return r, k - r * (r - 1) // 2
+
+
 class UnitWorld:
     """World of an environment and a robot mesh in the normalised unit frame."""
 
@@ -575,30 +585,40 @@ class UnitWorld:
 
     def calculate_visibility_matrix2(self, qs0, qs0_are_unit_states, qs1, qs1_are_unit_states, verify_magnitude,
                                      enable_mt=True):
-        """int8 [M, N] of isValidTransition(qs0[i], qs1[j]) (unit_world.cc:761-797)."""
-        a = self._maybe_unit(qs0, qs0_are_unit_states)
-        b = self._maybe_unit(qs1, qs1_are_unit_states)
+        """int8 [M, N] of isValidTransition(qs0[i], qs1[j]) (unit_world.cc:761-797).
+        The (i, j) pairs are decoded on the device from flat indices, in chunks."""
+        a = self._dev_states(self._maybe_unit(qs0, qs0_are_unit_states))
+        b = self._dev_states(self._maybe_unit(qs1, qs1_are_unit_states))
         M, N = a.shape[0], b.shape[0]
-        out = np.zeros((M, N), dtype=np.int8)
-        rows = max(1, (1 << 22) // max(N, 1))
-        for r0 in range(0, M, rows):
-            r1 = min(M, r0 + rows)
-            A = np.repeat(a[r0:r1], N, axis=0)
-            B = np.tile(b, (r1 - r0, 1))
-            out[r0:r1] = self._pairs_first(A, B, verify_magnitude).reshape(r1 - r0, N)
-        return out
+        out = torch.zeros(M * N, dtype=torch.int8, device=self._device)
+        for k0 in range(0, M * N, self._PAIR_CHUNK):
+            k = torch.arange(k0, min(M * N, k0 + self._PAIR_CHUNK), dtype=torch.int64, device=self._device)
+            out[k0:k0 + k.shape[0]] = self._visible(a.index_select(0, k // N), b.index_select(0, k % N),
+                                                    verify_magnitude)
+        return out.reshape(M, N).cpu().numpy()
 
     def calculate_visibility_matrix(self, qs, is_unit_states, verify_magnitude):
-        """Symmetric int8 [N, N] over pairs i < j (unit_world.cc:740-759); the diagonal is 0."""
-        q = self._maybe_unit(qs, is_unit_states)
+        """Symmetric int8 [N, N]: isValidTransition(qs[i], qs[j]) for i < j, mirrored
+        (unit_world.cc:740-759).  The diagonal, which the reference leaves
+        uninitialised, is 0.  The pairs are decoded on the device from flat
+        indices of the strict triangle, in chunks."""
+        q = self._dev_states(self._maybe_unit(qs, is_unit_states))
         N = q.shape[0]
-        iu, ju = np.triu_indices(N, k=1)
-        out = np.zeros((N, N), dtype=np.int8)
-        if iu.size:
-            v = self._pairs_first(np.ascontiguousarray(q[iu]), np.ascontiguousarray(q[ju]), verify_magnitude)
-            out[iu, ju] = v
-            out[ju, iu] = v
-        return out
+        out = torch.zeros((N, N), dtype=torch.int8, device=self._device)
+        total = N * (N - 1) // 2
+        for k0 in range(0, total, self._PAIR_CHUNK):
+            k = torch.arange(k0, min(total, k0 + self._PAIR_CHUNK), dtype=torch.int64, device=self._device)
+            hi, lo = _strict_tril_pairs(k)                  # lo < hi: from = qs[lo], to = qs[hi]
+            v = self._visible(q.index_select(0, lo), q.index_select(0, hi), verify_magnitude)
+            out[lo, hi] = v
+            out[hi, lo] = v
+        return out.cpu().numpy()
+
+    _PAIR_CHUNK = 1 << 22
+
+    def _visible(self, a: torch.Tensor, b: torch.Tensor, verify_magnitude) -> torch.Tensor:
+        k = self.first_contact_steps(a, b, verify_magnitude, _lib.PW_SEG_TRANSITION)
+        return (k == _lib.PW_STEP_FREE).to(torch.int8)
 
     # ----------------------------------------------------------- contacts and geometry
     def intersecting_segments(self, unitq):

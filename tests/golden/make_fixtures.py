@@ -1,8 +1,8 @@
 """Generate the committed golden fixtures of tests/golden/.
 
-Run in a container that has the reference checkout (read-only) at
-/root/reference; the GPU machine does not have it, so the tests read only the
-files this script writes.
+Run where the reference checkout (read-only) is present: PW_REFERENCE_DIR
+names it, by default a sibling of this repository named "reference".  Machines
+without the checkout read only the files this script writes.
 
 * alpha_puzzle.npz -- the reference's alpha puzzle (res/alpha/alpha_env-1.2.org.obj,
   res/alpha/alpha-1.2.org.obj) parsed by objio.load_obj, the OMPL robot centre
@@ -32,7 +32,7 @@ sys.path.insert(0, ROOT)
 from oracle import oracle as O  # noqa: E402
 from puzzletunneldiscovery_gb300 import objio, workloads  # noqa: E402
 
-REF = "/root/reference"
+REF = os.environ.get("PW_REFERENCE_DIR", os.path.join(os.path.dirname(ROOT), "reference"))
 
 
 def alpha():

@@ -1,7 +1,8 @@
 """Generate tests/golden/screening_golden.npz from the reference's own task
 partitioner and disjoint set (src/GP/pipeline/partt.py, disjoint_set.py),
-loaded from the read-only reference checkout at /root/reference.  The GPU
-box does not have the checkout: the tests read only the file written here.
+loaded from the read-only reference checkout (PW_REFERENCE_DIR, by default a
+sibling of this repository named "reference").  Machines without the checkout
+read only the file written here.
 
 Contents:
 * partition cases (nkey_total, max_chunks, min_chunk_size): the task count of
@@ -22,7 +23,9 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-PIPELINE = "/root/reference/src/GP/pipeline"
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REF = os.environ.get("PW_REFERENCE_DIR", os.path.join(os.path.dirname(ROOT), "reference"))
+PIPELINE = os.path.join(REF, "src", "GP", "pipeline")
 RESERVED = 2
 SCHEMES = ("ge", "nt", "nn")
 
