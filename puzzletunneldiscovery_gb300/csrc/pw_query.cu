@@ -125,16 +125,22 @@ __device__ __noinline__ bool retest_entry(const WorldDev &W, const StateSrc &src
 	return retest64(W, q, e.env_tri, e.rob_tri);
 }
 
+// Per-lane counters of one kernel launch.  32-bit (the kernels flush them into the
+// 64-bit query counters before they can wrap): 64-bit lane counters cost registers
+// the traversal loop needs.
 struct LaneStats {
-	unsigned long long node = 0, leaf = 0, inl = 0;
+	uint32_t node = 0, leaf = 0, inl = 0;
 };
 
-// Queue the buffered uncertain pairs whose slot is not in `skip`.  When the
-// queue (CAP entries) is full the pair is re-tested here; returns the mask of
-// slots such an inline FP64 re-test found in contact.
+// Queue the buffered uncertain pairs whose slot is not in `skip`.  A pair that does
+// not fit the queue (CAP entries) is not dropped silently: the mask of the slots
+// that lost a pair is returned, and the caller answers those slots again after the
+// traversal with inline FP64 re-tests.  (Keeping the FP64 test out of this loop
+// keeps a function call out of the traversal, whose registers it would otherwise
+// force to local memory.)
 template <uint64_t CAP>
 __device__ uint32_t flush_unc(const WarpSmem &sm, int nunc, uint32_t skip, int lane, QueryCounters *ctr,
-                              RetestEntry *rq, const WorldDev &W, const StateSrc &src, LaneStats &st)
+                              RetestEntry *rq)
 {
 	const int slot = lane < nunc ? (int)sm.unc_slot[lane] : 0;
 	const bool mine = lane < nunc && !((skip >> slot) & 1u);
@@ -145,23 +151,39 @@ __device__ uint32_t flush_unc(const WarpSmem &sm, int nunc, uint32_t skip, int l
 	if (lane == 0)
 		base = atomicAdd(&ctr->retest_count, (unsigned long long)__popc(mm));
 	base = __shfl_sync(FULL, base, 0);
-	uint32_t hits = 0u;
+	bool lost = false;
 	if (mine) {
 		const unsigned long long idx = base + __popc(mm & ((1u << lane) - 1u));
+		if (idx < CAP) {
+			RetestEntry e;
+			e.query = sm.slot_query[slot];
+			e.step = sm.slot_step[slot];
+			e.env_tri = sm.unc[lane].x;
+			e.rob_tri = sm.unc[lane].y;
+			rq[idx] = e;
+		} else {
+			lost = true;
+		}
+	}
+	return __reduce_or_sync(FULL, lost ? (1u << slot) : 0u);
+}
+
+// Inline FP64 re-test of this round's uncertain pairs (at most one per lane):
+// the mask of slots found in contact.
+__device__ __forceinline__ uint32_t retest_inline(const WorldDev &W, const WarpSmem &sm, const StateSrc &src,
+                                                  bool unc, uint2 up, int slot, LaneStats &st)
+{
+	bool h = false;
+	if (unc) {
+		st.inl++;
 		RetestEntry e;
 		e.query = sm.slot_query[slot];
 		e.step = sm.slot_step[slot];
-		e.env_tri = sm.unc[lane].x;
-		e.rob_tri = sm.unc[lane].y;
-		if (idx < CAP) {
-			rq[idx] = e;
-		} else {
-			st.inl++;
-			if (retest_entry(W, src, e))
-				hits = 1u << slot;
-		}
+		e.env_tri = up.x;
+		e.rob_tri = up.y;
+		h = retest_entry(W, src, e);
 	}
-	return __reduce_or_sync(FULL, hits);
+	return __reduce_or_sync(FULL, h ? (1u << slot) : 0u);
 }
 
 // One warp answers up to 32 queries at once (slots = set bits of `open`;
@@ -169,9 +191,13 @@ __device__ uint32_t flush_unc(const WarpSmem &sm, int nunc, uint32_t skip, int l
 // carries its slot, lanes test pairs of any open slot, and a slot closes at its
 // first certified contact.  Returns the mask of slots in contact.  Uncertain
 // pairs of slots still open at the end go to the FP64 queue.
-template <uint64_t CAP>
+// INLINE = false: uncertain pairs go to the FP64 queue; the slots that lost a pair
+// to a full queue are returned in `ovf`.  INLINE = true (the second pass over such
+// slots): every uncertain pair is re-tested in FP64 at once.
+template <uint64_t CAP, bool INLINE>
 __device__ uint32_t traverse_batch(const WorldDev &W, WarpSmem &sm, int lane, uint32_t open, int soft_cap,
-                                   QueryCounters *ctr, RetestEntry *rq, const StateSrc &src, LaneStats &st)
+                                   QueryCounters *ctr, RetestEntry *rq, const StateSrc &src, LaneStats &st,
+                                   uint32_t &ovf)
 {
 	const uint32_t ebase = (uint32_t)W.env.leaf_base, rbase = (uint32_t)W.rob.leaf_base;
 	const unsigned lt_mask = (1u << lane) - 1u;
@@ -185,19 +211,19 @@ __device__ uint32_t traverse_batch(const WorldDev &W, WarpSmem &sm, int lane, ui
 
 	auto add_unc = [&](bool unc, uint2 up, int slot) {
 		unc = unc && !((done >> slot) & 1u);
-		unsigned um = __ballot_sync(FULL, unc);
+		if (INLINE) {
+			const uint32_t ih = retest_inline(W, sm, src, unc, up, slot, st);
+			hit |= ih;
+			done |= ih;
+			return;
+		}
+		const unsigned um = __ballot_sync(FULL, unc);
 		if (!um)
 			return;
 		if (nunc + __popc(um) > UNC_CAP) {
-			const uint32_t ih = flush_unc<CAP>(sm, nunc, done, lane, ctr, rq, W, src, st);
+			ovf |= flush_unc<CAP>(sm, nunc, done, lane, ctr, rq);
 			nunc = 0;
 			__syncwarp();
-			if (ih) {
-				hit |= ih;
-				done |= ih;
-				unc = unc && !((done >> slot) & 1u);
-				um = __ballot_sync(FULL, unc);
-			}
 		}
 		if (unc) {
 			const int o = nunc + __popc(um & lt_mask);
@@ -304,11 +330,8 @@ __device__ uint32_t traverse_batch(const WorldDev &W, WarpSmem &sm, int lane, ui
 			run_leaves(32);
 	}
 	__syncwarp();
-	if (nunc > 0 && done != FULL) {
-		const uint32_t ih = flush_unc<CAP>(sm, nunc, done, lane, ctr, rq, W, src, st);
-		hit |= ih;
-		done |= ih;
-	}
+	if (!INLINE && nunc > 0 && done != FULL)
+		ovf |= flush_unc<CAP>(sm, nunc, done, lane, ctr, rq);
 	__syncwarp();
 	return hit;
 }
@@ -353,11 +376,12 @@ __device__ __noinline__ void chunk_step_qf(const WorldDev &W, const StateSrc &sr
 //   and ranges split in halves around their middle step down to single steps,
 //   which take the per-step leaf tests.
 // Returns the lowest step in contact as a one-bit mask (0 when none).
-template <uint64_t CAP>
+// INLINE and `ovf` as in traverse_batch.
+template <uint64_t CAP, bool INLINE>
 __device__ uint32_t traverse_chunk(const WorldDev &W, WarpSmem &sm, int lane, int nopen, int cnt, int anchor,
                                    float motion, int soft_cap, QueryCounters *ctr, RetestEntry *rq,
                                    const StateSrc &src, LaneStats &st, uint32_t seg, int64_t ckslot,
-                                   unsigned long long &ndetailed)
+                                   uint32_t &ndetailed, uint32_t &ovf)
 {
 	const uint32_t ebase = (uint32_t)W.env.leaf_base, rbase = (uint32_t)W.rob.leaf_base;
 	const unsigned lt_mask = (1u << lane) - 1u;
@@ -379,18 +403,19 @@ __device__ uint32_t traverse_chunk(const WorldDev &W, WarpSmem &sm, int lane, in
 	// buffer the uncertain pairs of this round (at most one per lane), flushing when full
 	auto add_unc = [&](bool unc, uint2 up, int slot) {
 		unc = unc && !((done >> slot) & 1u);
-		unsigned um = __ballot_sync(FULL, unc);
+		if (INLINE) {
+			const uint32_t ih = retest_inline(W, sm, src, unc, up, slot, st);
+			if (ih)
+				settle(ih);
+			return;
+		}
+		const unsigned um = __ballot_sync(FULL, unc);
 		if (!um)
 			return;
 		if (nunc + __popc(um) > UNC_CAP) {
-			const uint32_t ih = flush_unc<CAP>(sm, nunc, done, lane, ctr, rq, W, src, st);
+			ovf |= flush_unc<CAP>(sm, nunc, done, lane, ctr, rq);
 			nunc = 0;
 			__syncwarp();
-			if (ih) {
-				settle(ih);
-				unc = unc && !((done >> slot) & 1u);
-				um = __ballot_sync(FULL, unc);
-			}
 		}
 		if (unc) {
 			const int o = nunc + __popc(um & lt_mask);
@@ -535,19 +560,17 @@ __device__ uint32_t traverse_chunk(const WorldDev &W, WarpSmem &sm, int lane, in
 			run_leaves(32);
 	}
 	__syncwarp();
-	if (nunc > 0 && done != FULL) {
-		const uint32_t ih = flush_unc<CAP>(sm, nunc, done, lane, ctr, rq, W, src, st);
-		if (ih)
-			settle(ih);
-	}
+	if (!INLINE && nunc > 0 && done != FULL)
+		ovf |= flush_unc<CAP>(sm, nunc, done, lane, ctr, rq);
 	__syncwarp();
 	return hit;
 }
 
-__device__ void flush_stats(QueryCounters *ctr, const LaneStats &st, unsigned long long queries,
+__device__ void flush_stats(QueryCounters *ctr, LaneStats &st, unsigned long long queries,
                             unsigned long long items, int lane)
 {
 	unsigned long long a = st.node, b = st.leaf, c = st.inl;
+	st = LaneStats();
 	for (int o = 16; o > 0; o >>= 1) {
 		a += __shfl_down_sync(FULL, a, o);
 		b += __shfl_down_sync(FULL, b, o);
@@ -563,6 +586,25 @@ __device__ void flush_stats(QueryCounters *ctr, const LaneStats &st, unsigned lo
 }
 
 // ------------------------------------------------------------------ states
+
+// Second pass over the slots of a state batch that lost uncertain pairs to a full
+// FP64 queue: the same traversal with every uncertain pair re-tested inline.
+// Returns the mask of those slots in contact.  Not inlined: the FP64 code stays out
+// of the register allocation of the kernel's main loop.
+template <uint64_t CAP>
+__device__ __noinline__ uint32_t resolve_states(const WorldDev &W, WarpSmem &sm, int lane, uint32_t open,
+                                                int soft_cap, QueryCounters *ctr, RetestEntry *rq,
+                                                const StateSrc &src, LaneStats &st)
+{
+	uint32_t unused = 0;
+	return traverse_batch<CAP, true>(W, sm, lane, open, soft_cap, ctr, rq, src, st, unused);
+}
+
+// Lane counters are flushed into the query counters before a 32-bit count can wrap.
+__device__ __forceinline__ bool stats_full(const LaneStats &st, int lane)
+{
+	return __any_sync(FULL, ((st.node | st.leaf | st.inl) >> 30) != 0u);
+}
 
 template <uint64_t CAP>
 __global__ void __launch_bounds__(WARPS * 32, 8) k_states(WorldDev W, const double *states, int64_t n,
@@ -600,11 +642,17 @@ __global__ void __launch_bounds__(WARPS * 32, 8) k_states(WorldDev W, const doub
 			atomicOr(&ctr->error, (unsigned)PW_DEVERR_NONFINITE);
 		__syncwarp();
 		const uint32_t open = (cnt == 32 ? FULL : ((1u << cnt) - 1u)) & ~bad;
-		const uint32_t hit = traverse_batch<CAP>(W, sm, lane, open, soft_cap, ctr, rq, src, st) | bad;
+		uint32_t ovf = 0u;
+		uint32_t hit = traverse_batch<CAP, false>(W, sm, lane, open, soft_cap, ctr, rq, src, st, ovf) | bad;
+		ovf &= ~hit;
+		if (ovf)
+			hit |= resolve_states<CAP>(W, sm, lane, ovf, soft_cap, ctr, rq, src, st);
 		if (lane < cnt)
 			out[base + lane] = ((hit >> lane) & 1u) ? 0 : 1;
 		queries += cnt;
 		items++;
+		if (stats_full(st, lane))
+			flush_stats(ctr, st, 0, 0, lane);
 		__syncwarp();
 	}
 	flush_stats(ctr, st, queries, items, lane);
@@ -862,6 +910,23 @@ __global__ void __launch_bounds__(1024) k_rounds(const uint32_t *sorted_keys, in
 	}
 }
 
+// Second pass over a segment chunk some of whose uncertain pairs did not fit the
+// FP64 queue: steps 0 .. nopen-1 traversed again with every uncertain pair
+// re-tested inline (the anchor frame reloaded first).  Returns the lowest step in
+// contact as a one-bit mask.  Not inlined, as resolve_states.
+__device__ __noinline__ uint32_t resolve_chunk(const WorldDev &W, WarpSmem &sm, int lane, int nopen, int cnt,
+                                               int anchor, float motion, int soft_cap, QueryCounters *ctr,
+                                               RetestEntry *rq, const StateSrc &src, LaneStats &st, uint32_t seg,
+                                               int64_t ckslot, uint32_t &ndetailed)
+{
+	if (lane < 5)
+		sm.qf[anchor].q[lane] = src.anchors[ckslot].q[lane];
+	__syncwarp();
+	uint32_t unused = 0;
+	return traverse_chunk<RETEST_CAP, true>(W, sm, lane, nopen, cnt, anchor, motion, soft_cap, ctr, rq, src, st,
+	                                        seg, ckslot, ndetailed, unused);
+}
+
 // Work item = (segment, 32-step chunk) in chunk-major order, so that early
 // contacts prune later chunks.  A warp computes the chunk's FP64 states lane-
 // parallel, then answers its steps with one swept traversal and records the
@@ -876,7 +941,7 @@ __global__ void __launch_bounds__(WARPS * 32, 8) k_segments(WorldDev W, StateSrc
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	WarpSmem &sm = reinterpret_cast<WarpSmem *>(smem_raw)[warp];
 	LaneStats st;
-	unsigned long long queries = 0, items = 0, detailed = 0;
+	uint32_t queries = 0, items = 0, detailed = 0;
 	const unsigned long long total = ctr->stat[STAT_TOTAL_ITEMS];
 	for (;;) {
 		unsigned long long item = 0;
@@ -926,14 +991,26 @@ __global__ void __launch_bounds__(WARPS * 32, 8) k_segments(WorldDev W, StateSrc
 		const int lim = (int)min((int64_t)cnt, (int64_t)cur - k0);
 		queries += lim;
 		const float motion = __double2float_ru(P.skip_scale);
-		const uint32_t hit = traverse_chunk<RETEST_CAP>(W, sm, lane, lim, cnt, anchor, motion, soft_cap, ctr, rq, src,
-		                                                st, s, ckslot, detailed);
+		uint32_t ovf = 0u;
+		uint32_t hit = traverse_chunk<RETEST_CAP, false>(W, sm, lane, lim, cnt, anchor, motion, soft_cap, ctr, rq,
+		                                                 src, st, s, ckslot, detailed, ovf);
+		// steps below the lowest contact that lost uncertain pairs to a full queue
+		if (ovf & (hit ? hit - 1u : FULL)) {
+			const uint32_t h2 = resolve_chunk(W, sm, lane, hit ? __ffs(hit) - 1 : lim, cnt, anchor, motion,
+			                                  soft_cap, ctr, rq, src, st, s, ckslot, detailed);
+			if (h2 && (!hit || h2 < hit))
+				hit = h2;
+		}
 		if (hit && lane == 0)
 			atomicMin(&first[s], k0 + (__ffs(hit) - 1));
+		if (((queries | items) >> 30) || stats_full(st, lane)) {
+			flush_stats(ctr, st, queries, items, lane);
+			queries = items = 0;
+		}
 		__syncwarp();
 	}
 	if (lane == 0 && detailed)
-		atomicAdd(&ctr->stat[STAT_DETAILED], detailed);
+		atomicAdd(&ctr->stat[STAT_DETAILED], (unsigned long long)detailed);
 	flush_stats(ctr, st, queries, items, lane);
 }
 
