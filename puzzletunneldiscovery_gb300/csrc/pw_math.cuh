@@ -17,6 +17,7 @@
 
 #include <math.h>
 #include <stdint.h>
+#include <string.h>
 
 #if defined(__CUDACC__)
 #define PW_HD __host__ __device__ __forceinline__
@@ -268,6 +269,90 @@ PW_HD double advance_delta(double delta, double dist, double step)
 		return dist < delta ? dist : delta;
 	}
 	return add(delta, step);
+}
+
+PW_HD uint64_t dbits(double x)
+{
+	uint64_t b;
+	memcpy(&b, &x, 8);
+	return b;
+}
+PW_HD double bitsd(uint64_t b)
+{
+	double x;
+	memcpy(&x, &b, 8);
+	return x;
+}
+
+// How many of the next (at most jmax) iterations of advance_delta from `delta`
+// can be taken at once, and their common increment *c: 0 when none.
+//
+// While delta stays in its binade [2^e, 2^(e+1)) it lies on the grid of
+// u = ulp(delta), and every rounded sum fl(delta + step) equals delta + c with
+// c = step rounded to a multiple of u (the grid is invariant under the shift by
+// delta), unless step / u falls exactly halfway between two integers (a tie,
+// whose rounding to even depends on delta: no jump then).  So k iterations give
+// delta + k c exactly (k c and the sum are multiples of u below 2^(e+1)), as
+// long as every exact sum stays inside the binade (delta + (k-1) c + step <=
+// 2^(e+1)) and no result passes dist (delta + k c <= dist: the clamp of the
+// reference loop is then never taken).  Both conditions are checked exactly.
+// The tie test and u work on the bit patterns; c is fl(delta + step) - delta
+// (exact); the run length is estimated in FP32 and only ever lowered, so the
+// FP64 work is a handful of adds and multiplies (no division).
+PW_HD int delta_jump(double delta, double dist, double step, int jmax, double *c)
+{
+	const uint64_t db = dbits(delta), sb = dbits(step);
+	const int64_t ed = (int64_t)(db >> 52), es = (int64_t)(sb >> 52);   // biased exponents (both positive)
+	if (!(delta > 0.0) || !(step > 0.0) || jmax <= 0 || ed < 60 || ed > 2000 || es == 0)
+		return 0;
+	// step = ms * 2^(es - 1075) with the 53-bit integer mantissa ms; u = 2^(ed - 1075)
+	const int64_t k = ed - es;                 // step / u = ms / 2^k
+	if (k > 53)
+		return 0;                              // step below half an ulp of delta: it never moves delta
+	if (k >= 1) {
+		const uint64_t ms = (sb & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull;
+		if ((ms & ((uint64_t(1) << k) - 1u)) == (uint64_t(1) << (k - 1)))
+			return 0;                          // a tie
+	}
+	const double top = bitsd((uint64_t)(ed + 1) << 52);   // 2^(e+1)
+	const double cc = sub(add(delta, step), delta);
+	if (!(cc > 0.0))
+		return 0;
+	// estimates of the two bounds (relative error below 4e-7: two roundings to FP32 and
+	// one correctly rounded division), lowered by 1e-6 before the floor, so that the
+	// count never exceeds the exact bound and the products below are exact
+	const float fc = (float)cc;
+	const float ka = (float)sub(sub(top, delta), step) / fc + 1.f;
+	const float kb = (float)sub(dist, delta) / fc;
+	float kf = fminf(fminf(ka, kb), (float)jmax);
+	kf = kf * (1.f - 1e-6f);
+	if (!(kf >= 1.f))
+		return 0;
+	int n = kf >= 2147483520.f ? 2147483520 : (int)kf;
+	n = n < jmax ? n : jmax;
+	const double last = add(delta, mul((double)(n - 1), cc));   // exact when the bounds hold
+	if (!(step <= sub(top, last) && add(last, cc) <= dist))
+		return 0;
+	*c = cc;
+	return n;
+}
+
+// delta after j iterations of advance_delta, bit-identical to running them
+// one by one (runs of iterations inside one binade are taken at once).
+PW_HD double walk_delta(double delta, double dist, double step, int j)
+{
+	while (j > 0) {
+		double c;
+		const int k = delta_jump(delta, dist, step, j, &c);
+		if (k > 0) {
+			delta = add(delta, mul((double)k, c));
+			j -= k;
+		} else {
+			delta = advance_delta(delta, dist, step);
+			j--;
+		}
+	}
+	return delta;
 }
 
 // ---------------------------------------------------------------- Moeller

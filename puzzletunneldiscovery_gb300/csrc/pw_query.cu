@@ -104,9 +104,7 @@ __device__ __forceinline__ void seg_slerp(const SegParams &P, pwm::SlerpParams &
 __device__ __noinline__ void seg_state64(const StateSrc &src, uint32_t s, uint32_t k, double *q)
 {
 	const SegParams &P = src.seg[s];
-	double delta = src.ckpt[P.ckpt_base + (k >> 5)];
-	for (uint32_t j = 0; j < (k & 31u); j++)
-		delta = pwm::advance_delta(delta, P.dist, P.step);
+	const double delta = pwm::walk_delta(src.ckpt[P.ckpt_base + (k >> 5)], P.dist, P.step, (int)(k & 31u));
 	const double tau = pwm::mul(delta, P.inv_dist);
 	pwm::SlerpParams S;
 	seg_slerp(P, S);
@@ -352,9 +350,7 @@ __device__ __noinline__ void chunk_step_qf(const WorldDev &W, const StateSrc &sr
                                            int lane, QFs &o)
 {
 	const SegParams &P = src.seg[s];
-	double delta = src.ckpt[ckslot];
-	for (int t = 0; t < lane; t++)
-		delta = pwm::advance_delta(delta, P.dist, P.step);
+	const double delta = pwm::walk_delta(src.ckpt[ckslot], P.dist, P.step, lane);
 	const double tau = pwm::mul(delta, P.inv_dist);
 	pwm::SlerpParams S;
 	seg_slerp(P, S);
@@ -767,9 +763,7 @@ __global__ void k_seg_anchors(WorldDev W, const double *from, const double *to, 
 		if (j >= (K + 31) / 32)
 			continue;                    // a slot past the segment's chunks (or no steps)
 		const int cnt = (int)min((int64_t)32, K - 32 * j);
-		double d = ckpt[c];
-		for (int i = 0; i < anchor_of(cnt); i++)
-			d = pwm::advance_delta(d, P.dist, P.step);
+		const double d = pwm::walk_delta(ckpt[c], P.dist, P.step, anchor_of(cnt));
 		seg_step_qf(W, from + 7 * lo, to + 7 * lo, P, d, anchors[c]);
 	}
 }
@@ -836,12 +830,11 @@ __global__ void k_seg_setup(WorldDev W, const double *from, const double *to, in
 				}
 				ckpt[P.ckpt_base + (K >> 5)] = delta;
 				// a chunk that ends well below dist (room counted in FP32, 8 steps of
-				// margin) takes every branch of the loop the same way: its deltas are the
-				// plain sums, so only the adds run (same FP64 values, bit for bit)
+				// margin) takes every branch of the loop the same way: its 32 updates are
+				// taken at once where they stay in one binade (same FP64 values, bit for bit)
 				const float room = __fdiv_rn((float)pwm::sub(dist, delta), (float)step);
 				if (room > 40.f) {
-					for (int i = 0; i < 32; i++)
-						delta = pwm::add(delta, step);
+					delta = pwm::walk_delta(delta, dist, step, 32);
 					K += 32;
 					continue;
 				}
@@ -1444,9 +1437,7 @@ __global__ void k_contact_states_ckpt(const double *from, const double *to, cons
 	const SegParams &P = params[i];
 	const int32_t k = first[i];
 	auto state_at = [&](int64_t j, double *q) {
-		double d = ckpt[P.ckpt_base + (j >> 5)];
-		for (int64_t r = 0; r < (j & 31); r++)
-			d = pwm::advance_delta(d, P.dist, P.step);
+		const double d = pwm::walk_delta(ckpt[P.ckpt_base + (j >> 5)], P.dist, P.step, (int)(j & 31));
 		const double t = pwm::mul(d, P.inv_dist);
 		pwm::SlerpParams S;
 		seg_slerp(P, S);

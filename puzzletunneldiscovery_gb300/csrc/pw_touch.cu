@@ -57,11 +57,10 @@ __global__ void k_contact_states(const double *from, const double *to, const int
 	pwm::slerp_setup(a, b, P);
 	// delta of step j is the value after j updates of the loop (step 0: verify_delta)
 	double prev = 0.0, delta = verify_delta;
-	int64_t j = 0;
 	if (k >= 0) {
-		for (; j < k; j++) {
-			prev = delta;
-			delta = pwm::advance_delta(delta, dist, verify_delta);
+		if (k > 0) {
+			prev = pwm::walk_delta(delta, dist, verify_delta, k - 1);
+			delta = pwm::advance_delta(prev, dist, verify_delta);
 		}
 		const double t = pwm::mul(delta, inv);
 		pwm::interpolate_p(a, b, P, t, st);
@@ -80,6 +79,13 @@ __global__ void k_contact_states(const double *from, const double *to, const int
 	}
 	// every step free: the last state the loop checked, done = true, outer tau 0
 	while (true) {
+		// runs of updates that stay at or below dist, taken at once (walk_delta's rule)
+		double c;
+		const int jump = pwm::delta_jump(delta, dist, verify_delta, 1 << 30, &c);
+		if (jump > 0) {
+			delta = pwm::add(delta, pwm::mul((double)jump, c));
+			continue;
+		}
 		const double next = pwm::advance_delta(delta, dist, verify_delta);
 		if (!(next <= dist))
 			break;
