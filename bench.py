@@ -532,6 +532,30 @@ def run_ours(args):
     tot_ms, tot_checks = max_time_sum_units(my_ms, my_checks, ws, dev)
     value = tot_checks / (tot_ms / 1e3)
 
+    # both kinds of BVH node box on the same batch: time per step and the tests they take
+    boxes = {}
+    default_kind = uw.get_node_boxes()
+    for kind in ("aligned", "oriented"):
+        uw.set_node_boxes(kind)
+        for _ in range(2):
+            work.gpu(uw, a, b)
+        bms, bst = [], None
+        for i in range(min(args.steps, 5)):
+            flush.zero_()
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            fb = work.gpu(uw, a, b)
+            s1.record(stream)
+            bst = uw.last_stats()
+            bms.append(s0.elapsed_time(s1))
+        if not torch.equal(fb, f):
+            raise RuntimeError("%s node boxes changed the results" % kind)
+        boxes[kind] = {"ms_per_step": sum(bms) / len(bms), "node_tests": bst["node_tests"],
+                       "leaf_tests": bst["leaf_tests"], "fp64_retests": bst["retests"],
+                       "traverse_ms": bst["traverse_ms"]}
+    uw.set_node_boxes(default_kind)
+    boxes["default"] = default_kind
+
     # the same query replayed as one CUDA graph (graph mode: no host synchronisation inside the step)
     graph_ms = None
     if args.workload == "segments":
@@ -628,7 +652,8 @@ def run_ours(args):
                             "leaf_tests": last["leaf_tests"], "fp64_retests": last["retests"],
                             "fp64_retest_rate_per_leaf": last["retests"] / max(1, last["leaf_tests"]),
                             "inline_retests": last["inline_retests"], "retest_ms": last["retest_ms"],
-                            "step_ms": step_ms, "autotune": tuned, "graph_replay_ms_per_step": graph_ms},
+                            "step_ms": step_ms, "autotune": tuned, "graph_replay_ms_per_step": graph_ms,
+                            "node_boxes": boxes},
                            **extra)}
     if sur is not None:
         line["detail"]["surrogate"] = sur

@@ -44,6 +44,10 @@ extern "C" {
 #define PW_SEG_TRANSIT 0       /* transit_state_to(_with_contact): step = verify_delta */
 #define PW_SEG_TRANSITION 1    /* is_valid_transition: step = min(dist / 2, verify_delta) */
 
+/* Node boxes of the BVH traversals (pw_world_set_node_boxes). */
+#define PW_BOXES_ALIGNED 0     /* boxes aligned with each mesh's own frame */
+#define PW_BOXES_ORIENTED 1    /* boxes along the principal axes of each node's vertices (default) */
+
 /* First-contact codes written by pw_segments_first_contact (>= 0: step index). */
 #define PW_STEP_FREE (-1)      /* every step free: the reference's `done` is true */
 #define PW_STEP_NONE (-2)      /* verify_delta >= dist: no step checked, `done` false (unit_world.cc:445-447) */
@@ -184,6 +188,14 @@ PW_API int pw_segments_reserve(pw_world *w, int64_t n, int64_t total_chunks, int
  * occupancy).  0 keeps the default.  Verdicts do not depend on it. */
 PW_API int pw_world_set_launch_config(pw_world *w, int kernel, int width, int soft_cap, int blocks);
 PW_API int pw_world_get_launch_config(pw_world *w, int kernel, int *width, int *soft_cap, int *blocks);
+
+/* The node boxes the traversal kernels test: PW_BOXES_ORIENTED (default) or
+ * PW_BOXES_ALIGNED.  Both are built with every mesh; verdicts are identical,
+ * only the number of box and triangle tests differs.  FCL's OBBRSS nodes
+ * (cdmodel.cc:17-18) are oriented boxes; the LBVH here fits both kinds to the
+ * same hierarchy.  Not allowed in graph mode (captured launches hold the kernel). */
+PW_API int pw_world_set_node_boxes(pw_world *w, int kind);
+PW_API int pw_world_get_node_boxes(pw_world *w, int *kind);
 
 /* The result tuple of transit_state_to_with_contact (unit_world.cc:405-474) for n
  * segments, from the codes pw_segments_first_contact(PW_SEG_TRANSIT) wrote for

@@ -26,6 +26,8 @@ PW_SEG_TRANSITION = 1
 PW_STEP_FREE = -1
 PW_STEP_NONE = -2
 PW_STEP_INVALID = -3
+PW_BOXES_ALIGNED = 0
+PW_BOXES_ORIENTED = 1
 
 # every entry point declared in include/pw_collide.h
 EXPORTS = (
@@ -39,7 +41,7 @@ EXPORTS = (
     "pw_segments_contact_states", "pw_world_segments_contact_states", "pw_world_set_graph_mode",
     "pw_segments_reserve", "pw_world_set_launch_config",
     "pw_world_get_launch_config", "pw_expansion_crossings", "pw_world_scratch_epoch", "pw_expand_states",
-    "pw_ompl_check_motions", "pw_ompl_motion_states",
+    "pw_ompl_check_motions", "pw_ompl_motion_states", "pw_world_set_node_boxes", "pw_world_get_node_boxes",
     # include/pw_mlp.h
     "pw_mlp_create", "pw_mlp_destroy", "pw_mlp_num_params", "pw_mlp_get_params", "pw_mlp_set_params",
     "pw_mlp_get_grads", "pw_mlp_predict", "pw_mlp_gradients", "pw_mlp_train_step", "pw_mlp_predict_mma",
@@ -142,6 +144,8 @@ def load():
         "pw_segments_reserve": (ctypes.c_int, [vp, i64, i64, i64]),
         "pw_world_set_launch_config": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
         "pw_world_get_launch_config": (ctypes.c_int, [vp, ctypes.c_int, i32p, i32p, i32p]),
+        "pw_world_set_node_boxes": (ctypes.c_int, [vp, ctypes.c_int]),
+        "pw_world_get_node_boxes": (ctypes.c_int, [vp, i32p]),
         "pw_segments_contact_states": (ctypes.c_int, [vp, vp, vp, i64, ctypes.c_double, vp, vp, vp, vp, vp, vp,
                                                       vp]),
         "pw_mlp_create": (ctypes.c_int, [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_uint64]),

@@ -102,6 +102,86 @@ PW_HD bool sat_disjoint32(const float4 &A0, const float4 &A1, const float4 &B0, 
 	return sat_sep32(A0, A1, B0, B1, Q0, Q1, Q2, Q3) > 0.f;
 }
 
+// Entrywise error of a stored FP32 axis row against the orthonormal FP64 frame it
+// rounds (half an ulp of an entry of magnitude <= 1, plus the FP64 frame's own
+// departure from orthonormality).
+constexpr float AXIS_ERR = 6.0e-8f;
+
+// Separating-axis test of two oriented node boxes: the env node (centre A0,
+// half-extents A1, axes as rows E0..E2, env frame) and the robot node (centre B0,
+// half-extents B1, axes as rows G0..G2, robot frame) placed by the slot's
+// transform (Q0..Q3 as in sat_sep32).  The robot box is brought into the env
+// box's frame: offset T = E (R c_r + t - c_e) and rotation M = E R G^T, whose
+// columns are the robot box's axes seen along the env box's axes.
+//   Error model: M differs entrywise from the exact rotation E* Q G*^T (E*, G*
+//   the exact orthonormal frames, Q the rotation closest to the state's) by at
+//   most 3 er + 5 AXIS_ERR + 15 u (two 3-term products of matrices with unit
+//   rows; u = 2^-24), doubled for safety; T differs from its exact value by the
+//   robot point placement error the margin covers, seen along unit axes
+//   (doubled margin), plus (AXIS_ERR + 4 u) |d|_1 (doubled) for the rounded env
+//   axes and the FP32 products.  Returns a lower bound on the distance when a
+//   separating axis is certified (> 0), else -1.
+PW_HD float sat_sep32_obb(const float4 &A0, const float4 &A1, const float4 &E0, const float4 &E1, const float4 &E2,
+                          const float4 &B0, const float4 &B1, const float4 &G0, const float4 &G1, const float4 &G2,
+                          const float4 &Q0, const float4 &Q1, const float4 &Q2, const float4 &Q3)
+{
+	// robot node centre in the env frame, relative to the env node centre
+	const float dx = fmaf(Q0.x, B0.x, fmaf(Q0.y, B0.y, fmaf(Q0.z, B0.z, Q0.w))) - A0.x;
+	const float dy = fmaf(Q1.x, B0.x, fmaf(Q1.y, B0.y, fmaf(Q1.z, B0.z, Q1.w))) - A0.y;
+	const float dz = fmaf(Q2.x, B0.x, fmaf(Q2.y, B0.y, fmaf(Q2.z, B0.z, Q2.w))) - A0.z;
+	const float T0 = fmaf(E0.x, dx, fmaf(E0.y, dy, E0.z * dz));
+	const float T1 = fmaf(E1.x, dx, fmaf(E1.y, dy, E1.z * dz));
+	const float T2 = fmaf(E2.x, dx, fmaf(E2.y, dy, E2.z * dz));
+	// robot box axis j in the env frame: N_j = R g_j
+	const float N00 = fmaf(Q0.x, G0.x, fmaf(Q0.y, G0.y, Q0.z * G0.z));
+	const float N10 = fmaf(Q1.x, G0.x, fmaf(Q1.y, G0.y, Q1.z * G0.z));
+	const float N20 = fmaf(Q2.x, G0.x, fmaf(Q2.y, G0.y, Q2.z * G0.z));
+	const float N01 = fmaf(Q0.x, G1.x, fmaf(Q0.y, G1.y, Q0.z * G1.z));
+	const float N11 = fmaf(Q1.x, G1.x, fmaf(Q1.y, G1.y, Q1.z * G1.z));
+	const float N21 = fmaf(Q2.x, G1.x, fmaf(Q2.y, G1.y, Q2.z * G1.z));
+	const float N02 = fmaf(Q0.x, G2.x, fmaf(Q0.y, G2.y, Q0.z * G2.z));
+	const float N12 = fmaf(Q1.x, G2.x, fmaf(Q1.y, G2.y, Q1.z * G2.z));
+	const float N22 = fmaf(Q2.x, G2.x, fmaf(Q2.y, G2.y, Q2.z * G2.z));
+	// M_ij = e_i . N_j
+	const float R00 = fmaf(E0.x, N00, fmaf(E0.y, N10, E0.z * N20));
+	const float R01 = fmaf(E0.x, N01, fmaf(E0.y, N11, E0.z * N21));
+	const float R02 = fmaf(E0.x, N02, fmaf(E0.y, N12, E0.z * N22));
+	const float R10 = fmaf(E1.x, N00, fmaf(E1.y, N10, E1.z * N20));
+	const float R11 = fmaf(E1.x, N01, fmaf(E1.y, N11, E1.z * N21));
+	const float R12 = fmaf(E1.x, N02, fmaf(E1.y, N12, E1.z * N22));
+	const float R20 = fmaf(E2.x, N00, fmaf(E2.y, N10, E2.z * N20));
+	const float R21 = fmaf(E2.x, N01, fmaf(E2.y, N11, E2.z * N21));
+	const float R22 = fmaf(E2.x, N02, fmaf(E2.y, N12, E2.z * N22));
+	const float a0 = A1.x, a1 = A1.y, a2 = A1.z, b0 = B1.x, b1 = B1.y, b2 = B1.z;
+	const float er = fmaf(6.f, Q3.x, 2.f * (5.f * AXIS_ERR + 15.f * U32));
+	const float eT = 2.f * (AXIS_ERR + 4.f * U32) * (fabsf(dx) + fabsf(dy) + fabsf(dz));
+	const float m = fmaf(er, (a0 + a1 + a2) + (b0 + b1 + b2), fmaf(2.f, Q3.y, eT));
+	const float shrink = 1.f - 4.f * er;
+	const float aR00 = fabsf(R00), aR01 = fabsf(R01), aR02 = fabsf(R02);
+	const float aR10 = fabsf(R10), aR11 = fabsf(R11), aR12 = fabsf(R12);
+	const float aR20 = fabsf(R20), aR21 = fabsf(R21), aR22 = fabsf(R22);
+	float g;
+	// env box axes (unit length)
+	if ((g = fabsf(T0) - (a0 + fmaf(b0, aR00, fmaf(b1, aR01, fmaf(b2, aR02, m))))) > 0.f) return g;
+	if ((g = fabsf(T1) - (a1 + fmaf(b0, aR10, fmaf(b1, aR11, fmaf(b2, aR12, m))))) > 0.f) return g;
+	if ((g = fabsf(T2) - (a2 + fmaf(b0, aR20, fmaf(b1, aR21, fmaf(b2, aR22, m))))) > 0.f) return g;
+	// robot box axes
+	if ((g = fabsf(fmaf(T0, R00, fmaf(T1, R10, T2 * R20))) - (b0 + fmaf(a0, aR00, fmaf(a1, aR10, fmaf(a2, aR20, m))))) > 0.f) return g * shrink;
+	if ((g = fabsf(fmaf(T0, R01, fmaf(T1, R11, T2 * R21))) - (b1 + fmaf(a0, aR01, fmaf(a1, aR11, fmaf(a2, aR21, m))))) > 0.f) return g * shrink;
+	if ((g = fabsf(fmaf(T0, R02, fmaf(T1, R12, T2 * R22))) - (b2 + fmaf(a0, aR02, fmaf(a1, aR12, fmaf(a2, aR22, m))))) > 0.f) return g * shrink;
+	// cross axes e_i x (column j of M)
+	if ((g = fabsf(T2 * R10 - T1 * R20) - fmaf(a1, aR20, fmaf(a2, aR10, fmaf(b1, aR02, fmaf(b2, aR01, m))))) > 0.f) return g * shrink;
+	if ((g = fabsf(T2 * R11 - T1 * R21) - fmaf(a1, aR21, fmaf(a2, aR11, fmaf(b0, aR02, fmaf(b2, aR00, m))))) > 0.f) return g * shrink;
+	if ((g = fabsf(T2 * R12 - T1 * R22) - fmaf(a1, aR22, fmaf(a2, aR12, fmaf(b0, aR01, fmaf(b1, aR00, m))))) > 0.f) return g * shrink;
+	if ((g = fabsf(T0 * R20 - T2 * R00) - fmaf(a0, aR20, fmaf(a2, aR00, fmaf(b1, aR12, fmaf(b2, aR11, m))))) > 0.f) return g * shrink;
+	if ((g = fabsf(T0 * R21 - T2 * R01) - fmaf(a0, aR21, fmaf(a2, aR01, fmaf(b0, aR12, fmaf(b2, aR10, m))))) > 0.f) return g * shrink;
+	if ((g = fabsf(T0 * R22 - T2 * R02) - fmaf(a0, aR22, fmaf(a2, aR02, fmaf(b0, aR11, fmaf(b1, aR10, m))))) > 0.f) return g * shrink;
+	if ((g = fabsf(T1 * R00 - T0 * R10) - fmaf(a0, aR10, fmaf(a1, aR00, fmaf(b1, aR22, fmaf(b2, aR21, m))))) > 0.f) return g * shrink;
+	if ((g = fabsf(T1 * R01 - T0 * R11) - fmaf(a0, aR11, fmaf(a1, aR01, fmaf(b0, aR22, fmaf(b2, aR20, m))))) > 0.f) return g * shrink;
+	if ((g = fabsf(T1 * R02 - T0 * R12) - fmaf(a0, aR12, fmaf(a1, aR02, fmaf(b0, aR21, fmaf(b1, aR20, m))))) > 0.f) return g * shrink;
+	return -1.f;
+}
+
 PW_HD float3 f3(float4 a) { return make_float3(a.x, a.y, a.z); }
 PW_HD float3 f3add(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
 PW_HD float3 f3sub(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }

@@ -17,18 +17,24 @@
 //   triA/B/C[slot] = FP32 vertex 0, edge 1-0, edge 2-0, each rounded once from FP64
 //   (w of triA = original face id).
 // Boxes are conservative: they contain the FP64 vertices exactly.
+//   Oriented boxes on the same hierarchy (obbA = (centre.xyz, left child),
+//   obbB = (half-extent.xyz, right child), obbR0..2 = the box's axes as rows, FP32
+//   roundings of an orthonormal FP64 frame): axes from the principal directions
+//   of the node's vertices, extents measured in FP64 around the FP32 centre and
+//   rounded up, so the box spanned by the exact FP64 frame contains the vertices.
 struct MeshDev {
 	int32_t ntri = 0;
 	int32_t nvert = 0;
 	int32_t leaf_base = 0;
 	int32_t depth = 0;
 	float4 *nodeA = nullptr, *nodeB = nullptr;
+	float4 *obbA = nullptr, *obbB = nullptr, *obbR0 = nullptr, *obbR1 = nullptr, *obbR2 = nullptr;
 	float4 *triA = nullptr, *triB = nullptr, *triC = nullptr;
 	double *V64 = nullptr;   // nvert x 3 (env: perturbation frame; robot: local frame)
 	int32_t *F = nullptr;    // ntri x 3
 	float r1 = 0.f;          // L1 bound of any point of any node box (robot: local frame)
 	double r2 = 0.0;         // max Euclidean norm of a vertex (robot: local frame)
-	float emax = 0.f;        // max |coordinate| of any vertex
+	float emax = 0.f;        // max |coordinate| of any vertex or oriented node box corner
 };
 
 struct WorldDev {
@@ -120,7 +126,8 @@ struct pw_world {
 	int launch_width[2] = { 0, 0 };     // queries a warp takes per grab (states kernel only)
 	int launch_soft_cap[2] = { 0, 0 };  // traversal stack soft cap
 	int launch_blocks[2] = { 0, 0 };    // resident blocks per SM of the persistent kernel
-	int grid_cache[2] = { 0, 0 };       // grid of the persistent kernels under that configuration
+	int grid_cache[4] = { 0, 0, 0, 0 }; // grid of the persistent kernels under that configuration, per box kind
+	int node_boxes = PW_BOXES_ORIENTED; // node boxes the traversals use (pw_world_set_node_boxes)
 	// the last segment query's inputs: its parameters and checkpoints stay in the
 	// scratch, so the transit tuples of the same batch can start from them
 	const double *last_seg_from = nullptr, *last_seg_to = nullptr;

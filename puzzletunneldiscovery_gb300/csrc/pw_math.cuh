@@ -337,22 +337,117 @@ PW_HD int delta_jump(double delta, double dist, double step, int jmax, double *c
 	return n;
 }
 
-// delta after j iterations of advance_delta, bit-identical to running them
-// one by one (runs of iterations inside one binade are taken at once).
+// Exactly k iterations of advance_delta from `delta` taken at once, when they stay
+// inside delta's binade, meet no rounding tie and end at or below dist: then
+// *res = delta + k c (c as for delta_jump) and the result is true.  No estimate
+// is needed: last = delta + (k-1) c is exact whenever it stays below 2^(e+1); if
+// (k-1) c or the sum rounds, the exact value is already at or above 2^(e+1), the
+// rounded one too (rounding is monotone and 2^(e+1) is representable), and the
+// binade test fails as it must.  For a constant k the FP64 work is two adds, a
+// subtract, a multiply by a constant and two compares.
+PW_HD bool delta_try(double delta, double dist, double step, int k, double *res)
+{
+	const uint64_t db = dbits(delta), sb = dbits(step);
+	const int64_t ed = (int64_t)(db >> 52), es = (int64_t)(sb >> 52);
+	if (!(delta > 0.0) || !(step > 0.0) || k <= 0 || ed < 60 || ed > 2000 || es == 0)
+		return false;
+	const int64_t sh = ed - es;
+	if (sh > 53)
+		return false;
+	if (sh >= 1) {
+		const uint64_t ms = (sb & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull;
+		if ((ms & ((uint64_t(1) << sh) - 1u)) == (uint64_t(1) << (sh - 1)))
+			return false;                      // a tie
+	}
+	const double top = bitsd((uint64_t)(ed + 1) << 52);
+	const double cc = sub(add(delta, step), delta);
+	if (!(cc > 0.0))
+		return false;
+	const double last = add(delta, mul((double)(k - 1), cc));
+	if (!(step <= sub(top, last)))
+		return false;
+	const double r = add(last, cc);
+	if (!(r <= dist))
+		return false;
+	*res = r;
+	return true;
+}
+
+// delta after j iterations of advance_delta, bit-identical to running them one
+// by one: the whole run at once where delta_try allows it, otherwise one
+// iteration and a new try (a run that crosses a binade boundary or meets dist).
 PW_HD double walk_delta(double delta, double dist, double step, int j)
 {
 	while (j > 0) {
-		double c;
-		const int k = delta_jump(delta, dist, step, j, &c);
-		if (k > 0) {
-			delta = add(delta, mul((double)k, c));
-			j -= k;
-		} else {
-			delta = advance_delta(delta, dist, step);
-			j--;
-		}
+		double r;
+		if (delta_try(delta, dist, step, j, &r))
+			return r;
+		delta = advance_delta(delta, dist, step);
+		j--;
 	}
 	return delta;
+}
+
+// Eigenvectors (rows of E, orthonormal) of the symmetric 3 x 3 matrix S (xx, yy, zz,
+// xy, xz, yz) by cyclic Jacobi rotations; the principal axes of an oriented node box.
+// Plain FP64 (any orthonormal frame gives a valid box: accuracy only tightens it).
+PW_HD void jacobi_eigen3(const double S[6], double E[9])
+{
+	double a[3][3] = { { S[0], S[3], S[4] }, { S[3], S[1], S[5] }, { S[4], S[5], S[2] } };
+	double v[3][3] = { { 1, 0, 0 }, { 0, 1, 0 }, { 0, 0, 1 } };
+	for (int sweep = 0; sweep < 32; sweep++) {
+		const double off = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
+		const double dia = fabs(a[0][0]) + fabs(a[1][1]) + fabs(a[2][2]);
+		if (!(off > 1e-300) || off <= 1e-18 * dia)
+			break;
+		for (int p = 0; p < 2; p++)
+			for (int q = p + 1; q < 3; q++) {
+				if (!(fabs(a[p][q]) > 1e-300))
+					continue;
+				const double th = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+				const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+				const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+				for (int k = 0; k < 3; k++) {
+					const double akp = a[k][p], akq = a[k][q];
+					a[k][p] = c * akp - s * akq;
+					a[k][q] = s * akp + c * akq;
+				}
+				for (int k = 0; k < 3; k++) {
+					const double apk = a[p][k], aqk = a[q][k];
+					a[p][k] = c * apk - s * aqk;
+					a[q][k] = s * apk + c * aqk;
+				}
+				for (int k = 0; k < 3; k++) {
+					const double vkp = v[k][p], vkq = v[k][q];
+					v[k][p] = c * vkp - s * vkq;
+					v[k][q] = s * vkp + c * vkq;
+				}
+			}
+	}
+	// columns of v are the eigenvectors; re-orthonormalise (Gram-Schmidt, then a cross product)
+	double e0[3] = { v[0][0], v[1][0], v[2][0] }, e1[3] = { v[0][1], v[1][1], v[2][1] };
+	const double n0 = sqrt(e0[0] * e0[0] + e0[1] * e0[1] + e0[2] * e0[2]);
+	for (int k = 0; k < 3; k++) e0[k] /= n0;
+	const double d = e0[0] * e1[0] + e0[1] * e1[1] + e0[2] * e1[2];
+	for (int k = 0; k < 3; k++) e1[k] -= d * e0[k];
+	const double n1 = sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+	if (!(n1 > 1e-6)) {
+		// a degenerate pair (never for Jacobi's orthogonal output): any perpendicular unit vector
+		const int m = fabs(e0[0]) < 0.6 ? 0 : 1;
+		double u[3] = { 0, 0, 0 };
+		u[m] = 1.0;
+		const double du = e0[m];
+		for (int k = 0; k < 3; k++) e1[k] = u[k] - du * e0[k];
+		const double nn = sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+		for (int k = 0; k < 3; k++) e1[k] /= nn;
+	} else {
+		for (int k = 0; k < 3; k++) e1[k] /= n1;
+	}
+	E[0] = e0[0]; E[1] = e0[1]; E[2] = e0[2];
+	E[3] = e1[0]; E[4] = e1[1]; E[5] = e1[2];
+	E[6] = e0[1] * e1[2] - e0[2] * e1[1];
+	E[7] = e0[2] * e1[0] - e0[0] * e1[2];
+	E[8] = e0[0] * e1[1] - e0[1] * e1[0];
 }
 
 // ---------------------------------------------------------------- Moeller

@@ -184,6 +184,30 @@ __device__ __forceinline__ uint32_t retest_inline(const WorldDev &W, const WarpS
 	return __reduce_or_sync(FULL, h ? (1u << slot) : 0u);
 }
 
+// Separating-axis test of env node e and robot node r under the slot transform
+// Q0..Q3, with axis-aligned node boxes (OBB = false: boxes in each mesh's frame)
+// or oriented ones (OBB = true).  Returns the certified separation (> 0) or -1,
+// and the two nodes' (centre, left child) and (half-extents, right child).
+template <bool OBB>
+__device__ __forceinline__ float node_pair_sep(const WorldDev &W, uint32_t e, uint32_t r, const float4 &Q0,
+                                               const float4 &Q1, const float4 &Q2, const float4 &Q3, float4 &A0,
+                                               float4 &A1, float4 &B0, float4 &B1)
+{
+	if (OBB) {
+		A0 = __ldg(W.env.obbA + e);
+		A1 = __ldg(W.env.obbB + e);
+		B0 = __ldg(W.rob.obbA + r);
+		B1 = __ldg(W.rob.obbB + r);
+		return sat_sep32_obb(A0, A1, __ldg(W.env.obbR0 + e), __ldg(W.env.obbR1 + e), __ldg(W.env.obbR2 + e), B0, B1,
+		                     __ldg(W.rob.obbR0 + r), __ldg(W.rob.obbR1 + r), __ldg(W.rob.obbR2 + r), Q0, Q1, Q2, Q3);
+	}
+	A0 = __ldg(W.env.nodeA + e);
+	A1 = __ldg(W.env.nodeB + e);
+	B0 = __ldg(W.rob.nodeA + r);
+	B1 = __ldg(W.rob.nodeB + r);
+	return sat_sep32(A0, A1, B0, B1, Q0, Q1, Q2, Q3);
+}
+
 // One warp answers up to 32 queries at once (slots = set bits of `open`;
 // sm.qf, sm.slot_query and sm.slot_step describe them): every stack entry
 // carries its slot, lanes test pairs of any open slot, and a slot closes at its
@@ -192,7 +216,7 @@ __device__ __forceinline__ uint32_t retest_inline(const WorldDev &W, const WarpS
 // INLINE = false: uncertain pairs go to the FP64 queue; the slots that lost a pair
 // to a full queue are returned in `ovf`.  INLINE = true (the second pass over such
 // slots): every uncertain pair is re-tested in FP64 at once.
-template <uint64_t CAP, bool INLINE>
+template <uint64_t CAP, bool INLINE, bool OBB>
 __device__ uint32_t traverse_batch(const WorldDev &W, WarpSmem &sm, int lane, uint32_t open, int soft_cap,
                                    QueryCounters *ctr, RetestEntry *rq, const StateSrc &src, LaneStats &st,
                                    uint32_t &ovf)
@@ -285,11 +309,10 @@ __device__ uint32_t traverse_batch(const WorldDev &W, WarpSmem &sm, int lane, ui
 		bool push = false, leaf = false;
 		uint2 c0 = make_uint2(0u, 0u), c1 = make_uint2(0u, 0u);
 		if (active) {
-			const float4 A0 = __ldg(W.env.nodeA + pr.x), A1 = __ldg(W.env.nodeB + pr.x);
-			const float4 B0 = __ldg(W.rob.nodeA + rn), B1 = __ldg(W.rob.nodeB + rn);
+			float4 A0, A1, B0, B1;
 			const QFs &Q = sm.qf[slot];
 			st.node++;
-			if (!sat_disjoint32(A0, A1, B0, B1, Q.q[0], Q.q[1], Q.q[2], Q.q[3])) {
+			if (!(node_pair_sep<OBB>(W, pr.x, rn, Q.q[0], Q.q[1], Q.q[2], Q.q[3], A0, A1, B0, B1) > 0.f)) {
 				const bool la = pr.x >= ebase, lb = rn >= rbase;
 				if (la && lb) {
 					leaf = true;
@@ -373,7 +396,7 @@ __device__ __noinline__ void chunk_step_qf(const WorldDev &W, const StateSrc &sr
 //   which take the per-step leaf tests.
 // Returns the lowest step in contact as a one-bit mask (0 when none).
 // INLINE and `ovf` as in traverse_batch.
-template <uint64_t CAP, bool INLINE>
+template <uint64_t CAP, bool INLINE, bool OBB>
 __device__ uint32_t traverse_chunk(const WorldDev &W, WarpSmem &sm, int lane, int nopen, int cnt, int anchor,
                                    float motion, int soft_cap, QueryCounters *ctr, RetestEntry *rq,
                                    const StateSrc &src, LaneStats &st, uint32_t seg, int64_t ckslot,
@@ -483,8 +506,7 @@ __device__ uint32_t traverse_chunk(const WorldDev &W, WarpSmem &sm, int lane, in
 		bool push2 = false, push1 = false, leaf = false, need = false;
 		uint2 c0 = make_uint2(0u, 0u), c1 = make_uint2(0u, 0u);
 		if (active) {
-			const float4 A0 = __ldg(W.env.nodeA + pr.x), A1 = __ldg(W.env.nodeB + pr.x);
-			const float4 B0 = __ldg(W.rob.nodeA + rn), B1 = __ldg(W.rob.nodeB + rn);
+			float4 A0, A1, B0, B1;
 			const int ref = detailed ? (s0 + s1) >> 1 : anchor;
 			const int reach = max(abs(s0 - ref), abs(s1 - ref));
 			const QFs &Q = sm.qf[ref];
@@ -496,7 +518,7 @@ __device__ uint32_t traverse_chunk(const WorldDev &W, WarpSmem &sm, int lane, in
 				Q3.y += infl;
 			}
 			st.node++;
-			if (!(sat_sep32(A0, A1, B0, B1, Q0, Q1, Q2, Q3) > 0.f)) {
+			if (!(node_pair_sep<OBB>(W, pr.x, rn, Q0, Q1, Q2, Q3, A0, A1, B0, B1) > 0.f)) {
 				const bool la = pr.x >= ebase, lb = rn >= rbase;
 				const float ext = fmaxf(fmaxf(fmaxf(A1.x, A1.y), A1.z), fmaxf(fmaxf(B1.x, B1.y), B1.z));
 				const bool fine = (la && lb) || infl > 0.5f * ext;
@@ -587,13 +609,13 @@ __device__ void flush_stats(QueryCounters *ctr, LaneStats &st, unsigned long lon
 // FP64 queue: the same traversal with every uncertain pair re-tested inline.
 // Returns the mask of those slots in contact.  Not inlined: the FP64 code stays out
 // of the register allocation of the kernel's main loop.
-template <uint64_t CAP>
+template <uint64_t CAP, bool OBB>
 __device__ __noinline__ uint32_t resolve_states(const WorldDev &W, WarpSmem &sm, int lane, uint32_t open,
                                                 int soft_cap, QueryCounters *ctr, RetestEntry *rq,
                                                 const StateSrc &src, LaneStats &st)
 {
 	uint32_t unused = 0;
-	return traverse_batch<CAP, true>(W, sm, lane, open, soft_cap, ctr, rq, src, st, unused);
+	return traverse_batch<CAP, true, OBB>(W, sm, lane, open, soft_cap, ctr, rq, src, st, unused);
 }
 
 // Lane counters are flushed into the query counters before a 32-bit count can wrap.
@@ -602,7 +624,7 @@ __device__ __forceinline__ bool stats_full(const LaneStats &st, int lane)
 	return __any_sync(FULL, ((st.node | st.leaf | st.inl) >> 30) != 0u);
 }
 
-template <uint64_t CAP>
+template <uint64_t CAP, bool OBB>
 __global__ void __launch_bounds__(WARPS * 32, 8) k_states(WorldDev W, const double *states, int64_t n,
                                                        uint8_t *out, QueryCounters *ctr, RetestEntry *rq,
                                                        int soft_cap, int width)
@@ -639,10 +661,10 @@ __global__ void __launch_bounds__(WARPS * 32, 8) k_states(WorldDev W, const doub
 		__syncwarp();
 		const uint32_t open = (cnt == 32 ? FULL : ((1u << cnt) - 1u)) & ~bad;
 		uint32_t ovf = 0u;
-		uint32_t hit = traverse_batch<CAP, false>(W, sm, lane, open, soft_cap, ctr, rq, src, st, ovf) | bad;
+		uint32_t hit = traverse_batch<CAP, false, OBB>(W, sm, lane, open, soft_cap, ctr, rq, src, st, ovf) | bad;
 		ovf &= ~hit;
 		if (ovf)
-			hit |= resolve_states<CAP>(W, sm, lane, ovf, soft_cap, ctr, rq, src, st);
+			hit |= resolve_states<CAP, OBB>(W, sm, lane, ovf, soft_cap, ctr, rq, src, st);
 		if (lane < cnt)
 			out[base + lane] = ((hit >> lane) & 1u) ? 0 : 1;
 		queries += cnt;
@@ -831,10 +853,17 @@ __global__ void k_seg_setup(WorldDev W, const double *from, const double *to, in
 				ckpt[P.ckpt_base + (K >> 5)] = delta;
 				// a chunk that ends well below dist (room counted in FP32, 8 steps of
 				// margin) takes every branch of the loop the same way: its 32 updates are
-				// taken at once where they stay in one binade (same FP64 values, bit for bit)
+				// taken at once when they stay in one binade, else run as plain adds (same
+				// FP64 values, bit for bit)
 				const float room = __fdiv_rn((float)pwm::sub(dist, delta), (float)step);
 				if (room > 40.f) {
-					delta = pwm::walk_delta(delta, dist, step, 32);
+					double r;
+					if (pwm::delta_try(delta, dist, step, 32, &r)) {
+						delta = r;
+					} else {
+						for (int i = 0; i < 32; i++)
+							delta = pwm::add(delta, step);
+					}
 					K += 32;
 					continue;
 				}
@@ -907,6 +936,7 @@ __global__ void __launch_bounds__(1024) k_rounds(const uint32_t *sorted_keys, in
 // FP64 queue: steps 0 .. nopen-1 traversed again with every uncertain pair
 // re-tested inline (the anchor frame reloaded first).  Returns the lowest step in
 // contact as a one-bit mask.  Not inlined, as resolve_states.
+template <bool OBB>
 __device__ __noinline__ uint32_t resolve_chunk(const WorldDev &W, WarpSmem &sm, int lane, int nopen, int cnt,
                                                int anchor, float motion, int soft_cap, QueryCounters *ctr,
                                                RetestEntry *rq, const StateSrc &src, LaneStats &st, uint32_t seg,
@@ -916,7 +946,7 @@ __device__ __noinline__ uint32_t resolve_chunk(const WorldDev &W, WarpSmem &sm, 
 		sm.qf[anchor].q[lane] = src.anchors[ckslot].q[lane];
 	__syncwarp();
 	uint32_t unused = 0;
-	return traverse_chunk<RETEST_CAP, true>(W, sm, lane, nopen, cnt, anchor, motion, soft_cap, ctr, rq, src, st,
+	return traverse_chunk<RETEST_CAP, true, OBB>(W, sm, lane, nopen, cnt, anchor, motion, soft_cap, ctr, rq, src, st,
 	                                        seg, ckslot, ndetailed, unused);
 }
 
@@ -924,6 +954,7 @@ __device__ __noinline__ uint32_t resolve_chunk(const WorldDev &W, WarpSmem &sm, 
 // contacts prune later chunks.  A warp computes the chunk's FP64 states lane-
 // parallel, then answers its steps with one swept traversal and records the
 // first step in contact with atomicMin.
+template <bool OBB>
 __global__ void __launch_bounds__(WARPS * 32, 8) k_segments(WorldDev W, StateSrc src, const uint32_t *order,
                                                          const int64_t *round_off, const int64_t *nrounds_p,
                                                          int32_t *first, QueryCounters *ctr, RetestEntry *rq,
@@ -985,11 +1016,11 @@ __global__ void __launch_bounds__(WARPS * 32, 8) k_segments(WorldDev W, StateSrc
 		queries += lim;
 		const float motion = __double2float_ru(P.skip_scale);
 		uint32_t ovf = 0u;
-		uint32_t hit = traverse_chunk<RETEST_CAP, false>(W, sm, lane, lim, cnt, anchor, motion, soft_cap, ctr, rq,
+		uint32_t hit = traverse_chunk<RETEST_CAP, false, OBB>(W, sm, lane, lim, cnt, anchor, motion, soft_cap, ctr, rq,
 		                                                 src, st, s, ckslot, detailed, ovf);
 		// steps below the lowest contact that lost uncertain pairs to a full queue
 		if (ovf & (hit ? hit - 1u : FULL)) {
-			const uint32_t h2 = resolve_chunk(W, sm, lane, hit ? __ffs(hit) - 1 : lim, cnt, anchor, motion,
+			const uint32_t h2 = resolve_chunk<OBB>(W, sm, lane, hit ? __ffs(hit) - 1 : lim, cnt, anchor, motion,
 			                                  soft_cap, ctr, rq, src, st, s, ckslot, detailed);
 			if (h2 && (!hit || h2 < hit))
 				hit = h2;
@@ -1179,16 +1210,17 @@ int ensure_query_scratch(pw_world *w)
 // Launch configuration of kernel 0 (states) / 1 (segments), as set by pw_world_set_launch_config.
 int launch_grid(pw_world *w, int kernel, const void *fn, size_t smem)
 {
-	if (w->grid_cache[kernel] > 0)
-		return w->grid_cache[kernel];
+	const int slot = kernel + 2 * (w->node_boxes == PW_BOXES_ORIENTED ? 1 : 0);
+	if (w->grid_cache[slot] > 0)
+		return w->grid_cache[slot];
 	int per_sm = 0;
 	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, WARPS * 32, smem);
 	if (per_sm < 1)
 		per_sm = 1;
 	if (w->launch_blocks[kernel] > 0 && w->launch_blocks[kernel] < per_sm)
 		per_sm = w->launch_blocks[kernel];
-	w->grid_cache[kernel] = per_sm * (w->num_sms > 0 ? w->num_sms : 1);
-	return w->grid_cache[kernel];
+	w->grid_cache[slot] = per_sm * (w->num_sms > 0 ? w->num_sms : 1);
+	return w->grid_cache[slot];
 }
 
 int launch_soft_cap(const pw_world *w, int kernel)
@@ -1216,6 +1248,28 @@ int set_smem_attr(const void *kernel, size_t smem)
 {
 	PW_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 	return PW_OK;
+}
+
+// The traversal kernels of the world's node-box kind.
+template <uint64_t CAP>
+const void *states_kernel(const pw_world *w)
+{
+	return w->node_boxes == PW_BOXES_ORIENTED ? (const void *)k_states<CAP, true> : (const void *)k_states<CAP, false>;
+}
+const void *segments_kernel(const pw_world *w)
+{
+	return w->node_boxes == PW_BOXES_ORIENTED ? (const void *)k_segments<true> : (const void *)k_segments<false>;
+}
+template <uint64_t CAP>
+void launch_states(const pw_world *w, int grid, size_t smem, cudaStream_t st, const double *states, int64_t n,
+                   uint8_t *valid, QueryCounters *ctr, RetestEntry *rq)
+{
+	if (w->node_boxes == PW_BOXES_ORIENTED)
+		k_states<CAP, true><<<grid, WARPS * 32, smem, st>>>(w->dev, states, n, valid, ctr, rq, launch_soft_cap(w, 0),
+		                                                    launch_width(w, 0));
+	else
+		k_states<CAP, false><<<grid, WARPS * 32, smem, st>>>(w->dev, states, n, valid, ctr, rq, launch_soft_cap(w, 0),
+		                                                     launch_width(w, 0));
 }
 
 } // namespace
@@ -1249,14 +1303,14 @@ extern "C" int pw_states_valid(pw_world *w, const double *states, int64_t n, uin
 		return PW_OK;
 	}
 	const size_t smem = warp_smem_bytes() * WARPS;
-	if (!w->graph_mode && (rc = set_smem_attr((const void *)k_states<RETEST_CAP>, smem)))
+	const void *kfn = states_kernel<RETEST_CAP>(w);
+	if (!w->graph_mode && (rc = set_smem_attr(kfn, smem)))
 		return rc;
-	const int grid = launch_grid(w, 0, (const void *)k_states<RETEST_CAP>, smem);
+	const int grid = launch_grid(w, 0, kfn, smem);
 	RetestEntry *rq = (RetestEntry *)w->retest.ptr;
 	if (!w->graph_mode && (rc = mark(w, 0, st)))
 		return rc;
-	k_states<RETEST_CAP><<<grid, WARPS * 32, smem, st>>>(w->dev, states, n, valid, ctr, rq, launch_soft_cap(w, 0),
-	                                                     launch_width(w, 0));
+	launch_states<RETEST_CAP>(w, grid, smem, st, states, n, valid, ctr, rq);
 	if (!w->graph_mode)
 		mark(w, 1, st);
 	StateSrc src{ states, nullptr, nullptr, nullptr, nullptr, nullptr };
@@ -1396,15 +1450,20 @@ extern "C" int pw_segments_first_contact(pw_world *w, const double *from, const 
 	k_rounds<<<1, 1024, 0, st>>>(keys2, n, round_off, round_cap, first_step, ctr);
 	PW_CUDA(cudaGetLastError());
 	const size_t smem = warp_smem_bytes() * WARPS;
-	if (!w->graph_mode && (rc = set_smem_attr((const void *)k_segments, smem)))
+	const void *kfn = segments_kernel(w);
+	if (!w->graph_mode && (rc = set_smem_attr(kfn, smem)))
 		return rc;
-	const int grid = launch_grid(w, 1, (const void *)k_segments, smem);
+	const int grid = launch_grid(w, 1, kfn, smem);
 	RetestEntry *rq = (RetestEntry *)w->retest.ptr;
 	StateSrc src{ nullptr, from, to, params, ckpt, anchors };
 	if (!w->graph_mode && (rc = mark(w, 0, st)))
 		return rc;
-	k_segments<<<grid, WARPS * 32, smem, st>>>(w->dev, src, vals2, round_off, round_off + round_cap + 1, first_step,
-	                                           ctr, rq, launch_soft_cap(w, 1));
+	if (w->node_boxes == PW_BOXES_ORIENTED)
+		k_segments<true><<<grid, WARPS * 32, smem, st>>>(w->dev, src, vals2, round_off, round_off + round_cap + 1,
+		                                                 first_step, ctr, rq, launch_soft_cap(w, 1));
+	else
+		k_segments<false><<<grid, WARPS * 32, smem, st>>>(w->dev, src, vals2, round_off, round_off + round_cap + 1,
+		                                                  first_step, ctr, rq, launch_soft_cap(w, 1));
 	if (!w->graph_mode)
 		mark(w, 1, st);
 	k_retest<RETEST_CAP><<<w->num_sms * 4, 256, 0, st>>>(w->dev, src, nullptr, first_step, ctr, rq);
@@ -1519,11 +1578,11 @@ extern "C" int pw_world_set_graph_mode(pw_world *w, int on)
 		// the attributes and occupancy queries the launches need, outside any capture
 		PW_CUDA(cudaSetDevice(w->device));
 		int rc = ensure_query_scratch(w);
-		if (rc || (rc = set_smem_attr((const void *)k_segments, warp_smem_bytes() * WARPS)) ||
-		    (rc = set_smem_attr((const void *)k_states<RETEST_CAP>, warp_smem_bytes() * WARPS)))
+		if (rc || (rc = set_smem_attr(segments_kernel(w), warp_smem_bytes() * WARPS)) ||
+		    (rc = set_smem_attr(states_kernel<RETEST_CAP>(w), warp_smem_bytes() * WARPS)))
 			return rc;
-		launch_grid(w, 0, (const void *)k_states<RETEST_CAP>, warp_smem_bytes() * WARPS);
-		launch_grid(w, 1, (const void *)k_segments, warp_smem_bytes() * WARPS);
+		launch_grid(w, 0, states_kernel<RETEST_CAP>(w), warp_smem_bytes() * WARPS);
+		launch_grid(w, 1, segments_kernel(w), warp_smem_bytes() * WARPS);
 	}
 	w->graph_mode = on != 0;
 	return PW_OK;
@@ -1582,7 +1641,7 @@ extern "C" int pw_world_set_launch_config(pw_world *w, int kernel, int width, in
 	w->launch_width[kernel] = width;
 	w->launch_soft_cap[kernel] = soft_cap;
 	w->launch_blocks[kernel] = blocks;
-	w->grid_cache[kernel] = 0;
+	w->grid_cache[kernel] = w->grid_cache[kernel + 2] = 0;
 	return PW_OK;
 }
 
@@ -1594,7 +1653,7 @@ extern "C" int pw_world_get_launch_config(pw_world *w, int kernel, int *width, i
 	*soft_cap = w->ready ? launch_soft_cap(w, kernel) : w->launch_soft_cap[kernel];
 	*blocks = w->launch_blocks[kernel];
 	if (*blocks == 0 && w->ready) {
-		const void *k = kernel == 0 ? (const void *)k_states<RETEST_CAP> : (const void *)k_segments;
+		const void *k = kernel == 0 ? states_kernel<RETEST_CAP>(w) : segments_kernel(w);
 		PW_CUDA(cudaSetDevice(w->device));
 		int rc = set_smem_attr(k, warp_smem_bytes() * WARPS);
 		if (rc)
@@ -1764,16 +1823,33 @@ extern "C" int pw_states_valid_noalloc(pw_world *w, const double *states, int64_
 		return PW_OK;
 	}
 	const size_t smem = warp_smem_bytes() * WARPS;
-	rc = set_smem_attr((const void *)k_states<NOALLOC_RETEST_CAP>, smem);
+	rc = set_smem_attr(states_kernel<NOALLOC_RETEST_CAP>(w), smem);
 	if (rc)
 		return rc;
 	// the world's launch configuration, as pw_states_valid uses it (both instances of the
 	// kernel have the same resources, so they share the cached grid)
-	const int grid = launch_grid(w, 0, (const void *)k_states<NOALLOC_RETEST_CAP>, smem);
-	k_states<NOALLOC_RETEST_CAP><<<grid, WARPS * 32, smem, st>>>(w->dev, states, n, valid, ctr, rq,
-	                                                             launch_soft_cap(w, 0), launch_width(w, 0));
+	const int grid = launch_grid(w, 0, states_kernel<NOALLOC_RETEST_CAP>(w), smem);
+	launch_states<NOALLOC_RETEST_CAP>(w, grid, smem, st, states, n, valid, ctr, rq);
 	StateSrc src{ states, nullptr, nullptr, nullptr, nullptr, nullptr };
 	k_retest<NOALLOC_RETEST_CAP><<<w->num_sms * 4, 256, 0, st>>>(w->dev, src, valid, nullptr, ctr, rq);
 	PW_CUDA(cudaGetLastError());
+	return PW_OK;
+}
+
+extern "C" int pw_world_set_node_boxes(pw_world *w, int kind)
+{
+	if (!w || (kind != PW_BOXES_ALIGNED && kind != PW_BOXES_ORIENTED))
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_set_node_boxes: bad argument");
+	if (w->graph_mode)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_set_node_boxes: not in graph mode (captured launches hold the kernel)");
+	w->node_boxes = kind;
+	return PW_OK;
+}
+
+extern "C" int pw_world_get_node_boxes(pw_world *w, int *kind)
+{
+	if (!w || !kind)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_get_node_boxes: NULL argument");
+	*kind = w->node_boxes;
 	return PW_OK;
 }

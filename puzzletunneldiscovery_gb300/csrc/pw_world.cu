@@ -199,6 +199,12 @@ extern "C" int pw_world_scale_to_unit(pw_world *w)
 	return PW_OK;
 }
 
+// Every device array of a mesh (the allocations a rebuild of the other mesh keeps).
+static std::vector<const void *> mesh_arrays(const MeshDev &m)
+{
+	return { m.nodeA, m.nodeB, m.obbA, m.obbB, m.obbR0, m.obbR1, m.obbR2, m.triA, m.triB, m.triC, m.V64, m.F };
+}
+
 static void apply_perturbation_to_env(pw_world *w)
 {
 	const size_t n = w->env_local.size() / 3;
@@ -276,12 +282,10 @@ extern "C" int pw_world_set_perturbation(pw_world *w, const double q[7])
 		PW_CUDA(cudaSetDevice(w->device));
 		apply_perturbation_to_env(w);
 		// rebuild only the env mesh; keep the robot
-		MeshDev rob = w->dev.rob;
+		const std::vector<const void *> rob = mesh_arrays(w->dev.rob);
 		std::vector<void *> keep;
 		for (void *p : w->mesh_allocs) {
-			bool robp = p == rob.nodeA || p == rob.nodeB || p == rob.triA || p == rob.triB || p == rob.triC ||
-			            p == rob.V64 || p == rob.F;
-			if (robp)
+			if (std::find(rob.begin(), rob.end(), (const void *)p) != rob.end())
 				keep.push_back(p);
 			else
 				cudaFree(p);
@@ -591,7 +595,8 @@ __device__ __forceinline__ int lcp_delta(const uint32_t *keys, int n, int i, int
 }
 
 // Karras 2012: internal node i covers a key range; children are internal or leaf nodes.
-__global__ void k_karras(const uint32_t *keys, int n, int32_t *left, int32_t *right, int32_t *parent)
+__global__ void k_karras(const uint32_t *keys, int n, int32_t *left, int32_t *right, int32_t *parent,
+                         int32_t *rlo, int32_t *rhi)
 {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n - 1)
@@ -622,6 +627,8 @@ __global__ void k_karras(const uint32_t *keys, int n, int32_t *left, int32_t *ri
 	right[i] = rc;
 	parent[lc] = i;
 	parent[rc] = i;
+	rlo[i] = min(i, j);      // the node's leaves, in slot order
+	rhi[i] = max(i, j);
 }
 
 // Leaves: permute triangles into slot order and write leaf boxes, then refit
@@ -689,6 +696,145 @@ __global__ void k_finalize(int nnodes, int n, const float *blo, const float *bhi
 	nb[i] = make_float4(h[0], h[1], h[2], __int_as_float(r));
 }
 
+// ------------------------------------------------------------------ oriented node boxes
+//
+// Principal axes (Gottschalk, Lin, Manocha 1996: the eigenvectors of the
+// covariance of the node's vertices) on the LBVH's hierarchy.  Vertex moments
+// are summed per slot and prefix-summed, so a node's covariance is the
+// difference of two prefix entries; the eigenvectors come from cyclic Jacobi
+// rotations (pwm::jacobi_eigen3); the extents are measured over the node's
+// vertices in FP64.
+
+// Per slot: the sums of the slot triangle's three vertices (relative to `org`)
+// and of their outer products: 9 arrays of n.
+__global__ void k_slot_moments(const double *V, const int32_t *F, const uint32_t *order, int n, const double *org,
+                               double *mom)
+{
+	const int j = blockIdx.x * blockDim.x + threadIdx.x;
+	if (j >= n)
+		return;
+	const int t = (int)order[j];
+	double s[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 };
+	for (int k = 0; k < 3; k++) {
+		const double *p = V + 3 * F[3 * t + k];
+		const double x = p[0] - org[0], y = p[1] - org[1], z = p[2] - org[2];
+		s[0] += x; s[1] += y; s[2] += z;
+		s[3] += x * x; s[4] += y * y; s[5] += z * z;
+		s[6] += x * y; s[7] += x * z; s[8] += y * z;
+	}
+	for (int k = 0; k < 9; k++)
+		mom[(size_t)k * n + j] = s[k];
+}
+
+// One warp per node (leaves included): axes from the covariance of the node's
+// slot range, then two passes over its vertices -- the extents along each axis,
+// the FP32 centre of that range, and the half-extents about that FP32 centre,
+// measured in FP64 and rounded up with a margin for the FP64 rounding.
+// Writes the oriented node arrays and the two magnitude bounds the error model
+// needs: max over node boxes of |corner|_1 (rb1) and |corner|_inf (rbinf), as
+// float bit patterns (non-negative floats order like their bits).
+__global__ void k_obb_fit(const double *V, const int32_t *F, const uint32_t *order, int n, const double *scan,
+                          const int32_t *rlo, const int32_t *rhi, const int32_t *left, const int32_t *right,
+                          const float4 *slot_a, float4 *oa, float4 *ob, float4 *r0, float4 *r1, float4 *r2,
+                          unsigned int *rb1, unsigned int *rbinf)
+{
+	const int warp = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+	const int lane = threadIdx.x & 31;
+	const int nnodes = 2 * n - 1;
+	if (warp >= nnodes)
+		return;
+	const int leaf_base = n - 1;
+	const bool leaf = warp >= leaf_base;
+	const int lo = leaf ? warp - leaf_base : rlo[warp];
+	const int hi = leaf ? warp - leaf_base : rhi[warp];
+	// covariance from the prefix sums of the slot moments (inclusive scans)
+	double m[9];
+	for (int k = 0; k < 9; k++) {
+		const double *sk = scan + (size_t)k * n;
+		m[k] = sk[hi] - (lo > 0 ? sk[lo - 1] : 0.0);
+	}
+	const double cnt = 3.0 * (double)(hi - lo + 1);
+	const double mu[3] = { m[0] / cnt, m[1] / cnt, m[2] / cnt };
+	const double S[6] = { m[3] / cnt - mu[0] * mu[0], m[4] / cnt - mu[1] * mu[1], m[5] / cnt - mu[2] * mu[2],
+	                      m[6] / cnt - mu[0] * mu[1], m[7] / cnt - mu[0] * mu[2], m[8] / cnt - mu[1] * mu[2] };
+	double E[9];
+	pwm::jacobi_eigen3(S, E);
+	// pass 1: the projections' range along each axis
+	double pmin[3] = { 1e300, 1e300, 1e300 }, pmax[3] = { -1e300, -1e300, -1e300 };
+	for (int j = lo + lane; j <= hi; j += 32) {
+		const int t = (int)order[j];
+		for (int k = 0; k < 3; k++) {
+			const double *p = V + 3 * F[3 * t + k];
+			for (int a = 0; a < 3; a++) {
+				const double pr = E[3 * a] * p[0] + E[3 * a + 1] * p[1] + E[3 * a + 2] * p[2];
+				pmin[a] = fmin(pmin[a], pr);
+				pmax[a] = fmax(pmax[a], pr);
+			}
+		}
+	}
+	for (int o = 16; o > 0; o >>= 1)
+		for (int a = 0; a < 3; a++) {
+			pmin[a] = fmin(pmin[a], __shfl_xor_sync(0xffffffffu, pmin[a], o));
+			pmax[a] = fmax(pmax[a], __shfl_xor_sync(0xffffffffu, pmax[a], o));
+		}
+	float c[3];
+	for (int k = 0; k < 3; k++) {
+		double ck = 0.0;
+		for (int a = 0; a < 3; a++)
+			ck += E[3 * a + k] * 0.5 * (pmin[a] + pmax[a]);
+		c[k] = __double2float_rn(ck);
+	}
+	// pass 2: half-extents about the FP32 centre, and the largest |x - c|_1 for the rounding margin
+	double h[3] = { 0, 0, 0 }, dmax = 0.0;
+	for (int j = lo + lane; j <= hi; j += 32) {
+		const int t = (int)order[j];
+		for (int k = 0; k < 3; k++) {
+			const double *p = V + 3 * F[3 * t + k];
+			const double d0 = p[0] - (double)c[0], d1 = p[1] - (double)c[1], d2 = p[2] - (double)c[2];
+			dmax = fmax(dmax, fabs(d0) + fabs(d1) + fabs(d2));
+			for (int a = 0; a < 3; a++)
+				h[a] = fmax(h[a], fabs(E[3 * a] * d0 + E[3 * a + 1] * d1 + E[3 * a + 2] * d2));
+		}
+	}
+	for (int o = 16; o > 0; o >>= 1) {
+		dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+		for (int a = 0; a < 3; a++)
+			h[a] = fmax(h[a], __shfl_xor_sync(0xffffffffu, h[a], o));
+	}
+	if (lane != 0)
+		return;
+	// the FP64 differences and dot products are off by a few ulps of |x - c|_1 (and of |x|, |c| in the subtraction)
+	const double cinf = fmax(fmax(fabs((double)c[0]), fabs((double)c[1])), fabs((double)c[2]));
+	const double pad = 1e-14 * (dmax + 2.0 * cinf) + 1e-300;
+	float hf[3];
+	for (int a = 0; a < 3; a++)
+		hf[a] = __double2float_ru(h[a] * (1.0 + 1e-14) + pad);
+	int l, r;
+	if (!leaf) {
+		l = left[warp];
+		r = right[warp];
+	} else {
+		l = __float_as_int(slot_a[warp - leaf_base].w);
+		r = -1;
+	}
+	float4 rows[3];
+	double b1 = fabs((double)c[0]) + fabs((double)c[1]) + fabs((double)c[2]);
+	double binf = cinf;
+	for (int a = 0; a < 3; a++) {
+		rows[a] = make_float4(__double2float_rn(E[3 * a]), __double2float_rn(E[3 * a + 1]),
+		                      __double2float_rn(E[3 * a + 2]), 0.f);
+		b1 += (double)hf[a] * (fabs(E[3 * a]) + fabs(E[3 * a + 1]) + fabs(E[3 * a + 2]));
+		binf += (double)hf[a];
+	}
+	oa[warp] = make_float4(c[0], c[1], c[2], __int_as_float(l));
+	ob[warp] = make_float4(hf[0], hf[1], hf[2], __int_as_float(r));
+	r0[warp] = rows[0];
+	r1[warp] = rows[1];
+	r2[warp] = rows[2];
+	atomicMax(rb1, __float_as_uint(__double2float_ru(b1 * (1.0 + 1e-12))));
+	atomicMax(rbinf, __float_as_uint(__double2float_ru(binf * (1.0 + 1e-12))));
+}
+
 __global__ void k_depth(int n, const int32_t *parent, int *maxdepth)
 {
 	const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -737,6 +883,11 @@ int pw_build_mesh_device(pw_world *w, MeshDev &m, const std::vector<double> &V64
 	const int nnodes = 2 * n - 1;
 	PW_CUDA(walloc(w, &m.nodeA, nnodes));
 	PW_CUDA(walloc(w, &m.nodeB, nnodes));
+	PW_CUDA(walloc(w, &m.obbA, nnodes));
+	PW_CUDA(walloc(w, &m.obbB, nnodes));
+	PW_CUDA(walloc(w, &m.obbR0, nnodes));
+	PW_CUDA(walloc(w, &m.obbR1, nnodes));
+	PW_CUDA(walloc(w, &m.obbR2, nnodes));
 	PW_CUDA(walloc(w, &m.triA, n));
 	PW_CUDA(walloc(w, &m.triB, n));
 	PW_CUDA(walloc(w, &m.triC, n));
@@ -745,9 +896,10 @@ int pw_build_mesh_device(pw_world *w, MeshDev &m, const std::vector<double> &V64
 	float4 *ta, *tb, *tc;
 	float *tlo, *thi, *cen, *bounds, *blo, *bhi;
 	uint32_t *keys, *vals, *keys2, *vals2;
-	int32_t *left, *right, *parent;
-	unsigned int *flags;
+	int32_t *left, *right, *parent, *rlo, *rhi;
+	unsigned int *flags, *obb_bounds;
 	int *maxdepth;
+	double *mom, *mscan, *org;
 	std::vector<void *> tmp;
 	auto tal = [&](void **p, size_t bytes) -> cudaError_t {
 		cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
@@ -786,6 +938,12 @@ int pw_build_mesh_device(pw_world *w, MeshDev &m, const std::vector<double> &V64
 	TAL(parent, sizeof(int32_t) * nnodes);
 	TAL(flags, sizeof(unsigned int) * nnodes);
 	TAL(maxdepth, sizeof(int));
+	TAL(rlo, sizeof(int32_t) * nnodes);
+	TAL(rhi, sizeof(int32_t) * nnodes);
+	TAL(obb_bounds, sizeof(unsigned int) * 2);
+	TAL(mom, sizeof(double) * 9 * (size_t)n);
+	TAL(mscan, sizeof(double) * 9 * (size_t)n);
+	TAL(org, sizeof(double) * 3);
 	const int B = 256;
 	const int G = (n + B - 1) / B;
 	cudaMemset(flags, 0, sizeof(unsigned int) * nnodes);
@@ -808,9 +966,39 @@ int pw_build_mesh_device(pw_world *w, MeshDev &m, const std::vector<double> &V64
 		return pw_cuda_fail(se, "BVH sort");
 	}
 	if (n > 1)
-		k_karras<<<(n - 1 + B - 1) / B, B>>>(keys2, n, left, right, parent);
+		k_karras<<<(n - 1 + B - 1) / B, B>>>(keys2, n, left, right, parent, rlo, rhi);
 	k_refit<<<G, B>>>(vals2, n, tlo, thi, ta, tb, tc, m.triA, m.triB, m.triC, blo, bhi, left, right, parent, flags);
 	k_finalize<<<(nnodes + B - 1) / B, B>>>(nnodes, n, blo, bhi, left, right, m.triA, m.nodeA, m.nodeB);
+	// oriented boxes on the same hierarchy: slot moments about the vertices' box centre,
+	// their prefix sums, then one warp per node
+	{
+		double vlo[3] = { 1e300, 1e300, 1e300 }, vhi[3] = { -1e300, -1e300, -1e300 };
+		for (size_t i = 0; i + 2 < V64.size(); i += 3)
+			for (int c = 0; c < 3; c++) {
+				vlo[c] = std::min(vlo[c], V64[i + c]);
+				vhi[c] = std::max(vhi[c], V64[i + c]);
+			}
+		const double o[3] = { 0.5 * (vlo[0] + vhi[0]), 0.5 * (vlo[1] + vhi[1]), 0.5 * (vlo[2] + vhi[2]) };
+		cudaMemcpy(org, o, sizeof(o), cudaMemcpyHostToDevice);
+	}
+	cudaMemset(obb_bounds, 0, sizeof(unsigned int) * 2);
+	k_slot_moments<<<G, B>>>(m.V64, m.F, vals2, n, org, mom);
+	{
+		size_t sbytes = 0;
+		se = cub::DeviceScan::InclusiveSum(nullptr, sbytes, mom, mscan, n);
+		void *scan_tmp = nullptr;
+		if (se == cudaSuccess)
+			TAL(scan_tmp, sbytes);
+		for (int k = 0; k < 9 && se == cudaSuccess; k++)
+			se = cub::DeviceScan::InclusiveSum(scan_tmp, sbytes, mom + (size_t)k * n, mscan + (size_t)k * n, n);
+		if (se != cudaSuccess) {
+			cleanup();
+			return pw_cuda_fail(se, "BVH moment scan");
+		}
+	}
+	k_obb_fit<<<(unsigned)(((int64_t)nnodes * 32 + B - 1) / B), B>>>(m.V64, m.F, vals2, n, mscan, rlo, rhi, left, right,
+	                                                                 m.triA, m.obbA, m.obbB, m.obbR0, m.obbR1, m.obbR2,
+	                                                                 obb_bounds, obb_bounds + 1);
 	k_depth<<<G, B>>>(n, parent, maxdepth);
 	cudaError_t e = cudaGetLastError();
 	if (e == cudaSuccess)
@@ -824,11 +1012,20 @@ int pw_build_mesh_device(pw_world *w, MeshDev &m, const std::vector<double> &V64
 	cudaMemcpy(&depth, maxdepth, sizeof(int), cudaMemcpyDeviceToHost);
 	cudaMemcpy(rootlo, blo, sizeof(float) * 3, cudaMemcpyDeviceToHost);
 	cudaMemcpy(roothi, bhi, sizeof(float) * 3, cudaMemcpyDeviceToHost);
+	unsigned int ob[2] = { 0, 0 };
+	cudaMemcpy(ob, obb_bounds, sizeof(ob), cudaMemcpyDeviceToHost);
+	float ob1, obinf;
+	memcpy(&ob1, &ob[0], 4);
+	memcpy(&obinf, &ob[1], 4);
 	m.depth = depth;
+	// r1 and emax bound the points of both kinds of node box (the oriented boxes'
+	// corners can reach past the vertices' coordinates)
 	double r1 = 0.0;
 	for (int c = 0; c < 3; c++)
 		r1 += std::max(std::fabs((double)rootlo[c]), std::fabs((double)roothi[c]));
+	r1 = std::max(r1, (double)ob1);
 	m.r1 = (float)r1 * 1.0001f + 1e-30f;
+	m.emax = std::max(m.emax, obinf * 1.0001f);
 	cleanup();
 #undef TAL
 	if (depth >= 4096)

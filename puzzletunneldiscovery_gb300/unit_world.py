@@ -318,6 +318,17 @@ class UnitWorld:
                                                  ctypes.byref(b)), "get_launch_config")
         return {"width": w.value, "soft_cap": c.value, "blocks": b.value}
 
+    def set_node_boxes(self, kind: str) -> None:
+        """Node boxes of the traversals: "oriented" (default) or "aligned"; the
+        verdicts do not depend on it."""
+        k = {"aligned": _lib.PW_BOXES_ALIGNED, "oriented": _lib.PW_BOXES_ORIENTED}[kind]
+        check(self._L.pw_world_set_node_boxes(self._h, k), "set_node_boxes")
+
+    def get_node_boxes(self) -> str:
+        k = ctypes.c_int32()
+        check(self._L.pw_world_get_node_boxes(self._h, ctypes.byref(k)), "get_node_boxes")
+        return "oriented" if k.value == _lib.PW_BOXES_ORIENTED else "aligned"
+
     def last_stats(self) -> dict:
         st = _lib.QueryStats()
         check(self._L.pw_world_last_stats(self._h, ctypes.byref(st)), "last_stats")

@@ -1,9 +1,9 @@
-// delta_walk.cc -- pwm::walk_delta / pwm::delta_jump (the kernels' shortcut for
+// delta_walk.cc -- pwm::walk_delta / delta_try / delta_jump (the kernels' shortcuts for
 // runs of the reference's delta updates, unit_world.cc:463-470) against the
 // updates taken one at a time, bit for bit.  Host-only; built with g++
 // -ffp-contract=off like the library's host code.
 //
-// usage: delta_walk <segments> <seed>; prints "mismatches M walks W jumped J ties T"
+// usage: delta_walk <segments> <seed>; prints "mismatches M walks W jumped J tried R ties T"
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -68,7 +68,7 @@ int main(int argc, char **argv)
 {
 	const long n = argc > 1 ? atol(argv[1]) : 10000;
 	rng_state ^= (uint64_t)(argc > 2 ? atol(argv[2]) : 1) * 0x9E3779B97F4A7C15ull;
-	long mism = 0, walks = 0, jumped = 0, ties = 0;
+	long mism = 0, walks = 0, jumped = 0, tried = 0, ties = 0;
 	std::vector<double> seq;
 	for (long i = 0; i < n; i++) {
 		const double step = pick_step();
@@ -95,6 +95,12 @@ int main(int argc, char **argv)
 			double c;
 			if (pwm::delta_jump(seq[a], dist, step, j, &c) > 0)
 				jumped++;
+			double r;
+			if (pwm::delta_try(seq[a], dist, step, j, &r)) {
+				tried++;
+				if (pwm::dbits(r) != pwm::dbits(seq[a + j]))
+					mism++;
+			}
 			ties += is_tie(seq[a], step) ? 1 : 0;
 		}
 		// the set-up kernel's loop: checkpoints every 32 updates, chunks far from dist in one walk
@@ -106,7 +112,13 @@ int main(int argc, char **argv)
 					bad++;
 				const float room = (float)pwm::sub(dist, d) / (float)step;
 				if (room > 40.f) {
-					d = pwm::walk_delta(d, dist, step, 32);
+					double r;
+					if (pwm::delta_try(d, dist, step, 32, &r)) {
+						d = r;
+					} else {
+						for (int i = 0; i < 32; i++)
+							d = pwm::add(d, step);
+					}
 					K += 32;
 					continue;
 				}
@@ -133,6 +145,6 @@ int main(int argc, char **argv)
 		if (pwm::dbits(d) != pwm::dbits(seq[L - 2]))
 			mism++;
 	}
-	printf("mismatches %ld walks %ld jumped %ld ties %ld\n", mism, walks, jumped, ties);
+	printf("mismatches %ld walks %ld jumped %ld tried %ld ties %ld\n", mism, walks, jumped, tried, ties);
 	return mism ? 1 : 0;
 }

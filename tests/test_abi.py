@@ -138,3 +138,14 @@ def test_headers_compile_standalone(lang, std, tmp_path):
     r = subprocess.run([cc, "-fsyntax-only", std, "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
                         str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_every_mesh_array_is_kept_on_a_partial_rebuild():
+    """pw_world_set_perturbation rebuilds the env mesh and keeps the robot's device
+    arrays: the keep list (mesh_arrays) must name every array the mesh build
+    allocates, or the robot's would be freed while still in use."""
+    src = open(os.path.join(ROOT, "puzzletunneldiscovery_gb300", "csrc", "pw_world.cu")).read()
+    allocated = set(re.findall(r"walloc\(w, &m\.(\w+),", src))
+    body = re.search(r"mesh_arrays\(const MeshDev &m\)\s*\{(.*?)\}", src, re.S).group(1)
+    kept = set(re.findall(r"m\.(\w+)", body))
+    assert allocated and allocated == kept, (allocated - kept, kept - allocated)

@@ -1,5 +1,5 @@
 """The kernels' shortcut for runs of the reference's delta updates
-(pwm::walk_delta / delta_jump; unit_world.cc:463-470 is one update per step)
+(pwm::walk_delta / delta_try / delta_jump; unit_world.cc:463-470 is one update per step)
 against the updates taken one at a time, bit for bit, on random and
 adversarial step sizes: rounding ties inside a binade, dist on and next to
 powers of two, dist an exact multiple of the step (CPU)."""
@@ -26,5 +26,6 @@ def test_walk_delta_equals_single_updates(harness, seed):
     f = r.stdout.split()
     fields = dict(zip(f[0::2], map(int, f[1::2])))
     assert r.returncode == 0 and fields["mismatches"] == 0, r.stdout
-    assert fields["jumped"] > fields["walks"] // 2       # the shortcut is taken
+    assert fields["jumped"] > fields["walks"] // 2       # the shortcuts are taken
+    assert fields["tried"] > fields["walks"] // 2
     assert fields["ties"] > 1000                         # and the tie fallback is exercised
