@@ -561,6 +561,8 @@ typedef struct {
 	double lo[3], hi[3];
 	int left, right;   /* children, -1 for a leaf */
 	int first, count;  /* leaf triangle range in `order` */
+	/* oriented box: axes as rows of E (orthonormal), centre c, half-extents h */
+	double E[9], c[3], h[3];
 } or_node;
 
 typedef struct {
@@ -597,6 +599,96 @@ static const double *or_tri_vertex(const or_mesh *m, int64_t tri, int k)
 	return m->V + 3 * (int64_t)m->F[3 * tri + k];
 }
 
+/* Eigenvectors (rows of E) of the symmetric matrix S = (xx, yy, zz, xy, xz, yz):
+ * cyclic Jacobi rotations (Golub and Van Loan, section 8.5), then Gram-Schmidt
+ * and a cross product so that E is orthonormal to rounding. */
+static void or_eigen3(const double S[6], double E[9])
+{
+	double a[3][3] = { { S[0], S[3], S[4] }, { S[3], S[1], S[5] }, { S[4], S[5], S[2] } };
+	double v[3][3] = { { 1, 0, 0 }, { 0, 1, 0 }, { 0, 0, 1 } };
+	for (int sweep = 0; sweep < 32; sweep++) {
+		const double off = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
+		const double dia = fabs(a[0][0]) + fabs(a[1][1]) + fabs(a[2][2]);
+		if (!(off > 1e-300) || off <= 1e-18 * dia)
+			break;
+		for (int p = 0; p < 2; p++)
+			for (int q = p + 1; q < 3; q++) {
+				if (!(fabs(a[p][q]) > 1e-300))
+					continue;
+				const double th = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+				const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+				const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+				for (int k = 0; k < 3; k++) {
+					const double x = a[k][p], y = a[k][q];
+					a[k][p] = c * x - sn * y;
+					a[k][q] = sn * x + c * y;
+				}
+				for (int k = 0; k < 3; k++) {
+					const double x = a[p][k], y = a[q][k];
+					a[p][k] = c * x - sn * y;
+					a[q][k] = sn * x + c * y;
+				}
+				for (int k = 0; k < 3; k++) {
+					const double x = v[k][p], y = v[k][q];
+					v[k][p] = c * x - sn * y;
+					v[k][q] = sn * x + c * y;
+				}
+			}
+	}
+	double e0[3] = { v[0][0], v[1][0], v[2][0] }, e1[3] = { v[0][1], v[1][1], v[2][1] };
+	const double n0 = sqrt(e0[0] * e0[0] + e0[1] * e0[1] + e0[2] * e0[2]);
+	for (int k = 0; k < 3; k++) e0[k] /= n0;
+	const double d = e0[0] * e1[0] + e0[1] * e1[1] + e0[2] * e1[2];
+	for (int k = 0; k < 3; k++) e1[k] -= d * e0[k];
+	const double n1 = sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+	for (int k = 0; k < 3; k++) e1[k] /= n1;
+	E[0] = e0[0]; E[1] = e0[1]; E[2] = e0[2];
+	E[3] = e1[0]; E[4] = e1[1]; E[5] = e1[2];
+	E[6] = e0[1] * e1[2] - e0[2] * e1[1];
+	E[7] = e0[2] * e1[0] - e0[0] * e1[2];
+	E[8] = e0[0] * e1[1] - e0[1] * e1[0];
+}
+
+/* Oriented box of the node's triangles: principal axes of their vertices, the
+ * projections' range, extents widened by 1e-12 of the coordinates (the FP64
+ * projections' rounding). */
+static void or_fit_obb(const or_mesh *m, or_node *n)
+{
+	double mu[3] = { 0, 0, 0 }, S[6] = { 0, 0, 0, 0, 0, 0 };
+	const double cnt = 3.0 * n->count;
+	for (int i = n->first; i < n->first + n->count; i++)
+		for (int k = 0; k < 3; k++) {
+			const double *p = or_tri_vertex(m, m->order[i], k);
+			for (int c = 0; c < 3; c++) mu[c] += p[c] / cnt;
+		}
+	for (int i = n->first; i < n->first + n->count; i++)
+		for (int k = 0; k < 3; k++) {
+			const double *p = or_tri_vertex(m, m->order[i], k);
+			const double d0 = p[0] - mu[0], d1 = p[1] - mu[1], d2 = p[2] - mu[2];
+			S[0] += d0 * d0; S[1] += d1 * d1; S[2] += d2 * d2;
+			S[3] += d0 * d1; S[4] += d0 * d2; S[5] += d1 * d2;
+		}
+	or_eigen3(S, n->E);
+	double lo[3] = { INFINITY, INFINITY, INFINITY }, hi[3] = { -INFINITY, -INFINITY, -INFINITY }, big = 0.0;
+	for (int i = n->first; i < n->first + n->count; i++)
+		for (int k = 0; k < 3; k++) {
+			const double *p = or_tri_vertex(m, m->order[i], k);
+			const double l1 = fabs(p[0]) + fabs(p[1]) + fabs(p[2]);
+			if (l1 > big) big = l1;
+			for (int a = 0; a < 3; a++) {
+				const double pr = n->E[3 * a] * p[0] + n->E[3 * a + 1] * p[1] + n->E[3 * a + 2] * p[2];
+				if (pr < lo[a]) lo[a] = pr;
+				if (pr > hi[a]) hi[a] = pr;
+			}
+		}
+	for (int k = 0; k < 3; k++) n->c[k] = 0.0;
+	for (int a = 0; a < 3; a++) {
+		const double mid = 0.5 * (lo[a] + hi[a]);
+		n->h[a] = 0.5 * (hi[a] - lo[a]) + 1e-12 * (1.0 + big);
+		for (int k = 0; k < 3; k++) n->c[k] += n->E[3 * a + k] * mid;
+	}
+}
+
 static int or_build_node(or_mesh *m, double *cent, int first, int count, int *next)
 {
 	const int id = (*next)++;
@@ -618,6 +710,7 @@ static int or_build_node(or_mesh *m, double *cent, int first, int count, int *ne
 		}
 	}
 	n->first = first; n->count = count; n->left = n->right = -1;
+	or_fit_obb(m, n);
 	if (count <= 4)
 		return id;
 	int axis = 0;
@@ -821,7 +914,7 @@ OR_EXPORT void or_world_vertices(const or_world *w, int which, double *out)
 
 typedef struct {
 	double R[9], t[3], AR[9];
-	double margin;
+	double margin, slack;
 	const or_world *w;
 	/* collection for intersecting_segments */
 	int collect;
@@ -836,6 +929,7 @@ static void or_query_init(or_query *qq, const or_world *w, const double q[7])
 	const double dev = fabs(1.0 - s);
 	const double slack = 1e-12 + 2.0 * dev;
 	for (int i = 0; i < 9; i++) qq->AR[i] = fabs(qq->R[i]) + slack;
+	qq->slack = 3.0 * slack;   /* |M| = |Ea R Eb^T|: the rotation's slack through two unit-row products */
 	const double W = fabs(q[0]) + fabs(q[1]) + fabs(q[2]) + w->rob.rmax + w->env.rmax;
 	qq->margin = 1e-12 * (1.0 + W) + 8.0 * dev * W;
 	qq->w = w;
@@ -844,18 +938,32 @@ static void or_query_init(or_query *qq, const or_world *w, const double q[7])
 	qq->pairs = NULL;
 }
 
+/* The two nodes' oriented boxes (as FCL's OBBRSS nodes are, cdmodel.cc:17-18):
+ * the robot box brought into the env box's frame, M = Ea R Eb^T and
+ * T = Ea (R cb + t - ca), then the separating-axis test with the query's slack
+ * on |M| and margins on the extents. */
 static int or_nodes_disjoint(const or_query *qq, const or_node *a, const or_node *b)
 {
-	double ca[3], ea[3], cb[3], eb[3], CB[3], T[3];
+	double ea[3], eb[3], CB[3], d[3], T[3], N[9], M[9], AM[9];
 	for (int c = 0; c < 3; c++) {
-		ca[c] = 0.5 * (a->lo[c] + a->hi[c]);
-		ea[c] = 0.5 * (a->hi[c] - a->lo[c]) + qq->margin;
-		cb[c] = 0.5 * (b->lo[c] + b->hi[c]);
-		eb[c] = 0.5 * (b->hi[c] - b->lo[c]) + qq->margin;
+		ea[c] = a->h[c] + qq->margin;
+		eb[c] = b->h[c] + qq->margin;
 	}
-	or_xform_point(qq->R, qq->t, cb, CB);
-	for (int c = 0; c < 3; c++) T[c] = CB[c] - ca[c];
-	return or_sat_disjoint(ea, eb, T, qq->R, qq->AR);
+	or_xform_point(qq->R, qq->t, b->c, CB);
+	for (int c = 0; c < 3; c++) d[c] = CB[c] - a->c[c];
+	for (int i = 0; i < 3; i++)
+		T[i] = (a->E[3 * i] * d[0] + a->E[3 * i + 1] * d[1]) + a->E[3 * i + 2] * d[2];
+	/* column j of N: robot box axis j in the env frame (R times row j of Eb) */
+	for (int i = 0; i < 3; i++)
+		for (int j = 0; j < 3; j++)
+			N[3 * i + j] = (qq->R[3 * i] * b->E[3 * j] + qq->R[3 * i + 1] * b->E[3 * j + 1]) +
+			               qq->R[3 * i + 2] * b->E[3 * j + 2];
+	for (int i = 0; i < 3; i++)
+		for (int j = 0; j < 3; j++) {
+			M[3 * i + j] = (a->E[3 * i] * N[j] + a->E[3 * i + 1] * N[3 + j]) + a->E[3 * i + 2] * N[6 + j];
+			AM[3 * i + j] = fabs(M[3 * i + j]) + qq->slack;
+		}
+	return or_sat_disjoint(ea, eb, T, M, AM);
 }
 
 /* Leaf-leaf: Moeller (eps 0) on every triangle pair.  Returns 1 on the first hit
@@ -916,7 +1024,7 @@ static int or_traverse(or_query *qq)
 			stack = (int *)realloc(stack, sizeof(int) * 2 * (size_t)cap);
 		}
 		double sa = 0, sb = 0;
-		for (int c = 0; c < 3; c++) { sa += a->hi[c] - a->lo[c]; sb += b->hi[c] - b->lo[c]; }
+		for (int c = 0; c < 3; c++) { sa += a->h[c]; sb += b->h[c]; }
 		if (!la && (lb || sa >= sb)) {
 			stack[top++] = a->right; stack[top++] = bi;
 			stack[top++] = a->left;  stack[top++] = bi;

@@ -1,11 +1,12 @@
 """Launch-shape autotuner and CUDA-graph replay for the traversal kernels.
 
-``autotune`` times the persistent traversal kernels of one world over a grid of
+``autotune`` times the persistent traversal kernels of one world on a sample of
+the caller's own workload: first the two kinds of BVH node box (axis-aligned or
+oriented, pw_world_set_node_boxes), then, under the faster one, a grid of
 launch configurations (queries a warp takes per grab, traversal stack soft cap
 -- the point where a warp narrows from breadth-first to depth-first -- and
-resident blocks per SM) on a sample of the caller's own workload, checks that
-every configuration returns the same verdicts, and keeps the fastest
-(pw_world_set_launch_config).  The best configuration depends on the meshes
+resident blocks per SM).  Every choice must return the same verdicts; the
+fastest is kept (pw_world_set_launch_config).  The best configuration depends on the meshes
 (BVH depth, how often queries collide), so it is chosen per world and can be
 cached per (mesh pair, GPU model) in a JSON file (``TuneCache``).
 
@@ -51,13 +52,30 @@ class TuneReport:
     table: list = field(default_factory=list)     # (config, ms)
 
 
+def _tune_boxes(uw, run, reps, stream, what):
+    """Time `run` under both node-box kinds (default launch shape) and keep the
+    faster kind on the world; the two must give identical results.  Returns
+    (kind, {kind: ms}, the results)."""
+    times, outs = {}, {}
+    for kind in ("aligned", "oriented"):
+        uw.set_node_boxes(kind)
+        run()
+        times[kind], outs[kind] = _time(run, reps, stream)
+    if not torch.equal(outs["aligned"], outs["oriented"]):
+        raise RuntimeError("the node-box kinds gave different %s" % what)
+    kind = min(times, key=times.get)
+    uw.set_node_boxes(kind)
+    return kind, times, outs[kind]
+
+
 def tune_states(uw, q: torch.Tensor, widths=(8, 16, 32), soft_caps=(128, 256, 512, 0), blocks=(0, 2, 3),
                 reps: int = 2) -> TuneReport:
-    """Pick the states-kernel configuration that answers `q` fastest."""
+    """Pick the states-kernel configuration that answers `q` fastest: first the
+    node-box kind (a world-wide setting), then the launch shape under it."""
     stream = torch.cuda.current_stream(q.device)
     uw.set_launch_config(0)
-    uw.is_valid_states(q)
-    default_ms, ref = _time(lambda: uw.is_valid_states(q), reps, stream)
+    kind, box_ms, ref = _tune_boxes(uw, lambda: uw.is_valid_states(q), reps, stream, "verdicts")
+    default_ms = box_ms[kind]
     table = []
     for w, c, b in itertools.product(widths, soft_caps, blocks):
         uw.set_launch_config(0, w, c, b)
@@ -72,17 +90,19 @@ def tune_states(uw, q: torch.Tensor, widths=(8, 16, 32), soft_caps=(128, 256, 51
     else:
         cfg, ms = {"width": 0, "soft_cap": 0, "blocks": 0}, default_ms
         uw.set_launch_config(0)
-    return TuneReport("states", cfg, default_ms, ms, table)
+    cfg = dict(cfg, boxes=kind)
+    return TuneReport("states", cfg, default_ms, ms, table + [({"boxes": k}, v) for k, v in box_ms.items()])
 
 
 def tune_segments(uw, q0: torch.Tensor, q1: torch.Tensor, verify_delta: float, soft_caps=(128, 256, 512, 0),
                   blocks=(0, 2, 3), reps: int = 2, mode: int = _lib.PW_SEG_TRANSIT) -> TuneReport:
-    """Pick the segments-kernel configuration that answers (q0, q1) fastest."""
+    """Pick the segments-kernel configuration that answers (q0, q1) fastest: first
+    the node-box kind (a world-wide setting), then the launch shape under it."""
     stream = torch.cuda.current_stream(q0.device)
     uw.set_launch_config(1)
     run = lambda: uw.first_contact_steps(q0, q1, verify_delta, mode)  # noqa: E731
-    run()
-    default_ms, ref = _time(run, reps, stream)
+    kind, box_ms, ref = _tune_boxes(uw, run, reps, stream, "first-contact steps")
+    default_ms = box_ms[kind]
     table = []
     for c, b in itertools.product(soft_caps, blocks):
         uw.set_launch_config(1, 0, c, b)
@@ -97,7 +117,8 @@ def tune_segments(uw, q0: torch.Tensor, q1: torch.Tensor, verify_delta: float, s
     else:
         cfg, ms = {"soft_cap": 0, "blocks": 0}, default_ms
         uw.set_launch_config(1)
-    return TuneReport("segments", cfg, default_ms, ms, table)
+    cfg = dict(cfg, boxes=kind)
+    return TuneReport("segments", cfg, default_ms, ms, table + [({"boxes": k}, v) for k, v in box_ms.items()])
 
 
 def tune_key(meshes, device_name: str, num_sms: int, kernel: str, extra: str = "") -> str:
@@ -153,6 +174,8 @@ def _world_key(uw, kernel: str) -> str:
 
 
 def _apply(uw, kernel: str, cfg: dict) -> None:
+    if "boxes" in cfg:
+        uw.set_node_boxes(cfg["boxes"])
     if kernel == "states":
         uw.set_launch_config(0, cfg.get("width", 0), cfg.get("soft_cap", 0), cfg.get("blocks", 0))
     else:
@@ -162,6 +185,10 @@ def _apply(uw, kernel: str, cfg: dict) -> None:
 def autotune(uw, states: torch.Tensor | None = None, segments=None, verify_delta: float = 0.001,
              cache: "TuneCache | str | bool | None" = None, **kw):
     """Tune both kernels on samples of the caller's workload; returns the reports.
+
+    The node-box kind (axis-aligned or oriented BVH boxes) is one setting per
+    world: when both kernels are tuned, the segments kernel's choice is the one
+    left on the world.
 
     With a cache (True for the default file, a path, or a TuneCache) a
     configuration already tuned for the same mesh pair on the same GPU model is

@@ -89,7 +89,9 @@ def test_autotune_keeps_verdicts(built_lib, oracle_mod):
     before_v = uw.is_valid_states(q).clone()
     before_s = uw.first_contact_steps(a, b, 0.001).clone()
     rep = autotune(uw, states=q, segments=(a, b), verify_delta=0.001, soft_caps=(128, 0), blocks=(0, 2), reps=1)
-    assert len(rep["states"].table) == 3 * 2 * 2 and len(rep["segments"].table) == 2 * 2
+    # the launch grid plus the two node-box kinds, timed first
+    assert len(rep["states"].table) == 3 * 2 * 2 + 2 and len(rep["segments"].table) == 2 * 2 + 2
+    assert rep["segments"].best["boxes"] == uw.get_node_boxes()
     assert torch.equal(uw.is_valid_states(q), before_v)
     assert torch.equal(uw.first_contact_steps(a, b, 0.001), before_s)
     cfg = uw.get_launch_config(0)
@@ -110,12 +112,13 @@ def test_autotune_cache_reapplies_a_tuned_configuration(built_lib, tmp_path):
     uw = _world()
     q = torch.from_numpy(W.uniform_states(100000, -2.0, 2.0, uw.scene_scale, seed=47)).cuda()
     first = autotune(uw, states=q, cache=path, soft_caps=(128, 0), blocks=(0, 2), reps=1)["states"]
-    assert len(first.table) == 3 * 2 * 2
+    assert len(first.table) == 3 * 2 * 2 + 2
     applied = uw.get_launch_config(0)
     second_world = _world()
     again = autotune(second_world, states=q, cache=path, soft_caps=(128, 0), blocks=(0, 2), reps=1)["states"]
     assert again.table == [] and again.best == first.best
     assert second_world.get_launch_config(0) == applied
+    assert second_world.get_node_boxes() == first.best["boxes"]
     assert torch.equal(second_world.is_valid_states(q), uw.is_valid_states(q))
     Ve, Fe, Vr, Fr = W.interlocking_tori(1.0, 0.25, 48, 24)
     other = pw.UnitWorld(0)
@@ -124,5 +127,5 @@ def test_autotune_cache_reapplies_a_tuned_configuration(built_lib, tmp_path):
     other.scaleToUnit()
     other.angleModel(0.0, 0.0)
     miss = autotune(other, states=q, cache=TuneCache(path), soft_caps=(0,), blocks=(0,), reps=1)["states"]
-    assert len(miss.table) == 3
+    assert len(miss.table) == 3 + 2
     assert len(TuneCache(path).load()) == 2
