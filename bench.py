@@ -69,7 +69,19 @@ WORKLOADS = {
                W.cfg_plate_knot, 4_000_000),
     "ompl": ("motions checked/sec (OMPL discrete motion check, validate_motion_pairs, alpha puzzle)",
              lambda: _alpha_ompl()[0], 1_000_000),
+    # the other rows of the path, each on the interlocking tori
+    "disentangled": ("is_disentangled checks/sec (interlocking tori)", W.cfg_interlocking_tori, 20_000_000),
+    "contacts": ("contact enumerations/sec (intersecting_segments on colliding interlocking-tori states)",
+                 W.cfg_interlocking_tori, 1024),
+    "keyconf": ("key-configuration candidates checked/sec (enum_free_configuration, 256 spins, only_median)",
+                W.cfg_interlocking_tori, 8192),
+    "touch": ("touch samples/sec (calc_touch: 128 random segments per key to first contact)",
+              W.cfg_interlocking_tori, 8192),
 }
+ROW_WORKLOADS = ("disentangled", "contacts", "keyconf", "touch")
+KEYCONF_SPINS = 256          # envconfig.py:134 NumberOfRotations
+KEYCONF_MARGIN = 1e-6        # envconfig.py:136 Margin
+TOUCH_PER_KEY = 128          # envconfig.py:141 OversamplingClearanceSample
 # OMPL motion workload: collision resolution and the spread of the motions' targets (OMPL units)
 OMPL_CDRES = 0.01
 OMPL_SIGMA = 2.0
@@ -1091,6 +1103,339 @@ def _cpu_plain_narrow(validated, target_s):
     return cpu, parity
 
 
+def _surface_pairs(V, F, Vr, Fr, n, rng):
+    """n (robot point, robot normal, env point, env normal) surface samples: a
+    triangle drawn by area, a uniform point on it, the face's unit normal."""
+    def draw(V, F):
+        a, b, c = V[F[:, 0]], V[F[:, 1]], V[F[:, 2]]
+        nrm = np.cross(b - a, c - a)
+        area = np.linalg.norm(nrm, axis=1)
+        t = rng.choice(len(F), n, p=area / area.sum())
+        u, v = rng.random(n), rng.random(n)
+        flip = u + v > 1
+        u[flip], v[flip] = 1 - u[flip], 1 - v[flip]
+        pts = a[t] + u[:, None] * (b[t] - a[t]) + v[:, None] * (c[t] - a[t])
+        return pts, nrm[t] / area[t][:, None]
+    rp, rn = draw(Vr, Fr)
+    ep, en = draw(V, F)
+    return rp, rn, ep, en
+
+
+class RowJob:
+    """One of the row workloads (is_disentangled, contact enumeration, key
+    configurations, touch sampling) on the interlocking tori: the batch of one
+    step, the GPU call through the public API, the oracle on a sample and the
+    comparison of their results."""
+
+    def __init__(self, name, uw, n, seed):
+        import torch
+        self.name, self.uw, self.n = name, uw, n
+        s = uw.scene_scale
+        rng = np.random.default_rng(3000 + seed)
+        self.dev = uw._device
+        self.device_timed = name == "disentangled"
+        if name == "disentangled":
+            self.q = W.uniform_states(n, -2.0, 2.0, s, seed=seed)
+            self.a = torch.from_numpy(self.q).to(self.dev)
+            self.units, self.unit = n, "checks/s"
+        elif name == "contacts":
+            q = W.uniform_states(8 * n, -0.6, 0.6, s, seed=seed)
+            hit = ~uw.is_valid_states(torch.from_numpy(q)).cpu().numpy()
+            self.q = q[hit][:n]
+            self.n = self.q.shape[0]
+            self.units, self.unit = self.n, "states/s"
+        elif name == "keyconf":
+            Ve, Fe = uw._cd(0)
+            Vr, Fr = uw._cd(1)
+            self.pairs = _surface_pairs(Ve, Fe, Vr, Fr, n, rng)
+            self.units, self.unit = n * KEYCONF_SPINS, "checks/s"
+        else:
+            q = W.uniform_states(4 * n, -2.0, 2.0, s, seed=seed)
+            ok = uw.is_valid_states(torch.from_numpy(q)).cpu().numpy()
+            self.keys = q[ok][:n]
+            self.units, self.unit = self.keys.shape[0] * TOUCH_PER_KEY, "segments/s"
+        self.seed = seed
+
+    def gpu(self):
+        """One step through the public API; returns the step's result."""
+        from puzzletunneldiscovery_gb300 import sampling as SP
+        uw = self.uw
+        if self.name == "disentangled":
+            return uw.is_disentangled_states(self.a)
+        if self.name == "contacts":
+            return [uw.intersecting_segments(q) for q in self.q]
+        if self.name == "keyconf":
+            rp, rn, ep, en = self.pairs
+            return SP.enum_free_configurations(uw, rp, rn, ep, en, KEYCONF_MARGIN, KEYCONF_SPINS, only_median=True)
+        res, self.to = SP.calc_touch_batch(uw, self.keys, TOUCH_PER_KEY, uw.recommended_cres,
+                                           np.random.default_rng(4000 + self.seed))
+        return res
+
+    def cpu(self, ow, m, threads):
+        """(units, seconds, result) of the oracle on the first m units of the step."""
+        from puzzletunneldiscovery_gb300 import sampling as SP
+        t0 = time.perf_counter()
+        if self.name == "disentangled":
+            res = ow.is_disentangled(self.q[:m], nthreads=threads)
+            units = m
+        elif self.name == "contacts":
+            import concurrent.futures as cf
+            with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+                res = list(ex.map(ow.intersecting_segments, self.q[:m]))
+            units = m
+        elif self.name == "keyconf":
+            rp, rn, ep, en = (x[:m] for x in self.pairs)
+            ang = np.broadcast_to(np.arange(KEYCONF_SPINS) * (2 * np.pi / KEYCONF_SPINS), (m, KEYCONF_SPINS))
+            qs = SP._touch_states(rp, rn, ep, en, KEYCONF_MARGIN, ang)
+            valid = ow.is_valid(np.ascontiguousarray(qs.reshape(-1, 7)), nthreads=threads).reshape(m, KEYCONF_SPINS)
+            res = SP._free_spins(qs, valid, True)
+            units = m * KEYCONF_SPINS
+        else:
+            k = m * TOUCH_PER_KEY
+            frm = np.repeat(self.keys[:m], TOUCH_PER_KEY, axis=0)
+            res, _ = ow.segments_first_contact(frm, self.to[:k], self.uw.recommended_cres, mode=0, nthreads=threads)
+            units = k
+        return units, time.perf_counter() - t0, res
+
+    def mismatches(self, ow, gpu_res, cpu_res, m):
+        """Results of the first m units that differ from the oracle's."""
+        if self.name == "disentangled":
+            return int((gpu_res[:m].cpu().numpy() != cpu_res).sum())
+        if self.name == "contacts":
+            bad = 0
+            for (b, e, mg, p), (b2, e2, mg2, p2, _) in zip(gpu_res[:m], cpu_res):
+                same = p.shape == p2.shape and (p == p2).all() and (b == b2).all() and (e == e2).all() \
+                    and (mg == mg2).all()
+                bad += 0 if same else 1
+            return bad
+        if self.name == "keyconf":
+            return sum(0 if np.array_equal(x, y) else 1 for x, y in zip(gpu_res[:m], cpu_res))
+        # touch: the GPU's tuples against the oracle's first contacts (done = no contact), and the
+        # full tuples of the first 256 segments against the oracle's transit loop
+        k = m * TOUCH_PER_KEY
+        lf, st, done, lt, tt = gpu_res
+        bad = int((done[:k].astype(bool) != (cpu_res == -1)).sum())
+        frm = np.repeat(self.keys[:m], TOUCH_PER_KEY, axis=0)
+        for i in range(min(k, 256)):
+            (wl, ws_, wd, wlt, wtt), _, _ = ow.transit_state_to_with_contact(frm[i], self.to[i],
+                                                                              self.uw.recommended_cres)
+            same = (lf[i] == wl).all() and (st[i] == ws_).all() and bool(done[i]) == wd and lt[i] == wlt \
+                and tt[i] == wtt
+            bad += 0 if same else 1
+        return bad
+
+
+def run_rows(args):
+    """--workload disentangled | contacts | keyconf | touch: one row of the path
+    through the public API, timed per step; the oracle on a sample of the same
+    step on the host cores, with its results compared."""
+    import torch
+
+    import puzzletunneldiscovery_gb300 as pw
+
+    ws, rank, local = _dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    Ve, Fe, Vr, Fr = _meshes(args.workload)
+    uw = pw.UnitWorld(local)
+    uw.load_env_mesh(Ve, Fe)
+    uw.load_robot_mesh(Vr, Fr)
+    uw.scaleToUnit()
+    uw.angleModel(0.0, 0.0)
+    job = RowJob(args.workload, uw, args.n, rank)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    for _ in range(args.warmup):
+        res = job.gpu()
+    torch.cuda.synchronize(dev)
+    step_ms = []
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize(dev)
+            if job.device_timed:
+                s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s0.record(stream)
+                res = job.gpu()
+                s1.record(stream)
+                torch.cuda.synchronize(dev)
+                step_ms.append(s0.elapsed_time(s1))
+            else:
+                t0 = time.perf_counter()
+                res = job.gpu()
+                torch.cuda.synchronize(dev)
+                step_ms.append(1e3 * (time.perf_counter() - t0))
+    ms = sum(step_ms) / len(step_ms)
+    value = job.units / (ms / 1e3)
+    # end to end: host inputs in, host results out, inside the timed region
+    if job.device_timed:
+        hq = torch.from_numpy(job.q).pin_memory()
+        e2e_ms = 0.0
+        for i in range(args.steps):
+            flush.zero_()
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            out = uw.is_disentangled_states(hq.to(dev, non_blocking=True)).cpu()
+            s1.record(stream)
+            torch.cuda.synchronize(dev)
+            e2e_ms += s0.elapsed_time(s1)
+        if not torch.equal(out, res.cpu()):
+            raise RuntimeError("host-array path disagrees with the device path")
+        e2e = {"value": job.units * args.steps / (e2e_ms / 1e3), "unit": job.unit,
+               "h2d_bytes_per_step": int(job.q.nbytes), "d2h_bytes_per_step": int(job.n)}
+    else:
+        # the public call takes host arrays and returns host arrays: the timed steps are end to end
+        e2e = {"value": value, "unit": job.unit, "h2d_bytes_per_step": _row_h2d(job),
+               "d2h_bytes_per_step": _row_d2h(job, res)}
+    if rank != 0:
+        return
+    roof = None
+    if args.workload == "disentangled":
+        # one thread per state, FP64 box test: 56 B in, 1 B out per state
+        peak, kind = _peaks()
+        ach = job.units * 57 / (ms / 1e3) / 1e9
+        roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "traffic": None,
+                "kernel": "k_disentangled", "kernel_ms": ms, "peak_source": kind, "algorithmic_bytes": job.units * 57}
+    cpu, parity = None, None
+    if ws == 1 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+        O.build()
+        ow = O.OracleWorld(Ve, Fe, Vr, Fr)
+        cores = os.cpu_count() or 1
+        m = max(1, min(job.n, 64 if args.workload in ("contacts", "keyconf", "touch") else 65536))
+        while True:
+            units, dt, cres = job.cpu(ow, m, cores)
+            if dt >= args.cpu_seconds or m >= job.n:
+                break
+            m = min(job.n, max(m * 2, int(m * args.cpu_seconds / max(dt, 1e-3) * 1.1)))
+        cpu = {"value": units / dt, "unit": job.unit, "cores": cores, "kind": "port",
+               "sample": "the first %d %s of the step (%d units, %.1f s)"
+                         % (m, {"disentangled": "states", "contacts": "states", "keyconf": "surface pairs",
+                                "touch": "keys"}[args.workload], units, dt)}
+        parity = {"mismatches": job.mismatches(ow, res, cres, m), "mismatch_sample": int(m),
+                  "compared": {"disentangled": "is_disentangled verdict of every state",
+                               "contacts": "contact rows (face pairs, segment ends, lengths) of every state",
+                               "keyconf": "the free median spins of every surface pair",
+                               "touch": "done flag of every segment; full transit tuples of the first 256"}[
+                      args.workload]}
+    cfg = {"workload": "%s/interlocking_tori" % args.workload, "units_per_step": job.units,
+           "l2": "flushed (256 MB write) between timed steps",
+           "parallelism": "replicas" if ws == 1 else "independent replicas"}
+    if args.workload == "keyconf":
+        cfg.update({"surface_pairs": job.n, "spins": KEYCONF_SPINS, "margin": KEYCONF_MARGIN, "only_median": True})
+    elif args.workload == "touch":
+        cfg.update({"keys": job.keys.shape[0], "segments_per_key": TOUCH_PER_KEY, "stepping": uw.recommended_cres})
+    elif args.workload == "contacts":
+        cfg.update({"states": job.n, "states_drawn_from": "colliding uniform states in [-0.6, 0.6]^3 (world)"})
+    detail = {"mismatches": parity["mismatches"] if parity else None,
+              "mismatch_sample": parity["mismatch_sample"] if parity else 0, "parity": parity, "step_ms": step_ms,
+              "node_boxes": uw.get_node_boxes()}
+    if args.workload == "contacts":
+        detail["contact_rows_per_state"] = sum(r[3].shape[0] for r in res) / max(1, len(res))
+    if args.workload == "keyconf":
+        detail["key_configurations_per_step"] = sum(r.shape[0] for r in res)
+    if args.workload == "touch":
+        detail["free_fraction"] = float(res[2].mean())
+    line = {"metric": WORKLOADS[args.workload][0], "value": value, "unit": job.unit, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 box test" if args.workload == "disentangled" else "f32 traversal + f64 state math/re-tests",
+            "data": "synthetic (seeded)", "config": cfg, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "clocks": clk.summary(),
+            # per step: k_disentangled; contacts: collect + evaluate per state; keyconf: traversal + re-test;
+            # touch: the segment query's 7 kernels and the contact-state rebuild
+            "gpu_launches": {"disentangled": 1, "contacts": 2 * job.n, "keyconf": 2, "touch": 8}[args.workload]
+            * args.steps,
+            "detail": detail}
+    print(json.dumps(line), flush=True)
+    if parity and parity["mismatches"]:
+        print("verdict mismatches against the oracle: %d" % parity["mismatches"], file=sys.stderr)
+        sys.exit(3)
+
+
+def _row_h2d(job):
+    if job.name == "contacts":
+        return int(job.q.nbytes)
+    if job.name == "keyconf":
+        return int(job.n * KEYCONF_SPINS * 56)
+    return int(job.units * 2 * 56)
+
+
+def _row_d2h(job, res):
+    if job.name == "contacts":
+        return int(sum(r[0].nbytes + r[1].nbytes + r[2].nbytes + r[3].nbytes for r in res))
+    if job.name == "keyconf":
+        return int(job.n * KEYCONF_SPINS)
+    return int(job.units * (2 * 56 + 1 + 8))
+
+
+class _RefRowJob(RowJob):
+    """The row workloads' batches built without a GPU (the oracle answers the
+    verdicts the GPU arm uses to pick its colliding or free inputs)."""
+
+    def __init__(self, name, ow, n, Fe, Fr):
+        self.name, self.n = name, n
+        s = ow.scene_scale
+        rng = np.random.default_rng(3000)
+        self.uw = type("_Stepping", (), {"recommended_cres": 0.001})()
+        if name == "disentangled":
+            self.q = W.uniform_states(n, -2.0, 2.0, s, seed=0)
+            self.units, self.unit = n, "checks/s"
+        elif name == "contacts":
+            q = W.uniform_states(8 * n, -0.6, 0.6, s, seed=0)
+            self.q = q[~ow.is_valid(q)][:n]
+            self.n = self.q.shape[0]
+            self.units, self.unit = self.n, "states/s"
+        elif name == "keyconf":
+            Ve, Vr = ow.vertices(0), ow.vertices(1)
+            self.pairs = _surface_pairs(Ve, np.asarray(Fe, np.int64), Vr, np.asarray(Fr, np.int64), n, rng)
+            self.units, self.unit = n * KEYCONF_SPINS, "checks/s"
+        else:
+            from puzzletunneldiscovery_gb300 import sampling as SP
+            q = W.uniform_states(4 * n, -2.0, 2.0, s, seed=0)
+            self.keys = q[ow.is_valid(q)][:n]
+            K = self.keys.shape[0]
+            r = np.random.default_rng(4000)
+            frm = np.repeat(self.keys, TOUCH_PER_KEY, axis=0)
+            self.to = SP.apply_rows(frm, SP.random_on_sphere(K * TOUCH_PER_KEY, 1.0, r),
+                                    SP.random_within_sphere(K * TOUCH_PER_KEY, 2 * np.pi, r))
+            self.units, self.unit = K * TOUCH_PER_KEY, "segments/s"
+
+
+def run_rows_reference(args):
+    """--impl reference for the row workloads: the oracle on the host cores, a
+    bounded sample of the step per timed step."""
+    ws, rank, _ = _dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    Ve, Fe, Vr, Fr = _meshes(args.workload)
+    ow = O.OracleWorld(Ve, Fe, Vr, Fr)
+    job = _RefRowJob(args.workload, ow, args.n, Fe, Fr)
+    cores = os.cpu_count() or 1
+    per = {"disentangled": 500, "contacts": 1, "keyconf": 1, "touch": 1}[args.workload]
+    div = {"disentangled": 1, "contacts": 8, "keyconf": 4, "touch": 4}[args.workload]
+    m = max(1, min(job.n, args.ref_sample // div * per))
+    times, units = [], 0
+    for it in range(args.warmup + args.steps):
+        u, dt, _ = job.cpu(ow, m, cores)
+        if it >= args.warmup:
+            times.append(dt)
+            units += u
+    value = units / sum(times)
+    line = {"impl": "reference", "metric": WORKLOADS[args.workload][0], "value": value, "unit": job.unit,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, same batch as the GPU arm)",
+            "config": {"workload": "%s/interlocking_tori" % args.workload, "units_per_step": job.units,
+                       "sample_per_step": m},
+            "cpu_baseline": {"value": value, "unit": job.unit, "cores": cores, "kind": "port",
+                             "sample": "the first %d of the step's %d inputs per step" % (m, job.n)},
+            "e2e": {"value": value, "unit": job.unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
 def _bf16_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -1189,8 +1534,9 @@ def _traffic_per_segment():
 
 def run_profile_case(args):
     """Small fixed workloads for ncu captures (no JSON line): `states`, `segments`,
-    `mlp`, `train`, `ompl` or `all` (every kernel of the engine once), with
-    --n units, on the interlocking tori (the alpha puzzle for `ompl`)."""
+    `mlp`, `train`, `plate`, `ompl` or `all` (every kernel of the engine once),
+    with --n units, on the interlocking tori (the plate and torus knot for
+    `plate`, the alpha puzzle for `ompl`); --node-boxes picks the BVH boxes."""
     import torch
 
     import puzzletunneldiscovery_gb300 as pw
@@ -1214,13 +1560,22 @@ def run_profile_case(args):
         torch.cuda.synchronize()
         print("done", states, float(v.float().mean()))
         return
-    Ve, Fe, Vr, Fr = W.cfg_interlocking_tori()
+    Ve, Fe, Vr, Fr = W.cfg_plate_knot() if what == "plate" else W.cfg_interlocking_tori()
     uw = pw.UnitWorld(0)
     uw.load_env_mesh(Ve, Fe)
     uw.load_robot_mesh(Vr, Fr)
     uw.scaleToUnit()
     uw.angleModel(0.0, 0.0)
+    if args.node_boxes:
+        uw.set_node_boxes(args.node_boxes)
     s = uw.scene_scale
+    if what == "plate":
+        q = torch.from_numpy(_batch(n, s, 0, "plate", Ve)[0]).to(dev)
+        for _ in range(3):
+            uw.is_valid_states(q)
+        torch.cuda.synchronize()
+        print("done", uw.last_stats())
+        return
     if what == "all":
         from puzzletunneldiscovery_gb300 import narrow as N
         q = torch.from_numpy(W.uniform_states(n, -2, 2, s, seed=0)).to(dev)
@@ -1295,8 +1650,10 @@ def main():
     ap.add_argument("--e2e-n", type=int, default=20_000_000, help="surrogate: candidates per end-to-end step")
     ap.add_argument("--sweep", type=lambda v: [float(x) for x in v.split(",") if x], default=[0.25, 0.5, 0.6],
                     help="surrogate: further checked fractions reported in detail")
-    ap.add_argument("--profile-case", choices=["states", "segments", "mlp", "train", "ompl", "all"], default=None,
+    ap.add_argument("--profile-case", choices=["states", "segments", "mlp", "train", "plate", "ompl", "all"], default=None,
                     help="run a small fixed workload for an ncu capture instead of the benchmark")
+    ap.add_argument("--node-boxes", choices=["aligned", "oriented"], default=None,
+                    help="profile cases: the BVH node boxes (default: the world's default)")
     args = ap.parse_args()
     if args.profile_case:
         args.n = args.n or 1_000_000
@@ -1314,6 +1671,8 @@ def main():
         run_ompl_reference(args) if args.impl == "reference" else run_ompl(args)
     elif args.workload == "surrogate":
         run_surrogate_reference(args) if args.impl == "reference" else run_surrogate(args)
+    elif args.workload in ROW_WORKLOADS:
+        run_rows_reference(args) if args.impl == "reference" else run_rows(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -139,20 +139,29 @@ def enum_free_configurations(uw: UnitWorld, rob_points, rob_normals, env_points,
     qs = _touch_states(rob_points, rob_normals, env_points, env_normals, margin, angles)
     flat = torch.from_numpy(np.ascontiguousarray(qs.reshape(-1, 7))).to(uw._device)
     valid = uw.is_valid_states(flat).cpu().numpy().reshape(P, denominator)
-    out = []
-    for p in range(P):
-        if not only_median:
-            out.append(qs[p][valid[p]])
-            continue
-        picks, run = [], []
-        for i in range(denominator):
-            if valid[p, i]:
-                run.append(i)
-            elif run:
-                picks.append(run[len(run) // 2])
-                run = []
-        out.append(qs[p][picks] if picks else np.zeros((0, 7)))
-    return out
+    return _free_spins(qs, valid, only_median)
+
+
+def _free_spins(qs, valid, only_median):
+    """The free spins of every surface pair ([P, A, 7] states, [P, A] verdicts):
+    all of them, or the middle spin of every run of consecutive free spins that
+    ends before the last spin (unit_world.cc:1367-1386)."""
+    P, A = valid.shape
+    if not only_median:
+        rows, cols = np.nonzero(valid)
+    else:
+        v = valid.astype(np.int8)
+        prev = np.zeros_like(v)
+        prev[:, 1:] = v[:, :-1]
+        nxt = np.zeros_like(v)
+        nxt[:, :-1] = v[:, 1:]
+        sr, sc = np.nonzero(v & (1 - prev))            # run starts, row-major
+        er, ec = np.nonzero(v & (1 - nxt))             # run ends, in the same order
+        keep = ec < A - 1                              # a run still open at the last spin is dropped
+        rows, cols = sr[keep], (sc + (ec - sc + 1) // 2)[keep]
+    picked = qs[rows, cols]
+    bounds = np.searchsorted(rows, np.arange(P + 1))
+    return [picked[bounds[p]:bounds[p + 1]] if bounds[p + 1] > bounds[p] else np.zeros((0, 7)) for p in range(P)]
 
 
 def enum_free_configuration(uw: UnitWorld, rob_surface_point, rob_surface_normal, env_surface_point,
@@ -230,6 +239,38 @@ def calc_touch(uw: UnitWorld, q0, batch_size: int, stepping: float, rng=None):
     b = torch.from_numpy(np.ascontiguousarray(to)).to(dev)
     lf, st, done, lt, tt = uw.transit_states_to_with_contact(a, b, stepping)
     return [lf.cpu().numpy(), st.cpu().numpy(), done.cpu().numpy(), lt.cpu().numpy(), tt.cpu().numpy()]
+
+
+def calc_touch_batch(uw: UnitWorld, keys, per_key: int, stepping: float, rng=None):
+    """calc_touch for K keys at once (the loop over keys of keyconf.py:306-316 and
+    preprocess_key.py:174): per_key random segments from every key (translation
+    on the unit sphere, rotation uniform within 2π, drawn for all keys in one
+    go), all stepped to their first contact in one batch.  Row i * per_key + j
+    of the five arrays belongs to key i.  Returns (the five arrays, the
+    segments' end states)."""
+    keys = np.atleast_2d(np.asarray(keys, np.float64))
+    rng = np.random.default_rng() if rng is None else rng
+    K = keys.shape[0]
+    frm = np.repeat(keys, per_key, axis=0)
+    tr = random_on_sphere(K * per_key, 1.0, rng)
+    aa = random_within_sphere(K * per_key, 2 * math.pi, rng)
+    to = apply_rows(frm, tr, aa)
+    dev = uw._device
+    a = torch.from_numpy(frm).to(dev)
+    b = torch.from_numpy(to).to(dev)
+    lf, st, done, lt, tt = uw.transit_states_to_with_contact(a, b, stepping)
+    return [lf.cpu().numpy(), st.cpu().numpy(), done.cpu().numpy(), lt.cpu().numpy(), tt.cpu().numpy()], to
+
+
+def apply_rows(states, tr, aa):
+    """osr::apply (osr_state.cc:244-259) row by row: state i translated by tr[i] and
+    rotated on the left by the angle-axis vector aa[i]."""
+    states = np.atleast_2d(np.asarray(states, np.float64))
+    rot = states[:, 3:] / np.linalg.norm(states[:, 3:], axis=1, keepdims=True)
+    ang = np.linalg.norm(aa, axis=1)
+    axis = np.where(ang[:, None] == 0.0, np.array([1.0, 0.0, 0.0]), aa / np.where(ang == 0.0, 1.0, ang)[:, None])
+    r = quat_mul(quat_from_angle_axis(ang, axis), rot)
+    return compose(states[:, :3] + tr, r)
 
 
 def sample_one_touch(uw: UnitWorld, q0, stepping: float, rng=None):

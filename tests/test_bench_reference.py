@@ -12,6 +12,10 @@ ARGS = {
     "segments": ["--n", "20000", "--ref-sample", "20"],
     "plate": ["--n", "100000", "--ref-sample", "20"],
     "ompl": ["--n", "20000", "--ref-sample", "40"],
+    "disentangled": ["--n", "100000", "--ref-sample", "20"],
+    "contacts": ["--n", "64", "--ref-sample", "32"],
+    "keyconf": ["--n", "256", "--ref-sample", "32"],
+    "touch": ["--n", "64", "--ref-sample", "16"],
 }
 
 

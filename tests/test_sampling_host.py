@@ -141,3 +141,41 @@ def test_autotune_cache_keys_and_file(tmp_path):
     c.put("other", {"config": {}, "default_ms": 1.0, "best_ms": 1.0})
     assert TuneCache(str(tmp_path / "sub" / "tune.json")).get(k)["config"]["width"] == 16
     assert sorted(p.name for p in (tmp_path / "sub").iterdir()) == ["tune.json"]
+
+
+def test_free_spins_follow_the_run_median_rule():
+    """_free_spins (vectorised) against the reference's loop (unit_world.cc:1367-1386):
+    each run of consecutive free spins contributes its middle spin, a run still
+    open at the last spin contributes nothing; without only_median every free
+    spin is kept."""
+    from puzzletunneldiscovery_gb300 import sampling as S
+    rng = np.random.default_rng(3)
+
+    def loop(qs, valid):
+        out = []
+        for p in range(valid.shape[0]):
+            picks, run = [], []
+            for i in range(valid.shape[1]):
+                if valid[p, i]:
+                    run.append(i)
+                elif run:
+                    picks.append(run[len(run) // 2])
+                    run = []
+            out.append(qs[p][picks] if picks else np.zeros((0, 7)))
+        return out
+
+    for _ in range(200):
+        P, D = int(rng.integers(1, 20)), int(rng.integers(1, 40))
+        valid = rng.random((P, D)) < rng.random()
+        qs = rng.random((P, D, 7))
+        assert all(np.array_equal(x, y) for x, y in zip(loop(qs, valid), S._free_spins(qs, valid, True)))
+        assert all(np.array_equal(qs[p][valid[p]], r) for p, r in enumerate(S._free_spins(qs, valid, False)))
+
+
+def test_apply_rows_matches_apply_batch():
+    from puzzletunneldiscovery_gb300 import sampling as S
+    rng = np.random.default_rng(4)
+    q = np.array([0.1, 0.2, 0.3, 0.9, 0.1, 0.2, 0.3])
+    tr, aa = rng.normal(size=(10, 3)), rng.normal(size=(10, 3))
+    aa[0] = 0.0
+    assert np.array_equal(S.apply_batch(q, tr, aa), S.apply_rows(np.repeat(q[None], 10, 0), tr, aa))
