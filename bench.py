@@ -72,7 +72,7 @@ WORKLOADS = {
     # the other rows of the path, each on the interlocking tori
     "disentangled": ("is_disentangled checks/sec (interlocking tori)", W.cfg_interlocking_tori, 20_000_000),
     "contacts": ("contact enumerations/sec (intersecting_segments on colliding interlocking-tori states)",
-                 W.cfg_interlocking_tori, 1024),
+                 W.cfg_interlocking_tori, 65536),
     "keyconf": ("key-configuration candidates checked/sec (enum_free_configuration, 256 spins, only_median)",
                 W.cfg_interlocking_tori, 8192),
     "touch": ("touch samples/sec (calc_touch: 128 random segments per key to first contact)",
@@ -182,6 +182,10 @@ def run_ompl(args):
             dist.barrier()
         torch.cuda.synchronize(dev)
 
+    # the states kernel's node boxes, picked on the motions themselves
+    from puzzletunneldiscovery_gb300.autotune import _tune_boxes
+    box_kind, box_ms, _ = _tune_boxes(uw, 0, lambda: OC._check_motions_dev(uw, a, b, lo, hi, OMPL_CDRES)[0], 1, stream,
+                                      "verdicts")
     for _ in range(args.warmup):
         OC._check_motions_dev(uw, a, b, lo, hi, OMPL_CDRES)
     barrier()
@@ -238,11 +242,12 @@ def run_ompl(args):
             "traffic": None, "kernel": "whole call (k_ompl_counts, k_ompl_states, k_states, k_ompl_reduce)",
             "peak_source": peak_kind, "algorithmic_bytes": alg_bytes,
             "note": "the states pass is bound by the traversal's SM issue, as in the plate workload"}
-    cpu = None
+    cpu, cpu_mism, cpu_n = None, None, 0
     if ws == 1 and not args.no_cpu_baseline:
         ow, _ = _ompl_oracle()
         cv, cn, cpm, cdt, ov = _ompl_cpu(ow, A, B, lo, hi, args.cpu_seconds)
-        if not np.array_equal(ov, verdicts[:cn]):
+        cpu_mism, cpu_n = int((ov != verdicts[:cn]).sum()), int(cn)
+        if cpu_mism:
             raise RuntimeError("GPU verdicts differ from the oracle's on the CPU sample")
         cpu = {"value": cv, "unit": "motions/s", "cores": os.cpu_count() or 1, "kind": "port",
                "sample": "first %d motions of the batch (OMPL's early-exit order, %.2f states checked per "
@@ -263,7 +268,9 @@ def run_ompl(args):
             # segment counts, three pass counts, then per window of a pass's states: generation,
             # traversal, re-test, reduction (a lower bound: each pass starts its own window)
             "gpu_launches": (4 + 4 * windows) * args.steps,
-            "detail": {"states_checked_per_step": states, "states_per_motion": states / args.n,
+            "detail": {"mismatches": cpu_mism, "mismatch_sample": cpu_n,
+                       "node_boxes": {"states": box_kind, "ms": box_ms},
+                       "states_checked_per_step": states, "states_per_motion": states / args.n,
                        "valid_fraction": float(verdicts.mean()), "windows": windows, "step_ms": step_ms}}
     print(json.dumps(line))
     if ws > 1:
@@ -546,9 +553,10 @@ def run_ours(args):
 
     # both kinds of BVH node box on the same batch: time per step and the tests they take
     boxes = {}
-    default_kind = uw.get_node_boxes()
+    bk = 1 if args.workload == "segments" else 0
+    default_kind = uw.get_node_boxes(bk)
     for kind in ("aligned", "oriented"):
-        uw.set_node_boxes(kind)
+        uw.set_node_boxes(kind, bk)
         for _ in range(2):
             work.gpu(uw, a, b)
         bms, bst = [], None
@@ -565,7 +573,7 @@ def run_ours(args):
         boxes[kind] = {"ms_per_step": sum(bms) / len(bms), "node_tests": bst["node_tests"],
                        "leaf_tests": bst["leaf_tests"], "fp64_retests": bst["retests"],
                        "traverse_ms": bst["traverse_ms"]}
-    uw.set_node_boxes(default_kind)
+    uw.set_node_boxes(default_kind, bk)
     boxes["default"] = default_kind
 
     # the same query replayed as one CUDA graph (graph mode: no host synchronisation inside the step)
@@ -760,6 +768,9 @@ def surrogate_measure(args, local, rank, n, steps, warmup, with_cpu, e2e=True):
 
     cand = draw(n)                            # resident candidates (not timed)
     prob = torch.empty(n, dtype=torch.float32, device=dev)
+    # the states kernel's node boxes, picked on a sample of the candidates
+    from puzzletunneldiscovery_gb300.autotune import pick_node_boxes
+    boxes = pick_node_boxes(uw, states=cand[: 1 << 22])
     # exact labels of a 4M sample: precision / recall of the network as a free-space predictor
     sample = cand[: 1 << 22]
     exact = uw.is_valid_states(sample)
@@ -829,7 +840,7 @@ def surrogate_measure(args, local, rank, n, steps, warmup, with_cpu, e2e=True):
            "top_frac": args.top_frac,
            "g_ms": g_ms, "p_ms": p_ms, "g_free": g_free, "p_free": p_free, "g_checked": g_checked,
            "precision": prec, "recall": rec, "false_free": false_free, "train_ms": train_ms, "rep": rep,
-           "sweep": sweep, "clocks": clk.summary(), "e2e": None, "cpu": None, "parity": None}
+           "sweep": sweep, "clocks": clk.summary(), "e2e": None, "cpu": None, "parity": None, "node_boxes": boxes}
 
     if e2e:
         # end to end: candidates from pinned host memory, accepted states back to the host
@@ -890,7 +901,8 @@ def surrogate_summary(m):
             "mismatches": m["parity"]["mismatches"] if m["parity"] else None,
             "mismatch_sample": m["parity"]["mismatch_sample"] if m["parity"] else 0,
             "train_ms": m["train_ms"], "roofline": m["roof"], "cpu_baseline": m["cpu"],
-            "top_fraction_sweep": {k: v["over_plain"] for k, v in b.items()}, "clocks": m["clocks"]}
+            "top_fraction_sweep": {k: v["over_plain"] for k, v in b.items()}, "clocks": m["clocks"],
+            "node_boxes": m["node_boxes"]}
 
 
 def run_surrogate(args):
@@ -932,7 +944,7 @@ def run_surrogate(args):
                        "train_ms": m["train_ms"], "train_steps": rep.steps,
                        "train_labels_per_s": rep.labels / (m["train_ms"] / 1e3),
                        "train_loss_first_last": [rep.losses[0][1], rep.losses[-1][1]] if rep.losses else None,
-                       "top_fraction_sweep": m["sweep"]}}
+                       "top_fraction_sweep": m["sweep"], "node_boxes": m["node_boxes"]}}
     print(json.dumps(line), flush=True)
     bad = (line["detail"]["mismatches"] or 0) + m["false_free"] + (m.get("false_free_oracle") or 0)
     if bad:
@@ -977,6 +989,16 @@ def run_narrow(args):
     train_steps = search.pretrain(warm_roots, args.narrow_train_labels)
     torch.cuda.synchronize(dev)
     train_s = time.perf_counter() - t0
+    # node boxes of both kernels, picked on crossing candidates of separate roots (the
+    # motions the searches validate, and their endpoints, which label the network)
+    from puzzletunneldiscovery_gb300.autotune import pick_node_boxes
+    R = warm_roots[: 1 << 18]
+    ends = N.expand(R, 64, 0.05 * s, 0.1, 12345)
+    ci = torch.nonzero(N.crossings(R, ends, 64, torch.from_numpy(np.ascontiguousarray(probes)).to(dev), 0.0,
+                                   extent)).flatten()[:65536]
+    boxes = pick_node_boxes(uw, states=ends.index_select(0, ci),
+                            segments=(R.index_select(0, ci // 64).contiguous(), ends.index_select(0, ci).contiguous()),
+                            verify_delta=DELTA, mode=1)
     # the plain arm gets its own world, so that the two searches' captured graphs
     # never invalidate each other's scratch
     uw_plain = pw.UnitWorld(local)
@@ -984,6 +1006,8 @@ def run_narrow(args):
     uw_plain.load_robot_mesh(Vr, Fr)
     uw_plain.scaleToUnit()
     uw_plain.angleModel(0.0, 0.0)
+    uw_plain.set_node_boxes(boxes["states"], 0)
+    uw_plain.set_node_boxes(boxes["segments"], 1)
     plain = N.NarrowPassageSearch(uw_plain, None, probes, 0.0, extent, per_root=64, sigma_t=0.05, sigma_rot=0.1,
                                   k=args.narrow_k, verify_delta=DELTA, seed=rank)
     for _ in range(args.warmup):
@@ -1057,6 +1081,7 @@ def run_narrow(args):
             "gpu_launches": 12 * sum(r.rounds for r in g_reps),
             "detail": {"mismatches": parity["mismatches"] if parity else None,
                        "mismatch_sample": parity["mismatch_sample"] if parity else 0, "parity": parity,
+                       "node_boxes": boxes,
                        "plain_escapes_per_s": plain_value, "guided_over_plain": value / max(plain_value, 1e-12),
                        "guided_yield": g_esc / max(1, sum(r.validated for r in g_reps)),
                        "plain_yield": p_esc / max(1, sum(r.validated for r in p_reps)),
@@ -1163,7 +1188,7 @@ class RowJob:
         if self.name == "disentangled":
             return uw.is_disentangled_states(self.a)
         if self.name == "contacts":
-            return [uw.intersecting_segments(q) for q in self.q]
+            return uw.intersecting_segments_batch(self.q)
         if self.name == "keyconf":
             rp, rn, ep, en = self.pairs
             return SP.enum_free_configurations(uw, rp, rn, ep, en, KEYCONF_MARGIN, KEYCONF_SPINS, only_median=True)
@@ -1244,6 +1269,22 @@ def run_rows(args):
     uw.angleModel(0.0, 0.0)
     job = RowJob(args.workload, uw, args.n, rank)
     stream = torch.cuda.current_stream(dev)
+    # the node boxes of the kernel the workload runs, picked on a sample of its own queries
+    from puzzletunneldiscovery_gb300 import sampling as SP
+    from puzzletunneldiscovery_gb300.autotune import pick_node_boxes
+    if args.workload == "keyconf":
+        rp, rn, ep, en = (x[:512] for x in job.pairs)
+        ang = np.broadcast_to(np.arange(KEYCONF_SPINS) * (2 * np.pi / KEYCONF_SPINS), (512, KEYCONF_SPINS))
+        pick_node_boxes(uw, states=torch.from_numpy(np.ascontiguousarray(
+            SP._touch_states(rp, rn, ep, en, KEYCONF_MARGIN, ang).reshape(-1, 7))).to(dev))
+    elif args.workload == "touch":
+        k = job.keys[:256]
+        r = np.random.default_rng(5)
+        frm = np.repeat(k, TOUCH_PER_KEY, axis=0)
+        to = SP.apply_rows(frm, SP.random_on_sphere(frm.shape[0], 1.0, r),
+                           SP.random_within_sphere(frm.shape[0], 2 * np.pi, r))
+        pick_node_boxes(uw, segments=(torch.from_numpy(frm).to(dev), torch.from_numpy(to).to(dev)),
+                        verify_delta=uw.recommended_cres)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     for _ in range(args.warmup):
         res = job.gpu()
@@ -1329,7 +1370,7 @@ def run_rows(args):
         cfg.update({"states": job.n, "states_drawn_from": "colliding uniform states in [-0.6, 0.6]^3 (world)"})
     detail = {"mismatches": parity["mismatches"] if parity else None,
               "mismatch_sample": parity["mismatch_sample"] if parity else 0, "parity": parity, "step_ms": step_ms,
-              "node_boxes": uw.get_node_boxes()}
+              "node_boxes": {"states": uw.get_node_boxes(0), "segments": uw.get_node_boxes(1)}}
     if args.workload == "contacts":
         detail["contact_rows_per_state"] = sum(r[3].shape[0] for r in res) / max(1, len(res))
     if args.workload == "keyconf":
@@ -1342,9 +1383,9 @@ def run_rows(args):
             "dtype": "f64 box test" if args.workload == "disentangled" else "f32 traversal + f64 state math/re-tests",
             "data": "synthetic (seeded)", "config": cfg, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "clocks": clk.summary(),
-            # per step: k_disentangled; contacts: collect + evaluate per state; keyconf: traversal + re-test;
+            # per step: k_disentangled; contacts: collect + evaluate per chunk of states; keyconf: traversal + re-test;
             # touch: the segment query's 7 kernels and the contact-state rebuild
-            "gpu_launches": {"disentangled": 1, "contacts": 2 * job.n, "keyconf": 2, "touch": 8}[args.workload]
+            "gpu_launches": {"disentangled": 1, "contacts": 2, "keyconf": 2, "touch": 8}[args.workload]
             * args.steps,
             "detail": detail}
     print(json.dumps(line), flush=True)

@@ -164,6 +164,15 @@ PW_API int pw_intersecting_segments(pw_world *w, const double q[7], int64_t capa
                              double *ends, double *mags, int32_t *face_pairs, int32_t *coplanar,
                              int64_t *count);
 
+/* host in, host out, synchronous: pw_intersecting_segments for n unit states at once
+ * (one warp per state on the device, instead of one call per state).  The rows of
+ * state i are rows offsets[i] .. offsets[i + 1] - 1 (offsets has n + 1 entries), each
+ * state's rows sorted by (env face, robot face); *total = rows of all states.
+ * Returns PW_ERR_CAPACITY (with offsets and *total set) when capacity < *total. */
+PW_API int pw_intersecting_segments_batch(pw_world *w, const double *q, int64_t n, int64_t capacity, double *begins,
+                                   double *ends, double *mags, int32_t *face_pairs, int32_t *coplanar,
+                                   int64_t *offsets, int64_t *total);
+
 /* Graph mode (on != 0): pw_segments_first_contact makes no host synchronisation
  * and no device allocation, so a caller can capture it into a CUDA graph and
  * replay it.  It then runs within the scratch sized by pw_segments_reserve or
@@ -189,13 +198,15 @@ PW_API int pw_segments_reserve(pw_world *w, int64_t n, int64_t total_chunks, int
 PW_API int pw_world_set_launch_config(pw_world *w, int kernel, int width, int soft_cap, int blocks);
 PW_API int pw_world_get_launch_config(pw_world *w, int kernel, int *width, int *soft_cap, int *blocks);
 
-/* The node boxes the traversal kernels test: PW_BOXES_ORIENTED (default) or
- * PW_BOXES_ALIGNED.  Both are built with every mesh; verdicts are identical,
- * only the number of box and triangle tests differs.  FCL's OBBRSS nodes
- * (cdmodel.cc:17-18) are oriented boxes; the LBVH here fits both kinds to the
- * same hierarchy.  Not allowed in graph mode (captured launches hold the kernel). */
-PW_API int pw_world_set_node_boxes(pw_world *w, int kind);
-PW_API int pw_world_get_node_boxes(pw_world *w, int *kind);
+/* The node boxes a traversal kernel tests (kernel 0 = states, 1 = segments, -1 =
+ * both): PW_BOXES_ORIENTED (default) or PW_BOXES_ALIGNED.  Both kinds are built
+ * with every mesh; verdicts are identical, only the number of box and triangle
+ * tests differs, and which is faster depends on the meshes and the workload (the
+ * autotuner picks per kernel).  FCL's OBBRSS nodes (cdmodel.cc:17-18) are
+ * oriented boxes; the LBVH here fits both kinds to the same hierarchy.  Not
+ * allowed in graph mode (captured launches hold the kernel). */
+PW_API int pw_world_set_node_boxes(pw_world *w, int kernel, int kind);
+PW_API int pw_world_get_node_boxes(pw_world *w, int kernel, int *kind);
 
 /* The result tuple of transit_state_to_with_contact (unit_world.cc:405-474) for n
  * segments, from the codes pw_segments_first_contact(PW_SEG_TRANSIT) wrote for

@@ -42,6 +42,7 @@ EXPORTS = (
     "pw_segments_reserve", "pw_world_set_launch_config",
     "pw_world_get_launch_config", "pw_expansion_crossings", "pw_world_scratch_epoch", "pw_expand_states",
     "pw_ompl_check_motions", "pw_ompl_motion_states", "pw_world_set_node_boxes", "pw_world_get_node_boxes",
+    "pw_intersecting_segments_batch",
     # include/pw_mlp.h
     "pw_mlp_create", "pw_mlp_destroy", "pw_mlp_num_params", "pw_mlp_get_params", "pw_mlp_set_params",
     "pw_mlp_get_grads", "pw_mlp_predict", "pw_mlp_gradients", "pw_mlp_train_step", "pw_mlp_predict_mma",
@@ -122,6 +123,7 @@ def load():
         "pw_states_disentangled": (ctypes.c_int, [vp, vp, i64, vp, vp]),
         "pw_segments_first_contact": (ctypes.c_int, [vp, vp, vp, i64, ctypes.c_double, ctypes.c_int, vp, vp]),
         "pw_intersecting_segments": (ctypes.c_int, [vp, dp, i64, dp, dp, dp, i32p, i32p, i64p]),
+        "pw_intersecting_segments_batch": (ctypes.c_int, [vp, dp, i64, i64, dp, dp, dp, i32p, i32p, i64p, i64p]),
         "pw_world_translate_to_unit": (ctypes.c_int, [vp, dp, i64, dp]),
         "pw_world_translate_from_unit": (ctypes.c_int, [vp, dp, i64, dp]),
         "pw_world_translate_ompl_to_unit": (ctypes.c_int, [vp, dp, i64, dp]),
@@ -144,8 +146,8 @@ def load():
         "pw_segments_reserve": (ctypes.c_int, [vp, i64, i64, i64]),
         "pw_world_set_launch_config": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
         "pw_world_get_launch_config": (ctypes.c_int, [vp, ctypes.c_int, i32p, i32p, i32p]),
-        "pw_world_set_node_boxes": (ctypes.c_int, [vp, ctypes.c_int]),
-        "pw_world_get_node_boxes": (ctypes.c_int, [vp, i32p]),
+        "pw_world_set_node_boxes": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
+        "pw_world_get_node_boxes": (ctypes.c_int, [vp, ctypes.c_int, i32p]),
         "pw_segments_contact_states": (ctypes.c_int, [vp, vp, vp, i64, ctypes.c_double, vp, vp, vp, vp, vp, vp,
                                                       vp]),
         "pw_mlp_create": (ctypes.c_int, [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_uint64]),

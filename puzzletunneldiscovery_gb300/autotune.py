@@ -2,7 +2,7 @@
 
 ``autotune`` times the persistent traversal kernels of one world on a sample of
 the caller's own workload: first the two kinds of BVH node box (axis-aligned or
-oriented, pw_world_set_node_boxes), then, under the faster one, a grid of
+oriented, pw_world_set_node_boxes, per kernel), then, under the faster one, a grid of
 launch configurations (queries a warp takes per grab, traversal stack soft cap
 -- the point where a warp narrows from breadth-first to depth-first -- and
 resident blocks per SM).  Every choice must return the same verdicts; the
@@ -52,29 +52,48 @@ class TuneReport:
     table: list = field(default_factory=list)     # (config, ms)
 
 
-def _tune_boxes(uw, run, reps, stream, what):
-    """Time `run` under both node-box kinds (default launch shape) and keep the
-    faster kind on the world; the two must give identical results.  Returns
-    (kind, {kind: ms}, the results)."""
+def _tune_boxes(uw, kernel, run, reps, stream, what):
+    """Time `run` under both node-box kinds of `kernel` (default launch shape) and
+    keep the faster kind; the two must give identical results.  Returns (kind,
+    {kind: ms}, the results)."""
     times, outs = {}, {}
     for kind in ("aligned", "oriented"):
-        uw.set_node_boxes(kind)
+        uw.set_node_boxes(kind, kernel)
         run()
         times[kind], outs[kind] = _time(run, reps, stream)
     if not torch.equal(outs["aligned"], outs["oriented"]):
         raise RuntimeError("the node-box kinds gave different %s" % what)
     kind = min(times, key=times.get)
-    uw.set_node_boxes(kind)
+    uw.set_node_boxes(kind, kernel)
     return kind, times, outs[kind]
+
+
+def pick_node_boxes(uw, states: torch.Tensor | None = None, segments=None, verify_delta: float = 0.001,
+                    mode: int = _lib.PW_SEG_TRANSIT, reps: int = 1) -> dict:
+    """Only the node-box kind of each kernel given a sample (states [N, 7], or
+    segments (q0, q1) stepped at verify_delta in `mode`): both kinds timed, the
+    faster kept.  Returns {"states": kind, "segments": kind, "ms": {...}} for the
+    kernels sampled."""
+    out = {"ms": {}}
+    if states is not None:
+        stream = torch.cuda.current_stream(states.device)
+        out["states"], out["ms"]["states"], _ = _tune_boxes(uw, 0, lambda: uw.is_valid_states(states), reps, stream,
+                                                             "verdicts")
+    if segments is not None:
+        q0, q1 = segments
+        stream = torch.cuda.current_stream(q0.device)
+        run = lambda: uw.first_contact_steps(q0, q1, verify_delta, mode)  # noqa: E731
+        out["segments"], out["ms"]["segments"], _ = _tune_boxes(uw, 1, run, reps, stream, "first-contact steps")
+    return out
 
 
 def tune_states(uw, q: torch.Tensor, widths=(8, 16, 32), soft_caps=(128, 256, 512, 0), blocks=(0, 2, 3),
                 reps: int = 2) -> TuneReport:
     """Pick the states-kernel configuration that answers `q` fastest: first the
-    node-box kind (a world-wide setting), then the launch shape under it."""
+    node-box kind, then the launch shape under it."""
     stream = torch.cuda.current_stream(q.device)
     uw.set_launch_config(0)
-    kind, box_ms, ref = _tune_boxes(uw, lambda: uw.is_valid_states(q), reps, stream, "verdicts")
+    kind, box_ms, ref = _tune_boxes(uw, 0, lambda: uw.is_valid_states(q), reps, stream, "verdicts")
     default_ms = box_ms[kind]
     table = []
     for w, c, b in itertools.product(widths, soft_caps, blocks):
@@ -97,11 +116,11 @@ def tune_states(uw, q: torch.Tensor, widths=(8, 16, 32), soft_caps=(128, 256, 51
 def tune_segments(uw, q0: torch.Tensor, q1: torch.Tensor, verify_delta: float, soft_caps=(128, 256, 512, 0),
                   blocks=(0, 2, 3), reps: int = 2, mode: int = _lib.PW_SEG_TRANSIT) -> TuneReport:
     """Pick the segments-kernel configuration that answers (q0, q1) fastest: first
-    the node-box kind (a world-wide setting), then the launch shape under it."""
+    the node-box kind, then the launch shape under it."""
     stream = torch.cuda.current_stream(q0.device)
     uw.set_launch_config(1)
     run = lambda: uw.first_contact_steps(q0, q1, verify_delta, mode)  # noqa: E731
-    kind, box_ms, ref = _tune_boxes(uw, run, reps, stream, "first-contact steps")
+    kind, box_ms, ref = _tune_boxes(uw, 1, run, reps, stream, "first-contact steps")
     default_ms = box_ms[kind]
     table = []
     for c, b in itertools.product(soft_caps, blocks):
@@ -175,7 +194,7 @@ def _world_key(uw, kernel: str) -> str:
 
 def _apply(uw, kernel: str, cfg: dict) -> None:
     if "boxes" in cfg:
-        uw.set_node_boxes(cfg["boxes"])
+        uw.set_node_boxes(cfg["boxes"], 0 if kernel == "states" else 1)
     if kernel == "states":
         uw.set_launch_config(0, cfg.get("width", 0), cfg.get("soft_cap", 0), cfg.get("blocks", 0))
     else:
@@ -186,9 +205,8 @@ def autotune(uw, states: torch.Tensor | None = None, segments=None, verify_delta
              cache: "TuneCache | str | bool | None" = None, **kw):
     """Tune both kernels on samples of the caller's workload; returns the reports.
 
-    The node-box kind (axis-aligned or oriented BVH boxes) is one setting per
-    world: when both kernels are tuned, the segments kernel's choice is the one
-    left on the world.
+    Each kernel gets its own node-box kind (axis-aligned or oriented BVH boxes)
+    and launch shape.
 
     With a cache (True for the default file, a path, or a TuneCache) a
     configuration already tuned for the same mesh pair on the same GPU model is

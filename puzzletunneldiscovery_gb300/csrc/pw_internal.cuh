@@ -127,7 +127,7 @@ struct pw_world {
 	int launch_soft_cap[2] = { 0, 0 };  // traversal stack soft cap
 	int launch_blocks[2] = { 0, 0 };    // resident blocks per SM of the persistent kernel
 	int grid_cache[4] = { 0, 0, 0, 0 }; // grid of the persistent kernels under that configuration, per box kind
-	int node_boxes = PW_BOXES_ORIENTED; // node boxes the traversals use (pw_world_set_node_boxes)
+	int node_boxes[2] = { PW_BOXES_ORIENTED, PW_BOXES_ORIENTED }; // per kernel (pw_world_set_node_boxes)
 	// the last segment query's inputs: its parameters and checkpoints stay in the
 	// scratch, so the transit tuples of the same batch can start from them
 	const double *last_seg_from = nullptr, *last_seg_to = nullptr;

@@ -1066,21 +1066,16 @@ __global__ void k_seg_finalize(int32_t *first, const SegParams *params, int64_t 
 
 constexpr int ISECT_CAP = 1 << 20;
 
-// One warp enumerates every leaf pair of state q that is not certified separate.
-__global__ void k_isect_collect(WorldDev W, const double *q, uint2 *cand, unsigned int *ncand, int soft_cap)
+// One warp enumerates every leaf pair of the state whose FP32 frame is in
+// sm.qf[0] that is not certified separate, calling emit(env face, robot face)
+// on the lanes that found one.
+template <typename Emit>
+__device__ void isect_traverse(const WorldDev &W, WarpSmem &sm, int lane, int soft_cap, Emit emit)
 {
-	extern __shared__ __align__(16) unsigned char smem_raw[];
-	const int lane = threadIdx.x & 31;
-	WarpSmem &sm = reinterpret_cast<WarpSmem *>(smem_raw)[0];
 	const uint32_t ebase = (uint32_t)W.env.leaf_base, rbase = (uint32_t)W.rob.leaf_base;
 	const unsigned gt_mask = ~(((1u << lane) - 1u) | (1u << lane));
-	if (lane == 0) {
-		double s[7];
-		for (int i = 0; i < 7; i++)
-			s[i] = q[i];
-		make_qf(s, W, sm.qf[0]);
+	if (lane == 0)
 		sm.stack[0] = make_uint2(0u, 0u);
-	}
 	__syncwarp();
 	const float4 Q0 = sm.qf[0].q[0], Q1 = sm.qf[0].q[1], Q2 = sm.qf[0].q[2], Q3 = sm.qf[0].q[3];
 	const float eg = sm.qf[0].q[4].x;
@@ -1111,11 +1106,8 @@ __global__ void k_isect_collect(WorldDev W, const double *q, uint2 *cand, unsign
 					             rc = __ldg(W.rob.triC + rs);
 					float gap;
 					const int r = tri_filter(f3(ta), f3(tb), f3(tc), f3(ra), f3(rb), f3(rc), Q0, Q1, Q2, Q3, eg, &gap);
-					if (r != 0) {
-						const unsigned idx = atomicAdd(ncand, 1u);
-						if (idx < ISECT_CAP)
-							cand[idx] = make_uint2((uint32_t)__float_as_int(ta.w), (uint32_t)__float_as_int(ra.w));
-					}
+					if (r != 0)
+						emit((uint32_t)__float_as_int(ta.w), (uint32_t)__float_as_int(ra.w));
 				} else {
 					const bool da = !la && (lb || (A1.x + A1.y + A1.z) >= (B1.x + B1.y + B1.z));
 					if (da) {
@@ -1136,6 +1128,71 @@ __global__ void k_isect_collect(WorldDev W, const double *q, uint2 *cand, unsign
 			sm.stack[o + 1] = c0;
 		}
 		top += 2 * __popc(pm);
+		__syncwarp();
+	}
+}
+
+// One warp enumerates every leaf pair of state q that is not certified separate.
+__global__ void k_isect_collect(WorldDev W, const double *q, uint2 *cand, unsigned int *ncand, int soft_cap)
+{
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	const int lane = threadIdx.x & 31;
+	WarpSmem &sm = reinterpret_cast<WarpSmem *>(smem_raw)[0];
+	if (lane == 0) {
+		double s[7];
+		for (int i = 0; i < 7; i++)
+			s[i] = q[i];
+		make_qf(s, W, sm.qf[0]);
+	}
+	__syncwarp();
+	isect_traverse(W, sm, lane, soft_cap, [&](uint32_t et, uint32_t rt) {
+		const unsigned idx = atomicAdd(ncand, 1u);
+		if (idx < ISECT_CAP)
+			cand[idx] = make_uint2(et, rt);
+	});
+}
+
+// Candidate pair of a batch: the state and the two original face ids.
+struct IsectCand {
+	uint32_t state, et, rt, pad;
+};
+
+// Persistent warps over a batch of states (one state per warp at a time); the
+// candidates of every state go to one buffer of `cap` entries.  *ncand counts
+// them all, so a caller sees an overflow as *ncand > cap.
+__global__ void __launch_bounds__(WARPS * 32) k_isect_collect_batch(WorldDev W, const double *states, int64_t n,
+                                                                    IsectCand *cand, unsigned long long *ncand,
+                                                                    unsigned long long cap, unsigned long long *work,
+                                                                    int soft_cap)
+{
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	WarpSmem &sm = reinterpret_cast<WarpSmem *>(smem_raw)[warp];
+	for (;;) {
+		unsigned long long i = 0;
+		if (lane == 0)
+			i = atomicAdd(work, 1ull);
+		i = __shfl_sync(FULL, i, 0);
+		if (i >= (unsigned long long)n)
+			break;
+		if (lane == 0) {
+			double s[7];
+			for (int k = 0; k < 7; k++)
+				s[k] = states[7 * i + k];
+			make_qf(s, W, sm.qf[0]);
+		}
+		__syncwarp();
+		isect_traverse(W, sm, lane, soft_cap, [&](uint32_t et, uint32_t rt) {
+			const unsigned long long idx = atomicAdd(ncand, 1ull);
+			if (idx < cap) {
+				IsectCand c;
+				c.state = (uint32_t)i;
+				c.et = et;
+				c.rt = rt;
+				c.pad = 0;
+				cand[idx] = c;
+			}
+		});
 		__syncwarp();
 	}
 }
@@ -1177,6 +1234,47 @@ __global__ void k_isect_eval(WorldDev W, const double *q, const uint2 *cand, con
 	}
 }
 
+struct IsectBatchRow {
+	double b[3], e[3], mag;
+	int32_t state, et, rt, cop;
+};
+
+// FP64 verdict of each candidate of a batch; hits get Moeller's segment at the
+// 1e-6 snap, with their state.
+__global__ void k_isect_eval_batch(WorldDev W, const double *states, const IsectCand *cand,
+                                   const unsigned long long *ncand, unsigned long long cap, IsectBatchRow *rows,
+                                   unsigned long long *nrows)
+{
+	const unsigned long long cnt = min(*ncand, cap);
+	for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < cnt;
+	     i += (unsigned long long)gridDim.x * blockDim.x) {
+		const IsectCand c = cand[i];
+		const double *q = states + 7 * (size_t)c.state;
+		double R[9], t[3], U[3][3];
+		pwm::state_transform(q, R, t);
+		for (int k = 0; k < 3; k++) {
+			const int vi = W.rob.F[3 * c.rt + k];
+			const double p[3] = { W.rob.V64[3 * vi], W.rob.V64[3 * vi + 1], W.rob.V64[3 * vi + 2] };
+			pwm::xform_point(R, t, p, U[k]);
+		}
+		const double *V0 = W.env.V64 + 3 * W.env.F[3 * c.et + 0];
+		const double *V1 = W.env.V64 + 3 * W.env.F[3 * c.et + 1];
+		const double *V2 = W.env.V64 + 3 * W.env.F[3 * c.et + 2];
+		if (!pwm::tri_tri(V0, V1, V2, U[0], U[1], U[2], 0.0))
+			continue;
+		IsectBatchRow r;
+		int cop = 0;
+		pwm::tri_tri_isect(V0, V1, V2, U[0], U[1], U[2], 1e-6, &cop, r.b, r.e);
+		const double dx = pwm::sub(r.e[0], r.b[0]), dy = pwm::sub(r.e[1], r.b[1]), dz = pwm::sub(r.e[2], r.b[2]);
+		r.mag = pwm::rt(pwm::add(pwm::add(pwm::mul(dx, dx), pwm::mul(dy, dy)), pwm::mul(dz, dz)));
+		r.state = (int32_t)c.state;
+		r.et = (int32_t)c.et;
+		r.rt = (int32_t)c.rt;
+		r.cop = cop;
+		rows[atomicAdd(nrows, 1ull)] = r;
+	}
+}
+
 // ------------------------------------------------------------------ host helpers
 
 size_t warp_smem_bytes() { return sizeof(WarpSmem); }
@@ -1210,7 +1308,7 @@ int ensure_query_scratch(pw_world *w)
 // Launch configuration of kernel 0 (states) / 1 (segments), as set by pw_world_set_launch_config.
 int launch_grid(pw_world *w, int kernel, const void *fn, size_t smem)
 {
-	const int slot = kernel + 2 * (w->node_boxes == PW_BOXES_ORIENTED ? 1 : 0);
+	const int slot = kernel + 2 * (w->node_boxes[kernel] == PW_BOXES_ORIENTED ? 1 : 0);
 	if (w->grid_cache[slot] > 0)
 		return w->grid_cache[slot];
 	int per_sm = 0;
@@ -1254,17 +1352,18 @@ int set_smem_attr(const void *kernel, size_t smem)
 template <uint64_t CAP>
 const void *states_kernel(const pw_world *w)
 {
-	return w->node_boxes == PW_BOXES_ORIENTED ? (const void *)k_states<CAP, true> : (const void *)k_states<CAP, false>;
+	return w->node_boxes[0] == PW_BOXES_ORIENTED ? (const void *)k_states<CAP, true>
+	                                              : (const void *)k_states<CAP, false>;
 }
 const void *segments_kernel(const pw_world *w)
 {
-	return w->node_boxes == PW_BOXES_ORIENTED ? (const void *)k_segments<true> : (const void *)k_segments<false>;
+	return w->node_boxes[1] == PW_BOXES_ORIENTED ? (const void *)k_segments<true> : (const void *)k_segments<false>;
 }
 template <uint64_t CAP>
 void launch_states(const pw_world *w, int grid, size_t smem, cudaStream_t st, const double *states, int64_t n,
                    uint8_t *valid, QueryCounters *ctr, RetestEntry *rq)
 {
-	if (w->node_boxes == PW_BOXES_ORIENTED)
+	if (w->node_boxes[0] == PW_BOXES_ORIENTED)
 		k_states<CAP, true><<<grid, WARPS * 32, smem, st>>>(w->dev, states, n, valid, ctr, rq, launch_soft_cap(w, 0),
 		                                                    launch_width(w, 0));
 	else
@@ -1458,7 +1557,7 @@ extern "C" int pw_segments_first_contact(pw_world *w, const double *from, const 
 	StateSrc src{ nullptr, from, to, params, ckpt, anchors };
 	if (!w->graph_mode && (rc = mark(w, 0, st)))
 		return rc;
-	if (w->node_boxes == PW_BOXES_ORIENTED)
+	if (w->node_boxes[1] == PW_BOXES_ORIENTED)
 		k_segments<true><<<grid, WARPS * 32, smem, st>>>(w->dev, src, vals2, round_off, round_off + round_cap + 1,
 		                                                 first_step, ctr, rq, launch_soft_cap(w, 1));
 	else
@@ -1721,6 +1820,101 @@ extern "C" int pw_intersecting_segments(pw_world *w, const double q[7], int64_t 
 	return PW_OK;
 }
 
+// Candidate pairs one batch call holds on the device (16 B each), and the
+// states it sends per chunk; a chunk whose candidates overflow is halved.
+constexpr unsigned long long ISECT_BATCH_CAP = 1ull << 21;
+constexpr int64_t ISECT_BATCH_CHUNK = 65536;
+
+extern "C" int pw_intersecting_segments_batch(pw_world *w, const double *q, int64_t n, int64_t capacity,
+                                              double *begins, double *ends, double *mags, int32_t *face_pairs,
+                                              int32_t *coplanar, int64_t *offsets, int64_t *total)
+{
+	PW_TRACE("pw_intersecting_segments_batch");
+	int rc = check_ready(w, "pw_intersecting_segments_batch");
+	if (rc)
+		return rc;
+	if (n < 0 || capacity < 0 || !offsets || !total || (n > 0 && !q) ||
+	    (capacity > 0 && (!begins || !ends || !mags || !face_pairs)))
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_intersecting_segments_batch: bad pointers or sizes");
+	if (n > (int64_t(1) << 31))
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_intersecting_segments_batch: at most 2^31 states per call");
+	*total = 0;
+	for (int64_t i = 0; i <= n; i++)
+		offsets[i] = 0;
+	if (n == 0 || w->dev.env.ntri == 0 || w->dev.rob.ntri == 0)
+		return PW_OK;
+	PW_CUDA(cudaSetDevice(w->device));
+	const int64_t chunk0 = std::min<int64_t>(n, ISECT_BATCH_CHUNK);
+	DeviceBuffer dq, dcand, drows, dctr;
+	PW_CUDA(dq.reserve(sizeof(double) * 7 * (size_t)chunk0));
+	PW_CUDA(dcand.reserve(sizeof(IsectCand) * ISECT_BATCH_CAP));
+	PW_CUDA(drows.reserve(sizeof(IsectBatchRow) * ISECT_BATCH_CAP));
+	PW_CUDA(dctr.reserve(sizeof(unsigned long long) * 3));
+	unsigned long long *ctr = (unsigned long long *)dctr.ptr;   // candidates, rows, work
+	const size_t smem = warp_smem_bytes() * WARPS;
+	if ((rc = set_smem_attr((const void *)k_isect_collect_batch, smem)))
+		return rc;
+	int per_sm = 0;
+	PW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_isect_collect_batch, WARPS * 32, smem));
+	const int grid = std::max(1, per_sm) * std::max(1, w->num_sms);
+	std::vector<IsectBatchRow> all, part;
+	int64_t chunk = chunk0;
+	for (int64_t s0 = 0; s0 < n;) {
+		const int64_t m = std::min(chunk, n - s0);
+		PW_CUDA(cudaMemcpy(dq.ptr, q + 7 * s0, sizeof(double) * 7 * (size_t)m, cudaMemcpyHostToDevice));
+		PW_CUDA(cudaMemset(ctr, 0, sizeof(unsigned long long) * 3));
+		k_isect_collect_batch<<<grid, WARPS * 32, smem>>>(w->dev, (const double *)dq.ptr, m, (IsectCand *)dcand.ptr,
+		                                                 ctr, ISECT_BATCH_CAP, ctr + 2, soft_cap_of(w));
+		PW_CUDA(cudaGetLastError());
+		unsigned long long c[2];
+		PW_CUDA(cudaMemcpy(c, ctr, sizeof(c), cudaMemcpyDeviceToHost));
+		if (c[0] > ISECT_BATCH_CAP) {
+			if (m == 1)
+				return pw_fail(PW_ERR_CAPACITY, "pw_intersecting_segments_batch: a state has more than 2^21 candidate pairs");
+			chunk = std::max<int64_t>(1, m / 2);
+			continue;
+		}
+		k_isect_eval_batch<<<w->num_sms * 4, 256>>>(w->dev, (const double *)dq.ptr, (const IsectCand *)dcand.ptr, ctr,
+		                                           ISECT_BATCH_CAP, (IsectBatchRow *)drows.ptr, ctr + 1);
+		PW_CUDA(cudaGetLastError());
+		PW_CUDA(cudaMemcpy(c, ctr, sizeof(c), cudaMemcpyDeviceToHost));
+		part.resize(c[1]);
+		if (c[1])
+			PW_CUDA(cudaMemcpy(part.data(), drows.ptr, sizeof(IsectBatchRow) * c[1], cudaMemcpyDeviceToHost));
+		for (IsectBatchRow &r : part) {
+			r.state += (int32_t)s0;
+			all.push_back(r);
+		}
+		s0 += m;
+	}
+	std::sort(all.begin(), all.end(), [](const IsectBatchRow &a, const IsectBatchRow &b) {
+		if (a.state != b.state)
+			return a.state < b.state;
+		return a.et != b.et ? a.et < b.et : a.rt < b.rt;
+	});
+	for (const IsectBatchRow &r : all)
+		offsets[r.state + 1]++;
+	for (int64_t i = 0; i < n; i++)
+		offsets[i + 1] += offsets[i];
+	*total = (int64_t)all.size();
+	const int64_t kept = std::min<int64_t>(capacity, *total);
+	for (int64_t i = 0; i < kept; i++) {
+		const IsectBatchRow &r = all[i];
+		for (int k = 0; k < 3; k++) {
+			begins[3 * i + k] = r.b[k];
+			ends[3 * i + k] = r.e[k];
+		}
+		mags[i] = r.mag;
+		face_pairs[2 * i] = r.et;
+		face_pairs[2 * i + 1] = r.rt;
+		if (coplanar)
+			coplanar[i] = r.cop;
+	}
+	if (capacity < *total)
+		return pw_fail(PW_ERR_CAPACITY, "pw_intersecting_segments_batch: capacity smaller than the row count");
+	return PW_OK;
+}
+
 extern "C" int pw_world_last_stats(pw_world *w, pw_query_stats *out)
 {
 	if (!w || !out)
@@ -1836,20 +2030,22 @@ extern "C" int pw_states_valid_noalloc(pw_world *w, const double *states, int64_
 	return PW_OK;
 }
 
-extern "C" int pw_world_set_node_boxes(pw_world *w, int kind)
+extern "C" int pw_world_set_node_boxes(pw_world *w, int kernel, int kind)
 {
-	if (!w || (kind != PW_BOXES_ALIGNED && kind != PW_BOXES_ORIENTED))
+	if (!w || kernel < -1 || kernel > 1 || (kind != PW_BOXES_ALIGNED && kind != PW_BOXES_ORIENTED))
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_set_node_boxes: bad argument");
 	if (w->graph_mode)
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_set_node_boxes: not in graph mode (captured launches hold the kernel)");
-	w->node_boxes = kind;
+	for (int k = 0; k < 2; k++)
+		if (kernel < 0 || kernel == k)
+			w->node_boxes[k] = kind;
 	return PW_OK;
 }
 
-extern "C" int pw_world_get_node_boxes(pw_world *w, int *kind)
+extern "C" int pw_world_get_node_boxes(pw_world *w, int kernel, int *kind)
 {
-	if (!w || !kind)
-		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_get_node_boxes: NULL argument");
-	*kind = w->node_boxes;
+	if (!w || !kind || kernel < 0 || kernel > 1)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_get_node_boxes: bad argument");
+	*kind = w->node_boxes[kernel];
 	return PW_OK;
 }

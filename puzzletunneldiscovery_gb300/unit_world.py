@@ -318,15 +318,15 @@ class UnitWorld:
                                                  ctypes.byref(b)), "get_launch_config")
         return {"width": w.value, "soft_cap": c.value, "blocks": b.value}
 
-    def set_node_boxes(self, kind: str) -> None:
-        """Node boxes of the traversals: "oriented" (default) or "aligned"; the
-        verdicts do not depend on it."""
+    def set_node_boxes(self, kind: str, kernel: int = -1) -> None:
+        """Node boxes a traversal kernel tests (0 = states, 1 = segments, -1 =
+        both): "oriented" (default) or "aligned"; the verdicts do not depend on it."""
         k = {"aligned": _lib.PW_BOXES_ALIGNED, "oriented": _lib.PW_BOXES_ORIENTED}[kind]
-        check(self._L.pw_world_set_node_boxes(self._h, k), "set_node_boxes")
+        check(self._L.pw_world_set_node_boxes(self._h, int(kernel), k), "set_node_boxes")
 
-    def get_node_boxes(self) -> str:
+    def get_node_boxes(self, kernel: int) -> str:
         k = ctypes.c_int32()
-        check(self._L.pw_world_get_node_boxes(self._h, ctypes.byref(k)), "get_node_boxes")
+        check(self._L.pw_world_get_node_boxes(self._h, int(kernel), ctypes.byref(k)), "get_node_boxes")
         return "oriented" if k.value == _lib.PW_BOXES_ORIENTED else "aligned"
 
     def last_stats(self) -> dict:
@@ -654,6 +654,32 @@ class UnitWorld:
             n = int(cnt.value)
             self._last_coplanar = c[:n].copy()
             return b[:n].copy(), e[:n].copy(), m[:n].copy(), p[:n].copy()
+
+    def intersecting_segments_batch(self, unitqs):
+        """intersecting_segments for many unit states in one call: a list of the
+        per-state tuples (begins, ends, lengths, face pairs), each as
+        intersecting_segments returns it."""
+        q = _states_np(unitqs)
+        n = q.shape[0]
+        offsets = np.zeros(n + 1, dtype=np.int64)
+        total = ctypes.c_int64(0)
+        cap = max(1024, 64 * n)
+        while True:
+            b = np.zeros((cap, 3))
+            e = np.zeros((cap, 3))
+            m = np.zeros(cap)
+            p = np.zeros((cap, 2), dtype=np.int32)
+            c = np.zeros(cap, dtype=np.int32)
+            rc = self._L.pw_intersecting_segments_batch(self._h, _dp(q), n, cap, _dp(b), _dp(e), _dp(m),
+                                                        p.ctypes.data_as(_lib.i32p), c.ctypes.data_as(_lib.i32p),
+                                                        offsets.ctypes.data_as(_lib.i64p), ctypes.byref(total))
+            if rc == _lib.PW_ERR_CAPACITY and total.value > cap:
+                cap = int(total.value)
+                continue
+            check(rc, "intersecting_segments_batch")
+            break
+        return [(b[o0:o1].copy(), e[o0:o1].copy(), m[o0:o1].copy(), p[o0:o1].copy())
+                for o0, o1 in zip(offsets[:-1], offsets[1:])]
 
     # contact forces (unit_world.cc:1015-1057) ---------------------------------
     def _face_normals(self, geo):

@@ -37,7 +37,7 @@ def plate(oracle_mod, built_lib):
 
 def test_default_is_oriented(tori):
     uw, _ = tori
-    assert uw.get_node_boxes() == "oriented"
+    assert uw.get_node_boxes(0) == "oriented" and uw.get_node_boxes(1) == "oriented"
 
 
 @pytest.mark.parametrize("kind", ["aligned", "oriented"])
@@ -98,4 +98,19 @@ def test_node_boxes_refused_in_graph_mode(tori):
             uw.set_node_boxes("aligned")
     finally:
         uw.set_graph_mode(False)
-    assert uw.get_node_boxes() == "oriented"
+    assert uw.get_node_boxes(0) == "oriented"
+
+
+def test_node_boxes_per_kernel(tori):
+    """Each kernel keeps its own kind: states aligned while segments stay oriented."""
+    uw, ow = tori
+    uw.set_node_boxes("aligned", 0)
+    try:
+        assert uw.get_node_boxes(0) == "aligned" and uw.get_node_boxes(1) == "oriented"
+        q = W.uniform_states(5000, -2.0, 2.0, ow.scene_scale, seed=45)
+        assert (uw.is_valid_states(torch.from_numpy(q)).cpu().numpy() == ow.is_valid(q)).all()
+        q0, q1 = W.segment_batch(300, -2.0, 2.0, ow.scene_scale, seed=46)
+        e, _ = ow.segments_first_contact(q0, q1, 0.001)
+        assert (uw.first_contact_steps(torch.from_numpy(q0), torch.from_numpy(q1), 0.001).cpu().numpy() == e).all()
+    finally:
+        uw.set_node_boxes("oriented")

@@ -91,7 +91,8 @@ def test_autotune_keeps_verdicts(built_lib, oracle_mod):
     rep = autotune(uw, states=q, segments=(a, b), verify_delta=0.001, soft_caps=(128, 0), blocks=(0, 2), reps=1)
     # the launch grid plus the two node-box kinds, timed first
     assert len(rep["states"].table) == 3 * 2 * 2 + 2 and len(rep["segments"].table) == 2 * 2 + 2
-    assert rep["segments"].best["boxes"] == uw.get_node_boxes()
+    assert rep["segments"].best["boxes"] == uw.get_node_boxes(1)
+    assert rep["states"].best["boxes"] == uw.get_node_boxes(0)
     assert torch.equal(uw.is_valid_states(q), before_v)
     assert torch.equal(uw.first_contact_steps(a, b, 0.001), before_s)
     cfg = uw.get_launch_config(0)
@@ -118,7 +119,7 @@ def test_autotune_cache_reapplies_a_tuned_configuration(built_lib, tmp_path):
     again = autotune(second_world, states=q, cache=path, soft_caps=(128, 0), blocks=(0, 2), reps=1)["states"]
     assert again.table == [] and again.best == first.best
     assert second_world.get_launch_config(0) == applied
-    assert second_world.get_node_boxes() == first.best["boxes"]
+    assert second_world.get_node_boxes(0) == first.best["boxes"]
     assert torch.equal(second_world.is_valid_states(q), uw.is_valid_states(q))
     Ve, Fe, Vr, Fr = W.interlocking_tori(1.0, 0.25, 48, 24)
     other = pw.UnitWorld(0)
