@@ -1626,6 +1626,7 @@ def run_profile_case(args):
         a, b = torch.from_numpy(q0).to(dev), torch.from_numpy(q1).to(dev)
         uw.transit_states_to_with_contact(a, b, DELTA)
         uw.intersecting_segments(np.array([0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0]))
+        uw.intersecting_segments_batch(W.uniform_states(4096, -0.6, 0.6, s, seed=1))
         ends = N.expand(q[:1000], 64, 0.01, 0.1, 5)
         N.crossings(q[:1000], ends, 64, torch.zeros((4, 3), dtype=torch.float64, device=dev), 0.0, 0.5)
         net = S.Surrogate(0, 1)
