@@ -1155,6 +1155,7 @@ class RowJob:
     def __init__(self, name, uw, n, seed):
         import torch
         self.name, self.uw, self.n = name, uw, n
+        self.launches = 0   # kernels the library reports for the contact enumerations made
         s = uw.scene_scale
         rng = np.random.default_rng(3000 + seed)
         self.dev = uw._device
@@ -1188,7 +1189,9 @@ class RowJob:
         if self.name == "disentangled":
             return uw.is_disentangled_states(self.a)
         if self.name == "contacts":
-            return uw.intersecting_segments_batch(self.q)
+            res = uw.intersecting_segments_batch(self.q, flat=True)
+            self.launches += uw.last_stats()["work_items"]
+            return res
         if self.name == "keyconf":
             rp, rn, ep, en = self.pairs
             return SP.enum_free_configurations(uw, rp, rn, ep, en, KEYCONF_MARGIN, KEYCONF_SPINS, only_median=True)
@@ -1228,7 +1231,9 @@ class RowJob:
             return int((gpu_res[:m].cpu().numpy() != cpu_res).sum())
         if self.name == "contacts":
             bad = 0
-            for (b, e, mg, p), (b2, e2, mg2, p2, _) in zip(gpu_res[:m], cpu_res):
+            b, e, mg, p, off = gpu_res
+            rows = [(b[o0:o1], e[o0:o1], mg[o0:o1], p[o0:o1]) for o0, o1 in zip(off[:m], off[1:m + 1])]
+            for (b, e, mg, p), (b2, e2, mg2, p2, _) in zip(rows, cpu_res):
                 same = p.shape == p2.shape and (p == p2).all() and (b == b2).all() and (e == e2).all() \
                     and (mg == mg2).all()
                 bad += 0 if same else 1
@@ -1290,6 +1295,7 @@ def run_rows(args):
         res = job.gpu()
     torch.cuda.synchronize(dev)
     step_ms = []
+    job.launches = 0
     with ClockSampler(local) as clk:
         for i in range(args.steps):
             flush.zero_()
@@ -1308,6 +1314,7 @@ def run_rows(args):
                 step_ms.append(1e3 * (time.perf_counter() - t0))
     ms = sum(step_ms) / len(step_ms)
     value = job.units / (ms / 1e3)
+    job.timed_launches = job.launches
     # end to end: host inputs in, host results out, inside the timed region
     if job.device_timed:
         hq = torch.from_numpy(job.q).pin_memory()
@@ -1372,7 +1379,7 @@ def run_rows(args):
               "mismatch_sample": parity["mismatch_sample"] if parity else 0, "parity": parity, "step_ms": step_ms,
               "node_boxes": {"states": uw.get_node_boxes(0), "segments": uw.get_node_boxes(1)}}
     if args.workload == "contacts":
-        detail["contact_rows_per_state"] = sum(r[3].shape[0] for r in res) / max(1, len(res))
+        detail["contact_rows_per_state"] = float(res[4][-1]) / max(1, job.n)
     if args.workload == "keyconf":
         detail["key_configurations_per_step"] = sum(r.shape[0] for r in res)
     if args.workload == "touch":
@@ -1383,10 +1390,11 @@ def run_rows(args):
             "dtype": "f64 box test" if args.workload == "disentangled" else "f32 traversal + f64 state math/re-tests",
             "data": "synthetic (seeded)", "config": cfg, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "clocks": clk.summary(),
-            # per step: k_disentangled; contacts: collect + evaluate per chunk of states; keyconf: traversal + re-test;
-            # touch: the segment query's 7 kernels and the contact-state rebuild
-            "gpu_launches": {"disentangled": 1, "contacts": 2, "keyconf": 2, "touch": 8}[args.workload]
-            * args.steps,
+            # per step: k_disentangled; contacts: collect, evaluate, sort keys and gather per chunk of states
+            # (counted by the library); keyconf: traversal + re-test; touch: the segment query's 7 kernels and
+            # the contact-state rebuild
+            "gpu_launches": job.timed_launches if args.workload == "contacts" else
+            {"disentangled": 1, "keyconf": 2, "touch": 8}[args.workload] * args.steps,
             "detail": detail}
     print(json.dumps(line), flush=True)
     if parity and parity["mismatches"]:
@@ -1404,7 +1412,7 @@ def _row_h2d(job):
 
 def _row_d2h(job, res):
     if job.name == "contacts":
-        return int(sum(r[0].nbytes + r[1].nbytes + r[2].nbytes + r[3].nbytes for r in res))
+        return int(sum(x.nbytes for x in res[:4]) + res[3].shape[0] * 4 + res[4].nbytes)
     if job.name == "keyconf":
         return int(job.n * KEYCONF_SPINS)
     return int(job.units * (2 * 56 + 1 + 8))

@@ -73,6 +73,9 @@ typedef struct pw_world_info {
 	int32_t device;
 } pw_world_info;
 
+/* After a contact enumeration (pw_intersecting_segments, _batch): queries = states,
+ * retests = candidate triangle pairs tested in FP64, retest_hits = rows,
+ * work_items = kernels of this library launched, reference_checks = states. */
 typedef struct pw_query_stats {
 	int64_t queries;             /* states or (segment, step) pairs examined */
 	int64_t node_tests;          /* BVH node-pair box tests */
@@ -165,10 +168,11 @@ PW_API int pw_intersecting_segments(pw_world *w, const double q[7], int64_t capa
                              int64_t *count);
 
 /* host in, host out, synchronous: pw_intersecting_segments for n unit states at once
- * (one warp per state on the device, instead of one call per state).  The rows of
+ * (one warp per state on the device, rows sorted on the device).  The rows of
  * state i are rows offsets[i] .. offsets[i + 1] - 1 (offsets has n + 1 entries), each
  * state's rows sorted by (env face, robot face); *total = rows of all states.
- * Returns PW_ERR_CAPACITY (with offsets and *total set) when capacity < *total. */
+ * Returns PW_ERR_CAPACITY (with offsets and *total set, rows not all written) when
+ * capacity < *total. */
 PW_API int pw_intersecting_segments_batch(pw_world *w, const double *q, int64_t n, int64_t capacity, double *begins,
                                    double *ends, double *mags, int32_t *face_pairs, int32_t *coplanar,
                                    int64_t *offsets, int64_t *total);

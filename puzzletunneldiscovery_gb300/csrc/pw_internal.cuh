@@ -110,6 +110,7 @@ struct pw_world {
 	DeviceBuffer retest;       // RetestEntry[retest_cap]
 	uint64_t retest_cap = 0;
 	DeviceBuffer seg_params, seg_ckpt, seg_anchor, seg_keys, seg_order, seg_keys2, seg_order2, round_off, cub_tmp, misc;
+	DeviceBuffer isect;        // contact enumeration (candidates, rows, sort keys, output columns)
 	cudaStream_t last_stream = nullptr;
 	cudaEvent_t ev[4] = { nullptr, nullptr, nullptr, nullptr }; // traversal start/end, re-test start/end
 	bool timed = false;

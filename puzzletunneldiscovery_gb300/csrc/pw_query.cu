@@ -1064,8 +1064,6 @@ __global__ void k_seg_finalize(int32_t *first, const SegParams *params, int64_t 
 
 // ------------------------------------------------------------------ intersecting segments
 
-constexpr int ISECT_CAP = 1 << 20;
-
 // One warp enumerates every leaf pair of the state whose FP32 frame is in
 // sm.qf[0] that is not certified separate, calling emit(env face, robot face)
 // on the lanes that found one.
@@ -1132,26 +1130,6 @@ __device__ void isect_traverse(const WorldDev &W, WarpSmem &sm, int lane, int so
 	}
 }
 
-// One warp enumerates every leaf pair of state q that is not certified separate.
-__global__ void k_isect_collect(WorldDev W, const double *q, uint2 *cand, unsigned int *ncand, int soft_cap)
-{
-	extern __shared__ __align__(16) unsigned char smem_raw[];
-	const int lane = threadIdx.x & 31;
-	WarpSmem &sm = reinterpret_cast<WarpSmem *>(smem_raw)[0];
-	if (lane == 0) {
-		double s[7];
-		for (int i = 0; i < 7; i++)
-			s[i] = q[i];
-		make_qf(s, W, sm.qf[0]);
-	}
-	__syncwarp();
-	isect_traverse(W, sm, lane, soft_cap, [&](uint32_t et, uint32_t rt) {
-		const unsigned idx = atomicAdd(ncand, 1u);
-		if (idx < ISECT_CAP)
-			cand[idx] = make_uint2(et, rt);
-	});
-}
-
 // Candidate pair of a batch: the state and the two original face ids.
 struct IsectCand {
 	uint32_t state, et, rt, pad;
@@ -1197,53 +1175,16 @@ __global__ void __launch_bounds__(WARPS * 32) k_isect_collect_batch(WorldDev W, 
 	}
 }
 
-struct IsectRow {
-	double b[3], e[3], mag;
-	int32_t et, rt, cop, pad;
-};
-
-// FP64 verdict of each candidate; hits get Moeller's segment at the 1e-6 snap.
-__global__ void k_isect_eval(WorldDev W, const double *q, const uint2 *cand, const unsigned int *ncand,
-                             IsectRow *rows, unsigned int *nrows)
-{
-	const unsigned cnt = min(*ncand, (unsigned)ISECT_CAP);
-	for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
-		const uint32_t et = cand[i].x, rt = cand[i].y;
-		double R[9], t[3], U[3][3];
-		pwm::state_transform(q, R, t);
-		for (int k = 0; k < 3; k++) {
-			const int vi = W.rob.F[3 * rt + k];
-			const double p[3] = { W.rob.V64[3 * vi], W.rob.V64[3 * vi + 1], W.rob.V64[3 * vi + 2] };
-			pwm::xform_point(R, t, p, U[k]);
-		}
-		const double *V0 = W.env.V64 + 3 * W.env.F[3 * et + 0];
-		const double *V1 = W.env.V64 + 3 * W.env.F[3 * et + 1];
-		const double *V2 = W.env.V64 + 3 * W.env.F[3 * et + 2];
-		if (!pwm::tri_tri(V0, V1, V2, U[0], U[1], U[2], 0.0))
-			continue;
-		IsectRow r;
-		int cop = 0;
-		pwm::tri_tri_isect(V0, V1, V2, U[0], U[1], U[2], 1e-6, &cop, r.b, r.e);
-		const double dx = pwm::sub(r.e[0], r.b[0]), dy = pwm::sub(r.e[1], r.b[1]), dz = pwm::sub(r.e[2], r.b[2]);
-		r.mag = pwm::rt(pwm::add(pwm::add(pwm::mul(dx, dx), pwm::mul(dy, dy)), pwm::mul(dz, dz)));
-		r.et = (int32_t)et;
-		r.rt = (int32_t)rt;
-		r.cop = cop;
-		r.pad = 0;
-		rows[atomicAdd(nrows, 1u)] = r;
-	}
-}
-
 struct IsectBatchRow {
 	double b[3], e[3], mag;
 	int32_t state, et, rt, cop;
 };
 
 // FP64 verdict of each candidate of a batch; hits get Moeller's segment at the
-// 1e-6 snap, with their state.
+// 1e-6 snap, with their state, and count one row of that state.
 __global__ void k_isect_eval_batch(WorldDev W, const double *states, const IsectCand *cand,
                                    const unsigned long long *ncand, unsigned long long cap, IsectBatchRow *rows,
-                                   unsigned long long *nrows)
+                                   unsigned long long *nrows, uint32_t *state_rows)
 {
 	const unsigned long long cnt = min(*ncand, cap);
 	for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < cnt;
@@ -1272,6 +1213,55 @@ __global__ void k_isect_eval_batch(WorldDev W, const double *states, const Isect
 		r.rt = (int32_t)c.rt;
 		r.cop = cop;
 		rows[atomicAdd(nrows, 1ull)] = r;
+		atomicAdd(state_rows + c.state, 1u);
+	}
+}
+
+// Sort keys of the rows: (state, env face, robot face) packed into `bits`
+// (state above env above robot face; be + br bits for the faces), or, when
+// state_bits is 0, only the two faces.
+__global__ void k_isect_keys(const IsectBatchRow *rows, const unsigned long long *nrows, int state_bits, int be,
+                             int br, uint64_t *key, uint32_t *idx)
+{
+	const unsigned long long n = *nrows;
+	for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+	     i += (unsigned long long)gridDim.x * blockDim.x) {
+		const IsectBatchRow &r = rows[i];
+		uint64_t k = ((uint64_t)(uint32_t)r.et << br) | (uint64_t)(uint32_t)r.rt;
+		if (state_bits)
+			k |= (uint64_t)(uint32_t)r.state << (be + br);
+		key[i] = k;
+		idx[i] = (uint32_t)i;
+	}
+}
+
+// The state of each row in the order of a face sort (second pass of a
+// two-pass sort when the packed key does not fit 64 bits).
+__global__ void k_isect_state_keys(const IsectBatchRow *rows, const unsigned long long *nrows, const uint32_t *idx,
+                                   uint32_t *key)
+{
+	const unsigned long long n = *nrows;
+	for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+	     i += (unsigned long long)gridDim.x * blockDim.x)
+		key[i] = (uint32_t)rows[idx[i]].state;
+}
+
+// Rows in sorted order, split into the caller's arrays.
+__global__ void k_isect_gather(const IsectBatchRow *rows, const uint32_t *idx, const unsigned long long *nrows,
+                               double *b, double *e, double *mag, int32_t *fp, int32_t *cop)
+{
+	const unsigned long long n = *nrows;
+	for (unsigned long long j = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; j < n;
+	     j += (unsigned long long)gridDim.x * blockDim.x) {
+		const IsectBatchRow &r = rows[idx[j]];
+		for (int k = 0; k < 3; k++) {
+			b[3 * j + k] = r.b[k];
+			e[3 * j + k] = r.e[k];
+		}
+		mag[j] = r.mag;
+		fp[2 * j] = r.et;
+		fp[2 * j + 1] = r.rt;
+		cop[j] = r.cop;
 	}
 }
 
@@ -1762,6 +1752,199 @@ extern "C" int pw_world_get_launch_config(pw_world *w, int kernel, int *width, i
 	return PW_OK;
 }
 
+// Candidate pairs one chunk of a contact enumeration holds on the device, and
+// the most states of one chunk.  The chunk's state count follows the
+// candidates per state seen so far; a chunk whose candidates overflow is
+// re-run with fewer states.
+constexpr unsigned long long ISECT_BATCH_CAP = 1ull << 22;
+constexpr int64_t ISECT_BATCH_CHUNK = 65536;
+
+// The world's contact-enumeration scratch, carved from one buffer.
+struct IsectScratch {
+	double *q;                 // ISECT_BATCH_CHUNK states
+	unsigned long long *ctr;   // candidates, rows, work
+	uint32_t *state_rows;      // rows per state of the chunk
+	int64_t *row_end;          // inclusive scan of state_rows
+	IsectCand *cand;
+	IsectBatchRow *rows;
+	uint64_t *key[2];
+	uint32_t *idx[2];
+	double *b, *e, *mag;
+	int32_t *fp, *cop;
+	void *tmp;
+	size_t tmp_bytes;
+};
+
+static int isect_scratch(pw_world *w, IsectScratch &S)
+{
+	const size_t C = ISECT_BATCH_CAP, M = ISECT_BATCH_CHUNK;
+	size_t t1 = 0, t2 = 0, t3 = 0;
+	PW_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, t1, (uint64_t *)nullptr, (uint64_t *)nullptr,
+	                                        (uint32_t *)nullptr, (uint32_t *)nullptr, (int)C, 0, 64));
+	PW_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, t2, (uint32_t *)nullptr, (uint32_t *)nullptr,
+	                                        (uint32_t *)nullptr, (uint32_t *)nullptr, (int)C, 0, 32));
+	PW_CUDA(cub::DeviceScan::InclusiveSum(nullptr, t3, (const uint32_t *)nullptr, (int64_t *)nullptr, (int)M));
+	S.tmp_bytes = std::max(t1, std::max(t2, t3));
+	const size_t sizes[] = { sizeof(double) * 7 * M, sizeof(unsigned long long) * 4, sizeof(uint32_t) * M,
+		                     sizeof(int64_t) * M, sizeof(IsectCand) * C, sizeof(IsectBatchRow) * C,
+		                     sizeof(uint64_t) * C, sizeof(uint64_t) * C, sizeof(uint32_t) * C, sizeof(uint32_t) * C,
+		                     sizeof(double) * 3 * C, sizeof(double) * 3 * C, sizeof(double) * C,
+		                     sizeof(int32_t) * 2 * C, sizeof(int32_t) * C, S.tmp_bytes };
+	constexpr int NS = sizeof(sizes) / sizeof(sizes[0]);
+	size_t off[NS], total = 0;
+	for (int i = 0; i < NS; i++) {
+		off[i] = total;
+		total += (sizes[i] + 255) & ~(size_t)255;
+	}
+	PW_CUDA(w->isect.reserve(total));
+	uint8_t *p = (uint8_t *)w->isect.ptr;
+	S.q = (double *)(p + off[0]);
+	S.ctr = (unsigned long long *)(p + off[1]);
+	S.state_rows = (uint32_t *)(p + off[2]);
+	S.row_end = (int64_t *)(p + off[3]);
+	S.cand = (IsectCand *)(p + off[4]);
+	S.rows = (IsectBatchRow *)(p + off[5]);
+	S.key[0] = (uint64_t *)(p + off[6]);
+	S.key[1] = (uint64_t *)(p + off[7]);
+	S.idx[0] = (uint32_t *)(p + off[8]);
+	S.idx[1] = (uint32_t *)(p + off[9]);
+	S.b = (double *)(p + off[10]);
+	S.e = (double *)(p + off[11]);
+	S.mag = (double *)(p + off[12]);
+	S.fp = (int32_t *)(p + off[13]);
+	S.cop = (int32_t *)(p + off[14]);
+	S.tmp = p + off[15];
+	return PW_OK;
+}
+
+static int bits_for(int64_t count) // bits of the largest index below count
+{
+	int b = 1;
+	while (b < 63 && (int64_t(1) << b) < count)
+		b++;
+	return b;
+}
+
+// Contact enumeration of n states (host arrays): rows of state i at
+// offsets[i] .. offsets[i + 1] - 1, sorted by (env face, robot face); rows past
+// `capacity` are not written.  who names the entry point in errors.
+static int isect_run(pw_world *w, const double *q, int64_t n, int64_t capacity, double *begins, double *ends,
+                     double *mags, int32_t *face_pairs, int32_t *coplanar, int64_t *offsets, int64_t *total,
+                     const char *who)
+{
+	*total = 0;
+	for (int64_t i = 0; i <= n; i++)
+		offsets[i] = 0;
+	if (n == 0 || w->dev.env.ntri == 0 || w->dev.rob.ntri == 0)
+		return PW_OK;
+	PW_CUDA(cudaSetDevice(w->device));
+	IsectScratch S;
+	int rc = isect_scratch(w, S);
+	if (rc)
+		return rc;
+	const size_t smem = warp_smem_bytes() * WARPS;
+	if ((rc = set_smem_attr((const void *)k_isect_collect_batch, smem)))
+		return rc;
+	int per_sm = 0;
+	PW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_isect_collect_batch, WARPS * 32, smem));
+	const int grid = std::max(1, per_sm) * std::max(1, w->num_sms);
+	const int egrid = std::max(1, w->num_sms) * 8;
+	const int be = bits_for(w->dev.env.ntri), br = bits_for(w->dev.rob.ntri);
+	std::vector<int64_t> ends_h;
+	int64_t chunk = std::min<int64_t>(n, ISECT_BATCH_CHUNK), base = 0;
+	unsigned long long launches = 0, tested = 0;
+	for (int64_t s0 = 0; s0 < n;) {
+		const int64_t m = std::min(chunk, n - s0);
+		PW_CUDA(cudaMemcpy(S.q, q + 7 * s0, sizeof(double) * 7 * (size_t)m, cudaMemcpyHostToDevice));
+		PW_CUDA(cudaMemset(S.ctr, 0, sizeof(unsigned long long) * 3));
+		PW_CUDA(cudaMemset(S.state_rows, 0, sizeof(uint32_t) * (size_t)m));
+		k_isect_collect_batch<<<grid, WARPS * 32, smem>>>(w->dev, S.q, m, S.cand, S.ctr, ISECT_BATCH_CAP, S.ctr + 2,
+		                                                 soft_cap_of(w));
+		PW_CUDA(cudaGetLastError());
+		launches++;
+		unsigned long long c[2];
+		PW_CUDA(cudaMemcpy(c, S.ctr, sizeof(c), cudaMemcpyDeviceToHost));
+		if (c[0] > ISECT_BATCH_CAP) {
+			if (m == 1)
+				return pw_fail(PW_ERR_CAPACITY, std::string(who) + ": a state has more than 2^22 candidate pairs");
+			chunk = std::max<int64_t>(1, std::min<int64_t>(m / 2, (int64_t)((double)m * 0.8 * ISECT_BATCH_CAP / c[0])));
+			continue;
+		}
+		k_isect_eval_batch<<<egrid, 256>>>(w->dev, S.q, S.cand, S.ctr, ISECT_BATCH_CAP, S.rows, S.ctr + 1,
+		                                   S.state_rows);
+		PW_CUDA(cudaGetLastError());
+		launches++;
+		tested += c[0];
+		PW_CUDA(cudaMemcpy(c, S.ctr, sizeof(c), cudaMemcpyDeviceToHost));
+		const int64_t nr = (int64_t)c[1];
+		size_t tb = S.tmp_bytes;
+		PW_CUDA(cub::DeviceScan::InclusiveSum(S.tmp, tb, (const uint32_t *)S.state_rows, S.row_end, (int)m));
+		ends_h.resize((size_t)m);
+		PW_CUDA(cudaMemcpy(ends_h.data(), S.row_end, sizeof(int64_t) * (size_t)m, cudaMemcpyDeviceToHost));
+		if (ends_h[(size_t)m - 1] != nr)
+			return pw_fail(PW_ERR_INTERNAL, std::string(who) + ": row counts disagree");
+		for (int64_t i = 0; i < m; i++)
+			offsets[s0 + i + 1] = base + ends_h[(size_t)i];
+		if (nr > 0 && base + nr <= capacity) {
+			const int sb = bits_for(m);
+			const uint32_t *order;
+			k_isect_keys<<<egrid, 256>>>(S.rows, S.ctr + 1, sb + be + br <= 64 ? sb : 0, be, br, S.key[0],
+			                             S.idx[0]);
+			PW_CUDA(cudaGetLastError());
+			tb = S.tmp_bytes;
+			if (sb + be + br <= 64) {
+				PW_CUDA(cub::DeviceRadixSort::SortPairs(S.tmp, tb, S.key[0], S.key[1], S.idx[0], S.idx[1], (int)nr, 0,
+				                                        sb + be + br));
+				order = S.idx[1];
+			} else {
+				// faces first, then a stable sort by state
+				PW_CUDA(cub::DeviceRadixSort::SortPairs(S.tmp, tb, S.key[0], S.key[1], S.idx[0], S.idx[1], (int)nr, 0,
+				                                        be + br));
+				uint32_t *k32a = (uint32_t *)S.key[0], *k32b = (uint32_t *)S.key[1];
+				k_isect_state_keys<<<egrid, 256>>>(S.rows, S.ctr + 1, S.idx[1], k32a);
+				PW_CUDA(cudaGetLastError());
+				tb = S.tmp_bytes;
+				PW_CUDA(cub::DeviceRadixSort::SortPairs(S.tmp, tb, k32a, k32b, S.idx[1], S.idx[0], (int)nr, 0, sb));
+				order = S.idx[0];
+				launches++;
+			}
+			k_isect_gather<<<egrid, 256>>>(S.rows, order, S.ctr + 1, S.b, S.e, S.mag, S.fp, S.cop);
+			PW_CUDA(cudaGetLastError());
+			launches += 2;
+			PW_CUDA(cudaMemcpy(begins + 3 * base, S.b, sizeof(double) * 3 * (size_t)nr, cudaMemcpyDeviceToHost));
+			PW_CUDA(cudaMemcpy(ends + 3 * base, S.e, sizeof(double) * 3 * (size_t)nr, cudaMemcpyDeviceToHost));
+			PW_CUDA(cudaMemcpy(mags + base, S.mag, sizeof(double) * (size_t)nr, cudaMemcpyDeviceToHost));
+			PW_CUDA(cudaMemcpy(face_pairs + 2 * base, S.fp, sizeof(int32_t) * 2 * (size_t)nr, cudaMemcpyDeviceToHost));
+			if (coplanar)
+				PW_CUDA(cudaMemcpy(coplanar + base, S.cop, sizeof(int32_t) * (size_t)nr, cudaMemcpyDeviceToHost));
+		}
+		base += nr;
+		s0 += m;
+		if (c[0] > 0)
+			chunk = std::max<int64_t>(1, std::min<int64_t>(ISECT_BATCH_CHUNK,
+			                                               (int64_t)((double)m * 0.8 * ISECT_BATCH_CAP / c[0])));
+		else
+			chunk = ISECT_BATCH_CHUNK;
+	}
+	*total = base;
+	// the figures pw_world_last_stats reports for this query
+	if ((rc = ensure_query_scratch(w)))
+		return rc;
+	QueryCounters hc;
+	memset(&hc, 0, sizeof(hc));
+	hc.stat[STAT_QUERIES] = (unsigned long long)n;
+	hc.stat[STAT_RETESTS] = tested;
+	hc.stat[STAT_RETEST_HITS] = (unsigned long long)base;
+	hc.stat[STAT_ITEMS] = launches;
+	PW_CUDA(cudaMemcpy(w->counters.ptr, &hc, sizeof(hc), cudaMemcpyHostToDevice));
+	w->last_states = n;
+	w->last_stream = nullptr;
+	w->timed = false;
+	if (capacity < base)
+		return pw_fail(PW_ERR_CAPACITY, std::string(who) + ": capacity smaller than the row count");
+	return PW_OK;
+}
+
 extern "C" int pw_intersecting_segments(pw_world *w, const double q[7], int64_t capacity, double *begins,
                                         double *ends, double *mags, int32_t *face_pairs, int32_t *coplanar,
                                         int64_t *count)
@@ -1772,58 +1955,10 @@ extern "C" int pw_intersecting_segments(pw_world *w, const double q[7], int64_t 
 		return rc;
 	if (!q || !count || capacity < 0 || (capacity > 0 && (!begins || !ends || !mags || !face_pairs)))
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_intersecting_segments: bad argument");
-	*count = 0;
-	if (w->dev.env.ntri == 0 || w->dev.rob.ntri == 0)
-		return PW_OK;
-	PW_CUDA(cudaSetDevice(w->device));
-	DeviceBuffer dq, dcand, dn, drows;
-	PW_CUDA(dq.reserve(sizeof(double) * 7));
-	PW_CUDA(dcand.reserve(sizeof(uint2) * ISECT_CAP));
-	PW_CUDA(dn.reserve(sizeof(unsigned int) * 2));
-	PW_CUDA(drows.reserve(sizeof(IsectRow) * ISECT_CAP));
-	PW_CUDA(cudaMemcpy(dq.ptr, q, sizeof(double) * 7, cudaMemcpyHostToDevice));
-	PW_CUDA(cudaMemset(dn.ptr, 0, sizeof(unsigned int) * 2));
-	const size_t smem = warp_smem_bytes();
-	rc = set_smem_attr((const void *)k_isect_collect, smem);
-	if (rc)
-		return rc;
-	unsigned int *ncand = (unsigned int *)dn.ptr;
-	k_isect_collect<<<1, 32, smem>>>(w->dev, (const double *)dq.ptr, (uint2 *)dcand.ptr, ncand, soft_cap_of(w));
-	k_isect_eval<<<w->num_sms, 256>>>(w->dev, (const double *)dq.ptr, (const uint2 *)dcand.ptr, ncand,
-	                                  (IsectRow *)drows.ptr, ncand + 1);
-	PW_CUDA(cudaGetLastError());
-	unsigned int nn[2];
-	PW_CUDA(cudaMemcpy(nn, dn.ptr, sizeof(nn), cudaMemcpyDeviceToHost));
-	if (nn[0] > (unsigned)ISECT_CAP)
-		return pw_fail(PW_ERR_CAPACITY, "pw_intersecting_segments: more than 2^20 candidate pairs");
-	std::vector<IsectRow> rows(nn[1]);
-	if (nn[1])
-		PW_CUDA(cudaMemcpy(rows.data(), drows.ptr, sizeof(IsectRow) * nn[1], cudaMemcpyDeviceToHost));
-	std::sort(rows.begin(), rows.end(), [](const IsectRow &a, const IsectRow &b) {
-		return a.et != b.et ? a.et < b.et : a.rt < b.rt;
-	});
-	*count = (int64_t)rows.size();
-	const int64_t m = std::min<int64_t>(capacity, *count);
-	for (int64_t i = 0; i < m; i++) {
-		for (int c = 0; c < 3; c++) {
-			begins[3 * i + c] = rows[i].b[c];
-			ends[3 * i + c] = rows[i].e[c];
-		}
-		mags[i] = rows[i].mag;
-		face_pairs[2 * i] = rows[i].et;
-		face_pairs[2 * i + 1] = rows[i].rt;
-		if (coplanar)
-			coplanar[i] = rows[i].cop;
-	}
-	if (capacity < *count)
-		return pw_fail(PW_ERR_CAPACITY, "pw_intersecting_segments: capacity smaller than the pair count");
-	return PW_OK;
+	int64_t offsets[2];
+	return isect_run(w, q, 1, capacity, begins, ends, mags, face_pairs, coplanar, offsets, count,
+	                 "pw_intersecting_segments");
 }
-
-// Candidate pairs one batch call holds on the device (16 B each), and the
-// states it sends per chunk; a chunk whose candidates overflow is halved.
-constexpr unsigned long long ISECT_BATCH_CAP = 1ull << 21;
-constexpr int64_t ISECT_BATCH_CHUNK = 65536;
 
 extern "C" int pw_intersecting_segments_batch(pw_world *w, const double *q, int64_t n, int64_t capacity,
                                               double *begins, double *ends, double *mags, int32_t *face_pairs,
@@ -1838,81 +1973,8 @@ extern "C" int pw_intersecting_segments_batch(pw_world *w, const double *q, int6
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_intersecting_segments_batch: bad pointers or sizes");
 	if (n > (int64_t(1) << 31))
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_intersecting_segments_batch: at most 2^31 states per call");
-	*total = 0;
-	for (int64_t i = 0; i <= n; i++)
-		offsets[i] = 0;
-	if (n == 0 || w->dev.env.ntri == 0 || w->dev.rob.ntri == 0)
-		return PW_OK;
-	PW_CUDA(cudaSetDevice(w->device));
-	const int64_t chunk0 = std::min<int64_t>(n, ISECT_BATCH_CHUNK);
-	DeviceBuffer dq, dcand, drows, dctr;
-	PW_CUDA(dq.reserve(sizeof(double) * 7 * (size_t)chunk0));
-	PW_CUDA(dcand.reserve(sizeof(IsectCand) * ISECT_BATCH_CAP));
-	PW_CUDA(drows.reserve(sizeof(IsectBatchRow) * ISECT_BATCH_CAP));
-	PW_CUDA(dctr.reserve(sizeof(unsigned long long) * 3));
-	unsigned long long *ctr = (unsigned long long *)dctr.ptr;   // candidates, rows, work
-	const size_t smem = warp_smem_bytes() * WARPS;
-	if ((rc = set_smem_attr((const void *)k_isect_collect_batch, smem)))
-		return rc;
-	int per_sm = 0;
-	PW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_isect_collect_batch, WARPS * 32, smem));
-	const int grid = std::max(1, per_sm) * std::max(1, w->num_sms);
-	std::vector<IsectBatchRow> all, part;
-	int64_t chunk = chunk0;
-	for (int64_t s0 = 0; s0 < n;) {
-		const int64_t m = std::min(chunk, n - s0);
-		PW_CUDA(cudaMemcpy(dq.ptr, q + 7 * s0, sizeof(double) * 7 * (size_t)m, cudaMemcpyHostToDevice));
-		PW_CUDA(cudaMemset(ctr, 0, sizeof(unsigned long long) * 3));
-		k_isect_collect_batch<<<grid, WARPS * 32, smem>>>(w->dev, (const double *)dq.ptr, m, (IsectCand *)dcand.ptr,
-		                                                 ctr, ISECT_BATCH_CAP, ctr + 2, soft_cap_of(w));
-		PW_CUDA(cudaGetLastError());
-		unsigned long long c[2];
-		PW_CUDA(cudaMemcpy(c, ctr, sizeof(c), cudaMemcpyDeviceToHost));
-		if (c[0] > ISECT_BATCH_CAP) {
-			if (m == 1)
-				return pw_fail(PW_ERR_CAPACITY, "pw_intersecting_segments_batch: a state has more than 2^21 candidate pairs");
-			chunk = std::max<int64_t>(1, m / 2);
-			continue;
-		}
-		k_isect_eval_batch<<<w->num_sms * 4, 256>>>(w->dev, (const double *)dq.ptr, (const IsectCand *)dcand.ptr, ctr,
-		                                           ISECT_BATCH_CAP, (IsectBatchRow *)drows.ptr, ctr + 1);
-		PW_CUDA(cudaGetLastError());
-		PW_CUDA(cudaMemcpy(c, ctr, sizeof(c), cudaMemcpyDeviceToHost));
-		part.resize(c[1]);
-		if (c[1])
-			PW_CUDA(cudaMemcpy(part.data(), drows.ptr, sizeof(IsectBatchRow) * c[1], cudaMemcpyDeviceToHost));
-		for (IsectBatchRow &r : part) {
-			r.state += (int32_t)s0;
-			all.push_back(r);
-		}
-		s0 += m;
-	}
-	std::sort(all.begin(), all.end(), [](const IsectBatchRow &a, const IsectBatchRow &b) {
-		if (a.state != b.state)
-			return a.state < b.state;
-		return a.et != b.et ? a.et < b.et : a.rt < b.rt;
-	});
-	for (const IsectBatchRow &r : all)
-		offsets[r.state + 1]++;
-	for (int64_t i = 0; i < n; i++)
-		offsets[i + 1] += offsets[i];
-	*total = (int64_t)all.size();
-	const int64_t kept = std::min<int64_t>(capacity, *total);
-	for (int64_t i = 0; i < kept; i++) {
-		const IsectBatchRow &r = all[i];
-		for (int k = 0; k < 3; k++) {
-			begins[3 * i + k] = r.b[k];
-			ends[3 * i + k] = r.e[k];
-		}
-		mags[i] = r.mag;
-		face_pairs[2 * i] = r.et;
-		face_pairs[2 * i + 1] = r.rt;
-		if (coplanar)
-			coplanar[i] = r.cop;
-	}
-	if (capacity < *total)
-		return pw_fail(PW_ERR_CAPACITY, "pw_intersecting_segments_batch: capacity smaller than the row count");
-	return PW_OK;
+	return isect_run(w, q, n, capacity, begins, ends, mags, face_pairs, coplanar, offsets, total,
+	                 "pw_intersecting_segments_batch");
 }
 
 extern "C" int pw_world_last_stats(pw_world *w, pw_query_stats *out)

@@ -655,21 +655,24 @@ class UnitWorld:
             self._last_coplanar = c[:n].copy()
             return b[:n].copy(), e[:n].copy(), m[:n].copy(), p[:n].copy()
 
-    def intersecting_segments_batch(self, unitqs):
+    def intersecting_segments_batch(self, unitqs, flat: bool = False):
         """intersecting_segments for many unit states in one call: a list of the
         per-state tuples (begins, ends, lengths, face pairs), each as
-        intersecting_segments returns it."""
+        intersecting_segments returns it (views into one set of arrays).  With
+        flat=True: (begins, ends, lengths, face pairs, offsets), the rows of
+        state i at offsets[i]:offsets[i + 1]."""
         q = _states_np(unitqs)
         n = q.shape[0]
         offsets = np.zeros(n + 1, dtype=np.int64)
         total = ctypes.c_int64(0)
-        cap = max(1024, 64 * n)
+        # rows per state seen by the last call sizes the first attempt
+        cap = max(1024, int(getattr(self, "_isect_rows_per_state", 64.0) * 1.25 * n))
         while True:
-            b = np.zeros((cap, 3))
-            e = np.zeros((cap, 3))
-            m = np.zeros(cap)
-            p = np.zeros((cap, 2), dtype=np.int32)
-            c = np.zeros(cap, dtype=np.int32)
+            b = np.empty((cap, 3))
+            e = np.empty((cap, 3))
+            m = np.empty(cap)
+            p = np.empty((cap, 2), dtype=np.int32)
+            c = np.empty(cap, dtype=np.int32)
             rc = self._L.pw_intersecting_segments_batch(self._h, _dp(q), n, cap, _dp(b), _dp(e), _dp(m),
                                                         p.ctypes.data_as(_lib.i32p), c.ctypes.data_as(_lib.i32p),
                                                         offsets.ctypes.data_as(_lib.i64p), ctypes.byref(total))
@@ -678,8 +681,13 @@ class UnitWorld:
                 continue
             check(rc, "intersecting_segments_batch")
             break
-        return [(b[o0:o1].copy(), e[o0:o1].copy(), m[o0:o1].copy(), p[o0:o1].copy())
-                for o0, o1 in zip(offsets[:-1], offsets[1:])]
+        t = int(total.value)
+        if n:
+            self._isect_rows_per_state = max(1.0, t / n)
+        b, e, m, p = b[:t], e[:t], m[:t], p[:t]
+        if flat:
+            return b, e, m, p, offsets
+        return [(b[o0:o1], e[o0:o1], m[o0:o1], p[o0:o1]) for o0, o1 in zip(offsets[:-1], offsets[1:])]
 
     # contact forces (unit_world.cc:1015-1057) ---------------------------------
     def _face_normals(self, geo):

@@ -65,3 +65,20 @@ def test_batch_chunks_and_empty(tori, monkeypatch):
     for a, b in zip(whole, flat):
         for x, y in zip(a, b):
             assert (x == y).all()
+
+
+def test_flat_rows_and_stats(tori):
+    uw, _ = tori
+    q, _ = _states(uw, 60, 73)
+    per = uw.intersecting_segments_batch(q)
+    b, e, m, p, off = uw.intersecting_segments_batch(q, flat=True)
+    st = uw.last_stats()
+    assert off.shape == (q.shape[0] + 1,) and off[0] == 0 and off[-1] == b.shape[0] == p.shape[0]
+    assert (np.diff(off) >= 0).all()
+    for i, t in enumerate(per):
+        assert (t[3] == p[off[i]:off[i + 1]]).all() and (t[0] == b[off[i]:off[i + 1]]).all()
+        # rows of one state sorted by (env face, robot face)
+        k = t[3][:, 0].astype(np.int64) * (1 << 32) + t[3][:, 1]
+        assert (np.diff(k) > 0).all()
+    assert st["queries"] == q.shape[0] and st["retest_hits"] == off[-1]
+    assert st["retests"] >= off[-1] and st["work_items"] >= 4
