@@ -86,7 +86,7 @@ __device__ __forceinline__ uint64_t now_ns()
 
 // Waits for the phase of `parity` to complete.  Gives up when another role has
 // aborted or after WAIT_LIMIT_NS, recording `where` in *err; returns false then.
-__device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag, int *err, int where)
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag, int *err, int where)
 {
 	if (mbar_test(bar, parity))
 		return true;
@@ -394,6 +394,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 					}
 				}
 				for (int sl = 0; sl < nslot; sl++) {
+					// the biases of K-block 0 load while the accumulator is still being computed
+					float bv[2][16];
+#pragma unroll
+					for (int i = 0; i < 4; i++)
+						*reinterpret_cast<float4 *>(bv[0] + 4 * i) =
+						    __ldg(reinterpret_cast<const float4 *>(bias + g * 16) + i);
 					if (!mbar_wait(bar(B_DONE + sl), done_ph[sl], s_abort, a.err, 4)) {
 						ok = false;
 						break;
@@ -403,39 +409,42 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 					uint8_t *act = sm + SM_ACT + sl * ACT_BYTES;
 					float head = 0.f;
 					// this warp's 16 columns j*64 + g*16 .. +15 of each K-block j; the tensor-memory
-					// load of block j + 1 is in flight while block j is computed
+					// load and the biases of block j + 1 are in flight while block j is computed
 					uint32_t rv[2][16];
 					tmem_ld16_nw(tmem + lane_off + (uint32_t)(sl * 256 + g * 16), rv[0]);
 					tmem_wait_ld();
 #pragma unroll
 					for (int j = 0; j < 4; j++) {
-						if (j < 3)
+						if (j < 3) {
 							tmem_ld16_nw(tmem + lane_off + (uint32_t)(sl * 256 + (j + 1) * KB + g * 16),
 							             rv[(j + 1) & 1]);
-						const int col = j * KB + g * 16;
-						float bv[16];
 #pragma unroll
-						for (int i = 0; i < 4; i++)
-							*reinterpret_cast<float4 *>(bv + 4 * i) = __ldg(reinterpret_cast<const float4 *>(bias + col) + i);
+							for (int i = 0; i < 4; i++)
+								*reinterpret_cast<float4 *>(bv[(j + 1) & 1] + 4 * i) = __ldg(
+								    reinterpret_cast<const float4 *>(bias + (j + 1) * KB + g * 16) + i);
+						}
+						const int col = j * KB + g * 16;
+						const float *bvj = bv[j & 1];
 						const uint32_t *cur = rv[j & 1];
 						uint32_t pk[8];
 #pragma unroll
 						for (int i = 0; i < 16; i += 2)
-							pk[i / 2] = silu_pair(cur[i], cur[i + 1], bv[i], bv[i + 1]);
+							pk[i / 2] = silu_pair(cur[i], cur[i + 1], bvj[i], bvj[i + 1]);
 						if (layer < 3) {
 							uint8_t *kb = act + j * ACT_KB_BYTES;
 							*reinterpret_cast<uint4 *>(kb + swz(r, 2 * g)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
 							*reinterpret_cast<uint4 *>(kb + swz(r, 2 * g + 1)) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
 						} else {
+							float wv[16];
 #pragma unroll
 							for (int i = 0; i < 4; i++)
-								*reinterpret_cast<float4 *>(bv + 4 * i) =
+								*reinterpret_cast<float4 *>(wv + 4 * i) =
 								    __ldg(reinterpret_cast<const float4 *>(a.ht + HT_W5 + col) + i);
 #pragma unroll
 							for (int i = 0; i < 8; i++) {
 								const __nv_bfloat162 hh = *reinterpret_cast<__nv_bfloat162 *>(&pk[i]);
-								head = fmaf(__low2float(hh), bv[2 * i], head);
-								head = fmaf(__high2float(hh), bv[2 * i + 1], head);
+								head = fmaf(__low2float(hh), wv[2 * i], head);
+								head = fmaf(__high2float(hh), wv[2 * i + 1], head);
 							}
 						}
 						if (j < 3)
