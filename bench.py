@@ -37,7 +37,8 @@ DELTA = 0.001
 # per-unit algorithmic bytes of the traversal kernel: each node-pair test reads two
 # FP32 boxes, each leaf test two FP32 triangles, each segment its two states and
 # writes its first-contact step
-BYTES_NODE_PAIR = 2 * 32      # env node + robot node (two float4 each)
+BYTES_NODE_PAIR = 2 * 32      # env node + robot node (two float4 each: aligned boxes)
+BYTES_NODE_PAIR_OBB = 2 * 80  # oriented boxes: centre, half-extents and three axis rows (five float4)
 BYTES_LEAF_PAIR = 2 * 48      # env triangle + robot triangle (three float4 each)
 BYTES_SEGMENT = 2 * 56 + 4    # two states in, one int32 out
 
@@ -624,7 +625,8 @@ def run_ours(args):
         return
 
     # roofline of the dominant (traversal) kernel
-    roof = traversal_roofline(stats, work.bytes_in() + work.bytes_out(), args.n, args.workload)
+    roof = traversal_roofline(stats, work.bytes_in() + work.bytes_out(), args.n, args.workload,
+                              uw.get_node_boxes(1 if args.workload == "segments" else 0))
     fc = f.cpu().numpy()
     cpu, parity = None, None
     if ws == 1 and not args.no_cpu_baseline:
@@ -689,7 +691,7 @@ def run_ours(args):
         sys.exit(3)
 
 
-def traversal_roofline(stats, io_bytes, n_units, workload):
+def traversal_roofline(stats, io_bytes, n_units, workload, boxes="aligned"):
     """Roofline record of the traversal kernel.  The algorithmic DRAM bytes are
     the queries' inputs and results; the BVH nodes and triangles the tests read
     are L2-resident, so those bytes are reported apart (cache_served), and the
@@ -713,7 +715,8 @@ def traversal_roofline(stats, io_bytes, n_units, workload):
         per_unit = _profile_value(prof, "dram_bytes_per_state")
     traffic = per_unit * n_units if per_unit is not None else None
     issue = _profile_value(prof, "smsp_issue_active_pct")
-    cache_bytes = node * BYTES_NODE_PAIR + leaf * BYTES_LEAF_PAIR
+    node_pair = BYTES_NODE_PAIR_OBB if boxes == "oriented" else BYTES_NODE_PAIR
+    cache_bytes = node * node_pair + leaf * BYTES_LEAF_PAIR
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic,
             "traffic_frac": (traffic / sec / 1e9 / peak) if traffic is not None else None,
@@ -726,7 +729,7 @@ def traversal_roofline(stats, io_bytes, n_units, workload):
             "limiter_source": "smsp__issue_active of the committed ncu capture (profiles/)",
             "cache_served": {"bytes": cache_bytes, "achieved": cache_bytes / sec / 1e9, "unit": "GB/s",
                              "what": "node-pair tests x %d B + leaf tests x %d B, read from L1/L2"
-                                     % (BYTES_NODE_PAIR, BYTES_LEAF_PAIR)}}
+                                     % (node_pair, BYTES_LEAF_PAIR)}}
 
 
 def surrogate_measure(args, local, rank, n, steps, warmup, with_cpu, e2e=True):
@@ -1050,7 +1053,7 @@ def run_narrow(args):
     gf, gt, gcodes = g_reps[0].validated_states
     uw.first_contact_steps(gf, gt, DELTA, 1)
     st = uw.last_stats()
-    roof = traversal_roofline([st], gf.shape[0] * (2 * 56 + 4), gf.shape[0], "narrow")
+    roof = traversal_roofline([st], gf.shape[0] * (2 * 56 + 4), gf.shape[0], "narrow", uw.get_node_boxes(1))
     roof["kernel_share"] = "exact validation is %.0f %% of a guided round" % (
         100.0 * st["traverse_ms"] * last.rounds / max(1e-9, 1e3 * g_reps[-1].seconds))
     cpu, parity = None, None
