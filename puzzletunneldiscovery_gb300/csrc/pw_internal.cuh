@@ -42,9 +42,15 @@ struct WorldDev {
 	float del_env;           // FP32 rounding bound of an env vertex coordinate
 };
 
+// Round phases of a segment query: phase p holds the rounds (32-step chunk
+// indices) SEG_PHASE_START[p] .. SEG_PHASE_START[p + 1] - 1; each phase computes
+// the anchor frames of its chunks that are still needed, then traverses them.
+constexpr int SEG_PHASES = 8;
+
 // Per-query device counters; zeroed before every query.
 struct QueryCounters {
 	unsigned long long work;        // next work item of the persistent kernels
+	unsigned long long phase_work[SEG_PHASES];   // next work item of each segment round phase
 	unsigned long long retest_count;
 	unsigned long long stat[10];    // see STAT_* below
 	unsigned long long ref_checks;  // isValid calls of the sequential reference loop

@@ -758,35 +758,59 @@ __device__ __forceinline__ void seg_step_qf(const WorldDev &W, const double *a, 
 	make_qf(q, W, o);
 }
 
-// The anchor frame of every chunk (k_seg_setup's checkpoints and step counts
-// in place), one thread per checkpoint slot over a grid-stride loop: the
-// chunk's segment by binary search of the slot offsets, its anchor step's
-// delta walked from the chunk's checkpoint with the reference's update, the
-// FP64 state interpolated and reduced to the FP32 frame.  Kept apart from the
-// sequential per-segment loop so that segments of very different lengths do
-// not leave the FP64 lanes of a warp idle.
-__global__ void k_seg_anchors(WorldDev W, const double *from, const double *to, int64_t n, const int64_t *slot_base,
-                              const SegParams *params, const double *ckpt, QFs *anchors)
+// First round of each phase of a segment query (the last phase is open).
+__constant__ int64_t SEG_PHASE_START[SEG_PHASES + 1] = { 0, 1, 2, 4, 8, 16, 32, 64, INT64_MAX / 4 };
+
+// Work items [begin, end) and first round of phase p, from the rounds' offsets.
+__device__ __forceinline__ void phase_items(const int64_t *round_off, int64_t nrounds, int p, int64_t &r0,
+                                            int64_t &r1, unsigned long long &begin, unsigned long long &end)
 {
-	const int64_t total = slot_base[n];
-	for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < total;
-	     c += (int64_t)gridDim.x * blockDim.x) {
-		int64_t lo = 0, hi = n;          // slot_base[lo] <= c < slot_base[hi]
-		while (hi - lo > 1) {
-			const int64_t mid = (lo + hi) >> 1;
-			if (slot_base[mid] <= c)
-				lo = mid;
-			else
-				hi = mid;
-		}
-		const SegParams &P = params[lo];
-		const int64_t j = c - slot_base[lo];
-		const int64_t K = P.nsteps;
-		if (j >= (K + 31) / 32)
-			continue;                    // a slot past the segment's chunks (or no steps)
-		const int cnt = (int)min((int64_t)32, K - 32 * j);
-		const double d = pwm::walk_delta(ckpt[c], P.dist, P.step, anchor_of(cnt));
-		seg_step_qf(W, from + 7 * lo, to + 7 * lo, P, d, anchors[c]);
+	r0 = min(SEG_PHASE_START[p], nrounds);
+	r1 = min(SEG_PHASE_START[p + 1], nrounds);
+	begin = (unsigned long long)round_off[r0];
+	end = (unsigned long long)round_off[r1];
+}
+
+// Round of work item `item` within rounds [r0, r1): round_off is non-decreasing
+// and round_off[r0] <= item < round_off[r1].
+__device__ __forceinline__ int64_t round_of(const int64_t *round_off, int64_t r0, int64_t r1, unsigned long long item)
+{
+	int64_t lo = r0, hi = r1;
+	while (hi - lo > 1) {
+		const int64_t mid = (lo + hi) >> 1;
+		if (round_off[mid] <= (int64_t)item)
+			lo = mid;
+		else
+			hi = mid;
+	}
+	return lo;
+}
+
+// The anchor frames of one round phase: one thread per work item (segment
+// chunk, in the traversal's chunk-major order), its anchor step's delta walked
+// from the chunk's checkpoint with the reference's update, the FP64 state
+// interpolated and reduced to the FP32 frame.  Chunks at or after a contact
+// that an earlier phase found are skipped: the traversal skips them as well.
+// Kept apart from the traversal so that segments of very different lengths do
+// not leave the FP64 lanes of a warp idle.
+__global__ void k_seg_anchors(WorldDev W, const double *from, const double *to, const uint32_t *order,
+                              const int64_t *round_off, const int64_t *nrounds_p, int phase, const SegParams *params,
+                              const double *ckpt, const int32_t *first, QFs *anchors)
+{
+	int64_t r0, r1;
+	unsigned long long begin, end;
+	phase_items(round_off, *nrounds_p, phase, r0, r1, begin, end);
+	for (unsigned long long item = begin + blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; item < end;
+	     item += (unsigned long long)gridDim.x * blockDim.x) {
+		const int64_t j = round_of(round_off, r0, r1, item);
+		const uint32_t s = order[item - round_off[j]];
+		const SegParams &P = params[s];
+		const int64_t K = P.nsteps, k0 = 32 * j;
+		if (k0 >= K || (int64_t)first[s] <= k0)
+			continue;
+		const int cnt = (int)min((int64_t)32, K - k0);
+		const double d = pwm::walk_delta(ckpt[P.ckpt_base + j], P.dist, P.step, anchor_of(cnt));
+		seg_step_qf(W, from + 7 * (size_t)s, to + 7 * (size_t)s, P, d, anchors[P.ckpt_base + j]);
 	}
 }
 
@@ -951,42 +975,33 @@ __device__ __noinline__ uint32_t resolve_chunk(const WorldDev &W, WarpSmem &sm, 
 }
 
 // Work item = (segment, 32-step chunk) in chunk-major order, so that early
-// contacts prune later chunks.  A warp computes the chunk's FP64 states lane-
-// parallel, then answers its steps with one swept traversal and records the
-// first step in contact with atomicMin.
+// contacts prune later chunks; one launch per round phase.  A warp computes the
+// chunk's FP64 states lane-parallel, then answers its steps with one swept
+// traversal and records the first step in contact with atomicMin.
 template <bool OBB>
 __global__ void __launch_bounds__(WARPS * 32, 8) k_segments(WorldDev W, StateSrc src, const uint32_t *order,
                                                          const int64_t *round_off, const int64_t *nrounds_p,
-                                                         int32_t *first, QueryCounters *ctr, RetestEntry *rq,
-                                                         int soft_cap)
+                                                         int phase, int32_t *first, QueryCounters *ctr,
+                                                         RetestEntry *rq, int soft_cap)
 {
-	const int64_t nrounds = *nrounds_p;
+	int64_t r0, r1;
+	unsigned long long begin, end;
+	phase_items(round_off, *nrounds_p, phase, r0, r1, begin, end);
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	WarpSmem &sm = reinterpret_cast<WarpSmem *>(smem_raw)[warp];
 	LaneStats st;
 	uint32_t queries = 0, items = 0, detailed = 0;
-	const unsigned long long total = ctr->stat[STAT_TOTAL_ITEMS];
 	for (;;) {
 		unsigned long long item = 0;
 		if (lane == 0)
-			item = atomicAdd(&ctr->work, 1ull);
+			item = begin + atomicAdd(&ctr->phase_work[phase], 1ull);
 		item = __shfl_sync(FULL, item, 0);
-		if (item >= total)
+		if (item >= end)
 			break;
 		int64_t j = 0;
-		if (lane == 0) {
-			// round_off[0] = 0 <= item < total = round_off[nrounds]; round_off is non-decreasing
-			int64_t lo = 0, hi = nrounds;
-			while (hi - lo > 1) {
-				const int64_t mid = (lo + hi) >> 1;
-				if (round_off[mid] <= (int64_t)item)
-					lo = mid;
-				else
-					hi = mid;
-			}
-			j = lo;
-		}
+		if (lane == 0)
+			j = round_of(round_off, r0, r1, item);
 		j = __shfl_sync(FULL, j, 0);
 		const uint32_t s = order[item - round_off[j]];
 		const SegParams &P = src.seg[s];
@@ -1520,7 +1535,6 @@ extern "C" int pw_segments_first_contact(pw_world *w, const double *from, const 
 	uint32_t *keys2 = (uint32_t *)w->seg_keys2.ptr, *vals2 = (uint32_t *)w->seg_order2.ptr;
 	k_seg_setup<<<G, B, 0, st>>>(w->dev, from, to, n, verify_delta, mode, slots, slot_base, params, ckpt,
 	                             first_step, keys, vals, ctr, ckpt_cap);
-	k_seg_anchors<<<(unsigned)(w->num_sms * 8), 256, 0, st>>>(w->dev, from, to, n, slot_base, params, ckpt, anchors);
 	PW_CUDA(cudaGetLastError());
 	PW_CUDA(cub::DeviceRadixSort::SortPairsDescending(w->cub_tmp.ptr, t2, keys, keys2, vals, vals2, (int)n, 0, 32, st));
 	if (!w->graph_mode) {
@@ -1547,12 +1561,20 @@ extern "C" int pw_segments_first_contact(pw_world *w, const double *from, const 
 	StateSrc src{ nullptr, from, to, params, ckpt, anchors };
 	if (!w->graph_mode && (rc = mark(w, 0, st)))
 		return rc;
-	if (w->node_boxes[1] == PW_BOXES_ORIENTED)
-		k_segments<true><<<grid, WARPS * 32, smem, st>>>(w->dev, src, vals2, round_off, round_off + round_cap + 1,
-		                                                 first_step, ctr, rq, launch_soft_cap(w, 1));
-	else
-		k_segments<false><<<grid, WARPS * 32, smem, st>>>(w->dev, src, vals2, round_off, round_off + round_cap + 1,
-		                                                  first_step, ctr, rq, launch_soft_cap(w, 1));
+	// per round phase: the anchor frames of the chunks still needed, then their traversal
+	const int64_t *nrounds = round_off + round_cap + 1;
+	const unsigned agrid = (unsigned)(w->num_sms * 8);
+	for (int p = 0; p < SEG_PHASES; p++) {
+		k_seg_anchors<<<agrid, 256, 0, st>>>(w->dev, from, to, vals2, round_off, nrounds, p, params, ckpt, first_step,
+		                                     anchors);
+		if (w->node_boxes[1] == PW_BOXES_ORIENTED)
+			k_segments<true><<<grid, WARPS * 32, smem, st>>>(w->dev, src, vals2, round_off, nrounds, p, first_step,
+			                                                 ctr, rq, launch_soft_cap(w, 1));
+		else
+			k_segments<false><<<grid, WARPS * 32, smem, st>>>(w->dev, src, vals2, round_off, nrounds, p, first_step,
+			                                                  ctr, rq, launch_soft_cap(w, 1));
+	}
+	PW_CUDA(cudaGetLastError());
 	if (!w->graph_mode)
 		mark(w, 1, st);
 	k_retest<RETEST_CAP><<<w->num_sms * 4, 256, 0, st>>>(w->dev, src, nullptr, first_step, ctr, rq);
