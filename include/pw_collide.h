@@ -48,6 +48,11 @@ extern "C" {
 #define PW_BOXES_ALIGNED 0     /* boxes aligned with each mesh's own frame */
 #define PW_BOXES_ORIENTED 1    /* boxes along the principal axes of each node's vertices (default) */
 
+/* Round phases of segment queries (pw_world_set_segment_phases). */
+#define PW_PHASES_AUTO 0       /* phases when a call has at least 2^22 32-step chunks (default) */
+#define PW_PHASES_OFF 1        /* every round in one phase */
+#define PW_PHASES_ON 2         /* always eight phases */
+
 /* First-contact codes written by pw_segments_first_contact (>= 0: step index). */
 #define PW_STEP_FREE (-1)      /* every step free: the reference's `done` is true */
 #define PW_STEP_NONE (-2)      /* verify_delta >= dist: no step checked, `done` false (unit_world.cc:445-447) */
@@ -211,6 +216,17 @@ PW_API int pw_world_get_launch_config(pw_world *w, int kernel, int *width, int *
  * allowed in graph mode (captured launches hold the kernel). */
 PW_API int pw_world_set_node_boxes(pw_world *w, int kernel, int kind);
 PW_API int pw_world_get_node_boxes(pw_world *w, int kernel, int *kind);
+
+/* Round phases of pw_segments_first_contact.  The work of a segment query is its
+ * 32-step chunks in chunk-major order (chunk j of every segment before chunk j + 1),
+ * so that a contact found in one chunk prunes the segment's later chunks.  In
+ * phases (rounds 0, 1, 2-3, 4-7, ..., 64 and above) the FP32 anchor frames of a
+ * phase are computed only for chunks ahead of the contacts earlier phases found,
+ * at the cost of one launch pair and one tail per phase: it pays for large
+ * batches of long segments.  Results do not depend on the mode.  Not allowed in
+ * graph mode (captured launches hold the phases). */
+PW_API int pw_world_set_segment_phases(pw_world *w, int mode);
+PW_API int pw_world_get_segment_phases(pw_world *w, int *mode);
 
 /* The result tuple of transit_state_to_with_contact (unit_world.cc:405-474) for n
  * segments, from the codes pw_segments_first_contact(PW_SEG_TRANSIT) wrote for

@@ -28,6 +28,9 @@ PW_STEP_NONE = -2
 PW_STEP_INVALID = -3
 PW_BOXES_ALIGNED = 0
 PW_BOXES_ORIENTED = 1
+PW_PHASES_AUTO = 0
+PW_PHASES_OFF = 1
+PW_PHASES_ON = 2
 
 # every entry point declared in include/pw_collide.h
 EXPORTS = (
@@ -42,6 +45,7 @@ EXPORTS = (
     "pw_segments_reserve", "pw_world_set_launch_config",
     "pw_world_get_launch_config", "pw_expansion_crossings", "pw_world_scratch_epoch", "pw_expand_states",
     "pw_ompl_check_motions", "pw_ompl_motion_states", "pw_world_set_node_boxes", "pw_world_get_node_boxes",
+    "pw_world_set_segment_phases", "pw_world_get_segment_phases",
     "pw_intersecting_segments_batch",
     # include/pw_mlp.h
     "pw_mlp_create", "pw_mlp_destroy", "pw_mlp_num_params", "pw_mlp_get_params", "pw_mlp_set_params",
@@ -148,6 +152,8 @@ def load():
         "pw_world_get_launch_config": (ctypes.c_int, [vp, ctypes.c_int, i32p, i32p, i32p]),
         "pw_world_set_node_boxes": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
         "pw_world_get_node_boxes": (ctypes.c_int, [vp, ctypes.c_int, i32p]),
+        "pw_world_set_segment_phases": (ctypes.c_int, [vp, ctypes.c_int]),
+        "pw_world_get_segment_phases": (ctypes.c_int, [vp, i32p]),
         "pw_segments_contact_states": (ctypes.c_int, [vp, vp, vp, i64, ctypes.c_double, vp, vp, vp, vp, vp, vp,
                                                       vp]),
         "pw_mlp_create": (ctypes.c_int, [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_uint64]),

@@ -123,18 +123,16 @@ struct pw_world {
 	int64_t last_states = -1;   // size of the last state batch (-1: the last query was segments)
 	int num_sms = 0;
 	// graph mode: segment queries make no host synchronisation and no allocation;
-	// they run within the scratch capacities below (set by pw_segments_reserve or
-	// by the last segment query made outside graph mode)
+	// they run within the scratch sizes that pw_segments_reserve or the last
+	// segment query made outside graph mode left
 	bool graph_mode = false;
-	int64_t cap_chunks = 0;     // checkpoint / anchor slots (32-step chunks) of one call
-	int64_t cap_rounds = 0;     // chunks of the longest segment of one call
-	int64_t cap_segments = 0;   // segments of one call
 	// launch configuration (pw_world_set_launch_config; 0 = default)
 	int launch_width[2] = { 0, 0 };     // queries a warp takes per grab (states kernel only)
 	int launch_soft_cap[2] = { 0, 0 };  // traversal stack soft cap
 	int launch_blocks[2] = { 0, 0 };    // resident blocks per SM of the persistent kernel
 	int grid_cache[4] = { 0, 0, 0, 0 }; // grid of the persistent kernels under that configuration, per box kind
 	int node_boxes[2] = { PW_BOXES_ORIENTED, PW_BOXES_ORIENTED }; // per kernel (pw_world_set_node_boxes)
+	int seg_phases = PW_PHASES_AUTO;   // round phases of segment queries (pw_world_set_segment_phases)
 	// the last segment query's inputs: its parameters and checkpoints stay in the
 	// scratch, so the transit tuples of the same batch can start from them
 	const double *last_seg_from = nullptr, *last_seg_to = nullptr;

@@ -758,15 +758,18 @@ __device__ __forceinline__ void seg_step_qf(const WorldDev &W, const double *a, 
 	make_qf(q, W, o);
 }
 
-// First round of each phase of a segment query (the last phase is open).
+// First round of each phase of a segment query (the last phase is open), and
+// the fewest 32-step chunk slots of a call that runs in phases.
 __constant__ int64_t SEG_PHASE_START[SEG_PHASES + 1] = { 0, 1, 2, 4, 8, 16, 32, 64, INT64_MAX / 4 };
+constexpr int64_t SEG_PHASED_MIN_CHUNKS = int64_t(1) << 22;
 
-// Work items [begin, end) and first round of phase p, from the rounds' offsets.
+// Work items [begin, end) and first round of phase p, from the rounds' offsets
+// (p < 0: every round in one phase).
 __device__ __forceinline__ void phase_items(const int64_t *round_off, int64_t nrounds, int p, int64_t &r0,
                                             int64_t &r1, unsigned long long &begin, unsigned long long &end)
 {
-	r0 = min(SEG_PHASE_START[p], nrounds);
-	r1 = min(SEG_PHASE_START[p + 1], nrounds);
+	r0 = p < 0 ? 0 : min(SEG_PHASE_START[p], nrounds);
+	r1 = p < 0 ? nrounds : min(SEG_PHASE_START[p + 1], nrounds);
 	begin = (unsigned long long)round_off[r0];
 	end = (unsigned long long)round_off[r1];
 }
@@ -995,7 +998,7 @@ __global__ void __launch_bounds__(WARPS * 32, 8) k_segments(WorldDev W, StateSrc
 	for (;;) {
 		unsigned long long item = 0;
 		if (lane == 0)
-			item = begin + atomicAdd(&ctr->phase_work[phase], 1ull);
+			item = begin + atomicAdd(&ctr->phase_work[phase < 0 ? 0 : phase], 1ull);
 		item = __shfl_sync(FULL, item, 0);
 		if (item >= end)
 			break;
@@ -1518,9 +1521,9 @@ extern "C" int pw_segments_first_contact(pw_world *w, const double *from, const 
 	// slots[n] = 0 so that slot_base[n] is the total
 	PW_CUDA(cudaMemsetAsync(slots + n, 0, sizeof(int64_t), st));
 	PW_CUDA(cub::DeviceScan::ExclusiveSum(w->cub_tmp.ptr, t1, slots, slot_base, (int)(n + 1), st));
+	int64_t total_slots = -1;   // this call's chunk slots (outside graph mode)
 	if (!w->graph_mode) {
 		// size the checkpoint arrays by the total (one small synchronous copy)
-		int64_t total_slots = 0;
 		PW_CUDA(cudaMemcpyAsync(&total_slots, slot_base + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
 		PW_CUDA(cudaStreamSynchronize(st));
 		if ((rc = grow<double>(w->seg_ckpt, (size_t)total_slots + 1)) ||
@@ -1561,10 +1564,16 @@ extern "C" int pw_segments_first_contact(pw_world *w, const double *from, const 
 	StateSrc src{ nullptr, from, to, params, ckpt, anchors };
 	if (!w->graph_mode && (rc = mark(w, 0, st)))
 		return rc;
-	// per round phase: the anchor frames of the chunks still needed, then their traversal
+	// per round phase: the anchor frames of the chunks still needed, then their traversal.
+	// Phases pay where there is enough work per phase to keep every warp busy; a
+	// smaller batch runs all rounds as one phase (each phase ends with a tail of
+	// its slowest chunks).
 	const int64_t *nrounds = round_off + round_cap + 1;
 	const unsigned agrid = (unsigned)(w->num_sms * 8);
-	for (int p = 0; p < SEG_PHASES; p++) {
+	const int64_t chunk_slots = w->graph_mode ? ckpt_cap : total_slots;
+	const bool phased = w->seg_phases == PW_PHASES_ON ||
+	                    (w->seg_phases == PW_PHASES_AUTO && chunk_slots >= SEG_PHASED_MIN_CHUNKS);
+	for (int p = phased ? 0 : -1; p < (phased ? SEG_PHASES : 0); p++) {
 		k_seg_anchors<<<agrid, 256, 0, st>>>(w->dev, from, to, vals2, round_off, nrounds, p, params, ckpt, first_step,
 		                                     anchors);
 		if (w->node_boxes[1] == PW_BOXES_ORIENTED)
@@ -2131,5 +2140,24 @@ extern "C" int pw_world_get_node_boxes(pw_world *w, int kernel, int *kind)
 	if (!w || !kind || kernel < 0 || kernel > 1)
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_get_node_boxes: bad argument");
 	*kind = w->node_boxes[kernel];
+	return PW_OK;
+}
+
+extern "C" int pw_world_set_segment_phases(pw_world *w, int mode)
+{
+	if (!w || (mode != PW_PHASES_AUTO && mode != PW_PHASES_OFF && mode != PW_PHASES_ON))
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_set_segment_phases: bad argument");
+	if (w->graph_mode)
+		return pw_fail(PW_ERR_INVALID_ARG,
+		               "pw_world_set_segment_phases: not in graph mode (captured launches hold the phases)");
+	w->seg_phases = mode;
+	return PW_OK;
+}
+
+extern "C" int pw_world_get_segment_phases(pw_world *w, int *mode)
+{
+	if (!w || !mode)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_get_segment_phases: bad argument");
+	*mode = w->seg_phases;
 	return PW_OK;
 }

@@ -329,6 +329,18 @@ class UnitWorld:
         check(self._L.pw_world_get_node_boxes(self._h, int(kernel), ctypes.byref(k)), "get_node_boxes")
         return "oriented" if k.value == _lib.PW_BOXES_ORIENTED else "aligned"
 
+    _PHASES = {"auto": _lib.PW_PHASES_AUTO, "off": _lib.PW_PHASES_OFF, "on": _lib.PW_PHASES_ON}
+
+    def set_segment_phases(self, mode: str) -> None:
+        """Round phases of segment queries: "auto" (default), "off" or "on"; the
+        results do not depend on it."""
+        check(self._L.pw_world_set_segment_phases(self._h, self._PHASES[mode]), "set_segment_phases")
+
+    def get_segment_phases(self) -> str:
+        k = ctypes.c_int32()
+        check(self._L.pw_world_get_segment_phases(self._h, ctypes.byref(k)), "get_segment_phases")
+        return {v: name for name, v in self._PHASES.items()}[k.value]
+
     def last_stats(self) -> dict:
         st = _lib.QueryStats()
         check(self._L.pw_world_last_stats(self._h, ctypes.byref(st)), "last_stats")
