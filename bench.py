@@ -18,6 +18,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -1131,6 +1132,13 @@ def _cpu_plain_narrow(validated, target_s):
     return cpu, parity
 
 
+def _keyconf_half_angles(spins):
+    """Cosine and sine of half of each enumFreeConfiguration spin angle i * 2 pi / spins."""
+    delta = 2 * math.pi / float(spins)
+    half = [0.5 * (i * delta) for i in range(spins)]
+    return [math.cos(h) for h in half], [math.sin(h) for h in half]
+
+
 def _surface_pairs(V, F, Vr, Fr, n, rng):
     """n (robot point, robot normal, env point, env normal) surface samples: a
     triangle drawn by area, a uniform point on it, the face's unit normal."""
@@ -1215,18 +1223,25 @@ class RowJob:
                 res = list(ex.map(ow.intersecting_segments, self.q[:m]))
             units = m
         elif self.name == "keyconf":
+            from oracle import oracle as O
             rp, rn, ep, en = (x[:m] for x in self.pairs)
-            ang = np.broadcast_to(np.arange(KEYCONF_SPINS) * (2 * np.pi / KEYCONF_SPINS), (m, KEYCONF_SPINS))
-            qs = SP._touch_states(rp, rn, ep, en, KEYCONF_MARGIN, ang)
-            valid = ow.is_valid(np.ascontiguousarray(qs.reshape(-1, 7)), nthreads=threads).reshape(m, KEYCONF_SPINS)
-            res = SP._free_spins(qs, valid, True)
+            hc, hs = _keyconf_half_angles(KEYCONF_SPINS)
+            qs = O.keyconf_states(rp, rn, ep, en, KEYCONF_MARGIN, hc, hs, nthreads=threads)
+            valid = ow.is_valid(qs.reshape(-1, 7), nthreads=threads).reshape(m, KEYCONF_SPINS)
+            res = O.free_spins(qs, valid, True)
             units = m * KEYCONF_SPINS
         else:
             k = m * TOUCH_PER_KEY
             frm = np.repeat(self.keys[:m], TOUCH_PER_KEY, axis=0)
-            res, _ = ow.segments_first_contact(frm, self.to[:k], self.uw.recommended_cres, mode=0, nthreads=threads)
+            res, _ = ow.segments_first_contact(frm, self._targets(k), self.uw.recommended_cres, mode=0,
+                                               nthreads=threads)
             units = k
         return units, time.perf_counter() - t0, res
+
+    def _targets(self, k):
+        """The first k touch targets of the last step, on the host."""
+        to = self.to[:k]
+        return to.cpu().numpy() if hasattr(to, "cpu") else to
 
     def mismatches(self, ow, gpu_res, cpu_res, m):
         """Results of the first m units that differ from the oracle's."""
@@ -1249,8 +1264,9 @@ class RowJob:
         lf, st, done, lt, tt = gpu_res
         bad = int((done[:k].astype(bool) != (cpu_res == -1)).sum())
         frm = np.repeat(self.keys[:m], TOUCH_PER_KEY, axis=0)
+        to = self._targets(min(k, 256))
         for i in range(min(k, 256)):
-            (wl, ws_, wd, wlt, wtt), _, _ = ow.transit_state_to_with_contact(frm[i], self.to[i],
+            (wl, ws_, wd, wlt, wtt), _, _ = ow.transit_state_to_with_contact(frm[i], to[i],
                                                                               self.uw.recommended_cres)
             same = (lf[i] == wl).all() and (st[i] == ws_).all() and bool(done[i]) == wd and lt[i] == wlt \
                 and tt[i] == wtt
@@ -1282,16 +1298,10 @@ def run_rows(args):
     from puzzletunneldiscovery_gb300.autotune import pick_node_boxes
     if args.workload == "keyconf":
         rp, rn, ep, en = (x[:512] for x in job.pairs)
-        ang = np.broadcast_to(np.arange(KEYCONF_SPINS) * (2 * np.pi / KEYCONF_SPINS), (512, KEYCONF_SPINS))
-        pick_node_boxes(uw, states=torch.from_numpy(np.ascontiguousarray(
-            SP._touch_states(rp, rn, ep, en, KEYCONF_MARGIN, ang).reshape(-1, 7))).to(dev))
+        hc, hs = _keyconf_half_angles(KEYCONF_SPINS)
+        pick_node_boxes(uw, states=SP.keyconf_states(uw, rp, rn, ep, en, KEYCONF_MARGIN, hc, hs).view(-1, 7))
     elif args.workload == "touch":
-        k = job.keys[:256]
-        r = np.random.default_rng(5)
-        frm = np.repeat(k, TOUCH_PER_KEY, axis=0)
-        to = SP.apply_rows(frm, SP.random_on_sphere(frm.shape[0], 1.0, r),
-                           SP.random_within_sphere(frm.shape[0], 2 * np.pi, r))
-        pick_node_boxes(uw, segments=(torch.from_numpy(frm).to(dev), torch.from_numpy(to).to(dev)),
+        pick_node_boxes(uw, segments=SP.touch_segments(uw, job.keys[:256], TOUCH_PER_KEY, 5),
                         verify_delta=uw.recommended_cres)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     for _ in range(args.warmup):

@@ -268,6 +268,31 @@ PW_API int pw_expansion_crossings(const double *roots, const double *ends, int64
 PW_API int pw_expand_states(const double *roots, int64_t nroots, int per_root, double sigma_t, double sigma_rot,
                             uint64_t seed, double *out, void *stream);
 
+/* device in, device out, async: the candidate states of
+ * UnitWorld::enumFreeConfiguration / sampleFreeConfiguration
+ * (lib/osr/unit_world.cc:1294-1389) for npairs surface pairs (points and
+ * normals [npairs x 3]) and nspins spins each: the robot surface point plus
+ * margin x normal placed on the environment's, normals opposed (shortest arc),
+ * then spun about the environment normal.  half_cos / half_sin: cosine and sine
+ * of half of each spin's angle, [nspins] shared by every pair (per_pair_angles
+ * 0) or [npairs x nspins] (1).  out: [npairs x nspins x 7] unit states, FP64
+ * with every operation rounded on its own in a fixed order (the oracle's
+ * or_keyconf_states gives the same bits). */
+PW_API int pw_keyconf_states(const double *rob_points, const double *rob_normals, const double *env_points,
+                             const double *env_normals, int64_t npairs, double margin, const double *half_cos,
+                             const double *half_sin, int64_t nspins, int per_pair_angles, double *out,
+                             void *stream);
+
+/* device in, device out, async: the random segments of touchq_util.calc_touch
+ * (src/GP/pipeline/touchq_util.py:8-27) for nkeys keys [nkeys x 7], per_key
+ * each: row i * per_key + j goes from key i (copied to from) to the key
+ * translated by a random point of the unit sphere and rotated on the left by a
+ * rotation vector uniform in the ball of radius 2 pi (osr::apply,
+ * osr_state.cc:244-259), normalised.  Counter-based random numbers: the same
+ * seed gives the same targets. */
+PW_API int pw_touch_targets(const double *keys, int64_t nkeys, int per_key, uint64_t seed, double *from,
+                            double *to, void *stream);
+
 /* host: state-frame conversions (unit_world.cc:526-539, 689-711, 713-737). */
 PW_API int pw_world_translate_to_unit(const pw_world *w, const double *in, int64_t n, double *out);
 PW_API int pw_world_translate_from_unit(const pw_world *w, const double *in, int64_t n, double *out);

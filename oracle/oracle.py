@@ -116,6 +116,8 @@ def lib():
         L.or_ompl_to_unit.argtypes = [ctypes.c_void_p, c_double_p, c_double_p]
         L.or_ompl_check_motions.argtypes = [ctypes.c_void_p, c_double_p, c_double_p, ctypes.c_int64, c_double_p,
                                             c_u8_p, c_i64_p, ctypes.c_int]
+        L.or_keyconf_states.argtypes = [c_double_p] * 4 + [ctypes.c_int64, ctypes.c_double, c_double_p, c_double_p,
+                                                          ctypes.c_int64, ctypes.c_int, c_double_p, ctypes.c_int]
         L.or_tri_tri.restype = ctypes.c_int
         L.or_tri_tri.argtypes = [c_double_p] * 6 + [ctypes.c_double]
         L.or_tri_tri_isect.restype = ctypes.c_int
@@ -336,4 +338,43 @@ def ompl_motion_states(a, b, lo, hi, cdres):
                                 _p(np.zeros(7), c_double_p))
     out = np.zeros((m, 7))
     L.or_ompl_motion_states(_p(a, c_double_p), _p(b, c_double_p), _p(lvs, c_double_p), m, _p(out, c_double_p))
+    return out
+
+
+def keyconf_states(rob_points, rob_normals, env_points, env_normals, margin, half_cos, half_sin, nthreads=0):
+    """[P, A, 7] candidate states of enumFreeConfiguration / sampleFreeConfiguration
+    (unit_world.cc:1294-1389) for P surface pairs; half_cos / half_sin [A] (the
+    same spins for every pair) or [P, A]."""
+    rp, rn, ep, en = (np.ascontiguousarray(np.atleast_2d(x), dtype=np.float64) for x in
+                      (rob_points, rob_normals, env_points, env_normals))
+    P = rp.shape[0]
+    hc = np.ascontiguousarray(half_cos, dtype=np.float64)
+    hs = np.ascontiguousarray(half_sin, dtype=np.float64)
+    per_pair = hc.ndim == 2
+    A = hc.shape[-1]
+    out = np.empty((P, A, 7))
+    lib().or_keyconf_states(_p(rp, c_double_p), _p(rn, c_double_p), _p(ep, c_double_p), _p(en, c_double_p), P,
+                            float(margin), _p(hc, c_double_p), _p(hs, c_double_p), A, int(per_pair),
+                            _p(out, c_double_p), int(nthreads))
+    return out
+
+
+def free_spins(qs, valid, only_median):
+    """The states enumFreeConfiguration returns per surface pair from its spins'
+    states [P, A, 7] and verdicts [P, A] (unit_world.cc:1367-1386): every free
+    spin, or, with only_median, the middle state of each run of consecutive free
+    spins that a colliding spin ends (a run open at the last spin is dropped)."""
+    out = []
+    for p in range(valid.shape[0]):
+        keep, run = [], []
+        for a in range(valid.shape[1]):
+            if not only_median:
+                if valid[p, a]:
+                    keep.append(qs[p, a])
+            elif valid[p, a]:
+                run.append(qs[p, a])
+            elif run:
+                keep.append(run[len(run) // 2])
+                run = []
+        out.append(np.array(keep).reshape(-1, 7))
     return out

@@ -1515,3 +1515,85 @@ OR_EXPORT void or_ompl_check_motions(const or_world *w, const double *from, cons
 		valid[i] = (uint8_t)ok;
 	}
 }
+
+/* ------------------------------------------------------------------------ */
+/* Key-configuration states (unit_world.cc:1294-1389)                        */
+/* ------------------------------------------------------------------------ */
+
+/* The candidate state of UnitWorld::enumFreeConfiguration /
+ * sampleFreeConfiguration for one surface pair and one spin, in Eigen's
+ * published forms (unit_world.cc:1301-1330 calls them): the robot point plus
+ * margin x normal goes to the environment point plus margin x normal, after
+ * rot_1 = Quaternion::setFromTwoVectors(rob normal, -env normal) (normalise
+ * both, c = v0.v1; w = s / 2 and vec = (v0 x v1) * (1 / s) with
+ * s = sqrt((1 + c) * 2); for c < -1 + 1e-12 a half turn about an axis
+ * perpendicular to v0) and rot_2 = AngleAxis(angle, env normal)
+ * = (cos(angle / 2), sin(angle / 2) * normal), rot_accum = rot_2 * rot_1;
+ * trans = env_o - rot_accum * rob_o with Eigen's quaternion-vector product
+ * (uv = u x v, uv += uv, v + w uv + u x uv); compose normalises the rotation.
+ * hc, hs: the half angle's cosine and sine. */
+static double or_norm3(const double v[3]) { return sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]); }
+
+static void or_keyconf_state(const double rp[3], const double rn[3], const double ep[3], const double en[3],
+                             double margin, double hc, double hs, double out[7])
+{
+	double rob_o[3], env_o[3], v0[3], v1[3], r1[4];
+	for (int i = 0; i < 3; i++) {
+		rob_o[i] = rp[i] + rn[i] * margin;
+		env_o[i] = ep[i] + en[i] * margin;
+	}
+	const double na = or_norm3(rn);
+	const double neg[3] = { -en[0], -en[1], -en[2] };
+	const double nb = or_norm3(neg);
+	for (int i = 0; i < 3; i++) {
+		v0[i] = rn[i] / na;
+		v1[i] = neg[i] / nb;
+	}
+	const double c = (v0[0] * v1[0] + v0[1] * v1[1]) + v0[2] * v1[2];
+	if (c < -1.0 + 1e-12) {
+		int k = 0;
+		if (fabs(v0[1]) < fabs(v0[k])) k = 1;
+		if (fabs(v0[2]) < fabs(v0[k])) k = 2;
+		const double e[3] = { k == 0 ? 1.0 : 0.0, k == 1 ? 1.0 : 0.0, k == 2 ? 1.0 : 0.0 };
+		double ax[3];
+		or_cross3(v0, e, ax);
+		const double n = or_norm3(ax);
+		r1[0] = 0.0; r1[1] = ax[0] / n; r1[2] = ax[1] / n; r1[3] = ax[2] / n;
+	} else {
+		const double s = sqrt((1.0 + c) * 2.0);
+		const double invs = 1.0 / s;
+		double ax[3];
+		or_cross3(v0, v1, ax);
+		r1[0] = s * 0.5; r1[1] = ax[0] * invs; r1[2] = ax[1] * invs; r1[3] = ax[2] * invs;
+	}
+	const double r2[4] = { hc, hs * en[0], hs * en[1], hs * en[2] };
+	double acc[4];
+	acc[0] = ((r2[0] * r1[0] - r2[1] * r1[1]) - r2[2] * r1[2]) - r2[3] * r1[3];
+	acc[1] = ((r2[0] * r1[1] + r2[1] * r1[0]) + r2[2] * r1[3]) - r2[3] * r1[2];
+	acc[2] = ((r2[0] * r1[2] - r2[1] * r1[3]) + r2[2] * r1[0]) + r2[3] * r1[1];
+	acc[3] = ((r2[0] * r1[3] + r2[1] * r1[2]) - r2[2] * r1[1]) + r2[3] * r1[0];
+	const double u[3] = { acc[1], acc[2], acc[3] };
+	double t[3], ut[3];
+	or_cross3(u, rob_o, t);
+	for (int i = 0; i < 3; i++)
+		t[i] = t[i] + t[i];
+	or_cross3(u, t, ut);
+	for (int i = 0; i < 3; i++)
+		out[i] = env_o[i] - ((rob_o[i] + acc[0] * t[i]) + ut[i]);
+	or_quat_normalize(acc, out + 3);
+}
+
+/* The states of npairs surface pairs x nspins spins ([npairs x nspins x 7]);
+ * the half-angle tables are [nspins] (per_pair 0) or [npairs x nspins]. */
+OR_EXPORT void or_keyconf_states(const double *rp, const double *rn, const double *ep, const double *en, int64_t np,
+                                 double margin, const double *hc, const double *hs, int64_t na, int per_pair,
+                                 double *out, int nthreads)
+{
+	if (nthreads > 0)
+		omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(static)
+	for (int64_t i = 0; i < np * na; i++) {
+		const int64_t p = i / na, a = i % na, k = per_pair ? i : a;
+		or_keyconf_state(rp + 3 * p, rn + 3 * p, ep + 3 * p, en + 3 * p, margin, hc[k], hs[k], out + 7 * i);
+	}
+}

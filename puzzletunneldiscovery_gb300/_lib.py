@@ -45,7 +45,7 @@ EXPORTS = (
     "pw_segments_reserve", "pw_world_set_launch_config",
     "pw_world_get_launch_config", "pw_expansion_crossings", "pw_world_scratch_epoch", "pw_expand_states",
     "pw_ompl_check_motions", "pw_ompl_motion_states", "pw_world_set_node_boxes", "pw_world_get_node_boxes",
-    "pw_world_set_segment_phases", "pw_world_get_segment_phases",
+    "pw_world_set_segment_phases", "pw_world_get_segment_phases", "pw_keyconf_states", "pw_touch_targets",
     "pw_intersecting_segments_batch",
     # include/pw_mlp.h
     "pw_mlp_create", "pw_mlp_destroy", "pw_mlp_num_params", "pw_mlp_get_params", "pw_mlp_set_params",
@@ -153,6 +153,8 @@ def load():
         "pw_world_set_node_boxes": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
         "pw_world_get_node_boxes": (ctypes.c_int, [vp, ctypes.c_int, i32p]),
         "pw_world_set_segment_phases": (ctypes.c_int, [vp, ctypes.c_int]),
+        "pw_keyconf_states": (ctypes.c_int, [vp, vp, vp, vp, i64, ctypes.c_double, vp, vp, i64, ctypes.c_int, vp, vp]),
+        "pw_touch_targets": (ctypes.c_int, [vp, i64, ctypes.c_int, ctypes.c_uint64, vp, vp, vp]),
         "pw_world_get_segment_phases": (ctypes.c_int, [vp, i32p]),
         "pw_segments_contact_states": (ctypes.c_int, [vp, vp, vp, i64, ctypes.c_double, vp, vp, vp, vp, vp, vp,
                                                       vp]),

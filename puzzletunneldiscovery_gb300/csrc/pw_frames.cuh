@@ -20,14 +20,7 @@ struct Frame {
 };
 
 // Hamilton product a * b, quaternions (w, x, y, z).
-PW_HD void quat_mul(const double *a, const double *b, double *o)
-{
-	using namespace pwm;
-	o[0] = sub(sub(sub(mul(a[0], b[0]), mul(a[1], b[1])), mul(a[2], b[2])), mul(a[3], b[3]));
-	o[1] = sub(add(add(mul(a[0], b[1]), mul(a[1], b[0])), mul(a[2], b[3])), mul(a[3], b[2]));
-	o[2] = add(add(sub(mul(a[0], b[2]), mul(a[1], b[3])), mul(a[2], b[0])), mul(a[3], b[1]));
-	o[3] = add(sub(add(mul(a[0], b[3]), mul(a[1], b[2])), mul(a[2], b[1])), mul(a[3], b[0]));
-}
+PW_HD void quat_mul(const double *a, const double *b, double *o) { pwm::quat_mul(a, b, o); }
 
 PW_HD void mat_vec(const double *R, const double *v, double *o)
 {

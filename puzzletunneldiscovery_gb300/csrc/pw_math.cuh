@@ -735,4 +735,100 @@ PW_HD int boxes_disjoint(const double *q, const double *rc, const double *rh,
 	return sat_disjoint(eh, rh, T, Rr, AR);
 }
 
+// ---------------------------------------------------------------- key configurations
+//
+// UnitWorld::enumFreeConfiguration / sampleFreeConfiguration
+// (lib/osr/unit_world.cc:1294-1389) place the robot so that its surface point
+// plus margin x normal meets the environment's, normals opposed, then spin it
+// about the environment normal.  Eigen's published forms, each operation
+// rounded on its own, in the order written:
+//   shortest arc a -> b (Quaternion::setFromTwoVectors): v0 = a / |a|,
+//     v1 = b / |b|, c = v0 . v1; w = s / 2, vec = (v0 x v1) * (1 / s) with
+//     s = sqrt((1 + c) * 2); for c < -1 + 1e-12 a half turn about a unit axis
+//     perpendicular to v0 (v0 x the basis vector of its smallest |component|);
+//   angle-axis (AngleAxis -> Quaternion): (cos(angle / 2), sin(angle / 2) * axis),
+//     the half-angle cosine and sine given (computed once on the host);
+//   rotation of v (Quaternion * vector): t = u x v, t = t + t, v + w t + u x t;
+//   compose: translation, quaternion normalised (quat_normalize).
+
+// |v| with the sum of squares in index order.
+PW_HD double norm3(const double *v) { return rt(add(add(mul(v[0], v[0]), mul(v[1], v[1])), mul(v[2], v[2]))); }
+
+// Shortest-arc rotation (w, x, y, z) taking direction a to direction b.
+PW_HD void shortest_arc(const double *a, const double *b, double *q)
+{
+	const double na = norm3(a), nb = norm3(b);
+	const double v0[3] = { dvd(a[0], na), dvd(a[1], na), dvd(a[2], na) };
+	const double v1[3] = { dvd(b[0], nb), dvd(b[1], nb), dvd(b[2], nb) };
+	const double c = add(add(mul(v0[0], v1[0]), mul(v0[1], v1[1])), mul(v0[2], v1[2]));
+	if (c < -1.0 + 1e-12) {
+		int k = 0;
+		if (dabs(v0[1]) < dabs(v0[k]))
+			k = 1;
+		if (dabs(v0[2]) < dabs(v0[k]))
+			k = 2;
+		const double e[3] = { k == 0 ? 1.0 : 0.0, k == 1 ? 1.0 : 0.0, k == 2 ? 1.0 : 0.0 };
+		double ax[3];
+		cross3(v0, e, ax);
+		const double n = norm3(ax);
+		q[0] = 0.0;
+		q[1] = dvd(ax[0], n);
+		q[2] = dvd(ax[1], n);
+		q[3] = dvd(ax[2], n);
+		return;
+	}
+	const double s = rt(mul(add(1.0, c), 2.0));
+	const double invs = dvd(1.0, s);
+	double ax[3];
+	cross3(v0, v1, ax);
+	q[0] = mul(s, 0.5);
+	q[1] = mul(ax[0], invs);
+	q[2] = mul(ax[1], invs);
+	q[3] = mul(ax[2], invs);
+}
+
+// Hamilton product a * b of (w, x, y, z) quaternions, each sum left to right.
+PW_HD void quat_mul(const double *a, const double *b, double *o)
+{
+	o[0] = sub(sub(sub(mul(a[0], b[0]), mul(a[1], b[1])), mul(a[2], b[2])), mul(a[3], b[3]));
+	o[1] = sub(add(add(mul(a[0], b[1]), mul(a[1], b[0])), mul(a[2], b[3])), mul(a[3], b[2]));
+	o[2] = add(add(sub(mul(a[0], b[2]), mul(a[1], b[3])), mul(a[2], b[0])), mul(a[3], b[1]));
+	o[3] = add(sub(add(mul(a[0], b[3]), mul(a[1], b[2])), mul(a[2], b[1])), mul(a[3], b[0]));
+}
+
+// v rotated by the quaternion q (w, x, y, z), unnormalised formula.
+PW_HD void quat_rotate(const double *q, const double *v, double *o)
+{
+	const double u[3] = { q[1], q[2], q[3] };
+	double t[3], ut[3];
+	cross3(u, v, t);
+	t[0] = add(t[0], t[0]);
+	t[1] = add(t[1], t[1]);
+	t[2] = add(t[2], t[2]);
+	cross3(u, t, ut);
+	for (int i = 0; i < 3; i++)
+		o[i] = add(add(v[i], mul(q[0], t[i])), ut[i]);
+}
+
+// The key-configuration state of one surface pair and one spin (half-angle
+// cosine hc and sine hs of the spin about the environment normal).
+PW_HD void keyconf_state(const double *rp, const double *rn, const double *ep, const double *en, double margin,
+                         double hc, double hs, double *out)
+{
+	double rob_o[3], env_o[3], neg_en[3];
+	for (int i = 0; i < 3; i++) {
+		rob_o[i] = add(rp[i], mul(rn[i], margin));
+		env_o[i] = add(ep[i], mul(en[i], margin));
+		neg_en[i] = -en[i];
+	}
+	double r1[4], acc[4], rv[3];
+	shortest_arc(rn, neg_en, r1);
+	const double r2[4] = { hc, mul(hs, en[0]), mul(hs, en[1]), mul(hs, en[2]) };
+	quat_mul(r2, r1, acc);
+	quat_rotate(acc, rob_o, rv);
+	for (int i = 0; i < 3; i++)
+		out[i] = sub(env_o[i], rv[i]);
+	quat_normalize(acc, out + 3);
+}
+
 } // namespace pwm

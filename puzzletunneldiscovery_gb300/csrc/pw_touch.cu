@@ -283,3 +283,106 @@ extern "C" int pw_expand_states(const double *roots, int64_t nroots, int per_roo
 	PW_CUDA(cudaGetLastError());
 	return PW_OK;
 }
+
+// ------------------------------------------------------------------ key configurations and touch targets
+
+namespace {
+
+// One thread per (surface pair, spin): the state of pwm::keyconf_state.
+__global__ void k_keyconf_states(const double *rp, const double *rn, const double *ep, const double *en, int64_t P,
+                                 int64_t A, double margin, const double *hc, const double *hs, int per_pair,
+                                 double *out)
+{
+	const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+	if (i >= P * A)
+		return;
+	const int64_t p = i / A, a = i - p * A;
+	const int64_t k = per_pair ? i : a;
+	pwm::keyconf_state(rp + 3 * p, rn + 3 * p, ep + 3 * p, en + 3 * p, margin, hc[k], hs[k], out + 7 * i);
+}
+
+// A uniform direction on the unit sphere from two 24-bit uniforms (z uniform in
+// (-1, 1), azimuth uniform), in FP32: sampling noise, not a verdict.
+__device__ __forceinline__ void unit_direction(uint64_t bits, float d[3])
+{
+	const float u1 = ((float)(uint32_t)(bits >> 40) + 0.5f) * (1.0f / 16777216.0f);
+	const float u2 = ((float)(uint32_t)((bits >> 16) & 0xFFFFFFu) + 0.5f) * (1.0f / 16777216.0f);
+	const float z = 1.0f - 2.0f * u1;
+	const float r = sqrtf(fmaxf(0.0f, 1.0f - z * z));
+	float s, c;
+	sincospif(2.0f * u2, &s, &c);
+	d[0] = r * c;
+	d[1] = r * s;
+	d[2] = z;
+}
+
+// Row i of a touch batch: the key i / per_key, and the target osr::apply
+// (osr_state.cc:244-259) makes of it with a random unit-sphere translation and
+// a rotation vector uniform in the ball of radius 2 pi, applied on the left.
+__global__ void k_touch_targets(const double *keys, int64_t n, int per_key, uint64_t seed, double *from, double *to)
+{
+	const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+	if (i >= n)
+		return;
+	const double *q = keys + 7 * (i / per_key);
+	const uint64_t base = mix64(seed ^ mix64((uint64_t)i));
+	float tr[3], ax[3];
+	unit_direction(mix64(base + 1), tr);
+	unit_direction(mix64(base + 2), ax);
+	const uint64_t b3 = mix64(base + 3);
+	const float u3 = ((float)(uint32_t)(b3 >> 40) + 0.5f) * (1.0f / 16777216.0f);
+	// radius of a point uniform in the ball: 2 pi * cbrt(u); half of it for the quaternion
+	const float half = 3.14159265f * cbrtf(u3);
+	float sh, ch;
+	sincosf(half, &sh, &ch);
+	const double qa[4] = { (double)ch, (double)(sh * ax[0]), (double)(sh * ax[1]), (double)(sh * ax[2]) };
+	double rot[4], r[4];
+	const double raw[4] = { q[3], q[4], q[5], q[6] };
+	pwm::quat_normalize(raw, rot);
+	pwm::quat_mul(qa, rot, r);
+	double *f = from + 7 * i, *o = to + 7 * i;
+	for (int c = 0; c < 7; c++)
+		f[c] = q[c];
+	for (int c = 0; c < 3; c++)
+		o[c] = pwm::add(q[c], (double)tr[c]);
+	pwm::quat_normalize(r, o + 3);
+}
+
+} // namespace
+
+extern "C" int pw_keyconf_states(const double *rob_points, const double *rob_normals, const double *env_points,
+                                 const double *env_normals, int64_t npairs, double margin, const double *half_cos,
+                                 const double *half_sin, int64_t nspins, int per_pair_angles, double *out,
+                                 void *stream)
+{
+	PW_TRACE("pw_keyconf_states");
+	if (npairs < 0 || nspins <= 0 || !(margin == margin) ||
+	    (npairs > 0 && (!rob_points || !rob_normals || !env_points || !env_normals || !half_cos || !half_sin || !out)))
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_keyconf_states: bad pointers or sizes");
+	if (npairs > (int64_t(1) << 40) / nspins)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_keyconf_states: too many states");
+	const int64_t n = npairs * nspins;
+	if (n == 0)
+		return PW_OK;
+	k_keyconf_states<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+	    rob_points, rob_normals, env_points, env_normals, npairs, nspins, margin, half_cos, half_sin,
+	    per_pair_angles ? 1 : 0, out);
+	PW_CUDA(cudaGetLastError());
+	return PW_OK;
+}
+
+extern "C" int pw_touch_targets(const double *keys, int64_t nkeys, int per_key, uint64_t seed, double *from,
+                                double *to, void *stream)
+{
+	PW_TRACE("pw_touch_targets");
+	if (nkeys < 0 || per_key <= 0 || (nkeys > 0 && (!keys || !from || !to)))
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_touch_targets: bad pointers or sizes");
+	if (nkeys > (int64_t(1) << 40) / per_key)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_touch_targets: too many segments");
+	const int64_t n = nkeys * per_key;
+	if (n == 0)
+		return PW_OK;
+	k_touch_targets<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(keys, n, per_key, seed, from, to);
+	PW_CUDA(cudaGetLastError());
+	return PW_OK;
+}

@@ -14,11 +14,15 @@ configurations.
   segments are one ``pw_segments_first_contact`` call plus one
   ``pw_segments_contact_states`` call.
 
-The rotations are built from the published formulas (shortest-arc quaternion,
-Melax 2000; angle-axis quaternion; Hamilton product) in FP64 numpy.  Verdicts
-on the resulting states are the engine's exact ones; agreement of the states
-themselves with Eigen's last-ulp rounding is not pinned (the reference cannot
-be built here).
+The key-configuration states are built on the device (``pw_keyconf_states``)
+from Eigen's published forms (shortest-arc quaternion, angle-axis quaternion,
+Hamilton product, quaternion-vector product), every FP64 operation rounded on
+its own in a fixed order, so the oracle's ``or_keyconf_states`` gives the same
+bits; agreement with Eigen's own last-ulp rounding is not pinned (the
+reference cannot be built here).  The touch segments' random targets are drawn
+on the device too (``pw_touch_targets``).  The numpy helpers below (quaternion
+products, ``apply_batch``, ``apply_rows``) serve callers that build single
+states on the host.
 """
 from __future__ import annotations
 
@@ -27,6 +31,7 @@ import math
 import numpy as np
 import torch
 
+from . import _lib
 from .unit_world import UnitWorld
 
 
@@ -42,48 +47,12 @@ def quat_mul(a, b):
                      w1 * y2 - x1 * z2 + y1 * w2 + z1 * x2, w1 * z2 + x1 * y2 - y1 * x2 + z1 * w2], axis=-1)
 
 
-def quat_rotate(q, v):
-    """Rotate [..., 3] vectors by unit quaternions [..., 4]."""
-    q = np.asarray(q, np.float64)
-    v = np.asarray(v, np.float64)
-    w = q[..., :1]
-    u = q[..., 1:]
-    t = 2.0 * np.cross(u, v)
-    return v + w * t + np.cross(u, t)
-
-
 def quat_from_angle_axis(angle, axis):
     """Quaternion of a rotation by `angle` about unit `axis` (broadcasting)."""
     angle = np.asarray(angle, np.float64)
     axis = np.asarray(axis, np.float64)
     h = 0.5 * angle
     return np.concatenate([np.cos(h)[..., None], np.sin(h)[..., None] * axis], axis=-1)
-
-
-def quat_between(a, b):
-    """Shortest-arc rotation taking direction a to direction b (Melax 2000).
-    For opposite directions, a half turn about an axis perpendicular to a."""
-    a = np.asarray(a, np.float64)
-    b = np.asarray(b, np.float64)
-    v0 = a / np.linalg.norm(a, axis=-1, keepdims=True)
-    v1 = b / np.linalg.norm(b, axis=-1, keepdims=True)
-    c = np.sum(v0 * v1, axis=-1)
-    out = np.empty(v0.shape[:-1] + (4,))
-    opp = c < -1.0 + 1e-12
-    s = np.sqrt(np.maximum(2.0 * (1.0 + c), 0.0))
-    with np.errstate(divide="ignore", invalid="ignore"):
-        axis = np.cross(v0, v1) / np.where(opp, 1.0, s)[..., None]
-    out[..., 0] = 0.5 * s
-    out[..., 1:] = axis
-    if np.any(opp):
-        v = v0[opp]
-        # any unit vector perpendicular to v: cross with the least aligned basis vector
-        basis = np.eye(3)[np.argmin(np.abs(v), axis=-1)]
-        perp = np.cross(v, basis)
-        perp /= np.linalg.norm(perp, axis=-1, keepdims=True)
-        out[opp, 0] = 0.0
-        out[opp, 1:] = perp
-    return out
 
 
 def compose(trans, rot):
@@ -108,21 +77,33 @@ def apply_batch(from_state, tr, aa):
 
 # ---------------------------------------------------------------- key configurations
 
-def _touch_states(rob_point, rob_normal, env_point, env_normal, margin, angles):
-    """[P, A, 7] states: robot point + margin·normal on env point + margin·normal,
-    normals opposed, spun by `angles` [P, A] about the env normal
-    (unit_world.cc:1307-1330, 1342-1366)."""
-    rp = np.atleast_2d(np.asarray(rob_point, np.float64))
-    rn = np.atleast_2d(np.asarray(rob_normal, np.float64))
-    ep = np.atleast_2d(np.asarray(env_point, np.float64))
-    en = np.atleast_2d(np.asarray(env_normal, np.float64))
-    rob_o = rp + rn * margin
-    env_o = ep + en * margin
-    rot1 = quat_between(rn, -en)                                     # [P, 4]
-    rot2 = quat_from_angle_axis(angles, en[:, None, :])              # [P, A, 4]
-    acc = quat_mul(rot2, rot1[:, None, :])                           # [P, A, 4]
-    trans = env_o[:, None, :] - quat_rotate(acc, np.broadcast_to(rob_o[:, None, :], acc.shape[:-1] + (3,)))
-    return compose(trans, acc)
+def _pairs_dev(dev, *arrays):
+    return [torch.from_numpy(np.ascontiguousarray(np.atleast_2d(np.asarray(x, np.float64)))).to(dev) for x in arrays]
+
+
+def keyconf_states(uw: UnitWorld, rob_points, rob_normals, env_points, env_normals, margin: float, half_cos,
+                   half_sin) -> torch.Tensor:
+    """Device tensor [P, A, 7] of the candidate states of P surface pairs and A
+    spins (unit_world.cc:1301-1330, 1342-1366): robot point + margin x normal on
+    env point + margin x normal, normals opposed, spun about the env normal by
+    the angle whose half has cosine half_cos and sine half_sin ([A] for every
+    pair, or [P, A])."""
+    dev = uw._device
+    rp, rn, ep, en = _pairs_dev(dev, rob_points, rob_normals, env_points, env_normals)
+    P = rp.shape[0]
+    hc = np.ascontiguousarray(half_cos, dtype=np.float64)
+    hs = np.ascontiguousarray(half_sin, dtype=np.float64)
+    per_pair = hc.ndim == 2
+    if per_pair and hc.shape[0] != P:
+        raise ValueError("half-angle tables must be [A] or [P, A]")
+    A = hc.shape[-1]
+    thc, ths = torch.from_numpy(hc).to(dev), torch.from_numpy(hs).to(dev)
+    out = torch.empty((P, A, 7), dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    _lib.check(uw._L.pw_keyconf_states(rp.data_ptr(), rn.data_ptr(), ep.data_ptr(), en.data_ptr(), P,
+                                       float(margin), thc.data_ptr(), ths.data_ptr(), A, int(per_pair),
+                                       out.data_ptr(), stream), "pw_keyconf_states")
+    return out
 
 
 def enum_free_configurations(uw: UnitWorld, rob_points, rob_normals, env_points, env_normals, margin: float,
@@ -133,19 +114,19 @@ def enum_free_configurations(uw: UnitWorld, rob_points, rob_normals, env_points,
     reference, a run still open at the last spin contributes nothing."""
     if denominator <= 0:
         raise ValueError("denominator must be positive")
-    P = np.atleast_2d(np.asarray(rob_points)).shape[0]
     delta = 2 * math.pi / float(denominator)
-    angles = np.broadcast_to(np.arange(denominator, dtype=np.float64) * delta, (P, denominator))
-    qs = _touch_states(rob_points, rob_normals, env_points, env_normals, margin, angles)
-    flat = torch.from_numpy(np.ascontiguousarray(qs.reshape(-1, 7))).to(uw._device)
-    valid = uw.is_valid_states(flat).cpu().numpy().reshape(P, denominator)
+    half = [0.5 * (i * delta) for i in range(denominator)]      # AngleAxis(i * delta, normal)
+    qs = keyconf_states(uw, rob_points, rob_normals, env_points, env_normals, margin,
+                        [math.cos(h) for h in half], [math.sin(h) for h in half])
+    P = qs.shape[0]
+    valid = uw.is_valid_states(qs.view(-1, 7)).cpu().numpy().reshape(P, denominator)
     return _free_spins(qs, valid, only_median)
 
 
 def _free_spins(qs, valid, only_median):
-    """The free spins of every surface pair ([P, A, 7] states, [P, A] verdicts):
-    all of them, or the middle spin of every run of consecutive free spins that
-    ends before the last spin (unit_world.cc:1367-1386)."""
+    """The free spins of every surface pair ([P, A, 7] states on the device, [P, A]
+    verdicts): all of them, or the middle spin of every run of consecutive free
+    spins that ends before the last spin (unit_world.cc:1367-1386)."""
     P, A = valid.shape
     if not only_median:
         rows, cols = np.nonzero(valid)
@@ -159,7 +140,8 @@ def _free_spins(qs, valid, only_median):
         er, ec = np.nonzero(v & (1 - nxt))             # run ends, in the same order
         keep = ec < A - 1                              # a run still open at the last spin is dropped
         rows, cols = sr[keep], (sc + (ec - sc + 1) // 2)[keep]
-    picked = qs[rows, cols]
+    idx = torch.from_numpy((rows * A + cols).astype(np.int64)).to(qs.device)
+    picked = qs.reshape(-1, 7).index_select(0, idx).cpu().numpy()
     bounds = np.searchsorted(rows, np.arange(P + 1))
     return [picked[bounds[p]:bounds[p + 1]] if bounds[p + 1] > bounds[p] else np.zeros((0, 7)) for p in range(P)]
 
@@ -183,13 +165,13 @@ def sample_free_configurations(uw: UnitWorld, rob_points, rob_normals, env_point
     rng = np.random.default_rng() if rng is None else rng
     P = np.atleast_2d(np.asarray(rob_points)).shape[0]
     A = max_trials + 1
-    angles = rng.uniform(0.0, 2 * math.pi, (P, A))
-    qs = _touch_states(rob_points, rob_normals, env_points, env_normals, margin, angles)
-    flat = torch.from_numpy(np.ascontiguousarray(qs.reshape(-1, 7))).to(uw._device)
-    valid = uw.is_valid_states(flat).cpu().numpy().reshape(P, A)
+    half = 0.5 * rng.uniform(0.0, 2 * math.pi, (P, A))
+    qs = keyconf_states(uw, rob_points, rob_normals, env_points, env_normals, margin, np.cos(half), np.sin(half))
+    valid = uw.is_valid_states(qs.view(-1, 7)).cpu().numpy().reshape(P, A)
     found = valid.any(axis=1)
     first = np.where(found, np.argmax(valid, axis=1), A - 1)
-    return qs[np.arange(P), first], found
+    idx = torch.from_numpy((np.arange(P) * A + first).astype(np.int64)).to(qs.device)
+    return qs.view(-1, 7).index_select(0, idx).cpu().numpy(), found
 
 
 def sample_free_configuration(uw: UnitWorld, rob_surface_point, rob_surface_normal, env_surface_point,
@@ -225,40 +207,44 @@ def random_within_sphere(n, scale=1.0, rng=None):
     return out[:n] * scale
 
 
+def touch_segments(uw: UnitWorld, keys, per_key: int, seed: int):
+    """Device tensors (from, to) [K * per_key, 7] of the random segments of
+    touchq_util.calc_touch for K keys: row i * per_key + j goes from key i to
+    the key translated by a random point of the unit sphere and rotated on the
+    left by a rotation vector uniform in the ball of radius 2 pi (osr::apply)."""
+    dev = uw._device
+    k = torch.from_numpy(np.ascontiguousarray(np.atleast_2d(np.asarray(keys, np.float64)))).to(dev)
+    n = k.shape[0] * per_key
+    frm = torch.empty((n, 7), dtype=torch.float64, device=dev)
+    to = torch.empty((n, 7), dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    _lib.check(uw._L.pw_touch_targets(k.data_ptr(), k.shape[0], int(per_key), int(seed) & (2 ** 64 - 1),
+                                      frm.data_ptr(), to.data_ptr(), stream), "pw_touch_targets")
+    return frm, to
+
+
+def _seed(rng):
+    rng = np.random.default_rng() if rng is None else rng
+    return int(rng.integers(0, 2 ** 63))
+
+
 def calc_touch(uw: UnitWorld, q0, batch_size: int, stepping: float, rng=None):
     """touchq_util.calc_touch: batch_size random segments from q0 (unit
-    translation on the sphere, rotation uniform within 2π), each stepped to its
+    translation on the sphere, rotation uniform within 2 pi), each stepped to its
     first contact.  Returns the reference's five arrays: last free states
     [B, 7], contact states [B, 7], done [B], last_tau [B], tau [B]."""
-    tr = random_on_sphere(batch_size, 1.0, rng)
-    aa = random_within_sphere(batch_size, 2 * math.pi, rng)
-    to = apply_batch(q0, tr, aa)
-    q0s = np.broadcast_to(np.asarray(q0, np.float64).reshape(1, 7), (batch_size, 7))
-    dev = uw._device
-    a = torch.from_numpy(np.ascontiguousarray(q0s)).to(dev)
-    b = torch.from_numpy(np.ascontiguousarray(to)).to(dev)
-    lf, st, done, lt, tt = uw.transit_states_to_with_contact(a, b, stepping)
-    return [lf.cpu().numpy(), st.cpu().numpy(), done.cpu().numpy(), lt.cpu().numpy(), tt.cpu().numpy()]
+    res, _ = calc_touch_batch(uw, np.asarray(q0, np.float64).reshape(1, 7), batch_size, stepping, rng)
+    return res
 
 
 def calc_touch_batch(uw: UnitWorld, keys, per_key: int, stepping: float, rng=None):
     """calc_touch for K keys at once (the loop over keys of keyconf.py:306-316 and
-    preprocess_key.py:174): per_key random segments from every key (translation
-    on the unit sphere, rotation uniform within 2π, drawn for all keys in one
-    go), all stepped to their first contact in one batch.  Row i * per_key + j
-    of the five arrays belongs to key i.  Returns (the five arrays, the
-    segments' end states)."""
-    keys = np.atleast_2d(np.asarray(keys, np.float64))
-    rng = np.random.default_rng() if rng is None else rng
-    K = keys.shape[0]
-    frm = np.repeat(keys, per_key, axis=0)
-    tr = random_on_sphere(K * per_key, 1.0, rng)
-    aa = random_within_sphere(K * per_key, 2 * math.pi, rng)
-    to = apply_rows(frm, tr, aa)
-    dev = uw._device
-    a = torch.from_numpy(frm).to(dev)
-    b = torch.from_numpy(to).to(dev)
-    lf, st, done, lt, tt = uw.transit_states_to_with_contact(a, b, stepping)
+    preprocess_key.py:174): per_key random segments from every key, drawn on the
+    device (``touch_segments``, seeded from rng), all stepped to their first
+    contact in one batch.  Row i * per_key + j of the five arrays belongs to key
+    i.  Returns (the five arrays, the segments' end states as a device tensor)."""
+    frm, to = touch_segments(uw, keys, per_key, _seed(rng))
+    lf, st, done, lt, tt = uw.transit_states_to_with_contact(frm, to, stepping)
     return [lf.cpu().numpy(), st.cpu().numpy(), done.cpu().numpy(), lt.cpu().numpy(), tt.cpu().numpy()], to
 
 

@@ -47,14 +47,37 @@ def test_calc_touch_matches_oracle(tori):
     uw, ow = tori
     q0 = np.array([0.0, 0.0, 0.5, 1.0, 0.0, 0.0, 0.0])   # free: the robot ring above the env ring
     assert uw.is_valid_state(q0)
-    rng = np.random.default_rng(7)
-    lf, st, done, lt, tt = S.calc_touch(uw, q0, 256, 0.01, rng)
-    rng = np.random.default_rng(7)
-    to = S.apply_batch(q0, S.random_on_sphere(256, 1.0, rng), S.random_within_sphere(256, 2 * math.pi, rng))
+    (lf, st, done, lt, tt), to = S.calc_touch_batch(uw, q0[None], 256, 0.01, np.random.default_rng(7))
+    to = to.cpu().numpy()
     assert done.sum() < 256 and done.sum() > 0
     for i in range(256):
         want, _, _ = ow.transit_state_to_with_contact(q0, to[i], 0.01)
         _same_tuple((lf[i], st[i], bool(done[i]), lt[i], tt[i]), want)
+    # the same rng state gives the same segments; calc_touch is calc_touch_batch of one key
+    again = S.calc_touch(uw, q0, 256, 0.01, np.random.default_rng(7))
+    assert all(np.array_equal(x, y) for x, y in zip(again, (lf, st, done, lt, tt)))
+
+
+def test_touch_targets_follow_apply(tori):
+    """pw_touch_targets: unit translations, rotations of angle <= 2 pi applied on the
+    left (osr::apply), unit quaternions; from rows repeat their key."""
+    from puzzletunneldiscovery_gb300 import sampling as S
+    uw, _ = tori
+    keys = W.uniform_states(50, -1.0, 1.0, uw.scene_scale, seed=5)
+    frm, to = S.touch_segments(uw, keys, 400, 99)
+    frm, to = frm.cpu().numpy(), to.cpu().numpy()
+    assert np.array_equal(frm, np.repeat(keys, 400, axis=0))
+    d = to[:, :3] - frm[:, :3]
+    assert np.allclose(np.linalg.norm(d, axis=1), 1.0, atol=1e-6)
+    assert abs(d.mean(axis=0)).max() < 0.05
+    assert np.allclose(np.linalg.norm(to[:, 3:], axis=1), 1.0, atol=1e-15)
+    # the left rotation r = to_rot * from_rot^-1 has angle 2 acos|w| uniform-in-ball distributed
+    fr, tr = frm[:, 3:], to[:, 3:]
+    w = np.abs(np.sum(tr * fr * np.array([1, 1, 1, 1]), axis=1))       # |<to, from>| = |cos(angle / 2)|
+    ang = 2 * np.arccos(np.clip(w, 0, 1))
+    assert ang.max() <= math.pi + 1e-6 and np.median(ang) > 1.0
+    f2, t2 = S.touch_segments(uw, keys, 400, 99)
+    assert np.array_equal(t2.cpu().numpy(), to)
 
 
 def test_enum_free_configuration_verdicts_match_oracle(tori):
@@ -70,14 +93,34 @@ def test_enum_free_configuration_verdicts_match_oracle(tori):
     rn = rng.normal(size=(P, 3))
     en /= np.linalg.norm(en, axis=1, keepdims=True)
     rn /= np.linalg.norm(rn, axis=1, keepdims=True)
+    en[0] = rn[0]                          # the half-turn branch of the shortest arc
     got = S.enum_free_configurations(uw, rp, rn, ep, en, 1e-3, D)
-    qs = S._touch_states(rp, rn, ep, en, 1e-3, np.broadcast_to(np.arange(D) * (2 * math.pi / D), (P, D)))
+    half = [0.5 * (i * (2 * math.pi / D)) for i in range(D)]
+    hc, hs = [math.cos(h) for h in half], [math.sin(h) for h in half]
+    qs = oracle_mod_keyconf(ow)(rp, rn, ep, en, 1e-3, hc, hs)
+    # the device's states are the oracle's, bit for bit
+    assert np.array_equal(S.keyconf_states(uw, rp, rn, ep, en, 1e-3, hc, hs).cpu().numpy(), qs)
     valid = ow.is_valid(qs.reshape(-1, 7)).reshape(P, D)
     assert 0 < valid.sum() < P * D
     for p in range(P):
         assert np.array_equal(got[p], qs[p][valid[p]])
+    med = S.enum_free_configurations(uw, rp, rn, ep, en, 1e-3, D, only_median=True)
+    from oracle import oracle as O
+    assert all(np.array_equal(x, y) for x, y in zip(med, O.free_spins(qs, valid, True)))
     q, found = S.sample_free_configurations(uw, rp, rn, ep, en, 1e-3, max_trials=15, rng=np.random.default_rng(2))
     assert ow.is_valid(q[found]).all()
+    # the random spins of sampleFreeConfiguration: first free spin, or the last one tried
+    rng = np.random.default_rng(2)
+    h = 0.5 * rng.uniform(0.0, 2 * math.pi, (P, 16))
+    qs2 = O.keyconf_states(rp, rn, ep, en, 1e-3, np.cos(h), np.sin(h))
+    v2 = ow.is_valid(qs2.reshape(-1, 7)).reshape(P, 16)
+    first = np.where(v2.any(axis=1), np.argmax(v2, axis=1), 15)
+    assert np.array_equal(q, qs2[np.arange(P), first]) and np.array_equal(found, v2.any(axis=1))
+
+
+def oracle_mod_keyconf(ow):
+    from oracle import oracle as O
+    return O.keyconf_states
 
 
 def test_checkpointed_transit_tuples_equal_full_loop(tori):

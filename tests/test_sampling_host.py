@@ -1,5 +1,5 @@
-"""Host logic of the batched samplers (puzzletunneldiscovery_gb300/sampling.py),
-on the CPU with a stand-in world whose verdicts are scripted."""
+"""Host logic of the batched samplers (puzzletunneldiscovery_gb300/sampling.py)
+and the oracle's key-configuration states, on the CPU."""
 import math
 
 import numpy as np
@@ -8,85 +8,66 @@ import torch
 from conftest import ROOT  # noqa: F401
 
 
-class ScriptedWorld:
-    """Answers is_valid_states from a fixed pattern, in call order."""
-
-    def __init__(self, pattern):
-        self.pattern = np.asarray(pattern, bool).ravel()
-        self._device = torch.device("cpu")
-        self.calls = []
-
-    def is_valid_states(self, q):
-        self.calls.append(q.shape[0])
-        assert q.shape[0] == self.pattern.shape[0]
-        return torch.from_numpy(self.pattern.copy())
-
-
 def _S():
     from puzzletunneldiscovery_gb300 import sampling
     return sampling
 
 
-def test_quat_between_and_rotate():
-    S = _S()
-    rng = np.random.default_rng(0)
-    a = rng.normal(size=(100, 3))
-    b = rng.normal(size=(100, 3))
-    b[0] = -a[0]                     # opposite directions
-    b[1] = 2.0 * a[1]                # same direction
-    q = S.quat_between(a, b)
-    assert np.allclose(np.linalg.norm(q, axis=1), 1.0)
-    ra = S.quat_rotate(q, a / np.linalg.norm(a, axis=1, keepdims=True))
-    assert np.allclose(ra, b / np.linalg.norm(b, axis=1, keepdims=True), atol=1e-12)
+def _rotate(q, v):
+    w, u = q[0], q[1:]
+    t = 2.0 * np.cross(u, v)
+    return v + w * t + np.cross(u, t)
 
 
-def test_touch_states_place_points_with_opposed_normals():
-    S = _S()
+def _half(angles):
+    h = 0.5 * np.asarray(angles, np.float64)
+    return np.cos(h), np.sin(h)
+
+
+def test_keyconf_states_place_points_with_opposed_normals(oracle_mod):
+    """The oracle's key-configuration states (unit_world.cc:1301-1330): the robot
+    point + margin x normal lands on the env point + margin x normal, the robot
+    normal turns into the opposed env normal; opposite and equal normals
+    included (the half-turn branch of the shortest arc)."""
     rng = np.random.default_rng(1)
-    P, A = 5, 7
+    P, A = 6, 7
     rp, ep = rng.normal(size=(P, 3)), rng.normal(size=(P, 3))
     rn = rng.normal(size=(P, 3))
     en = rng.normal(size=(P, 3))
     rn /= np.linalg.norm(rn, axis=1, keepdims=True)
     en /= np.linalg.norm(en, axis=1, keepdims=True)
-    ang = rng.uniform(0, 2 * math.pi, (P, A))
-    qs = S._touch_states(rp, rn, ep, en, 0.01, ang)
+    en[0] = -rn[0]                   # normals opposed already: the identity arc
+    en[1] = rn[1]                    # equal normals: a half turn
+    hc, hs = _half(rng.uniform(0, 2 * math.pi, (P, A)))
+    qs = oracle_mod.keyconf_states(rp, rn, ep, en, 0.01, hc, hs)
+    assert qs.shape == (P, A, 7)
     for p in range(P):
         for i in range(A):
             q = qs[p, i]
-            rob_o = rp[p] + 0.01 * rn[p]
-            placed = S.quat_rotate(q[3:], rob_o) + q[:3]
+            assert abs(np.linalg.norm(q[3:]) - 1.0) < 1e-15
+            placed = _rotate(q[3:], rp[p] + 0.01 * rn[p]) + q[:3]
             assert np.allclose(placed, ep[p] + 0.01 * en[p], atol=1e-12)
-            assert np.allclose(S.quat_rotate(q[3:], rn[p]), -en[p], atol=1e-12)
+            assert np.allclose(_rotate(q[3:], rn[p]), -en[p], atol=1e-12)
+    # the shared spin table gives the per-pair table's states when every row repeats it
+    hc1, hs1 = _half(np.arange(A) * (2 * math.pi / A))
+    a = oracle_mod.keyconf_states(rp, rn, ep, en, 0.01, hc1, hs1)
+    b = oracle_mod.keyconf_states(rp, rn, ep, en, 0.01, np.tile(hc1, (P, 1)), np.tile(hs1, (P, 1)))
+    assert np.array_equal(a, b)
 
 
-def test_enum_free_configuration_median_runs():
-    S = _S()
-    # runs of free spins: [1..3] -> 2, [5] -> 5, trailing [8, 9] is not reported (reference quirk)
-    pattern = np.array([0, 1, 1, 1, 0, 1, 0, 0, 1, 1], bool)
-    uw = ScriptedWorld(pattern)
-    z = np.zeros(3)
-    n = np.array([0.0, 0.0, 1.0])
-    all_free = S.enum_free_configuration(uw, z, n, z, n, 0.0, 10, only_median=False)
-    assert all_free.shape == (6, 7)
-    med = S.enum_free_configuration(uw, z, n, z, n, 0.0, 10, only_median=True)
-    qs = S._touch_states(z, n, z, n, 0.0, (np.arange(10) * (2 * math.pi / 10))[None, :])[0]
-    assert np.array_equal(med, qs[[2, 5]])
-
-
-def test_sample_free_configuration_first_free_or_last_tried():
-    S = _S()
-    pattern = np.array([[0, 0, 1, 1], [0, 0, 0, 0]], bool)
-    uw = ScriptedWorld(pattern)
-    pts = np.zeros((2, 3))
-    nrm = np.tile([0.0, 1.0, 0.0], (2, 1))
-    rng = np.random.default_rng(3)
-    q, found = S.sample_free_configurations(uw, pts, nrm, pts, nrm, 0.0, max_trials=3, rng=rng)
-    assert list(found) == [True, False]
-    rng = np.random.default_rng(3)
-    ang = rng.uniform(0.0, 2 * math.pi, (2, 4))
-    qs = S._touch_states(pts, nrm, pts, nrm, 0.0, ang)
-    assert np.array_equal(q[0], qs[0, 2]) and np.array_equal(q[1], qs[1, 3])
+def test_free_spins_on_device_style_tensors(oracle_mod):
+    """_free_spins takes the states as a tensor [P, A, 7] and gathers the picks by
+    index; the picks equal the oracle's restatement of the reference loop."""
+    from puzzletunneldiscovery_gb300 import sampling as S
+    rng = np.random.default_rng(2)
+    for _ in range(50):
+        P, A = int(rng.integers(1, 12)), int(rng.integers(1, 30))
+        valid = rng.random((P, A)) < rng.random()
+        qs = rng.random((P, A, 7))
+        for med in (False, True):
+            got = S._free_spins(torch.from_numpy(qs), valid, med)
+            want = oracle_mod.free_spins(qs, valid, med)
+            assert all(np.array_equal(x, y) for x, y in zip(got, want))
 
 
 def test_apply_batch_matches_single_apply():
@@ -168,8 +149,9 @@ def test_free_spins_follow_the_run_median_rule():
         P, D = int(rng.integers(1, 20)), int(rng.integers(1, 40))
         valid = rng.random((P, D)) < rng.random()
         qs = rng.random((P, D, 7))
-        assert all(np.array_equal(x, y) for x, y in zip(loop(qs, valid), S._free_spins(qs, valid, True)))
-        assert all(np.array_equal(qs[p][valid[p]], r) for p, r in enumerate(S._free_spins(qs, valid, False)))
+        t = torch.from_numpy(qs)
+        assert all(np.array_equal(x, y) for x, y in zip(loop(qs, valid), S._free_spins(t, valid, True)))
+        assert all(np.array_equal(qs[p][valid[p]], r) for p, r in enumerate(S._free_spins(t, valid, False)))
 
 
 def test_apply_rows_matches_apply_batch():
