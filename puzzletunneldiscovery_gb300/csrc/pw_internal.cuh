@@ -96,6 +96,15 @@ struct DeviceBuffer {
 	~DeviceBuffer() { release(); }
 };
 
+// Page-locked host memory (staging of device-to-host copies).
+struct PinnedBuffer {
+	void *ptr = nullptr;
+	size_t bytes = 0;
+	cudaError_t reserve(size_t need);
+	void release();
+	~PinnedBuffer() { release(); }
+};
+
 struct pw_world {
 	int device = 0;
 	bool has_env = false, has_rob = false, scaled = false, ready = false;
@@ -117,6 +126,7 @@ struct pw_world {
 	uint64_t retest_cap = 0;
 	DeviceBuffer seg_params, seg_ckpt, seg_anchor, seg_keys, seg_order, seg_keys2, seg_order2, round_off, cub_tmp, misc;
 	DeviceBuffer isect;        // contact enumeration (candidates, rows, sort keys, output columns)
+	PinnedBuffer isect_stage;  // two halves: one chunk's output columns on their way to the caller
 	cudaStream_t last_stream = nullptr;
 	cudaEvent_t ev[4] = { nullptr, nullptr, nullptr, nullptr }; // traversal start/end, re-test start/end
 	bool timed = false;

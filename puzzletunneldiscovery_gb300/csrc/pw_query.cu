@@ -23,6 +23,8 @@
 #include <climits>
 #include <cstring>
 #include <mutex>
+#include <thread>
+#include <vector>
 
 #include "pw_internal.cuh"
 #include "pw_math.cuh"
@@ -1848,6 +1850,48 @@ static int isect_scratch(pw_world *w, IsectScratch &S)
 	return PW_OK;
 }
 
+// Host copies split over threads: a large result's first touch of the
+// caller's fresh pages (its page faults) is what these copies cost, and the
+// faults of different threads proceed in parallel.
+struct HostCopy {
+	void *dst;
+	const void *src;
+	size_t bytes;
+};
+static void parallel_copy(const std::vector<HostCopy> &jobs)
+{
+	size_t total = 0;
+	for (const HostCopy &j : jobs)
+		total += j.bytes;
+	const unsigned hw = std::thread::hardware_concurrency();
+	const unsigned T = (unsigned)std::max<size_t>(1, std::min<size_t>({ (size_t)(hw ? hw : 1), (size_t)16,
+	                                                                    total / (size_t(4) << 20) }));
+	if (T <= 1) {
+		for (const HostCopy &j : jobs)
+			if (j.bytes)
+				memcpy(j.dst, j.src, j.bytes);
+		return;
+	}
+	// thread t copies bytes [t * per, (t + 1) * per) of the jobs laid end to end
+	const size_t per = (total + T - 1) / T;
+	auto work = [&jobs, per](unsigned t) {
+		size_t lo = t * per, hi = lo + per, at = 0;
+		for (const HostCopy &j : jobs) {
+			const size_t a = std::max(lo, at), b = std::min(hi, at + j.bytes);
+			if (a < b)
+				memcpy((char *)j.dst + (a - at), (const char *)j.src + (a - at), b - a);
+			at += j.bytes;
+		}
+	};
+	std::vector<std::thread> th;
+	th.reserve(T - 1);
+	for (unsigned t = 1; t < T; t++)
+		th.emplace_back(work, t);
+	work(0);
+	for (std::thread &x : th)
+		x.join();
+}
+
 static int bits_for(int64_t count) // bits of the largest index below count
 {
 	int b = 1;
@@ -1884,6 +1928,11 @@ static int isect_run(pw_world *w, const double *q, int64_t n, int64_t capacity, 
 	std::vector<int64_t> ends_h;
 	int64_t chunk = std::min<int64_t>(n, ISECT_BATCH_CHUNK), base = 0;
 	unsigned long long launches = 0, tested = 0;
+	// a chunk's output columns go to one half of the pinned stage; their copy into the
+	// caller's arrays runs while the next chunk's candidates are collected
+	constexpr size_t ROW_BYTES = 7 * sizeof(double) + 3 * sizeof(int32_t);
+	std::vector<HostCopy> pending;
+	int half = 0;
 	for (int64_t s0 = 0; s0 < n;) {
 		const int64_t m = std::min(chunk, n - s0);
 		PW_CUDA(cudaMemcpy(S.q, q + 7 * s0, sizeof(double) * 7 * (size_t)m, cudaMemcpyHostToDevice));
@@ -1893,6 +1942,8 @@ static int isect_run(pw_world *w, const double *q, int64_t n, int64_t capacity, 
 		                                                 soft_cap_of(w));
 		PW_CUDA(cudaGetLastError());
 		launches++;
+		parallel_copy(pending);
+		pending.clear();
 		unsigned long long c[2];
 		PW_CUDA(cudaMemcpy(c, S.ctr, sizeof(c), cudaMemcpyDeviceToHost));
 		if (c[0] > ISECT_BATCH_CAP) {
@@ -1942,12 +1993,32 @@ static int isect_run(pw_world *w, const double *q, int64_t n, int64_t capacity, 
 			k_isect_gather<<<egrid, 256>>>(S.rows, order, S.ctr + 1, S.b, S.e, S.mag, S.fp, S.cop);
 			PW_CUDA(cudaGetLastError());
 			launches += 2;
-			PW_CUDA(cudaMemcpy(begins + 3 * base, S.b, sizeof(double) * 3 * (size_t)nr, cudaMemcpyDeviceToHost));
-			PW_CUDA(cudaMemcpy(ends + 3 * base, S.e, sizeof(double) * 3 * (size_t)nr, cudaMemcpyDeviceToHost));
-			PW_CUDA(cudaMemcpy(mags + base, S.mag, sizeof(double) * (size_t)nr, cudaMemcpyDeviceToHost));
-			PW_CUDA(cudaMemcpy(face_pairs + 2 * base, S.fp, sizeof(int32_t) * 2 * (size_t)nr, cudaMemcpyDeviceToHost));
-			if (coplanar)
-				PW_CUDA(cudaMemcpy(coplanar + base, S.cop, sizeof(int32_t) * (size_t)nr, cudaMemcpyDeviceToHost));
+			// the columns, back to back in this chunk's half of the stage
+			const size_t cb[5] = { sizeof(double) * 3 * (size_t)nr, sizeof(double) * 3 * (size_t)nr,
+				                   sizeof(double) * (size_t)nr, sizeof(int32_t) * 2 * (size_t)nr,
+				                   sizeof(int32_t) * (size_t)nr };
+			const void *from[5] = { S.b, S.e, S.mag, S.fp, S.cop };
+			void *to[5] = { begins + 3 * base, ends + 3 * base, mags + base, face_pairs + 2 * base,
+				            coplanar ? (void *)(coplanar + base) : nullptr };
+			const size_t need = ROW_BYTES * (size_t)nr;
+			if (w->isect_stage.bytes < 2 * need) {
+				// a larger stage: the copies still pending read the old one
+				parallel_copy(pending);
+				pending.clear();
+				PW_CUDA(w->isect_stage.reserve(2 * (need + need / 4)));
+			}
+			const size_t half_bytes = w->isect_stage.bytes / 2;
+			char *stage = (char *)w->isect_stage.ptr + half * half_bytes;
+			size_t at = 0;
+			for (int k = 0; k < 5; k++) {
+				if (!to[k])
+					continue;
+				PW_CUDA(cudaMemcpyAsync(stage + at, from[k], cb[k], cudaMemcpyDeviceToHost, 0));
+				pending.push_back(HostCopy{ to[k], stage + at, cb[k] });
+				at += cb[k];
+			}
+			PW_CUDA(cudaStreamSynchronize(0));
+			half ^= 1;
 		}
 		base += nr;
 		s0 += m;
@@ -1957,6 +2028,7 @@ static int isect_run(pw_world *w, const double *q, int64_t n, int64_t capacity, 
 		else
 			chunk = ISECT_BATCH_CHUNK;
 	}
+	parallel_copy(pending);
 	*total = base;
 	// the figures pw_world_last_stats reports for this query
 	if ((rc = ensure_query_scratch(w)))

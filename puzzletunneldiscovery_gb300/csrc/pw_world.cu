@@ -59,6 +59,30 @@ void DeviceBuffer::release()
 	bytes = 0;
 }
 
+cudaError_t PinnedBuffer::reserve(size_t need)
+{
+	if (need <= bytes && ptr)
+		return cudaSuccess;
+	release();
+	size_t n = need < 4096 ? 4096 : need;
+	cudaError_t e = cudaMallocHost(&ptr, n);
+	if (e != cudaSuccess) {
+		ptr = nullptr;
+		bytes = 0;
+		return e;
+	}
+	bytes = n;
+	return cudaSuccess;
+}
+
+void PinnedBuffer::release()
+{
+	if (ptr)
+		cudaFreeHost(ptr);
+	ptr = nullptr;
+	bytes = 0;
+}
+
 extern "C" const char *pw_last_error(void) { return g_last_error.c_str(); }
 
 // ------------------------------------------------------------------ life cycle

@@ -11,6 +11,7 @@ Every query goes through libpwcollide.so; there is no CPU path.
 """
 from __future__ import annotations
 
+import collections.abc
 import ctypes
 import math
 
@@ -51,6 +52,31 @@ def _strict_tril_pairs(k: torch.Tensor):
     r = torch.where(r * (r - 1) // 2 > k, r - 1, r)
     r = torch.where((r + 1) * r // 2 <= k, r + 1, r)
     return r, k - r * (r - 1) // 2
+
+
+class ContactRows(collections.abc.Sequence):
+    """The per-state rows of a batched contact enumeration: item i is state i's
+    tuple (begins [m, 3], ends [m, 3], lengths [m], face pairs [m, 2]), views into
+    the batch's arrays."""
+
+    def __init__(self, begins, ends, lengths, face_pairs, offsets):
+        self.begins, self.ends, self.lengths, self.face_pairs = begins, ends, lengths, face_pairs
+        self.offsets = offsets
+
+    def __len__(self):
+        return self.offsets.shape[0] - 1
+
+    def __getitem__(self, i):
+        if isinstance(i, slice):
+            return [self[j] for j in range(*i.indices(len(self)))]
+        n = len(self)
+        i = int(i)
+        if i < 0:
+            i += n
+        if not 0 <= i < n:
+            raise IndexError("state index out of range")
+        o0, o1 = int(self.offsets[i]), int(self.offsets[i + 1])
+        return self.begins[o0:o1], self.ends[o0:o1], self.lengths[o0:o1], self.face_pairs[o0:o1]
 
 
 class UnitWorld:
@@ -668,11 +694,12 @@ class UnitWorld:
             return b[:n].copy(), e[:n].copy(), m[:n].copy(), p[:n].copy()
 
     def intersecting_segments_batch(self, unitqs, flat: bool = False):
-        """intersecting_segments for many unit states in one call: a list of the
-        per-state tuples (begins, ends, lengths, face pairs), each as
-        intersecting_segments returns it (views into one set of arrays).  With
-        flat=True: (begins, ends, lengths, face pairs, offsets), the rows of
-        state i at offsets[i]:offsets[i + 1]."""
+        """intersecting_segments for many unit states in one call: a sequence
+        (ContactRows) whose item i is state i's tuple (begins, ends, lengths,
+        face pairs) as intersecting_segments returns it (views into one set of
+        arrays, made when the item is read).  With flat=True: (begins, ends,
+        lengths, face pairs, offsets), the rows of state i at
+        offsets[i]:offsets[i + 1]."""
         q = _states_np(unitqs)
         n = q.shape[0]
         offsets = np.zeros(n + 1, dtype=np.int64)
@@ -699,7 +726,7 @@ class UnitWorld:
         b, e, m, p = b[:t], e[:t], m[:t], p[:t]
         if flat:
             return b, e, m, p, offsets
-        return [(b[o0:o1], e[o0:o1], m[o0:o1], p[o0:o1]) for o0, o1 in zip(offsets[:-1], offsets[1:])]
+        return ContactRows(b, e, m, p, offsets)
 
     # contact forces (unit_world.cc:1015-1057) ---------------------------------
     def _face_normals(self, geo):
