@@ -373,4 +373,97 @@ PW_HD int tri_filter(float3 V0, float3 e1, float3 e2, float3 x0, float3 g1, floa
 }
 
 
+// ---------------------------------------------------------------- isDisentangled in FP32
+//
+// UnitWorld::isDisentangled (unit_world.cc:249-264, CDModel::collideBB,
+// cdmodel.cc:180-197): the robot's bounding box (centre rc, half-extents rh,
+// robot frame) placed by the state against the environment's box (ec, eh)
+// placed by the perturbation (Re, te); pwm::boxes_disjoint computes it in FP64.
+// Here the same separating-axis test runs in FP32 with one error bound e for
+// all 15 axes:
+//   1  (disjoint) if some axis has  |tl| - (ra + rb) >  e,
+//   0  (overlap)  if every axis has |tl| - (ra + rb) < -e,
+//   -1 otherwise: the FP64 test decides.
+// e bounds |g32 - g| + |g64 - g| for every axis value g (exact), g32 (this
+// code), g64 (the FP64 test).  R is the rotation formula on the state's raw
+// quaternion (as the FP64 test and Eigen's toRotationMatrix apply it, unit or
+// not), so its entries are bounded by K = max(1, 2 |q|^2).  With u = 2^-24, the
+// entrywise error of R is at most 10 K u (the rounded coefficients and the
+// quadratic entries), of d = R rc + t - ce at most (10 K + 6) u (|rc|_1 +
+// |t|_inf + |ce|_inf + |d|_inf), of T = Re^T d at most 2 eps_d + 4u |d|_1, of
+// Re^T R at most (20 K + 5) u; the axis values are sums of at most six such
+// terms weighted by |T|_inf <= |d|_1, the extents and K, so
+// e = 1100u K (|rc|_1 + |t|_inf + |ce|_inf + 2 |d|_1 + sum eh + sum rh) covers
+// the FP32 side with a factor above 1.5 and the FP64 side (the same sums at
+// 2^-53) many times over.  tests/harness/disentangled_bounds.cc checks it
+// against pwm::boxes_disjoint near the boundary (slack scales e; the kernels
+// use 1, the harness also runs 0 to show that the check has teeth).
+struct DisBoxes32 {
+	float rc[3], rh[3];    // robot box (robot frame)
+	float Re[9];           // perturbation rotation (row-major)
+	float ce[3];           // env box centre placed by the perturbation, Re ec + te (FP64, rounded)
+	float eh[3];           // env box half-extents
+	float ce_abs;          // |ce|_inf, rounded up
+};
+
+PW_HD int boxes_disjoint32(const double *q, const DisBoxes32 &B, float slack = 1.f)
+{
+	const float w = (float)q[3], x = (float)q[4], y = (float)q[5], z = (float)q[6];
+	const float n2 = ((w * w + x * x) + y * y) + z * z;
+	if (!(n2 < 1.0e30f))
+		return -1;                           // not finite or huge: the FP64 test decides
+	const float K = fmaxf(1.f, 2.f * n2) * (1.f + 8.f * U32);
+	const float R[9] = { 1.f - 2.f * (y * y + z * z), 2.f * (x * y - w * z), 2.f * (x * z + w * y),
+		                 2.f * (x * y + w * z), 1.f - 2.f * (x * x + z * z), 2.f * (y * z - w * x),
+		                 2.f * (x * z - w * y), 2.f * (y * z + w * x), 1.f - 2.f * (x * x + y * y) };
+	const float t[3] = { (float)q[0], (float)q[1], (float)q[2] };
+	float d[3];
+	for (int k = 0; k < 3; k++)
+		d[k] = ((R[3 * k] * B.rc[0] + R[3 * k + 1] * B.rc[1]) + R[3 * k + 2] * B.rc[2] + t[k]) - B.ce[k];
+	float T[3], Rr[9], AR[9];
+	for (int i = 0; i < 3; i++) {
+		T[i] = (B.Re[i] * d[0] + B.Re[3 + i] * d[1]) + B.Re[6 + i] * d[2];
+		for (int j = 0; j < 3; j++) {
+			Rr[3 * i + j] = (B.Re[i] * R[j] + B.Re[3 + i] * R[3 + j]) + B.Re[6 + i] * R[6 + j];
+			AR[3 * i + j] = fabsf(Rr[3 * i + j]);
+		}
+	}
+	const float d1 = (fabsf(d[0]) + fabsf(d[1])) + fabsf(d[2]);
+	const float tinf = fmaxf(fmaxf(fabsf(t[0]), fabsf(t[1])), fabsf(t[2]));
+	const float scale = ((fabsf(B.rc[0]) + fabsf(B.rc[1])) + fabsf(B.rc[2])) + tinf + B.ce_abs + 2.f * d1 +
+	                    ((B.eh[0] + B.eh[1]) + B.eh[2]) + ((B.rh[0] + B.rh[1]) + B.rh[2]);
+	const float e = slack * (1100.f * U32 * K * scale);
+	if (!(e < 1.0e30f))
+		return -1;                           // not finite: the FP64 test decides
+	bool undecided = false;
+	auto axis = [&](float g) {
+		if (g > e)
+			return true;
+		if (!(g < -e))
+			undecided = true;
+		return false;
+	};
+	for (int i = 0; i < 3; i++)
+		if (axis(fabsf(T[i]) - (B.eh[i] + ((B.rh[0] * AR[3 * i] + B.rh[1] * AR[3 * i + 1]) + B.rh[2] * AR[3 * i + 2]))))
+			return 1;
+	for (int j = 0; j < 3; j++) {
+		const float tl = (T[0] * Rr[j] + T[1] * Rr[3 + j]) + T[2] * Rr[6 + j];
+		const float ra = (B.eh[0] * AR[j] + B.eh[1] * AR[3 + j]) + B.eh[2] * AR[6 + j];
+		if (axis(fabsf(tl) - (ra + B.rh[j])))
+			return 1;
+	}
+	for (int i = 0; i < 3; i++) {
+		const int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+		for (int j = 0; j < 3; j++) {
+			const int j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+			const float tl = T[i2] * Rr[3 * i1 + j] - T[i1] * Rr[3 * i2 + j];
+			const float ra = B.eh[i1] * AR[3 * i2 + j] + B.eh[i2] * AR[3 * i1 + j];
+			const float rb = B.rh[j1] * AR[3 * i + j2] + B.rh[j2] * AR[3 * i + j1];
+			if (axis(fabsf(tl) - (ra + rb)))
+				return 1;
+		}
+	}
+	return undecided ? -1 : 0;
+}
+
 } // namespace pwf

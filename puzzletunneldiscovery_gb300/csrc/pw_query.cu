@@ -705,14 +705,38 @@ struct BoxParams {
 	double rc[3], rh[3], Re[9], te[3], ec[3], eh[3];
 };
 
-__global__ void k_disentangled(BoxParams B, const double *states, int64_t n, uint8_t *out)
+// The FP32 test decides almost every state; the rest take the FP64 test.
+__global__ void k_disentangled(BoxParams B, pwf::DisBoxes32 B32, const double *states, int64_t n, uint8_t *out)
 {
 	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
 		double q[7];
 		for (int k = 0; k < 7; k++)
 			q[k] = states[7 * i + k];
-		out[i] = (uint8_t)pwm::boxes_disjoint(q, B.rc, B.rh, B.Re, B.te, B.ec, B.eh);
+		int v = pwf::boxes_disjoint32(q, B32);
+		if (v < 0)
+			v = pwm::boxes_disjoint(q, B.rc, B.rh, B.Re, B.te, B.ec, B.eh);
+		out[i] = (uint8_t)v;
 	}
+}
+
+// The FP32 constants of the box test.
+static pwf::DisBoxes32 dis_boxes32(const BoxParams &B)
+{
+	pwf::DisBoxes32 o;
+	double ce[3];
+	pwm::xform_point(B.Re, B.te, B.ec, ce);
+	float cabs = 0.f;
+	for (int c = 0; c < 3; c++) {
+		o.rc[c] = (float)B.rc[c];
+		o.rh[c] = (float)B.rh[c];
+		o.eh[c] = (float)B.eh[c];
+		o.ce[c] = (float)ce[c];
+		cabs = std::max(cabs, std::fabs(o.ce[c]));
+	}
+	for (int i = 0; i < 9; i++)
+		o.Re[i] = (float)B.Re[i];
+	o.ce_abs = cabs * (1.f + 1e-6f);
+	return o;
 }
 
 // ------------------------------------------------------------------ segments
@@ -1455,7 +1479,7 @@ extern "C" int pw_states_disentangled(pw_world *w, const double *states, int64_t
 	for (int i = 0; i < 9; i++)
 		B.Re[i] = w->pertR[i];
 	const int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)w->num_sms * 16);
-	k_disentangled<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(B, states, n, out);
+	k_disentangled<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(B, dis_boxes32(B), states, n, out);
 	PW_CUDA(cudaGetLastError());
 	return PW_OK;
 }

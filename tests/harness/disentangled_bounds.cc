@@ -1,0 +1,168 @@
+// disentangled_bounds.cc -- pwf::boxes_disjoint32 (the FP32 isDisentangled test)
+// against pwm::boxes_disjoint (FP64, the verdict of record) on states moved by
+// bisection to just either side of the boxes' contact, and on random states.
+// Host-only; built with g++.
+//
+// usage: disentangled_bounds <pairs> <seed> <slack>; prints
+// "wrong W certified C undecided U states S far_undecided F far_states N"
+// (far: the two states per pair drawn away from the contact) and exits 1 if W > 0.
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+
+#include "pw_filter.cuh"
+
+static uint64_t rng_state = 88172645463325252ull;
+static uint64_t next_u64()
+{
+	rng_state ^= rng_state << 13;
+	rng_state ^= rng_state >> 7;
+	rng_state ^= rng_state << 17;
+	return rng_state;
+}
+static double uniform() { return (double)(next_u64() >> 11) * (1.0 / 9007199254740992.0); }
+static double normal()
+{
+	const double u1 = uniform() + 1e-300, u2 = uniform();
+	return std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+}
+
+static void random_quat(double q[4])
+{
+	double n = 0;
+	for (int k = 0; k < 4; k++) {
+		q[k] = normal();
+		n += q[k] * q[k];
+	}
+	n = std::sqrt(n);
+	for (int k = 0; k < 4; k++)
+		q[k] /= n;
+}
+
+static void quat_matrix(const double q[4], double R[9])
+{
+	const double w = q[0], x = q[1], y = q[2], z = q[3];
+	R[0] = 1 - 2 * (y * y + z * z); R[1] = 2 * (x * y - w * z); R[2] = 2 * (x * z + w * y);
+	R[3] = 2 * (x * y + w * z); R[4] = 1 - 2 * (x * x + z * z); R[5] = 2 * (y * z - w * x);
+	R[6] = 2 * (x * z - w * y); R[7] = 2 * (y * z + w * x); R[8] = 1 - 2 * (x * x + y * y);
+}
+
+struct Boxes {
+	double rc[3], rh[3], Re[9], te[3], ec[3], eh[3];
+	pwf::DisBoxes32 b32;
+};
+
+static void make_boxes(Boxes &B)
+{
+	const double s = std::exp(normal());                  // scene scale around 1
+	for (int c = 0; c < 3; c++) {
+		B.rc[c] = 0.3 * s * normal();
+		B.rh[c] = s * (0.01 + uniform());
+		B.ec[c] = 0.3 * s * normal();
+		B.eh[c] = s * (0.01 + uniform());
+		B.te[c] = (next_u64() & 1) ? 0.0 : 0.2 * s * normal();
+	}
+	double qe[4] = { 1, 0, 0, 0 };
+	if (next_u64() & 1)
+		random_quat(qe);
+	quat_matrix(qe, B.Re);
+	double ce[3];
+	pwm::xform_point(B.Re, B.te, B.ec, ce);
+	float cabs = 0.f;
+	for (int c = 0; c < 3; c++) {
+		B.b32.rc[c] = (float)B.rc[c];
+		B.b32.rh[c] = (float)B.rh[c];
+		B.b32.eh[c] = (float)B.eh[c];
+		B.b32.ce[c] = (float)ce[c];
+		cabs = std::fmax(cabs, std::fabs(B.b32.ce[c]));
+	}
+	for (int i = 0; i < 9; i++)
+		B.b32.Re[i] = (float)B.Re[i];
+	B.b32.ce_abs = cabs * (1.f + 1e-6f);
+}
+
+int main(int argc, char **argv)
+{
+	const long pairs = argc > 1 ? atol(argv[1]) : 10000;
+	rng_state ^= (uint64_t)(argc > 2 ? atol(argv[2]) : 1) * 0x9E3779B97F4A7C15ull;
+	const float slack = argc > 3 ? (float)atof(argv[3]) : 1.f;
+	long wrong = 0, certified = 0, undecided = 0, states = 0, far_und = 0, far_states = 0;
+	auto check = [&](const Boxes &B, const double q[7]) {
+		const int ref = pwm::boxes_disjoint(q, B.rc, B.rh, B.Re, B.te, B.ec, B.eh);
+		const int v = pwf::boxes_disjoint32(q, B.b32, slack);
+		states++;
+		if (v < 0) {
+			undecided++;
+			return;
+		}
+		certified++;
+		if (v != ref)
+			wrong++;
+	};
+	for (long p = 0; p < pairs; p++) {
+		Boxes B;
+		make_boxes(B);
+		double q[7];
+		double rq[4];
+		random_quat(rq);
+		// a quaternion that is not normalised, as states may come
+		const double sc = 0.5 + uniform();
+		for (int k = 0; k < 4; k++)
+			q[3 + k] = rq[k] * sc;
+		// direction of travel of the robot box's centre, from overlap (near the env centre) outwards
+		double v[3], base[3], ce[3];
+		pwm::xform_point(B.Re, B.te, B.ec, ce);
+		for (int c = 0; c < 3; c++) {
+			v[c] = normal();
+			base[c] = ce[c];
+		}
+		// t puts the placed robot centre at base + s v: t = base + s v - R rc
+		double R[9], tt[3], Rrc[3];
+		pwm::state_transform(q, R, tt);
+		const double zero[3] = { 0, 0, 0 };
+		pwm::xform_point(R, zero, B.rc, Rrc);
+		auto at = [&](double s, double out[7]) {
+			for (int c = 0; c < 3; c++)
+				out[c] = base[c] + s * v[c] - Rrc[c];
+			for (int k = 3; k < 7; k++)
+				out[k] = q[k];
+		};
+		double lo = 0.0, hi = 1.0, st[7];
+		at(lo, st);
+		if (pwm::boxes_disjoint(st, B.rc, B.rh, B.Re, B.te, B.ec, B.eh))
+			continue;                                   // centres together yet disjoint: degenerate draw
+		for (int g = 0; g < 60; g++) {
+			at(hi, st);
+			if (pwm::boxes_disjoint(st, B.rc, B.rh, B.Re, B.te, B.ec, B.eh))
+				break;
+			hi *= 2.0;
+		}
+		for (int it = 0; it < 80 && hi - lo > 1e-17 * hi; it++) {
+			const double mid = 0.5 * (lo + hi);
+			at(mid, st);
+			if (pwm::boxes_disjoint(st, B.rc, B.rh, B.Re, B.te, B.ec, B.eh))
+				hi = mid;
+			else
+				lo = mid;
+		}
+		// both sides of the contact, points near it at several distances, and far states
+		const double offs[] = { 0.0, 1e-12, 1e-9, 1e-7, 1e-6, 1e-5, 1e-4, 1e-3, 1e-2, 1e-1 };
+		for (double o : offs) {
+			at(lo * (1.0 - o), st);
+			check(B, st);
+			at(hi * (1.0 + o), st);
+			check(B, st);
+		}
+		const long u0 = undecided;
+		at(hi * (1.0 + 10.0 * uniform()), st);
+		check(B, st);
+		at(lo * uniform(), st);
+		check(B, st);
+		far_und += undecided - u0;
+		far_states += 2;
+	}
+	printf("wrong %ld certified %ld undecided %ld states %ld far_undecided %ld far_states %ld\n", wrong, certified,
+	       undecided, states, far_und, far_states);
+	return wrong ? 1 : 0;
+}

@@ -46,3 +46,34 @@ def test_certified_verdicts_match_fp64(harness, seed):
     assert fields["certified_hits"] > 100_000       # the filter does certify contacts
     assert fields["oriented_violations"] == 0
     assert fields["oriented_separations"] > 100_000 and fields["touching_cases"] > 500_000
+
+
+@pytest.fixture(scope="module")
+def dis_harness(tmp_path_factory):
+    exe = str(tmp_path_factory.mktemp("db") / "disentangled_bounds")
+    src = os.path.join(ROOT, "tests", "harness", "disentangled_bounds.cc")
+    cmd = ["g++", "-O2", "-std=c++17", "-x", "c++", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"),
+           "-I", os.path.join(ROOT, "puzzletunneldiscovery_gb300", "csrc"), "-I", _cuda_include(), src, "-o", exe]
+    subprocess.run(cmd, check=True)
+    return exe
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_disentangled_fp32_verdicts_match_fp64(dis_harness, seed):
+    """pwf::boxes_disjoint32 (isDisentangled in FP32, unit_world.cc:249-264) never
+    certifies a verdict that differs from the FP64 test, on states bisected to
+    within 1e-17 of the boxes' contact and at growing distances from it."""
+    r = subprocess.run([dis_harness, "200000", str(seed), "1"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    f = r.stdout.split()
+    wrong, cert, und, states, far_und, far = (int(f[i]) for i in (1, 3, 5, 7, 9, 11))
+    assert wrong == 0 and states > 3_000_000 and cert > 1_000_000
+    # states within about 1e-3 (relative) of contact stay undecided; states away from it do not
+    assert far_und / far < 0.02, r.stdout
+
+
+def test_disentangled_check_has_teeth(dis_harness):
+    """The same run without the error bound certifies wrong verdicts."""
+    r = subprocess.run([dis_harness, "50000", "3", "0"], capture_output=True, text=True)
+    f = r.stdout.split()
+    assert int(f[1]) > 100, r.stdout
