@@ -78,7 +78,9 @@ typedef struct pw_world_info {
 	int32_t device;
 } pw_world_info;
 
-/* After a contact enumeration (pw_intersecting_segments, _batch): queries = states,
+/* After pw_states_disentangled: retests = states the FP32 box test left to the
+ * FP64 one (the others are 0).
+ * After a contact enumeration (pw_intersecting_segments, _batch): queries = states,
  * retests = candidate triangle pairs tested in FP64, retest_hits = rows,
  * work_items = kernels of this library launched, reference_checks = states. */
 typedef struct pw_query_stats {

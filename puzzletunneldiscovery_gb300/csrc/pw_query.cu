@@ -705,17 +705,73 @@ struct BoxParams {
 	double rc[3], rh[3], Re[9], te[3], ec[3], eh[3];
 };
 
-// The FP32 test decides almost every state; the rest take the FP64 test.
-__global__ void k_disentangled(BoxParams B, pwf::DisBoxes32 B32, const double *states, int64_t n, uint8_t *out)
+// The FP32 test decides almost every state.  A block stages its 256 states
+// (56 B each) in shared memory with 16-byte loads; the undecided ones are queued
+// (warp-aggregated) for k_disentangled64, or tested in FP64 on the spot when
+// the queue is full.
+constexpr int DIS_BLOCK = 256;
+__global__ void __launch_bounds__(DIS_BLOCK) k_disentangled(BoxParams B, pwf::DisBoxes32 B32, const double *states,
+                                                            int64_t n, uint8_t *out, int64_t *queue,
+                                                            unsigned long long qcap, QueryCounters *ctr)
 {
-	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+	__shared__ __align__(16) double sq[DIS_BLOCK * 7];
+	const int lane = threadIdx.x & 31;
+	for (int64_t b0 = (int64_t)blockIdx.x * DIS_BLOCK; b0 < n; b0 += (int64_t)gridDim.x * DIS_BLOCK) {
+		const int cnt = (int)min((int64_t)DIS_BLOCK, n - b0);
+		const double *src = states + 7 * b0;
+		if (cnt == DIS_BLOCK && (((uintptr_t)src) & 15) == 0) {
+			const float4 *f4 = reinterpret_cast<const float4 *>(src);
+			float4 *d4 = reinterpret_cast<float4 *>(sq);
+			for (int k = threadIdx.x; k < DIS_BLOCK * 7 / 2; k += DIS_BLOCK)
+				d4[k] = __ldg(f4 + k);
+		} else {
+			for (int k = threadIdx.x; k < cnt * 7; k += DIS_BLOCK)
+				sq[k] = src[k];
+		}
+		__syncthreads();
+		const int64_t i = b0 + threadIdx.x;
+		int v = 0;
+		bool undecided = false;
+		if (threadIdx.x < cnt) {
+			v = pwf::boxes_disjoint32(sq + 7 * threadIdx.x, B32);
+			undecided = v < 0;
+		}
+		const unsigned m = __ballot_sync(0xffffffffu, undecided);
+		unsigned long long base = 0;
+		if (m) {
+			if (lane == 0)
+				base = atomicAdd(&ctr->retest_count, (unsigned long long)__popc(m));
+			base = __shfl_sync(0xffffffffu, base, 0);
+		}
+		if (undecided) {
+			const unsigned long long slot = base + __popc(m & ((1u << lane) - 1u));
+			if (slot < qcap) {
+				queue[slot] = i;
+				v = 0;                          // k_disentangled64 writes the verdict
+			} else {
+				v = pwm::boxes_disjoint(sq + 7 * threadIdx.x, B.rc, B.rh, B.Re, B.te, B.ec, B.eh);
+			}
+		}
+		if (threadIdx.x < cnt)
+			out[i] = (uint8_t)v;
+		__syncthreads();
+	}
+}
+
+// The FP64 test of the queued states, one thread each.
+__global__ void k_disentangled64(BoxParams B, const double *states, const int64_t *queue,
+                                 unsigned long long qcap, QueryCounters *ctr, uint8_t *out)
+{
+	const unsigned long long cnt = min(ctr->retest_count, qcap);
+	if (blockIdx.x == 0 && threadIdx.x == 0)
+		ctr->stat[STAT_RETESTS] = ctr->retest_count;
+	for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < cnt;
+	     k += (unsigned long long)gridDim.x * blockDim.x) {
+		const int64_t i = queue[k];
 		double q[7];
-		for (int k = 0; k < 7; k++)
-			q[k] = states[7 * i + k];
-		int v = pwf::boxes_disjoint32(q, B32);
-		if (v < 0)
-			v = pwm::boxes_disjoint(q, B.rc, B.rh, B.Re, B.te, B.ec, B.eh);
-		out[i] = (uint8_t)v;
+		for (int c = 0; c < 7; c++)
+			q[c] = states[7 * i + c];
+		out[i] = (uint8_t)pwm::boxes_disjoint(q, B.rc, B.rh, B.Re, B.te, B.ec, B.eh);
 	}
 }
 
@@ -1478,8 +1534,22 @@ extern "C" int pw_states_disentangled(pw_world *w, const double *states, int64_t
 	}
 	for (int i = 0; i < 9; i++)
 		B.Re[i] = w->pertR[i];
-	const int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)w->num_sms * 16);
-	k_disentangled<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(B, dis_boxes32(B), states, n, out);
+	cudaStream_t st = (cudaStream_t)stream;
+	int rc = ensure_query_scratch(w);
+	if (rc)
+		return rc;
+	// the queue of undecided states: the FP64 re-test buffer, as int64 state indices
+	const unsigned long long qcap = (unsigned long long)(w->retest.bytes / sizeof(int64_t));
+	QueryCounters *ctr = (QueryCounters *)w->counters.ptr;
+	PW_CUDA(cudaMemsetAsync(ctr, 0, sizeof(QueryCounters), st));
+	w->last_stream = st;
+	w->timed = false;
+	w->last_states = n;
+	const int64_t blocks = std::min<int64_t>((n + DIS_BLOCK - 1) / DIS_BLOCK, (int64_t)w->num_sms * 8);
+	k_disentangled<<<(unsigned)blocks, DIS_BLOCK, 0, st>>>(B, dis_boxes32(B), states, n, out,
+	                                                      (int64_t *)w->retest.ptr, qcap, ctr);
+	k_disentangled64<<<(unsigned)(w->num_sms * 4), 256, 0, st>>>(B, states, (const int64_t *)w->retest.ptr, qcap,
+	                                                             ctr, out);
 	PW_CUDA(cudaGetLastError());
 	return PW_OK;
 }

@@ -353,3 +353,45 @@ def test_ompl_screening_of_the_alpha_path(alpha):
     got = OC.validate_states(uw, Q)
     assert 0 < got.sum() < len(Q)
     assert (got == ow.is_valid(U).astype(np.int32)).all()
+
+
+def test_disentangled_fp32_and_fp64_paths(tori):
+    """is_disentangled_states (FP32 box test, FP64 for undecided states queued to a
+    second kernel) equals the oracle (unit_world.cc:249-264) on states built to lie
+    within rounding of the boxes' contact, on a misaligned batch (scalar staging)
+    and on a ragged tail."""
+    uw, ow = tori
+    s = ow.scene_scale
+    q = W.uniform_states(300_001, -2.0, 2.0, s, seed=41)
+    got = uw.is_disentangled_states(torch.from_numpy(q)).cpu().numpy()
+    assert (got == ow.is_disentangled(q)).all()
+    # near contact: bisect the translation scale between a touching and a separated state
+    rng = np.random.default_rng(42)
+    near = []
+    for _ in range(2000):
+        a = W.uniform_states(1, -0.3, 0.3, s, seed=int(rng.integers(1 << 30)))[0]
+        v = rng.normal(size=3)
+        lo, hi = 0.0, 8.0
+        b = a.copy()
+        b[:3] = a[:3] + hi * v
+        if not ow.is_disentangled(a[None])[0] and ow.is_disentangled(b[None])[0]:
+            for _ in range(60):
+                mid = 0.5 * (lo + hi)
+                c = a.copy()
+                c[:3] = a[:3] + mid * v
+                if ow.is_disentangled(c[None])[0]:
+                    hi = mid
+                else:
+                    lo = mid
+            for t in (lo, hi):
+                c = a.copy()
+                c[:3] = a[:3] + t * v
+                near.append(c)
+    near = np.array(near)
+    got = uw.is_disentangled_states(torch.from_numpy(near)).cpu().numpy()
+    assert (got == ow.is_disentangled(near)).all() and got.sum() > 100 and (got == 0).sum() > 100
+    assert uw.last_stats()["retests"] > 0.5 * near.shape[0]        # near contact: the FP64 test decided
+    # an offset view: 8-byte aligned rows, the scalar staging path
+    dq = torch.from_numpy(q).cuda().reshape(-1)[7:].reshape(-1, 7)
+    got = uw.is_disentangled_states(dq).cpu().numpy()
+    assert (got == ow.is_disentangled(q[1:])).all()
