@@ -127,6 +127,7 @@ struct pw_world {
 	DeviceBuffer seg_params, seg_ckpt, seg_anchor, seg_keys, seg_order, seg_keys2, seg_order2, round_off, cub_tmp, misc;
 	DeviceBuffer isect;        // contact enumeration (candidates, rows, sort keys, output columns)
 	PinnedBuffer isect_stage;  // two halves: one chunk's output columns on their way to the caller
+	DeviceBuffer dis_queue;    // states the FP32 isDisentangled test left undecided
 	cudaStream_t last_stream = nullptr;
 	cudaEvent_t ev[4] = { nullptr, nullptr, nullptr, nullptr }; // traversal start/end, re-test start/end
 	bool timed = false;

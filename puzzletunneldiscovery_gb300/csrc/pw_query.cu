@@ -707,12 +707,11 @@ struct BoxParams {
 
 // The FP32 test decides almost every state.  A block stages its 256 states
 // (56 B each) in shared memory with 16-byte loads; the undecided ones are queued
-// (warp-aggregated) for k_disentangled64, or tested in FP64 on the spot when
-// the queue is full.
+// (warp-aggregated) for k_disentangled64.  The queue holds n entries, so it
+// cannot fill.
 constexpr int DIS_BLOCK = 256;
-__global__ void __launch_bounds__(DIS_BLOCK) k_disentangled(BoxParams B, pwf::DisBoxes32 B32, const double *states,
-                                                            int64_t n, uint8_t *out, int64_t *queue,
-                                                            unsigned long long qcap, QueryCounters *ctr)
+__global__ void __launch_bounds__(DIS_BLOCK) k_disentangled(pwf::DisBoxes32 B32, const double *states, int64_t n,
+                                                            uint8_t *out, uint32_t *queue, QueryCounters *ctr)
 {
 	__shared__ __align__(16) double sq[DIS_BLOCK * 7];
 	const int lane = threadIdx.x & 31;
@@ -745,12 +744,9 @@ __global__ void __launch_bounds__(DIS_BLOCK) k_disentangled(BoxParams B, pwf::Di
 		}
 		if (undecided) {
 			const unsigned long long slot = base + __popc(m & ((1u << lane) - 1u));
-			if (slot < qcap) {
-				queue[slot] = i;
-				v = 0;                          // k_disentangled64 writes the verdict
-			} else {
-				v = pwm::boxes_disjoint(sq + 7 * threadIdx.x, B.rc, B.rh, B.Re, B.te, B.ec, B.eh);
-			}
+			if (slot < (unsigned long long)n)
+				queue[slot] = (uint32_t)i;
+			v = 0;                              // k_disentangled64 writes the verdict
 		}
 		if (threadIdx.x < cnt)
 			out[i] = (uint8_t)v;
@@ -759,15 +755,15 @@ __global__ void __launch_bounds__(DIS_BLOCK) k_disentangled(BoxParams B, pwf::Di
 }
 
 // The FP64 test of the queued states, one thread each.
-__global__ void k_disentangled64(BoxParams B, const double *states, const int64_t *queue,
-                                 unsigned long long qcap, QueryCounters *ctr, uint8_t *out)
+__global__ void k_disentangled64(BoxParams B, const double *states, const uint32_t *queue, int64_t n,
+                                 QueryCounters *ctr, uint8_t *out)
 {
-	const unsigned long long cnt = min(ctr->retest_count, qcap);
+	const unsigned long long cnt = min(ctr->retest_count, (unsigned long long)n);
 	if (blockIdx.x == 0 && threadIdx.x == 0)
 		ctr->stat[STAT_RETESTS] = ctr->retest_count;
 	for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < cnt;
 	     k += (unsigned long long)gridDim.x * blockDim.x) {
-		const int64_t i = queue[k];
+		const int64_t i = (int64_t)queue[k];
 		double q[7];
 		for (int c = 0; c < 7; c++)
 			q[c] = states[7 * i + c];
@@ -1512,6 +1508,17 @@ extern "C" int pw_states_valid(pw_world *w, const double *states, int64_t n, uin
 	return PW_OK;
 }
 
+template <typename T>
+static int grow(DeviceBuffer &b, size_t count, bool may_allocate = true)
+{
+	const size_t need = sizeof(T) * (count ? count : 1);
+	if (!may_allocate && b.bytes < need)
+		return pw_fail(PW_ERR_CAPACITY, "graph mode: scratch not reserved for this batch (call pw_segments_reserve "
+		                                "or run the batch once with graph mode off)");
+	PW_CUDA(b.reserve(need));
+	return PW_OK;
+}
+
 extern "C" int pw_states_disentangled(pw_world *w, const double *states, int64_t n, uint8_t *out, void *stream)
 {
 	PW_TRACE("pw_states_disentangled");
@@ -1538,32 +1545,24 @@ extern "C" int pw_states_disentangled(pw_world *w, const double *states, int64_t
 	int rc = ensure_query_scratch(w);
 	if (rc)
 		return rc;
-	// the queue of undecided states: the FP64 re-test buffer, as int64 state indices
-	const unsigned long long qcap = (unsigned long long)(w->retest.bytes / sizeof(int64_t));
+	// the queue of undecided states (32-bit state indices, room for all of them)
+	if (n > (int64_t)UINT32_MAX)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_states_disentangled: at most 2^32 - 1 states per call");
+	if ((rc = grow<uint32_t>(w->dis_queue, (size_t)n)))
+		return rc;
 	QueryCounters *ctr = (QueryCounters *)w->counters.ptr;
 	PW_CUDA(cudaMemsetAsync(ctr, 0, sizeof(QueryCounters), st));
 	w->last_stream = st;
 	w->timed = false;
 	w->last_states = n;
 	const int64_t blocks = std::min<int64_t>((n + DIS_BLOCK - 1) / DIS_BLOCK, (int64_t)w->num_sms * 8);
-	k_disentangled<<<(unsigned)blocks, DIS_BLOCK, 0, st>>>(B, dis_boxes32(B), states, n, out,
-	                                                      (int64_t *)w->retest.ptr, qcap, ctr);
-	k_disentangled64<<<(unsigned)(w->num_sms * 4), 256, 0, st>>>(B, states, (const int64_t *)w->retest.ptr, qcap,
-	                                                             ctr, out);
+	uint32_t *queue = (uint32_t *)w->dis_queue.ptr;
+	k_disentangled<<<(unsigned)blocks, DIS_BLOCK, 0, st>>>(dis_boxes32(B), states, n, out, queue, ctr);
+	k_disentangled64<<<(unsigned)(w->num_sms * 4), 256, 0, st>>>(B, states, queue, n, ctr, out);
 	PW_CUDA(cudaGetLastError());
 	return PW_OK;
 }
 
-template <typename T>
-static int grow(DeviceBuffer &b, size_t count, bool may_allocate = true)
-{
-	const size_t need = sizeof(T) * (count ? count : 1);
-	if (!may_allocate && b.bytes < need)
-		return pw_fail(PW_ERR_CAPACITY, "graph mode: scratch not reserved for this batch (call pw_segments_reserve "
-		                                "or run the batch once with graph mode off)");
-	PW_CUDA(b.reserve(need));
-	return PW_OK;
-}
 
 extern "C" int pw_segments_first_contact(pw_world *w, const double *from, const double *to, int64_t n,
                                          double verify_delta, int mode, int32_t *first_step, void *stream)
