@@ -37,9 +37,16 @@ struct MeshDev {
 	float emax = 0.f;        // max |coordinate| of any vertex or oriented node box corner
 };
 
+// Node pairs a single-query traversal starts from: a partition of the root
+// pair (env root, robot root) into up to 32 pairs, so that a warp's first round
+// has work for its lanes.
+constexpr int MAX_SEEDS = 32;
+
 struct WorldDev {
 	MeshDev env, rob;
 	float del_env;           // FP32 rounding bound of an env vertex coordinate
+	int32_t nseeds = 0;
+	const uint2 *seeds = nullptr;   // nseeds (env node, robot node) pairs, device memory
 };
 
 // Round phases of a segment query: phase p holds the rounds (32-step chunk
@@ -128,6 +135,7 @@ struct pw_world {
 	DeviceBuffer isect;        // contact enumeration (candidates, rows, sort keys, output columns)
 	PinnedBuffer isect_stage;  // two halves: one chunk's output columns on their way to the caller
 	DeviceBuffer dis_queue;    // states the FP32 isDisentangled test left undecided
+	DeviceBuffer seeds;        // the traversals' seed pairs (WorldDev::seeds)
 	cudaStream_t last_stream = nullptr;
 	cudaEvent_t ev[4] = { nullptr, nullptr, nullptr, nullptr }; // traversal start/end, re-test start/end
 	bool timed = false;

@@ -407,10 +407,19 @@ __device__ uint32_t traverse_chunk(const WorldDev &W, WarpSmem &sm, int lane, in
 	const uint32_t ebase = (uint32_t)W.env.leaf_base, rbase = (uint32_t)W.rob.leaf_base;
 	const unsigned lt_mask = (1u << lane) - 1u;
 	const unsigned gt_mask = ~(lt_mask | (1u << lane));
-	if (lane == 0)
-		sm.stack[0] = make_uint2(0u, range_bits(0, nopen - 1));
+	// start from the world's seed pairs (a partition of the root pair), all steps open;
+	// the count comes from a ballot, which the compiler sees as warp-uniform
+	int top;
+	{
+		const bool has = lane < W.nseeds;
+		if (has) {
+			const uint2 sd = __ldg(W.seeds + lane);
+			sm.stack[lane] = make_uint2(sd.x, sd.y | range_bits(0, nopen - 1));
+		}
+		top = __popc(__ballot_sync(FULL, has));
+	}
 	__syncwarp();
-	int top = 1, nunc = 0, nleaf = 0;
+	int nunc = 0, nleaf = 0;
 	bool detailed = false;
 	uint32_t done = nopen >= 32 ? 0u : ~((1u << nopen) - 1u), hit = 0u;
 
@@ -1168,12 +1177,14 @@ __device__ void isect_traverse(const WorldDev &W, WarpSmem &sm, int lane, int so
 {
 	const uint32_t ebase = (uint32_t)W.env.leaf_base, rbase = (uint32_t)W.rob.leaf_base;
 	const unsigned gt_mask = ~(((1u << lane) - 1u) | (1u << lane));
-	if (lane == 0)
-		sm.stack[0] = make_uint2(0u, 0u);
+	// start from the world's seed pairs (a partition of the root pair)
+	const bool has = lane < W.nseeds;
+	if (has)
+		sm.stack[lane] = __ldg(W.seeds + lane);
+	int top = __popc(__ballot_sync(FULL, has));
 	__syncwarp();
 	const float4 Q0 = sm.qf[0].q[0], Q1 = sm.qf[0].q[1], Q2 = sm.qf[0].q[2], Q3 = sm.qf[0].q[3];
 	const float eg = sm.qf[0].q[4].x;
-	int top = 1;
 	while (top > 0) {
 		int p = min(top, 32);
 		const int room = soft_cap - top;

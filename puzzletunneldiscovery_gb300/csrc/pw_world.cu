@@ -252,6 +252,83 @@ static void local_box(const std::vector<double> &V, double c[3], double h[3])
 	}
 }
 
+
+// The seed pairs of a world's meshes: starting from the root pair, the pair with
+// the largest boxes (sum of both half-extents) is replaced by the pairs of its
+// larger non-leaf side's children (the traversal's own descent rule), until 32
+// pairs or only leaf pairs remain.  The pairs partition the root pair's leaf
+// pairs, so a traversal from them tests what one from the root tests.
+static int compute_seeds(pw_world *w)
+{
+	struct Node {
+		float h[3];
+		uint32_t left, right;
+		bool leaf;
+	};
+	auto fetch = [&](const MeshDev &m, uint32_t id, Node &o) -> int {
+		float4 a, b;
+		PW_CUDA(cudaMemcpy(&a, m.nodeA + id, sizeof(float4), cudaMemcpyDeviceToHost));
+		PW_CUDA(cudaMemcpy(&b, m.nodeB + id, sizeof(float4), cudaMemcpyDeviceToHost));
+		o.h[0] = b.x;
+		o.h[1] = b.y;
+		o.h[2] = b.z;
+		memcpy(&o.left, &a.w, 4);
+		memcpy(&o.right, &b.w, 4);
+		o.leaf = (int64_t)id >= (int64_t)m.leaf_base;
+		return PW_OK;
+	};
+	struct Pair {
+		uint32_t e, r;
+		Node ne, nr;
+	};
+	std::vector<Pair> pairs(1);
+	pairs[0].e = pairs[0].r = 0;
+	int rc;
+	if ((rc = fetch(w->dev.env, 0, pairs[0].ne)) || (rc = fetch(w->dev.rob, 0, pairs[0].nr)))
+		return rc;
+	auto size = [](const Node &n) { return n.h[0] + n.h[1] + n.h[2]; };
+	while ((int)pairs.size() < MAX_SEEDS) {
+		int best = -1;
+		float bs = -1.f;
+		for (int i = 0; i < (int)pairs.size(); i++) {
+			const Pair &p = pairs[i];
+			if (p.ne.leaf && p.nr.leaf)
+				continue;
+			const float sz = size(p.ne) + size(p.nr);
+			if (sz > bs) {
+				bs = sz;
+				best = i;
+			}
+		}
+		if (best < 0)
+			break;
+		const Pair p = pairs[best];
+		const bool da = !p.ne.leaf && (p.nr.leaf || size(p.ne) >= size(p.nr));
+		Pair a = p, b = p;
+		if (da) {
+			a.e = p.ne.left;
+			b.e = p.ne.right;
+			if ((rc = fetch(w->dev.env, a.e, a.ne)) || (rc = fetch(w->dev.env, b.e, b.ne)))
+				return rc;
+		} else {
+			a.r = p.nr.left;
+			b.r = p.nr.right;
+			if ((rc = fetch(w->dev.rob, a.r, a.nr)) || (rc = fetch(w->dev.rob, b.r, b.nr)))
+				return rc;
+		}
+		pairs[best] = a;
+		pairs.push_back(b);
+	}
+	std::vector<uint2> h(pairs.size());
+	for (size_t i = 0; i < pairs.size(); i++)
+		h[i] = make_uint2(pairs[i].e, pairs[i].r);
+	PW_CUDA(w->seeds.reserve(sizeof(uint2) * MAX_SEEDS));
+	PW_CUDA(cudaMemcpy(w->seeds.ptr, h.data(), sizeof(uint2) * h.size(), cudaMemcpyHostToDevice));
+	w->dev.seeds = (const uint2 *)w->seeds.ptr;
+	w->dev.nseeds = (int32_t)pairs.size();
+	return PW_OK;
+}
+
 extern "C" int pw_world_angle_model(pw_world *w, float latitude, float longitude)
 {
 	PW_TRACE("pw_world_angle_model");
@@ -289,6 +366,8 @@ extern "C" int pw_world_angle_model(pw_world *w, float latitude, float longitude
 	if (rc)
 		return rc;
 	w->dev.del_env = 5.9604645e-08f * w->dev.env.emax * 1.0001f;
+	if ((rc = compute_seeds(w)))
+		return rc;
 	w->ready = true;
 	return PW_OK;
 }
@@ -320,6 +399,8 @@ extern "C" int pw_world_set_perturbation(pw_world *w, const double q[7])
 		if (rc)
 			return rc;
 		w->dev.del_env = 5.9604645e-08f * w->dev.env.emax * 1.0001f;
+		if ((rc = compute_seeds(w)))
+			return rc;
 		w->ready = true;
 	}
 	return PW_OK;
