@@ -1177,14 +1177,14 @@ __device__ void isect_traverse(const WorldDev &W, WarpSmem &sm, int lane, int so
 {
 	const uint32_t ebase = (uint32_t)W.env.leaf_base, rbase = (uint32_t)W.rob.leaf_base;
 	const unsigned gt_mask = ~(((1u << lane) - 1u) | (1u << lane));
-	// start from the world's seed pairs (a partition of the root pair)
-	const bool has = lane < W.nseeds;
-	if (has)
-		sm.stack[lane] = __ldg(W.seeds + lane);
-	int top = __popc(__ballot_sync(FULL, has));
+	// every contact of a colliding state is enumerated, so there is no early exit to
+	// reach sooner: the root pair (seed pairs measured 4 % slower here)
+	if (lane == 0)
+		sm.stack[0] = make_uint2(0u, 0u);
 	__syncwarp();
 	const float4 Q0 = sm.qf[0].q[0], Q1 = sm.qf[0].q[1], Q2 = sm.qf[0].q[2], Q3 = sm.qf[0].q[3];
 	const float eg = sm.qf[0].q[4].x;
+	int top = 1;
 	while (top > 0) {
 		int p = min(top, 32);
 		const int room = soft_cap - top;
