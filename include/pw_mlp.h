@@ -55,7 +55,10 @@ PW_API int pw_mlp_set_adam(pw_mlp *m, const float *m1_in, const float *m2_in, in
 /* P(collision free) of n states (device float64 [n x 7] -> device float32 [n]):
  * one fused, persistent kernel on the tcgen05 tensor cores (weights streamed by
  * bulk copies, accumulators in tensor memory).  Its waits are bounded;
- * pw_mlp_check reports whether one gave up. */
+ * pw_mlp_check reports whether one gave up.  Asynchronous on stream, except that
+ * the first call after the weights changed (a training step, pw_mlp_set_params)
+ * synchronises the stream once to copy the epilogue constants (biases, head) to
+ * the host: each launch passes them in its parameters. */
 PW_API int pw_mlp_predict(pw_mlp *m, const double *states, int64_t n, float *prob, void *stream);
 
 /* The logit of the same network (the score before the sigmoid): a ranking

@@ -508,6 +508,7 @@ struct pw_mlp {
 	bool mma_training = false;   // train with the mma.sync kernels instead
 	bool withhold_next = false;  // the next tcgen05 forward launch issues no weight copies
 	bool wimg_dirty = true;
+	std::vector<float> ht_host;  // the epilogue constants (tc::HT_*), passed in each forward launch's parameters
 	int num_sms = 1;
 	int64_t cap = 0;             // rows the activation buffers hold
 	int64_t step = 0;
@@ -824,6 +825,12 @@ static int mlp_forward_tc(pw_mlp *m, const double *states, int64_t n, float *pro
 		    (const float *)m->params.ptr, (int64_t)m->off_b[0], (int64_t)m->off_b[1], (int64_t)m->off_b[2],
 		    (int64_t)m->off_b[3], (int64_t)m->off_w5, (int64_t)m->off_b5, mlp_head_table(m));
 		PW_CUDA(cudaGetLastError());
+		// the epilogue reads its constants from the launch's parameter bank (warp-uniform
+		// operands), so keep a host copy: one small synchronous copy per weight update
+		m->ht_host.resize(tc::HT_FLOATS);
+		PW_CUDA(cudaMemcpyAsync(m->ht_host.data(), mlp_head_table(m), sizeof(float) * tc::HT_FLOATS,
+		                        cudaMemcpyDeviceToHost, st));
+		PW_CUDA(cudaStreamSynchronize(st));
 		m->wimg_dirty = false;
 	}
 	static bool attr_set = false;
@@ -839,7 +846,7 @@ static int mlp_forward_tc(pw_mlp *m, const double *states, int64_t n, float *pro
 	a.states = states;
 	a.n = n;
 	a.wimg = (const bf16 *)m->wimg.ptr;
-	a.ht = mlp_head_table(m);
+	memcpy(a.ht, m->ht_host.data(), sizeof(a.ht));
 	a.prob = prob;
 	a.logits = logits;
 	a.withhold = m->withhold_next ? 1 : 0;

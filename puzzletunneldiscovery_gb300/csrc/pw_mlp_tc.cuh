@@ -228,11 +228,11 @@ struct FwdArgs {
 	const double *states;
 	int64_t n;
 	const bf16 *wimg;        // NWBLOCK images of WBLOCK_BYTES (weights scaled by 1/2)
-	const float *ht;         // epilogue constants (HT_*)
 	float *prob;
 	int logits;              // 1: write the logit (a ranking score that does not saturate) instead of P(free)
 	int withhold;            // 1: issue no weight copies (the test of the bounded waits: they run out)
 	int *err;
+	float ht[HT_FLOATS];     // epilogue constants (HT_*), in the launch's parameter bank
 };
 
 __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
@@ -354,7 +354,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 		// ---------------- epilogue: 16 warps, warp (q = lane quarter, g = column group)
 		const int e = warp - 2;
 		const int q = warp & 3;
-		const int g = e >> 2;
+		const int g = __shfl_sync(0xffffffffu, e >> 2, 0);   // warp-uniform: constant-bank operands
 		const int r = q * 32 + lane;                  // tile row of this thread
 		const uint32_t lane_off = (uint32_t)(q * 32) << 16;
 		uint32_t done_ph[2] = { 0, 0 }, head_ph[2] = { 0, 0 };
@@ -399,7 +399,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 #pragma unroll
 					for (int i = 0; i < 4; i++)
 						*reinterpret_cast<float4 *>(bv[0] + 4 * i) =
-						    __ldg(reinterpret_cast<const float4 *>(bias + g * 16) + i);
+						    *(reinterpret_cast<const float4 *>(bias + g * 16) + i);
 					if (!mbar_wait(bar(B_DONE + sl), done_ph[sl], s_abort, a.err, 4)) {
 						ok = false;
 						break;
@@ -420,7 +420,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 							             rv[(j + 1) & 1]);
 #pragma unroll
 							for (int i = 0; i < 4; i++)
-								*reinterpret_cast<float4 *>(bv[(j + 1) & 1] + 4 * i) = __ldg(
+								*reinterpret_cast<float4 *>(bv[(j + 1) & 1] + 4 * i) = *(
 								    reinterpret_cast<const float4 *>(bias + (j + 1) * KB + g * 16) + i);
 						}
 						const int col = j * KB + g * 16;
@@ -439,7 +439,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_forward_tc(FwdArgs a)
 #pragma unroll
 							for (int i = 0; i < 4; i++)
 								*reinterpret_cast<float4 *>(wv + 4 * i) =
-								    __ldg(reinterpret_cast<const float4 *>(a.ht + HT_W5 + col) + i);
+								    *(reinterpret_cast<const float4 *>(a.ht + HT_W5 + col) + i);
 #pragma unroll
 							for (int i = 0; i < 8; i++) {
 								const __nv_bfloat162 hh = *reinterpret_cast<__nv_bfloat162 *>(&pk[i]);
