@@ -1596,7 +1596,7 @@ def _traffic_per_segment():
 
 def run_profile_case(args):
     """Small fixed workloads for ncu captures (no JSON line): `states`, `segments`,
-    `mlp`, `train`, `plate`, `ompl` or `all` (every kernel of the engine once),
+    `mlp`, `train`, `plate`, `ompl`, `disentangled` or `all` (every kernel of the engine once),
     with --n units, on the interlocking tori (the plate and torus knot for
     `plate`, the alpha puzzle for `ompl`); --node-boxes picks the BVH boxes."""
     import torch
@@ -1678,6 +1678,13 @@ def run_profile_case(args):
         torch.cuda.synchronize()
         print("done")
         return
+    if what == "disentangled":
+        q = torch.from_numpy(W.uniform_states(n, -2, 2, s, seed=0)).to(dev)
+        for _ in range(3):
+            uw.is_disentangled_states(q)
+        torch.cuda.synchronize()
+        print("done", uw.last_stats())
+        return
     if what == "states":
         q = torch.from_numpy(W.uniform_states(n, -2, 2, s, seed=0)).to(dev)
         for _ in range(3):
@@ -1713,7 +1720,8 @@ def main():
     ap.add_argument("--e2e-n", type=int, default=20_000_000, help="surrogate: candidates per end-to-end step")
     ap.add_argument("--sweep", type=lambda v: [float(x) for x in v.split(",") if x], default=[0.25, 0.5, 0.6],
                     help="surrogate: further checked fractions reported in detail")
-    ap.add_argument("--profile-case", choices=["states", "segments", "mlp", "train", "plate", "ompl", "all"], default=None,
+    ap.add_argument("--profile-case", choices=["states", "segments", "mlp", "train", "plate", "ompl", "disentangled", "all"],
+                    default=None,
                     help="run a small fixed workload for an ncu capture instead of the benchmark")
     ap.add_argument("--node-boxes", choices=["aligned", "oriented"], default=None,
                     help="profile cases: the BVH node boxes (default: the world's default)")
