@@ -7,7 +7,6 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
-#include <string.h>
 
 #include "pw_math.cuh"
 
@@ -396,8 +395,7 @@ PW_HD int tri_filter(float3 V0, float3 e1, float3 e2, float3 x0, float3 g1, floa
 // terms weighted by |T|_inf <= |d|_1, the extents and K, so
 // e = 1100u K (|rc|_1 + |t|_inf + |ce|_inf + 2 |d|_1 + sum eh + sum rh) covers
 // the FP32 side with a factor above 1.5 and the FP64 side (the same sums at
-// 2^-53) many times over.  The state's doubles are truncated to FP32 (error
-// 2u, not u), which the constant's 1300 instead of 1100 absorbs.  tests/harness/disentangled_bounds.cc checks it
+// 2^-53) many times over.  tests/harness/disentangled_bounds.cc checks it
 // against pwm::boxes_disjoint near the boundary (slack scales e; the kernels
 // use 1, the harness also runs 0 to show that the check has teeth).
 struct DisBoxes32 {
@@ -408,30 +406,9 @@ struct DisBoxes32 {
 	float ce_abs;          // |ce|_inf, rounded up
 };
 
-// FP64 -> FP32 by truncation of the mantissa, with integer operations (GB300's
-// FP64 pipe, which the cvt instruction uses, is narrow): |result - x| < 2^-23 |x|
-// for |x| in the normal FP32 range; ok is cleared for anything else (zero
-// excepted: it converts exactly).
-PW_HD float f32_trunc(double x, bool &ok)
-{
-	uint64_t b;
-	memcpy(&b, &x, sizeof(b));
-	const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
-	const int e = (int)((b >> 52) & 0x7FF) - 1023 + 127;
-	if ((b << 1) == 0)
-		return sign ? -0.f : 0.f;
-	if (e <= 0 || e >= 255)
-		ok = false;
-	const uint32_t f = sign | ((uint32_t)(e & 0xFF) << 23) | (uint32_t)((b >> 29) & 0x7FFFFFu);
-	float r;
-	memcpy(&r, &f, sizeof(r));
-	return r;
-}
-
 PW_HD int boxes_disjoint32(const double *q, const DisBoxes32 &B, float slack = 1.f)
 {
-	bool ok = true;
-	const float w = f32_trunc(q[3], ok), x = f32_trunc(q[4], ok), y = f32_trunc(q[5], ok), z = f32_trunc(q[6], ok);
+	const float w = (float)q[3], x = (float)q[4], y = (float)q[5], z = (float)q[6];
 	const float n2 = ((w * w + x * x) + y * y) + z * z;
 	if (!(n2 < 1.0e30f))
 		return -1;                           // not finite or huge: the FP64 test decides
@@ -439,9 +416,7 @@ PW_HD int boxes_disjoint32(const double *q, const DisBoxes32 &B, float slack = 1
 	const float R[9] = { 1.f - 2.f * (y * y + z * z), 2.f * (x * y - w * z), 2.f * (x * z + w * y),
 		                 2.f * (x * y + w * z), 1.f - 2.f * (x * x + z * z), 2.f * (y * z - w * x),
 		                 2.f * (x * z - w * y), 2.f * (y * z + w * x), 1.f - 2.f * (x * x + y * y) };
-	const float t[3] = { f32_trunc(q[0], ok), f32_trunc(q[1], ok), f32_trunc(q[2], ok) };
-	if (!ok)
-		return -1;                           // outside FP32's normal range: the FP64 test decides
+	const float t[3] = { (float)q[0], (float)q[1], (float)q[2] };
 	float d[3];
 	for (int k = 0; k < 3; k++)
 		d[k] = ((R[3 * k] * B.rc[0] + R[3 * k + 1] * B.rc[1]) + R[3 * k + 2] * B.rc[2] + t[k]) - B.ce[k];
@@ -457,7 +432,7 @@ PW_HD int boxes_disjoint32(const double *q, const DisBoxes32 &B, float slack = 1
 	const float tinf = fmaxf(fmaxf(fabsf(t[0]), fabsf(t[1])), fabsf(t[2]));
 	const float scale = ((fabsf(B.rc[0]) + fabsf(B.rc[1])) + fabsf(B.rc[2])) + tinf + B.ce_abs + 2.f * d1 +
 	                    ((B.eh[0] + B.eh[1]) + B.eh[2]) + ((B.rh[0] + B.rh[1]) + B.rh[2]);
-	const float e = slack * (1300.f * U32 * K * scale);
+	const float e = slack * (1100.f * U32 * K * scale);
 	if (!(e < 1.0e30f))
 		return -1;                           // not finite: the FP64 test decides
 	bool undecided = false;
