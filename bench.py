@@ -77,13 +77,16 @@ WORKLOADS = {
                  W.cfg_interlocking_tori, 65536),
     "keyconf": ("key-configuration candidates checked/sec (enum_free_configuration, 256 spins, only_median)",
                 W.cfg_interlocking_tori, 8192),
+    "visibility": ("is_valid_transition pairs/sec (calculate_visibility_matrix of free interlocking-tori "
+                   "states, verify_magnitude 0.00625)", W.cfg_interlocking_tori, 2048),
     "touch": ("touch samples/sec (calc_touch: 128 random segments per key to first contact)",
               W.cfg_interlocking_tori, 8192),
 }
-ROW_WORKLOADS = ("disentangled", "contacts", "keyconf", "touch")
+ROW_WORKLOADS = ("disentangled", "contacts", "keyconf", "touch", "visibility")
 KEYCONF_SPINS = 256          # envconfig.py:134 NumberOfRotations
 KEYCONF_MARGIN = 1e-6        # envconfig.py:136 Margin
 TOUCH_PER_KEY = 128          # envconfig.py:141 OversamplingClearanceSample
+VIS_DELTA = 0.0125 * 4 / 8   # visibility-finder.py:33, the visibility matrix's verify_magnitude
 # OMPL motion workload: collision resolution and the spread of the motions' targets (OMPL units)
 OMPL_CDRES = 0.01
 OMPL_SIGMA = 2.0
@@ -664,9 +667,10 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(work.bytes_in() * ws),
                     "d2h_bytes_per_step": int(work.bytes_out() * ws)},
             "clocks": clk.summary(),
-            # segments: bounds, set-up, anchors, rounds, traversal, re-test, finalise (CUB's scan and
-            # sort not counted); states: traversal, re-test
-            "gpu_launches": (7 if args.workload == "segments" else 2) * args.steps,
+            # the library's own count per query (segments: bounds, set-up, rounds, anchors and
+            # traversal per round phase, re-test, finalise; states: traversal, re-test; CUB's scans
+            # and sorts not counted), summed over the timed steps
+            "gpu_launches": int(sum(st["kernel_launches"] for st in stats)),
             "detail": dict({"mismatches": parity["mismatches"] if parity else None,
                             "mismatch_sample": parity["mismatch_sample"] if parity else 0,
                             "parity": parity,
@@ -1186,6 +1190,12 @@ class RowJob:
             Vr, Fr = uw._cd(1)
             self.pairs = _surface_pairs(Ve, Fe, Vr, Fr, n, rng)
             self.units, self.unit = n * KEYCONF_SPINS, "checks/s"
+        elif name == "visibility":
+            q = W.uniform_states(4 * n, -2.0, 2.0, s, seed=seed)
+            ok = uw.is_valid_states(torch.from_numpy(q)).cpu().numpy()
+            self.keys = np.ascontiguousarray(q[ok][:n])
+            self.n = self.keys.shape[0]
+            self.units, self.unit = self.n * (self.n - 1) // 2, "pairs/s"
         else:
             q = W.uniform_states(4 * n, -2.0, 2.0, s, seed=seed)
             ok = uw.is_valid_states(torch.from_numpy(q)).cpu().numpy()
@@ -1194,21 +1204,36 @@ class RowJob:
         self.seed = seed
 
     def gpu(self):
-        """One step through the public API; returns the step's result."""
+        """One step through the public API; returns the step's result.  Counts the
+        library's kernel launches (its own report after each query, plus the
+        world-free state generators)."""
         from puzzletunneldiscovery_gb300 import sampling as SP
         uw = self.uw
         if self.name == "disentangled":
-            return uw.is_disentangled_states(self.a)
-        if self.name == "contacts":
+            res = uw.is_disentangled_states(self.a)
+        elif self.name == "contacts":
             res = uw.intersecting_segments_batch(self.q, flat=True)
-            self.launches += uw.last_stats()["work_items"]
-            return res
-        if self.name == "keyconf":
+        elif self.name == "keyconf":
             rp, rn, ep, en = self.pairs
-            return SP.enum_free_configurations(uw, rp, rn, ep, en, KEYCONF_MARGIN, KEYCONF_SPINS, only_median=True)
-        res, self.to = SP.calc_touch_batch(uw, self.keys, TOUCH_PER_KEY, uw.recommended_cres,
-                                           np.random.default_rng(4000 + self.seed))
+            res = SP.enum_free_configurations(uw, rp, rn, ep, en, KEYCONF_MARGIN, KEYCONF_SPINS, only_median=True)
+            self.launches += 1                                       # pw_keyconf_states
+        elif self.name == "visibility":
+            res = self._visibility(uw)
+            return res
+        else:
+            res, self.to = SP.calc_touch_batch(uw, self.keys, TOUCH_PER_KEY, uw.recommended_cres,
+                                               np.random.default_rng(4000 + self.seed))
+            self.launches += 1                                       # pw_touch_targets
+        self.launches += uw.last_stats()["kernel_launches"]
         return res
+
+    def _visibility(self, uw):
+        """calculate_visibility_matrix in chunks of pairs, each chunk's launches counted."""
+        out = uw.calculate_visibility_matrix(self.keys, True, VIS_DELTA)
+        # one segment query per chunk of 2^22 pairs; the last one's report stands for each
+        chunks = -(-self.units // uw._PAIR_CHUNK)
+        self.launches += chunks * uw.last_stats()["kernel_launches"]
+        return out
 
     def cpu(self, ow, m, threads):
         """(units, seconds, result) of the oracle on the first m units of the step."""
@@ -1222,6 +1247,12 @@ class RowJob:
             with cf.ThreadPoolExecutor(max_workers=threads) as ex:
                 res = list(ex.map(ow.intersecting_segments, self.q[:m]))
             units = m
+        elif self.name == "visibility":
+            lo, hi = np.triu_indices(m, 1)
+            codes, _ = ow.segments_first_contact(self.keys[lo], self.keys[hi], VIS_DELTA, mode=1, nthreads=threads)
+            res = np.zeros((m, m), np.int8)
+            res[lo, hi] = res[hi, lo] = (codes == -1)
+            units = lo.shape[0]
         elif self.name == "keyconf":
             from oracle import oracle as O
             rp, rn, ep, en = (x[:m] for x in self.pairs)
@@ -1258,6 +1289,9 @@ class RowJob:
             return bad
         if self.name == "keyconf":
             return sum(0 if np.array_equal(x, y) else 1 for x, y in zip(gpu_res[:m], cpu_res))
+        if self.name == "visibility":
+            lo, hi = np.triu_indices(m, 1)
+            return int((gpu_res[:m, :m][lo, hi] != cpu_res[lo, hi]).sum())
         # touch: the GPU's tuples against the oracle's first contacts (done = no contact), and the
         # full tuples of the first 256 segments against the oracle's transit loop
         k = m * TOUCH_PER_KEY
@@ -1363,21 +1397,26 @@ def run_rows(args):
         O.build()
         ow = O.OracleWorld(Ve, Fe, Vr, Fr)
         cores = os.cpu_count() or 1
-        m = max(1, min(job.n, 64 if args.workload in ("contacts", "keyconf", "touch") else 65536))
+        m = max(1, min(job.n, 64 if args.workload in ("contacts", "keyconf", "touch", "visibility") else 65536))
         while True:
             units, dt, cres = job.cpu(ow, m, cores)
             if dt >= args.cpu_seconds or m >= job.n:
                 break
-            m = min(job.n, max(m * 2, int(m * args.cpu_seconds / max(dt, 1e-3) * 1.1)))
+            grow = args.cpu_seconds / max(dt, 1e-3)
+            if args.workload == "visibility":
+                grow = math.sqrt(grow)               # all pairs among m keys: units grow as m^2
+            m = min(job.n, max(m * 2, int(m * grow * 1.05)))
         cpu = {"value": units / dt, "unit": job.unit, "cores": cores, "kind": "port",
                "sample": "the first %d %s of the step (%d units, %.1f s)"
                          % (m, {"disentangled": "states", "contacts": "states", "keyconf": "surface pairs",
-                                "touch": "keys"}[args.workload], units, dt)}
+                                "touch": "keys", "visibility": "keys (all pairs among them)"}[args.workload], units,
+                            dt)}
         parity = {"mismatches": job.mismatches(ow, res, cres, m), "mismatch_sample": int(m),
                   "compared": {"disentangled": "is_disentangled verdict of every state",
                                "contacts": "contact rows (face pairs, segment ends, lengths) of every state",
                                "keyconf": "the free median spins of every surface pair",
-                               "touch": "done flag of every segment; full transit tuples of the first 256"}[
+                               "touch": "done flag of every segment; full transit tuples of the first 256",
+                               "visibility": "every pair's visibility bit among the sampled keys"}[
                       args.workload]}
     cfg = {"workload": "%s/interlocking_tori" % args.workload, "units_per_step": job.units,
            "l2": "flushed (256 MB write) between timed steps",
@@ -1388,6 +1427,9 @@ def run_rows(args):
         cfg.update({"keys": job.keys.shape[0], "segments_per_key": TOUCH_PER_KEY, "stepping": uw.recommended_cres})
     elif args.workload == "contacts":
         cfg.update({"states": job.n, "states_drawn_from": "colliding uniform states in [-0.6, 0.6]^3 (world)"})
+    elif args.workload == "visibility":
+        cfg.update({"keys": job.n, "pairs": job.units, "verify_magnitude": VIS_DELTA,
+                    "keys_drawn_from": "free uniform states in [-2, 2]^3 (world)"})
     detail = {"mismatches": parity["mismatches"] if parity else None,
               "mismatch_sample": parity["mismatch_sample"] if parity else 0, "parity": parity, "step_ms": step_ms,
               "node_boxes": {"states": uw.get_node_boxes(0), "segments": uw.get_node_boxes(1)}}
@@ -1403,11 +1445,8 @@ def run_rows(args):
             "dtype": "f64 box test" if args.workload == "disentangled" else "f32 traversal + f64 state math/re-tests",
             "data": "synthetic (seeded)", "config": cfg, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "clocks": clk.summary(),
-            # per step: k_disentangled; contacts: collect, evaluate, sort keys and gather per chunk of states
-            # (counted by the library); keyconf: traversal + re-test; touch: the segment query's 7 kernels and
-            # the contact-state rebuild
-            "gpu_launches": job.timed_launches if args.workload == "contacts" else
-            {"disentangled": 1, "keyconf": 2, "touch": 8}[args.workload] * args.steps,
+            # counted by the library per query (CUB's sorts and scans not counted)
+            "gpu_launches": job.timed_launches,
             "detail": detail}
     print(json.dumps(line), flush=True)
     if parity and parity["mismatches"]:
@@ -1418,12 +1457,16 @@ def run_rows(args):
 def _row_h2d(job):
     if job.name == "contacts":
         return int(job.q.nbytes)
+    if job.name == "visibility":
+        return int(job.keys.nbytes)
     if job.name == "keyconf":
         return int(job.n * KEYCONF_SPINS * 56)
     return int(job.units * 2 * 56)
 
 
 def _row_d2h(job, res):
+    if job.name == "visibility":
+        return int(job.n * job.n)
     if job.name == "contacts":
         return int(sum(x.nbytes for x in res[:4]) + res[3].shape[0] * 4 + res[4].nbytes)
     if job.name == "keyconf":
@@ -1448,6 +1491,11 @@ class _RefRowJob(RowJob):
             self.q = q[~ow.is_valid(q)][:n]
             self.n = self.q.shape[0]
             self.units, self.unit = self.n, "states/s"
+        elif name == "visibility":
+            q = W.uniform_states(4 * n, -2.0, 2.0, s, seed=0)
+            self.keys = np.ascontiguousarray(q[ow.is_valid(q)][:n])
+            self.n = self.keys.shape[0]
+            self.units, self.unit = self.n * (self.n - 1) // 2, "pairs/s"
         elif name == "keyconf":
             Ve, Vr = ow.vertices(0), ow.vertices(1)
             self.pairs = _surface_pairs(Ve, np.asarray(Fe, np.int64), Vr, np.asarray(Fr, np.int64), n, rng)
@@ -1476,8 +1524,8 @@ def run_rows_reference(args):
     ow = O.OracleWorld(Ve, Fe, Vr, Fr)
     job = _RefRowJob(args.workload, ow, args.n, Fe, Fr)
     cores = os.cpu_count() or 1
-    per = {"disentangled": 500, "contacts": 1, "keyconf": 1, "touch": 1}[args.workload]
-    div = {"disentangled": 1, "contacts": 8, "keyconf": 4, "touch": 4}[args.workload]
+    per = {"disentangled": 500, "contacts": 1, "keyconf": 1, "touch": 1, "visibility": 1}[args.workload]
+    div = {"disentangled": 1, "contacts": 8, "keyconf": 4, "touch": 4, "visibility": 16}[args.workload]
     m = max(1, min(job.n, args.ref_sample // div * per))
     times, units = [], 0
     for it in range(args.warmup + args.steps):

@@ -98,6 +98,9 @@ typedef struct pw_query_stats {
 	int64_t device_errors;       /* PW_DEVERR_* bits: a device-side capacity or consistency check
 	                                failed (the affected segments carry PW_STEP_INVALID), or a
 	                                state was not finite */
+	int64_t kernel_launches;     /* kernels of this library the query launched (CUB's sorts and scans
+	                                not counted); pw_world_segments_contact_states adds its one to the
+	                                segment query it follows */
 } pw_query_stats;
 
 /* Thread-local message for the last failing call on this thread. */

@@ -78,7 +78,8 @@ class QueryStats(ctypes.Structure):
                 ("inline_retests", ctypes.c_int64), ("work_items", ctypes.c_int64),
                 ("reference_checks", ctypes.c_int64), ("detailed_chunks", ctypes.c_int64),
                 ("traverse_ms", ctypes.c_double),
-                ("retest_ms", ctypes.c_double), ("device_errors", ctypes.c_int64)]
+                ("retest_ms", ctypes.c_double), ("device_errors", ctypes.c_int64),
+                ("kernel_launches", ctypes.c_int64)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}

@@ -140,6 +140,7 @@ struct pw_world {
 	cudaEvent_t ev[4] = { nullptr, nullptr, nullptr, nullptr }; // traversal start/end, re-test start/end
 	bool timed = false;
 	int64_t last_states = -1;   // size of the last state batch (-1: the last query was segments)
+	int64_t last_launches = 0;  // kernels of this library the last query launched (pw_query_stats)
 	int num_sms = 0;
 	// graph mode: segment queries make no host synchronisation and no allocation;
 	// they run within the scratch sizes that pw_segments_reserve or the last

@@ -1507,6 +1507,7 @@ extern "C" int pw_states_valid(pw_world *w, const double *states, int64_t n, uin
 	if (!w->graph_mode && (rc = mark(w, 0, st)))
 		return rc;
 	launch_states<RETEST_CAP>(w, grid, smem, st, states, n, valid, ctr, rq);
+	w->last_launches = 2;
 	if (!w->graph_mode)
 		mark(w, 1, st);
 	StateSrc src{ states, nullptr, nullptr, nullptr, nullptr, nullptr };
@@ -1570,6 +1571,7 @@ extern "C" int pw_states_disentangled(pw_world *w, const double *states, int64_t
 	uint32_t *queue = (uint32_t *)w->dis_queue.ptr;
 	k_disentangled<<<(unsigned)blocks, DIS_BLOCK, 0, st>>>(dis_boxes32(B), states, n, out, queue, ctr);
 	k_disentangled64<<<(unsigned)(w->num_sms * 4), 256, 0, st>>>(B, states, queue, n, ctr, out);
+	w->last_launches = 2;
 	PW_CUDA(cudaGetLastError());
 	return PW_OK;
 }
@@ -1699,6 +1701,7 @@ extern "C" int pw_segments_first_contact(pw_world *w, const double *from, const 
 	}
 	k_seg_finalize<<<G, B, 0, st>>>(first_step, params, n, ctr);
 	PW_CUDA(cudaGetLastError());
+	w->last_launches = 3 + 2 * (phased ? SEG_PHASES : 1) + 2;   // bound, set-up, rounds; the phases; re-test, finalise
 	w->last_seg_from = from;
 	w->last_seg_to = to;
 	w->last_seg_n = n;
@@ -1783,6 +1786,7 @@ extern "C" int pw_world_segments_contact_states(pw_world *w, const double *from,
 	const bool same = w->last_seg_n == n && w->last_seg_from == from && w->last_seg_to == to &&
 	                  w->last_seg_delta == verify_delta && w->last_seg_mode == PW_SEG_TRANSIT &&
 	                  w->seg_params.ptr && n > 0;
+	w->last_launches += 1;   // either path launches one kernel
 	if (!same)
 		return pw_segments_contact_states(from, to, first_step, n, verify_delta, last_free, contact, done, last_tau,
 		                                  tau, err_flag, stream);
@@ -2147,6 +2151,7 @@ static int isect_run(pw_world *w, const double *q, int64_t n, int64_t capacity, 
 	w->last_states = n;
 	w->last_stream = nullptr;
 	w->timed = false;
+	w->last_launches = (int64_t)launches;
 	if (capacity < base)
 		return pw_fail(PW_ERR_CAPACITY, std::string(who) + ": capacity smaller than the row count");
 	return PW_OK;
@@ -2205,6 +2210,7 @@ extern "C" int pw_world_last_stats(pw_world *w, pw_query_stats *out)
 	out->reference_checks = w->last_states >= 0 ? w->last_states : (int64_t)c.ref_checks;
 	out->detailed_chunks = (int64_t)c.stat[STAT_DETAILED];
 	out->device_errors = (int64_t)c.error;
+	out->kernel_launches = w->last_launches;
 	if (w->timed) {
 		float a = 0.f, b = 0.f;
 		PW_CUDA(cudaEventElapsedTime(&a, w->ev[0], w->ev[1]));
@@ -2293,6 +2299,7 @@ extern "C" int pw_states_valid_noalloc(pw_world *w, const double *states, int64_
 	// kernel have the same resources, so they share the cached grid)
 	const int grid = launch_grid(w, 0, states_kernel<NOALLOC_RETEST_CAP>(w), smem);
 	launch_states<NOALLOC_RETEST_CAP>(w, grid, smem, st, states, n, valid, ctr, rq);
+	w->last_launches = 2;
 	StateSrc src{ states, nullptr, nullptr, nullptr, nullptr, nullptr };
 	k_retest<NOALLOC_RETEST_CAP><<<w->num_sms * 4, 256, 0, st>>>(w->dev, src, valid, nullptr, ctr, rq);
 	PW_CUDA(cudaGetLastError());

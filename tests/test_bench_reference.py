@@ -16,6 +16,7 @@ ARGS = {
     "contacts": ["--n", "64", "--ref-sample", "32"],
     "keyconf": ["--n", "256", "--ref-sample", "32"],
     "touch": ["--n", "64", "--ref-sample", "16"],
+    "visibility": ["--n", "64", "--ref-sample", "160"],
 }
 
 
