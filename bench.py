@@ -87,6 +87,7 @@ KEYCONF_SPINS = 256          # envconfig.py:134 NumberOfRotations
 KEYCONF_MARGIN = 1e-6        # envconfig.py:136 Margin
 TOUCH_PER_KEY = 128          # envconfig.py:141 OversamplingClearanceSample
 VIS_DELTA = 0.0125 * 4 / 8   # visibility-finder.py:33, the visibility matrix's verify_magnitude
+BVH_KIND = "topdown"         # the worlds' BVH hierarchy (--bvh)
 # OMPL motion workload: collision resolution and the spread of the motions' targets (OMPL units)
 OMPL_CDRES = 0.01
 OMPL_SIGMA = 2.0
@@ -175,6 +176,7 @@ def run_ompl(args):
     uw.load_robot_mesh(Vr, Fr)
     uw.enforceRobotCenter(c)
     uw.scaleToUnit()
+    uw.set_bvh(BVH_KIND)
     uw.angleModel(0.0, 0.0)
     A, B, lo, hi = _ompl_motions(P, args.n, rank)
     a = torch.from_numpy(A).to(dev)
@@ -513,6 +515,7 @@ def run_ours(args):
     uw.load_env_mesh(Ve, Fe)
     uw.load_robot_mesh(Vr, Fr)
     uw.scaleToUnit()
+    uw.set_bvh(BVH_KIND)
     uw.angleModel(0.0, 0.0)
     work = Work(args.workload, args.n, rank, uw.scene_scale, Ve)
     a = torch.from_numpy(work.q0).to(dev)
@@ -658,7 +661,7 @@ def run_ours(args):
                   "n_states_per_gpu": args.n}
         extra = {"free_fraction": float(fc.astype(bool).mean())}
     config.update({"l2": "flushed (256 MB write) between timed steps; per-step working set > L2",
-                   "parallelism": "replicas" if ws == 1 else "shard-per-rank (weak)"})
+                   "parallelism": "replicas" if ws == 1 else "shard-per-rank (weak)", "bvh": BVH_KIND})
     line = {"metric": work.metric, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 traversal + f64 state math/re-tests",
@@ -757,6 +760,7 @@ def surrogate_measure(args, local, rank, n, steps, warmup, with_cpu, e2e=True):
     uw.load_env_mesh(Ve, Fe)
     uw.load_robot_mesh(Vr, Fr)
     uw.scaleToUnit()
+    uw.set_bvh(BVH_KIND)
     uw.angleModel(0.0, 0.0)
     gen = torch.Generator(device=dev)
     gen.manual_seed(1000 + rank)
@@ -980,6 +984,7 @@ def run_narrow(args):
     uw.load_env_mesh(Ve, Fe)
     uw.load_robot_mesh(Vr, Fr)
     uw.scaleToUnit()
+    uw.set_bvh(BVH_KIND)
     uw.angleModel(0.0, 0.0)
     s = uw.scene_scale
     lo, hi = Ve.min(0) - 0.5, Ve.max(0) + 0.5
@@ -1013,6 +1018,7 @@ def run_narrow(args):
     uw_plain.load_env_mesh(Ve, Fe)
     uw_plain.load_robot_mesh(Vr, Fr)
     uw_plain.scaleToUnit()
+    uw_plain.set_bvh(BVH_KIND)
     uw_plain.angleModel(0.0, 0.0)
     uw_plain.set_node_boxes(boxes["states"], 0)
     uw_plain.set_node_boxes(boxes["segments"], 1)
@@ -1324,6 +1330,7 @@ def run_rows(args):
     uw.load_env_mesh(Ve, Fe)
     uw.load_robot_mesh(Vr, Fr)
     uw.scaleToUnit()
+    uw.set_bvh(BVH_KIND)
     uw.angleModel(0.0, 0.0)
     job = RowJob(args.workload, uw, args.n, rank)
     stream = torch.cuda.current_stream(dev)
@@ -1662,6 +1669,7 @@ def run_profile_case(args):
         uw.load_robot_mesh(Vr, Fr)
         uw.enforceRobotCenter(c)
         uw.scaleToUnit()
+        uw.set_bvh(BVH_KIND)
         uw.angleModel(0.0, 0.0)
         A, B, lo, hi = _ompl_motions(P, n, 0)
         a, b = torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev)
@@ -1675,6 +1683,7 @@ def run_profile_case(args):
     uw.load_env_mesh(Ve, Fe)
     uw.load_robot_mesh(Vr, Fr)
     uw.scaleToUnit()
+    uw.set_bvh(BVH_KIND)
     uw.angleModel(0.0, 0.0)
     if args.node_boxes:
         uw.set_node_boxes(args.node_boxes)
@@ -1771,9 +1780,13 @@ def main():
     ap.add_argument("--profile-case", choices=["states", "segments", "mlp", "train", "plate", "ompl", "disentangled", "all"],
                     default=None,
                     help="run a small fixed workload for an ncu capture instead of the benchmark")
+    ap.add_argument("--bvh", choices=["topdown", "morton"], default="topdown",
+                    help="the BVH hierarchy of the worlds (top-down principal-axis splits or Morton LBVH)")
     ap.add_argument("--node-boxes", choices=["aligned", "oriented"], default=None,
                     help="profile cases: the BVH node boxes (default: the world's default)")
     args = ap.parse_args()
+    global BVH_KIND
+    BVH_KIND = args.bvh
     if args.profile_case:
         args.n = args.n or 1_000_000
         run_profile_case(args)

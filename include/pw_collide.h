@@ -48,6 +48,10 @@ extern "C" {
 #define PW_BOXES_ALIGNED 0     /* boxes aligned with each mesh's own frame */
 #define PW_BOXES_ORIENTED 1    /* boxes along the principal axes of each node's vertices (default) */
 
+/* Hierarchy of the BVHs (pw_world_set_bvh). */
+#define PW_BVH_TOPDOWN 0       /* top-down splits on each node's principal axis (default) */
+#define PW_BVH_MORTON 1        /* Karras's LBVH over Morton codes */
+
 /* Round phases of segment queries (pw_world_set_segment_phases). */
 #define PW_PHASES_AUTO 0       /* phases when a call has at least 2^22 32-step chunks (default) */
 #define PW_PHASES_OFF 1        /* every round in one phase */
@@ -221,6 +225,15 @@ PW_API int pw_world_get_launch_config(pw_world *w, int kernel, int *width, int *
  * allowed in graph mode (captured launches hold the kernel). */
 PW_API int pw_world_set_node_boxes(pw_world *w, int kernel, int kind);
 PW_API int pw_world_get_node_boxes(pw_world *w, int kernel, int *kind);
+
+/* host: the hierarchy the next BVH build (pw_world_angle_model) uses.  Top-down:
+ * each range of triangles split at the mean of their centroids projected on the
+ * principal axis of their vertices (the OBBTree split, as FCL's OBBRSS build
+ * splits along a node's box axis); Morton: Karras's LBVH.  Both carry the
+ * same leaf order semantics and both node-box kinds; verdicts do not depend on
+ * the choice. */
+PW_API int pw_world_set_bvh(pw_world *w, int kind);
+PW_API int pw_world_get_bvh(const pw_world *w, int *kind);
 
 /* Round phases of pw_segments_first_contact.  The work of a segment query is its
  * 32-step chunks in chunk-major order (chunk j of every segment before chunk j + 1),

@@ -28,6 +28,8 @@ PW_STEP_NONE = -2
 PW_STEP_INVALID = -3
 PW_BOXES_ALIGNED = 0
 PW_BOXES_ORIENTED = 1
+PW_BVH_TOPDOWN = 0
+PW_BVH_MORTON = 1
 PW_PHASES_AUTO = 0
 PW_PHASES_OFF = 1
 PW_PHASES_ON = 2
@@ -46,6 +48,7 @@ EXPORTS = (
     "pw_world_get_launch_config", "pw_expansion_crossings", "pw_world_scratch_epoch", "pw_expand_states",
     "pw_ompl_check_motions", "pw_ompl_motion_states", "pw_world_set_node_boxes", "pw_world_get_node_boxes",
     "pw_world_set_segment_phases", "pw_world_get_segment_phases", "pw_keyconf_states", "pw_touch_targets",
+    "pw_world_set_bvh", "pw_world_get_bvh",
     "pw_intersecting_segments_batch",
     # include/pw_mlp.h
     "pw_mlp_create", "pw_mlp_destroy", "pw_mlp_num_params", "pw_mlp_get_params", "pw_mlp_set_params",
@@ -154,6 +157,8 @@ def load():
         "pw_world_set_node_boxes": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
         "pw_world_get_node_boxes": (ctypes.c_int, [vp, ctypes.c_int, i32p]),
         "pw_world_set_segment_phases": (ctypes.c_int, [vp, ctypes.c_int]),
+        "pw_world_set_bvh": (ctypes.c_int, [vp, ctypes.c_int]),
+        "pw_world_get_bvh": (ctypes.c_int, [vp, i32p]),
         "pw_keyconf_states": (ctypes.c_int, [vp, vp, vp, vp, i64, ctypes.c_double, vp, vp, i64, ctypes.c_int, vp, vp]),
         "pw_touch_targets": (ctypes.c_int, [vp, i64, ctypes.c_int, ctypes.c_uint64, vp, vp, vp]),
         "pw_world_get_segment_phases": (ctypes.c_int, [vp, i32p]),

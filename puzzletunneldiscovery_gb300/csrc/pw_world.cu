@@ -372,6 +372,22 @@ extern "C" int pw_world_angle_model(pw_world *w, float latitude, float longitude
 	return PW_OK;
 }
 
+extern "C" int pw_world_set_bvh(pw_world *w, int kind)
+{
+	if (!w || (kind != PW_BVH_TOPDOWN && kind != PW_BVH_MORTON))
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_set_bvh: bad argument");
+	w->bvh_topdown = kind == PW_BVH_TOPDOWN;
+	return PW_OK;
+}
+
+extern "C" int pw_world_get_bvh(const pw_world *w, int *kind)
+{
+	if (!w || !kind)
+		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_get_bvh: bad argument");
+	*kind = w->bvh_topdown ? PW_BVH_TOPDOWN : PW_BVH_MORTON;
+	return PW_OK;
+}
+
 extern "C" int pw_world_set_perturbation(pw_world *w, const double q[7])
 {
 	if (!w || !q)
@@ -954,6 +970,112 @@ __global__ void k_depth(int n, const int32_t *parent, int *maxdepth)
 	atomicMax(maxdepth, d);
 }
 
+// Top-down hierarchy over the triangles (the OBBTree split, Gottschalk, Lin and
+// Manocha 1996): a range of triangles is split at the mean of their centroids
+// projected on the principal axis of their vertices; where that leaves one side
+// empty, or below depth 40, at the median of the projections instead, which
+// bounds the depth.  Internal nodes are numbered in preorder (root 0) and cover
+// the contiguous slot range rlo..rhi; leaf j (the triangle order[j]) is node
+// n - 1 + j.  Oriented boxes fitted to these nodes are tighter than to the
+// Morton-order hierarchy, whose splits are axis-aligned by construction.
+static void build_topdown(const std::vector<double> &V, const std::vector<uint32_t> &F, std::vector<uint32_t> &order,
+                          std::vector<int32_t> &left, std::vector<int32_t> &right, std::vector<int32_t> &parent,
+                          std::vector<int32_t> &rlo, std::vector<int32_t> &rhi)
+{
+	const int n = (int)(F.size() / 3);
+	const int leaf_base = n - 1;
+	order.resize(n);
+	for (int i = 0; i < n; i++)
+		order[i] = (uint32_t)i;
+	left.assign(n > 1 ? n - 1 : 0, -1);
+	right.assign(n > 1 ? n - 1 : 0, -1);
+	rlo.assign(n > 1 ? n - 1 : 0, 0);
+	rhi.assign(n > 1 ? n - 1 : 0, 0);
+	parent.assign(n > 0 ? 2 * n - 1 : 0, -1);
+	if (n < 2)
+		return;
+	std::vector<double> cen(3 * (size_t)n), proj(n);
+	for (int t = 0; t < n; t++)
+		for (int c = 0; c < 3; c++)
+			cen[3 * t + c] = (V[3 * F[3 * t] + c] + V[3 * F[3 * t + 1] + c] + V[3 * F[3 * t + 2] + c]) / 3.0;
+	struct Task {
+		int a, b, id, depth;
+	};
+	std::vector<Task> stack;
+	stack.push_back(Task{ 0, n, 0, 0 });
+	int next = 1;
+	while (!stack.empty()) {
+		const Task k = stack.back();
+		stack.pop_back();
+		// principal axis of the range's vertices
+		double mu[3] = { 0, 0, 0 };
+		const double inv = 1.0 / (3.0 * (k.b - k.a));
+		for (int i = k.a; i < k.b; i++)
+			for (int v = 0; v < 3; v++)
+				for (int c = 0; c < 3; c++)
+					mu[c] += V[3 * F[3 * order[i] + v] + c] * inv;
+		double S[6] = { 0, 0, 0, 0, 0, 0 };
+		for (int i = k.a; i < k.b; i++)
+			for (int v = 0; v < 3; v++) {
+				const double *p = &V[3 * F[3 * order[i] + v]];
+				const double d[3] = { p[0] - mu[0], p[1] - mu[1], p[2] - mu[2] };
+				S[0] += d[0] * d[0]; S[1] += d[1] * d[1]; S[2] += d[2] * d[2];
+				S[3] += d[0] * d[1]; S[4] += d[0] * d[2]; S[5] += d[1] * d[2];
+			}
+		double E[9];
+		pwm::jacobi_eigen3(S, E);
+		// the row of E with the largest variance
+		int best = 0;
+		double bv = -1.0;
+		for (int r = 0; r < 3; r++) {
+			const double *e = E + 3 * r;
+			const double var = e[0] * (S[0] * e[0] + S[3] * e[1] + S[4] * e[2]) +
+			                   e[1] * (S[3] * e[0] + S[1] * e[1] + S[5] * e[2]) +
+			                   e[2] * (S[4] * e[0] + S[5] * e[1] + S[2] * e[2]);
+			if (var > bv) {
+				bv = var;
+				best = r;
+			}
+		}
+		const double *ax = E + 3 * best;
+		double mean = 0.0;
+		for (int i = k.a; i < k.b; i++) {
+			const double *c = &cen[3 * order[i]];
+			proj[order[i]] = ax[0] * c[0] + ax[1] * c[1] + ax[2] * c[2];
+			mean += proj[order[i]];
+		}
+		mean /= (double)(k.b - k.a);
+		int mid = k.a;
+		if (k.depth < 40) {
+			int i = k.a, j = k.b - 1;
+			while (i <= j) {
+				if (proj[order[i]] < mean)
+					i++;
+				else
+					std::swap(order[i], order[j--]);
+			}
+			mid = i;
+		}
+		if (mid == k.a || mid == k.b) {
+			mid = (k.a + k.b) / 2;
+			std::nth_element(order.begin() + k.a, order.begin() + mid, order.begin() + k.b,
+			                 [&](uint32_t x, uint32_t y) { return proj[x] < proj[y] || (proj[x] == proj[y] && x < y); });
+		}
+		const int lc = mid - k.a == 1 ? leaf_base + k.a : next++;
+		if (mid - k.a > 1)
+			stack.push_back(Task{ k.a, mid, lc, k.depth + 1 });
+		const int rc = k.b - mid == 1 ? leaf_base + mid : next++;
+		if (k.b - mid > 1)
+			stack.push_back(Task{ mid, k.b, rc, k.depth + 1 });
+		left[k.id] = lc;
+		right[k.id] = rc;
+		parent[lc] = k.id;
+		parent[rc] = k.id;
+		rlo[k.id] = k.a;
+		rhi[k.id] = k.b - 1;
+	}
+}
+
 template <typename T>
 static cudaError_t walloc(pw_world *w, T **p, size_t count)
 {
@@ -1055,23 +1177,39 @@ int pw_build_mesh_device(pw_world *w, MeshDev &m, const std::vector<double> &V64
 	cudaMemset(maxdepth, 0, sizeof(int));
 	cudaMemset(parent, 0xff, sizeof(int32_t) * nnodes);
 	k_tri_prep<<<G, B>>>(m.V64, m.F, n, ta, tb, tc, tlo, thi, cen);
-	k_bounds<<<1, 256>>>(cen, n, bounds);
-	k_morton<<<G, B>>>(cen, n, bounds, keys, vals);
-	size_t tmp_bytes = 0;
-	cudaError_t se = cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys2, vals, vals2, n, 0, 30);
-	if (se != cudaSuccess) {
-		cleanup();
-		return pw_cuda_fail(se, "BVH sort (size query)");
+	cudaError_t se = cudaSuccess;
+	if (w->bvh_topdown) {
+		// the hierarchy built on the host (build_topdown), uploaded in the Karras layout
+		std::vector<uint32_t> h_order;
+		std::vector<int32_t> h_left, h_right, h_parent, h_rlo, h_rhi;
+		build_topdown(V64, F, h_order, h_left, h_right, h_parent, h_rlo, h_rhi);
+		cudaMemcpy(vals2, h_order.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice);
+		cudaMemcpy(parent, h_parent.data(), sizeof(int32_t) * nnodes, cudaMemcpyHostToDevice);
+		if (n > 1) {
+			cudaMemcpy(left, h_left.data(), sizeof(int32_t) * (n - 1), cudaMemcpyHostToDevice);
+			cudaMemcpy(right, h_right.data(), sizeof(int32_t) * (n - 1), cudaMemcpyHostToDevice);
+			cudaMemcpy(rlo, h_rlo.data(), sizeof(int32_t) * (n - 1), cudaMemcpyHostToDevice);
+			cudaMemcpy(rhi, h_rhi.data(), sizeof(int32_t) * (n - 1), cudaMemcpyHostToDevice);
+		}
+	} else {
+		k_bounds<<<1, 256>>>(cen, n, bounds);
+		k_morton<<<G, B>>>(cen, n, bounds, keys, vals);
+		size_t tmp_bytes = 0;
+		se = cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys2, vals, vals2, n, 0, 30);
+		if (se != cudaSuccess) {
+			cleanup();
+			return pw_cuda_fail(se, "BVH sort (size query)");
+		}
+		void *cub_tmp = nullptr;
+		TAL(cub_tmp, tmp_bytes);
+		se = cub::DeviceRadixSort::SortPairs(cub_tmp, tmp_bytes, keys, keys2, vals, vals2, n, 0, 30);
+		if (se != cudaSuccess) {
+			cleanup();
+			return pw_cuda_fail(se, "BVH sort");
+		}
+		if (n > 1)
+			k_karras<<<(n - 1 + B - 1) / B, B>>>(keys2, n, left, right, parent, rlo, rhi);
 	}
-	void *cub_tmp = nullptr;
-	TAL(cub_tmp, tmp_bytes);
-	se = cub::DeviceRadixSort::SortPairs(cub_tmp, tmp_bytes, keys, keys2, vals, vals2, n, 0, 30);
-	if (se != cudaSuccess) {
-		cleanup();
-		return pw_cuda_fail(se, "BVH sort");
-	}
-	if (n > 1)
-		k_karras<<<(n - 1 + B - 1) / B, B>>>(keys2, n, left, right, parent, rlo, rhi);
 	k_refit<<<G, B>>>(vals2, n, tlo, thi, ta, tb, tc, m.triA, m.triB, m.triC, blo, bhi, left, right, parent, flags);
 	k_finalize<<<(nnodes + B - 1) / B, B>>>(nnodes, n, blo, bhi, left, right, m.triA, m.nodeA, m.nodeB);
 	// oriented boxes on the same hierarchy: slot moments about the vertices' box centre,

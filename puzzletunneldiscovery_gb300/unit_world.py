@@ -355,6 +355,18 @@ class UnitWorld:
         check(self._L.pw_world_get_node_boxes(self._h, int(kernel), ctypes.byref(k)), "get_node_boxes")
         return "oriented" if k.value == _lib.PW_BOXES_ORIENTED else "aligned"
 
+    _BVH = {"topdown": _lib.PW_BVH_TOPDOWN, "morton": _lib.PW_BVH_MORTON}
+
+    def set_bvh(self, kind: str) -> None:
+        """The hierarchy the next BVH build (angleModel) uses: "topdown" (default)
+        or "morton"; the verdicts do not depend on it."""
+        check(self._L.pw_world_set_bvh(self._h, self._BVH[kind]), "set_bvh")
+
+    def get_bvh(self) -> str:
+        k = ctypes.c_int32()
+        check(self._L.pw_world_get_bvh(self._h, ctypes.byref(k)), "get_bvh")
+        return {v: name for name, v in self._BVH.items()}[k.value]
+
     _PHASES = {"auto": _lib.PW_PHASES_AUTO, "off": _lib.PW_PHASES_OFF, "on": _lib.PW_PHASES_ON}
 
     def set_segment_phases(self, mode: str) -> None:
