@@ -189,10 +189,10 @@ def run_ompl(args):
             dist.barrier()
         torch.cuda.synchronize(dev)
 
-    # the states kernel's node boxes, picked on the motions themselves
-    from puzzletunneldiscovery_gb300.autotune import _tune_boxes
-    box_kind, box_ms, _ = _tune_boxes(uw, 0, lambda: OC._check_motions_dev(uw, a, b, lo, hi, OMPL_CDRES)[0], 1, stream,
-                                      "verdicts")
+    # the BVH hierarchy and the states kernel's node boxes, picked on the motions themselves
+    from puzzletunneldiscovery_gb300.autotune import pick_bvh
+    picked = pick_bvh(uw, run=lambda: OC._check_motions_dev(uw, a, b, lo, hi, OMPL_CDRES)[0], kernel=0)
+    box_kind, box_ms = picked["boxes"]["states"], picked["ms"]
     for _ in range(args.warmup):
         OC._check_motions_dev(uw, a, b, lo, hi, OMPL_CDRES)
     barrier()
@@ -276,7 +276,7 @@ def run_ompl(args):
             # traversal, re-test, reduction (a lower bound: each pass starts its own window)
             "gpu_launches": (4 + 4 * windows) * args.steps,
             "detail": {"mismatches": cpu_mism, "mismatch_sample": cpu_n,
-                       "node_boxes": {"states": box_kind, "ms": box_ms},
+                       "node_boxes": {"states": box_kind, "ms": box_ms}, "bvh": picked["bvh"],
                        "states_checked_per_step": states, "states_per_motion": states / args.n,
                        "valid_fraction": float(verdicts.mean()), "windows": windows, "step_ms": step_ms}}
     print(json.dumps(line))

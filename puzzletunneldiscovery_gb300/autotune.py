@@ -1,7 +1,10 @@
 """Launch-shape autotuner and CUDA-graph replay for the traversal kernels.
 
-``autotune`` times the persistent traversal kernels of one world on a sample of
-the caller's own workload: first the two kinds of BVH node box (axis-aligned or
+``pick_bvh`` rebuilds a world with each BVH hierarchy (top-down principal-axis
+splits, or the Morton LBVH) and keeps the faster one with its faster node-box
+kind for a sample of the caller's queries.  ``autotune`` times the persistent
+traversal kernels of one world on a sample of the caller's own workload: first
+the two kinds of BVH node box (axis-aligned or
 oriented, pw_world_set_node_boxes, per kernel), then, under the faster one, a grid of
 launch configurations (queries a warp takes per grab, traversal stack soft cap
 -- the point where a warp narrows from breadth-first to depth-first -- and
@@ -85,6 +88,48 @@ def pick_node_boxes(uw, states: torch.Tensor | None = None, segments=None, verif
         run = lambda: uw.first_contact_steps(q0, q1, verify_delta, mode)  # noqa: E731
         out["segments"], out["ms"]["segments"], _ = _tune_boxes(uw, 1, run, reps, stream, "first-contact steps")
     return out
+
+
+def pick_bvh(uw, states: torch.Tensor | None = None, segments=None, verify_delta: float = 0.001,
+             mode: int = _lib.PW_SEG_TRANSIT, reps: int = 1, run=None, kernel: int | None = None) -> dict:
+    """The BVH hierarchy and node-box kind for a world's workload: the world is
+    rebuilt with each hierarchy (pw_world_set_bvh, then angleModel), the box
+    kinds timed under each on the sample (states [N, 7], segments (q0, q1), or
+    any callable `run` returning a tensor, with the traversal `kernel` it
+    exercises: 0 states, 1 segments), and the fastest pair kept (the world is
+    left built with it).  Every combination must give the same results.
+    Returns {"bvh": kind, "boxes": {...}, "ms": {hierarchy: {box kind: ms}}}."""
+    if sum(x is not None for x in (states, segments, run)) != 1:
+        raise ValueError("pick_bvh: give one of states, segments or run")
+    if run is not None:
+        if kernel not in (0, 1):
+            raise ValueError("pick_bvh: a run needs its kernel (0 states, 1 segments)")
+        what = "results"
+        dev = torch.device("cuda", torch.cuda.current_device())
+    elif states is not None:
+        kernel, dev, what = 0, states.device, "verdicts"
+        run = lambda: uw.is_valid_states(states)  # noqa: E731
+    else:
+        kernel, dev, what = 1, segments[0].device, "first-contact steps"
+        run = lambda: uw.first_contact_steps(segments[0], segments[1], verify_delta, mode)  # noqa: E731
+    stream = torch.cuda.current_stream(dev)
+    ms, ref, best = {}, None, None
+    for bvh in ("topdown", "morton"):
+        uw.set_bvh(bvh)
+        uw.angleModel(0.0, 0.0)
+        kind, times, out = _tune_boxes(uw, kernel, run, reps, stream, what)
+        if ref is None:
+            ref = out
+        elif not torch.equal(ref, out):
+            raise RuntimeError("the BVH hierarchies gave different %s" % what)
+        ms[bvh] = times
+        if best is None or times[kind] < best[2]:
+            best = (bvh, kind, times[kind])
+    if uw.get_bvh() != best[0]:
+        uw.set_bvh(best[0])
+        uw.angleModel(0.0, 0.0)
+    uw.set_node_boxes(best[1], kernel)
+    return {"bvh": best[0], "boxes": {"states" if kernel == 0 else "segments": best[1]}, "ms": ms}
 
 
 def tune_states(uw, q: torch.Tensor, widths=(8, 16, 32), soft_caps=(128, 256, 512, 0), blocks=(0, 2, 3),

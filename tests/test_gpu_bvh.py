@@ -59,3 +59,17 @@ def test_topdown_depth_is_bounded_on_the_plate(oracle_mod, built_lib):
     Ve = ow.Ve
     q = W.uniform_states(20000, Ve.min(0) - 0.5, Ve.max(0) + 0.5, ow.scene_scale, seed=9)
     assert (uw.is_valid_states(torch.from_numpy(q)).cpu().numpy() == ow.is_valid(q)).all()
+
+
+def test_pick_bvh_keeps_the_fastest_and_the_verdicts(tori):
+    from puzzletunneldiscovery_gb300.autotune import pick_bvh
+    m, ow = tori
+    uw = _world(m, "topdown")
+    q = torch.from_numpy(W.uniform_states(200_000, -1.0, 1.0, ow.scene_scale, seed=12)).cuda()
+    want = uw.is_valid_states(q).cpu().numpy()
+    r = pick_bvh(uw, states=q)
+    assert r["bvh"] in ("topdown", "morton") and uw.get_bvh() == r["bvh"]
+    assert set(r["ms"]) == {"topdown", "morton"} and all(set(v) == {"aligned", "oriented"} for v in r["ms"].values())
+    best = min(t for v in r["ms"].values() for t in v.values())
+    assert r["ms"][r["bvh"]][r["boxes"]["states"]] == best
+    assert (uw.is_valid_states(q).cpu().numpy() == want).all()
