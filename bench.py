@@ -1780,7 +1780,7 @@ def main():
     ap.add_argument("--profile-case", choices=["states", "segments", "mlp", "train", "plate", "ompl", "disentangled", "all"],
                     default=None,
                     help="run a small fixed workload for an ncu capture instead of the benchmark")
-    ap.add_argument("--bvh", choices=["topdown", "morton"], default="topdown",
+    ap.add_argument("--bvh", choices=["topdown", "sah", "morton"], default="topdown",
                     help="the BVH hierarchy of the worlds (top-down principal-axis splits or Morton LBVH)")
     ap.add_argument("--node-boxes", choices=["aligned", "oriented"], default=None,
                     help="profile cases: the BVH node boxes (default: the world's default)")

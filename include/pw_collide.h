@@ -49,8 +49,9 @@ extern "C" {
 #define PW_BOXES_ORIENTED 1    /* boxes along the principal axes of each node's vertices (default) */
 
 /* Hierarchy of the BVHs (pw_world_set_bvh). */
-#define PW_BVH_TOPDOWN 0       /* top-down splits on each node's principal axis (default) */
+#define PW_BVH_TOPDOWN 0       /* top-down (default): surface-area splits for meshes up to 65536 triangles, mean splits above */
 #define PW_BVH_MORTON 1        /* Karras's LBVH over Morton codes */
+#define PW_BVH_SAH 2           /* top-down, surface-area splits at any size */
 
 /* Round phases of segment queries (pw_world_set_segment_phases). */
 #define PW_PHASES_AUTO 0       /* phases when a call has at least 2^22 32-step chunks (default) */
@@ -227,11 +228,12 @@ PW_API int pw_world_set_node_boxes(pw_world *w, int kernel, int kind);
 PW_API int pw_world_get_node_boxes(pw_world *w, int kernel, int *kind);
 
 /* host: the hierarchy the next BVH build (pw_world_angle_model) uses.  Top-down:
- * each range of triangles split at the mean of their centroids projected on the
- * principal axis of their vertices (the OBBTree split, as FCL's OBBRSS build
- * splits along a node's box axis); Morton: Karras's LBVH.  Both carry the
- * same leaf order semantics and both node-box kinds; verdicts do not depend on
- * the choice. */
+ * each range of triangles split in the frame of its vertices' principal axes,
+ * either at the mean of the centroids' projections on the first axis (the
+ * OBBTree split, as FCL's OBBRSS build splits along a node's box axis) or at
+ * the plane of least binned surface-area cost (16 bins on each axis); Morton:
+ * Karras's LBVH.  All carry both node-box kinds; verdicts do not depend on the
+ * choice. */
 PW_API int pw_world_set_bvh(pw_world *w, int kind);
 PW_API int pw_world_get_bvh(const pw_world *w, int *kind);
 

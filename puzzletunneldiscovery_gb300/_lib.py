@@ -30,6 +30,7 @@ PW_BOXES_ALIGNED = 0
 PW_BOXES_ORIENTED = 1
 PW_BVH_TOPDOWN = 0
 PW_BVH_MORTON = 1
+PW_BVH_SAH = 2
 PW_PHASES_AUTO = 0
 PW_PHASES_OFF = 1
 PW_PHASES_ON = 2

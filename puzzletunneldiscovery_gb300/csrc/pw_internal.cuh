@@ -153,7 +153,7 @@ struct pw_world {
 	int grid_cache[4] = { 0, 0, 0, 0 }; // grid of the persistent kernels under that configuration, per box kind
 	int node_boxes[2] = { PW_BOXES_ORIENTED, PW_BOXES_ORIENTED }; // per kernel (pw_world_set_node_boxes)
 	int seg_phases = PW_PHASES_AUTO;   // round phases of segment queries (pw_world_set_segment_phases)
-	bool bvh_topdown = true;           // hierarchy: top-down principal-axis splits (else Morton LBVH)
+	int bvh_kind = PW_BVH_TOPDOWN;     // hierarchy of the next build (pw_world_set_bvh)
 	// the last segment query's inputs: its parameters and checkpoints stay in the
 	// scratch, so the transit tuples of the same batch can start from them
 	const double *last_seg_from = nullptr, *last_seg_to = nullptr;

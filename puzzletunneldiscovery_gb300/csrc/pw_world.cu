@@ -374,9 +374,9 @@ extern "C" int pw_world_angle_model(pw_world *w, float latitude, float longitude
 
 extern "C" int pw_world_set_bvh(pw_world *w, int kind)
 {
-	if (!w || (kind != PW_BVH_TOPDOWN && kind != PW_BVH_MORTON))
+	if (!w || (kind != PW_BVH_TOPDOWN && kind != PW_BVH_MORTON && kind != PW_BVH_SAH))
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_set_bvh: bad argument");
-	w->bvh_topdown = kind == PW_BVH_TOPDOWN;
+	w->bvh_kind = kind;
 	return PW_OK;
 }
 
@@ -384,7 +384,7 @@ extern "C" int pw_world_get_bvh(const pw_world *w, int *kind)
 {
 	if (!w || !kind)
 		return pw_fail(PW_ERR_INVALID_ARG, "pw_world_get_bvh: bad argument");
-	*kind = w->bvh_topdown ? PW_BVH_TOPDOWN : PW_BVH_MORTON;
+	*kind = w->bvh_kind;
 	return PW_OK;
 }
 
@@ -980,7 +980,7 @@ __global__ void k_depth(int n, const int32_t *parent, int *maxdepth)
 // Morton-order hierarchy, whose splits are axis-aligned by construction.
 static void build_topdown(const std::vector<double> &V, const std::vector<uint32_t> &F, std::vector<uint32_t> &order,
                           std::vector<int32_t> &left, std::vector<int32_t> &right, std::vector<int32_t> &parent,
-                          std::vector<int32_t> &rlo, std::vector<int32_t> &rhi)
+                          std::vector<int32_t> &rlo, std::vector<int32_t> &rhi, bool sah)
 {
 	const int n = (int)(F.size() / 3);
 	const int leaf_base = n - 1;
@@ -1038,6 +1038,110 @@ static void build_topdown(const std::vector<double> &V, const std::vector<uint32
 			}
 		}
 		const double *ax = E + 3 * best;
+		if (sah && k.depth < 40 && k.b - k.a > 2) {
+			// binned surface-area cost in the node's principal frame: the split plane (one of
+			// 15 bin boundaries on each of the three axes) that minimises the children's
+			// box areas (in that frame) weighted by their triangle counts
+			constexpr int NB = 16;
+			double bestc = 1e300;
+			int bax = -1;
+			double bcut = 0.0;
+			for (int a3 = 0; a3 < 3; a3++) {
+				const double *e = E + 3 * a3;
+				double lo = 1e300, hi = -1e300;
+				for (int i = k.a; i < k.b; i++) {
+					const double *c = &cen[3 * order[i]];
+					const double pr = e[0] * c[0] + e[1] * c[1] + e[2] * c[2];
+					lo = std::min(lo, pr);
+					hi = std::max(hi, pr);
+				}
+				if (!(hi > lo))
+					continue;
+				double bl[NB][3], bh[NB][3];
+				int cnt[NB] = { 0 };
+				for (int b = 0; b < NB; b++)
+					for (int c = 0; c < 3; c++) {
+						bl[b][c] = 1e300;
+						bh[b][c] = -1e300;
+					}
+				for (int i = k.a; i < k.b; i++) {
+					const uint32_t t = order[i];
+					const double *c = &cen[3 * t];
+					const double pr = e[0] * c[0] + e[1] * c[1] + e[2] * c[2];
+					int b = (int)((pr - lo) / (hi - lo) * NB);
+					b = b < 0 ? 0 : (b >= NB ? NB - 1 : b);
+					cnt[b]++;
+					for (int v = 0; v < 3; v++) {
+						const double *p = &V[3 * F[3 * t + v]];
+						for (int r = 0; r < 3; r++) {
+							const double q = E[3 * r] * p[0] + E[3 * r + 1] * p[1] + E[3 * r + 2] * p[2];
+							bl[b][r] = std::min(bl[b][r], q);
+							bh[b][r] = std::max(bh[b][r], q);
+						}
+					}
+				}
+				auto area = [](const double *l, const double *h) {
+					const double x = h[0] - l[0], y = h[1] - l[1], z = h[2] - l[2];
+					return x * y + y * z + z * x;
+				};
+				// prefix (left) boxes and counts; suffix (right) sweep
+				double pl[NB][3], ph[NB][3];
+				int pc[NB];
+				for (int b = 0; b < NB; b++) {
+					for (int c = 0; c < 3; c++) {
+						pl[b][c] = b ? std::min(pl[b - 1][c], bl[b][c]) : bl[b][c];
+						ph[b][c] = b ? std::max(ph[b - 1][c], bh[b][c]) : bh[b][c];
+					}
+					pc[b] = (b ? pc[b - 1] : 0) + cnt[b];
+				}
+				double sl[3] = { 1e300, 1e300, 1e300 }, sh[3] = { -1e300, -1e300, -1e300 };
+				int sc = 0;
+				for (int b = NB - 1; b >= 1; b--) {
+					for (int c = 0; c < 3; c++) {
+						sl[c] = std::min(sl[c], bl[b][c]);
+						sh[c] = std::max(sh[c], bh[b][c]);
+					}
+					sc += cnt[b];
+					const int nl = pc[b - 1];
+					if (nl == 0 || sc == 0)
+						continue;
+					const double cost = area(pl[b - 1], ph[b - 1]) * nl + area(sl, sh) * sc;
+					if (cost < bestc) {
+						bestc = cost;
+						bax = a3;
+						bcut = lo + (hi - lo) * b / NB;
+					}
+				}
+			}
+			if (bax >= 0) {
+				const double *e = E + 3 * bax;
+				int i = k.a, j = k.b - 1;
+				while (i <= j) {
+					const double *c = &cen[3 * order[i]];
+					const double pr = e[0] * c[0] + e[1] * c[1] + e[2] * c[2];
+					if (pr < bcut)
+						i++;
+					else
+						std::swap(order[i], order[j--]);
+				}
+				const int mid = i;
+				if (mid > k.a && mid < k.b) {
+					const int lc = mid - k.a == 1 ? leaf_base + k.a : next++;
+					if (mid - k.a > 1)
+						stack.push_back(Task{ k.a, mid, lc, k.depth + 1 });
+					const int rc = k.b - mid == 1 ? leaf_base + mid : next++;
+					if (k.b - mid > 1)
+						stack.push_back(Task{ mid, k.b, rc, k.depth + 1 });
+					left[k.id] = lc;
+					right[k.id] = rc;
+					parent[lc] = k.id;
+					parent[rc] = k.id;
+					rlo[k.id] = k.a;
+					rhi[k.id] = k.b - 1;
+					continue;
+				}
+			}
+		}
 		double mean = 0.0;
 		for (int i = k.a; i < k.b; i++) {
 			const double *c = &cen[3 * order[i]];
@@ -1075,6 +1179,9 @@ static void build_topdown(const std::vector<double> &V, const std::vector<uint32
 		rhi[k.id] = k.b - 1;
 	}
 }
+
+// The largest mesh whose default (top-down) hierarchy takes surface-area splits.
+constexpr int SAH_MAX_TRIANGLES = 1 << 16;
 
 template <typename T>
 static cudaError_t walloc(pw_world *w, T **p, size_t count)
@@ -1178,11 +1285,15 @@ int pw_build_mesh_device(pw_world *w, MeshDev &m, const std::vector<double> &V64
 	cudaMemset(parent, 0xff, sizeof(int32_t) * nnodes);
 	k_tri_prep<<<G, B>>>(m.V64, m.F, n, ta, tb, tc, tlo, thi, cen);
 	cudaError_t se = cudaSuccess;
-	if (w->bvh_topdown) {
+	if (w->bvh_kind != PW_BVH_MORTON) {
 		// the hierarchy built on the host (build_topdown), uploaded in the Karras layout
 		std::vector<uint32_t> h_order;
 		std::vector<int32_t> h_left, h_right, h_parent, h_rlo, h_rhi;
-		build_topdown(V64, F, h_order, h_left, h_right, h_parent, h_rlo, h_rhi);
+		// surface-area splits where the mesh is small enough for their build cost (measured:
+		// the 4096-triangle tori's segment step 131.5 ms against 138.7 with mean splits;
+		// the 320k-triangle plate 179.3 against 176.5 ms, and 0.9 against 0.27 s to build)
+		const bool sah = w->bvh_kind == PW_BVH_SAH || (w->bvh_kind == PW_BVH_TOPDOWN && n <= SAH_MAX_TRIANGLES);
+		build_topdown(V64, F, h_order, h_left, h_right, h_parent, h_rlo, h_rhi, sah);
 		cudaMemcpy(vals2, h_order.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice);
 		cudaMemcpy(parent, h_parent.data(), sizeof(int32_t) * nnodes, cudaMemcpyHostToDevice);
 		if (n > 1) {

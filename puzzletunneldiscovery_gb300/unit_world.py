@@ -355,11 +355,11 @@ class UnitWorld:
         check(self._L.pw_world_get_node_boxes(self._h, int(kernel), ctypes.byref(k)), "get_node_boxes")
         return "oriented" if k.value == _lib.PW_BOXES_ORIENTED else "aligned"
 
-    _BVH = {"topdown": _lib.PW_BVH_TOPDOWN, "morton": _lib.PW_BVH_MORTON}
+    _BVH = {"topdown": _lib.PW_BVH_TOPDOWN, "morton": _lib.PW_BVH_MORTON, "sah": _lib.PW_BVH_SAH}
 
     def set_bvh(self, kind: str) -> None:
-        """The hierarchy the next BVH build (angleModel) uses: "topdown" (default)
-        or "morton"; the verdicts do not depend on it."""
+        """The hierarchy the next BVH build (angleModel) uses: "topdown" (default),
+        "sah" or "morton"; the verdicts do not depend on it."""
         check(self._L.pw_world_set_bvh(self._h, self._BVH[kind]), "set_bvh")
 
     def get_bvh(self) -> str:

@@ -29,7 +29,7 @@ def tori(oracle_mod, built_lib):
     return m, oracle_mod.OracleWorld(*m)
 
 
-@pytest.mark.parametrize("bvh", ["topdown", "morton"])
+@pytest.mark.parametrize("bvh", ["topdown", "sah", "morton"])
 @pytest.mark.parametrize("boxes", ["oriented", "aligned"])
 def test_hierarchies_match_oracle(tori, bvh, boxes):
     m, ow = tori
