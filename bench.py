@@ -197,7 +197,7 @@ def run_ompl(args):
         OC._check_motions_dev(uw, a, b, lo, hi, OMPL_CDRES)
     barrier()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    checked = []
+    checked, launches = [], 0
     with ClockSampler(local) as clk:
         barrier()
         for i in range(args.steps):
@@ -206,6 +206,7 @@ def run_ompl(args):
             v, n_states = OC._check_motions_dev(uw, a, b, lo, hi, OMPL_CDRES)
             ev[i][1].record(stream)
             checked.append(n_states)
+            launches += uw.last_stats()["kernel_launches"]
         barrier()
     step_ms = [s0.elapsed_time(s1) for s0, s1 in ev]
     tot_ms, tot_motions = max_time_sum_units(sum(step_ms), args.n * args.steps, ws, dev)
@@ -237,7 +238,6 @@ def run_ompl(args):
         return
 
     states = checked[-1]
-    windows = -(-states // (1 << 22))
     ms = tot_ms / args.steps
     # per checked state: generated and written (56 B), read by the check (56 B), its verdict
     # written and read (2 B); per motion: both ends read by the count and state kernels
@@ -272,13 +272,13 @@ def run_ompl(args):
             "e2e": {"value": e2e_value, "unit": "motions/s", "h2d_bytes_per_step": int(args.n * 112 * ws),
                     "d2h_bytes_per_step": int(args.n * ws)},
             "clocks": clk.summary(),
-            # segment counts, three pass counts, then per window of a pass's states: generation,
-            # traversal, re-test, reduction (a lower bound: each pass starts its own window)
-            "gpu_launches": (4 + 4 * windows) * args.steps,
+            # segment counts; per pass its counts, then per window of its states: generation,
+            # traversal, re-test, reduction (the library's own count)
+            "gpu_launches": launches,
             "detail": {"mismatches": cpu_mism, "mismatch_sample": cpu_n,
                        "node_boxes": {"states": box_kind, "ms": box_ms}, "bvh": picked["bvh"],
                        "states_checked_per_step": states, "states_per_motion": states / args.n,
-                       "valid_fraction": float(verdicts.mean()), "windows": windows, "step_ms": step_ms}}
+                       "valid_fraction": float(verdicts.mean()), "step_ms": step_ms}}
     print(json.dumps(line))
     if ws > 1:
         dist.barrier()

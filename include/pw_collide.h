@@ -327,10 +327,12 @@ PW_API int pw_world_translate_unit_to_ompl(const pw_world *w, const double *in, 
  * (setStateValidityCheckingResolution, ompldriver.cc:676-677).  valid[i] = 1 when to[i] and
  * every state interpolate(from[i], to[i], k / nd), k = 1 .. nd - 1, are collision free;
  * from[i] itself is not checked, as in OMPL.  A motion with a non-finite component gets 0.
- * The states are checked in three passes, each over the motions still valid: the targets,
- * the middle states (k = nd / 2, the first OMPL checks), the rest; *states_checked (may be
- * NULL) = the states the passes checked.  Rejects cdres outside (0, 1), bounds with lo > hi
- * or no extent, and motions of more than 2^31 - 1 segments. */
+ * The states are checked in passes, each over the motions still valid: the targets, then
+ * dyadic levels (with m = nd - 1 and T = floor(log2 m), level l holds the odd multiples of
+ * 2^(T - l) in 1 .. m), up to the first level no valid motion has; *states_checked (may be
+ * NULL) = the states the passes checked, and pw_world_last_stats' kernel_launches counts the
+ * whole call's kernels.  Rejects cdres outside (0, 1), bounds with lo > hi or no extent, and
+ * motions of more than 2^31 - 1 segments. */
 PW_API int pw_ompl_check_motions(pw_world *w, const double *from, const double *to, int64_t n,
                                  const double lo[3], const double hi[3], double cdres, uint8_t *valid,
                                  int64_t *states_checked, void *stream);

@@ -25,14 +25,17 @@
 // the engine's exact verdict after translateOMPLStateToUnitState
 // (unit_world.cc:689-711), as for validateStates.
 //
-// The check runs in three passes, each over the motions that are still valid:
-// the targets, then the middle state k = nd / 2 (the first one OMPL's queue
-// checks), then every other k.  A motion's verdict is the AND of all its
-// states either way; the passes only skip the states of motions already
-// known to collide, as OMPL's early exit does.  In a pass, a scan of the
-// per-motion counts numbers the pass's states; they are generated, converted
-// to the unit frame and checked window by window, and a colliding state clears
-// its motion's verdict.
+// The check runs in passes, each over the motions that are still valid: the
+// targets, then dyadic levels of k.  With m = nd - 1 and T = floor(log2 m),
+// level l holds the odd multiples of 2^(T - l) in 1 .. m, so level 0 is the
+// single state k = 2^T, each further level halves the spacing of the states
+// checked so far, and levels 0 .. T list every k once.  A motion's verdict is
+// the AND of all its states either way; the passes only skip the states of
+// motions already known to collide, as the early exit of OMPL's bisection
+// order does, and stop at the first level no valid motion has.  In a pass, a
+// scan of the per-motion counts numbers the pass's states; they are
+// generated, converted to the unit frame and checked window by window, and a
+// colliding state clears its motion's verdict.
 #include <cub/cub.cuh>
 
 #include <cfloat>
@@ -73,7 +76,7 @@ __device__ __forceinline__ bool finite7(const double *q)
 }
 
 // The passes, and the listing of every state a motion's check looks at.
-enum { PASS_ALL = 0, PASS_TARGET = 1, PASS_MID = 2, PASS_REST = 3 };
+enum { PASS_ALL = 0, PASS_TARGET = 1, PASS_LEVEL = 2 };
 
 // Per motion: OMPL's segment count nd, and the verdict's starting value (0, and
 // nd = 0, for a motion with a non-finite component).
@@ -105,37 +108,45 @@ __global__ void k_ompl_counts(const double *from, const double *to, int64_t n, O
 	valid[i] = 1;
 }
 
+// Exponent of the spacing of level l's states (-1: the motion has no such level).
+__device__ __forceinline__ int level_shift(int64_t nd, int level)
+{
+	if (nd < 2)
+		return -1;
+	const int T = 63 - __clzll((unsigned long long)(nd - 1));
+	return T - level;
+}
+
 // States of a motion in a pass: all of them (the target and k = 1 .. nd - 1), the
-// target, the middle one, or the rest; the last three only while the motion is valid.
-__device__ __forceinline__ int64_t pass_count(int pass, int64_t nd, uint8_t valid)
+// target, or one level's; the last two only while the motion is valid.
+__device__ __forceinline__ int64_t pass_count(int pass, int level, int64_t nd, uint8_t valid)
 {
 	switch (pass) {
 	case PASS_ALL: return nd >= 2 ? nd : 1;
 	case PASS_TARGET: return valid ? 1 : 0;
-	case PASS_MID: return valid && nd >= 2 ? 1 : 0;
-	default: return valid && nd >= 3 ? nd - 2 : 0;
+	default: {
+		const int e = level_shift(nd, level);
+		return valid && e >= 0 ? (((nd - 1) >> e) + 1) >> 1 : 0;
+	}
 	}
 }
 
 // Index k of the r-th state of a motion in a pass (0: the target).
-__device__ __forceinline__ int64_t pass_index(int pass, int64_t nd, int64_t r)
+__device__ __forceinline__ int64_t pass_index(int pass, int level, int64_t nd, int64_t r)
 {
 	switch (pass) {
 	case PASS_ALL: return r;
 	case PASS_TARGET: return 0;
-	case PASS_MID: return nd / 2;
-	default: {
-		const int64_t k = r + 1;
-		return k >= nd / 2 ? k + 1 : k;
-	}
+	default: return (2 * r + 1) << level_shift(nd, level);
 	}
 }
 
-__global__ void k_ompl_pass_counts(const int64_t *nd, const uint8_t *valid, int64_t n, int pass, int64_t *cnt)
+__global__ void k_ompl_pass_counts(const int64_t *nd, const uint8_t *valid, int64_t n, int pass, int level,
+                                   int64_t *cnt)
 {
 	const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
 	if (i < n)
-		cnt[i] = pass_count(pass, nd[i], valid[i]);
+		cnt[i] = pass_count(pass, level, nd[i], valid[i]);
 }
 
 // The motion that state g of a pass belongs to: the last i with offs[i] <= g, so
@@ -177,12 +188,13 @@ __device__ __forceinline__ void ompl_interpolate(const double *a, const double *
 
 // States [first, first + cnt) of a pass, in the unit frame.
 __global__ void k_ompl_states(const double *from, const double *to, int64_t n, const int64_t *nd,
-                              const int64_t *offs, int pass, int64_t first, int64_t cnt, pwfr::Frame F, double *out)
+                              const int64_t *offs, int pass, int level, int64_t first, int64_t cnt, pwfr::Frame F,
+                              double *out)
 {
 	for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < cnt; k += (int64_t)gridDim.x * blockDim.x) {
 		const int64_t g = first + k;
 		const int64_t i = owner(offs, n, g);
-		const int64_t j = pass_index(pass, nd[i], g - offs[i]);
+		const int64_t j = pass_index(pass, level, nd[i], g - offs[i]);
 		const double *a = from + 7 * i, *b = to + 7 * i;
 		double s[7];
 		if (j == 0) {
@@ -256,12 +268,13 @@ int ompl_counts(const double *from, const double *to, int64_t n, const OmplSpace
 }
 
 // A pass's per-motion counts, their scan (B.offs, n + 1 entries) and its total.
-int ompl_scan(int64_t n, int pass, const uint8_t *valid, cudaStream_t st, OmplScratch &B, int64_t *total)
+int ompl_scan(int64_t n, int pass, int level, const uint8_t *valid, cudaStream_t st, OmplScratch &B, int64_t *total)
 {
 	PW_CUDA(B.cnt.reserve(sizeof(int64_t) * (size_t)n));
 	PW_CUDA(B.offs.reserve(sizeof(int64_t) * (size_t)(n + 1)));
 	int64_t *cnt = (int64_t *)B.cnt.ptr, *offs = (int64_t *)B.offs.ptr;
-	k_ompl_pass_counts<<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const int64_t *)B.nd.ptr, valid, n, pass, cnt);
+	k_ompl_pass_counts<<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const int64_t *)B.nd.ptr, valid, n, pass, level,
+	                                                                 cnt);
 	PW_CUDA(cudaMemsetAsync(offs, 0, sizeof(int64_t), st));
 	size_t tmp_bytes = 0;
 	PW_CUDA(cub::DeviceScan::InclusiveSum(nullptr, tmp_bytes, cnt, offs + 1, n, st));
@@ -273,33 +286,37 @@ int ompl_scan(int64_t n, int pass, const uint8_t *valid, cudaStream_t st, OmplSc
 }
 
 // One pass of the check: its states, window by window, clear the verdicts of the
-// motions they collide on.
-int ompl_pass(pw_world *w, const double *from, const double *to, int64_t n, int pass, uint8_t *valid,
-              cudaStream_t st, OmplScratch &B, int64_t *checked)
+// motions they collide on.  *total = the pass's states; *launches counts the
+// kernels of this library it launched.
+int ompl_pass(pw_world *w, const double *from, const double *to, int64_t n, int pass, int level, uint8_t *valid,
+              cudaStream_t st, OmplScratch &B, int64_t *total, int64_t *launches)
 {
-	int64_t total = 0;
-	int rc = ompl_scan(n, pass, valid, st, B, &total);
+	int rc = ompl_scan(n, pass, level, valid, st, B, total);
 	if (rc)
 		return rc;
-	if (total == 0)
+	*launches += 1;
+	if (*total == 0)
 		return PW_OK;
-	const int64_t win = total < WINDOW ? total : WINDOW;
+	const int64_t all = *total;
+	const int64_t win = all < WINDOW ? all : WINDOW;
 	PW_CUDA(B.states.reserve(sizeof(double) * 7 * (size_t)win));
 	PW_CUDA(B.ok.reserve((size_t)win));
 	const int64_t *nd = (const int64_t *)B.nd.ptr, *offs = (const int64_t *)B.offs.ptr;
 	double *states = (double *)B.states.ptr;
 	uint8_t *ok = (uint8_t *)B.ok.ptr;
 	const pwfr::Frame F = world_frame(w);
-	for (int64_t first = 0; first < total; first += win) {
-		const int64_t cnt = total - first < win ? total - first : win;
-		k_ompl_states<<<blocks_for(w, cnt), 256, 0, st>>>(from, to, n, nd, offs, pass, first, cnt, F, states);
+	for (int64_t first = 0; first < all; first += win) {
+		const int64_t cnt = all - first < win ? all - first : win;
+		k_ompl_states<<<blocks_for(w, cnt), 256, 0, st>>>(from, to, n, nd, offs, pass, level, first, cnt, F,
+		                                                  states);
 		PW_CUDA(cudaGetLastError());
+		w->last_launches = 0;
 		if ((rc = pw_states_valid(w, states, cnt, ok, (void *)st)))
 			return rc;
 		k_ompl_reduce<<<blocks_for(w, cnt), 256, 0, st>>>(ok, first, cnt, offs, n, valid);
 		PW_CUDA(cudaGetLastError());
+		*launches += 2 + w->last_launches;
 	}
-	*checked += total;
 	return PW_OK;
 }
 
@@ -338,12 +355,19 @@ extern "C" int pw_ompl_check_motions(pw_world *w, const double *from, const doub
 	OmplScratch B;
 	if ((rc = ompl_counts(from, to, n, S, st, B, valid, who)))
 		return rc;
-	int64_t checked = 0;
-	for (int pass : { PASS_TARGET, PASS_MID, PASS_REST })
-		if ((rc = ompl_pass(w, from, to, n, pass, valid, st, B, &checked)))
+	int64_t checked = 0, launches = 1, total = 0;
+	if ((rc = ompl_pass(w, from, to, n, PASS_TARGET, 0, valid, st, B, &total, &launches)))
+		return rc;
+	checked += total;
+	// levels 0 .. 62 cover every nd below 2^63; the first empty level ends the check
+	for (int level = 0; total > 0 && level < 63; level++) {
+		if ((rc = ompl_pass(w, from, to, n, PASS_LEVEL, level, valid, st, B, &total, &launches)))
 			return rc;
+		checked += total;
+	}
 	// the scratch is freed on return: the batch's work must be done by then
 	PW_CUDA(cudaStreamSynchronize(st));
+	w->last_launches = launches;
 	if (states_checked)
 		*states_checked = checked;
 	return PW_OK;
@@ -374,7 +398,7 @@ extern "C" int pw_ompl_motion_states(pw_world *w, const double *from, const doub
 	uint8_t *valid = (uint8_t *)valid_buf.ptr;
 	if ((rc = ompl_counts(from, to, n, S, st, B, valid, who)))
 		return rc;
-	if ((rc = ompl_scan(n, PASS_ALL, valid, st, B, total)))
+	if ((rc = ompl_scan(n, PASS_ALL, 0, valid, st, B, total)))
 		return rc;
 	if (offsets)
 		PW_CUDA(cudaMemcpyAsync(offsets, B.offs.ptr, sizeof(int64_t) * (size_t)(n + 1), cudaMemcpyDeviceToDevice,
@@ -384,7 +408,7 @@ extern "C" int pw_ompl_motion_states(pw_world *w, const double *from, const doub
 		return pw_fail(PW_ERR_CAPACITY, std::string(who) + ": more states than the capacity");
 	}
 	k_ompl_states<<<blocks_for(w, *total), 256, 0, st>>>(from, to, n, (const int64_t *)B.nd.ptr,
-	                                                    (const int64_t *)B.offs.ptr, PASS_ALL, 0, *total,
+	                                                    (const int64_t *)B.offs.ptr, PASS_ALL, 0, 0, *total,
 	                                                    world_frame(w), states);
 	PW_CUDA(cudaGetLastError());
 	PW_CUDA(cudaStreamSynchronize(st));

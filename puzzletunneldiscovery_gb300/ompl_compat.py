@@ -28,9 +28,10 @@ space's translation bounds and collision resolution, and
 validator does (``pw_ompl_check_motions``: the target state and the states
 k / nd along OMPL's SE(3) interpolation, nd from the resolution times each
 component's extent), all motions of a batch in one call.  The states are
-checked in three passes over the motions still valid (the targets, the middle
-states, the rest), which skips most states of colliding motions as OMPL's
-early exit does, without changing any verdict.
+checked in passes over the motions still valid (the targets, then dyadic
+levels of k, each halving the spacing of the states checked so far), which
+skips most states of colliding motions as OMPL's early exit does, without
+changing any verdict.
 """
 from __future__ import annotations
 

@@ -59,17 +59,23 @@ def _motions(P, n, seed, sigma=2.0):
 
 
 def _expected_checks(ok, counts):
-    """States the three passes check, given every state's verdict in listing order:
-    each target, the middle state (k = nd // 2) of motions whose target is free,
-    and the rest of the motions whose target and middle state are free."""
+    """States the passes check, given every state's verdict in listing order (the
+    target, then k = 1 .. nd - 1): each target, then level by level while every
+    state checked so far is free, level l of a motion with m = nd - 1 and
+    T = floor(log2 m) holding the odd multiples of 2^(T - l) in 1 .. m."""
     starts = np.concatenate([[0], np.cumsum(counts)[:-1]])
     total = 0
-    for s, m in zip(starts, counts):
+    for s, nd in zip(starts, counts):
         total += 1
-        if m >= 2 and ok[s]:
-            total += 1
-            if m >= 3 and ok[s + m // 2]:
-                total += m - 2
+        free = bool(ok[s])
+        m = int(nd) - 1
+        T = m.bit_length() - 1
+        for e in range(T, -1, -1):
+            if not free:
+                break
+            ks = np.arange(1 << e, m + 1, 2 << e)
+            total += len(ks)
+            free = bool(ok[s + ks].all())
     return total
 
 
