@@ -68,6 +68,8 @@ extern "C" {
 #define PW_DEVERR_CKPT_CAP 2   /* graph mode: reserved checkpoint slots too few for a segment */
 #define PW_DEVERR_ROUND_CAP 4  /* graph mode: the longest segment has more chunks than reserved */
 #define PW_DEVERR_NONFINITE 8  /* a state had a NaN / infinite component; its verdict is 0 (not free) */
+#define PW_DEVERR_WAIT 16      /* a bounded wait for a bulk copy ran out (never expected); the call's
+                                  verdicts are not valid */
 
 typedef struct pw_world pw_world;
 

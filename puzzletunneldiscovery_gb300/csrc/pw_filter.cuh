@@ -7,12 +7,33 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "pw_math.cuh"
 
 namespace pwf {
 
 constexpr float U32 = 5.9604645e-08f;     // 2^-24
+
+// FP32 value of x by truncation toward zero, computed with integer operations
+// (GB300 runs FP64-to-FP32 conversions on its narrow FP64 pipe):
+// |result - x| < 2^-23 |x| for 2^-126 <= |x| < 2^128; a smaller |x| gives a
+// result of magnitude below 2^-126, a larger one (or a non-finite x) a finite
+// result of magnitude at least 2^127.
+PW_HD float f32_trunc(double x)
+{
+	uint64_t b;
+	memcpy(&b, &x, sizeof(b));
+	const uint32_t hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
+	constexpr uint32_t LO_EXP = 896u << 20;                  // FP64 exponent 2^-127: FP32 exponent field 0
+	constexpr uint32_t HI_ABS = (1150u << 20) | 0xFFFFFu;    // largest FP64 exponent kept, 2^127
+	uint32_t a = hi & 0x7FFFFFFFu;
+	a = a < LO_EXP ? LO_EXP : (a > HI_ABS ? HI_ABS : a);
+	const uint32_t f = (((a - LO_EXP) << 3) | (lo >> 29)) | (hi & 0x80000000u);
+	float r;
+	memcpy(&r, &f, sizeof(r));
+	return r;
+}
 
 // Per-query FP32 transform and error bounds: five float4 per query slot in
 // shared memory (80-byte stride, so lanes reading different slots hit
@@ -389,8 +410,8 @@ PW_HD int tri_filter(float3 V0, float3 e1, float3 e2, float3 x0, float3 g1, floa
 // quaternion (as the FP64 test and Eigen's toRotationMatrix apply it, unit or
 // not), so its entries are bounded by K = max(1, 2 |q|^2).  With u = 2^-24, the
 // entrywise error of R is at most 10 K u (the rounded coefficients and the
-// quadratic entries), of d = R rc + t - ce at most (10 K + 6) u (|rc|_1 +
-// |t|_inf + |ce|_inf + |d|_inf), of T = Re^T d at most 2 eps_d + 4u |d|_1, of
+// quadratic entries), of d = R rc + t - ce at most (10 K + 7) u (|rc|_1 +
+// |t|_inf + |ce|_inf + |d|_inf; t is truncated by f32_trunc, 2u), of T = Re^T d at most 2 eps_d + 4u |d|_1, of
 // Re^T R at most (20 K + 5) u; the axis values are sums of at most six such
 // terms weighted by |T|_inf <= |d|_1, the extents and K, so
 // e = 1100u K (|rc|_1 + |t|_inf + |ce|_inf + 2 |d|_1 + sum eh + sum rh) covers
@@ -406,6 +427,12 @@ struct DisBoxes32 {
 	float ce_abs;          // |ce|_inf, rounded up
 };
 
+// ROT = false when the perturbation rotation Re is exactly the identity: then
+// Re^T d = d and Re^T R = R exactly (products by 1 and sums with zeros), so
+// both are taken as they are.  The verdict comes from the largest axis value
+// g_max: 1 when g_max > e, 0 when g_max < -e, -1 otherwise; with n2 and e
+// finite and below 1e30 every axis value is finite.
+template <bool ROT>
 PW_HD int boxes_disjoint32(const double *q, const DisBoxes32 &B, float slack = 1.f)
 {
 	const float w = (float)q[3], x = (float)q[4], y = (float)q[5], z = (float)q[6];
@@ -416,15 +443,15 @@ PW_HD int boxes_disjoint32(const double *q, const DisBoxes32 &B, float slack = 1
 	const float R[9] = { 1.f - 2.f * (y * y + z * z), 2.f * (x * y - w * z), 2.f * (x * z + w * y),
 		                 2.f * (x * y + w * z), 1.f - 2.f * (x * x + z * z), 2.f * (y * z - w * x),
 		                 2.f * (x * z - w * y), 2.f * (y * z + w * x), 1.f - 2.f * (x * x + y * y) };
-	const float t[3] = { (float)q[0], (float)q[1], (float)q[2] };
+	const float t[3] = { f32_trunc(q[0]), f32_trunc(q[1]), f32_trunc(q[2]) };
 	float d[3];
 	for (int k = 0; k < 3; k++)
 		d[k] = ((R[3 * k] * B.rc[0] + R[3 * k + 1] * B.rc[1]) + R[3 * k + 2] * B.rc[2] + t[k]) - B.ce[k];
 	float T[3], Rr[9], AR[9];
 	for (int i = 0; i < 3; i++) {
-		T[i] = (B.Re[i] * d[0] + B.Re[3 + i] * d[1]) + B.Re[6 + i] * d[2];
+		T[i] = ROT ? (B.Re[i] * d[0] + B.Re[3 + i] * d[1]) + B.Re[6 + i] * d[2] : d[i];
 		for (int j = 0; j < 3; j++) {
-			Rr[3 * i + j] = (B.Re[i] * R[j] + B.Re[3 + i] * R[3 + j]) + B.Re[6 + i] * R[6 + j];
+			Rr[3 * i + j] = ROT ? (B.Re[i] * R[j] + B.Re[3 + i] * R[3 + j]) + B.Re[6 + i] * R[6 + j] : R[3 * i + j];
 			AR[3 * i + j] = fabsf(Rr[3 * i + j]);
 		}
 	}
@@ -435,22 +462,13 @@ PW_HD int boxes_disjoint32(const double *q, const DisBoxes32 &B, float slack = 1
 	const float e = slack * (1100.f * U32 * K * scale);
 	if (!(e < 1.0e30f))
 		return -1;                           // not finite: the FP64 test decides
-	bool undecided = false;
-	auto axis = [&](float g) {
-		if (g > e)
-			return true;
-		if (!(g < -e))
-			undecided = true;
-		return false;
-	};
+	float g = -3.0e38f;
 	for (int i = 0; i < 3; i++)
-		if (axis(fabsf(T[i]) - (B.eh[i] + ((B.rh[0] * AR[3 * i] + B.rh[1] * AR[3 * i + 1]) + B.rh[2] * AR[3 * i + 2]))))
-			return 1;
+		g = fmaxf(g, fabsf(T[i]) - (B.eh[i] + ((B.rh[0] * AR[3 * i] + B.rh[1] * AR[3 * i + 1]) + B.rh[2] * AR[3 * i + 2])));
 	for (int j = 0; j < 3; j++) {
 		const float tl = (T[0] * Rr[j] + T[1] * Rr[3 + j]) + T[2] * Rr[6 + j];
 		const float ra = (B.eh[0] * AR[j] + B.eh[1] * AR[3 + j]) + B.eh[2] * AR[6 + j];
-		if (axis(fabsf(tl) - (ra + B.rh[j])))
-			return 1;
+		g = fmaxf(g, fabsf(tl) - (ra + B.rh[j]));
 	}
 	for (int i = 0; i < 3; i++) {
 		const int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
@@ -459,11 +477,10 @@ PW_HD int boxes_disjoint32(const double *q, const DisBoxes32 &B, float slack = 1
 			const float tl = T[i2] * Rr[3 * i1 + j] - T[i1] * Rr[3 * i2 + j];
 			const float ra = B.eh[i1] * AR[3 * i2 + j] + B.eh[i2] * AR[3 * i1 + j];
 			const float rb = B.rh[j1] * AR[3 * i + j2] + B.rh[j2] * AR[3 * i + j1];
-			if (axis(fabsf(tl) - (ra + rb)))
-				return 1;
+			g = fmaxf(g, fabsf(tl) - (ra + rb));
 		}
 	}
-	return undecided ? -1 : 0;
+	return g > e ? 1 : (g < -e ? 0 : -1);
 }
 
 } // namespace pwf

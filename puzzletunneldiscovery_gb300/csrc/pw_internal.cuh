@@ -142,6 +142,7 @@ struct pw_world {
 	int64_t last_states = -1;   // size of the last state batch (-1: the last query was segments)
 	int64_t last_launches = 0;  // kernels of this library the last query launched (pw_query_stats)
 	int num_sms = 0;
+	int dis_per_sm[2] = { 0, 0 };   // resident blocks per SM of the isDisentangled kernels (0: not yet asked)
 	// graph mode: segment queries make no host synchronisation and no allocation;
 	// they run within the scratch sizes that pw_segments_reserve or the last
 	// segment query made outside graph mode left

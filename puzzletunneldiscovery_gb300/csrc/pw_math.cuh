@@ -716,23 +716,37 @@ PW_HD int sat_disjoint(const double *ea, const double *eb, const double *T, cons
 	return 0;
 }
 
+// isDisentangled box test with the env box's centre already placed, ce = Re ec + te.
+// ROT = false takes Re as exactly the identity: for a finite state Re^T d and
+// Re^T R then equal d and R up to the sign of zeros (products by 1, sums with
+// products by 0), which no comparison of the test sees; callers use it only
+// for finite states (a non-finite one gives NaN products in the general form).
+template <bool ROT = true>
+PW_HD int boxes_disjoint_placed(const double *q, const double *rc, const double *rh, const double *Re,
+                                const double *ce, const double *eh)
+{
+	double R[9], t[3], cr[3], d[3], Rr[9], T[3], AR[9];
+	state_transform(q, R, t);
+	xform_point(R, t, rc, cr);
+	for (int c = 0; c < 3; c++) d[c] = sub(cr[c], ce[c]);
+	for (int i = 0; i < 3; i++) {
+		T[i] = ROT ? add(add(mul(Re[0 + i], d[0]), mul(Re[3 + i], d[1])), mul(Re[6 + i], d[2])) : d[i];
+		for (int j = 0; j < 3; j++)
+			Rr[3 * i + j] = ROT ? add(add(mul(Re[0 + i], R[0 + j]), mul(Re[3 + i], R[3 + j])), mul(Re[6 + i], R[6 + j]))
+			                    : R[3 * i + j];
+	}
+	for (int i = 0; i < 9; i++) AR[i] = dabs(Rr[i]);
+	return sat_disjoint(eh, rh, T, Rr, AR);
+}
+
 // isDisentangled box test: robot local AABB box (rc, rh) placed by the state,
 // env box (ec, eh) placed by the perturbation transform (Re, te).
 PW_HD int boxes_disjoint(const double *q, const double *rc, const double *rh,
                          const double *Re, const double *te, const double *ec, const double *eh)
 {
-	double R[9], t[3], cr[3], ce[3], d[3], Rr[9], T[3], AR[9];
-	state_transform(q, R, t);
-	xform_point(R, t, rc, cr);
+	double ce[3];
 	xform_point(Re, te, ec, ce);
-	for (int c = 0; c < 3; c++) d[c] = sub(cr[c], ce[c]);
-	for (int i = 0; i < 3; i++) {
-		T[i] = add(add(mul(Re[0 + i], d[0]), mul(Re[3 + i], d[1])), mul(Re[6 + i], d[2]));
-		for (int j = 0; j < 3; j++)
-			Rr[3 * i + j] = add(add(mul(Re[0 + i], R[0 + j]), mul(Re[3 + i], R[3 + j])), mul(Re[6 + i], R[6 + j]));
-	}
-	for (int i = 0; i < 9; i++) AR[i] = dabs(Rr[i]);
-	return sat_disjoint(eh, rh, T, Rr, AR);
+	return boxes_disjoint_placed(q, rc, rh, Re, ce, eh);
 }
 
 // ---------------------------------------------------------------- key configurations

@@ -19,6 +19,7 @@
 #include <string>
 #include <vector>
 
+#include "pw_async.cuh"
 #include "pw_internal.cuh"
 #include "pw_mlp.h"
 

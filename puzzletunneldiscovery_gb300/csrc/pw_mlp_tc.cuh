@@ -52,37 +52,13 @@ static_assert(SMEM_BYTES <= 232448, "shared memory budget of one CTA");
 constexpr int B_FULL = 0, B_EMPTY = NSTAGE, B_ACT = 2 * NSTAGE, B_DONE = B_ACT + 2, B_HEAD = B_DONE + 2,
               B_FINAL = B_HEAD + 2;
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
-{
-	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t bar)
-{
-	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
-{
-	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity)
-{
-	uint32_t ok;
-	asm volatile("{\n\t.reg .pred p;\n\t"
-	             "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-	             "selp.u32 %0, 1, 0, p;\n\t}"
-	             : "=r"(ok)
-	             : "r"(bar), "r"(parity)
-	             : "memory");
-	return ok != 0;
-}
-__device__ __forceinline__ uint64_t now_ns()
-{
-	uint64_t t;
-	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-	return t;
-}
+using pwa::bulk_g2s;
+using pwa::mbar_arrive;
+using pwa::mbar_expect_tx;
+using pwa::mbar_init;
+using pwa::mbar_test;
+using pwa::now_ns;
+using pwa::smem_u32;
 
 // Waits for the phase of `parity` to complete.  Gives up when another role has
 // aborted or after WAIT_LIMIT_NS, recording `where` in *err; returns false then.
@@ -110,13 +86,6 @@ __device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity)
 	const uint64_t t0 = now_ns();
 	while (!mbar_test(bar, parity) && now_ns() - t0 < WAIT_LIMIT_NS) {
 	}
-}
-
-__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar)
-{
-	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-	             "l"(src), "r"(bytes), "r"(bar)
-	             : "memory");
 }
 
 // Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, rows of

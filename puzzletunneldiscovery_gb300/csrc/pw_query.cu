@@ -29,6 +29,7 @@
 #include "pw_internal.cuh"
 #include "pw_math.cuh"
 #include "pw_filter.cuh"
+#include "pw_async.cuh"
 
 namespace {
 
@@ -712,59 +713,133 @@ __global__ void k_retest(WorldDev W, StateSrc src, uint8_t *valid_out, int32_t *
 
 struct BoxParams {
 	double rc[3], rh[3], Re[9], te[3], ec[3], eh[3];
+	double ce[3];   // Re ec + te (pwm::xform_point, the FP64 test's own placement)
 };
 
-// The FP32 test decides almost every state.  A block stages its 256 states
-// (56 B each) in shared memory with 16-byte loads; the undecided ones are queued
+// The FP32 test decides almost every state; the undecided ones are queued
 // (warp-aggregated) for k_disentangled64.  The queue holds n entries, so it
-// cannot fill.
+// cannot fill.  A persistent block takes tiles of 256 states (56 B each, 14 KB)
+// round robin: full tiles of a 16-byte aligned batch stream through a ring of
+// DIS_STAGES shared-memory stages filled by bulk copies, so the copies of the
+// next tiles are in flight while one is tested; the last partial tile (and
+// every tile of a batch that is not 16-byte aligned) is read with plain loads.
+// A bulk copy that does not land within DIS_WAIT_NS sets PW_DEVERR_WAIT; the
+// block then waits (bounded) for its copies in flight and stops.
 constexpr int DIS_BLOCK = 256;
+constexpr int DIS_STAGES = 3;
+constexpr uint32_t DIS_TILE_BYTES = DIS_BLOCK * 7 * sizeof(double);
+constexpr size_t DIS_SMEM = DIS_STAGES * (size_t)DIS_TILE_BYTES + DIS_STAGES * sizeof(uint64_t);
+constexpr uint64_t DIS_WAIT_NS = 1000000000ull;
+
+// One state's FP32 verdict; undecided states go to the queue (verdict 0 until
+// k_disentangled64 writes it).  All threads of the block call it.
+template <bool ROT>
+__device__ __forceinline__ void dis_decide(const pwf::DisBoxes32 &B32, const double *q, bool has, int64_t i,
+                                           int64_t n, uint8_t *out, uint32_t *queue, QueryCounters *ctr)
+{
+	const int lane = threadIdx.x & 31;
+	int v = 0;
+	bool undecided = false;
+	if (has) {
+		v = pwf::boxes_disjoint32<ROT>(q, B32);
+		undecided = v < 0;
+	}
+	const unsigned m = __ballot_sync(0xffffffffu, undecided);
+	unsigned long long base = 0;
+	if (m) {
+		if (lane == 0)
+			base = atomicAdd(&ctr->retest_count, (unsigned long long)__popc(m));
+		base = __shfl_sync(0xffffffffu, base, 0);
+	}
+	if (undecided) {
+		const unsigned long long slot = base + __popc(m & ((1u << lane) - 1u));
+		if (slot < (unsigned long long)n)
+			queue[slot] = (uint32_t)i;
+		v = 0;
+	}
+	if (has)
+		out[i] = (uint8_t)v;
+}
+
+// ROT: the perturbation rotation is not exactly the identity.
+template <bool ROT>
 __global__ void __launch_bounds__(DIS_BLOCK) k_disentangled(pwf::DisBoxes32 B32, const double *states, int64_t n,
                                                             uint8_t *out, uint32_t *queue, QueryCounters *ctr)
 {
-	__shared__ __align__(16) double sq[DIS_BLOCK * 7];
-	const int lane = threadIdx.x & 31;
-	for (int64_t b0 = (int64_t)blockIdx.x * DIS_BLOCK; b0 < n; b0 += (int64_t)gridDim.x * DIS_BLOCK) {
-		const int cnt = (int)min((int64_t)DIS_BLOCK, n - b0);
-		const double *src = states + 7 * b0;
-		if (cnt == DIS_BLOCK && (((uintptr_t)src) & 15) == 0) {
-			const float4 *f4 = reinterpret_cast<const float4 *>(src);
-			float4 *d4 = reinterpret_cast<float4 *>(sq);
-			for (int k = threadIdx.x; k < DIS_BLOCK * 7 / 2; k += DIS_BLOCK)
-				d4[k] = __ldg(f4 + k);
-		} else {
-			for (int k = threadIdx.x; k < cnt * 7; k += DIS_BLOCK)
-				sq[k] = src[k];
+	extern __shared__ __align__(128) unsigned char dis_smem[];
+	double *sq = reinterpret_cast<double *>(dis_smem);
+	const uint32_t bar0 = pwa::smem_u32(dis_smem + DIS_STAGES * DIS_TILE_BYTES);
+	const bool lead = threadIdx.x == 0;
+	const int64_t nfull = (((uintptr_t)states) & 15) == 0 ? n / DIS_BLOCK : 0;
+	int64_t tile = blockIdx.x;
+	if (tile < nfull) {
+		const uint32_t sbase = pwa::smem_u32(dis_smem);
+		const int64_t stride = gridDim.x;
+		auto issue = [&](int s, int64_t t) {
+			pwa::mbar_expect_tx(bar0 + 8 * s, DIS_TILE_BYTES);
+			pwa::bulk_g2s(sbase + s * DIS_TILE_BYTES, states + t * (DIS_BLOCK * 7), DIS_TILE_BYTES, bar0 + 8 * s);
+		};
+		__shared__ int stop;
+		if (lead) {
+			stop = 0;
+			for (int s = 0; s < DIS_STAGES; s++)
+				pwa::mbar_init(bar0 + 8 * s, 1);
+			pwa::fence_mbar_init();
+			for (int s = 0; s < DIS_STAGES && tile + s * stride < nfull; s++)
+				issue(s, tile + s * stride);
 		}
 		__syncthreads();
-		const int64_t i = b0 + threadIdx.x;
-		int v = 0;
-		bool undecided = false;
-		if (threadIdx.x < cnt) {
-			v = pwf::boxes_disjoint32(sq + 7 * threadIdx.x, B32);
-			undecided = v < 0;
+		uint32_t k = 0;
+		for (; tile < nfull; tile += stride, k++) {
+			const int s = (int)(k % DIS_STAGES);
+			const uint32_t parity = (k / DIS_STAGES) & 1u;
+			// one thread polls; the others wait at the block barrier, which also orders
+			// the landed copy before their reads
+			if (lead && !pwa::mbar_wait_for(bar0 + 8 * s, parity, DIS_WAIT_NS))
+				stop = 1;
+			__syncthreads();
+			if (stop)
+				break;
+			const int64_t i = tile * DIS_BLOCK + threadIdx.x;
+			dis_decide<ROT>(B32, sq + (size_t)s * DIS_BLOCK * 7 + 7 * threadIdx.x, true, i, n, out, queue, ctr);
+			__syncthreads();   // every thread is done with stage s
+			const int64_t next = tile + (int64_t)DIS_STAGES * stride;
+			if (lead && next < nfull) {
+				pwa::fence_proxy_async();
+				issue(s, next);
+			}
 		}
-		const unsigned m = __ballot_sync(0xffffffffu, undecided);
-		unsigned long long base = 0;
-		if (m) {
-			if (lane == 0)
-				base = atomicAdd(&ctr->retest_count, (unsigned long long)__popc(m));
-			base = __shfl_sync(0xffffffffu, base, 0);
+		if (stop) {
+			// the copies still in flight land before the block's shared memory is released
+			if (lead) {
+				atomicOr(&ctr->error, (unsigned)PW_DEVERR_WAIT);
+				for (uint32_t d = 0; d < (uint32_t)DIS_STAGES && tile + d * stride < nfull; d++)
+					pwa::mbar_wait_for(bar0 + 8 * ((k + d) % DIS_STAGES), ((k + d) / DIS_STAGES) & 1u, DIS_WAIT_NS);
+			}
+			return;
 		}
-		if (undecided) {
-			const unsigned long long slot = base + __popc(m & ((1u << lane) - 1u));
-			if (slot < (unsigned long long)n)
-				queue[slot] = (uint32_t)i;
-			v = 0;                              // k_disentangled64 writes the verdict
-		}
-		if (threadIdx.x < cnt)
-			out[i] = (uint8_t)v;
+		__syncthreads();
+	}
+	// the partial last tile, or every tile of an unaligned batch
+	for (; tile * DIS_BLOCK < n; tile += gridDim.x) {
+		const int64_t b0 = tile * DIS_BLOCK;
+		const int cnt = (int)min((int64_t)DIS_BLOCK, n - b0);
+		const double *src = states + 7 * b0;
+		for (int k = threadIdx.x; k < cnt * 7; k += DIS_BLOCK)
+			sq[k] = src[k];
+		__syncthreads();
+		dis_decide<ROT>(B32, sq + 7 * threadIdx.x, (int)threadIdx.x < cnt, b0 + threadIdx.x, n, out, queue, ctr);
 		__syncthreads();
 	}
 }
 
-// The FP64 test of the queued states, one thread each.
-__global__ void k_disentangled64(BoxParams B, const double *states, const uint32_t *queue, int64_t n,
+// The FP64 test of the queued states (ROT as for k_disentangled), one thread each, in one-warp blocks so that
+// a short queue spreads over every SM (GB300's FP64 pipe is narrow: a block of
+// 256 queued states on one SM took several times longer than the same states on
+// eight).
+constexpr int DIS64_BLOCK = 32;
+template <bool ROT>
+__global__ void __launch_bounds__(DIS64_BLOCK) k_disentangled64(BoxParams B, const double *states, const uint32_t *queue, int64_t n,
                                  QueryCounters *ctr, uint8_t *out)
 {
 	const unsigned long long cnt = min(ctr->retest_count, (unsigned long long)n);
@@ -776,7 +851,11 @@ __global__ void k_disentangled64(BoxParams B, const double *states, const uint32
 		double q[7];
 		for (int c = 0; c < 7; c++)
 			q[c] = states[7 * i + c];
-		out[i] = (uint8_t)pwm::boxes_disjoint(q, B.rc, B.rh, B.Re, B.te, B.ec, B.eh);
+		bool finite = true;
+		for (int c = 0; c < 7; c++)
+			finite = finite && isfinite(q[c]);
+		out[i] = (uint8_t)(ROT || !finite ? pwm::boxes_disjoint_placed<true>(q, B.rc, B.rh, B.Re, B.ce, B.eh)
+		                                  : pwm::boxes_disjoint_placed<false>(q, B.rc, B.rh, B.Re, B.ce, B.eh));
 	}
 }
 
@@ -784,14 +863,12 @@ __global__ void k_disentangled64(BoxParams B, const double *states, const uint32
 static pwf::DisBoxes32 dis_boxes32(const BoxParams &B)
 {
 	pwf::DisBoxes32 o;
-	double ce[3];
-	pwm::xform_point(B.Re, B.te, B.ec, ce);
 	float cabs = 0.f;
 	for (int c = 0; c < 3; c++) {
 		o.rc[c] = (float)B.rc[c];
 		o.rh[c] = (float)B.rh[c];
 		o.eh[c] = (float)B.eh[c];
-		o.ce[c] = (float)ce[c];
+		o.ce[c] = (float)B.ce[c];
 		cabs = std::max(cabs, std::fabs(o.ce[c]));
 	}
 	for (int i = 0; i < 9; i++)
@@ -1553,6 +1630,7 @@ extern "C" int pw_states_disentangled(pw_world *w, const double *states, int64_t
 	}
 	for (int i = 0; i < 9; i++)
 		B.Re[i] = w->pertR[i];
+	pwm::xform_point(B.Re, B.te, B.ec, B.ce);
 	cudaStream_t st = (cudaStream_t)stream;
 	int rc = ensure_query_scratch(w);
 	if (rc)
@@ -1567,10 +1645,25 @@ extern "C" int pw_states_disentangled(pw_world *w, const double *states, int64_t
 	w->last_stream = st;
 	w->timed = false;
 	w->last_states = n;
-	const int64_t blocks = std::min<int64_t>((n + DIS_BLOCK - 1) / DIS_BLOCK, (int64_t)w->num_sms * 8);
+	bool rot = false;
+	for (int i = 0; i < 9; i++)
+		rot = rot || B.Re[i] != (i % 4 == 0 ? 1.0 : 0.0);
+	const void *kfn = rot ? (const void *)k_disentangled<true> : (const void *)k_disentangled<false>;
+	int &per_sm = w->dis_per_sm[rot ? 1 : 0];
+	if (per_sm <= 0) {
+		PW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, DIS_BLOCK, DIS_SMEM));
+		per_sm = std::max(per_sm, 1);
+	}
+	const int64_t blocks = std::min<int64_t>((n + DIS_BLOCK - 1) / DIS_BLOCK, (int64_t)w->num_sms * per_sm);
 	uint32_t *queue = (uint32_t *)w->dis_queue.ptr;
-	k_disentangled<<<(unsigned)blocks, DIS_BLOCK, 0, st>>>(dis_boxes32(B), states, n, out, queue, ctr);
-	k_disentangled64<<<(unsigned)(w->num_sms * 4), 256, 0, st>>>(B, states, queue, n, ctr, out);
+	const unsigned grid64 = (unsigned)(w->num_sms * 32);
+	if (rot) {
+		k_disentangled<true><<<(unsigned)blocks, DIS_BLOCK, DIS_SMEM, st>>>(dis_boxes32(B), states, n, out, queue, ctr);
+		k_disentangled64<true><<<grid64, DIS64_BLOCK, 0, st>>>(B, states, queue, n, ctr, out);
+	} else {
+		k_disentangled<false><<<(unsigned)blocks, DIS_BLOCK, DIS_SMEM, st>>>(dis_boxes32(B), states, n, out, queue, ctr);
+		k_disentangled64<false><<<grid64, DIS64_BLOCK, 0, st>>>(B, states, queue, n, ctr, out);
+	}
 	w->last_launches = 2;
 	PW_CUDA(cudaGetLastError());
 	return PW_OK;

@@ -299,7 +299,7 @@ class UnitWorld:
         if rc == _lib.PW_ERR_NO_MODEL:
             raise RuntimeError("Pain in the ass: models not loaded")
         check(rc, "is_disentangled")
-        return out.bool()
+        return out.view(torch.bool)   # verdicts are 0 / 1: the same bytes, no conversion kernel
 
     def first_contact_steps(self, q0: torch.Tensor, q1: torch.Tensor, verify_delta: float,
                             mode: int = _lib.PW_SEG_TRANSIT) -> torch.Tensor:

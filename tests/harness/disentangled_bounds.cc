@@ -88,9 +88,39 @@ int main(int argc, char **argv)
 	rng_state ^= (uint64_t)(argc > 2 ? atol(argv[2]) : 1) * 0x9E3779B97F4A7C15ull;
 	const float slack = argc > 3 ? (float)atof(argv[3]) : 1.f;
 	long wrong = 0, certified = 0, undecided = 0, states = 0, far_und = 0, far_states = 0;
+	// pwf::f32_trunc: truncation error below 2^-23 |x| in the normal FP32 range, a
+	// magnitude below 2^-126 under it, a finite magnitude of at least 2^127 above it
+	auto conv_ok = [](double x) {
+		const float f = pwf::f32_trunc(x);
+		const double ax = std::fabs(x), af = std::fabs((double)f);
+		if (!std::isfinite(f))
+			return false;
+		if (!(ax < 1e300) || ax >= std::ldexp(1.0, 128))   // non-finite or beyond FP32
+			return af >= std::ldexp(1.0, 127);
+		if (ax < std::ldexp(1.0, -126))
+			return af < std::ldexp(1.0, -126);
+		return af <= ax && ax - af < std::ldexp(ax, -23) && (x == 0.0 || std::signbit(x) == std::signbit(f));
+	};
+	const double specials[] = { 0.0, -0.0, 1.0, -1.0, std::ldexp(1.0, -126), std::ldexp(1.0, -127),
+		                        std::ldexp(1.0, -149), 1e-300, std::ldexp(1.0, 127), std::ldexp(1.0, 128),
+		                        -std::ldexp(1.0, 128), 1e300, HUGE_VAL, -HUGE_VAL, NAN,
+		                        std::nextafter(std::ldexp(1.0, 128), 0.0), std::nextafter(1.0, 2.0) };
+	for (double x : specials)
+		if (!conv_ok(x))
+			wrong++;
+	for (long i = 0; i < 200000; i++) {
+		const double x = std::ldexp(uniform() + 0.5, (int)(next_u64() % 600) - 300) * ((next_u64() & 1) ? 1 : -1);
+		if (!conv_ok(x))
+			wrong++;
+	}
 	auto check = [&](const Boxes &B, const double q[7]) {
 		const int ref = pwm::boxes_disjoint(q, B.rc, B.rh, B.Re, B.te, B.ec, B.eh);
-		const int v = pwf::boxes_disjoint32(q, B.b32, slack);
+		// the general form, and the identity-rotation form where Re is exactly the identity
+		const bool ident = B.Re[0] == 1.0 && B.Re[4] == 1.0 && B.Re[8] == 1.0 && B.Re[1] == 0.0 && B.Re[2] == 0.0 &&
+		                   B.Re[3] == 0.0 && B.Re[5] == 0.0 && B.Re[6] == 0.0 && B.Re[7] == 0.0;
+		const int v = pwf::boxes_disjoint32<true>(q, B.b32, slack);
+		if (ident && pwf::boxes_disjoint32<false>(q, B.b32, slack) != v)
+			wrong++;
 		states++;
 		if (v < 0) {
 			undecided++;

@@ -117,6 +117,9 @@ def test_non_finite_states_are_not_free(built_lib, tori, oracle_mod):
     v2 = uw.is_valid_states(torch.from_numpy(q[~bad]).cuda())
     assert uw.last_stats()["device_errors"] == 0
     assert (v2.cpu().numpy() == want[~bad]).all()
+    # isDisentangled on the same batch: the non-finite states take the general FP64 box test
+    d = uw.is_disentangled_states(torch.from_numpy(q).cuda()).cpu().numpy()
+    assert (d == oracle_mod.OracleWorld(*tori).is_disentangled(q)).all()
 
 
 def test_non_finite_segments_take_no_step(built_lib, tori, oracle_mod):

@@ -244,6 +244,9 @@ def test_perturbation(tori, oracle_mod):
         q = W.uniform_states(5000, -2.0, 2.0, ow.scene_scale, seed=6)
         assert (uw.is_valid_states(torch.from_numpy(q)).cpu().numpy() == ow.is_valid(q)).all()
         assert (uw.is_disentangled_states(torch.from_numpy(q)).cpu().numpy() == ow.is_disentangled(q)).all()
+        # the rotated-perturbation form of the FP32 box test over many tiles per block
+        q2 = W.uniform_states(1_500_007, -2.0, 2.0, ow.scene_scale, seed=7)
+        assert (uw.is_disentangled_states(torch.from_numpy(q2)).cpu().numpy() == ow.is_disentangled(q2)).all()
     finally:
         ident = np.array([0, 0, 0, 1, 0, 0, 0.0])
         uw.set_perturbation(ident)
@@ -395,3 +398,8 @@ def test_disentangled_fp32_and_fp64_paths(tori):
     dq = torch.from_numpy(q).cuda().reshape(-1)[7:].reshape(-1, 7)
     got = uw.is_disentangled_states(dq).cpu().numpy()
     assert (got == ow.is_disentangled(q[1:])).all()
+    # a batch of many tiles per block: the bulk-copy ring wraps around its stages several times
+    big = W.uniform_states(4_000_037, -2.0, 2.0, s, seed=43)
+    got = uw.is_disentangled_states(torch.from_numpy(big)).cpu().numpy()
+    assert (got == ow.is_disentangled(big)).all()
+    assert uw.last_stats()["device_errors"] == 0
