@@ -81,6 +81,11 @@ PW_HD void make_qf(const double *q, float r1_rob, float emax_env, float del_env,
 // separating axis is certified (> 0), or -1 when they may overlap.  The slack
 // covers FP32 placement and arithmetic error and the distance of R32 from a
 // rotation; the result is scaled down for axes whose length may exceed 1.
+// EARLY: return at the first certified axis; otherwise (the kernels' form) every
+// axis is evaluated without branches and the largest bound is returned: the
+// same sign, and fewer instructions where most pairs of a warp overlap
+// (measured: the chunk traversal 4 %, the plate's states traversal 13 % faster).
+template <bool EARLY = false>
 PW_HD float sat_sep32(const float4 &A0, const float4 &A1, const float4 &B0, const float4 &B1, const float4 &Q0,
                       const float4 &Q1, const float4 &Q2, const float4 &Q3)
 {
@@ -95,26 +100,58 @@ PW_HD float sat_sep32(const float4 &A0, const float4 &A1, const float4 &B0, cons
 	const float aR00 = fabsf(R00), aR01 = fabsf(R01), aR02 = fabsf(R02);
 	const float aR10 = fabsf(R10), aR11 = fabsf(R11), aR12 = fabsf(R12);
 	const float aR20 = fabsf(R20), aR21 = fabsf(R21), aR22 = fabsf(R22);
-	float g;
+	float g, gA = -3.0e38f, gB = -3.0e38f;
 	// env axes (unit length)
-	if ((g = fabsf(T0) - (a0 + fmaf(b0, aR00, fmaf(b1, aR01, fmaf(b2, aR02, m))))) > 0.f) return g;
-	if ((g = fabsf(T1) - (a1 + fmaf(b0, aR10, fmaf(b1, aR11, fmaf(b2, aR12, m))))) > 0.f) return g;
-	if ((g = fabsf(T2) - (a2 + fmaf(b0, aR20, fmaf(b1, aR21, fmaf(b2, aR22, m))))) > 0.f) return g;
+	g = fabsf(T0) - (a0 + fmaf(b0, aR00, fmaf(b1, aR01, fmaf(b2, aR02, m))));
+	if (EARLY && g > 0.f) return g;
+	gA = fmaxf(gA, g);
+	g = fabsf(T1) - (a1 + fmaf(b0, aR10, fmaf(b1, aR11, fmaf(b2, aR12, m))));
+	if (EARLY && g > 0.f) return g;
+	gA = fmaxf(gA, g);
+	g = fabsf(T2) - (a2 + fmaf(b0, aR20, fmaf(b1, aR21, fmaf(b2, aR22, m))));
+	if (EARLY && g > 0.f) return g;
+	gA = fmaxf(gA, g);
 	// robot axes
-	if ((g = fabsf(fmaf(T0, R00, fmaf(T1, R10, T2 * R20))) - (b0 + fmaf(a0, aR00, fmaf(a1, aR10, fmaf(a2, aR20, m))))) > 0.f) return g * shrink;
-	if ((g = fabsf(fmaf(T0, R01, fmaf(T1, R11, T2 * R21))) - (b1 + fmaf(a0, aR01, fmaf(a1, aR11, fmaf(a2, aR21, m))))) > 0.f) return g * shrink;
-	if ((g = fabsf(fmaf(T0, R02, fmaf(T1, R12, T2 * R22))) - (b2 + fmaf(a0, aR02, fmaf(a1, aR12, fmaf(a2, aR22, m))))) > 0.f) return g * shrink;
+	g = fabsf(fmaf(T0, R00, fmaf(T1, R10, T2 * R20))) - (b0 + fmaf(a0, aR00, fmaf(a1, aR10, fmaf(a2, aR20, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	g = fabsf(fmaf(T0, R01, fmaf(T1, R11, T2 * R21))) - (b1 + fmaf(a0, aR01, fmaf(a1, aR11, fmaf(a2, aR21, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	g = fabsf(fmaf(T0, R02, fmaf(T1, R12, T2 * R22))) - (b2 + fmaf(a0, aR02, fmaf(a1, aR12, fmaf(a2, aR22, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
 	// cross axes e_i x (column j of R), length at most that of the column
-	if ((g = fabsf(T2 * R10 - T1 * R20) - fmaf(a1, aR20, fmaf(a2, aR10, fmaf(b1, aR02, fmaf(b2, aR01, m))))) > 0.f) return g * shrink;
-	if ((g = fabsf(T2 * R11 - T1 * R21) - fmaf(a1, aR21, fmaf(a2, aR11, fmaf(b0, aR02, fmaf(b2, aR00, m))))) > 0.f) return g * shrink;
-	if ((g = fabsf(T2 * R12 - T1 * R22) - fmaf(a1, aR22, fmaf(a2, aR12, fmaf(b0, aR01, fmaf(b1, aR00, m))))) > 0.f) return g * shrink;
-	if ((g = fabsf(T0 * R20 - T2 * R00) - fmaf(a0, aR20, fmaf(a2, aR00, fmaf(b1, aR12, fmaf(b2, aR11, m))))) > 0.f) return g * shrink;
-	if ((g = fabsf(T0 * R21 - T2 * R01) - fmaf(a0, aR21, fmaf(a2, aR01, fmaf(b0, aR12, fmaf(b2, aR10, m))))) > 0.f) return g * shrink;
-	if ((g = fabsf(T0 * R22 - T2 * R02) - fmaf(a0, aR22, fmaf(a2, aR02, fmaf(b0, aR11, fmaf(b1, aR10, m))))) > 0.f) return g * shrink;
-	if ((g = fabsf(T1 * R00 - T0 * R10) - fmaf(a0, aR10, fmaf(a1, aR00, fmaf(b1, aR22, fmaf(b2, aR21, m))))) > 0.f) return g * shrink;
-	if ((g = fabsf(T1 * R01 - T0 * R11) - fmaf(a0, aR11, fmaf(a1, aR01, fmaf(b0, aR22, fmaf(b2, aR20, m))))) > 0.f) return g * shrink;
-	if ((g = fabsf(T1 * R02 - T0 * R12) - fmaf(a0, aR12, fmaf(a1, aR02, fmaf(b0, aR21, fmaf(b1, aR20, m))))) > 0.f) return g * shrink;
-	return -1.f;
+	g = fabsf(T2 * R10 - T1 * R20) - fmaf(a1, aR20, fmaf(a2, aR10, fmaf(b1, aR02, fmaf(b2, aR01, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	g = fabsf(T2 * R11 - T1 * R21) - fmaf(a1, aR21, fmaf(a2, aR11, fmaf(b0, aR02, fmaf(b2, aR00, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	g = fabsf(T2 * R12 - T1 * R22) - fmaf(a1, aR22, fmaf(a2, aR12, fmaf(b0, aR01, fmaf(b1, aR00, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	g = fabsf(T0 * R20 - T2 * R00) - fmaf(a0, aR20, fmaf(a2, aR00, fmaf(b1, aR12, fmaf(b2, aR11, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	g = fabsf(T0 * R21 - T2 * R01) - fmaf(a0, aR21, fmaf(a2, aR01, fmaf(b0, aR12, fmaf(b2, aR10, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	g = fabsf(T0 * R22 - T2 * R02) - fmaf(a0, aR22, fmaf(a2, aR02, fmaf(b0, aR11, fmaf(b1, aR10, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	g = fabsf(T1 * R00 - T0 * R10) - fmaf(a0, aR10, fmaf(a1, aR00, fmaf(b1, aR22, fmaf(b2, aR21, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	g = fabsf(T1 * R01 - T0 * R11) - fmaf(a0, aR11, fmaf(a1, aR01, fmaf(b0, aR22, fmaf(b2, aR20, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	g = fabsf(T1 * R02 - T0 * R12) - fmaf(a0, aR12, fmaf(a1, aR02, fmaf(b0, aR21, fmaf(b1, aR20, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	// a robot or cross axis counts only with a positive scale (shrink < 0: rotation error too large)
+	const float sep = fmaxf(gA, gB > 0.f ? gB * shrink : -1.f);
+	return sep > 0.f ? sep : -1.f;
 }
 
 PW_HD bool sat_disjoint32(const float4 &A0, const float4 &A1, const float4 &B0, const float4 &B1, const float4 &Q0,
@@ -141,7 +178,8 @@ constexpr float AXIS_ERR = 6.0e-8f;
 //   robot point placement error the margin covers, seen along unit axes
 //   (doubled margin), plus (AXIS_ERR + 4 u) |d|_1 (doubled) for the rounded env
 //   axes and the FP32 products.  Returns a lower bound on the distance when a
-//   separating axis is certified (> 0), else -1.
+//   separating axis is certified (> 0), else -1; EARLY as for sat_sep32.
+template <bool EARLY = false>
 PW_HD float sat_sep32_obb(const float4 &A0, const float4 &A1, const float4 &E0, const float4 &E1, const float4 &E2,
                           const float4 &B0, const float4 &B1, const float4 &G0, const float4 &G1, const float4 &G2,
                           const float4 &Q0, const float4 &Q1, const float4 &Q2, const float4 &Q3)
@@ -181,26 +219,58 @@ PW_HD float sat_sep32_obb(const float4 &A0, const float4 &A1, const float4 &E0, 
 	const float aR00 = fabsf(R00), aR01 = fabsf(R01), aR02 = fabsf(R02);
 	const float aR10 = fabsf(R10), aR11 = fabsf(R11), aR12 = fabsf(R12);
 	const float aR20 = fabsf(R20), aR21 = fabsf(R21), aR22 = fabsf(R22);
-	float g;
+	float g, gA = -3.0e38f, gB = -3.0e38f;
 	// env box axes (unit length)
-	if ((g = fabsf(T0) - (a0 + fmaf(b0, aR00, fmaf(b1, aR01, fmaf(b2, aR02, m))))) > 0.f) return g;
-	if ((g = fabsf(T1) - (a1 + fmaf(b0, aR10, fmaf(b1, aR11, fmaf(b2, aR12, m))))) > 0.f) return g;
-	if ((g = fabsf(T2) - (a2 + fmaf(b0, aR20, fmaf(b1, aR21, fmaf(b2, aR22, m))))) > 0.f) return g;
+	g = fabsf(T0) - (a0 + fmaf(b0, aR00, fmaf(b1, aR01, fmaf(b2, aR02, m))));
+	if (EARLY && g > 0.f) return g;
+	gA = fmaxf(gA, g);
+	g = fabsf(T1) - (a1 + fmaf(b0, aR10, fmaf(b1, aR11, fmaf(b2, aR12, m))));
+	if (EARLY && g > 0.f) return g;
+	gA = fmaxf(gA, g);
+	g = fabsf(T2) - (a2 + fmaf(b0, aR20, fmaf(b1, aR21, fmaf(b2, aR22, m))));
+	if (EARLY && g > 0.f) return g;
+	gA = fmaxf(gA, g);
 	// robot box axes
-	if ((g = fabsf(fmaf(T0, R00, fmaf(T1, R10, T2 * R20))) - (b0 + fmaf(a0, aR00, fmaf(a1, aR10, fmaf(a2, aR20, m))))) > 0.f) return g * shrink;
-	if ((g = fabsf(fmaf(T0, R01, fmaf(T1, R11, T2 * R21))) - (b1 + fmaf(a0, aR01, fmaf(a1, aR11, fmaf(a2, aR21, m))))) > 0.f) return g * shrink;
-	if ((g = fabsf(fmaf(T0, R02, fmaf(T1, R12, T2 * R22))) - (b2 + fmaf(a0, aR02, fmaf(a1, aR12, fmaf(a2, aR22, m))))) > 0.f) return g * shrink;
+	g = fabsf(fmaf(T0, R00, fmaf(T1, R10, T2 * R20))) - (b0 + fmaf(a0, aR00, fmaf(a1, aR10, fmaf(a2, aR20, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	g = fabsf(fmaf(T0, R01, fmaf(T1, R11, T2 * R21))) - (b1 + fmaf(a0, aR01, fmaf(a1, aR11, fmaf(a2, aR21, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	g = fabsf(fmaf(T0, R02, fmaf(T1, R12, T2 * R22))) - (b2 + fmaf(a0, aR02, fmaf(a1, aR12, fmaf(a2, aR22, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
 	// cross axes e_i x (column j of M)
-	if ((g = fabsf(T2 * R10 - T1 * R20) - fmaf(a1, aR20, fmaf(a2, aR10, fmaf(b1, aR02, fmaf(b2, aR01, m))))) > 0.f) return g * shrink;
-	if ((g = fabsf(T2 * R11 - T1 * R21) - fmaf(a1, aR21, fmaf(a2, aR11, fmaf(b0, aR02, fmaf(b2, aR00, m))))) > 0.f) return g * shrink;
-	if ((g = fabsf(T2 * R12 - T1 * R22) - fmaf(a1, aR22, fmaf(a2, aR12, fmaf(b0, aR01, fmaf(b1, aR00, m))))) > 0.f) return g * shrink;
-	if ((g = fabsf(T0 * R20 - T2 * R00) - fmaf(a0, aR20, fmaf(a2, aR00, fmaf(b1, aR12, fmaf(b2, aR11, m))))) > 0.f) return g * shrink;
-	if ((g = fabsf(T0 * R21 - T2 * R01) - fmaf(a0, aR21, fmaf(a2, aR01, fmaf(b0, aR12, fmaf(b2, aR10, m))))) > 0.f) return g * shrink;
-	if ((g = fabsf(T0 * R22 - T2 * R02) - fmaf(a0, aR22, fmaf(a2, aR02, fmaf(b0, aR11, fmaf(b1, aR10, m))))) > 0.f) return g * shrink;
-	if ((g = fabsf(T1 * R00 - T0 * R10) - fmaf(a0, aR10, fmaf(a1, aR00, fmaf(b1, aR22, fmaf(b2, aR21, m))))) > 0.f) return g * shrink;
-	if ((g = fabsf(T1 * R01 - T0 * R11) - fmaf(a0, aR11, fmaf(a1, aR01, fmaf(b0, aR22, fmaf(b2, aR20, m))))) > 0.f) return g * shrink;
-	if ((g = fabsf(T1 * R02 - T0 * R12) - fmaf(a0, aR12, fmaf(a1, aR02, fmaf(b0, aR21, fmaf(b1, aR20, m))))) > 0.f) return g * shrink;
-	return -1.f;
+	g = fabsf(T2 * R10 - T1 * R20) - fmaf(a1, aR20, fmaf(a2, aR10, fmaf(b1, aR02, fmaf(b2, aR01, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	g = fabsf(T2 * R11 - T1 * R21) - fmaf(a1, aR21, fmaf(a2, aR11, fmaf(b0, aR02, fmaf(b2, aR00, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	g = fabsf(T2 * R12 - T1 * R22) - fmaf(a1, aR22, fmaf(a2, aR12, fmaf(b0, aR01, fmaf(b1, aR00, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	g = fabsf(T0 * R20 - T2 * R00) - fmaf(a0, aR20, fmaf(a2, aR00, fmaf(b1, aR12, fmaf(b2, aR11, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	g = fabsf(T0 * R21 - T2 * R01) - fmaf(a0, aR21, fmaf(a2, aR01, fmaf(b0, aR12, fmaf(b2, aR10, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	g = fabsf(T0 * R22 - T2 * R02) - fmaf(a0, aR22, fmaf(a2, aR02, fmaf(b0, aR11, fmaf(b1, aR10, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	g = fabsf(T1 * R00 - T0 * R10) - fmaf(a0, aR10, fmaf(a1, aR00, fmaf(b1, aR22, fmaf(b2, aR21, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	g = fabsf(T1 * R01 - T0 * R11) - fmaf(a0, aR11, fmaf(a1, aR01, fmaf(b0, aR22, fmaf(b2, aR20, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	g = fabsf(T1 * R02 - T0 * R12) - fmaf(a0, aR12, fmaf(a1, aR02, fmaf(b0, aR21, fmaf(b1, aR20, m))));
+	if (EARLY && g > 0.f) return g * shrink;
+	gB = fmaxf(gB, g);
+	// a robot or cross axis counts only with a positive scale (shrink < 0: rotation error too large)
+	const float sep = fmaxf(gA, gB > 0.f ? gB * shrink : -1.f);
+	return sep > 0.f ? sep : -1.f;
 }
 
 PW_HD float3 f3(float4 a) { return make_float3(a.x, a.y, a.z); }

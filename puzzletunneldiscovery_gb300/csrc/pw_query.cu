@@ -191,6 +191,7 @@ __device__ __forceinline__ uint32_t retest_inline(const WorldDev &W, const WarpS
 // Q0..Q3, with axis-aligned node boxes (OBB = false: boxes in each mesh's frame)
 // or oriented ones (OBB = true).  Returns the certified separation (> 0) or -1,
 // and the two nodes' (centre, left child) and (half-extents, right child).
+// All 15 axes are evaluated without branches (sat_sep32's default form).
 template <bool OBB>
 __device__ __forceinline__ float node_pair_sep(const WorldDev &W, uint32_t e, uint32_t r, const float4 &Q0,
                                                const float4 &Q1, const float4 &Q2, const float4 &Q3, float4 &A0,

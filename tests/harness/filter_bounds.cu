@@ -277,7 +277,22 @@ int main(int argc, char **argv)
 			B0 = make_float4(c[0], c[1], c[2], 0.f);
 			B1 = make_float4(h[0], h[1], h[2], 0.f);
 		}
-		const float sep = sat_sep32(A0, A1, B0, B1, Q.q[0], Q.q[1], Q.q[2], Q.q[3]);
+		const float sep = sat_sep32<true>(A0, A1, B0, B1, Q.q[0], Q.q[1], Q.q[2], Q.q[3]);
+		// the branch-free form: the same sign, and its bound (the largest axis's) is a bound too
+		const float sepbf = sat_sep32<false>(A0, A1, B0, B1, Q.q[0], Q.q[1], Q.q[2], Q.q[3]);
+		if ((sepbf > 0.f) != (sep > 0.f) ||
+		    (!truth && sepbf > 0.f && (double)sepbf > tri_dist(V, Uw) * (1 + 1e-9) + 1e-14))
+			sviol++;
+		{
+			// a larger rotation error bound only widens the slack, up to one too large for the
+			// scaled axes (shrink <= 0): both forms agree, and neither separates touching boxes
+			float4 Q3 = Q.q[3];
+			Q3.x = Q3.x + 0.75f * (float)P(rng);
+			const float s1 = sat_sep32<true>(A0, A1, B0, B1, Q.q[0], Q.q[1], Q.q[2], Q3);
+			const float s2 = sat_sep32<false>(A0, A1, B0, B1, Q.q[0], Q.q[1], Q.q[2], Q3);
+			if ((s1 > 0.f) != (s2 > 0.f) || (truth && (s1 > 0.f || s2 > 0.f)))
+				sviol++;
+		}
 		if (truth && sep > 0.f) {
 			bviol++;
 			if (bviol < 5) printf("box violation: case %ld L=%g off=%g\n", it, L, off);
@@ -292,8 +307,21 @@ int main(int argc, char **argv)
 			double EE[9], EG[9];
 			fit_obb(V, 3, oA0, oA1, oE, EE);
 			fit_obb(x, 3, oB0, oB1, oG, EG);
-			const float osep = sat_sep32_obb(oA0, oA1, oE[0], oE[1], oE[2], oB0, oB1, oG[0], oG[1], oG[2], Q.q[0],
+			const float osep = sat_sep32_obb<true>(oA0, oA1, oE[0], oE[1], oE[2], oB0, oB1, oG[0], oG[1], oG[2], Q.q[0],
 			                                 Q.q[1], Q.q[2], Q.q[3]);
+			const float osepbf = sat_sep32_obb<false>(oA0, oA1, oE[0], oE[1], oE[2], oB0, oB1, oG[0], oG[1], oG[2],
+			                                          Q.q[0], Q.q[1], Q.q[2], Q.q[3]);
+			if ((osepbf > 0.f) != (osep > 0.f) ||
+			    (!truth && osepbf > 0.f && (double)osepbf > tri_dist(V, Uw) * (1 + 1e-9) + 1e-14))
+				oviol++;
+			float4 Q3 = Q.q[3];
+			Q3.x = Q3.x + 0.5f * (float)P(rng);
+			const float o1 = sat_sep32_obb<true>(oA0, oA1, oE[0], oE[1], oE[2], oB0, oB1, oG[0], oG[1], oG[2], Q.q[0], Q.q[1],
+			                               Q.q[2], Q3);
+			const float o2 = sat_sep32_obb<false>(oA0, oA1, oE[0], oE[1], oE[2], oB0, oB1, oG[0], oG[1], oG[2], Q.q[0],
+			                                      Q.q[1], Q.q[2], Q3);
+			if ((o1 > 0.f) != (o2 > 0.f) || (truth && (o1 > 0.f || o2 > 0.f)))
+				oviol++;
 			if (osep > 0.f) {
 				oseps++;
 				if (truth || (double)osep > tri_dist(V, Uw) * (1 + 1e-9) + 1e-14) {
@@ -316,8 +344,11 @@ int main(int argc, char **argv)
 			double EE[9], EG[9];
 			fit_obb(pe, 12, tA0, tA1, tE, EE);
 			fit_obb(pr, 12, tB0, tB1, tG, EG);
-			const float tsep = sat_sep32_obb(tA0, tA1, tE[0], tE[1], tE[2], tB0, tB1, tG[0], tG[1], tG[2], Q.q[0],
+			const float tsep = sat_sep32_obb<true>(tA0, tA1, tE[0], tE[1], tE[2], tB0, tB1, tG[0], tG[1], tG[2], Q.q[0],
 			                                 Q.q[1], Q.q[2], Q.q[3]);
+			if ((sat_sep32_obb<false>(tA0, tA1, tE[0], tE[1], tE[2], tB0, tB1, tG[0], tG[1], tG[2], Q.q[0], Q.q[1],
+			                          Q.q[2], Q.q[3]) > 0.f) != (tsep > 0.f))
+				oviol++;
 			const double ca[3] = { tA0.x, tA0.y, tA0.z }, ha[3] = { tA1.x, tA1.y, tA1.z };
 			const double hb[3] = { tB1.x, tB1.y, tB1.z }, cbl[3] = { tB0.x, tB0.y, tB0.z };
 			double cb[3], Eb[9];
@@ -362,10 +393,12 @@ int main(int argc, char **argv)
 						continue;   // not inside after all (the overlap is not monotone along every line)
 					QFs Q2;
 					make_qf(q2, (float)r1 * 1.0001f, (float)emax * 1.0001f, 5.9604645e-08f * (float)emax * 1.0001f, Q2);
-					const float s2 = sat_sep32_obb(tA0, tA1, tE[0], tE[1], tE[2], tB0, tB1, tG[0], tG[1], tG[2],
+					const float s2 = sat_sep32_obb<true>(tA0, tA1, tE[0], tE[1], tE[2], tB0, tB1, tG[0], tG[1], tG[2],
 					                               Q2.q[0], Q2.q[1], Q2.q[2], Q2.q[3]);
+					const float s2bf = sat_sep32_obb<false>(tA0, tA1, tE[0], tE[1], tE[2], tB0, tB1, tG[0], tG[1],
+					                                        tG[2], Q2.q[0], Q2.q[1], Q2.q[2], Q2.q[3]);
 					otouch++;
-					if (s2 > 0.f) {
+					if (s2 > 0.f || s2bf > 0.f) {
 						oviol++;
 						if (oviol < 5) printf("touching oriented box violation: case %ld back=%g\n", it, back);
 					}
