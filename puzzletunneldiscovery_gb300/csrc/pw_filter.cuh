@@ -49,7 +49,10 @@ struct QFs {
 	float4 q[5];
 };
 
-PW_HD void make_qf(const double *q, float r1_rob, float emax_env, float del_env, QFs &o)
+// state_ulps: a further entrywise error of the state's rotation matrix against the
+// reference's, in units of 2^-24, when q is not the reference's own state (1 for
+// pwm::interpolate_w's frames).
+PW_HD void make_qf(const double *q, float r1_rob, float emax_env, float del_env, QFs &o, float state_ulps = 0.f)
 {
 	const float x = (float)q[4], y = (float)q[5], z = (float)q[6], w = (float)q[3];
 	const float tx = 2.f * x, ty = 2.f * y, tz = 2.f * z;
@@ -62,7 +65,7 @@ PW_HD void make_qf(const double *q, float r1_rob, float emax_env, float del_env,
 	o.q[2] = make_float4(txz - twy, tyz + twx, 1.f - (txx + tyy), t2);
 	const float s = x * x + y * y + z * z + w * w;
 	const float dev = fabsf(1.f - s) + 8.f * U32 * s;        // |1 - |q|^2| for the FP64 quaternion
-	const float epsR = (10.f * s + 4.f) * U32;                // |R32 - R(q64)| entrywise
+	const float epsR = (10.f * s + 4.f + state_ulps) * U32;   // |R32 - R(q64)| entrywise
 	const float r1 = r1_rob;                                  // |x|_1 of any robot point (local frame)
 	const float tinf = fmaxf(fmaxf(fabsf(t0), fabsf(t1)), fabsf(t2));
 	const float rs = (1.f + 2.f * dev) * r1;                  // bound of |R x|_inf

@@ -88,6 +88,7 @@ struct RetestEntry {
 struct SegParams {
 	double qa[4], qb[4];      // normalised rotations
 	double d, theta, stheta;  // slerp constants
+	double inv_stheta;        // 1 / stheta (0 on the linear branch): the filter frames' slerp weights
 	double dist, inv_dist, step;
 	double skip_scale;        // bound on the motion of any robot point from one step to the next
 	int32_t linear;

@@ -254,6 +254,38 @@ PW_HD void interpolate_p(const double *a, const double *b, const SlerpParams &P,
 		out[3 + i] = add(mul(s0, P.qa[i]), mul(s1, P.qb[i]));
 }
 
+// The same state with the slerp weights multiplied by inv_stheta = 1 / stheta
+// instead of divided by stheta (two FP64 divisions fewer), for frames that only
+// feed the certified FP32 filters.  On the slerp branch theta <= pi / 2, so each
+// weight is at most 1 and differs from the divided one by at most 3 * 2^-53
+// (three roundings); with unit rotations qa, qb and the two products and the
+// sum rounded in each version, the rotation's components differ from the
+// reference's by less than 2^-48 and the raw-quaternion rotation matrix's
+// entries by less than 2^-44, far inside the one more unit of 2^-24 the filters'
+// frames allow for it (pwf::make_qf's state_ulps).  The translation is computed
+// as in interpolate_p, so it is the reference's.
+PW_HD void interpolate_w(const double *a, const double *b, const SlerpParams &P, double inv_stheta, double tau,
+                         double *out)
+{
+	const double omt = sub(1.0, tau);
+#pragma unroll
+	for (int i = 0; i < 3; i++)
+		out[i] = add(mul(a[i], omt), mul(b[i], tau));
+	double s0, s1;
+	if (P.linear) {
+		s0 = omt;
+		s1 = tau;
+	} else {
+		s0 = mul(sin_q(mul(omt, P.theta)), inv_stheta);
+		s1 = mul(sin_q(mul(tau, P.theta)), inv_stheta);
+	}
+	if (P.d < 0.0)
+		s1 = -s1;
+#pragma unroll
+	for (int i = 0; i < 4; i++)
+		out[3 + i] = add(mul(s0, P.qa[i]), mul(s1, P.qb[i]));
+}
+
 PW_HD void interpolate(const double *a, const double *b, double tau, double *out)
 {
 	SlerpParams P;

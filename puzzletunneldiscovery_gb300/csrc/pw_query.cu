@@ -70,9 +70,9 @@ struct StateSrc {
 	const QFs *anchors;        // per chunk: FP32 transform of the anchor step
 };
 
-__device__ __forceinline__ void make_qf(const double *q, const WorldDev &W, QFs &o)
+__device__ __forceinline__ void make_qf(const double *q, const WorldDev &W, QFs &o, float state_ulps = 0.f)
 {
-	pwf::make_qf(q, W.rob.r1, W.env.emax, W.del_env, o);
+	pwf::make_qf(q, W.rob.r1, W.env.emax, W.del_env, o, state_ulps);
 }
 
 // FP64 re-test of one triangle pair at state q: exactly the oracle's arithmetic.
@@ -391,8 +391,8 @@ __device__ __noinline__ void chunk_step_qf(const WorldDev &W, const StateSrc &sr
 	pwm::SlerpParams S;
 	seg_slerp(P, S);
 	double q[7];
-	pwm::interpolate_p(src.from + 7 * (size_t)s, src.to + 7 * (size_t)s, S, tau, q);
-	make_qf(q, W, o);
+	pwm::interpolate_w(src.from + 7 * (size_t)s, src.to + 7 * (size_t)s, S, P.inv_stheta, tau, q);
+	make_qf(q, W, o, 1.f);
 }
 
 // Traversal of the steps 0..nopen-1 of one segment chunk of cnt steps (slots =
@@ -928,8 +928,8 @@ __device__ __forceinline__ void seg_step_qf(const WorldDev &W, const double *a, 
 	pwm::SlerpParams S;
 	seg_slerp(P, S);
 	double q[7];
-	pwm::interpolate_p(a, b, S, tau, q);
-	make_qf(q, W, o);
+	pwm::interpolate_w(a, b, S, P.inv_stheta, tau, q);
+	make_qf(q, W, o, 1.f);
 }
 
 // First round of each phase of a segment query (the last phase is open), and
@@ -1012,6 +1012,7 @@ __global__ void k_seg_setup(WorldDev W, const double *from, const double *to, in
 	P.d = S.d;
 	P.theta = S.theta;
 	P.stheta = S.stheta;
+	P.inv_stheta = S.linear ? 0.0 : pwm::dvd(1.0, S.stheta);
 	P.linear = S.linear;
 	P.dist = dist;
 	P.inv_dist = pwm::dvd(1.0, dist);

@@ -145,6 +145,58 @@ int main(int argc, char **argv)
 		if (pwm::dbits(d) != pwm::dbits(seq[L - 2]))
 			mism++;
 	}
-	printf("mismatches %ld walks %ld jumped %ld tried %ld ties %ld\n", mism, walks, jumped, tried, ties);
+	// pwm::interpolate_w (slerp weights times 1 / stheta, the filter frames) against
+	// pwm::interpolate_p (the reference's division): the translation equal, the
+	// rotation's components within 2^-48 and its matrix entries within 2^-44
+	long interp = 0;
+	for (long i = 0; i < n; i++) {
+		double a[7], b[7];
+		for (int c = 0; c < 3; c++) {
+			a[c] = 4.0 * uniform() - 2.0;
+			b[c] = 4.0 * uniform() - 2.0;
+		}
+		double na = 0.0, nb = 0.0;
+		for (int c = 3; c < 7; c++) {
+			a[c] = 2.0 * uniform() - 1.0;
+			na += a[c] * a[c];
+		}
+		switch (next_u64() % 4) {
+		case 0:   // nearly the same rotation
+			for (int c = 3; c < 7; c++) b[c] = a[c] + 1e-6 * (2.0 * uniform() - 1.0);
+			break;
+		case 1:   // nearly the opposite quaternion (the same rotation, the other sign)
+			for (int c = 3; c < 7; c++) b[c] = -a[c] + 1e-4 * (2.0 * uniform() - 1.0);
+			break;
+		default:
+			for (int c = 3; c < 7; c++) b[c] = 2.0 * uniform() - 1.0;
+		}
+		for (int c = 3; c < 7; c++)
+			nb += b[c] * b[c];
+		if (na < 1e-6 || nb < 1e-6)
+			continue;
+		pwm::SlerpParams S;
+		pwm::slerp_setup(a, b, S);
+		const double inv = S.linear ? 0.0 : pwm::dvd(1.0, S.stheta);
+		for (int t = 0; t < 8; t++) {
+			const double tau = t == 0 ? 0.0 : (t == 1 ? 1.0 : uniform());
+			double qp[7], qw[7], Rp[9], Rw[9];
+			pwm::interpolate_p(a, b, S, tau, qp);
+			pwm::interpolate_w(a, b, S, inv, tau, qw);
+			pwm::quat_to_matrix(qp + 3, Rp);
+			pwm::quat_to_matrix(qw + 3, Rw);
+			interp++;
+			bool bad = false;
+			for (int c = 0; c < 3; c++)
+				bad = bad || pwm::dbits(qp[c]) != pwm::dbits(qw[c]);
+			for (int c = 3; c < 7; c++)
+				bad = bad || !(__builtin_fabs(qp[c] - qw[c]) < __builtin_ldexp(1.0, -48));
+			for (int e = 0; e < 9; e++)
+				bad = bad || !(__builtin_fabs(Rp[e] - Rw[e]) < __builtin_ldexp(1.0, -44));
+			if (bad)
+				mism++;
+		}
+	}
+	printf("mismatches %ld walks %ld jumped %ld tried %ld ties %ld interpolations %ld\n", mism, walks, jumped, tried,
+	       ties, interp);
 	return mism ? 1 : 0;
 }

@@ -2,7 +2,9 @@
 (pwm::walk_delta / delta_try / delta_jump; unit_world.cc:463-470 is one update per step)
 against the updates taken one at a time, bit for bit, on random and
 adversarial step sizes: rounding ties inside a binade, dist on and next to
-powers of two, dist an exact multiple of the step (CPU)."""
+powers of two, dist an exact multiple of the step; and the filter frames'
+slerp weights (a reciprocal instead of a division) within their stated error
+of the reference's interpolation (CPU)."""
 import os
 import subprocess
 
@@ -29,3 +31,4 @@ def test_walk_delta_equals_single_updates(harness, seed):
     assert fields["jumped"] > fields["walks"] // 2       # the shortcuts are taken
     assert fields["tried"] > fields["walks"] // 2
     assert fields["ties"] > 1000                         # and the tie fallback is exercised
+    assert fields["interpolations"] > 100_000            # the filter frames' slerp weights were compared
