@@ -49,9 +49,9 @@ struct QFs {
 	float4 q[5];
 };
 
-// state_ulps: a further entrywise error of the state's rotation matrix against the
-// reference's, in units of 2^-24, when q is not the reference's own state (1 for
-// pwm::interpolate_w's frames).
+// state_ulps: a further entrywise error of the state's rotation matrix against
+// the reference's, in units of 2^-24, when q is not the reference's own state
+// (1 for pwm::interpolate_w's frames, whose translation is the reference's).
 PW_HD void make_qf(const double *q, float r1_rob, float emax_env, float del_env, QFs &o, float state_ulps = 0.f)
 {
 	const float x = (float)q[4], y = (float)q[5], z = (float)q[6], w = (float)q[3];

@@ -33,12 +33,14 @@ PW_HD double sub(double a, double b) { return __dsub_rn(a, b); }
 PW_HD double mul(double a, double b) { return __dmul_rn(a, b); }
 PW_HD double dvd(double a, double b) { return __ddiv_rn(a, b); }
 PW_HD double rt(double a) { return __dsqrt_rn(a); }
+PW_HD double fmad(double a, double b, double c) { return __fma_rn(a, b, c); }
 #else
 PW_HD double add(double a, double b) { return a + b; }
 PW_HD double sub(double a, double b) { return a - b; }
 PW_HD double mul(double a, double b) { return a * b; }
 PW_HD double dvd(double a, double b) { return a / b; }
 PW_HD double rt(double a) { return sqrt(a); }
+PW_HD double fmad(double a, double b, double c) { return fma(a, b, c); }
 #endif
 PW_HD double dabs(double a) { return a >= 0.0 ? a : -a; }
 
@@ -84,6 +86,45 @@ PW_HD double sin_q(double x)
 	if (x <= PIO4_HI)
 		return sin_kernel(x);
 	return cos_kernel(add(sub(PIO2_HI, x), PIO2_LO));
+}
+
+// The same polynomials evaluated with fused multiply-adds (half the FP64
+// instructions), for frames that only feed the certified FP32 filters: not the
+// reference's rounding, within a few units of 2^-53 of sin_q on its range.
+PW_HD double sin_kernel_f(double x)
+{
+	const double z = mul(x, x);
+	double p = 2.8114572543455207632e-15;
+	p = fmad(p, z, -7.6471637318198164759e-13);
+	p = fmad(p, z, 1.6059043836821614599e-10);
+	p = fmad(p, z, -2.5052108385441718775e-08);
+	p = fmad(p, z, 2.7557319223985890653e-06);
+	p = fmad(p, z, -1.9841269841269841270e-04);
+	p = fmad(p, z, 8.3333333333333333333e-03);
+	p = fmad(p, z, -1.6666666666666666667e-01);
+	return fmad(mul(x, z), p, x);
+}
+
+PW_HD double cos_kernel_f(double y)
+{
+	const double z = mul(y, y);
+	double p = -1.5619206968586225271e-16;
+	p = fmad(p, z, 4.7794773323873852974e-14);
+	p = fmad(p, z, -1.1470745597729724714e-11);
+	p = fmad(p, z, 2.0876756987868098979e-09);
+	p = fmad(p, z, -2.7557319223985890653e-07);
+	p = fmad(p, z, 2.4801587301587301587e-05);
+	p = fmad(p, z, -1.3888888888888888889e-03);
+	p = fmad(p, z, 4.1666666666666666667e-02);
+	p = fmad(p, z, -5.0000000000000000000e-01);
+	return fmad(z, p, 1.0);
+}
+
+PW_HD double sin_qf(double x)
+{
+	if (x <= PIO4_HI)
+		return sin_kernel_f(x);
+	return cos_kernel_f(add(sub(PIO2_HI, x), PIO2_LO));
 }
 
 // atan(z) for z in [0, 1].
@@ -254,16 +295,16 @@ PW_HD void interpolate_p(const double *a, const double *b, const SlerpParams &P,
 		out[3 + i] = add(mul(s0, P.qa[i]), mul(s1, P.qb[i]));
 }
 
-// The same state with the slerp weights multiplied by inv_stheta = 1 / stheta
-// instead of divided by stheta (two FP64 divisions fewer), for frames that only
-// feed the certified FP32 filters.  On the slerp branch theta <= pi / 2, so each
-// weight is at most 1 and differs from the divided one by at most 3 * 2^-53
-// (three roundings); with unit rotations qa, qb and the two products and the
-// sum rounded in each version, the rotation's components differ from the
-// reference's by less than 2^-48 and the raw-quaternion rotation matrix's
-// entries by less than 2^-44, far inside the one more unit of 2^-24 the filters'
-// frames allow for it (pwf::make_qf's state_ulps).  The translation is computed
-// as in interpolate_p, so it is the reference's.
+// The same state for frames that only feed the certified FP32 filters: the
+// slerp weights multiplied by inv_stheta = 1 / stheta instead of divided by
+// stheta (two FP64 divisions fewer), the sines and the rotation's combination
+// evaluated with fused multiply-adds (sin_qf).  On the slerp branch theta <=
+// pi / 2, so each weight is at most 1 and lies within 2^-49 of the reference's;
+// with unit rotations qa, qb the rotation's components lie within 2^-47 of the
+// reference's and the raw-quaternion rotation matrix's entries within 2^-43.
+// The filters' frames allow one more unit of 2^-24 for it (pwf::make_qf's
+// state_ulps); tests/harness/delta_walk.cc checks the stated bounds against
+// the reference's interpolation.  The translation is the reference's.
 PW_HD void interpolate_w(const double *a, const double *b, const SlerpParams &P, double inv_stheta, double tau,
                          double *out)
 {
@@ -276,14 +317,14 @@ PW_HD void interpolate_w(const double *a, const double *b, const SlerpParams &P,
 		s0 = omt;
 		s1 = tau;
 	} else {
-		s0 = mul(sin_q(mul(omt, P.theta)), inv_stheta);
-		s1 = mul(sin_q(mul(tau, P.theta)), inv_stheta);
+		s0 = mul(sin_qf(mul(omt, P.theta)), inv_stheta);
+		s1 = mul(sin_qf(mul(tau, P.theta)), inv_stheta);
 	}
 	if (P.d < 0.0)
 		s1 = -s1;
 #pragma unroll
 	for (int i = 0; i < 4; i++)
-		out[3 + i] = add(mul(s0, P.qa[i]), mul(s1, P.qb[i]));
+		out[3 + i] = fmad(s1, P.qb[i], mul(s0, P.qa[i]));
 }
 
 PW_HD void interpolate(const double *a, const double *b, double tau, double *out)

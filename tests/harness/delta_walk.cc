@@ -145,9 +145,9 @@ int main(int argc, char **argv)
 		if (pwm::dbits(d) != pwm::dbits(seq[L - 2]))
 			mism++;
 	}
-	// pwm::interpolate_w (slerp weights times 1 / stheta, the filter frames) against
-	// pwm::interpolate_p (the reference's division): the translation equal, the
-	// rotation's components within 2^-48 and its matrix entries within 2^-44
+	// pwm::interpolate_w (the filter frames: reciprocal slerp weights, fused
+	// multiply-adds) against pwm::interpolate_p (the reference's): the translation
+	// equal, the rotation's components within 2^-47, its matrix entries within 2^-43
 	long interp = 0;
 	for (long i = 0; i < n; i++) {
 		double a[7], b[7];
@@ -189,9 +189,9 @@ int main(int argc, char **argv)
 			for (int c = 0; c < 3; c++)
 				bad = bad || pwm::dbits(qp[c]) != pwm::dbits(qw[c]);
 			for (int c = 3; c < 7; c++)
-				bad = bad || !(__builtin_fabs(qp[c] - qw[c]) < __builtin_ldexp(1.0, -48));
+				bad = bad || !(__builtin_fabs(qp[c] - qw[c]) < __builtin_ldexp(1.0, -47));
 			for (int e = 0; e < 9; e++)
-				bad = bad || !(__builtin_fabs(Rp[e] - Rw[e]) < __builtin_ldexp(1.0, -44));
+				bad = bad || !(__builtin_fabs(Rp[e] - Rw[e]) < __builtin_ldexp(1.0, -43));
 			if (bad)
 				mism++;
 		}
