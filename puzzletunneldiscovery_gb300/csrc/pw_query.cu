@@ -843,14 +843,15 @@ __global__ void __launch_bounds__(DIS_BLOCK) k_disentangled(pwf::DisBoxes32 B32,
 	}
 }
 
-// The FP64 test of the queued states (ROT as for k_disentangled), one thread each, in one-warp blocks so that
-// a short queue spreads over every SM (GB300's FP64 pipe is narrow: a block of
-// 256 queued states on one SM took several times longer than the same states on
-// eight).
+// The FP64 test of the queued states (ROT as for k_disentangled), one thread
+// each, in one-warp blocks so that a short queue spreads over every SM (GB300's
+// FP64 pipe is narrow: a block of 256 queued states on one SM took several
+// times longer than the same states on eight).
 constexpr int DIS64_BLOCK = 32;
 template <bool ROT>
-__global__ void __launch_bounds__(DIS64_BLOCK) k_disentangled64(BoxParams B, const double *states, const uint32_t *queue, int64_t n,
-                                 QueryCounters *ctr, uint8_t *out)
+__global__ void __launch_bounds__(DIS64_BLOCK) k_disentangled64(BoxParams B, const double *states,
+                                                                const uint32_t *queue, int64_t n,
+                                                                QueryCounters *ctr, uint8_t *out)
 {
 	const unsigned long long cnt = min(ctr->retest_count, (unsigned long long)n);
 	if (blockIdx.x == 0 && threadIdx.x == 0)
