@@ -484,8 +484,9 @@ PW_HD int tri_filter(float3 V0, float3 e1, float3 e2, float3 x0, float3 g1, floa
 // not), so its entries are bounded by K = max(1, 2 |q|^2).  With u = 2^-24, the
 // entrywise error of R is at most 10 K u (the rounded coefficients and the
 // quadratic entries), of d = R rc + t - ce at most (10 K + 7) u (|rc|_1 +
-// |t|_inf + |ce|_inf + |d|_inf; t is truncated by f32_trunc, 2u), of T = Re^T d at most 2 eps_d + 4u |d|_1, of
-// Re^T R at most (20 K + 5) u; the axis values are sums of at most six such
+// |t|_inf + |ce|_inf + |d|_inf; t is truncated by f32_trunc, 2u), of
+// T = Re^T d at most 2 eps_d + 4u |d|_1, of Re^T R at most (20 K + 5) u (each
+// operation rounded once or, fused, fewer times); the axis values are sums of at most six such
 // terms weighted by |T|_inf <= |d|_1, the extents and K, so
 // e = 1100u K (|rc|_1 + |t|_inf + |ce|_inf + 2 |d|_1 + sum eh + sum rh) covers
 // the FP32 side with a factor above 1.5 and the FP64 side (the same sums at
@@ -500,60 +501,167 @@ struct DisBoxes32 {
 	float ce_abs;          // |ce|_inf, rounded up
 };
 
-// ROT = false when the perturbation rotation Re is exactly the identity: then
-// Re^T d = d and Re^T R = R exactly (products by 1 and sums with zeros), so
-// both are taken as they are.  The verdict comes from the largest axis value
-// g_max: 1 when g_max > e, 0 when g_max < -e, -1 otherwise; with n2 and e
-// finite and below 1e30 every axis value is finite.
-template <bool ROT>
-PW_HD int boxes_disjoint32(const double *q, const DisBoxes32 &B, float slack = 1.f)
+// Two FP32 lanes computed together: packed f32x2 instructions on the device
+// (each lane rounded as the scalar instruction rounds it, two lanes per
+// instruction), scalar code on the host.  The box test below runs on either a
+// float or an F2, so one state or two share the same arithmetic.
+struct F2 {
+	float x, y;
+};
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ unsigned long long f2pack(F2 a)
 {
-	const float w = (float)q[3], x = (float)q[4], y = (float)q[5], z = (float)q[6];
-	const float n2 = ((w * w + x * x) + y * y) + z * z;
-	if (!(n2 < 1.0e30f))
-		return -1;                           // not finite or huge: the FP64 test decides
-	const float K = fmaxf(1.f, 2.f * n2) * (1.f + 8.f * U32);
-	const float R[9] = { 1.f - 2.f * (y * y + z * z), 2.f * (x * y - w * z), 2.f * (x * z + w * y),
-		                 2.f * (x * y + w * z), 1.f - 2.f * (x * x + z * z), 2.f * (y * z - w * x),
-		                 2.f * (x * z - w * y), 2.f * (y * z + w * x), 1.f - 2.f * (x * x + y * y) };
-	const float t[3] = { f32_trunc(q[0]), f32_trunc(q[1]), f32_trunc(q[2]) };
-	float d[3];
+	unsigned long long r;
+	asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+	return r;
+}
+__device__ __forceinline__ F2 f2unpack(unsigned long long v)
+{
+	F2 r;
+	asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+	return r;
+}
+__device__ __forceinline__ F2 vadd(F2 a, F2 b)
+{
+	unsigned long long r;
+	asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2pack(a)), "l"(f2pack(b)));
+	return f2unpack(r);
+}
+__device__ __forceinline__ F2 vsub(F2 a, F2 b)
+{
+	unsigned long long r;
+	asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2pack(a)), "l"(f2pack(b)));
+	return f2unpack(r);
+}
+__device__ __forceinline__ F2 vmul(F2 a, F2 b)
+{
+	unsigned long long r;
+	asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2pack(a)), "l"(f2pack(b)));
+	return f2unpack(r);
+}
+__device__ __forceinline__ F2 vfma(F2 a, F2 b, F2 c)
+{
+	unsigned long long r;
+	asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(f2pack(a)), "l"(f2pack(b)), "l"(f2pack(c)));
+	return f2unpack(r);
+}
+#else
+inline F2 vadd(F2 a, F2 b) { return { a.x + b.x, a.y + b.y }; }
+inline F2 vsub(F2 a, F2 b) { return { a.x - b.x, a.y - b.y }; }
+inline F2 vmul(F2 a, F2 b) { return { a.x * b.x, a.y * b.y }; }
+inline F2 vfma(F2 a, F2 b, F2 c) { return { fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y) }; }
+#endif
+PW_HD F2 vabs(F2 a) { return { fabsf(a.x), fabsf(a.y) }; }
+PW_HD F2 vmax(F2 a, F2 b) { return { fmaxf(a.x, b.x), fmaxf(a.y, b.y) }; }
+PW_HD float vadd(float a, float b) { return a + b; }
+PW_HD float vsub(float a, float b) { return a - b; }
+PW_HD float vmul(float a, float b) { return a * b; }
+PW_HD float vfma(float a, float b, float c) { return fmaf(a, b, c); }
+PW_HD float vabs(float a) { return fabsf(a); }
+PW_HD float vmax(float a, float b) { return fmaxf(a, b); }
+template <typename V> PW_HD V vset(float a);
+template <> PW_HD float vset<float>(float a) { return a; }
+template <> PW_HD F2 vset<F2>(float a) { return { a, a }; }
+
+// The 15 axis values of the box test for the state (w, x, y, z, t): the largest
+// (g), the error bound e and |q|^2 (n2), lane by lane.  ROT = false when the
+// perturbation rotation Re is exactly the identity: then Re^T d = d and
+// Re^T R = R exactly (products by 1 and sums with zeros), so both are taken as
+// they are.
+template <bool ROT, typename V>
+PW_HD void box_axes(V w, V x, V y, V z, const V t[3], const DisBoxes32 &B, float slack, V &g, V &e, V &n2)
+{
+	const V one = vset<V>(1.f), two = vset<V>(2.f), mtwo = vset<V>(-2.f);
+	n2 = vfma(z, z, vfma(y, y, vfma(x, x, vmul(w, w))));
+	const V K = vmul(vmax(one, vmul(two, n2)), vset<V>(1.f + 8.f * U32));
+	const V nw = vsub(vset<V>(0.f), w);
+	V R[9];
+	R[0] = vfma(mtwo, vfma(y, y, vmul(z, z)), one);
+	R[1] = vmul(two, vfma(x, y, vmul(nw, z)));
+	R[2] = vmul(two, vfma(x, z, vmul(w, y)));
+	R[3] = vmul(two, vfma(x, y, vmul(w, z)));
+	R[4] = vfma(mtwo, vfma(x, x, vmul(z, z)), one);
+	R[5] = vmul(two, vfma(y, z, vmul(nw, x)));
+	R[6] = vmul(two, vfma(x, z, vmul(nw, y)));
+	R[7] = vmul(two, vfma(y, z, vmul(w, x)));
+	R[8] = vfma(mtwo, vfma(x, x, vmul(y, y)), one);
+	V d[3];
 	for (int k = 0; k < 3; k++)
-		d[k] = ((R[3 * k] * B.rc[0] + R[3 * k + 1] * B.rc[1]) + R[3 * k + 2] * B.rc[2] + t[k]) - B.ce[k];
-	float T[3], Rr[9], AR[9];
+		d[k] = vsub(vadd(vfma(R[3 * k + 2], vset<V>(B.rc[2]),
+		                      vfma(R[3 * k + 1], vset<V>(B.rc[1]), vmul(R[3 * k], vset<V>(B.rc[0])))),
+		                 t[k]),
+		            vset<V>(B.ce[k]));
+	V T[3], Rr[9], AR[9];
 	for (int i = 0; i < 3; i++) {
-		T[i] = ROT ? (B.Re[i] * d[0] + B.Re[3 + i] * d[1]) + B.Re[6 + i] * d[2] : d[i];
+		T[i] = ROT ? vfma(vset<V>(B.Re[6 + i]), d[2], vfma(vset<V>(B.Re[3 + i]), d[1], vmul(vset<V>(B.Re[i]), d[0])))
+		           : d[i];
 		for (int j = 0; j < 3; j++) {
-			Rr[3 * i + j] = ROT ? (B.Re[i] * R[j] + B.Re[3 + i] * R[3 + j]) + B.Re[6 + i] * R[6 + j] : R[3 * i + j];
-			AR[3 * i + j] = fabsf(Rr[3 * i + j]);
+			Rr[3 * i + j] = ROT ? vfma(vset<V>(B.Re[6 + i]), R[6 + j],
+			                           vfma(vset<V>(B.Re[3 + i]), R[3 + j], vmul(vset<V>(B.Re[i]), R[j])))
+			                    : R[3 * i + j];
+			AR[3 * i + j] = vabs(Rr[3 * i + j]);
 		}
 	}
-	const float d1 = (fabsf(d[0]) + fabsf(d[1])) + fabsf(d[2]);
-	const float tinf = fmaxf(fmaxf(fabsf(t[0]), fabsf(t[1])), fabsf(t[2]));
-	const float scale = ((fabsf(B.rc[0]) + fabsf(B.rc[1])) + fabsf(B.rc[2])) + tinf + B.ce_abs + 2.f * d1 +
+	const V d1 = vadd(vadd(vabs(d[0]), vabs(d[1])), vabs(d[2]));
+	const V tinf = vmax(vmax(vabs(t[0]), vabs(t[1])), vabs(t[2]));
+	const float fixed = ((fabsf(B.rc[0]) + fabsf(B.rc[1])) + fabsf(B.rc[2])) + B.ce_abs +
 	                    ((B.eh[0] + B.eh[1]) + B.eh[2]) + ((B.rh[0] + B.rh[1]) + B.rh[2]);
-	const float e = slack * (1100.f * U32 * K * scale);
-	if (!(e < 1.0e30f))
-		return -1;                           // not finite: the FP64 test decides
-	float g = -3.0e38f;
+	const V scale = vadd(vfma(two, d1, tinf), vset<V>(fixed));
+	e = vmul(vset<V>(slack * 1100.f * U32), vmul(K, scale));
+	g = vset<V>(-3.0e38f);
 	for (int i = 0; i < 3; i++)
-		g = fmaxf(g, fabsf(T[i]) - (B.eh[i] + ((B.rh[0] * AR[3 * i] + B.rh[1] * AR[3 * i + 1]) + B.rh[2] * AR[3 * i + 2])));
+		g = vmax(g, vsub(vabs(T[i]), vadd(vset<V>(B.eh[i]),
+		                                  vfma(vset<V>(B.rh[2]), AR[3 * i + 2],
+		                                       vfma(vset<V>(B.rh[1]), AR[3 * i + 1], vmul(vset<V>(B.rh[0]), AR[3 * i]))))));
 	for (int j = 0; j < 3; j++) {
-		const float tl = (T[0] * Rr[j] + T[1] * Rr[3 + j]) + T[2] * Rr[6 + j];
-		const float ra = (B.eh[0] * AR[j] + B.eh[1] * AR[3 + j]) + B.eh[2] * AR[6 + j];
-		g = fmaxf(g, fabsf(tl) - (ra + B.rh[j]));
+		const V tl = vfma(T[2], Rr[6 + j], vfma(T[1], Rr[3 + j], vmul(T[0], Rr[j])));
+		const V ra = vfma(vset<V>(B.eh[2]), AR[6 + j], vfma(vset<V>(B.eh[1]), AR[3 + j], vmul(vset<V>(B.eh[0]), AR[j])));
+		g = vmax(g, vsub(vabs(tl), vadd(ra, vset<V>(B.rh[j]))));
 	}
 	for (int i = 0; i < 3; i++) {
 		const int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
 		for (int j = 0; j < 3; j++) {
 			const int j1 = (j + 1) % 3, j2 = (j + 2) % 3;
-			const float tl = T[i2] * Rr[3 * i1 + j] - T[i1] * Rr[3 * i2 + j];
-			const float ra = B.eh[i1] * AR[3 * i2 + j] + B.eh[i2] * AR[3 * i1 + j];
-			const float rb = B.rh[j1] * AR[3 * i + j2] + B.rh[j2] * AR[3 * i + j1];
-			g = fmaxf(g, fabsf(tl) - (ra + rb));
+			const V tl = vfma(T[i2], Rr[3 * i1 + j], vmul(vsub(vset<V>(0.f), T[i1]), Rr[3 * i2 + j]));
+			const V ra = vfma(vset<V>(B.eh[i1]), AR[3 * i2 + j], vmul(vset<V>(B.eh[i2]), AR[3 * i1 + j]));
+			const V rb = vfma(vset<V>(B.rh[j1]), AR[3 * i + j2], vmul(vset<V>(B.rh[j2]), AR[3 * i + j1]));
+			g = vmax(g, vsub(vabs(tl), vadd(ra, rb)));
 		}
 	}
+}
+
+// A lane's verdict from box_axes: 1 (disjoint) when g > e, 0 (overlap) when
+// g < -e, -1 (the FP64 test decides) otherwise or when |q|^2 or e is not finite
+// and below 1e30 (then every axis value is finite).
+PW_HD int box_verdict(float g, float e, float n2)
+{
+	if (!(n2 < 1.0e30f) || !(e < 1.0e30f))
+		return -1;
 	return g > e ? 1 : (g < -e ? 0 : -1);
+}
+
+template <bool ROT>
+PW_HD int boxes_disjoint32(const double *q, const DisBoxes32 &B, float slack = 1.f)
+{
+	const float t[3] = { f32_trunc(q[0]), f32_trunc(q[1]), f32_trunc(q[2]) };
+	float g, e, n2;
+	box_axes<ROT, float>((float)q[3], (float)q[4], (float)q[5], (float)q[6], t, B, slack, g, e, n2);
+	return box_verdict(g, e, n2);
+}
+
+// The same test for two states at once (packed arithmetic on the device).
+template <bool ROT>
+PW_HD void boxes_disjoint32x2(const double *qa, const double *qb, const DisBoxes32 &B, int &va, int &vb,
+                              float slack = 1.f)
+{
+	F2 t[3];
+	for (int c = 0; c < 3; c++)
+		t[c] = { f32_trunc(qa[c]), f32_trunc(qb[c]) };
+	F2 g, e, n2;
+	box_axes<ROT, F2>({ (float)qa[3], (float)qb[3] }, { (float)qa[4], (float)qb[4] }, { (float)qa[5], (float)qb[5] },
+	                  { (float)qa[6], (float)qb[6] }, t, B, slack, g, e, n2);
+	va = box_verdict(g.x, e.x, n2.x);
+	vb = box_verdict(g.y, e.y, n2.y);
 }
 
 } // namespace pwf

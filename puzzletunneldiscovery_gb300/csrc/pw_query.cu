@@ -733,27 +733,25 @@ struct BoxParams {
 // DIS_STAGES shared-memory stages filled by bulk copies, so the copies of the
 // next tiles are in flight while one is tested; the last partial tile (and
 // every tile of a batch that is not 16-byte aligned) is read with plain loads.
-// A bulk copy that does not land within DIS_WAIT_NS sets PW_DEVERR_WAIT; the
-// block then waits (bounded) for its copies in flight and stops.
-constexpr int DIS_BLOCK = 256;
+// Each thread tests two states of a tile (t and t + 128) with packed f32x2
+// arithmetic.  A bulk copy that does not land within DIS_WAIT_NS sets
+// PW_DEVERR_WAIT; the block then waits (bounded) for its copies in flight and
+// stops.
+constexpr int DIS_BLOCK = 256;     // states per tile
+constexpr int DIS_THREADS = 128;   // threads per block: two states each
 constexpr int DIS_STAGES = 3;
 constexpr uint32_t DIS_TILE_BYTES = DIS_BLOCK * 7 * sizeof(double);
 constexpr size_t DIS_SMEM = DIS_STAGES * (size_t)DIS_TILE_BYTES + DIS_STAGES * sizeof(uint64_t);
 constexpr uint64_t DIS_WAIT_NS = 1000000000ull;
 
-// One state's FP32 verdict; undecided states go to the queue (verdict 0 until
-// k_disentangled64 writes it).  All threads of the block call it.
-template <bool ROT>
-__device__ __forceinline__ void dis_decide(const pwf::DisBoxes32 &B32, const double *q, bool has, int64_t i,
-                                           int64_t n, uint8_t *out, uint32_t *queue, QueryCounters *ctr)
+// Records one state's FP32 verdict v (has: the state exists); undecided states
+// go to the queue (verdict 0 until k_disentangled64 writes it).  All threads of
+// the block call it.
+__device__ __forceinline__ void dis_record(int v, bool has, int64_t i, int64_t n, uint8_t *out, uint32_t *queue,
+                                           QueryCounters *ctr)
 {
 	const int lane = threadIdx.x & 31;
-	int v = 0;
-	bool undecided = false;
-	if (has) {
-		v = pwf::boxes_disjoint32<ROT>(q, B32);
-		undecided = v < 0;
-	}
+	const bool undecided = has && v < 0;
 	const unsigned m = __ballot_sync(0xffffffffu, undecided);
 	unsigned long long base = 0;
 	if (m) {
@@ -771,10 +769,22 @@ __device__ __forceinline__ void dis_decide(const pwf::DisBoxes32 &B32, const dou
 		out[i] = (uint8_t)v;
 }
 
+// The two states of this thread in a tile staged at sq (states b0 .. b0 + cnt - 1).
+template <bool ROT>
+__device__ __forceinline__ void dis_tile(const pwf::DisBoxes32 &B32, const double *sq, int64_t b0, int cnt, int64_t n,
+                                         uint8_t *out, uint32_t *queue, QueryCounters *ctr)
+{
+	const int ta = threadIdx.x, tb = threadIdx.x + DIS_THREADS;
+	int va = 0, vb = 0;
+	pwf::boxes_disjoint32x2<ROT>(sq + 7 * ta, sq + 7 * tb, B32, va, vb);
+	dis_record(va, ta < cnt, b0 + ta, n, out, queue, ctr);
+	dis_record(vb, tb < cnt, b0 + tb, n, out, queue, ctr);
+}
+
 // ROT: the perturbation rotation is not exactly the identity.
 template <bool ROT>
-__global__ void __launch_bounds__(DIS_BLOCK) k_disentangled(pwf::DisBoxes32 B32, const double *states, int64_t n,
-                                                            uint8_t *out, uint32_t *queue, QueryCounters *ctr)
+__global__ void __launch_bounds__(DIS_THREADS) k_disentangled(pwf::DisBoxes32 B32, const double *states, int64_t n,
+                                                              uint8_t *out, uint32_t *queue, QueryCounters *ctr)
 {
 	extern __shared__ __align__(128) unsigned char dis_smem[];
 	double *sq = reinterpret_cast<double *>(dis_smem);
@@ -810,8 +820,7 @@ __global__ void __launch_bounds__(DIS_BLOCK) k_disentangled(pwf::DisBoxes32 B32,
 			__syncthreads();
 			if (stop)
 				break;
-			const int64_t i = tile * DIS_BLOCK + threadIdx.x;
-			dis_decide<ROT>(B32, sq + (size_t)s * DIS_BLOCK * 7 + 7 * threadIdx.x, true, i, n, out, queue, ctr);
+			dis_tile<ROT>(B32, sq + (size_t)s * DIS_BLOCK * 7, tile * DIS_BLOCK, DIS_BLOCK, n, out, queue, ctr);
 			__syncthreads();   // every thread is done with stage s
 			const int64_t next = tile + (int64_t)DIS_STAGES * stride;
 			if (lead && next < nfull) {
@@ -835,10 +844,10 @@ __global__ void __launch_bounds__(DIS_BLOCK) k_disentangled(pwf::DisBoxes32 B32,
 		const int64_t b0 = tile * DIS_BLOCK;
 		const int cnt = (int)min((int64_t)DIS_BLOCK, n - b0);
 		const double *src = states + 7 * b0;
-		for (int k = threadIdx.x; k < cnt * 7; k += DIS_BLOCK)
-			sq[k] = src[k];
+		for (int k = threadIdx.x; k < DIS_BLOCK * 7; k += DIS_THREADS)
+			sq[k] = k < cnt * 7 ? src[k] : 0.0;
 		__syncthreads();
-		dis_decide<ROT>(B32, sq + 7 * threadIdx.x, (int)threadIdx.x < cnt, b0 + threadIdx.x, n, out, queue, ctr);
+		dis_tile<ROT>(B32, sq, b0, cnt, n, out, queue, ctr);
 		__syncthreads();
 	}
 }
@@ -1663,17 +1672,19 @@ extern "C" int pw_states_disentangled(pw_world *w, const double *states, int64_t
 	const void *kfn = rot ? (const void *)k_disentangled<true> : (const void *)k_disentangled<false>;
 	int &per_sm = w->dis_per_sm[rot ? 1 : 0];
 	if (per_sm <= 0) {
-		PW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, DIS_BLOCK, DIS_SMEM));
+		PW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, DIS_THREADS, DIS_SMEM));
 		per_sm = std::max(per_sm, 1);
 	}
 	const int64_t blocks = std::min<int64_t>((n + DIS_BLOCK - 1) / DIS_BLOCK, (int64_t)w->num_sms * per_sm);
 	uint32_t *queue = (uint32_t *)w->dis_queue.ptr;
 	const unsigned grid64 = (unsigned)(w->num_sms * 32);
 	if (rot) {
-		k_disentangled<true><<<(unsigned)blocks, DIS_BLOCK, DIS_SMEM, st>>>(dis_boxes32(B), states, n, out, queue, ctr);
+		k_disentangled<true><<<(unsigned)blocks, DIS_THREADS, DIS_SMEM, st>>>(dis_boxes32(B), states, n, out, queue,
+		                                                                      ctr);
 		k_disentangled64<true><<<grid64, DIS64_BLOCK, 0, st>>>(B, states, queue, n, ctr, out);
 	} else {
-		k_disentangled<false><<<(unsigned)blocks, DIS_BLOCK, DIS_SMEM, st>>>(dis_boxes32(B), states, n, out, queue, ctr);
+		k_disentangled<false><<<(unsigned)blocks, DIS_THREADS, DIS_SMEM, st>>>(dis_boxes32(B), states, n, out, queue,
+		                                                                       ctr);
 		k_disentangled64<false><<<grid64, DIS64_BLOCK, 0, st>>>(B, states, queue, n, ctr, out);
 	}
 	w->last_launches = 2;

@@ -113,8 +113,16 @@ int main(int argc, char **argv)
 		if (!conv_ok(x))
 			wrong++;
 	}
+	double prev[7] = { 0, 0, 0, 1, 0, 0, 0 };
 	auto check = [&](const Boxes &B, const double q[7]) {
 		const int ref = pwm::boxes_disjoint(q, B.rc, B.rh, B.Re, B.te, B.ec, B.eh);
+		// the two-state form on (the previous state, this one) gives the one-state verdicts
+		int va, vb;
+		pwf::boxes_disjoint32x2<true>(prev, q, B.b32, va, vb, slack);
+		if (va != pwf::boxes_disjoint32<true>(prev, B.b32, slack) || vb != pwf::boxes_disjoint32<true>(q, B.b32, slack))
+			wrong++;
+		for (int c = 0; c < 7; c++)
+			prev[c] = q[c];
 		// the general form, and the identity-rotation form where Re is exactly the identity
 		const bool ident = B.Re[0] == 1.0 && B.Re[4] == 1.0 && B.Re[8] == 1.0 && B.Re[1] == 0.0 && B.Re[2] == 0.0 &&
 		                   B.Re[3] == 0.0 && B.Re[5] == 0.0 && B.Re[6] == 0.0 && B.Re[7] == 0.0;
