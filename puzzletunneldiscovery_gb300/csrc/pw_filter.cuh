@@ -481,10 +481,14 @@ PW_HD int tri_filter(float3 V0, float3 e1, float3 e2, float3 x0, float3 g1, floa
 // e bounds |g32 - g| + |g64 - g| for every axis value g (exact), g32 (this
 // code), g64 (the FP64 test).  R is the rotation formula on the state's raw
 // quaternion (as the FP64 test and Eigen's toRotationMatrix apply it, unit or
-// not), so its entries are bounded by K = max(1, 2 |q|^2).  With u = 2^-24, the
-// entrywise error of R is at most 10 K u (the rounded coefficients and the
-// quadratic entries), of d = R rc + t - ce at most (10 K + 7) u (|rc|_1 +
-// |t|_inf + |ce|_inf + |d|_inf; t is truncated by f32_trunc, 2u), of
+// not), so its entries are bounded by K = max(1, 2 |q|^2).  The state's seven
+// components are truncated to FP32 with integer operations (f32_trunc, relative
+// error below 2u; the FP64 pipe is GB300's narrowest), so the computed |q|^2 is
+// at least |q|^2 (1 - 7u) and K carries a factor 1 + 16u.  With u = 2^-24, the
+// entrywise error of R is at most 10 K u (from the truncated components and the
+// roundings of the quadratic entries: at most 7 K u on the diagonal, 3 K u off
+// it), of d = R rc + t - ce at most (10 K + 7) u (|rc|_1 +
+// |t|_inf + |ce|_inf + |d|_inf; t truncated, 2u), of
 // T = Re^T d at most 2 eps_d + 4u |d|_1, of Re^T R at most (20 K + 5) u (each
 // operation rounded once or, fused, fewer times); the axis values are sums of at most six such
 // terms weighted by |T|_inf <= |d|_1, the extents and K, so
@@ -573,7 +577,7 @@ PW_HD void box_axes(V w, V x, V y, V z, const V t[3], const DisBoxes32 &B, float
 {
 	const V one = vset<V>(1.f), two = vset<V>(2.f), mtwo = vset<V>(-2.f);
 	n2 = vfma(z, z, vfma(y, y, vfma(x, x, vmul(w, w))));
-	const V K = vmul(vmax(one, vmul(two, n2)), vset<V>(1.f + 8.f * U32));
+	const V K = vmul(vmax(one, vmul(two, n2)), vset<V>(1.f + 16.f * U32));
 	const V nw = vsub(vset<V>(0.f), w);
 	V R[9];
 	R[0] = vfma(mtwo, vfma(y, y, vmul(z, z)), one);
@@ -645,7 +649,7 @@ PW_HD int boxes_disjoint32(const double *q, const DisBoxes32 &B, float slack = 1
 {
 	const float t[3] = { f32_trunc(q[0]), f32_trunc(q[1]), f32_trunc(q[2]) };
 	float g, e, n2;
-	box_axes<ROT, float>((float)q[3], (float)q[4], (float)q[5], (float)q[6], t, B, slack, g, e, n2);
+	box_axes<ROT, float>(f32_trunc(q[3]), f32_trunc(q[4]), f32_trunc(q[5]), f32_trunc(q[6]), t, B, slack, g, e, n2);
 	return box_verdict(g, e, n2);
 }
 
@@ -658,8 +662,9 @@ PW_HD void boxes_disjoint32x2(const double *qa, const double *qb, const DisBoxes
 	for (int c = 0; c < 3; c++)
 		t[c] = { f32_trunc(qa[c]), f32_trunc(qb[c]) };
 	F2 g, e, n2;
-	box_axes<ROT, F2>({ (float)qa[3], (float)qb[3] }, { (float)qa[4], (float)qb[4] }, { (float)qa[5], (float)qb[5] },
-	                  { (float)qa[6], (float)qb[6] }, t, B, slack, g, e, n2);
+	box_axes<ROT, F2>({ f32_trunc(qa[3]), f32_trunc(qb[3]) }, { f32_trunc(qa[4]), f32_trunc(qb[4]) },
+	                  { f32_trunc(qa[5]), f32_trunc(qb[5]) }, { f32_trunc(qa[6]), f32_trunc(qb[6]) }, t, B, slack, g, e,
+	                  n2);
 	va = box_verdict(g.x, e.x, n2.x);
 	vb = box_verdict(g.y, e.y, n2.y);
 }
